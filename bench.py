@@ -1,0 +1,331 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 raycaster on the raycaster workload, printed as one JSON line.
+
+Workload (the reference publishes no benchmark; seeded synthetic input): a subdivided
+icosphere of 1,310,720 triangles radially displaced by 3-octave value noise (amplitude
+0.1) and 16,777,216 rays with origins uniform in a box 3x the mesh bounds and directions
+uniform on the sphere. One step = one closest-hit query (Raycaster::intersects) over all
+16M rays; the any-hit query (Raycaster::intersectsAny) is timed the same way and reported
+beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+* value     -- Mrays/s, rays resident in HBM, CUDA events on the launching stream.
+* e2e       -- Mrays/s through the public API with host (pinned) buffers: host->device copy
+               of the rays and device->host copy of the hits inside the timed region.
+* roofline  -- the traversal kernel against the measured HBM bandwidth; algorithmic bytes
+               per ray = 32 (ray) + 16 (hit) + 64 x inner nodes visited + 48 x triangles
+               tested, visit counts measured on a 1M-ray sample of the same set.
+* cpu_baseline -- the C restatement of the reference Raycaster (oracle/port), reference
+               threading (hardware threads - 1), on a bounded sample of the same rays.
+* --impl reference -- only that CPU path, as the reference arm.
+Under torchrun (N > 1) every rank traces its own 16M rays (weak scaling, no collective on
+the data path); value = all rays / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SUBDIV = 8
+N_RAYS = 1 << 24
+SEED = 20261204
+WORKLOAD = ("raycaster: displaced icosphere, 1,310,720 triangles; 16,777,216 rays, origins uniform in 3x bounds, "
+            "directions uniform on the sphere; closest hit per step")
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[3 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        return dist, dist.get_rank(), ws
+    return None, 0, 1
+
+
+def _sync_all(dist, torch):
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+        torch.cuda.synchronize()
+
+
+def _max_over_ranks(dist, torch, v: float) -> float:
+    if dist is None:
+        return v
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_raycaster_rate(mesh, rays, target_s: float, threads: int):
+    """The C restatement of Raycaster on host cores: Mrays/s on a sample sized to run
+    about target_s seconds. Returns (Mrays_per_s, sample_rays, build_s)."""
+    from oracle import oracle as O
+
+    O.build_port()
+    port = O.PortRaycaster()
+    port.add_mesh(mesh.positions, mesh.indices)
+    t0 = time.perf_counter()
+    port.build()
+    build_s = time.perf_counter() - t0
+    probe = min(len(rays), 1 << 18)
+    t0 = time.perf_counter()
+    port.intersect(rays[:probe], threads=threads)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    m = int(min(len(rays), max(probe, probe * target_s / dt)))
+    t0 = time.perf_counter()
+    port.intersect(rays[:m], threads=threads)
+    dt = time.perf_counter() - t0
+    return m / dt / 1e6, m, build_s
+
+
+def run_reference(args):
+    """Reference arm: the reference's Raycaster algorithm (C restatement; the reference's own
+    sources do not travel to this host) on all host threads, same workload and metric."""
+    from rendu_gb300 import scenes as S
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    mesh, rays = S.raycaster_workload(SUBDIV, N_RAYS, SEED)
+    from oracle import oracle as O
+
+    O.build_port()
+    threads = os.cpu_count() or 1
+    port = O.PortRaycaster()
+    port.add_mesh(mesh.positions, mesh.indices)
+    port.build()
+    probe = 1 << 18
+    t0 = time.perf_counter()
+    port.intersect(rays[:probe], threads=threads)
+    per_ray = (time.perf_counter() - t0) / probe
+    m = int(min(len(rays), max(probe, 6.0 / max(per_ray, 1e-12))))
+    rng = np.random.default_rng(1)
+    for _ in range(args.warmup):
+        s = int(rng.integers(0, len(rays) - m + 1))
+        port.intersect(rays[s:s + m], threads=threads)
+    times = []
+    for _ in range(args.steps):
+        s = int(rng.integers(0, len(rays) - m + 1))
+        t0 = time.perf_counter()
+        port.intersect(rays[s:s + m], threads=threads)
+        times.append(time.perf_counter() - t0)
+    value = m * len(times) / sum(times) / 1e6
+    out = {
+        "impl": "reference", "metric": "Mrays/s (closest hit, raycaster workload)", "value": round(value, 3),
+        "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1000 * sum(times) / len(times), 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "triangles": mesh.triangle_count, "rays": len(rays)},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{m} contiguous rays of the 16,777,216-ray set per step"},
+        "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    dist, rank, world = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    from rendu_gb300 import build as B
+
+    B.build()
+    import rendu_gb300 as R
+    from rendu_gb300 import scenes as S
+
+    mesh, rays = S.raycaster_workload(SUBDIV, N_RAYS, SEED + 1000 * rank)
+    n = len(rays)
+    rc = R.Raycaster(local)
+    rc.add_mesh(mesh.positions, mesh.indices)
+    rc.updateHierarchy()
+    st = rc.stats()
+
+    pinned = torch.empty((n, 8), dtype=torch.float32, pin_memory=True)
+    pinned.numpy()[:] = rays
+    d_rays = pinned.to(f"cuda:{local}", non_blocking=False)
+    d_hits = torch.empty((n, 4), dtype=torch.float32, device=f"cuda:{local}")
+    d_occ = torch.empty(n, dtype=torch.uint8, device=f"cuda:{local}")
+    stream = torch.cuda.current_stream()
+
+    for _ in range(max(3, args.warmup)):
+        rc.intersect_batch(d_rays, out=d_hits)
+        rc.intersect_any_batch(d_rays, out=d_occ)
+    _sync_all(dist, torch)
+
+    # ---- timed: closest hit, rays resident in HBM (512 MB of rays per step > L2) --------
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        _sync_all(dist, torch)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            rc.intersect_batch(d_rays, out=d_hits)
+        ev1.record(stream)
+        _sync_all(dist, torch)
+    t_closest = ev0.elapsed_time(ev1) / 1000.0
+    t_closest = _max_over_ranks(dist, torch, t_closest)
+
+    ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    _sync_all(dist, torch)
+    ea.record(stream)
+    for _ in range(args.steps):
+        rc.intersect_any_batch(d_rays, out=d_occ)
+    eb.record(stream)
+    _sync_all(dist, torch)
+    t_any = _max_over_ranks(dist, torch, ea.elapsed_time(eb) / 1000.0)
+
+    # ---- e2e through the public API with host buffers ----------------------------------
+    host_hits = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy().view(R.HIT_DTYPE).reshape(-1)
+    host_rays = pinned.numpy()
+    rc.intersect_batch(host_rays, out=host_hits)
+    _sync_all(dist, torch)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc.intersect_batch(host_rays, out=host_hits)
+    _sync_all(dist, torch)
+    t_e2e = _max_over_ranks(dist, torch, time.perf_counter() - t0)
+
+    # ---- algorithmic bytes per ray (visit counts on a 1M-ray sample) -------------------
+    nv, nt = rc.count_visits(rays[: 1 << 20])
+    v_node, v_tri = float(nv.mean()), float(nt.mean())
+    bytes_per_ray = 32 + 16 + 64 * v_node + 48 * v_tri
+    avg_launch = t_closest / args.steps
+    achieved = bytes_per_ray * n / avg_launch / 1e9
+    peak, peak_kind = _peaks()
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "raycaster_closest_16M.txt")) as f:
+            for ln in f:
+                if ln.startswith("traffic_bytes_per_launch:"):
+                    traffic = float(ln.split(":")[1])
+    except OSError:
+        pass
+
+    total_rays = n * world
+    value = total_rays * args.steps / t_closest / 1e6
+    if rank == 0:
+        out = {
+            "metric": "Mrays/s (closest hit, raycaster workload)",
+            "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1000 * t_closest / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "triangles": mesh.triangle_count, "rays_per_gpu": n,
+                       "l2": "inputs larger than L2 (512 MB of rays per step)", "parallelism": f"replicas x{world}"},
+            "any_hit": {"value": round(total_rays * args.steps / t_any / 1e6, 2), "unit": "Mrays/s",
+                        "ms_per_step": round(1000 * t_any / args.steps, 4)},
+            "e2e": {"value": round(total_rays * args.steps / t_e2e / 1e6, 2), "unit": "Mrays/s",
+                    "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 16},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_kind": peak_kind, "bytes_per_ray": round(bytes_per_ray, 1),
+                         "node_visits_per_ray": round(v_node, 3), "tri_tests_per_ray": round(v_tri, 3),
+                         "io_only_frac": round(48 * n / avg_launch / 1e9 / peak, 4)},
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps,
+            "bvh": {"build_ms": round(st["build_ms"], 2), "nodes": st["nodes"], "leaves": st["leaves"],
+                    "sah_cost": round(st["sah_cost"], 2), "device_mb": round(st["device_bytes"] / 2**20, 1)},
+        }
+        if not args.no_cpu:
+            threads = max((os.cpu_count() or 2) - 1, 1)
+            rate, m, build_s = cpu_raycaster_rate(mesh, rays, args.cpu_seconds, threads)
+            out["cpu_baseline"] = {"value": round(rate, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                                   "sample": f"first {m} rays of the same 16,777,216-ray set",
+                                   "build_s": round(build_s, 2)}
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,249 @@
+/*
+ * rendu_gb300 -- C-ABI of the GB300 (sm_103a) BVH raycaster and offline path tracer.
+ *
+ * This is the drop-in boundary for Rendu's offline rendering path. Every entry point
+ * replaces one member of the reference's C++ API (cited per function as file:line of
+ * kosua20/Rendu) with a batched, device-backed equivalent:
+ *
+ *   Raycaster  (src/engine/raycaster/Raycaster.hpp:51-97)  ->  rt_*
+ *   PathTracer (src/apps/pathtracer/PathTracer.hpp:18-29)   ->  pt_*
+ *
+ * Conventions
+ *  - Plain pointers and sizes only; no C++ or framework types cross this boundary.
+ *  - Every call returns an int status (RT_OK == 0). The reference reports errors with
+ *    log lines and early returns (PathTracer.cpp:162-168); here they are status codes,
+ *    and rt_last_error() gives the message of the calling thread's last failure.
+ *  - Host pointers are the default: the library copies inputs in and results out, and
+ *    the call returns when the results are in host memory. With RT_FLAG_DEVICE_PTRS the
+ *    ray/hit/image pointers are CUDA device pointers; the call is then asynchronous on
+ *    `stream` (a cudaStream_t passed as void*, NULL = the context's own stream).
+ *  - Matrices are 4x4 column-major float[16] (glm layout), NULL meaning identity.
+ *  - A context is bound to the CUDA device given at creation. Calls on one context must
+ *    not overlap from several host threads.
+ */
+#ifndef RENDU_GB300_H
+#define RENDU_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------- */
+#define RT_OK 0
+#define RT_ERR_ARG 1     /* invalid argument (null pointer, bad index, bad size)          */
+#define RT_ERR_OOM 2     /* device or host allocation failed                               */
+#define RT_ERR_CUDA 3    /* a CUDA runtime call failed                                     */
+#define RT_ERR_TIMEOUT 4 /* a bounded device loop gave up (status word set by the kernel) */
+#define RT_ERR_STATE 5   /* call out of order (e.g. intersect before update_hierarchy)    */
+#define RT_ERR_OVERFLOW 6 /* a device traversal stack or queue exceeded its capacity       */
+
+/* ---- flags -------------------------------------------------------------------------- */
+#define RT_FLAG_DEVICE_PTRS 0x1u /* ray/hit/image pointers are device pointers (async)   */
+
+/* Marks a miss in rt_hit.prim. */
+#define RT_NO_HIT 0xFFFFFFFFu
+
+/* A ray: origin + [tmin, tmax] distance window + direction (need not be normalised;
+ * the library normalises it exactly as Ray::Ray does, Intersection.cpp:3-5). 32 bytes.
+ * The window is the (mini, maxi) pair of Raycaster::intersects (Raycaster.hpp:64);
+ * the reference defaults are tmin = 1e-4f, tmax = 1e8f. */
+typedef struct rt_ray {
+    float ox, oy, oz, tmin;
+    float dx, dy, dz, tmax;
+} rt_ray;
+
+/* A closest-hit record, 16 bytes. Replaces Raycaster::Hit (Raycaster.hpp:16-42):
+ *   hit    = (prim != RT_NO_HIT)
+ *   dist   = t          (FLT_MAX on a miss, like Hit::Hit())
+ *   u, v   = barycentrics, w = 1 - u - v
+ *   prim   = global triangle id in addMesh order; rt_prim_info() maps it back to
+ *            (meshId, localId) with localId = 3 * triangle index inside the mesh. */
+typedef struct rt_hit {
+    float t, u, v;
+    uint32_t prim;
+} rt_hit;
+
+/* Build / memory statistics of a context. */
+typedef struct rt_stats {
+    uint64_t triangles;
+    uint64_t vertices;
+    uint64_t meshes;
+    uint64_t nodes;       /* inner nodes of the device hierarchy                         */
+    uint64_t leaves;
+    uint64_t device_bytes; /* bytes held by the hierarchy + triangle arrays              */
+    float build_ms;       /* device time of the last rt_update_hierarchy                 */
+    float sah_cost;       /* surface-area cost of the hierarchy (traversal quality)      */
+} rt_stats;
+
+typedef struct rt_ctx rt_ctx;
+
+/* Create a raycaster on CUDA device `device`. Replaces Raycaster::Raycaster()
+ * (Raycaster.hpp:46). */
+int rt_create(rt_ctx **ctx, int device);
+
+/* Release all device and host memory of the context. */
+int rt_destroy(rt_ctx *ctx);
+
+/* Append a triangle mesh, its vertices transformed by `model` (skipped when NULL or the
+ * identity, as at Raycaster.cpp:22-26). positions: vertex_count x 3 floats; indices:
+ * index_count uint32 (a multiple of 3, each < vertex_count). *mesh_id receives the mesh
+ * index (addMesh call order). Replaces Raycaster::addMesh (Raycaster.cpp:14-52). */
+int rt_add_mesh(rt_ctx *ctx, const float *positions, size_t vertex_count, const uint32_t *indices,
+                size_t index_count, const float *model, uint32_t *mesh_id);
+
+/* Build the device hierarchy over every mesh added so far. Replaces
+ * Raycaster::updateHierarchy (Raycaster.cpp:54-142); the hierarchy differs (a GPU LBVH
+ * with surface-area leaf collapsing) but every query answers the same. */
+int rt_update_hierarchy(rt_ctx *ctx);
+
+/* Closest hit for n rays. Replaces Raycaster::intersects(origin, direction, mini, maxi)
+ * (Raycaster.cpp:144-185) for a batch. Ties at exactly equal distance go to the smaller
+ * prim id (the reference keeps the first found in its own traversal order). */
+int rt_intersect(rt_ctx *ctx, const rt_ray *rays, size_t n, rt_hit *hits, void *stream, uint32_t flags);
+
+/* Occlusion for n rays: occluded[i] = 1 if any triangle is hit inside (tmin, tmax).
+ * Replaces Raycaster::intersectsAny (Raycaster.cpp:187-224). */
+int rt_intersect_any(rt_ctx *ctx, const rt_ray *rays, size_t n, uint8_t *occluded, void *stream, uint32_t flags);
+
+/* Segment visibility for n point pairs: segs is n x 6 floats {p0.xyz, p1.xyz};
+ * visible[i] = 1 when nothing is hit between them. Replaces Raycaster::visible
+ * (Raycaster.cpp:226-230): window (1e-4, |p1 - p0|). */
+int rt_visible(rt_ctx *ctx, const float *segs, size_t n, uint8_t *visible, void *stream, uint32_t flags);
+
+/* Map a global triangle id to (meshId, localId) as stored in Raycaster::Hit. */
+int rt_prim_info(const rt_ctx *ctx, uint32_t prim, uint32_t *mesh_id, uint32_t *local_id);
+
+/* Statistics of the current hierarchy. */
+int rt_get_stats(const rt_ctx *ctx, rt_stats *out);
+
+/* Count, for each ray, the inner nodes and triangles the device traversal visits
+ * (closest-hit mode). node_visits / tri_visits are n uint32 each (host or device per
+ * flags). Used to state the algorithmic bytes per ray of the roofline. */
+int rt_count_visits(rt_ctx *ctx, const rt_ray *rays, size_t n, uint32_t *node_visits, uint32_t *tri_visits,
+                    void *stream, uint32_t flags);
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *rt_last_error(void);
+
+/* ======================================================================================
+ * Path tracer
+ * ====================================================================================== */
+
+/* Material types, numbered as Material::Type (src/engine/scene/Material.hpp:68-80). The
+ * path tracer shades Emissive as an emitter and every other type as the Lambert+GGX
+ * Regular material (PathTracer.cpp:228-276). */
+#define PT_MAT_REGULAR 1
+#define PT_MAT_EMISSIVE 8
+
+/* Background modes, numbered as Scene::Background (src/engine/scene/Scene.hpp:70-75). */
+#define PT_BG_COLOR 0
+#define PT_BG_IMAGE 1
+#define PT_BG_SKYBOX 2
+
+/* Light types (src/engine/scene/lights/). */
+#define PT_LIGHT_POINT 0
+#define PT_LIGHT_DIRECTIONAL 1
+#define PT_LIGHT_SPOT 2
+
+/* One mesh with the per-vertex attributes the path tracer reads (Mesh.hpp:126-132).
+ * normals/tangents/bitangents: vertex_count x 3 floats (required); texcoords:
+ * vertex_count x 2 floats or NULL (an object whose mesh has no texcoords does not use
+ * them, Object.cpp:4-8). */
+typedef struct pt_mesh_desc {
+    const float *positions;
+    const float *normals;
+    const float *tangents;
+    const float *bitangents;
+    const float *texcoords;
+    size_t vertex_count;
+    const uint32_t *indices;
+    size_t index_count;
+} pt_mesh_desc;
+
+/* A material: its type, alpha masking and three textures ids from pt_scene_add_texture:
+ * tex[0] albedo+alpha (or emitted colour), tex[1] normal map, tex[2] roughness/metalness/AO
+ * (Material.hpp:12-16). */
+typedef struct pt_material_desc {
+    int32_t type;
+    int32_t masked;
+    uint32_t tex[3];
+} pt_material_desc;
+
+/* An analytic light (PointLight.cpp:68-87, DirectionalLight.cpp:40-44, SpotLight.cpp:52-78).
+ * Spot angles are the (inner, outer) half angles in radians. */
+typedef struct pt_light_desc {
+    int32_t type;
+    int32_t cast_shadows;
+    float color[3];
+    float position[3];
+    float direction[3];
+    float radius;
+    float inner_angle, outer_angle;
+} pt_light_desc;
+
+/* A pinhole camera as Camera::pose + projection (Camera.cpp:10-25); the image-plane
+ * corner and steps are derived as in Camera::pixelShifts (Camera.cpp:42-49). */
+typedef struct pt_camera_desc {
+    float eye[3];
+    float center[3];
+    float up[3];
+    float fov;   /* vertical field of view, radians (default 1.3) */
+    float ratio; /* width / height */
+} pt_camera_desc;
+
+/* Per-render counters. rays = primary + bounce + shadow rays cast. */
+typedef struct pt_render_stats {
+    uint64_t primary_rays;
+    uint64_t bounce_rays;
+    uint64_t shadow_rays;
+    uint64_t paths;
+    float device_ms;
+} pt_render_stats;
+
+typedef struct pt_scene pt_scene;
+
+/* Create an empty scene on CUDA device `device`. */
+int pt_scene_create(pt_scene **scene, int device);
+int pt_scene_destroy(pt_scene *scene);
+
+/* Add a float image (width x height x channels, row-major, channels 1..4) used as a
+ * texture; sampled with bilinear wrap filtering as Image::rgbal (Image.cpp:86-106). */
+int pt_scene_add_texture(pt_scene *scene, uint32_t width, uint32_t height, uint32_t channels, const float *pixels,
+                         uint32_t *tex_id);
+int pt_scene_add_mesh(pt_scene *scene, const pt_mesh_desc *mesh, uint32_t *mesh_id);
+int pt_scene_add_material(pt_scene *scene, const pt_material_desc *mat, uint32_t *material_id);
+/* Add an object (Object.hpp:25): mesh + material + model matrix. */
+int pt_scene_add_object(pt_scene *scene, uint32_t mesh_id, uint32_t material_id, const float *model,
+                        uint32_t *object_id);
+int pt_scene_add_light(pt_scene *scene, const pt_light_desc *light);
+/* COLOR: color[3] used; IMAGE: tex[0]; SKYBOX: tex[0..5] = +x,-x,+y,-y,+z,-z faces
+ * (Texture.cpp:141-191). */
+int pt_scene_set_background(pt_scene *scene, int32_t mode, const float *color, const uint32_t *tex);
+
+/* Upload the scene and build its raycaster: every object's mesh is added in object order
+ * (so meshId == object index) and the hierarchy is built. Replaces
+ * PathTracer::PathTracer(scene) (PathTracer.cpp:11-21). */
+int pt_scene_commit(pt_scene *scene);
+
+/* Render `samples` (rounded to a power of two as at PathTracer.cpp:169-173) paths of at
+ * most `depth` segments per pixel and ACCUMULATE the normalised result into `image`
+ * (width x height x components floats, components >= 3, RGB in the first three), as
+ * PathTracer::render(camera, samples, depth, image) does (PathTracer.cpp:159-299):
+ * image.rgb = (image.rgb + sum_s min(L_s, 5)) / spp. `seed` selects the random sequence.
+ * Host pointer by default; device pointer with RT_FLAG_DEVICE_PTRS. */
+int pt_render(pt_scene *scene, const pt_camera_desc *camera, uint32_t samples, uint32_t depth, uint64_t seed,
+              float *image, uint32_t width, uint32_t height, uint32_t components, void *stream, uint32_t flags);
+
+/* Counters of the last pt_render on this scene. */
+int pt_get_render_stats(const pt_scene *scene, pt_render_stats *out);
+
+/* The raycaster built by pt_scene_commit (PathTracer::raycaster(), PathTracer.hpp:29). */
+rt_ctx *pt_scene_raycaster(pt_scene *scene);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RENDU_GB300_H */

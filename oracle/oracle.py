@@ -1,0 +1,243 @@
+"""Python access to the two CPU oracles -- test infrastructure only.
+
+* ``liboracle_port.so``  -- the plain-C restatement of the reference's raycaster and path
+  tracer (oracle/port/). Builds anywhere (``make -C oracle port``); it is the CPU
+  baseline timed on the measurement host and the parity checker used by the GPU tests.
+* ``_ref/libref_oracle.so`` -- the reference's own sources compiled in place
+  (``make -C oracle ref``) with the glue in oracle/ref_capi.cpp. Present only where the
+  reference tree is; it pins the restatement and generates tests/golden/.
+
+Only tests/, bench.py's CPU-baseline leg and the smoke check import this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "liboracle_port.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref_oracle.so")
+REF_ROOT_DEFAULT = "/root/reference"
+
+NO_HIT = 0xFFFFFFFF
+HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4")])
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+_hitp = np.ctypeslib.ndpointer(HIT_DTYPE, flags="C_CONTIGUOUS")
+
+
+def build_port(quiet: bool = True) -> str:
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True, capture_output=quiet)
+    return PORT_LIB
+
+
+def build_ref(quiet: bool = True, jobs: int = 8) -> str | None:
+    """Compile the reference oracle when the reference tree exists; None otherwise."""
+    root = os.environ.get("RENDU_REFERENCE_ROOT", REF_ROOT_DEFAULT)
+    if not os.path.isdir(os.path.join(root, "src", "engine", "raycaster")):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, f"-j{jobs}", "ref", f"REF_ROOT={root}"], check=True,
+                   capture_output=quiet)
+    return REF_LIB
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def _model_colmajor(model):
+    if model is None:
+        return None
+    m = np.asarray(model, np.float32)
+    return np.ascontiguousarray(m.T.reshape(16))
+
+
+_port = None
+
+
+def port_lib():
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_LIB):
+            build_port()
+        lib = C.CDLL(PORT_LIB)
+        lib.port_rc_create.restype = C.c_void_p
+        lib.port_rc_destroy.argtypes = [C.c_void_p]
+        lib.port_rc_add_mesh.argtypes = [C.c_void_p, _f32p, C.c_size_t, _u32p, C.c_size_t, C.c_void_p]
+        lib.port_rc_build.argtypes = [C.c_void_p]
+        lib.port_rc_node_count.argtypes = [C.c_void_p]
+        lib.port_rc_node_count.restype = C.c_size_t
+        lib.port_rc_intersect.argtypes = [C.c_void_p, _f32p, C.c_size_t, _hitp, C.c_int, C.c_void_p]
+        lib.port_rc_intersect_any.argtypes = [C.c_void_p, _f32p, C.c_size_t, _u8p, C.c_int]
+        lib.port_rc_brute.argtypes = [C.c_void_p, _f32p, C.c_size_t, _hitp, C.c_int]
+        lib.port_rc_test_triangle.argtypes = [C.c_void_p, _f32p, C.c_uint32, _hitp]
+        lib.port_default_threads.restype = C.c_int
+        _port = lib
+    return _port
+
+
+_ref = None
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_LIB):
+            raise FileNotFoundError("reference oracle not built (needs the reference tree)")
+        lib = C.CDLL(REF_LIB)
+        lib.ref_rc_create.restype = C.c_void_p
+        lib.ref_rc_destroy.argtypes = [C.c_void_p]
+        lib.ref_rc_add_mesh.argtypes = [C.c_void_p, _f32p, C.c_size_t, _u32p, C.c_size_t, C.c_void_p]
+        lib.ref_rc_build.argtypes = [C.c_void_p]
+        lib.ref_rc_intersect.argtypes = [C.c_void_p, _f32p, C.c_size_t, _hitp, C.c_int]
+        lib.ref_rc_intersect_any.argtypes = [C.c_void_p, _f32p, C.c_size_t, _u8p, C.c_int]
+        lib.ref_rc_visible.argtypes = [C.c_void_p, _f32p, C.c_size_t, _u8p]
+        lib.ref_ggx_eval.argtypes = [_f32p, C.c_size_t, _f32p]
+        lib.ref_ggx_sample.argtypes = [_f32p, _u32p, C.c_size_t, _f32p, _f32p]
+        lib.ref_cosine_hemisphere.argtypes = [_u32p, C.c_size_t, _f32p]
+        lib.ref_pixel_shifts.argtypes = [C.c_void_p, _f32p]
+        lib.ref_pt_create.restype = C.c_void_p
+        lib.ref_pt_destroy.argtypes = [C.c_void_p]
+        lib.ref_pt_add_texture.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, _f32p]
+        lib.ref_pt_add_mesh.argtypes = [C.c_void_p, C.c_void_p]
+        lib.ref_pt_add_material.argtypes = [C.c_void_p, C.c_void_p]
+        lib.ref_pt_add_object.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
+        lib.ref_pt_add_light.argtypes = [C.c_void_p, C.c_void_p]
+        lib.ref_pt_set_background.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        lib.ref_pt_commit.argtypes = [C.c_void_p]
+        lib.ref_pt_render.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, _f32p,
+                                      C.c_uint32, C.c_uint32]
+        _ref = lib
+    return _ref
+
+
+class _RaycasterBase:
+    _prefix = ""
+
+    def __init__(self, lib):
+        self.lib = lib
+        self.h = getattr(lib, self._prefix + "rc_create")()
+        self._keep = []
+        self.tri_offsets = []
+        self.tris = 0
+
+    def add_mesh(self, positions, indices, model=None) -> int:
+        pos = np.ascontiguousarray(positions, np.float32).reshape(-1)
+        idx = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+        m = _model_colmajor(model)
+        self._keep += [pos, idx, m]
+        mp = m.ctypes.data if m is not None else None
+        r = getattr(self.lib, self._prefix + "rc_add_mesh")(self.h, pos, len(pos) // 3, idx, len(idx), mp)
+        if r < 0:
+            raise ValueError("add_mesh rejected the mesh")
+        self.tri_offsets.append(self.tris)
+        self.tris += len(idx) // 3
+        return r
+
+    def build(self):
+        getattr(self.lib, self._prefix + "rc_build")(self.h)
+
+    def close(self):
+        if self.h:
+            getattr(self.lib, self._prefix + "rc_destroy")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PortRaycaster(_RaycasterBase):
+    """The C restatement of Raycaster (oracle/port/rt_port.c)."""
+
+    _prefix = "port_"
+
+    def __init__(self):
+        super().__init__(port_lib())
+
+    def intersect(self, rays, threads: int = 0, counters: bool = False):
+        rays = np.ascontiguousarray(rays, np.float32)
+        out = np.zeros(len(rays), HIT_DTYPE)
+        cnt = np.zeros(2, np.uint64)
+        self.lib.port_rc_intersect(self.h, rays.reshape(-1), len(rays), out, threads, cnt.ctypes.data)
+        return (out, cnt) if counters else out
+
+    def intersect_any(self, rays, threads: int = 0):
+        rays = np.ascontiguousarray(rays, np.float32)
+        out = np.zeros(len(rays), np.uint8)
+        self.lib.port_rc_intersect_any(self.h, rays.reshape(-1), len(rays), out, threads)
+        return out
+
+    def brute(self, rays, threads: int = 0):
+        rays = np.ascontiguousarray(rays, np.float32)
+        out = np.zeros(len(rays), HIT_DTYPE)
+        self.lib.port_rc_brute(self.h, rays.reshape(-1), len(rays), out, threads)
+        return out
+
+    def test_triangle(self, ray, prim):
+        ray = np.ascontiguousarray(ray, np.float32).reshape(-1)
+        out = np.zeros(1, HIT_DTYPE)
+        r = self.lib.port_rc_test_triangle(self.h, ray, int(prim), out)
+        return r, out[0]
+
+    @property
+    def node_count(self):
+        return self.lib.port_rc_node_count(self.h)
+
+
+class RefRaycaster(_RaycasterBase):
+    """The reference's own Raycaster, compiled from its sources."""
+
+    _prefix = "ref_"
+
+    def __init__(self):
+        super().__init__(ref_lib())
+
+    def intersect(self, rays, parallel: bool = True):
+        rays = np.ascontiguousarray(rays, np.float32)
+        out = np.zeros(len(rays), HIT_DTYPE)
+        self.lib.ref_rc_intersect(self.h, rays.reshape(-1), len(rays), out, int(parallel))
+        return out
+
+    def intersect_any(self, rays, parallel: bool = True):
+        rays = np.ascontiguousarray(rays, np.float32)
+        out = np.zeros(len(rays), np.uint8)
+        self.lib.ref_rc_intersect_any(self.h, rays.reshape(-1), len(rays), out, int(parallel))
+        return out
+
+    def visible(self, segs):
+        segs = np.ascontiguousarray(segs, np.float32)
+        out = np.zeros(len(segs), np.uint8)
+        self.lib.ref_rc_visible(self.h, segs.reshape(-1), len(segs), out)
+        return out
+
+
+def ref_ggx_eval(cases):
+    cases = np.ascontiguousarray(cases, np.float32)
+    out = np.zeros((len(cases), 3), np.float32)
+    ref_lib().ref_ggx_eval(cases.reshape(-1), len(cases), out.reshape(-1))
+    return out
+
+
+def ref_ggx_sample(cases, seeds):
+    cases = np.ascontiguousarray(cases, np.float32)
+    seeds = np.ascontiguousarray(seeds, np.uint32)
+    uni = np.zeros((len(cases), 3), np.float32)
+    out = np.zeros((len(cases), 6), np.float32)
+    ref_lib().ref_ggx_sample(cases.reshape(-1), seeds, len(cases), uni.reshape(-1), out.reshape(-1))
+    return uni, out
+
+
+def ref_cosine_hemisphere(seeds):
+    seeds = np.ascontiguousarray(seeds, np.uint32)
+    out = np.zeros((len(seeds), 5), np.float32)
+    ref_lib().ref_cosine_hemisphere(seeds, len(seeds), out.reshape(-1))
+    return out

@@ -1,0 +1,122 @@
+"""ctypes binding of ``librendu_gb300.so`` (the C-ABI declared in include/rendu_gb300.h).
+
+The library is the only compute path: if it is missing or cannot be loaded, every entry
+point raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "librendu_gb300.so")
+
+RT_OK = 0
+RT_ERR_ARG = 1
+RT_ERR_OOM = 2
+RT_ERR_CUDA = 3
+RT_ERR_TIMEOUT = 4
+RT_ERR_STATE = 5
+RT_ERR_OVERFLOW = 6
+RT_FLAG_DEVICE_PTRS = 0x1
+RT_NO_HIT = 0xFFFFFFFF
+
+_STATUS_NAMES = {1: "RT_ERR_ARG", 2: "RT_ERR_OOM", 3: "RT_ERR_CUDA", 4: "RT_ERR_TIMEOUT", 5: "RT_ERR_STATE",
+                 6: "RT_ERR_OVERFLOW"}
+
+
+class RenduError(RuntimeError):
+    def __init__(self, code: int, func: str, msg: str):
+        super().__init__(f"{func}: {_STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class rt_stats(C.Structure):
+    _fields_ = [("triangles", C.c_uint64), ("vertices", C.c_uint64), ("meshes", C.c_uint64), ("nodes", C.c_uint64),
+                ("leaves", C.c_uint64), ("device_bytes", C.c_uint64), ("build_ms", C.c_float),
+                ("sah_cost", C.c_float)]
+
+
+class pt_mesh_desc(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("normals", C.c_void_p), ("tangents", C.c_void_p),
+                ("bitangents", C.c_void_p), ("texcoords", C.c_void_p), ("vertex_count", C.c_size_t),
+                ("indices", C.c_void_p), ("index_count", C.c_size_t)]
+
+
+class pt_material_desc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("masked", C.c_int32), ("tex", C.c_uint32 * 3)]
+
+
+class pt_light_desc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("cast_shadows", C.c_int32), ("color", C.c_float * 3),
+                ("position", C.c_float * 3), ("direction", C.c_float * 3), ("radius", C.c_float),
+                ("inner_angle", C.c_float), ("outer_angle", C.c_float)]
+
+
+class pt_camera_desc(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("center", C.c_float * 3), ("up", C.c_float * 3), ("fov", C.c_float),
+                ("ratio", C.c_float)]
+
+
+class pt_render_stats(C.Structure):
+    _fields_ = [("primary_rays", C.c_uint64), ("bounce_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
+                ("paths", C.c_uint64), ("device_ms", C.c_float)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+_VP = C.c_void_p
+_SIGS = {
+    "rt_create": ([C.POINTER(C.c_void_p), C.c_int], C.c_int),
+    "rt_destroy": ([_VP], C.c_int),
+    "rt_add_mesh": ([_VP, _VP, C.c_size_t, _VP, C.c_size_t, _VP, C.POINTER(C.c_uint32)], C.c_int),
+    "rt_update_hierarchy": ([_VP], C.c_int),
+    "rt_intersect": ([_VP, _VP, C.c_size_t, _VP, _VP, C.c_uint32], C.c_int),
+    "rt_intersect_any": ([_VP, _VP, C.c_size_t, _VP, _VP, C.c_uint32], C.c_int),
+    "rt_visible": ([_VP, _VP, C.c_size_t, _VP, _VP, C.c_uint32], C.c_int),
+    "rt_prim_info": ([_VP, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)], C.c_int),
+    "rt_get_stats": ([_VP, C.POINTER(rt_stats)], C.c_int),
+    "rt_count_visits": ([_VP, _VP, C.c_size_t, _VP, _VP, _VP, C.c_uint32], C.c_int),
+    "rt_last_error": ([], C.c_char_p),
+    "pt_scene_create": ([C.POINTER(C.c_void_p), C.c_int], C.c_int),
+    "pt_scene_destroy": ([_VP], C.c_int),
+    "pt_scene_add_texture": ([_VP, C.c_uint32, C.c_uint32, C.c_uint32, _VP, C.POINTER(C.c_uint32)], C.c_int),
+    "pt_scene_add_mesh": ([_VP, C.POINTER(pt_mesh_desc), C.POINTER(C.c_uint32)], C.c_int),
+    "pt_scene_add_material": ([_VP, C.POINTER(pt_material_desc), C.POINTER(C.c_uint32)], C.c_int),
+    "pt_scene_add_object": ([_VP, C.c_uint32, C.c_uint32, _VP, C.POINTER(C.c_uint32)], C.c_int),
+    "pt_scene_add_light": ([_VP, C.POINTER(pt_light_desc)], C.c_int),
+    "pt_scene_set_background": ([_VP, C.c_int32, _VP, _VP], C.c_int),
+    "pt_scene_commit": ([_VP], C.c_int),
+    "pt_render": ([_VP, C.POINTER(pt_camera_desc), C.c_uint32, C.c_uint32, C.c_uint64, _VP, C.c_uint32, C.c_uint32,
+                   C.c_uint32, _VP, C.c_uint32], C.c_int),
+    "pt_get_render_stats": ([_VP, C.POINTER(pt_render_stats)], C.c_int),
+    "pt_scene_raycaster": ([_VP], _VP),
+}
+
+
+def lib():
+    """Load the library once; raise if it is absent (build it with __graft_entry__.build())."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(f"{LIB_PATH} is missing: the CUDA library must be built (rendu_gb300.build)")
+            h = C.CDLL(LIB_PATH)
+            for name, (args, res) in _SIGS.items():
+                f = getattr(h, name)
+                f.argtypes = args
+                f.restype = res
+            _lib = h
+    return _lib
+
+
+def check(code: int, func: str):
+    if code != RT_OK:
+        msg = lib().rt_last_error()
+        raise RenduError(code, func, msg.decode() if msg else "")
+
+
+def call(func: str, *args):
+    check(getattr(lib(), func)(*args), func)

@@ -1,0 +1,369 @@
+// C-ABI of the raycaster (include/rendu_gb300.h): context life cycle, mesh intake,
+// hierarchy build, batched queries with host or device buffers.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "rt_context.hpp"
+
+namespace rgb {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+void clear_error() { g_last_error.clear(); }
+
+int DevBuf::reserve(size_t need) {
+    if (need <= bytes && ptr) return RT_OK;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    if (cudaMalloc(&ptr, need ? need : 16) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("device allocation of " + std::to_string(need) + " bytes failed");
+        return RT_ERR_OOM;
+    }
+    bytes = need;
+    return RT_OK;
+}
+
+void DevBuf::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+int build_hierarchy(rt_ctx *ctx);
+int trace_count(rt_ctx *ctx, const rt_ray *d_rays, size_t n, uint32_t *nc, uint32_t *tc, rt_hit *scratch,
+                cudaStream_t st);
+int segments_to_rays(const float *d_segs, size_t n, rt_ray *d_rays, cudaStream_t st);
+int invert_bytes(uint8_t *d, size_t n, cudaStream_t st);
+
+int check_status(rt_ctx *ctx, cudaStream_t st) {
+    unsigned s = 0;
+    RT_CUDA_TRY(cudaMemcpyAsync(&s, ctx->d_status.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    RT_CUDA_TRY(cudaStreamSynchronize(st));
+    if (s) {
+        RT_CUDA_TRY(cudaMemsetAsync(ctx->d_status.ptr, 0, sizeof(unsigned), st));
+        if (s & RT_DEV_TIMEOUT) {
+            set_error("a bounded device loop gave up");
+            return RT_ERR_TIMEOUT;
+        }
+        set_error("a traversal stack or queue overflowed");
+        return RT_ERR_OVERFLOW;
+    }
+    return RT_OK;
+}
+
+}  // namespace rgb
+
+using namespace rgb;
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+int require_built(rt_ctx *ctx) {
+    if (!ctx) {
+        set_error("null context");
+        return RT_ERR_ARG;
+    }
+    if (!ctx->built || ctx->dirty) {
+        set_error("rt_update_hierarchy must be called after the last rt_add_mesh");
+        return RT_ERR_STATE;
+    }
+    return RT_OK;
+}
+
+// Runs `fn(d_in, count, d_out, stream)` over host buffers in chunks: copy in, compute,
+// copy out, all on the context stream (device allocations grow once and are reused).
+template <class Fn>
+int host_chunked(rt_ctx *ctx, const void *h_in, size_t in_stride, size_t n, void *h_out, size_t out_stride, Fn fn) {
+    const size_t chunk = size_t(1) << 22;
+    const size_t cn = n < chunk ? n : chunk;
+    if (ctx->d_rays.reserve(cn * in_stride) != RT_OK) return RT_ERR_OOM;
+    if (ctx->d_out.reserve(cn * out_stride) != RT_OK) return RT_ERR_OOM;
+    cudaStream_t st = ctx->stream;
+    for (size_t s = 0; s < n; s += chunk) {
+        const size_t m = (n - s) < chunk ? (n - s) : chunk;
+        RT_CUDA_TRY(cudaMemcpyAsync(ctx->d_rays.ptr, static_cast<const char *>(h_in) + s * in_stride, m * in_stride,
+                                    cudaMemcpyHostToDevice, st));
+        const int r = fn(ctx->d_rays.ptr, m, ctx->d_out.ptr, st);
+        if (r != RT_OK) return r;
+        RT_CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(h_out) + s * out_stride, ctx->d_out.ptr, m * out_stride,
+                                    cudaMemcpyDeviceToHost, st));
+    }
+    RT_CUDA_TRY(cudaStreamSynchronize(st));
+    return check_status(ctx, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *rt_last_error(void) { return g_last_error.c_str(); }
+
+int rt_create(rt_ctx **out, int device) {
+    clear_error();
+    if (!out) {
+        set_error("null output pointer");
+        return RT_ERR_ARG;
+    }
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        set_error("CUDA device " + std::to_string(device) + " is not available");
+        return RT_ERR_CUDA;
+    }
+    DeviceGuard g(device);
+    rt_ctx *ctx = new rt_ctx();
+    ctx->device = device;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev_a) != cudaSuccess || cudaEventCreate(&ctx->ev_b) != cudaSuccess) {
+        set_error(std::string("stream/event creation failed: ") + cudaGetErrorString(cudaGetLastError()));
+        delete ctx;
+        return RT_ERR_CUDA;
+    }
+    if (ctx->d_status.reserve(16) != RT_OK) {
+        delete ctx;
+        return RT_ERR_OOM;
+    }
+    cudaMemset(ctx->d_status.ptr, 0, 16);
+    *out = ctx;
+    return RT_OK;
+}
+
+int rt_destroy(rt_ctx *ctx) {
+    if (!ctx) return RT_OK;
+    DeviceGuard g(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->d_nodes.release();
+    ctx->d_tris.release();
+    ctx->d_verts.release();
+    ctx->d_status.release();
+    ctx->d_rays.release();
+    ctx->d_out.release();
+    ctx->d_out2.release();
+    if (ctx->ev_a) cudaEventDestroy(ctx->ev_a);
+    if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return RT_OK;
+}
+
+int rt_add_mesh(rt_ctx *ctx, const float *positions, size_t vertex_count, const uint32_t *indices, size_t index_count,
+                const float *model, uint32_t *mesh_id) {
+    clear_error();
+    if (!ctx || (vertex_count && !positions) || (index_count && !indices)) {
+        set_error("null argument");
+        return RT_ERR_ARG;
+    }
+    if (index_count % 3) {
+        set_error("index_count must be a multiple of 3");
+        return RT_ERR_ARG;
+    }
+    const uint64_t total_tris = ctx->h_indices.size() / 3 + index_count / 3;
+    if (total_tris >= 0x7FFFFFFFull || ctx->h_positions.size() / 3 + vertex_count >= 0xFFFFFFFFull) {
+        set_error("too many triangles or vertices for 32-bit ids");
+        return RT_ERR_ARG;
+    }
+    for (size_t i = 0; i < index_count; ++i) {
+        if (indices[i] >= vertex_count) {
+            set_error("index " + std::to_string(i) + " out of range");
+            return RT_ERR_ARG;
+        }
+    }
+    MeshRecord rec;
+    rec.first_vertex = ctx->h_positions.size() / 3;
+    rec.vertex_count = vertex_count;
+    rec.first_tri = ctx->h_indices.size() / 3;
+    rec.tri_count = index_count / 3;
+    rec.identity = true;
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            const float v = model ? model[4 * c + r] : (c == r ? 1.0f : 0.0f);
+            rec.model[4 * c + r] = v;
+            // Raycaster.cpp:22: the transform is skipped only for the exact identity.
+            if (v != (c == r ? 1.0f : 0.0f)) rec.identity = false;
+        }
+    ctx->h_positions.insert(ctx->h_positions.end(), positions, positions + 3 * vertex_count);
+    const uint32_t off = (uint32_t)rec.first_vertex;
+    const size_t base = ctx->h_indices.size();
+    ctx->h_indices.resize(base + index_count);
+    for (size_t i = 0; i < index_count; ++i) ctx->h_indices[base + i] = indices[i] + off;
+    ctx->meshes.push_back(rec);
+    ctx->dirty = true;
+    if (mesh_id) *mesh_id = (uint32_t)(ctx->meshes.size() - 1);
+    return RT_OK;
+}
+
+int rt_update_hierarchy(rt_ctx *ctx) {
+    clear_error();
+    if (!ctx) {
+        set_error("null context");
+        return RT_ERR_ARG;
+    }
+    DeviceGuard g(ctx->device);
+    const int r = build_hierarchy(ctx);
+    if (r != RT_OK) return r;
+    if (ctx->depth > 256) {
+        set_error("hierarchy deeper than the traversal stack (256)");
+        return RT_ERR_OVERFLOW;
+    }
+    ctx->built = true;
+    ctx->dirty = false;
+    return RT_OK;
+}
+
+int rt_intersect(rt_ctx *ctx, const rt_ray *rays, size_t n, rt_hit *hits, void *stream, uint32_t flags) {
+    clear_error();
+    int r = require_built(ctx);
+    if (r != RT_OK) return r;
+    if (n && (!rays || !hits)) {
+        set_error("null rays or hits");
+        return RT_ERR_ARG;
+    }
+    DeviceGuard g(ctx->device);
+    if (flags & RT_FLAG_DEVICE_PTRS) {
+        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+        return trace_closest(ctx, rays, n, hits, st);
+    }
+    return host_chunked(ctx, rays, sizeof(rt_ray), n, hits, sizeof(rt_hit),
+                        [ctx](void *in, size_t m, void *out, cudaStream_t st) {
+                            return trace_closest(ctx, static_cast<const rt_ray *>(in), m, static_cast<rt_hit *>(out), st);
+                        });
+}
+
+int rt_intersect_any(rt_ctx *ctx, const rt_ray *rays, size_t n, uint8_t *occluded, void *stream, uint32_t flags) {
+    clear_error();
+    int r = require_built(ctx);
+    if (r != RT_OK) return r;
+    if (n && (!rays || !occluded)) {
+        set_error("null rays or output");
+        return RT_ERR_ARG;
+    }
+    DeviceGuard g(ctx->device);
+    if (flags & RT_FLAG_DEVICE_PTRS) {
+        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+        return trace_any(ctx, rays, n, occluded, st);
+    }
+    return host_chunked(ctx, rays, sizeof(rt_ray), n, occluded, 1,
+                        [ctx](void *in, size_t m, void *out, cudaStream_t st) {
+                            return trace_any(ctx, static_cast<const rt_ray *>(in), m, static_cast<uint8_t *>(out), st);
+                        });
+}
+
+int rt_visible(rt_ctx *ctx, const float *segs, size_t n, uint8_t *visible, void *stream, uint32_t flags) {
+    clear_error();
+    int r = require_built(ctx);
+    if (r != RT_OK) return r;
+    if (n && (!segs || !visible)) {
+        set_error("null segments or output");
+        return RT_ERR_ARG;
+    }
+    DeviceGuard g(ctx->device);
+    auto run = [ctx](const float *d_segs, size_t m, uint8_t *d_vis, cudaStream_t st) -> int {
+        if (ctx->d_out2.reserve(m * sizeof(rt_ray)) != RT_OK) return RT_ERR_OOM;
+        rt_ray *d_r = ctx->d_out2.as<rt_ray>();
+        int rr = segments_to_rays(d_segs, m, d_r, st);
+        if (rr != RT_OK) return rr;
+        rr = trace_any(ctx, d_r, m, d_vis, st);
+        if (rr != RT_OK) return rr;
+        return invert_bytes(d_vis, m, st);
+    };
+    if (flags & RT_FLAG_DEVICE_PTRS) {
+        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+        return run(segs, n, visible, st);
+    }
+    return host_chunked(ctx, segs, 6 * sizeof(float), n, visible, 1,
+                        [run](void *in, size_t m, void *out, cudaStream_t st) {
+                            return run(static_cast<const float *>(in), m, static_cast<uint8_t *>(out), st);
+                        });
+}
+
+int rt_count_visits(rt_ctx *ctx, const rt_ray *rays, size_t n, uint32_t *node_visits, uint32_t *tri_visits,
+                    void *stream, uint32_t flags) {
+    clear_error();
+    int r = require_built(ctx);
+    if (r != RT_OK) return r;
+    if (n && (!rays || !node_visits || !tri_visits)) {
+        set_error("null argument");
+        return RT_ERR_ARG;
+    }
+    DeviceGuard g(ctx->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+    if (flags & RT_FLAG_DEVICE_PTRS) {
+        if (ctx->d_out2.reserve(n * sizeof(rt_hit)) != RT_OK) return RT_ERR_OOM;
+        return trace_count(ctx, rays, n, node_visits, tri_visits, ctx->d_out2.as<rt_hit>(), st);
+    }
+    DevBuf dr, dn, dt, dh;
+    if (dr.reserve(n * sizeof(rt_ray)) || dn.reserve(n * 4) || dt.reserve(n * 4) || dh.reserve(n * sizeof(rt_hit))) {
+        dr.release(); dn.release(); dt.release(); dh.release();
+        return RT_ERR_OOM;
+    }
+    int rc = RT_OK;
+    if (cudaMemcpyAsync(dr.ptr, rays, n * sizeof(rt_ray), cudaMemcpyHostToDevice, st) != cudaSuccess) rc = RT_ERR_CUDA;
+    if (rc == RT_OK) rc = trace_count(ctx, dr.as<rt_ray>(), n, dn.as<uint32_t>(), dt.as<uint32_t>(), dh.as<rt_hit>(), st);
+    if (rc == RT_OK && (cudaMemcpyAsync(node_visits, dn.ptr, n * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                        cudaMemcpyAsync(tri_visits, dt.ptr, n * 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                        cudaStreamSynchronize(st) != cudaSuccess))
+        rc = RT_ERR_CUDA;
+    if (rc == RT_OK) rc = check_status(ctx, st);
+    dr.release(); dn.release(); dt.release(); dh.release();
+    return rc;
+}
+
+int rt_prim_info(const rt_ctx *ctx, uint32_t prim, uint32_t *mesh_id, uint32_t *local_id) {
+    clear_error();
+    if (!ctx || !mesh_id || !local_id) {
+        set_error("null argument");
+        return RT_ERR_ARG;
+    }
+    size_t lo = 0, hi = ctx->meshes.size();
+    if (hi == 0 || prim >= ctx->h_indices.size() / 3) {
+        set_error("triangle id out of range");
+        return RT_ERR_ARG;
+    }
+    --hi;
+    while (lo < hi) {  // last non-empty mesh whose first triangle <= prim
+        const size_t mid = (lo + hi + 1) / 2;
+        if (ctx->meshes[mid].first_tri <= prim) lo = mid;
+        else hi = mid - 1;
+    }
+    while (ctx->meshes[lo].tri_count == 0 && lo > 0) --lo;
+    *mesh_id = (uint32_t)lo;
+    *local_id = (uint32_t)(3 * (prim - ctx->meshes[lo].first_tri));
+    return RT_OK;
+}
+
+int rt_get_stats(const rt_ctx *ctx, rt_stats *out) {
+    clear_error();
+    if (!ctx || !out) {
+        set_error("null argument");
+        return RT_ERR_ARG;
+    }
+    std::memset(out, 0, sizeof(*out));
+    out->triangles = ctx->h_indices.size() / 3;
+    out->vertices = ctx->h_positions.size() / 3;
+    out->meshes = ctx->meshes.size();
+    out->nodes = ctx->n_inner;
+    out->leaves = ctx->n_leaves;
+    out->device_bytes = ctx->n_inner * sizeof(BvhNode) + ctx->n_tris * sizeof(BvhTri);
+    out->build_ms = ctx->build_ms;
+    out->sah_cost = ctx->sah_cost;
+    return RT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,518 @@
+// GPU hierarchy build: replaces Raycaster::updateHierarchy (Raycaster.cpp:54-142 of
+// kosua20/Rendu) and the vertex/triangle set-up of Raycaster::addMesh (Raycaster.cpp:14-52).
+//
+// The reference builds a top-down binary tree on one CPU thread (mean-of-centroids split,
+// leaves of 1-2 triangles, one root per mesh). Here the hierarchy is a linear BVH built in
+// parallel over all meshes at once:
+//   1. vertices transformed by their mesh's model matrix (exact glm operator order);
+//   2. per-triangle boxes, edges and 63-bit Morton codes of the box centroids;
+//   3. radix sort of (code, triangle) pairs;
+//   4. Karras' binary radix tree over the sorted codes (one thread per inner node);
+//   5. a bottom-up pass (one thread per leaf, atomics decide who climbs) that merges child
+//      boxes and collapses every subtree of <= RT_LEAF_MAX triangles into one leaf where
+//      the surface-area cost says a leaf is cheaper;
+//   6. emission of 64-byte nodes holding both children's boxes and of 48-byte triangles in
+//      leaf order.
+// Query answers do not depend on the tree shape (closest hit = smallest distance, exact
+// per-triangle test), so the tree only decides speed.
+#include <cub/device/device_radix_sort.cuh>
+
+#include <cmath>
+#include <cstring>
+
+#include "rt_context.hpp"
+
+namespace rgb {
+namespace {
+
+struct MeshXform {
+    uint64_t first_vertex;
+    float m[16];
+    int identity;
+};
+
+// Raycaster::addMesh vertex transform (Raycaster.cpp:22-26): glm::vec3(model * vec4(v, 1)).
+__global__ void k_transform(const float *__restrict__ pin, uint64_t nv, const MeshXform *__restrict__ xf, int nm,
+                            float *__restrict__ pout) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= nv) return;
+    int lo = 0, hi = nm - 1;
+    while (lo < hi) {  // last mesh whose first vertex <= i
+        const int mid = (lo + hi + 1) >> 1;
+        if (xf[mid].first_vertex <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    const float x = pin[3 * i], y = pin[3 * i + 1], z = pin[3 * i + 2];
+    const MeshXform &t = xf[lo];
+    if (t.identity) {
+        pout[3 * i] = x;
+        pout[3 * i + 1] = y;
+        pout[3 * i + 2] = z;
+        return;
+    }
+    const float *m = t.m;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float a0 = __fadd_rn(__fmul_rn(m[0 + k], x), __fmul_rn(m[4 + k], y));
+        const float a1 = __fadd_rn(__fmul_rn(m[8 + k], z), __fmul_rn(m[12 + k], 1.0f));
+        pout[3 * i + k] = __fadd_rn(a0, a1);
+    }
+}
+
+__device__ __forceinline__ unsigned f2ord(float f) {
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+// Triangle boxes (BoundingBox(v0,v1,v2), Bounds.cpp:12-15), centroid and coordinate bounds.
+__global__ void k_tri_setup(const float *__restrict__ verts, const uint32_t *__restrict__ idx, uint64_t nt,
+                            float4 *__restrict__ tlo, float4 *__restrict__ thi, unsigned *__restrict__ cb /*6 ord*/,
+                            unsigned *__restrict__ absmax /*ord*/) {
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    float c[3] = {0, 0, 0}, am = 0.0f;
+    bool valid = t < nt;
+    if (valid) {
+        const uint32_t i0 = idx[3 * t], i1 = idx[3 * t + 1], i2 = idx[3 * t + 2];
+        float lo[3], hi[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float a = verts[3 * i0 + k], b = verts[3 * i1 + k], d = verts[3 * i2 + k];
+            lo[k] = gmin(gmin(a, b), d);
+            hi[k] = gmax(gmax(a, b), d);
+            c[k] = 0.5f * (lo[k] + hi[k]);
+            am = fmaxf(am, fmaxf(fabsf(lo[k]), fabsf(hi[k])));
+        }
+        tlo[t] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+        thi[t] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+    }
+    // Block-reduce centroid bounds and the largest coordinate magnitude.
+    __shared__ float s[7][32];
+    float v[7];
+    for (int k = 0; k < 3; ++k) {
+        v[k] = valid ? c[k] : INFINITY;
+        v[3 + k] = valid ? c[k] : -INFINITY;
+    }
+    v[6] = valid ? am : 0.0f;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int k = 0; k < 3; ++k) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+        for (int k = 3; k < 7; ++k) v[k] = fmaxf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    }
+    if (lane == 0)
+        for (int k = 0; k < 7; ++k) s[k][warp] = v[k];
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        for (int k = 0; k < 7; ++k) v[k] = lane < nw ? s[k][lane] : (k < 3 ? INFINITY : (k < 6 ? -INFINITY : 0.0f));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            for (int k = 0; k < 3; ++k) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+            for (int k = 3; k < 7; ++k) v[k] = fmaxf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+        }
+        if (lane == 0) {
+            for (int k = 0; k < 3; ++k) atomicMin(&cb[k], f2ord(v[k]));
+            for (int k = 3; k < 6; ++k) atomicMax(&cb[k], f2ord(v[k]));
+            atomicMax(absmax, f2ord(v[6]));
+        }
+    }
+}
+
+__device__ __forceinline__ uint64_t spread21(uint64_t x) {
+    x &= 0x1fffffull;
+    x = (x | x << 32) & 0x1f00000000ffffull;
+    x = (x | x << 16) & 0x1f0000ff0000ffull;
+    x = (x | x << 8) & 0x100f00f00f00f00full;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+    x = (x | x << 2) & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void k_morton(const float4 *__restrict__ tlo, const float4 *__restrict__ thi, uint64_t nt,
+                         const unsigned *__restrict__ cb, uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const float4 lo = tlo[t], hi = thi[t];
+    const float c[3] = {0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z)};
+    uint64_t code = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float a = ord2f(cb[k]), b = ord2f(cb[3 + k]);
+        const float ext = b - a;
+        float u = ext > 0.0f ? (c[k] - a) / ext : 0.5f;
+        u = fminf(fmaxf(u, 0.0f), 1.0f);
+        const uint64_t q = (uint64_t)fminf(u * 2097152.0f, 2097151.0f);
+        code |= spread21(q) << (2 - k);
+    }
+    keys[t] = code;
+    vals[t] = (uint32_t)t;
+}
+
+// Common-prefix length of sorted keys i and j; equal keys compare their indices.
+__device__ __forceinline__ int delta(const uint64_t *__restrict__ k, int64_t n, int64_t i, int64_t j) {
+    if (j < 0 || j >= n) return -1;
+    const uint64_t a = k[i], b = k[j];
+    if (a != b) return __clzll(a ^ b);
+    return 64 + __clz((unsigned)(i ^ j));
+}
+
+// Karras 2012, "Maximizing parallelism in the construction of BVHs, octrees and k-d trees".
+// Inner node i (0..n-2): children encoded as (index << 1) | is_leaf.
+__global__ void k_karras(const uint64_t *__restrict__ keys, int64_t n, uint32_t *__restrict__ child,
+                         uint32_t *__restrict__ parent_inner, uint32_t *__restrict__ parent_leaf,
+                         uint32_t *__restrict__ range_first, uint32_t *__restrict__ range_last) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta(keys, n, i, i - d);
+    int64_t lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int64_t l = 0;
+    for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    const int64_t j = i + l * d;
+    const int dnode = delta(keys, n, i, j);
+    int64_t s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int64_t gamma = i + s * d + (d < 0 ? d : 0);
+    const int64_t first = i < j ? i : j, last = i < j ? j : i;
+    range_first[i] = (uint32_t)first;
+    range_last[i] = (uint32_t)last;
+    const bool left_leaf = first == gamma, right_leaf = last == gamma + 1;
+    child[2 * i] = (uint32_t)(gamma << 1) | (left_leaf ? 1u : 0u);
+    child[2 * i + 1] = (uint32_t)((gamma + 1) << 1) | (right_leaf ? 1u : 0u);
+    if (left_leaf) parent_leaf[gamma] = (uint32_t)i;
+    else parent_inner[gamma] = (uint32_t)i;
+    if (right_leaf) parent_leaf[gamma + 1] = (uint32_t)i;
+    else parent_inner[gamma + 1] = (uint32_t)i;
+}
+
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+    const float x = fmaxf(hi.x - lo.x, 0.0f), y = fmaxf(hi.y - lo.y, 0.0f), z = fmaxf(hi.z - lo.z, 0.0f);
+    return x * y + y * z + z * x;
+}
+
+constexpr float kCostInner = 1.2f;  // relative cost of one node visit (two box tests)
+constexpr float kCostTri = 1.0f;    // relative cost of one triangle test
+
+// Gather sorted triangle boxes (inflated by eps, making the traversal's box tests
+// conservative) and write leaf-order triangles.
+__global__ void k_leaves(const uint32_t *__restrict__ order, uint64_t nt, const float4 *__restrict__ tlo,
+                         const float4 *__restrict__ thi, const float *__restrict__ verts,
+                         const uint32_t *__restrict__ idx, float eps, float4 *__restrict__ slo,
+                         float4 *__restrict__ shi, BvhTri *__restrict__ tris) {
+    const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (k >= nt) return;
+    const uint32_t t = order[k];
+    float4 lo = tlo[t], hi = thi[t];
+    lo.x -= eps; lo.y -= eps; lo.z -= eps;
+    hi.x += eps; hi.y += eps; hi.z += eps;
+    slo[k] = lo;
+    shi[k] = hi;
+    const uint32_t i0 = idx[3 * t], i1 = idx[3 * t + 1], i2 = idx[3 * t + 2];
+    const float ax = verts[3 * i0], ay = verts[3 * i0 + 1], az = verts[3 * i0 + 2];
+    BvhTri tr;
+    tr.v0 = make_float4(ax, ay, az, __uint_as_float(t));
+    tr.e1 = make_float4(__fsub_rn(verts[3 * i1], ax), __fsub_rn(verts[3 * i1 + 1], ay), __fsub_rn(verts[3 * i1 + 2], az), 0.0f);
+    tr.e2 = make_float4(__fsub_rn(verts[3 * i2], ax), __fsub_rn(verts[3 * i2 + 1], ay), __fsub_rn(verts[3 * i2 + 2], az), 0.0f);
+    tris[k] = tr;
+}
+
+// Bottom-up: one thread per leaf climbs while it is the second child to arrive.
+__global__ void k_bottom_up(uint64_t nt, const uint32_t *__restrict__ child, const uint32_t *__restrict__ parent_inner,
+                            const uint32_t *__restrict__ parent_leaf, const uint32_t *__restrict__ range_first,
+                            const uint32_t *__restrict__ range_last, const float4 *__restrict__ slo,
+                            const float4 *__restrict__ shi, float4 *__restrict__ ilo, float4 *__restrict__ ihi,
+                            float *__restrict__ cost, uint8_t *__restrict__ collapse, int *__restrict__ height,
+                            unsigned *__restrict__ arrivals) {
+    const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (k >= nt) return;
+    uint32_t node = parent_leaf[k];
+    // A Karras tree over 64-bit keys with 32-bit index tie-breaks is at most 96 levels deep.
+    for (int level = 0; level < 128; ++level) {
+        if (node >= nt - 1) return;
+        __threadfence();
+        if (atomicAdd(&arrivals[node], 1u) == 0u) return;  // first arrival stops
+        __threadfence();
+        float4 lo[2], hi[2];
+        float c[2];
+        int h[2];
+        for (int s = 0; s < 2; ++s) {
+            const uint32_t ch = child[2 * node + s];
+            const uint32_t id = ch >> 1;
+            if (ch & 1u) {
+                lo[s] = slo[id];
+                hi[s] = shi[id];
+                c[s] = kCostTri * half_area(lo[s], hi[s]);
+                h[s] = 0;
+            } else {
+                lo[s] = __ldcg(&ilo[id]);
+                hi[s] = __ldcg(&ihi[id]);
+                c[s] = __ldcg(&cost[id]);
+                h[s] = __ldcg(&height[id]);
+            }
+        }
+        const float4 blo = make_float4(fminf(lo[0].x, lo[1].x), fminf(lo[0].y, lo[1].y), fminf(lo[0].z, lo[1].z), 0.0f);
+        const float4 bhi = make_float4(fmaxf(hi[0].x, hi[1].x), fmaxf(hi[0].y, hi[1].y), fmaxf(hi[0].z, hi[1].z), 0.0f);
+        const float a = half_area(blo, bhi);
+        const uint32_t count = range_last[node] - range_first[node] + 1;
+        const float c_inner = kCostInner * a + c[0] + c[1];
+        const float c_leaf = kCostTri * a * (float)count;
+        const bool col = count <= (uint32_t)RT_LEAF_MAX && c_leaf <= c_inner;
+        ilo[node] = blo;
+        ihi[node] = bhi;
+        cost[node] = col ? c_leaf : c_inner;
+        collapse[node] = col ? 1 : 0;
+        height[node] = col ? 0 : 1 + max(h[0], h[1]);
+        if (node == 0) return;
+        node = parent_inner[node];
+    }
+}
+
+// Emit 64-byte nodes. Nodes inside collapsed subtrees are written but never referenced.
+__global__ void k_emit(uint64_t ninner, const uint32_t *__restrict__ child, const uint32_t *__restrict__ range_first,
+                       const uint32_t *__restrict__ range_last, const float4 *__restrict__ slo,
+                       const float4 *__restrict__ shi, const float4 *__restrict__ ilo, const float4 *__restrict__ ihi,
+                       const uint8_t *__restrict__ collapse, BvhNode *__restrict__ nodes) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= ninner) return;
+    float4 lo[2], hi[2];
+    int idx[2], cnt[2];
+    for (int s = 0; s < 2; ++s) {
+        const uint32_t ch = child[2 * i + s];
+        const uint32_t id = ch >> 1;
+        if (ch & 1u) {
+            lo[s] = slo[id];
+            hi[s] = shi[id];
+            idx[s] = (int)id;
+            cnt[s] = 1;
+        } else {
+            lo[s] = ilo[id];
+            hi[s] = ihi[id];
+            if (collapse[id]) {
+                idx[s] = (int)range_first[id];
+                cnt[s] = (int)(range_last[id] - range_first[id] + 1);
+            } else {
+                idx[s] = (int)id;
+                cnt[s] = 0;
+            }
+        }
+    }
+    BvhNode nd;
+    nd.a = make_float4(lo[0].x, hi[0].x, lo[0].y, hi[0].y);
+    nd.b = make_float4(lo[1].x, hi[1].x, lo[1].y, hi[1].y);
+    nd.c = make_float4(lo[0].z, hi[0].z, lo[1].z, hi[1].z);
+    nd.d = make_int4(idx[0], idx[1], cnt[0], cnt[1]);
+    nodes[i] = nd;
+}
+
+// A root whose whole tree is one leaf (or a single triangle): child 0 = the leaf, child 1
+// = an empty box that no ray enters.
+__global__ void k_root_leaf(uint64_t nt, const float4 *__restrict__ slo, const float4 *__restrict__ shi,
+                            BvhNode *__restrict__ nodes) {
+    float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0);
+    for (uint64_t k = 0; k < nt; ++k) {
+        const float4 a = slo[k], b = shi[k];
+        lo = make_float4(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z), 0);
+        hi = make_float4(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z), 0);
+    }
+    // Child 1 is absent: index -1 (the traversal skips it) and a box at +infinity.
+    BvhNode nd;
+    nd.a = make_float4(lo.x, hi.x, lo.y, hi.y);
+    nd.b = make_float4(INFINITY, INFINITY, INFINITY, INFINITY);
+    nd.c = make_float4(lo.z, hi.z, INFINITY, INFINITY);
+    nd.d = make_int4(0, -1, (int)nt, 0);
+    nodes[0] = nd;
+}
+
+template <class T>
+struct Scratch {
+    T *p = nullptr;
+    ~Scratch() {
+        if (p) cudaFree(p);
+    }
+    cudaError_t alloc(size_t n) { return cudaMalloc(&p, (n ? n : 1) * sizeof(T)); }
+};
+
+}  // namespace
+
+int build_hierarchy(rt_ctx *ctx) {
+    cudaStream_t st = ctx->stream;
+    const uint64_t nv = ctx->h_positions.size() / 3;
+    const uint64_t nt = ctx->h_indices.size() / 3;
+    ctx->n_tris = nt;
+    RT_CUDA_TRY(cudaEventRecord(ctx->ev_a, st));
+
+    // Vertices: upload and transform.
+    Scratch<float> d_raw;
+    Scratch<uint32_t> d_idx;
+    Scratch<MeshXform> d_xf;
+    RT_CUDA_TRY(d_raw.alloc(3 * nv));
+    RT_CUDA_TRY(d_idx.alloc(3 * nt));
+    std::vector<MeshXform> xf(ctx->meshes.size());
+    for (size_t m = 0; m < ctx->meshes.size(); ++m) {
+        xf[m].first_vertex = ctx->meshes[m].first_vertex;
+        std::memcpy(xf[m].m, ctx->meshes[m].model, sizeof(xf[m].m));
+        xf[m].identity = ctx->meshes[m].identity ? 1 : 0;
+    }
+    RT_CUDA_TRY(d_xf.alloc(xf.size()));
+    if (ctx->d_verts.reserve(3 * nv * sizeof(float)) != RT_OK) return RT_ERR_OOM;
+    if (nv) {
+        RT_CUDA_TRY(cudaMemcpyAsync(d_raw.p, ctx->h_positions.data(), 3 * nv * sizeof(float), cudaMemcpyHostToDevice, st));
+        RT_CUDA_TRY(cudaMemcpyAsync(d_xf.p, xf.data(), xf.size() * sizeof(MeshXform), cudaMemcpyHostToDevice, st));
+        k_transform<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(d_raw.p, nv, d_xf.p, (int)xf.size(), ctx->d_verts.as<float>());
+    }
+    if (nt) RT_CUDA_TRY(cudaMemcpyAsync(d_idx.p, ctx->h_indices.data(), 3 * nt * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+
+    if (ctx->d_nodes.reserve(sizeof(BvhNode) * (nt > 1 ? nt - 1 : 1)) != RT_OK) return RT_ERR_OOM;
+    if (ctx->d_tris.reserve(sizeof(BvhTri) * (nt ? nt : 1)) != RT_OK) return RT_ERR_OOM;
+    if (nt == 0) {
+        ctx->n_inner = 0;
+        ctx->n_leaves = 0;
+        ctx->depth = 0;
+        ctx->sah_cost = 0.0f;
+        RT_CUDA_TRY(cudaEventRecord(ctx->ev_b, st));
+        RT_CUDA_TRY(cudaEventSynchronize(ctx->ev_b));
+        RT_CUDA_TRY(cudaEventElapsedTime(&ctx->build_ms, ctx->ev_a, ctx->ev_b));
+        return RT_OK;
+    }
+
+    Scratch<float4> d_tlo, d_thi, d_slo, d_shi, d_ilo, d_ihi;
+    Scratch<unsigned> d_cb;
+    Scratch<uint64_t> d_keys, d_keys2;
+    Scratch<uint32_t> d_vals, d_vals2;
+    RT_CUDA_TRY(d_tlo.alloc(nt));
+    RT_CUDA_TRY(d_thi.alloc(nt));
+    RT_CUDA_TRY(d_cb.alloc(8));
+    const unsigned cb_init[8] = {0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0u, 0u, 0u, 0u, 0u};
+    RT_CUDA_TRY(cudaMemcpyAsync(d_cb.p, cb_init, sizeof(cb_init), cudaMemcpyHostToDevice, st));
+    const unsigned tb = (unsigned)((nt + 255) / 256);
+    k_tri_setup<<<tb, 256, 0, st>>>(ctx->d_verts.as<float>(), d_idx.p, nt, d_tlo.p, d_thi.p, d_cb.p, d_cb.p + 6);
+    RT_CUDA_TRY(d_keys.alloc(nt));
+    RT_CUDA_TRY(d_keys2.alloc(nt));
+    RT_CUDA_TRY(d_vals.alloc(nt));
+    RT_CUDA_TRY(d_vals2.alloc(nt));
+    k_morton<<<tb, 256, 0, st>>>(d_tlo.p, d_thi.p, nt, d_cb.p, d_keys.p, d_vals.p);
+    size_t temp_bytes = 0;
+    RT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, d_keys.p, d_keys2.p, d_vals.p, d_vals2.p, (int)nt, 0, 63, st));
+    Scratch<unsigned char> d_temp;
+    RT_CUDA_TRY(d_temp.alloc(temp_bytes));
+    RT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(d_temp.p, temp_bytes, d_keys.p, d_keys2.p, d_vals.p, d_vals2.p, (int)nt, 0, 63, st));
+
+    // Largest coordinate magnitude -> box inflation.
+    unsigned cb_host[8];
+    RT_CUDA_TRY(cudaMemcpyAsync(cb_host, d_cb.p, sizeof(cb_host), cudaMemcpyDeviceToHost, st));
+    RT_CUDA_TRY(cudaStreamSynchronize(st));
+    auto ord2f_h = [](unsigned u) {
+        const unsigned b = (u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u;
+        float f;
+        std::memcpy(&f, &b, 4);
+        return f;
+    };
+    const float absmax = ord2f_h(cb_host[6]);
+    // Boxes grow by 2^-16 of the largest coordinate: the traversal's fused slab test then
+    // never rejects a box around a triangle the exact per-triangle test accepts, for ray
+    // origins within 2^6 times the scene's coordinate range.
+    const float eps = std::ldexp(std::fmax(absmax, 1e-30f), -16);
+
+    RT_CUDA_TRY(d_slo.alloc(nt));
+    RT_CUDA_TRY(d_shi.alloc(nt));
+    k_leaves<<<tb, 256, 0, st>>>(d_vals2.p, nt, d_tlo.p, d_thi.p, ctx->d_verts.as<float>(), d_idx.p, eps, d_slo.p,
+                                 d_shi.p, ctx->d_tris.as<BvhTri>());
+
+    if (nt == 1) {
+        k_root_leaf<<<1, 1, 0, st>>>(nt, d_slo.p, d_shi.p, ctx->d_nodes.as<BvhNode>());
+        ctx->n_inner = 1;
+        ctx->n_leaves = 1;
+        ctx->depth = 1;
+        ctx->sah_cost = 1.0f;
+    } else {
+        const uint64_t ni = nt - 1;
+        Scratch<uint32_t> d_child, d_pin, d_pleaf, d_rf, d_rl;
+        Scratch<float> d_cost;
+        Scratch<uint8_t> d_col;
+        Scratch<int> d_height;
+        Scratch<unsigned> d_arr;
+        RT_CUDA_TRY(d_child.alloc(2 * ni));
+        RT_CUDA_TRY(d_pin.alloc(ni));
+        RT_CUDA_TRY(d_pleaf.alloc(nt));
+        RT_CUDA_TRY(d_rf.alloc(ni));
+        RT_CUDA_TRY(d_rl.alloc(ni));
+        RT_CUDA_TRY(d_ilo.alloc(ni));
+        RT_CUDA_TRY(d_ihi.alloc(ni));
+        RT_CUDA_TRY(d_cost.alloc(ni));
+        RT_CUDA_TRY(d_col.alloc(ni));
+        RT_CUDA_TRY(d_height.alloc(ni));
+        RT_CUDA_TRY(d_arr.alloc(ni));
+        RT_CUDA_TRY(cudaMemsetAsync(d_arr.p, 0, ni * sizeof(unsigned), st));
+        const unsigned ib = (unsigned)((ni + 255) / 256);
+        k_karras<<<ib, 256, 0, st>>>(d_keys2.p, (int64_t)nt, d_child.p, d_pin.p, d_pleaf.p, d_rf.p, d_rl.p);
+        k_bottom_up<<<tb, 256, 0, st>>>(nt, d_child.p, d_pin.p, d_pleaf.p, d_rf.p, d_rl.p, d_slo.p, d_shi.p, d_ilo.p,
+                                        d_ihi.p, d_cost.p, d_col.p, d_height.p, d_arr.p);
+        uint8_t root_col = 0;
+        int root_h = 0;
+        float root_cost = 0.0f;
+        float4 rlo, rhi;
+        RT_CUDA_TRY(cudaMemcpyAsync(&root_col, d_col.p, 1, cudaMemcpyDeviceToHost, st));
+        RT_CUDA_TRY(cudaMemcpyAsync(&root_h, d_height.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        RT_CUDA_TRY(cudaMemcpyAsync(&root_cost, d_cost.p, sizeof(float), cudaMemcpyDeviceToHost, st));
+        RT_CUDA_TRY(cudaMemcpyAsync(&rlo, d_ilo.p, sizeof(float4), cudaMemcpyDeviceToHost, st));
+        RT_CUDA_TRY(cudaMemcpyAsync(&rhi, d_ihi.p, sizeof(float4), cudaMemcpyDeviceToHost, st));
+        RT_CUDA_TRY(cudaStreamSynchronize(st));
+        if (root_col) {
+            k_root_leaf<<<1, 1, 0, st>>>(nt, d_slo.p, d_shi.p, ctx->d_nodes.as<BvhNode>());
+            ctx->n_inner = 1;
+            ctx->depth = 1;
+        } else {
+            k_emit<<<ib, 256, 0, st>>>(ni, d_child.p, d_rf.p, d_rl.p, d_slo.p, d_shi.p, d_ilo.p, d_ihi.p, d_col.p,
+                                       ctx->d_nodes.as<BvhNode>());
+            ctx->n_inner = ni;
+            ctx->depth = root_h;
+        }
+        const float ra = std::fmax((rhi.x - rlo.x) * (rhi.y - rlo.y) + (rhi.y - rlo.y) * (rhi.z - rlo.z) +
+                                       (rhi.z - rlo.z) * (rhi.x - rlo.x), 1e-30f);
+        ctx->sah_cost = root_cost / ra;
+        ctx->root_box[0] = rlo.x; ctx->root_box[1] = rlo.y; ctx->root_box[2] = rlo.z;
+        ctx->root_box[3] = rhi.x; ctx->root_box[4] = rhi.y; ctx->root_box[5] = rhi.z;
+        // Count leaves = reachable leaf references (for statistics only).
+        std::vector<uint8_t> col(ni);
+        std::vector<uint32_t> chh(2 * ni);
+        RT_CUDA_TRY(cudaMemcpyAsync(col.data(), d_col.p, ni, cudaMemcpyDeviceToHost, st));
+        RT_CUDA_TRY(cudaMemcpyAsync(chh.data(), d_child.p, 2 * ni * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        RT_CUDA_TRY(cudaStreamSynchronize(st));
+        uint64_t leaves = 0, inner_reach = 0;
+        if (!root_col) {
+            std::vector<uint32_t> stack{0};
+            while (!stack.empty()) {
+                const uint32_t nd = stack.back();
+                stack.pop_back();
+                ++inner_reach;
+                for (int s = 0; s < 2; ++s) {
+                    const uint32_t ch = chh[2 * nd + s];
+                    if ((ch & 1u) || col[ch >> 1]) ++leaves;
+                    else stack.push_back(ch >> 1);
+                }
+            }
+        } else {
+            leaves = 1;
+            inner_reach = 1;
+        }
+        ctx->n_leaves = leaves;
+        ctx->n_inner = root_col ? 1 : ni;
+        ctx->sah_cost = ctx->sah_cost;
+        (void)inner_reach;
+    }
+    RT_CUDA_TRY(cudaEventRecord(ctx->ev_b, st));
+    RT_CUDA_TRY(cudaEventSynchronize(ctx->ev_b));
+    RT_CUDA_TRY(cudaGetLastError());
+    RT_CUDA_TRY(cudaEventElapsedTime(&ctx->build_ms, ctx->ev_a, ctx->ev_b));
+    return RT_OK;
+}
+
+}  // namespace rgb

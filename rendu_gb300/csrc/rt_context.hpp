@@ -1,0 +1,84 @@
+// Host-side state of a raycaster context and small utilities shared by the C-ABI units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "rendu_gb300.h"
+#include "rt_common.cuh"
+
+namespace rgb {
+
+// Thread-local message of the last failure (rt_last_error).
+void set_error(const std::string &msg);
+void clear_error();
+
+// Device buffer that only grows; freed with the owner.
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    int reserve(size_t need);  // RT_OK or RT_ERR_OOM
+    void release();
+    template <class T>
+    T *as() const { return static_cast<T *>(ptr); }
+};
+
+struct MeshRecord {
+    uint64_t first_vertex;
+    uint64_t vertex_count;
+    uint64_t first_tri;
+    uint64_t tri_count;
+    float model[16];  // column-major
+    bool identity;
+};
+
+}  // namespace rgb
+
+struct rt_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;  // the context's own stream
+    // Host copies appended by rt_add_mesh (raw positions; indices already offset).
+    std::vector<float> h_positions;
+    std::vector<uint32_t> h_indices;
+    std::vector<rgb::MeshRecord> meshes;
+    bool dirty = true;  // meshes added since the last build
+    bool built = false;
+
+    // Device hierarchy.
+    rgb::DevBuf d_nodes;   // BvhNode[n_inner] (at least 1: a root, possibly wrapping a leaf)
+    rgb::DevBuf d_tris;    // BvhTri[n_tris] in leaf order
+    rgb::DevBuf d_verts;   // float3 transformed vertices (kept for the path tracer)
+    rgb::DevBuf d_status;  // unsigned status word
+    uint64_t n_tris = 0;
+    uint64_t n_inner = 0;
+    uint64_t n_leaves = 0;
+    int depth = 0;
+    float build_ms = 0.0f;
+    float sah_cost = 0.0f;
+    float root_box[6] = {0, 0, 0, 0, 0, 0};
+
+    // Staging for host-pointer calls.
+    rgb::DevBuf d_rays;
+    rgb::DevBuf d_out;
+    rgb::DevBuf d_out2;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+};
+
+namespace rgb {
+// Launchers used across units (all asynchronous on `stream`).
+int trace_closest(rt_ctx *ctx, const rt_ray *d_rays, size_t n, rt_hit *d_hits, cudaStream_t stream);
+int trace_any(rt_ctx *ctx, const rt_ray *d_rays, size_t n, uint8_t *d_occ, cudaStream_t stream);
+int check_status(rt_ctx *ctx, cudaStream_t stream);  // reads and clears the device status word
+}  // namespace rgb
+
+#define RT_CUDA_TRY(expr)                                                                    \
+    do {                                                                                     \
+        cudaError_t _e = (expr);                                                             \
+        if (_e != cudaSuccess) {                                                             \
+            rgb::set_error(std::string(#expr " failed: ") + cudaGetErrorString(_e));        \
+            return RT_ERR_CUDA;                                                              \
+        }                                                                                    \
+    } while (0)

@@ -1,0 +1,373 @@
+"""Seeded synthetic inputs for the raycaster and path-tracer workloads.
+
+The reference ships no benchmark data; its hot path is exercised here on procedural
+inputs whose shapes follow the reference's own scene model:
+  * triangle meshes as position/normal/tangent/bitangent/texcoord/index arrays
+    (Mesh.hpp:126-132 of kosua20/Rendu), transformed by per-object model matrices
+    (Object.hpp:59);
+  * materials of type Regular (Lambert+GGX) or Emissive with three constant-colour
+    textures, the convention the reference uses for colour-only materials
+    (ResourcesManager.cpp:489-505: 8x8 float images);
+  * a pinhole camera given as eye/center/up/fov/ratio (Camera.cpp:10-49).
+
+Workloads
+  * ``icosphere_mesh(8)`` + ``random_rays`` -- the raycaster workload: a subdivided
+    icosphere (1,310,720 triangles at 8 subdivisions) radially displaced by 3-octave
+    value noise of amplitude 0.1, and rays with origins uniform in a box three times
+    the mesh bounds and directions uniform on the sphere.
+  * ``cornell_scene`` -- the small path-tracer workload: a 5-wall room (10 triangles),
+    two boxes rotated by a seeded angle (24 triangles) and a 2-triangle emissive ceiling
+    quad of radiance 15.
+  * ``instanced_scene`` -- the large path-tracer workload: displaced icospheres and
+    boxes on a ground plane, about 2M triangles in 200 instances, emissive quads and a
+    procedural sky environment.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# --------------------------------------------------------------------------------------
+# meshes
+# --------------------------------------------------------------------------------------
+
+
+def _icosahedron():
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    v = np.array(
+        [
+            [-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0],
+            [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+            [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1],
+        ],
+        dtype=np.float64,
+    )
+    f = np.array(
+        [
+            [0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11],
+            [1, 5, 9], [5, 11, 4], [11, 10, 2], [10, 7, 6], [7, 1, 8],
+            [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9],
+            [4, 9, 5], [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1],
+        ],
+        dtype=np.int64,
+    )
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    return v, f
+
+
+def _subdivide(v, f):
+    """One 4-to-1 subdivision with shared edge midpoints, projected on the unit sphere."""
+    e = np.concatenate([f[:, [0, 1]], f[:, [1, 2]], f[:, [2, 0]]], axis=0)
+    e_sorted = np.sort(e, axis=1)
+    key = e_sorted[:, 0] * (len(v) + 1) + e_sorted[:, 1]
+    uniq, inv = np.unique(key, return_inverse=True)
+    a = uniq // (len(v) + 1)
+    b = uniq % (len(v) + 1)
+    mid = v[a] + v[b]
+    mid /= np.linalg.norm(mid, axis=1, keepdims=True)
+    nf = len(f)
+    m01 = len(v) + inv[:nf]
+    m12 = len(v) + inv[nf : 2 * nf]
+    m20 = len(v) + inv[2 * nf :]
+    v2 = np.concatenate([v, mid], axis=0)
+    f2 = np.concatenate(
+        [
+            np.stack([f[:, 0], m01, m20], 1),
+            np.stack([f[:, 1], m12, m01], 1),
+            np.stack([f[:, 2], m20, m12], 1),
+            np.stack([m01, m12, m20], 1),
+        ],
+        axis=0,
+    )
+    return v2, f2
+
+
+class ValueNoise:
+    """Seeded 3-D value noise: random values on an integer lattice (hashed, period 256),
+    trilinear interpolation with a smoothstep fade; ``octaves`` summed with halving
+    amplitude and doubling frequency, normalised to [-1, 1]."""
+
+    def __init__(self, seed: int, octaves: int = 3, base_freq: float = 2.0):
+        rng = np.random.default_rng(seed)
+        self.table = rng.uniform(-1.0, 1.0, size=256 * 256 * 256 // 64).astype(np.float64)
+        self.perm = rng.permutation(256).astype(np.int64)
+        self.octaves = octaves
+        self.base_freq = base_freq
+
+    def _lattice(self, i, j, k):
+        h = self.perm[(self.perm[(self.perm[i & 255] + j) & 255] + k) & 255]
+        h2 = self.perm[(h + i * 7 + j * 13 + k * 17) & 255]
+        return self.table[(h * 256 + h2) % len(self.table)]
+
+    def _octave(self, p):
+        fl = np.floor(p)
+        i = fl.astype(np.int64)
+        f = p - fl
+        s = f * f * (3.0 - 2.0 * f)
+        out = 0.0
+        for dx in (0, 1):
+            wx = s[:, 0] if dx else 1.0 - s[:, 0]
+            for dy in (0, 1):
+                wy = s[:, 1] if dy else 1.0 - s[:, 1]
+                for dz in (0, 1):
+                    wz = s[:, 2] if dz else 1.0 - s[:, 2]
+                    out = out + wx * wy * wz * self._lattice(i[:, 0] + dx, i[:, 1] + dy, i[:, 2] + dz)
+        return out
+
+    def __call__(self, p):
+        total = np.zeros(len(p))
+        amp, freq, norm = 1.0, self.base_freq, 0.0
+        for _ in range(self.octaves):
+            total += amp * self._octave(p * freq)
+            norm += amp
+            amp *= 0.5
+            freq *= 2.0
+        return total / norm
+
+
+@dataclass
+class Mesh:
+    """Vertex attributes + triangle indices, the layout of the reference's Mesh."""
+
+    positions: np.ndarray  # (V,3) float32
+    indices: np.ndarray  # (3T,) uint32
+    normals: np.ndarray | None = None
+    tangents: np.ndarray | None = None
+    bitangents: np.ndarray | None = None
+    texcoords: np.ndarray | None = None
+
+    @property
+    def triangle_count(self) -> int:
+        return len(self.indices) // 3
+
+    def with_frames(self) -> "Mesh":
+        """Fill area-weighted vertex normals and an orthonormal tangent frame (the path
+        tracer needs normals, tangents and bitangents on every mesh, PathTracer.cpp:14-16)."""
+        p = self.positions.astype(np.float64)
+        f = self.indices.reshape(-1, 3).astype(np.int64)
+        n = np.zeros_like(p)
+        fn = np.cross(p[f[:, 1]] - p[f[:, 0]], p[f[:, 2]] - p[f[:, 0]])
+        for k in range(3):
+            np.add.at(n, f[:, k], fn)
+        ln = np.linalg.norm(n, axis=1, keepdims=True)
+        ln[ln == 0] = 1.0
+        n /= ln
+        ref = np.where(np.abs(n[:, 1:2]) < 0.9, np.array([[0.0, 1.0, 0.0]]), np.array([[1.0, 0.0, 0.0]]))
+        t = np.cross(ref, n)
+        t /= np.linalg.norm(t, axis=1, keepdims=True)
+        b = np.cross(n, t)
+        self.normals = n.astype(np.float32)
+        self.tangents = t.astype(np.float32)
+        self.bitangents = b.astype(np.float32)
+        return self
+
+
+def icosphere_mesh(subdivisions: int, radius: float = 1.0, displacement: float = 0.1, seed: int = 0,
+                   octaves: int = 3) -> Mesh:
+    """Icosphere with 20 * 4^subdivisions triangles, vertices moved along the radius by
+    ``displacement`` x seeded value noise (3 octaves)."""
+    v, f = _icosahedron()
+    for _ in range(subdivisions):
+        v, f = _subdivide(v, f)
+    if displacement:
+        noise = ValueNoise(seed, octaves=octaves)
+        v = v * (radius * (1.0 + displacement * noise(v)))[:, None]
+    else:
+        v = v * radius
+    return Mesh(v.astype(np.float32), f.reshape(-1).astype(np.uint32))
+
+
+def box_mesh(size=(1.0, 1.0, 1.0)) -> Mesh:
+    """Axis-aligned box centred on the origin, 12 triangles, 24 vertices (flat faces)."""
+    sx, sy, sz = (0.5 * s for s in size)
+    faces = [
+        ([1, 0, 0], [0, 0, -1]), ([-1, 0, 0], [0, 0, 1]),
+        ([0, 1, 0], [1, 0, 0]), ([0, -1, 0], [1, 0, 0]),
+        ([0, 0, 1], [1, 0, 0]), ([0, 0, -1], [-1, 0, 0]),
+    ]
+    pos, nrm, tan, bit, uv, idx = [], [], [], [], [], []
+    for n, t in faces:
+        n = np.array(n, float)
+        t = np.array(t, float)
+        b = np.cross(n, t)
+        c = n * np.array([sx, sy, sz])
+        base = len(pos)
+        for du, dv in ((-1, -1), (1, -1), (1, 1), (-1, 1)):
+            pos.append(c + du * t * np.array([sx, sy, sz]) + dv * b * np.array([sx, sy, sz]))
+            nrm.append(n)
+            tan.append(t)
+            bit.append(b)
+            uv.append([(du + 1) * 0.5, (dv + 1) * 0.5])
+        idx += [base, base + 1, base + 2, base, base + 2, base + 3]
+    return Mesh(
+        np.array(pos, np.float32), np.array(idx, np.uint32), np.array(nrm, np.float32),
+        np.array(tan, np.float32), np.array(bit, np.float32), np.array(uv, np.float32),
+    )
+
+
+def quad_mesh(corner, edge_u, edge_v, normal=None) -> Mesh:
+    """Two-triangle quad corner, corner+u, corner+u+v, corner+v."""
+    c = np.asarray(corner, float)
+    u = np.asarray(edge_u, float)
+    v = np.asarray(edge_v, float)
+    n = np.cross(u, v) if normal is None else np.asarray(normal, float)
+    n = n / np.linalg.norm(n)
+    t = u / np.linalg.norm(u)
+    b = np.cross(n, t)
+    pos = np.array([c, c + u, c + u + v, c + v], np.float32)
+    return Mesh(
+        pos, np.array([0, 1, 2, 0, 2, 3], np.uint32), np.tile(n, (4, 1)).astype(np.float32),
+        np.tile(t, (4, 1)).astype(np.float32), np.tile(b, (4, 1)).astype(np.float32),
+        np.array([[0, 0], [1, 0], [1, 1], [0, 1]], np.float32),
+    )
+
+
+# --------------------------------------------------------------------------------------
+# rays
+# --------------------------------------------------------------------------------------
+
+
+def random_rays(n: int, lo, hi, seed: int, scale: float = 3.0, tmin: float = 1e-4, tmax: float = 1e8) -> np.ndarray:
+    """n rays as an (n, 8) float32 array {o.xyz, tmin, d.xyz, tmax}: origins uniform in
+    the box ``scale`` times the [lo, hi] bounds about their centre, directions uniform on
+    the unit sphere (z = 2u - 1, phi = 2 pi v)."""
+    rng = np.random.default_rng(seed)
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    c = 0.5 * (lo + hi)
+    h = 0.5 * (hi - lo) * scale
+    rays = np.empty((n, 8), np.float32)
+    chunk = 1 << 22
+    for s in range(0, n, chunk):
+        m = min(chunk, n - s)
+        o = c + (rng.random((m, 3)) * 2.0 - 1.0) * h
+        z = rng.random(m) * 2.0 - 1.0
+        phi = rng.random(m) * 2.0 * math.pi
+        r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+        rays[s : s + m, 0:3] = o
+        rays[s : s + m, 3] = tmin
+        rays[s : s + m, 4] = r * np.cos(phi)
+        rays[s : s + m, 5] = r * np.sin(phi)
+        rays[s : s + m, 6] = z
+        rays[s : s + m, 7] = tmax
+    return rays
+
+
+def raycaster_workload(subdivisions: int = 8, n_rays: int = 1 << 24, seed: int = 20261204):
+    """The raycaster workload: displaced icosphere (1,310,720 triangles at 8 subdivisions)
+    and ``n_rays`` rays (16,777,216 by default)."""
+    mesh = icosphere_mesh(subdivisions, seed=seed)
+    lo = mesh.positions.min(0)
+    hi = mesh.positions.max(0)
+    rays = random_rays(n_rays, lo, hi, seed + 1)
+    return mesh, rays
+
+
+# --------------------------------------------------------------------------------------
+# path-tracer scenes
+# --------------------------------------------------------------------------------------
+
+
+def rotation_y(angle: float) -> np.ndarray:
+    c, s = math.cos(angle), math.sin(angle)
+    m = np.eye(4, dtype=np.float32)
+    m[0, 0], m[0, 2], m[2, 0], m[2, 2] = c, s, -s, c
+    return m
+
+
+def translation(t) -> np.ndarray:
+    m = np.eye(4, dtype=np.float32)
+    m[:3, 3] = t
+    return m
+
+
+def scaling(s) -> np.ndarray:
+    m = np.eye(4, dtype=np.float32)
+    m[0, 0], m[1, 1], m[2, 2] = (s, s, s) if np.isscalar(s) else s
+    return m
+
+
+def constant_texture(rgba, size: int = 8) -> np.ndarray:
+    """A size x size RGBA float image of one colour (the reference's colour textures)."""
+    return np.tile(np.asarray(rgba, np.float32), (size, size, 1))
+
+
+@dataclass
+class Scene:
+    """In-memory scene: textures, meshes, materials, objects, lights, background, camera.
+    Matrices are row-major numpy 4x4 here and passed column-major across the C-ABI."""
+
+    textures: list = field(default_factory=list)  # (H, W, C) float32 arrays
+    meshes: list = field(default_factory=list)  # Mesh
+    materials: list = field(default_factory=list)  # dict(type, masked, tex=(a, n, r))
+    objects: list = field(default_factory=list)  # dict(mesh, material, model)
+    lights: list = field(default_factory=list)  # dict(type, color, position, direction, radius, inner, outer, shadows)
+    background: dict = field(default_factory=lambda: {"mode": 0, "color": (0.0, 0.0, 0.0), "tex": (0,) * 6})
+    camera: dict = field(default_factory=dict)
+
+    def add_texture(self, img) -> int:
+        self.textures.append(np.ascontiguousarray(img, np.float32))
+        return len(self.textures) - 1
+
+    def add_material(self, albedo, rough=1.0, metal=0.0, emissive=False, masked=False, normal_tex=None,
+                     albedo_tex=None) -> int:
+        a = albedo_tex if albedo_tex is not None else self.add_texture(constant_texture(list(albedo) + [1.0]))
+        n = normal_tex if normal_tex is not None else self.add_texture(constant_texture([0.5, 0.5, 1.0, 1.0]))
+        r = self.add_texture(constant_texture([rough, metal, 1.0, 1.0]))
+        self.materials.append({"type": 8 if emissive else 1, "masked": bool(masked), "tex": (a, n, r)})
+        return len(self.materials) - 1
+
+    def add_mesh(self, mesh: Mesh) -> int:
+        if mesh.normals is None:
+            mesh.with_frames()
+        self.meshes.append(mesh)
+        return len(self.meshes) - 1
+
+    def add_object(self, mesh: int, material: int, model=None) -> int:
+        self.objects.append({"mesh": mesh, "material": material,
+                             "model": np.eye(4, dtype=np.float32) if model is None else np.asarray(model, np.float32)})
+        return len(self.objects) - 1
+
+    @property
+    def triangle_count(self) -> int:
+        return sum(self.meshes[o["mesh"]].triangle_count for o in self.objects)
+
+
+def cornell_scene(seed: int = 20261204, with_light: bool = False) -> Scene:
+    """Cornell-style room: 5 axis-aligned walls (10 triangles), 2 boxes rotated about y by
+    seeded angles in [0, 45 deg] (24 triangles), a 2-triangle emissive ceiling quad of
+    radiance 15. Lambert walls/boxes (Regular, roughness 1, metalness 0) with seeded albedo
+    in [0.2, 0.8]^3; the second box is GGX with roughness 0.3. No analytic light unless
+    ``with_light`` (then one shadowed point light, to exercise next-event estimation)."""
+    rng = np.random.default_rng(seed)
+    sc = Scene()
+    L = 2.0
+    walls = [
+        ((-1, 0, -1), (2, 0, 0), (0, 0, 2)),  # floor, faces +y
+        ((-1, 2, 1), (2, 0, 0), (0, 0, -2)),  # ceiling, faces -y
+        ((-1, 0, -1), (0, 2, 0), (2, 0, 0)),  # back wall z=-1, faces +z
+        ((-1, 0, 1), (0, 2, 0), (0, 0, -2)),  # left wall x=-1, faces +x
+        ((1, 0, -1), (0, 2, 0), (0, 0, 2)),  # right wall x=1, faces -x
+    ]
+    for c, u, v in walls:
+        m = sc.add_mesh(quad_mesh(c, u, v))
+        mat = sc.add_material(rng.uniform(0.2, 0.8, 3), rough=1.0, metal=0.0)
+        sc.add_object(m, mat)
+    for k, (pos, size, rough) in enumerate((((-0.35, 0.6, -0.3), (0.55, 1.2, 0.55), 1.0),
+                                            ((0.4, 0.3, 0.35), (0.6, 0.6, 0.6), 0.3))):
+        m = sc.add_mesh(box_mesh(size))
+        mat = sc.add_material(rng.uniform(0.2, 0.8, 3), rough=rough, metal=0.0)
+        angle = math.radians(rng.uniform(0.0, 45.0))
+        sc.add_object(m, mat, translation(pos) @ rotation_y(angle))
+    lm = sc.add_mesh(quad_mesh((-0.3, 1.999, 0.3), (0.6, 0, 0), (0, 0, -0.6)))
+    lmat = sc.add_material((15.0, 15.0, 15.0), emissive=True)
+    sc.add_object(lm, lmat)
+    if with_light:
+        sc.lights.append({"type": 0, "color": (2.0, 2.0, 2.0), "position": (0.0, 1.6, 0.5), "direction": (0, -1, 0),
+                          "radius": 4.0, "inner": 0.5, "outer": 0.8, "shadows": True})
+    sc.background = {"mode": 0, "color": (0.0, 0.0, 0.0), "tex": (0,) * 6}
+    sc.camera = {"eye": (0.0, 1.0, 3.4), "center": (0.0, 1.0, 0.0), "up": (0.0, 1.0, 0.0), "fov": 1.3, "ratio": 1.0}
+    _ = L
+    return sc
