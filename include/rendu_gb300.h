@@ -27,6 +27,12 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define RT_API __attribute__((visibility("default")))
+#else
+#define RT_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -82,51 +88,51 @@ typedef struct rt_ctx rt_ctx;
 
 /* Create a raycaster on CUDA device `device`. Replaces Raycaster::Raycaster()
  * (Raycaster.hpp:46). */
-int rt_create(rt_ctx **ctx, int device);
+RT_API int rt_create(rt_ctx **ctx, int device);
 
 /* Release all device and host memory of the context. */
-int rt_destroy(rt_ctx *ctx);
+RT_API int rt_destroy(rt_ctx *ctx);
 
 /* Append a triangle mesh, its vertices transformed by `model` (skipped when NULL or the
  * identity, as at Raycaster.cpp:22-26). positions: vertex_count x 3 floats; indices:
  * index_count uint32 (a multiple of 3, each < vertex_count). *mesh_id receives the mesh
  * index (addMesh call order). Replaces Raycaster::addMesh (Raycaster.cpp:14-52). */
-int rt_add_mesh(rt_ctx *ctx, const float *positions, size_t vertex_count, const uint32_t *indices,
+RT_API int rt_add_mesh(rt_ctx *ctx, const float *positions, size_t vertex_count, const uint32_t *indices,
                 size_t index_count, const float *model, uint32_t *mesh_id);
 
 /* Build the device hierarchy over every mesh added so far. Replaces
  * Raycaster::updateHierarchy (Raycaster.cpp:54-142); the hierarchy differs (a GPU LBVH
  * with surface-area leaf collapsing) but every query answers the same. */
-int rt_update_hierarchy(rt_ctx *ctx);
+RT_API int rt_update_hierarchy(rt_ctx *ctx);
 
 /* Closest hit for n rays. Replaces Raycaster::intersects(origin, direction, mini, maxi)
  * (Raycaster.cpp:144-185) for a batch. Ties at exactly equal distance go to the smaller
  * prim id (the reference keeps the first found in its own traversal order). */
-int rt_intersect(rt_ctx *ctx, const rt_ray *rays, size_t n, rt_hit *hits, void *stream, uint32_t flags);
+RT_API int rt_intersect(rt_ctx *ctx, const rt_ray *rays, size_t n, rt_hit *hits, void *stream, uint32_t flags);
 
 /* Occlusion for n rays: occluded[i] = 1 if any triangle is hit inside (tmin, tmax).
  * Replaces Raycaster::intersectsAny (Raycaster.cpp:187-224). */
-int rt_intersect_any(rt_ctx *ctx, const rt_ray *rays, size_t n, uint8_t *occluded, void *stream, uint32_t flags);
+RT_API int rt_intersect_any(rt_ctx *ctx, const rt_ray *rays, size_t n, uint8_t *occluded, void *stream, uint32_t flags);
 
 /* Segment visibility for n point pairs: segs is n x 6 floats {p0.xyz, p1.xyz};
  * visible[i] = 1 when nothing is hit between them. Replaces Raycaster::visible
  * (Raycaster.cpp:226-230): window (1e-4, |p1 - p0|). */
-int rt_visible(rt_ctx *ctx, const float *segs, size_t n, uint8_t *visible, void *stream, uint32_t flags);
+RT_API int rt_visible(rt_ctx *ctx, const float *segs, size_t n, uint8_t *visible, void *stream, uint32_t flags);
 
 /* Map a global triangle id to (meshId, localId) as stored in Raycaster::Hit. */
-int rt_prim_info(const rt_ctx *ctx, uint32_t prim, uint32_t *mesh_id, uint32_t *local_id);
+RT_API int rt_prim_info(const rt_ctx *ctx, uint32_t prim, uint32_t *mesh_id, uint32_t *local_id);
 
 /* Statistics of the current hierarchy. */
-int rt_get_stats(const rt_ctx *ctx, rt_stats *out);
+RT_API int rt_get_stats(const rt_ctx *ctx, rt_stats *out);
 
 /* Count, for each ray, the inner nodes and triangles the device traversal visits
  * (closest-hit mode). node_visits / tri_visits are n uint32 each (host or device per
  * flags). Used to state the algorithmic bytes per ray of the roofline. */
-int rt_count_visits(rt_ctx *ctx, const rt_ray *rays, size_t n, uint32_t *node_visits, uint32_t *tri_visits,
+RT_API int rt_count_visits(rt_ctx *ctx, const rt_ray *rays, size_t n, uint32_t *node_visits, uint32_t *tri_visits,
                     void *stream, uint32_t flags);
 
 /* Message of the calling thread's last failed call ("" if none). */
-const char *rt_last_error(void);
+RT_API const char *rt_last_error(void);
 
 /* ======================================================================================
  * Path tracer
@@ -206,42 +212,54 @@ typedef struct pt_render_stats {
 typedef struct pt_scene pt_scene;
 
 /* Create an empty scene on CUDA device `device`. */
-int pt_scene_create(pt_scene **scene, int device);
-int pt_scene_destroy(pt_scene *scene);
+RT_API int pt_scene_create(pt_scene **scene, int device);
+RT_API int pt_scene_destroy(pt_scene *scene);
 
 /* Add a float image (width x height x channels, row-major, channels 1..4) used as a
  * texture; sampled with bilinear wrap filtering as Image::rgbal (Image.cpp:86-106). */
-int pt_scene_add_texture(pt_scene *scene, uint32_t width, uint32_t height, uint32_t channels, const float *pixels,
+RT_API int pt_scene_add_texture(pt_scene *scene, uint32_t width, uint32_t height, uint32_t channels, const float *pixels,
                          uint32_t *tex_id);
-int pt_scene_add_mesh(pt_scene *scene, const pt_mesh_desc *mesh, uint32_t *mesh_id);
-int pt_scene_add_material(pt_scene *scene, const pt_material_desc *mat, uint32_t *material_id);
+RT_API int pt_scene_add_mesh(pt_scene *scene, const pt_mesh_desc *mesh, uint32_t *mesh_id);
+RT_API int pt_scene_add_material(pt_scene *scene, const pt_material_desc *mat, uint32_t *material_id);
 /* Add an object (Object.hpp:25): mesh + material + model matrix. */
-int pt_scene_add_object(pt_scene *scene, uint32_t mesh_id, uint32_t material_id, const float *model,
+RT_API int pt_scene_add_object(pt_scene *scene, uint32_t mesh_id, uint32_t material_id, const float *model,
                         uint32_t *object_id);
-int pt_scene_add_light(pt_scene *scene, const pt_light_desc *light);
+RT_API int pt_scene_add_light(pt_scene *scene, const pt_light_desc *light);
 /* COLOR: color[3] used; IMAGE: tex[0]; SKYBOX: tex[0..5] = +x,-x,+y,-y,+z,-z faces
  * (Texture.cpp:141-191). */
-int pt_scene_set_background(pt_scene *scene, int32_t mode, const float *color, const uint32_t *tex);
+RT_API int pt_scene_set_background(pt_scene *scene, int32_t mode, const float *color, const uint32_t *tex);
 
 /* Upload the scene and build its raycaster: every object's mesh is added in object order
  * (so meshId == object index) and the hierarchy is built. Replaces
  * PathTracer::PathTracer(scene) (PathTracer.cpp:11-21). */
-int pt_scene_commit(pt_scene *scene);
+RT_API int pt_scene_commit(pt_scene *scene);
 
 /* Render `samples` (rounded to a power of two as at PathTracer.cpp:169-173) paths of at
  * most `depth` segments per pixel and ACCUMULATE the normalised result into `image`
  * (width x height x components floats, components >= 3, RGB in the first three), as
  * PathTracer::render(camera, samples, depth, image) does (PathTracer.cpp:159-299):
  * image.rgb = (image.rgb + sum_s min(L_s, 5)) / spp. `seed` selects the random sequence.
- * Host pointer by default; device pointer with RT_FLAG_DEVICE_PTRS. */
-int pt_render(pt_scene *scene, const pt_camera_desc *camera, uint32_t samples, uint32_t depth, uint64_t seed,
+ * Host pointer by default; device pointer with RT_FLAG_DEVICE_PTRS (work ordered on
+ * `stream`). The call returns when the image is final. */
+RT_API int pt_render(pt_scene *scene, const pt_camera_desc *camera, uint32_t samples, uint32_t depth, uint64_t seed,
               float *image, uint32_t width, uint32_t height, uint32_t components, void *stream, uint32_t flags);
 
 /* Counters of the last pt_render on this scene. */
-int pt_get_render_stats(const pt_scene *scene, pt_render_stats *out);
+RT_API int pt_get_render_stats(const pt_scene *scene, pt_render_stats *out);
+
+/* MaterialGGX::eval (src/apps/pathtracer/MaterialGGX.cpp:94-101) for n cases on device
+ * `device`: cases = n x 11 floats {wo.xyz, base.rgb, roughness, metalness, wi.xyz} (local
+ * frame, host memory); out = n x 3 floats. */
+RT_API int pt_material_eval(const float *cases, size_t n, float *out, int device);
+
+/* MaterialGGX::sampleAndEval (MaterialGGX.cpp:54-92) for n cases on device `device`:
+ * cases = n x 8 floats {wo.xyz, base.rgb, roughness, metalness}; uniforms = n x 3 floats,
+ * the three numbers the reference draws (lobe choice, then the two lobe coordinates);
+ * out = n x 6 floats {weight.rgb, wi.xyz}. */
+RT_API int pt_material_sample(const float *cases, const float *uniforms, size_t n, float *out, int device);
 
 /* The raycaster built by pt_scene_commit (PathTracer::raycaster(), PathTracer.hpp:29). */
-rt_ctx *pt_scene_raycaster(pt_scene *scene);
+RT_API rt_ctx *pt_scene_raycaster(pt_scene *scene);
 
 #ifdef __cplusplus
 }

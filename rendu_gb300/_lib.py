@@ -93,6 +93,8 @@ _SIGS = {
                    C.c_uint32, _VP, C.c_uint32], C.c_int),
     "pt_get_render_stats": ([_VP, C.POINTER(pt_render_stats)], C.c_int),
     "pt_scene_raycaster": ([_VP], _VP),
+    "pt_material_eval": ([_VP, C.c_size_t, _VP, C.c_int], C.c_int),
+    "pt_material_sample": ([_VP, _VP, C.c_size_t, _VP, C.c_int], C.c_int),
 }
 
 

@@ -1,0 +1,525 @@
+// C-ABI of the path tracer (include/rendu_gb300.h, pt_*): scene intake, upload
+// (PathTracer::PathTracer, PathTracer.cpp:11-21 of kosua20/Rendu) and the render driver
+// (PathTracer::render, PathTracer.cpp:159-299).
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "pt_scene.hpp"
+
+using namespace rgb;
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+int arg_error(const char *msg) {
+    set_error(msg);
+    return RT_ERR_ARG;
+}
+
+template <class T>
+int upload(DevBuf &b, const std::vector<T> &v, cudaStream_t st) {
+    if (b.reserve(sizeof(T) * (v.empty() ? 1 : v.size())) != RT_OK) return RT_ERR_OOM;
+    if (!v.empty()) RT_CUDA_TRY(cudaMemcpyAsync(b.ptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st));
+    return RT_OK;
+}
+
+// ---- float vector helpers in glm's operation order (host) --------------------------------
+struct V3 {
+    float x, y, z;
+};
+V3 vsub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+V3 vadd(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+V3 vscale(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+float vdot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+V3 vcross(V3 x, V3 y) { return {x.y * y.z - y.y * x.z, x.z * y.x - y.z * x.x, x.x * y.y - y.x * x.y}; }
+V3 vnormalize(V3 v) {
+    const float s = 1.0f / std::sqrt(vdot(v, v));
+    return {v.x * s, v.y * s, v.z * s};
+}
+
+// Camera::pose (Camera.cpp:10-18) followed by Camera::pixelShifts (Camera.cpp:42-49).
+void pixel_shifts(const pt_camera_desc &c, float corner[3], float dx[3], float dy[3], float eye[3]) {
+    const V3 e{c.eye[0], c.eye[1], c.eye[2]}, ce{c.center[0], c.center[1], c.center[2]};
+    V3 up = vnormalize(V3{c.up[0], c.up[1], c.up[2]});
+    const V3 view = vnormalize(vsub(ce, e));
+    const V3 right = vcross(view, up);
+    up = vcross(right, view);
+    const float hs = std::tan(0.5f * c.fov);
+    const float ws = c.ratio * hs;
+    const V3 de = vsub(ce, e);
+    const float dist = std::sqrt(vdot(de, de));
+    const V3 k = vadd(vscale(-ws, right), vscale(hs, up));
+    const V3 co = vadd(ce, vscale(dist, k));
+    const V3 ddx = vscale(2.0f * ws * dist, right);
+    const V3 ddy = vscale(-2.0f * hs * dist, up);
+    corner[0] = co.x; corner[1] = co.y; corner[2] = co.z;
+    dx[0] = ddx.x; dx[1] = ddx.y; dx[2] = ddx.z;
+    dy[0] = ddy.x; dy[1] = ddy.y; dy[2] = ddy.z;
+    eye[0] = e.x; eye[1] = e.y; eye[2] = e.z;
+}
+
+// inverse(transpose(mat3(model))) as a row-major 3x3 acting on column vectors.
+void normal_matrix(const float *m, float out[9]) {
+    double a[3][3];  // a[r][c] = model column c, row r
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) a[r][c] = m[4 * c + r];
+    const double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) - a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+                       a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+    double inv[3][3];
+    inv[0][0] = (a[1][1] * a[2][2] - a[1][2] * a[2][1]) / det;
+    inv[0][1] = (a[0][2] * a[2][1] - a[0][1] * a[2][2]) / det;
+    inv[0][2] = (a[0][1] * a[1][2] - a[0][2] * a[1][1]) / det;
+    inv[1][0] = (a[1][2] * a[2][0] - a[1][0] * a[2][2]) / det;
+    inv[1][1] = (a[0][0] * a[2][2] - a[0][2] * a[2][0]) / det;
+    inv[1][2] = (a[0][2] * a[1][0] - a[0][0] * a[1][2]) / det;
+    inv[2][0] = (a[1][0] * a[2][1] - a[1][1] * a[2][0]) / det;
+    inv[2][1] = (a[0][1] * a[2][0] - a[0][0] * a[2][1]) / det;
+    inv[2][2] = (a[0][0] * a[1][1] - a[0][1] * a[1][0]) / det;
+    // (M^-1)^T
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) out[3 * r + c] = (float)inv[c][r];
+}
+
+}  // namespace
+
+extern "C" {
+
+int pt_scene_create(pt_scene **out, int device) {
+    clear_error();
+    if (!out) return arg_error("null output pointer");
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        set_error("CUDA device " + std::to_string(device) + " is not available");
+        return RT_ERR_CUDA;
+    }
+    pt_scene *s = new pt_scene();
+    s->device = device;
+    *out = s;
+    return RT_OK;
+}
+
+int pt_scene_destroy(pt_scene *s) {
+    if (!s) return RT_OK;
+    DeviceGuard g(s->device);
+    if (s->rc) rt_destroy(s->rc);
+    for (DevBuf *b : {&s->d_objects, &s->d_meshes, &s->d_materials, &s->d_tex, &s->d_texels, &s->d_normals,
+                      &s->d_tangents, &s->d_bitangents, &s->d_uvs, &s->d_indices, &s->d_lights, &s->w_atten,
+                      &s->w_color, &s->w_ndc, &s->w_qray0, &s->w_qray1, &s->w_qpath0, &s->w_qpath1, &s->w_hits,
+                      &s->w_sray, &s->w_scontrib, &s->w_counters, &s->w_stats, &s->w_accum, &s->w_image})
+        b->release();
+    delete s;
+    return RT_OK;
+}
+
+int pt_scene_add_texture(pt_scene *s, uint32_t width, uint32_t height, uint32_t channels, const float *pixels,
+                         uint32_t *tex_id) {
+    clear_error();
+    if (!s || !pixels) return arg_error("null argument");
+    if (width == 0 || height == 0 || channels < 1 || channels > 4) return arg_error("bad texture size or channels");
+    HostTex t;
+    t.w = width;
+    t.h = height;
+    t.rgba.resize((size_t)width * height * 4);
+    for (size_t p = 0; p < (size_t)width * height; ++p)
+        for (uint32_t c = 0; c < 4; ++c) t.rgba[4 * p + c] = c < channels ? pixels[channels * p + c] : (c == 3 ? 1.0f : 0.0f);
+    s->textures.push_back(std::move(t));
+    if (tex_id) *tex_id = (uint32_t)(s->textures.size() - 1);
+    s->committed = false;
+    return RT_OK;
+}
+
+int pt_scene_add_mesh(pt_scene *s, const pt_mesh_desc *m, uint32_t *mesh_id) {
+    clear_error();
+    if (!s || !m) return arg_error("null argument");
+    if (!m->positions || !m->normals || !m->tangents || !m->bitangents || (m->index_count && !m->indices))
+        return arg_error("the path tracer requires positions, normals, tangents and bitangents (PathTracer.cpp:14-16)");
+    if (m->index_count % 3) return arg_error("index_count must be a multiple of 3");
+    for (size_t i = 0; i < m->index_count; ++i)
+        if (m->indices[i] >= m->vertex_count) return arg_error("mesh index out of range");
+    HostMesh h;
+    const size_t nv = m->vertex_count;
+    h.pos.assign(m->positions, m->positions + 3 * nv);
+    h.nrm.assign(m->normals, m->normals + 3 * nv);
+    h.tan.assign(m->tangents, m->tangents + 3 * nv);
+    h.bit.assign(m->bitangents, m->bitangents + 3 * nv);
+    if (m->texcoords) h.uv.assign(m->texcoords, m->texcoords + 2 * nv);
+    h.idx.assign(m->indices, m->indices + m->index_count);
+    s->meshes.push_back(std::move(h));
+    if (mesh_id) *mesh_id = (uint32_t)(s->meshes.size() - 1);
+    s->committed = false;
+    return RT_OK;
+}
+
+int pt_scene_add_material(pt_scene *s, const pt_material_desc *d, uint32_t *material_id) {
+    clear_error();
+    if (!s || !d) return arg_error("null argument");
+    if (d->type < 0 || d->type > 10) return arg_error("unknown material type");
+    for (int k = 0; k < 3; ++k)
+        if (d->tex[k] >= s->textures.size()) return arg_error("material texture id out of range");
+    s->materials.push_back(*d);
+    if (material_id) *material_id = (uint32_t)(s->materials.size() - 1);
+    s->committed = false;
+    return RT_OK;
+}
+
+int pt_scene_add_object(pt_scene *s, uint32_t mesh_id, uint32_t material_id, const float *model, uint32_t *object_id) {
+    clear_error();
+    if (!s) return arg_error("null scene");
+    if (mesh_id >= s->meshes.size() || material_id >= s->materials.size()) return arg_error("mesh or material id out of range");
+    HostObject o;
+    o.mesh = mesh_id;
+    o.material = material_id;
+    for (int k = 0; k < 16; ++k) o.model[k] = model ? model[k] : ((k % 5) == 0 ? 1.0f : 0.0f);
+    s->objects.push_back(o);
+    if (object_id) *object_id = (uint32_t)(s->objects.size() - 1);
+    s->committed = false;
+    return RT_OK;
+}
+
+int pt_scene_add_light(pt_scene *s, const pt_light_desc *l) {
+    clear_error();
+    if (!s || !l) return arg_error("null argument");
+    if (l->type < PT_LIGHT_POINT || l->type > PT_LIGHT_SPOT) return arg_error("unknown light type");
+    s->lights.push_back(*l);
+    s->committed = false;
+    return RT_OK;
+}
+
+int pt_scene_set_background(pt_scene *s, int32_t mode, const float *color, const uint32_t *tex) {
+    clear_error();
+    if (!s) return arg_error("null scene");
+    if (mode == PT_BG_COLOR) {
+        if (!color) return arg_error("COLOR background needs a colour");
+        std::memcpy(s->bg_color, color, sizeof(s->bg_color));
+    } else if (mode == PT_BG_IMAGE || mode == PT_BG_SKYBOX) {
+        const int n = mode == PT_BG_IMAGE ? 1 : 6;
+        if (!tex) return arg_error("background needs texture ids");
+        for (int k = 0; k < n; ++k) {
+            if (tex[k] >= s->textures.size()) return arg_error("background texture id out of range");
+            s->bg_tex[k] = tex[k];
+        }
+    } else {
+        return arg_error("unsupported background mode");
+    }
+    s->bg_mode = mode;
+    s->committed = false;
+    return RT_OK;
+}
+
+int pt_scene_commit(pt_scene *s) {
+    clear_error();
+    if (!s) return arg_error("null scene");
+    DeviceGuard g(s->device);
+    if (s->rc) rt_destroy(s->rc);
+    s->rc = nullptr;
+    int r = rt_create(&s->rc, s->device);
+    if (r != RT_OK) return r;
+    // Every object's mesh is added in object order: meshId == object index (PathTracer.cpp:16-18).
+    for (const HostObject &o : s->objects) {
+        const HostMesh &m = s->meshes[o.mesh];
+        r = rt_add_mesh(s->rc, m.pos.data(), m.pos.size() / 3, m.idx.data(), m.idx.size(), o.model, nullptr);
+        if (r != RT_OK) return r;
+    }
+    r = rt_update_hierarchy(s->rc);
+    if (r != RT_OK) return r;
+    cudaStream_t st = s->rc->stream;
+
+    std::vector<PtMesh> meshes(s->meshes.size());
+    std::vector<float> nrm, tan, bit, uv;
+    std::vector<uint32_t> idx;
+    for (size_t k = 0; k < s->meshes.size(); ++k) {
+        const HostMesh &m = s->meshes[k];
+        meshes[k].first_vertex = (uint32_t)(nrm.size() / 3);
+        meshes[k].first_index = (uint32_t)idx.size();
+        meshes[k].has_uv = m.uv.empty() ? 0 : 1;
+        nrm.insert(nrm.end(), m.nrm.begin(), m.nrm.end());
+        tan.insert(tan.end(), m.tan.begin(), m.tan.end());
+        bit.insert(bit.end(), m.bit.begin(), m.bit.end());
+        if (m.uv.empty()) uv.resize(uv.size() + 2 * (m.pos.size() / 3), 0.0f);
+        else uv.insert(uv.end(), m.uv.begin(), m.uv.end());
+        idx.insert(idx.end(), m.idx.begin(), m.idx.end());
+    }
+    std::vector<PtObject> objects(s->objects.size());
+    bool any_masked = false;
+    for (size_t k = 0; k < s->objects.size(); ++k) {
+        const HostObject &o = s->objects[k];
+        objects[k].mesh = o.mesh;
+        objects[k].material = o.material;
+        objects[k].first_tri = (uint32_t)s->rc->meshes[k].first_tri;
+        // Object::Object: texture coordinates are used when the mesh had some (Object.cpp:4-8).
+        objects[k].use_uv = meshes[o.mesh].has_uv;
+        normal_matrix(o.model, objects[k].invtp);
+        if (s->materials[o.material].masked) any_masked = true;
+    }
+    std::vector<PtMaterial> mats(s->materials.size());
+    for (size_t k = 0; k < mats.size(); ++k) {
+        mats[k].type = s->materials[k].type;
+        mats[k].masked = s->materials[k].masked ? 1 : 0;
+        for (int t = 0; t < 3; ++t) mats[k].tex[t] = s->materials[k].tex[t];
+    }
+    std::vector<PtTex> texd(s->textures.size());
+    std::vector<float> texels;
+    for (size_t k = 0; k < texd.size(); ++k) {
+        const HostTex &t = s->textures[k];
+        texd[k].w = t.w;
+        texd[k].h = t.h;
+        texd[k].offset = texels.size() / 4;
+        bool constant = true;
+        for (size_t p = 4; p < t.rgba.size() && constant; ++p) constant = t.rgba[p] == t.rgba[p % 4];
+        texd[k].constant = constant ? 1 : 0;
+        texd[k].value = make_float4(t.rgba[0], t.rgba[1], t.rgba[2], t.rgba[3]);
+        texels.insert(texels.end(), t.rgba.begin(), t.rgba.end());
+    }
+    std::vector<PtLight> lights(s->lights.size());
+    bool any_shadow = false;
+    for (size_t k = 0; k < lights.size(); ++k) {
+        const pt_light_desc &d = s->lights[k];
+        PtLight &l = lights[k];
+        l.type = d.type;
+        l.shadows = d.cast_shadows ? 1 : 0;
+        any_shadow |= l.shadows != 0;
+        std::memcpy(l.color, d.color, sizeof(l.color));
+        std::memcpy(l.position, d.position, sizeof(l.position));
+        // DirectionalLight / SpotLight normalise their direction at construction.
+        const V3 n = vnormalize(V3{d.direction[0], d.direction[1], d.direction[2]});
+        if (d.type == PT_LIGHT_POINT) {
+            l.direction[0] = d.direction[0]; l.direction[1] = d.direction[1]; l.direction[2] = d.direction[2];
+        } else {
+            l.direction[0] = n.x; l.direction[1] = n.y; l.direction[2] = n.z;
+        }
+        l.radius = d.radius;
+        l.half_inner = 0.5f * d.inner_angle;  // SpotLight.cpp:8
+        l.half_outer = 0.5f * d.outer_angle;
+    }
+    if ((r = upload(s->d_meshes, meshes, st)) || (r = upload(s->d_normals, nrm, st)) || (r = upload(s->d_tangents, tan, st)) ||
+        (r = upload(s->d_bitangents, bit, st)) || (r = upload(s->d_uvs, uv, st)) || (r = upload(s->d_indices, idx, st)) ||
+        (r = upload(s->d_objects, objects, st)) || (r = upload(s->d_materials, mats, st)) ||
+        (r = upload(s->d_tex, texd, st)) || (r = upload(s->d_texels, texels, st)) || (r = upload(s->d_lights, lights, st)))
+        return r;
+    RT_CUDA_TRY(cudaStreamSynchronize(st));
+
+    PtScene &d = s->dev;
+    d.nodes = s->rc->d_nodes.as<BvhNode>();
+    d.tris = s->rc->d_tris.as<BvhTri>();
+    d.status = s->rc->d_status.as<unsigned>();
+    d.big_stack = s->rc->depth > 64 ? 1 : 0;
+    d.empty = s->rc->n_tris == 0 ? 1 : 0;
+    d.objects = s->d_objects.as<PtObject>();
+    d.nobjects = (int)objects.size();
+    d.meshes = s->d_meshes.as<PtMesh>();
+    d.materials = s->d_materials.as<PtMaterial>();
+    d.textures = s->d_tex.as<PtTex>();
+    d.texels = s->d_texels.as<float4>();
+    d.normals = s->d_normals.as<float>();
+    d.tangents = s->d_tangents.as<float>();
+    d.bitangents = s->d_bitangents.as<float>();
+    d.uvs = s->d_uvs.as<float>();
+    d.indices = s->d_indices.as<uint32_t>();
+    d.lights = s->d_lights.as<PtLight>();
+    d.nlights = (int)lights.size();
+    d.any_masked = any_masked ? 1 : 0;
+    d.bg_mode = s->bg_mode;
+    std::memcpy(d.bg_color, s->bg_color, sizeof(d.bg_color));
+    std::memcpy(d.bg_tex, s->bg_tex, sizeof(d.bg_tex));
+    (void)any_shadow;
+    s->committed = true;
+    return RT_OK;
+}
+
+static int material_batch(const float *cases, size_t in_stride, const float *uniforms, size_t n, float *out,
+                          size_t out_stride, int device) {
+    if (!cases || !out || n >= (1ull << 31)) return arg_error("null argument or too many cases");
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        set_error("CUDA device " + std::to_string(device) + " is not available");
+        return RT_ERR_CUDA;
+    }
+    if (n == 0) return RT_OK;
+    DeviceGuard g(device);
+    DevBuf dc, du, dout;
+    int r = RT_OK;
+    if ((r = dc.reserve(n * in_stride * 4)) || (uniforms && (r = du.reserve(n * 12))) ||
+        (r = dout.reserve(n * out_stride * 4))) {
+        dc.release(); du.release(); dout.release();
+        return r;
+    }
+    if (cudaMemcpy(dc.ptr, cases, n * in_stride * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        (uniforms && cudaMemcpy(du.ptr, uniforms, n * 12, cudaMemcpyHostToDevice) != cudaSuccess))
+        r = RT_ERR_CUDA;
+    if (r == RT_OK) r = pt_launch_material(dc.as<float>(), uniforms ? du.as<float>() : nullptr, (uint32_t)n, dout.as<float>(), 0);
+    if (r == RT_OK && cudaMemcpy(out, dout.ptr, n * out_stride * 4, cudaMemcpyDeviceToHost) != cudaSuccess) r = RT_ERR_CUDA;
+    if (r == RT_ERR_CUDA) set_error(std::string("material batch failed: ") + cudaGetErrorString(cudaGetLastError()));
+    dc.release(); du.release(); dout.release();
+    return r;
+}
+
+int pt_material_eval(const float *cases, size_t n, float *out, int device) {
+    clear_error();
+    return material_batch(cases, 11, nullptr, n, out, 3, device);
+}
+
+int pt_material_sample(const float *cases, const float *uniforms, size_t n, float *out, int device) {
+    clear_error();
+    if (!uniforms) return arg_error("null uniforms");
+    return material_batch(cases, 8, uniforms, n, out, 6, device);
+}
+
+rt_ctx *pt_scene_raycaster(pt_scene *s) { return s ? s->rc : nullptr; }
+
+int pt_get_render_stats(const pt_scene *s, pt_render_stats *out) {
+    clear_error();
+    if (!s || !out) return arg_error("null argument");
+    *out = s->last;
+    return RT_OK;
+}
+
+int pt_render(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, uint32_t depth, uint64_t seed, float *image,
+              uint32_t width, uint32_t height, uint32_t components, void *stream, uint32_t flags) {
+    clear_error();
+    if (!s || !camera || !image) return arg_error("null argument");
+    if (!s->committed) {
+        set_error("pt_scene_commit must be called after the last scene change");
+        return RT_ERR_STATE;
+    }
+    if (width == 0 || height == 0) return arg_error("empty image");
+    if (components < 3) return arg_error("the image needs at least 3 components (PathTracer.cpp:166-168)");
+    if (samples == 0) return arg_error("samples must be at least 1");
+    if ((uint64_t)width * height >= (1ull << 31)) return arg_error("image too large");
+    DeviceGuard g(s->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->rc->stream;
+
+    // Power-of-two sample count and stratification grid (PathTracer.cpp:169-178, 57-69).
+    const uint32_t spp = (uint32_t)std::pow(2.0, std::round(std::log2((float)samples)));
+    const int k = (int)std::floor(std::log2((double)spp));
+    uint32_t cx = (uint32_t)std::pow(2, k / 2), cy = cx;
+    if (k % 2 == 1) {
+        cx = (uint32_t)std::pow(2, (k + 1) / 2);
+        cy = (uint32_t)std::pow(2, (k - 1) / 2);
+    }
+    PtFrame f{};
+    pixel_shifts(*camera, f.corner, f.dx, f.dy, f.eye);
+    f.W = width;
+    f.H = height;
+    f.npix = width * height;
+    f.spp = spp;
+    f.cx = cx;
+    f.cy = cy;
+    f.cell_x = 1.0f / (float)cx;
+    f.cell_y = 1.0f / (float)cy;
+    f.depth = depth;
+    f.seed_lo = (uint32_t)seed;
+    f.seed_hi = (uint32_t)(seed >> 32);
+    // Wave: every pixel x S samples, S a power of two dividing spp, about 8M paths.
+    const uint64_t target = 1ull << 23;
+    uint32_t S = 1;
+    while (S * 2 <= spp && (uint64_t)f.npix * S * 2 <= target) S *= 2;
+    f.S = S;
+    const uint64_t P = (uint64_t)f.npix * S;
+    if (P >= (1ull << 31)) return arg_error("image too large for one wave");
+
+    if (P > s->wave_cap) {
+        int r = RT_OK;
+        if ((r = s->w_atten.reserve(P * 16)) || (r = s->w_color.reserve(P * 16)) || (r = s->w_ndc.reserve(P * 8)) ||
+            (r = s->w_qray0.reserve(P * 32)) || (r = s->w_qray1.reserve(P * 32)) || (r = s->w_qpath0.reserve(P * 4)) ||
+            (r = s->w_qpath1.reserve(P * 4)) || (r = s->w_hits.reserve(P * 16)) || (r = s->w_sray.reserve(P * 32)) ||
+            (r = s->w_scontrib.reserve(P * 16)))
+            return r;
+        s->wave_cap = P;
+    }
+    if (s->w_counters.reserve(64) || s->w_stats.reserve(64)) return RT_ERR_OOM;
+    if (f.npix > s->accum_cap) {
+        if (s->w_accum.reserve((size_t)f.npix * 12)) return RT_ERR_OOM;
+        s->accum_cap = f.npix;
+    }
+    PtWave w{};
+    w.atten = s->w_atten.as<float4>();
+    w.color = s->w_color.as<float4>();
+    w.ndc = s->w_ndc.as<float2>();
+    w.qray[0] = s->w_qray0.as<rt_ray>();
+    w.qray[1] = s->w_qray1.as<rt_ray>();
+    w.qpath[0] = s->w_qpath0.as<uint32_t>();
+    w.qpath[1] = s->w_qpath1.as<uint32_t>();
+    w.hits = s->w_hits.as<rt_hit>();
+    w.sray = s->w_sray.as<rt_ray>();
+    w.scontrib = s->w_scontrib.as<float4>();
+    w.counters = s->w_counters.as<uint32_t>();
+    w.stats = s->w_stats.as<unsigned long long>();
+    w.accum = s->w_accum.as<float>();
+
+    const size_t img_bytes = (size_t)f.npix * components * sizeof(float);
+    float *d_img = image;
+    if (!(flags & RT_FLAG_DEVICE_PTRS)) {
+        if (s->w_image.reserve(img_bytes)) return RT_ERR_OOM;
+        d_img = s->w_image.as<float>();
+        RT_CUDA_TRY(cudaMemcpyAsync(d_img, image, img_bytes, cudaMemcpyHostToDevice, st));
+    }
+    cudaEvent_t e0, e1;
+    RT_CUDA_TRY(cudaEventCreate(&e0));
+    RT_CUDA_TRY(cudaEventCreate(&e1));
+    RT_CUDA_TRY(cudaEventRecord(e0, st));
+    RT_CUDA_TRY(cudaMemsetAsync(w.stats, 0, 64, st));
+    int r = pt_launch_load(d_img, components, f.npix, w.accum, st);
+    const uint32_t cap = (uint32_t)P;
+    for (uint32_t s0 = 0; r == RT_OK && s0 < spp; s0 += S) {
+        f.s0 = s0;
+        r = pt_launch_raygen(f, w, st);
+        int cur = 0;
+        for (uint32_t did = 0; r == RT_OK && did < depth; ++did) {
+            r = pt_launch_trace(s->dev, w, cur, cap, did == 0 ? 0 : 1, st);
+            if (r != RT_OK) break;
+            if (cudaMemsetAsync(&w.counters[cur ^ 1], 0, 4, st) != cudaSuccess ||
+                cudaMemsetAsync(&w.counters[2], 0, 4, st) != cudaSuccess) {
+                set_error("cudaMemsetAsync failed");
+                r = RT_ERR_CUDA;
+                break;
+            }
+            r = pt_launch_shade(s->dev, f, w, cur, did, cap, st);
+            if (r == RT_OK && s->dev.nlights > 0) r = pt_launch_shadow(s->dev, w, cap, st);
+            cur ^= 1;
+        }
+        if (r == RT_OK) r = pt_launch_accumulate(f, w, st);
+    }
+    if (r == RT_OK) r = pt_launch_store(w.accum, f.npix, (float)spp, components, d_img, st);
+    if (r == RT_OK && cudaEventRecord(e1, st) != cudaSuccess) r = RT_ERR_CUDA;
+    unsigned long long stats[3] = {0, 0, 0};
+    if (r == RT_OK && cudaMemcpyAsync(stats, w.stats, sizeof(stats), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        r = RT_ERR_CUDA;
+    if (r == RT_OK && !(flags & RT_FLAG_DEVICE_PTRS) &&
+        cudaMemcpyAsync(image, d_img, img_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        r = RT_ERR_CUDA;
+    if (r == RT_OK && cudaStreamSynchronize(st) != cudaSuccess) {
+        set_error(std::string("render failed: ") + cudaGetErrorString(cudaGetLastError()));
+        r = RT_ERR_CUDA;
+    }
+    if (r == RT_OK) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        s->last.primary_rays = stats[0];
+        s->last.bounce_rays = stats[1];
+        s->last.shadow_rays = stats[2];
+        s->last.paths = (uint64_t)f.npix * spp;
+        s->last.device_ms = ms;
+        r = check_status(s->rc, st);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return r;
+}
+
+}  // extern "C"

@@ -1,0 +1,328 @@
+// Device-side scene model and shading functions of the path tracer.
+//
+// Restates, for sm_103a, the per-sample math of kosua20/Rendu's offline path tracer:
+//   MaterialGGX::F/D/V/alphaFromRoughness/GGX/sampleAndEval/eval  MaterialGGX.cpp:5-101
+//   Random::sampleDisk / sampleCosineHemisphere                   Random.cpp:41-70
+//   Image::rgbl / rgbal (bilinear, wrapped)                        Image.cpp:64-106
+//   Texture::sampleCubemap                                         Texture.cpp:141-191
+//   PointLight/DirectionalLight/SpotLight::sample                  PointLight.cpp:68-87,
+//                                                                  DirectionalLight.cpp:40-44,
+//                                                                  SpotLight.cpp:52-78
+//   PathTracer::buildLocalFrame / evalBackground                   PathTracer.cpp:23-55, 86-122
+// The reference draws its random numbers from per-thread std::mt19937 streams; here every
+// draw comes from a counter-based generator (Philox-4x32-10, Salmon et al., SC'11) keyed by
+// the render seed and indexed by (pixel, sample, bounce), so a render is reproducible and
+// independent of the launch shape. The draws are consumed in the reference's order.
+#pragma once
+
+#include "rt_common.cuh"
+
+namespace rgb {
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kOneOverPi = 0.318309886183790671538f;  // glm::one_over_pi<float>()
+constexpr float kTwoPi = 6.28318530717958647692f;       // glm::two_pi<float>()
+
+// ---- Philox-4x32-10 --------------------------------------------------------------------
+struct U4 {
+    uint32_t x, y, z, w;
+};
+
+__host__ __device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
+__host__ __device__ __forceinline__ U4 philox(U4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = mulhi32(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const uint32_t hi1 = mulhi32(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+// Uniform float in [0, 1) from the top 24 bits.
+__host__ __device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+// Uniform integer in [0, n) (multiply-high).
+__host__ __device__ __forceinline__ uint32_t uint_below(uint32_t x, uint32_t n) { return mulhi32(x, n); }
+
+// ---- device scene -----------------------------------------------------------------------
+struct PtTex {
+    uint32_t w, h;
+    uint64_t offset;  // into the float4 texel pool
+    int constant;     // all texels equal: `value` is returned without filtering
+    float4 value;
+};
+
+struct PtMesh {
+    uint32_t first_vertex;  // into the attribute pools
+    uint32_t first_index;   // into the index pool (mesh-local vertex indices)
+    uint32_t has_uv;
+    uint32_t pad;
+};
+
+struct PtObject {
+    uint32_t mesh, material, first_tri, use_uv;
+    float invtp[9];  // inverse(transpose(mat3(model))), row-major
+};
+
+struct PtMaterial {
+    int type, masked;
+    uint32_t tex[3];
+};
+
+struct PtLight {
+    int type, shadows;
+    float color[3], position[3], direction[3];  // direction normalised as the constructors do
+    float radius, half_inner, half_outer;
+};
+
+struct PtScene {
+    const BvhNode *nodes;
+    const BvhTri *tris;
+    unsigned *status;
+    int big_stack, empty;
+    const PtObject *objects;
+    int nobjects;
+    const PtMesh *meshes;
+    const PtMaterial *materials;
+    const PtTex *textures;
+    const float4 *texels;
+    const float *normals, *tangents, *bitangents, *uvs;
+    const uint32_t *indices;
+    const PtLight *lights;
+    int nlights;
+    int any_masked;
+    int bg_mode;
+    float bg_color[3];
+    uint32_t bg_tex[6];
+};
+
+// ---- textures ----------------------------------------------------------------------------
+__device__ __forceinline__ int mod_pos(int x, int w) { return ((x % w) + w) % w; }
+
+__device__ __forceinline__ int f2i_sat(float f) {
+    return (int)fminf(fmaxf(f, -2147483520.0f), 2147483520.0f);
+}
+
+// Image::rgbal (Image.cpp:86-106): bilinear with wrapping.
+__device__ __forceinline__ float4 tex_rgbal(const PtScene &s, uint32_t id, float x, float y) {
+    const PtTex t = s.textures[id];
+    if (t.constant) return t.value;
+    const float xi = x * (float)t.w, yi = y * (float)t.h;
+    const float xb = floorf(xi), yb = floorf(yi);
+    const float dx = xi - xb, dy = yi - yb;
+    const int ixb = f2i_sat(xb), iyb = f2i_sat(yb);
+    const int x0 = mod_pos(ixb, (int)t.w), y0 = mod_pos(iyb, (int)t.h);
+    const int x1 = mod_pos(ixb + 1, (int)t.w), y1 = mod_pos(iyb + 1, (int)t.h);
+    const float4 *px = s.texels + t.offset;
+    const float4 p00 = px[(size_t)y0 * t.w + x0], p01 = px[(size_t)y1 * t.w + x0];
+    const float4 p10 = px[(size_t)y0 * t.w + x1], p11 = px[(size_t)y1 * t.w + x1];
+    const float a = 1.0f - dx, b = 1.0f - dy;
+    return make_float4(a * (b * p00.x + dy * p01.x) + dx * (b * p10.x + dy * p11.x),
+                       a * (b * p00.y + dy * p01.y) + dx * (b * p10.y + dy * p11.y),
+                       a * (b * p00.z + dy * p01.z) + dx * (b * p10.z + dy * p11.z),
+                       a * (b * p00.w + dy * p01.w) + dx * (b * p10.w + dy * p11.w));
+}
+
+// Texture::sampleCubemap (Texture.cpp:141-191); faces +x,-x,+y,-y,+z,-z.
+__device__ __forceinline__ f3 cubemap(const PtScene &s, f3 dir) {
+    const float ax = fabsf(dir.x), ay = fabsf(dir.y), az = fabsf(dir.z);
+    int face = 0;
+    float x = 0.0f, y = 0.0f, denom = 1.0f;
+    if (ax >= ay && ax >= az) {
+        denom = ax;
+        y = dir.y;
+        face = dir.x >= 0.0f ? 0 : 1;
+        x = dir.x >= 0.0f ? -dir.z : dir.z;
+    } else if (ay >= ax && ay >= az) {
+        denom = ay;
+        x = dir.x;
+        face = dir.y >= 0.0f ? 2 : 3;
+        y = dir.y >= 0.0f ? -dir.z : dir.z;
+    } else if (az >= ax && az >= ay) {
+        denom = az;
+        y = dir.y;
+        face = dir.z >= 0.0f ? 4 : 5;
+        x = dir.z >= 0.0f ? dir.x : -dir.x;
+    }
+    x = 0.5f * (x / denom) + 0.5f;
+    y = 0.5f * (-y / denom) + 0.5f;
+    const PtTex t = s.textures[s.bg_tex[face]];
+    const float eps = 1.0f / (float)min(t.w, t.h);
+    x = fminf(fmaxf(x, eps), 1.0f - eps);
+    y = fminf(fmaxf(y, eps), 1.0f - eps);
+    const float4 c = tex_rgbal(s, s.bg_tex[face], x, y);
+    return mk(c.x, c.y, c.z);
+}
+
+// PathTracer::evalBackground (PathTracer.cpp:23-55): COLOR and IMAGE only for primary
+// misses (IMAGE indexed by the screen position), SKYBOX for every miss.
+__device__ __forceinline__ f3 eval_background(const PtScene &s, f3 dir, float ndc_x, float ndc_y, bool direct) {
+    if (s.bg_mode == PT_BG_SKYBOX) return cubemap(s, normalize(dir));
+    if (!direct) return mk(0.0f, 0.0f, 0.0f);
+    if (s.bg_mode == PT_BG_IMAGE) {
+        const float4 c = tex_rgbal(s, s.bg_tex[0], ndc_x, ndc_y);
+        return mk(c.x, c.y, c.z);
+    }
+    return mk(s.bg_color[0], s.bg_color[1], s.bg_color[2]);
+}
+
+// ---- MaterialGGX (MaterialGGX.cpp:5-101) --------------------------------------------------
+__device__ __forceinline__ f3 ggx_F(f3 F0, float VdotH) {
+    const float p = powf(1.0f - VdotH, 5.0f);
+    return mk(F0.x + p * (1.0f - F0.x), F0.y + p * (1.0f - F0.y), F0.z + p * (1.0f - F0.z));
+}
+
+__device__ __forceinline__ float ggx_D(float NdotH, float alpha) {
+    const float halfDenum = NdotH * NdotH * (alpha * alpha - 1.0f) + 1.0f;
+    const float halfTerm = alpha / fmaxf(0.0001f, halfDenum);
+    return halfTerm * halfTerm * kOneOverPi;
+}
+
+__device__ __forceinline__ float ggx_V(float NdotL, float NdotV, float alpha) {
+    const float alpha2 = alpha * alpha;
+    const float visL = NdotV * sqrtf((-NdotL * alpha2 + NdotL) * NdotL + alpha2);
+    const float visV = NdotL * sqrtf((-NdotV * alpha2 + NdotV) * NdotV + alpha2);
+    return 0.5f / fmaxf(0.0001f, visV + visL);
+}
+
+__device__ __forceinline__ float alpha_from_roughness(float roughness) {
+    const float rc = fmaxf(0.045f, roughness);
+    return fmaxf(0.0001f, rc * rc);
+}
+
+// The reference names wo.z "NdotL" and wi.z "NdotV" (MaterialGGX.cpp:35-36); kept.
+__device__ __forceinline__ f3 ggx_brdf(f3 wo, f3 base, float alpha, float metallic, f3 wi, float *pdf) {
+    const f3 h = normalize(wi + wo);
+    const float NdotH = fmaxf(h.z, 0.0f);
+    const float VdotH = fmaxf(dot(wi, h), 0.0f);
+    const float NdotL = fmaxf(wo.z, 0.0f);
+    const float NdotV = fmaxf(wi.z, 0.0f);
+    const float Dh = ggx_D(NdotH, alpha);
+    if (pdf) *pdf = Dh * NdotH / (4.0f * fmaxf(0.0001f, VdotH));
+    const f3 F0 = mk(0.04f + (base.x - 0.04f) * metallic, 0.04f + (base.y - 0.04f) * metallic,
+                     0.04f + (base.z - 0.04f) * metallic);
+    const float dv = Dh * ggx_V(NdotL, NdotV, alpha);
+    const f3 F = ggx_F(F0, VdotH);
+    const float kd = (1.0f - metallic) * kOneOverPi;
+    const float ms = 2.0f * alpha * alpha * NdotV;  // multi-scattering adjustment (MaterialGGX.cpp:49)
+    f3 r;
+    r.x = (kd * base.x * (1.0f - F0.x) + dv * F.x * (1.0f + ms * F0.x)) * NdotV;
+    r.y = (kd * base.y * (1.0f - F0.y) + dv * F.y * (1.0f + ms * F0.y)) * NdotV;
+    r.z = (kd * base.z * (1.0f - F0.z) + dv * F.z * (1.0f + ms * F0.z)) * NdotV;
+    return r;
+}
+
+// Random::sampleDisk + sampleCosineHemisphere (Random.cpp:41-70) from two uniforms.
+__device__ __forceinline__ f3 cosine_hemisphere(float u0, float u1) {
+    const float x = 2.0f * u0 - 1.0f, y = 2.0f * u1 - 1.0f;
+    float dx = 0.0f, dy = 0.0f;
+    if (!(x == 0.0f && y == 0.0f)) {
+        float angle, radius;
+        if (fabsf(x) > fabsf(y)) {
+            radius = x;
+            angle = 0.25f * kPi * y / x;
+        } else {
+            radius = y;
+            angle = 0.5f * kPi - 0.25f * kPi * x / y;
+        }
+        dx = radius * cosf(angle);
+        dy = radius * sinf(angle);
+    }
+    const float z = sqrtf(fmaxf(0.0f, 1.0f - dx * dx - dy * dy));
+    return mk(dx, dy, z);
+}
+
+// MaterialGGX::sampleAndEval (MaterialGGX.cpp:54-92): u0 picks the lobe, u1 and u2 sample it.
+__device__ __forceinline__ f3 ggx_sample_eval(f3 wo, f3 base, float roughness, float metallic, float u0, float u1,
+                                              float u2, f3 &wi) {
+    const float pmean = (base.x + base.y + base.z) / 3.0f;
+    const float pdiff = 1.0f / (pmean + 1.0f);
+    const float probaSpecular = pdiff + (1.0f - pdiff) * metallic;  // glm::mix(pdiff, 1, metallic)
+    const float alpha = alpha_from_roughness(roughness);
+    if (u0 < probaSpecular) {
+        const float a2 = alpha * alpha;
+        const float x = u1;
+        const float phiH = u2 * kTwoPi;
+        const float cosThetaHSqr = fminf((1.0f - x) / ((a2 - 1.0f) * x + 1.0f), 1.0f);
+        const float cosThetaH = sqrtf(cosThetaHSqr);
+        const float sinThetaH = sqrtf(1.0f - cosThetaHSqr);
+        const f3 lh = mk(sinThetaH * cosf(phiH), sinThetaH * sinf(phiH), cosThetaH);
+        const float k = 2.0f * dot(wo, lh);
+        wi = mk(k * lh.x - wo.x, k * lh.y - wo.y, k * lh.z - wo.z);
+    } else {
+        wi = cosine_hemisphere(u1, u2);
+        if (wo.z < 0.0f) wi.z = -wi.z;
+    }
+    if (wi.z < 0.0f) return mk(0.0f, 0.0f, 0.0f);
+    float pdfSpec = 0.0f;
+    const f3 brdf = ggx_brdf(wo, base, alpha, metallic, wi, &pdfSpec);
+    const float pd = kOneOverPi * fmaxf(wi.z, 0.0f);
+    const float pdf = pd + (pdfSpec - pd) * probaSpecular;  // glm::mix(pd, pdfSpec, probaSpecular)
+    if (pdf == 0.0f) return mk(0.0f, 0.0f, 0.0f);
+    return mk(brdf.x / pdf, brdf.y / pdf, brdf.z / pdf);
+}
+
+// MaterialGGX::eval (MaterialGGX.cpp:94-101).
+__device__ __forceinline__ f3 ggx_eval(f3 wo, f3 base, float roughness, float metallic, f3 wi) {
+    if (wi.z < 0.0f) return mk(0.0f, 0.0f, 0.0f);
+    return ggx_brdf(wo, base, alpha_from_roughness(roughness), metallic, wi, nullptr);
+}
+
+// ---- lights -------------------------------------------------------------------------------
+// Light::sample(position, dist, attenuation) for the three analytic types.
+__device__ __forceinline__ f3 light_sample(const PtLight &l, f3 p, float &dist, float &atten) {
+    atten = 0.0f;
+    if (l.type == PT_LIGHT_DIRECTIONAL) {
+        atten = 1.0f;
+        dist = FLT_MAX;
+        return mk(-l.direction[0], -l.direction[1], -l.direction[2]);
+    }
+    f3 d = mk(l.position[0] - p.x, l.position[1] - p.y, l.position[2] - p.z);
+    dist = sqrtf(dot(d, d));
+    if (dist > l.radius) return mk(0.0f, 0.0f, 0.0f);
+    if (dist > 0.0f) d = d / dist;
+    const float rr = dist / l.radius;
+    const float num = fminf(fmaxf(1.0f - rr * rr, 0.0f), 1.0f);
+    if (l.type == PT_LIGHT_POINT) {
+        atten = num * num;
+        return d;
+    }
+    const float currentCos = -(d.x * l.direction[0] + d.y * l.direction[1] + d.z * l.direction[2]);
+    const float outerCos = cosf(l.half_outer);
+    // The reference compares with cos(outerCos), not outerCos (SpotLight.cpp:68); kept.
+    if (currentCos < cosf(outerCos)) return mk(0.0f, 0.0f, 0.0f);
+    const float innerCos = cosf(l.half_inner);
+    const float ang = fminf(fmaxf((currentCos - outerCos) / (innerCos - outerCos), 0.0f), 1.0f);
+    atten = ang * num * num;
+    return d;
+}
+
+// ---- geometry helpers --------------------------------------------------------------------
+__device__ __forceinline__ int find_object(const PtScene &s, uint32_t prim) {
+    int lo = 0, hi = s.nobjects - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s.objects[mid].first_tri <= prim) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ f3 ld3(const float *a, uint32_t i) { return mk(a[3 * i], a[3 * i + 1], a[3 * i + 2]); }
+
+__device__ __forceinline__ f3 mat3_mul(const float *m, f3 v) {
+    return mk(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+              m[6] * v.x + m[7] * v.y + m[8] * v.z);
+}
+
+}  // namespace rgb

@@ -1,0 +1,391 @@
+// Wavefront kernels of the path tracer: replace the per-sample loop body of
+// PathTracer::render (PathTracer.cpp:186-293 of kosua20/Rendu).
+//
+// One wave = every pixel x a run of S consecutive sample indices (P = W*H*S paths).
+// Per bounce:
+//   trace  -- closest hit for the compacted ray queue (rt_traverse.cuh);
+//   shade  -- the reference's hit logic (background on miss, alpha cut-out, emission,
+//             local frame, NEE light pick + evaluation, BSDF sampling), appending
+//             continuing paths to the next queue and shadow rays to the shadow queue with
+//             one atomic per warp;
+//   shadow -- PathTracer::checkVisibility for every queued shadow ray: one any-hit query
+//             when the scene has no alpha-masked material, else the reference's walk of
+//             closest hits through transparent texels.
+// After the last bounce, `accumulate` adds min(L, 5) of each sample to its pixel in sample
+// order (the reference's order), and `store` divides by spp.
+#include "pt_scene.hpp"
+#include "rt_traverse.cuh"
+
+namespace rgb {
+namespace {
+
+__device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool pred) {
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, pred);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(act) - 1;
+    uint32_t base = 0;
+    if (lane == leader && m) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(act, base, leader);
+    return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+}
+
+__global__ void k_raygen(PtFrame f, PtWave w) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t P = f.npix * f.S;
+    if (p == 0) w.counters[0] = P;
+    if (p >= P) return;
+    const uint32_t pixel = p % f.npix;
+    const uint32_t sid = f.s0 + p / f.npix;
+    const uint32_t x = pixel % f.W, y = pixel / f.W;
+    const U4 r = philox(U4{pixel, sid, 0u, 0u}, f.seed_lo, f.seed_hi);
+    const float jx = u01(r.x), jy = u01(r.y);
+    // PathTracer::getSamplePosition (PathTracer.cpp:71-84) and the ray set-up (:191-198).
+    const int sidy = (int)sid / (int)f.cx, sidx = (int)sid % (int)f.cx;
+    const float sx = (float)x + ((float)sidx + jx) * f.cell_x;
+    const float sy = (float)y + ((float)sidy + jy) * f.cell_y;
+    const float nx = sx / (float)f.W, ny = sy / (float)f.H;
+    const f3 world = mk(f.corner[0] + nx * f.dx[0] + ny * f.dy[0], f.corner[1] + nx * f.dx[1] + ny * f.dy[1],
+                        f.corner[2] + nx * f.dx[2] + ny * f.dy[2]);
+    const f3 dir = xnormalize(xsub(world, mk(f.eye[0], f.eye[1], f.eye[2])));
+    w.qray[0][p] = rt_ray{f.eye[0], f.eye[1], f.eye[2], 1e-4f, dir.x, dir.y, dir.z, 1e8f};
+    w.qpath[0][p] = p;
+    w.atten[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    w.color[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    w.ndc[p] = make_float2(nx, ny);
+}
+
+template <int STACK>
+__global__ void __launch_bounds__(128) k_trace_queue(PtScene s, const rt_ray *__restrict__ q,
+                                                     const uint32_t *__restrict__ count, rt_hit *__restrict__ hits,
+                                                     unsigned long long *stats, int stat_slot) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = *count;
+    if (i == 0) atomicAdd(&stats[stat_slot], (unsigned long long)n);
+    if (i >= n) return;
+    const float4 *rp = reinterpret_cast<const float4 *>(q + i);
+    const RayState r = make_ray_state(rp[0], rp[1]);
+    TraceResult res;
+    res.found = false;
+    res.t = FLT_MAX;
+    res.u = res.v = 0.0f;
+    res.prim = RT_NO_HIT;
+    uint32_t a = 0, b = 0;
+    if (r.valid && !s.empty) res = traverse<false, false, STACK>(s.nodes, s.tris, r, s.status, a, b);
+    hits[i] = rt_hit{res.t, res.u, res.v, res.found ? res.prim : RT_NO_HIT};
+}
+
+struct SurfaceHit {
+    int obj;
+    uint32_t i0, i1, i2;  // global vertex indices into the attribute pools
+    float u, v, w;
+};
+
+__device__ __forceinline__ SurfaceHit surface(const PtScene &s, uint32_t prim, float u, float v) {
+    SurfaceHit h;
+    h.obj = find_object(s, prim);
+    const PtObject &o = s.objects[h.obj];
+    const PtMesh m = s.meshes[o.mesh];
+    const uint32_t local = prim - o.first_tri;
+    const uint32_t *ix = s.indices + m.first_index + 3 * local;
+    h.i0 = m.first_vertex + ix[0];
+    h.i1 = m.first_vertex + ix[1];
+    h.i2 = m.first_vertex + ix[2];
+    h.u = u;
+    h.v = v;
+    h.w = 1.0f - u - v;  // Raycaster::Hit (Raycaster.cpp:10-12)
+    return h;
+}
+
+// Raycaster::interpolateAttribute (Raycaster.hpp:90-97).
+__device__ __forceinline__ f3 interp3(const float *a, const SurfaceHit &h) {
+    const f3 a0 = ld3(a, h.i0), a1 = ld3(a, h.i1), a2 = ld3(a, h.i2);
+    return mk(h.w * a0.x + h.u * a1.x + h.v * a2.x, h.w * a0.y + h.u * a1.y + h.v * a2.y,
+              h.w * a0.z + h.u * a1.z + h.v * a2.z);
+}
+
+__device__ __forceinline__ float2 interp_uv(const float *a, const SurfaceHit &h) {
+    return make_float2(h.w * a[2 * h.i0] + h.u * a[2 * h.i1] + h.v * a[2 * h.i2],
+                       h.w * a[2 * h.i0 + 1] + h.u * a[2 * h.i1 + 1] + h.v * a[2 * h.i2 + 1]);
+}
+
+__global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, int cur, uint32_t did) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = w.counters[cur];
+    if (i >= n) return;
+    const int nxt = cur ^ 1;
+    const uint32_t path = w.qpath[cur][i];
+    const rt_ray ray = w.qray[cur][i];
+    const rt_hit hit = w.hits[i];
+    const f3 pos = mk(ray.ox, ray.oy, ray.oz);
+    const f3 dir = mk(ray.dx, ray.dy, ray.dz);
+    float4 c4 = w.color[path], a4 = w.atten[path];
+    f3 color = mk(c4.x, c4.y, c4.z), atten = mk(a4.x, a4.y, a4.z);
+    bool cont = false, shadow = false;
+    f3 next_o = pos, next_d = dir, sh_o = pos, sh_d = dir, sh_c = mk(0, 0, 0);
+    float sh_max = 0.0f;
+
+    if (hit.prim == RT_NO_HIT) {
+        // PathTracer.cpp:206-209.
+        const float2 ndc = w.ndc[path];
+        color += atten * eval_background(s, dir, ndc.x, ndc.y, did == 0);
+    } else {
+        const SurfaceHit sh = surface(s, hit.prim, hit.u, hit.v);
+        const PtObject &obj = s.objects[sh.obj];
+        const PtMaterial mat = s.materials[obj.material];
+        const f3 p = mk(pos.x + hit.t * dir.x, pos.y + hit.t * dir.y, pos.z + hit.t * dir.z);
+        const float2 uv = obj.use_uv ? interp_uv(s.uvs, sh) : make_float2(0.5f, 0.5f);
+        const float4 bcol = tex_rgbal(s, mat.tex[0], uv.x, uv.y);
+        if (mat.masked && bcol.w < 0.01f) {
+            // Alpha cut-out: same direction from the hit point, one bounce consumed (:223-226).
+            cont = did + 1 < f.depth;
+            next_o = p;
+        } else if (mat.type == PT_MAT_EMISSIVE) {
+            color += atten * mk(bcol.x, bcol.y, bcol.z);  // :228-234
+        } else {
+            // PathTracer::buildLocalFrame (:86-122).
+            const f3 nn = normalize(interp3(s.normals, sh));
+            const f3 tt = normalize(interp3(s.tangents, sh));
+            const f3 bb = normalize(interp3(s.bitangents, sh));
+            f3 t0 = mat3_mul(obj.invtp, tt), t1 = mat3_mul(obj.invtp, bb), t2 = mat3_mul(obj.invtp, nn);
+            if (!(dot(t2, dir) < 0.0f)) t2 = -t2;
+            if (obj.use_uv) {
+                const float4 img = tex_rgbal(s, mat.tex[1], uv.x, uv.y);
+                const f3 ln = normalize(mk(2.0f * img.x - 1.0f, 2.0f * img.y - 1.0f, 2.0f * img.z - 1.0f));
+                t2 = mk(t0.x * ln.x + t1.x * ln.y + t2.x * ln.z, t0.y * ln.x + t1.y * ln.y + t2.y * ln.z,
+                        t0.z * ln.x + t1.z * ln.y + t2.z * ln.z);
+            }
+            t2 = normalize(t2);
+            t1 = normalize(cross(t2, normalize(t0)));
+            t0 = normalize(cross(t1, t2));
+            // World -> local is the transpose of the frame.
+            const f3 mdir = -dir;
+            const f3 wo = normalize(mk(dot(t0, mdir), dot(t1, mdir), dot(t2, mdir)));
+            const f3 base = mk(powf(bcol.x, 2.2f), powf(bcol.y, 2.2f), powf(bcol.z, 2.2f));
+            const float4 rmao = tex_rgbal(s, mat.tex[2], uv.x, uv.y);
+            const U4 rnd = philox(U4{path % f.npix, f.s0 + path / f.npix, did + 1u, 0u}, f.seed_lo, f.seed_hi);
+            if (s.nlights > 0) {
+                // Next-event estimation on one uniformly picked analytic light (:248-272).
+                const PtLight &L = s.lights[uint_below(rnd.x, (uint32_t)s.nlights)];
+                const f3 ps = mk(p.x + 0.001f * t2.x, p.y + 0.001f * t2.y, p.z + 0.001f * t2.z);
+                float maxd, fall;
+                const f3 ld = light_sample(L, ps, maxd, fall);
+                if (fall > 0.0f) {
+                    const f3 lwi = normalize(mk(dot(t0, ld), dot(t1, ld), dot(t2, ld)));
+                    const f3 ev = ggx_eval(wo, base, rmao.x, rmao.y, lwi);
+                    const float inv_pdf = (float)s.nlights;  // 1 / (1 / lights)
+                    const f3 ill = mk(fall * ev.x * L.color[0] * inv_pdf, fall * ev.y * L.color[1] * inv_pdf,
+                                      fall * ev.z * L.color[2] * inv_pdf);
+                    const f3 contrib = atten * ill;
+                    if (L.shadows) {
+                        shadow = true;
+                        sh_o = ps;
+                        sh_d = ld;
+                        sh_max = maxd;
+                        sh_c = contrib;
+                    } else {
+                        color += contrib;
+                    }
+                }
+            }
+            f3 wi;
+            const f3 weight = ggx_sample_eval(wo, base, rmao.x, rmao.y, u01(rnd.y), u01(rnd.z), u01(rnd.w), wi);
+            const f3 nd = normalize(mk(t0.x * wi.x + t1.x * wi.y + t2.x * wi.z, t0.y * wi.x + t1.y * wi.y + t2.y * wi.z,
+                                       t0.z * wi.x + t1.z * wi.y + t2.z * wi.z));
+            atten *= weight;
+            if (did + 1 < f.depth) {
+                cont = true;
+                next_o = p;
+                next_d = normalize(nd);
+            }
+        }
+    }
+    w.color[path] = make_float4(color.x, color.y, color.z, 0.0f);
+    w.atten[path] = make_float4(atten.x, atten.y, atten.z, 0.0f);
+    const uint32_t slot = warp_append(&w.counters[nxt], cont);
+    if (cont) {
+        w.qray[nxt][slot] = rt_ray{next_o.x, next_o.y, next_o.z, 1e-4f, next_d.x, next_d.y, next_d.z, 1e8f};
+        w.qpath[nxt][slot] = path;
+    }
+    const uint32_t ss = warp_append(&w.counters[2], shadow);
+    if (shadow) {
+        w.sray[ss] = rt_ray{sh_o.x, sh_o.y, sh_o.z, 0.001f, sh_d.x, sh_d.y, sh_d.z, sh_max};
+        w.scontrib[ss] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(path));
+    }
+}
+
+// PathTracer::checkVisibility (PathTracer.cpp:124-157).
+template <int STACK>
+__global__ void __launch_bounds__(128) k_shadow(PtScene s, PtWave w) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = w.counters[2];
+    if (i == 0) atomicAdd(&w.stats[2], (unsigned long long)n);
+    if (i >= n) return;
+    const rt_ray ray = w.sray[i];
+    const float4 c = w.scontrib[i];
+    const uint32_t path = __float_as_uint(c.w);
+    bool visible = true;
+    uint32_t a = 0, b = 0;
+    if (!s.empty) {
+        if (!s.any_masked) {
+            const float4 *rp = reinterpret_cast<const float4 *>(&ray);
+            const RayState r = make_ray_state(rp[0], rp[1]);
+            if (r.valid) visible = !traverse<true, false, STACK>(s.nodes, s.tris, r, s.status, a, b).found;
+        } else {
+            f3 lpos = mk(ray.ox, ray.oy, ray.oz);
+            const f3 d = mk(ray.dx, ray.dy, ray.dz);
+            float maxd = ray.tmax;
+            int steps = 0;
+            while (maxd > 0.0f) {
+                if (++steps > 256) {  // bounded walk: report and treat as occluded
+                    atomicOr(s.status, RT_DEV_TIMEOUT);
+                    visible = false;
+                    break;
+                }
+                if (steps > 1) atomicAdd(&w.stats[2], 1ull);
+                const RayState r = make_ray_state(make_float4(lpos.x, lpos.y, lpos.z, 0.001f),
+                                                  make_float4(d.x, d.y, d.z, maxd));
+                if (!r.valid) break;
+                const TraceResult h = traverse<false, false, STACK>(s.nodes, s.tris, r, s.status, a, b);
+                if (!h.found) break;
+                const SurfaceHit sh = surface(s, h.prim, h.u, h.v);
+                const PtObject &obj = s.objects[sh.obj];
+                const PtMaterial mat = s.materials[obj.material];
+                if (!mat.masked || !obj.use_uv) {
+                    visible = false;
+                    break;
+                }
+                const float2 uv = interp_uv(s.uvs, sh);
+                if (tex_rgbal(s, mat.tex[0], uv.x, uv.y).w < 0.01f) {
+                    maxd = maxd - h.t;
+                    lpos = mk(lpos.x + h.t * d.x, lpos.y + h.t * d.y, lpos.z + h.t * d.z);
+                } else {
+                    visible = false;
+                    break;
+                }
+            }
+        }
+    }
+    if (visible) {
+        float4 col = w.color[path];
+        col.x += c.x;
+        col.y += c.y;
+        col.z += c.z;
+        w.color[path] = col;
+    }
+}
+
+// render.rgb(x, y) += min(sampleColor, 5) in sample order (PathTracer.cpp:288).
+__global__ void k_accumulate(PtFrame f, PtWave w) {
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+    if (px >= f.npix) return;
+    float r = w.accum[3 * (size_t)px], g = w.accum[3 * (size_t)px + 1], b = w.accum[3 * (size_t)px + 2];
+    for (uint32_t s = 0; s < f.S; ++s) {
+        const float4 c = w.color[(size_t)s * f.npix + px];
+        r += gmin(c.x, 5.0f);
+        g += gmin(c.y, 5.0f);
+        b += gmin(c.z, 5.0f);
+    }
+    w.accum[3 * (size_t)px] = r;
+    w.accum[3 * (size_t)px + 1] = g;
+    w.accum[3 * (size_t)px + 2] = b;
+}
+
+__global__ void k_load(const float *__restrict__ img, uint32_t comps, uint32_t npix, float *__restrict__ accum) {
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+    if (px >= npix) return;
+    for (int k = 0; k < 3; ++k) accum[3 * (size_t)px + k] = img[(size_t)px * comps + k];
+}
+
+// render.rgb(x, y) /= samples (PathTracer.cpp:291-292).
+__global__ void k_store(const float *__restrict__ accum, uint32_t npix, float spp, uint32_t comps,
+                        float *__restrict__ img) {
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+    if (px >= npix) return;
+    for (int k = 0; k < 3; ++k) img[(size_t)px * comps + k] = accum[3 * (size_t)px + k] / spp;
+}
+
+__global__ void k_mat_eval(const float *__restrict__ c, uint32_t n, float *__restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *q = c + 11 * (size_t)i;
+    const f3 r = ggx_eval(mk(q[0], q[1], q[2]), mk(q[3], q[4], q[5]), q[6], q[7], mk(q[8], q[9], q[10]));
+    out[3 * (size_t)i] = r.x;
+    out[3 * (size_t)i + 1] = r.y;
+    out[3 * (size_t)i + 2] = r.z;
+}
+
+__global__ void k_mat_sample(const float *__restrict__ c, const float *__restrict__ u, uint32_t n,
+                             float *__restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *q = c + 8 * (size_t)i;
+    const float *uu = u + 3 * (size_t)i;
+    f3 wi = mk(0.0f, 0.0f, 0.0f);
+    const f3 r = ggx_sample_eval(mk(q[0], q[1], q[2]), mk(q[3], q[4], q[5]), q[6], q[7], uu[0], uu[1], uu[2], wi);
+    float *o = out + 6 * (size_t)i;
+    o[0] = r.x; o[1] = r.y; o[2] = r.z;
+    o[3] = wi.x; o[4] = wi.y; o[5] = wi.z;
+}
+
+}  // namespace
+
+int pt_launch_material(const float *cases, const float *uniforms, uint32_t n, float *out, cudaStream_t st) {
+    if (n == 0) return RT_OK;
+    if (uniforms) k_mat_sample<<<(n + 127) / 128, 128, 0, st>>>(cases, uniforms, n, out);
+    else k_mat_eval<<<(n + 127) / 128, 128, 0, st>>>(cases, n, out);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pt_launch_raygen(const PtFrame &f, const PtWave &w, cudaStream_t st) {
+    const uint32_t P = f.npix * f.S;
+    k_raygen<<<(P + 255) / 256, 256, 0, st>>>(f, w);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pt_launch_trace(const PtScene &s, const PtWave &w, int cur, uint32_t cap, int stat_slot, cudaStream_t st) {
+    const unsigned blocks = (cap + 127) / 128;
+    if (s.big_stack)
+        k_trace_queue<256><<<blocks, 128, 0, st>>>(s, w.qray[cur], &w.counters[cur], w.hits, w.stats, stat_slot);
+    else
+        k_trace_queue<64><<<blocks, 128, 0, st>>>(s, w.qray[cur], &w.counters[cur], w.hits, w.stats, stat_slot);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pt_launch_shade(const PtScene &s, const PtFrame &f, const PtWave &w, int cur, uint32_t did, uint32_t cap,
+                    cudaStream_t st) {
+    k_shade<<<(cap + 127) / 128, 128, 0, st>>>(s, f, w, cur, did);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pt_launch_shadow(const PtScene &s, const PtWave &w, uint32_t cap, cudaStream_t st) {
+    const unsigned blocks = (cap + 127) / 128;
+    if (s.big_stack) k_shadow<256><<<blocks, 128, 0, st>>>(s, w);
+    else k_shadow<64><<<blocks, 128, 0, st>>>(s, w);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pt_launch_accumulate(const PtFrame &f, const PtWave &w, cudaStream_t st) {
+    k_accumulate<<<(f.npix + 255) / 256, 256, 0, st>>>(f, w);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pt_launch_load(const float *img, uint32_t comps, uint32_t npix, float *accum, cudaStream_t st) {
+    k_load<<<(npix + 255) / 256, 256, 0, st>>>(img, comps, npix, accum);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pt_launch_store(const float *accum, uint32_t npix, float spp, uint32_t comps, float *img, cudaStream_t st) {
+    k_store<<<(npix + 255) / 256, 256, 0, st>>>(accum, npix, spp, comps, img);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+}  // namespace rgb

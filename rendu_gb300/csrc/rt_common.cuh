@@ -15,6 +15,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "rendu_gb300.h"
+
 namespace rgb {
 
 struct f3 {

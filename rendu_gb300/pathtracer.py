@@ -1,0 +1,137 @@
+"""Host-side mirror of Rendu's ``PathTracer`` (src/apps/pathtracer/PathTracer.hpp:11-76)
+over the C-ABI ``pt_*`` entry points.
+
+``PathTracer(scene)`` uploads the scene and builds its raycaster (PathTracer.cpp:11-21);
+``render(camera, samples, depth, image)`` accumulates ``samples`` (rounded to a power of
+two) paths per pixel into ``image`` and normalises, as PathTracer::render does
+(PathTracer.cpp:159-299). ``image`` is a float32 array (H, W, C>=3) on the host or a CUDA
+tensor of the same shape.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .raycaster import Raycaster
+
+
+def _f3(v):
+    return (C.c_float * 3)(*[float(x) for x in v])
+
+
+def camera_desc(cam: dict) -> L.pt_camera_desc:
+    return L.pt_camera_desc(_f3(cam["eye"]), _f3(cam["center"]), _f3(cam["up"]), float(cam.get("fov", 1.3)),
+                            float(cam.get("ratio", 1.0)))
+
+
+def light_desc(l: dict) -> L.pt_light_desc:
+    return L.pt_light_desc(int(l["type"]), int(bool(l.get("shadows", False))), _f3(l.get("color", (1, 1, 1))),
+                           _f3(l.get("position", (0, 0, 0))), _f3(l.get("direction", (0, -1, 0))),
+                           float(l.get("radius", 1.0)), float(l.get("inner", 0.5)), float(l.get("outer", 0.8)))
+
+
+class PathTracer:
+    """Device path tracer over an in-memory scene (rendu_gb300.scenes.Scene)."""
+
+    def __init__(self, scene, device: int = 0):
+        h = C.c_void_p()
+        L.call("pt_scene_create", C.byref(h), int(device))
+        self._h = h
+        self.device = device
+        self._keep = []
+        self.scene = scene
+        try:
+            self._upload(scene)
+        except Exception:
+            self.close()
+            raise
+
+    def _upload(self, sc):
+        tid = C.c_uint32()
+        for img in sc.textures:
+            a = np.ascontiguousarray(img, np.float32)
+            hgt, wid = a.shape[:2]
+            ch = 1 if a.ndim == 2 else a.shape[2]
+            L.call("pt_scene_add_texture", self._h, wid, hgt, ch, a.ctypes.data, C.byref(tid))
+        for m in sc.meshes:
+            arrs = [np.ascontiguousarray(x, np.float32).reshape(-1) for x in (m.positions, m.normals, m.tangents,
+                                                                                m.bitangents)]
+            uv = None if m.texcoords is None else np.ascontiguousarray(m.texcoords, np.float32).reshape(-1)
+            idx = np.ascontiguousarray(m.indices, np.uint32).reshape(-1)
+            self._keep += arrs + [uv, idx]
+            d = L.pt_mesh_desc(arrs[0].ctypes.data, arrs[1].ctypes.data, arrs[2].ctypes.data, arrs[3].ctypes.data,
+                               uv.ctypes.data if uv is not None else None, len(arrs[0]) // 3, idx.ctypes.data, len(idx))
+            L.call("pt_scene_add_mesh", self._h, C.byref(d), C.byref(tid))
+        for mat in sc.materials:
+            d = L.pt_material_desc(int(mat["type"]), int(bool(mat["masked"])), (C.c_uint32 * 3)(*mat["tex"]))
+            L.call("pt_scene_add_material", self._h, C.byref(d), C.byref(tid))
+        for o in sc.objects:
+            m = np.ascontiguousarray(np.asarray(o["model"], np.float32).T.reshape(16))
+            L.call("pt_scene_add_object", self._h, int(o["mesh"]), int(o["material"]), m.ctypes.data, C.byref(tid))
+        for l in sc.lights:
+            L.call("pt_scene_add_light", self._h, C.byref(light_desc(l)))
+        bg = sc.background
+        L.call("pt_scene_set_background", self._h, int(bg["mode"]), _f3(bg.get("color", (0, 0, 0))),
+               (C.c_uint32 * 6)(*bg.get("tex", (0,) * 6)))
+        L.call("pt_scene_commit", self._h)
+
+    def render(self, camera, samples: int, depth: int, image, seed: int = 0):
+        """PathTracer::render(camera, samples, depth, image): accumulate and normalise into
+        ``image`` (H, W, C) float32, host array or CUDA tensor; returns ``image``."""
+        cam = camera_desc(camera if isinstance(camera, dict) else camera.__dict__)
+        if type(image).__module__.startswith("torch") and getattr(image, "is_cuda", False):
+            import torch
+
+            hgt, wid, comp = image.shape
+            assert image.is_contiguous() and image.dtype == torch.float32
+            L.call("pt_render", self._h, C.byref(cam), int(samples), int(depth), int(seed), C.c_void_p(image.data_ptr()),
+                   wid, hgt, comp, C.c_void_p(torch.cuda.current_stream().cuda_stream), L.RT_FLAG_DEVICE_PTRS)
+            return image
+        if not (isinstance(image, np.ndarray) and image.dtype == np.float32 and image.flags.c_contiguous):
+            raise TypeError("image must be a C-contiguous float32 array (H, W, C)")
+        hgt, wid, comp = image.shape
+        L.call("pt_render", self._h, C.byref(cam), int(samples), int(depth), int(seed), image.ctypes.data, wid, hgt,
+               comp, None, 0)
+        return image
+
+    def last_stats(self) -> dict:
+        s = L.pt_render_stats()
+        L.call("pt_get_render_stats", self._h, C.byref(s))
+        d = {k: getattr(s, k) for k, _ in s._fields_}
+        d["rays"] = d["primary_rays"] + d["bounce_rays"] + d["shadow_rays"]
+        return d
+
+    def raycaster(self) -> Raycaster:
+        """PathTracer::raycaster() (PathTracer.hpp:29): the scene's raycaster (not owned)."""
+        return Raycaster(self.device, _handle=L.lib().pt_scene_raycaster(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            L.lib().pt_scene_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def material_eval(cases):
+    """MaterialGGX::eval on the device for n cases {wo.xyz, base.rgb, rough, metal, wi.xyz}."""
+    c = np.ascontiguousarray(cases, np.float32).reshape(-1, 11)
+    out = np.zeros((len(c), 3), np.float32)
+    L.call("pt_material_eval", c.ctypes.data, len(c), out.ctypes.data, 0)
+    return out
+
+
+def material_sample(cases, uniforms):
+    """MaterialGGX::sampleAndEval on the device for n cases {wo.xyz, base.rgb, rough, metal}
+    with the three uniforms it draws given per case; returns (n, 6) {weight.rgb, wi.xyz}."""
+    c = np.ascontiguousarray(cases, np.float32).reshape(-1, 8)
+    u = np.ascontiguousarray(uniforms, np.float32).reshape(-1, 3)
+    out = np.zeros((len(c), 6), np.float32)
+    L.call("pt_material_sample", c.ctypes.data, u.ctypes.data, len(c), out.ctypes.data, 0)
+    return out
