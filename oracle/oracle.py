@@ -102,15 +102,7 @@ def ref_lib():
         lib.ref_ggx_sample.argtypes = [_f32p, _u32p, C.c_size_t, _f32p, _f32p]
         lib.ref_cosine_hemisphere.argtypes = [_u32p, C.c_size_t, _f32p]
         lib.ref_pixel_shifts.argtypes = [C.c_void_p, _f32p]
-        lib.ref_pt_create.restype = C.c_void_p
-        lib.ref_pt_destroy.argtypes = [C.c_void_p]
-        lib.ref_pt_add_texture.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, _f32p]
-        lib.ref_pt_add_mesh.argtypes = [C.c_void_p, C.c_void_p]
-        lib.ref_pt_add_material.argtypes = [C.c_void_p, C.c_void_p]
-        lib.ref_pt_add_object.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
-        lib.ref_pt_add_light.argtypes = [C.c_void_p, C.c_void_p]
-        lib.ref_pt_set_background.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
-        lib.ref_pt_commit.argtypes = [C.c_void_p]
+        _pt_sigs(_Names(lib), "ref_pt_")
         lib.ref_pt_render.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, _f32p,
                                       C.c_uint32, C.c_uint32]
         _ref = lib
@@ -240,4 +232,153 @@ def ref_cosine_hemisphere(seeds):
     seeds = np.ascontiguousarray(seeds, np.uint32)
     out = np.zeros((len(seeds), 5), np.float32)
     ref_lib().ref_cosine_hemisphere(seeds, len(seeds), out.reshape(-1))
+    return out
+
+
+# ---- path tracer oracles ------------------------------------------------------------------
+def _pt_sigs(lib, prefix):
+    lib[prefix + "create"].restype = C.c_void_p
+    lib[prefix + "destroy"].argtypes = [C.c_void_p]
+    lib[prefix + "add_texture"].argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, _f32p]
+    lib[prefix + "add_mesh"].argtypes = [C.c_void_p, C.c_void_p]
+    lib[prefix + "add_material"].argtypes = [C.c_void_p, C.c_void_p]
+    lib[prefix + "add_object"].argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
+    lib[prefix + "add_light"].argtypes = [C.c_void_p, C.c_void_p]
+    lib[prefix + "set_background"].argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    lib[prefix + "commit"].argtypes = [C.c_void_p]
+
+
+class _OracleTracer:
+    """Loads an in-memory scene (rendu_gb300.scenes.Scene) into a CPU path tracer oracle."""
+
+    def __init__(self, lib, prefix, scene):
+        from rendu_gb300 import _lib as L
+        from rendu_gb300.pathtracer import light_desc
+
+        self.lib, self.p = lib, prefix
+        f = lambda n: getattr(lib, prefix + n)  # noqa: E731
+        self.h = f("create")()
+        self._keep = []
+        for img in scene.textures:
+            a = np.ascontiguousarray(img, np.float32)
+            hgt, wid = a.shape[:2]
+            ch = 1 if a.ndim == 2 else a.shape[2]
+            self._keep.append(a)
+            f("add_texture")(self.h, wid, hgt, ch, a.reshape(-1))
+        for m in scene.meshes:
+            arrs = [np.ascontiguousarray(x, np.float32).reshape(-1) for x in (m.positions, m.normals, m.tangents,
+                                                                                m.bitangents)]
+            uv = None if m.texcoords is None else np.ascontiguousarray(m.texcoords, np.float32).reshape(-1)
+            idx = np.ascontiguousarray(m.indices, np.uint32).reshape(-1)
+            self._keep += arrs + [uv, idx]
+            d = L.pt_mesh_desc(arrs[0].ctypes.data, arrs[1].ctypes.data, arrs[2].ctypes.data, arrs[3].ctypes.data,
+                               uv.ctypes.data if uv is not None else None, len(arrs[0]) // 3, idx.ctypes.data, len(idx))
+            f("add_mesh")(self.h, C.byref(d))
+        for mat in scene.materials:
+            d = L.pt_material_desc(int(mat["type"]), int(bool(mat["masked"])), (C.c_uint32 * 3)(*mat["tex"]))
+            f("add_material")(self.h, C.byref(d))
+        for o in scene.objects:
+            m = np.ascontiguousarray(np.asarray(o["model"], np.float32).T.reshape(16))
+            self._keep.append(m)
+            f("add_object")(self.h, int(o["mesh"]), int(o["material"]), m.ctypes.data)
+        for l in scene.lights:
+            f("add_light")(self.h, C.byref(light_desc(l)))
+        bg = scene.background
+        col = (C.c_float * 3)(*[float(x) for x in bg.get("color", (0, 0, 0))])
+        f("set_background")(self.h, int(bg["mode"]), col, (C.c_uint32 * 6)(*bg.get("tex", (0,) * 6)))
+        f("commit")(self.h)
+
+    def close(self):
+        if self.h:
+            getattr(self.lib, self.p + "destroy")(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PortPathTracer(_OracleTracer):
+    """The C restatement of PathTracer (oracle/port/pt_port.c); Philox random stream."""
+
+    def __init__(self, scene):
+        lib = port_lib()
+        if not hasattr(lib, "_pt_ready"):
+            _pt_sigs(_Names(lib), "port_pt_")
+            lib.port_pt_render.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, _f32p,
+                                           C.c_uint32, C.c_uint32, C.c_int, _u64p]
+            lib.port_ggx_eval.argtypes = [_f32p, C.c_size_t, _f32p]
+            lib.port_ggx_sample.argtypes = [_f32p, _f32p, C.c_size_t, _f32p]
+            lib.port_pixel_shifts.argtypes = [C.c_void_p, _f32p]
+            lib._pt_ready = True
+        super().__init__(lib, "port_pt_", scene)
+
+    def render(self, camera, samples, depth, width, height, seed=0, threads=0, image=None):
+        from rendu_gb300.pathtracer import camera_desc
+
+        img = np.zeros((height, width, 3), np.float32) if image is None else image
+        rays = np.zeros(3, np.uint64)
+        cam = camera_desc(camera)
+        r = self.lib.port_pt_render(self.h, C.byref(cam), int(samples), int(depth), int(seed), img.reshape(-1), width,
+                                    height, int(threads), rays)
+        if r != 0:
+            raise RuntimeError("port render failed")
+        self.rays = rays
+        return img
+
+
+class RefPathTracer(_OracleTracer):
+    """The reference's own PathTracer compiled from its sources (mt19937 random streams)."""
+
+    def __init__(self, scene):
+        super().__init__(ref_lib(), "ref_pt_", scene)
+
+    def render(self, camera, samples, depth, width, height, seed=0):
+        from rendu_gb300.pathtracer import camera_desc
+
+        img = np.zeros((height, width, 3), np.float32)
+        cam = camera_desc(camera)
+        self.lib.ref_pt_render(self.h, C.byref(cam), int(samples), int(depth), int(seed), img.reshape(-1), width,
+                               height)
+        return img
+
+
+class _Names(dict):
+    def __init__(self, lib):
+        super().__init__()
+        self.lib = lib
+
+    def __getitem__(self, k):
+        return getattr(self.lib, k)
+
+
+def port_ggx_eval(cases):
+    lib = port_lib()
+    lib.port_ggx_eval.argtypes = [_f32p, C.c_size_t, _f32p]
+    c = np.ascontiguousarray(cases, np.float32)
+    out = np.zeros((len(c), 3), np.float32)
+    lib.port_ggx_eval(c.reshape(-1), len(c), out.reshape(-1))
+    return out
+
+
+def port_ggx_sample(cases, uniforms):
+    lib = port_lib()
+    lib.port_ggx_sample.argtypes = [_f32p, _f32p, C.c_size_t, _f32p]
+    c = np.ascontiguousarray(cases, np.float32)
+    u = np.ascontiguousarray(uniforms, np.float32)
+    out = np.zeros((len(c), 6), np.float32)
+    lib.port_ggx_sample(c.reshape(-1), u.reshape(-1), len(c), out.reshape(-1))
+    return out
+
+
+def port_pixel_shifts(camera: dict):
+    from rendu_gb300.pathtracer import camera_desc
+
+    lib = port_lib()
+    lib.port_pixel_shifts.argtypes = [C.c_void_p, _f32p]
+    out = np.zeros(12, np.float32)
+    cam = camera_desc(camera)
+    lib.port_pixel_shifts(C.byref(cam), out)
     return out

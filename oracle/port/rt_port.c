@@ -569,6 +569,45 @@ int port_rc_test_triangle(const port_rc *rc, const float *ray8, uint32_t global_
     return -1;
 }
 
+/* Single-ray queries for the path-tracer restatement (oracle/port/pt_port.c); each host
+ * thread keeps its own traversal stack. */
+static _Thread_local uint64_t *tl_stack = NULL;
+static _Thread_local size_t tl_cap = 0;
+
+static int ensure_stack(const port_rc *rc) {
+    const size_t need = (size_t)rc->mesh_count + 256;
+    if (tl_cap >= need) return 0;
+    uint64_t *p = (uint64_t *)realloc(tl_stack, need * sizeof(uint64_t));
+    if (!p) return -1;
+    tl_stack = p;
+    tl_cap = need;
+    return 0;
+}
+
+int port_rc_closest1(const port_rc *rc, const float *ray8, port_hit *out) {
+    uint64_t nb = 0, nt = 0;
+    if (ensure_stack(rc)) return -1;
+    closest_one(rc, ray8, out, &nb, &nt, &tl_stack, &tl_cap);
+    return out->prim != PORT_NO_HIT;
+}
+
+int port_rc_any1(const port_rc *rc, const float *ray8) {
+    if (ensure_stack(rc)) return -1;
+    return any_one(rc, ray8, &tl_stack, &tl_cap);
+}
+
+uint32_t port_rc_prim_mesh(const port_rc *rc, uint32_t prim) {
+    uint32_t lo = 0, hi = rc->mesh_count ? rc->mesh_count - 1 : 0;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) / 2;
+        if (rc->mesh_tri_offset[mid] <= prim) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+uint32_t port_rc_mesh_first_tri(const port_rc *rc, uint32_t mesh) { return rc->mesh_tri_offset[mesh]; }
+
 /* Copy of the transformed, merged vertex soup (addMesh order), for tests. */
 int port_rc_vertices(const port_rc *rc, float *out, size_t cap_floats) {
     if (!rc || cap_floats < 3 * rc->nverts) return -1;

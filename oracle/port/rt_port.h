@@ -35,6 +35,10 @@ int port_rc_intersect(const port_rc *rc, const float *rays, size_t n, port_hit *
 int port_rc_intersect_any(const port_rc *rc, const float *rays, size_t n, uint8_t *any, int threads);
 int port_rc_brute(const port_rc *rc, const float *rays, size_t n, port_hit *hits, int threads);
 int port_rc_test_triangle(const port_rc *rc, const float *ray8, uint32_t global_tri, port_hit *out);
+int port_rc_closest1(const port_rc *rc, const float *ray8, port_hit *out);
+int port_rc_any1(const port_rc *rc, const float *ray8);
+uint32_t port_rc_prim_mesh(const port_rc *rc, uint32_t prim);
+uint32_t port_rc_mesh_first_tri(const port_rc *rc, uint32_t mesh);
 int port_rc_vertices(const port_rc *rc, float *out, size_t cap_floats);
 
 #ifdef __cplusplus

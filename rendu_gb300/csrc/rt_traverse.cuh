@@ -4,9 +4,9 @@
 //
 //  * Ray set-up exactly as Ray::Ray (Intersection.cpp:3-5): d = normalize(dir),
 //    invdir = 1 / d, with the reference's rounding.
-//  * Box tests use a fused slab test (one FFMA per slab). Boxes were grown at build time
-//    so that this test is conservative; it decides only which triangles are visited,
-//    never the answer.
+//  * Box tests use a fused slab test (one FFMA per slab) with finite reciprocals. Boxes
+//    were grown at build time so that this test is conservative; it decides only which
+//    triangles are visited, never the answer.
 //  * The per-triangle test is Moller-Trumbore with the reference's exact operation order,
 //    rejection threshold |det| < FLT_EPSILON and inclusive/exclusive bounds
 //    (Raycaster.cpp:232-262), so every (ray, triangle) pair is accepted or rejected with
@@ -34,7 +34,14 @@ __device__ __forceinline__ RayState make_ray_state(float4 r0, float4 r1) {
     s.tmin = r0.w;
     s.tmax = r1.w;
     s.d = xnormalize(mk(r1.x, r1.y, r1.z));
-    s.inv = mk(__fdiv_rn(1.0f, s.d.x), __fdiv_rn(1.0f, s.d.y), __fdiv_rn(1.0f, s.d.z));
+    // The box test uses a reciprocal of the direction with components below 1e-20 in
+    // magnitude replaced by +-1e-20: an infinite reciprocal would turn the fused slab test
+    // into inf - inf = NaN for origins inside a slab. The exact direction still drives the
+    // per-triangle test, so only the (conservative) culling sees the difference.
+    const float ex = fabsf(s.d.x) < 1e-20f ? copysignf(1e-20f, s.d.x) : s.d.x;
+    const float ey = fabsf(s.d.y) < 1e-20f ? copysignf(1e-20f, s.d.y) : s.d.y;
+    const float ez = fabsf(s.d.z) < 1e-20f ? copysignf(1e-20f, s.d.z) : s.d.z;
+    s.inv = mk(1.0f / ex, 1.0f / ey, 1.0f / ez);
     s.oinv = mk(s.o.x * s.inv.x, s.o.y * s.inv.y, s.o.z * s.inv.z);
     // A zero-length or non-finite direction never hits (the reference's comparisons with
     // NaN all fail); neither does an empty window.

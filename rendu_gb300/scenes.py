@@ -313,6 +313,8 @@ class Scene:
 
     def add_material(self, albedo, rough=1.0, metal=0.0, emissive=False, masked=False, normal_tex=None,
                      albedo_tex=None) -> int:
+        """A Regular (Lambert+GGX) or Emissive material from constant colours, or from a
+        given albedo / normal-map texture id."""
         a = albedo_tex if albedo_tex is not None else self.add_texture(constant_texture(list(albedo) + [1.0]))
         n = normal_tex if normal_tex is not None else self.add_texture(constant_texture([0.5, 0.5, 1.0, 1.0]))
         r = self.add_texture(constant_texture([rough, metal, 1.0, 1.0]))
@@ -370,4 +372,60 @@ def cornell_scene(seed: int = 20261204, with_light: bool = False) -> Scene:
     sc.background = {"mode": 0, "color": (0.0, 0.0, 0.0), "tex": (0,) * 6}
     sc.camera = {"eye": (0.0, 1.0, 3.4), "center": (0.0, 1.0, 0.0), "up": (0.0, 1.0, 0.0), "fov": 1.3, "ratio": 1.0}
     _ = L
+    return sc
+
+
+def _checker(n, c0, c1, cells=4):
+    ij = np.indices((n, n)).sum(0) // max(1, n // cells)
+    img = np.where((ij % 2)[..., None] == 0, np.asarray(c0, np.float32), np.asarray(c1, np.float32))
+    return img.astype(np.float32)
+
+
+def feature_scene(seed: int = 20261204) -> Scene:
+    """A small scene exercising every shading feature of the reference path tracer:
+    textured albedo with wrapped texture coordinates, a normal map, an alpha cut-out
+    (masked) quad, a metallic GGX sphere without texture coordinates, an emissive quad,
+    point/spot lights with shadows and a directional light without, and a SKYBOX
+    (cubemap) background seen by every bounce."""
+    rng = np.random.default_rng(seed)
+    sc = Scene()
+    # Ground: checker albedo, UVs scaled x3 so that sampling wraps.
+    g = quad_mesh((-2, 0, -2), (4, 0, 0), (0, 0, 4))
+    g.texcoords = g.texcoords * 3.0
+    alb = sc.add_texture(_checker(16, (0.8, 0.8, 0.8, 1.0), (0.2, 0.3, 0.6, 1.0)))
+    gm = sc.add_material(None, rough=0.7, metal=0.0, albedo_tex=alb)
+    sc.add_object(sc.add_mesh(g), gm)
+    # Box with a bumpy normal map.
+    nrm = rng.normal(0.0, 0.25, (8, 8, 3))
+    nrm[..., 2] = 1.0
+    nrm /= np.linalg.norm(nrm, axis=2, keepdims=True)
+    ntex = sc.add_texture(np.concatenate([0.5 * nrm + 0.5, np.ones((8, 8, 1))], 2).astype(np.float32))
+    bm = sc.add_material((0.7, 0.4, 0.2), rough=0.5, metal=0.0, normal_tex=ntex)
+    sc.add_object(sc.add_mesh(box_mesh((0.6, 0.6, 0.6))), bm, translation((-0.7, 0.3, -0.2)) @ rotation_y(0.5))
+    # Metallic sphere without texture coordinates.
+    sph = icosphere_mesh(3, seed=seed, displacement=0.0)
+    sph.with_frames()
+    sm = sc.add_material((0.9, 0.8, 0.5), rough=0.2, metal=1.0)
+    sc.add_object(sc.add_mesh(sph), sm, translation((0.6, 0.45, 0.1)) @ scaling(0.45))
+    # Alpha cut-out quad (checker alpha).
+    cut = quad_mesh((-1.5, 0.0, 0.8), (1.2, 0, 0), (0, 1.2, 0))
+    ctex = sc.add_texture(_checker(8, (0.3, 0.8, 0.3, 1.0), (0.3, 0.8, 0.3, 0.0), cells=4))
+    cm = sc.add_material(None, rough=0.9, metal=0.0, masked=True, albedo_tex=ctex)
+    sc.add_object(sc.add_mesh(cut), cm, rotation_y(0.3))
+    # Small emitter.
+    em = sc.add_material((4.0, 3.5, 3.0), emissive=True)
+    sc.add_object(sc.add_mesh(quad_mesh((0.2, 1.6, -0.8), (0.5, 0, 0), (0, 0, 0.5))), em)
+    sc.lights += [
+        {"type": 0, "color": (3.0, 3.0, 3.0), "position": (0.5, 1.8, 1.0), "radius": 6.0, "shadows": True},
+        {"type": 2, "color": (4.0, 4.0, 3.0), "position": (-1.0, 2.0, 1.5), "direction": (0.4, -1.0, -0.6),
+         "radius": 8.0, "inner": 0.6, "outer": 1.2, "shadows": True},
+        {"type": 1, "color": (0.6, 0.6, 0.7), "direction": (-0.3, -1.0, -0.2), "shadows": False},
+    ]
+    faces = []
+    for f in range(6):
+        base = np.array([0.2 + 0.1 * f, 0.3, 0.5 - 0.05 * f], np.float32)
+        ramp = np.linspace(0.5, 1.5, 8, dtype=np.float32)[:, None, None]
+        faces.append(sc.add_texture(np.broadcast_to(base * ramp, (8, 8, 3)).copy()))
+    sc.background = {"mode": 2, "color": (0, 0, 0), "tex": tuple(faces)}
+    sc.camera = {"eye": (0.0, 1.2, 3.0), "center": (0.0, 0.4, 0.0), "up": (0.0, 1.0, 0.0), "fov": 1.1, "ratio": 1.0}
     return sc

@@ -6,6 +6,7 @@ inputs, and stores inputs and outputs as compressed .npz files. The fixtures are
 the reference tree is only needed to regenerate them:
 
     python tests/golden/make_golden.py            (needs the reference tree)
+    python tests/golden/make_golden.py --renders  (reference path-tracer renders)
 """
 from __future__ import annotations
 
@@ -159,9 +160,33 @@ def make_camera():
     print("camera.npz: 16 cameras")
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and "--renders" not in sys.argv:
     if O.build_ref() is None:
         sys.exit("the reference tree is needed to regenerate the fixtures")
     make_raycaster()
     make_material()
     make_camera()
+
+
+def make_renders():
+    """Renders of the reference's own PathTracer (two independent runs per scene: the
+    second calibrates the Monte-Carlo noise floor of a same-spp comparison)."""
+    out = {}
+    for name, sc, w, h, spp, depth in [
+        ("cornell", S.cornell_scene(SEED), 48, 48, 256, 5),
+        ("cornell_lit", S.cornell_scene(SEED, with_light=True), 48, 48, 256, 5),
+        ("mixed", S.feature_scene(SEED), 40, 40, 256, 4),
+    ]:
+        tr = O.RefPathTracer(sc)
+        a = tr.render(sc.camera, spp, depth, w, h, seed=SEED)
+        b = tr.render(sc.camera, spp, depth, w, h, seed=SEED + 1)
+        out[f"{name}_a"] = a
+        out[f"{name}_b"] = b
+        out[f"{name}_cfg"] = np.array([w, h, spp, depth], np.int32)
+        tr.close()
+    np.savez_compressed(os.path.join(HERE, "renders.npz"), **out)
+    print("renders.npz:", ", ".join(k for k in out if k.endswith("_a")))
+
+
+if __name__ == "__main__" and "--renders" in sys.argv:
+    make_renders()

@@ -1,0 +1,68 @@
+"""The C restatement of the path tracer (oracle/port/pt_port.c) against the reference's own
+code: material functions and camera set-up against golden vectors, whole renders against
+the reference's renders at equal spp (statistically: the reference's random streams are
+not reproducible)."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from render_stats import assert_same_distribution
+
+
+def test_port_material_matches_reference(port_lib):
+    O = port_lib
+    g = load_golden("material_ggx.npz")
+    ev = O.port_ggx_eval(g["eval_in"])
+    np.testing.assert_allclose(ev, g["eval_out"], rtol=2e-5, atol=1e-6)
+    sm = O.port_ggx_sample(g["sample_in"], g["sample_uniforms"])
+    close = np.isclose(sm, g["sample_out"], rtol=2e-4, atol=2e-5).all(axis=1)
+    # A uniform within an ulp of the lobe threshold may pick the other lobe.
+    assert close.mean() > 0.999, f"{(~close).sum()} of {len(close)} samples differ"
+
+
+def test_port_cosine_hemisphere_matches_reference(port_lib):
+    O = port_lib
+    g = load_golden("material_ggx.npz")
+    cos = g["cosine"]
+    # sampleAndEval's diffuse lobe = sampleCosineHemisphere; evaluate it through a case
+    # that always takes the diffuse lobe (metalness 0, lobe uniform 0.999999).
+    n = len(cos)
+    cases = np.zeros((n, 8), np.float32)
+    cases[:, 2] = 1.0  # wo = +z
+    cases[:, 3:6] = 0.5
+    cases[:, 6] = 1.0
+    uni = np.stack([np.full(n, 0.999999, np.float32), cos[:, 0], cos[:, 1]], 1)
+    out = O.port_ggx_sample(cases, uni)
+    np.testing.assert_allclose(out[:, 3:6], cos[:, 2:5], rtol=1e-5, atol=1e-6)
+
+
+def test_port_pixel_shifts_match_reference(port_lib):
+    O = port_lib
+    g = load_golden("camera.npz")
+    for cam, ref in zip(g["cameras"], g["shifts"]):
+        c = {"eye": cam[0:3], "center": cam[3:6], "up": cam[6:9], "fov": cam[9], "ratio": cam[10]}
+        np.testing.assert_allclose(O.port_pixel_shifts(c), ref, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("name", ["cornell", "cornell_lit", "mixed"])
+def test_port_render_matches_reference_statistically(port_lib, name):
+    from rendu_gb300 import scenes as S
+
+    g = load_golden("renders.npz")
+    w, h, spp, depth = (int(x) for x in g[f"{name}_cfg"])
+    sc = {"cornell": lambda: S.cornell_scene(20261203), "cornell_lit": lambda: S.cornell_scene(20261203, True),
+          "mixed": lambda: S.feature_scene(20261203)}[name]()
+    img = port_lib.PortPathTracer(sc).render(sc.camera, spp, depth, w, h, seed=5)
+    assert_same_distribution(img, g[f"{name}_a"], g[f"{name}_b"])
+
+
+def test_port_render_is_deterministic_and_thread_independent(port_lib):
+    from rendu_gb300 import scenes as S
+
+    sc = S.feature_scene(3)
+    tr = port_lib.PortPathTracer(sc)
+    a = tr.render(sc.camera, 8, 4, 24, 20, seed=11, threads=1)
+    b = tr.render(sc.camera, 8, 4, 24, 20, seed=11, threads=5)
+    c = tr.render(sc.camera, 8, 4, 24, 20, seed=12, threads=5)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, c)

@@ -29,7 +29,10 @@ def _port_from_meshes(O, meshes):
 
 def _assert_closest_equal(h, ref_prim, ref_t, ref_u, ref_v, rays, port):
     """t bit-exact everywhere; ids equal unless both triangles give the same t."""
-    assert np.array_equal(h["t"].view(np.uint32), ref_t.view(np.uint32))
+    bad = np.nonzero(h["t"].view(np.uint32) != ref_t.view(np.uint32))[0]
+    assert len(bad) == 0, (f"{len(bad)} distances differ, e.g. rays {bad[:5].tolist()}: gpu t/prim "
+                           f"{h['t'][bad[:5]].tolist()} {h['prim'][bad[:5]].tolist()} vs "
+                           f"{ref_t[bad[:5]].tolist()} {ref_prim[bad[:5]].tolist()}")
     diff = np.nonzero(h["prim"] != ref_prim)[0]
     for i in diff:
         r_a, a = port.test_triangle(rays[i], h["prim"][i])
