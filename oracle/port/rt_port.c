@@ -268,7 +268,7 @@ static void nth_element_axis(tri_info *a, size_t n, size_t k, int axis) {
 int port_rc_build(port_rc *rc) {
     if (!rc) return -1;
     typedef struct { uint64_t id, begin, count; } set_info;
-    size_t scap = 64, ssz = 0;
+    size_t scap = 64 + (size_t)rc->mesh_count, ssz = 0;
     set_info *stack = (set_info *)malloc(scap * sizeof(set_info));
     if (!stack) return -2;
     /* Reset any previous hierarchy: keep only the mesh roots (addMesh stored begin/count). */

@@ -26,6 +26,11 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
+# Per-unit flags. The shading unit follows the reference's float rounding (no FMA
+# contraction of separate multiplies and adds; explicit fmaf calls are kept).
+UNIT_FLAGS = {"pt_kernels.cu": ["-fmad=false"]}
+
+
 def nvcc() -> str:
     for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and os.path.exists(cand):
@@ -43,7 +48,8 @@ def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src).replace(".cu", ".o"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _headers_mtime()):
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, f"-I{INCLUDE}", f"-I{CSRC}", "-c", src, "-o", obj]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *UNIT_FLAGS.get(os.path.basename(src), []), f"-I{INCLUDE}", f"-I{CSRC}", "-c",
+           src, "-o", obj]
     if verbose:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

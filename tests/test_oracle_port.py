@@ -95,3 +95,26 @@ def test_port_matches_compiled_reference_on_fresh_inputs(port_lib):
     assert np.array_equal(hp["prim"], hr["prim"])
     assert np.array_equal(hp["t"].view(np.uint32), hr["t"].view(np.uint32))
     assert np.array_equal(p.intersect_any(rays), r.intersect_any(rays))
+
+
+def test_port_many_meshes_match_reference(port_lib):
+    """200 transformed instances: one root per mesh in both (Raycaster.cpp:64-69)."""
+    O = port_lib
+    if O.build_ref() is None:
+        pytest.skip("reference tree not present")
+    from rendu_gb300 import scenes as S
+
+    rng = np.random.default_rng(8)
+    sph, box = S.icosphere_mesh(2, seed=4), S.box_mesh()
+    p, r = O.PortRaycaster(), O.RefRaycaster()
+    for k in range(200):
+        m = S.translation(rng.uniform(-10, 10, 3)) @ S.rotation_y(rng.uniform(0, 6.28)) @ S.scaling(rng.uniform(0.3, 1.5))
+        src = sph if k % 2 else box
+        for x in (p, r):
+            x.add_mesh(src.positions, src.indices, m)
+    p.build()
+    r.build()
+    rays = S.random_rays(50000, (-11, -11, -11), (11, 11, 11), seed=9, scale=1.0)
+    hp, hr = p.intersect(rays), r.intersect(rays)
+    assert np.array_equal(hp["prim"], hr["prim"])
+    assert np.array_equal(hp["t"].view(np.uint32), hr["t"].view(np.uint32))
