@@ -13,10 +13,11 @@
  *  - Every call returns an int status (RT_OK == 0). The reference reports errors with
  *    log lines and early returns (PathTracer.cpp:162-168); here they are status codes,
  *    and rt_last_error() gives the message of the calling thread's last failure.
- *  - Host pointers are the default: the library copies inputs in and results out, and
- *    the call returns when the results are in host memory. With RT_FLAG_DEVICE_PTRS the
- *    ray/hit/image pointers are CUDA device pointers; the call is then asynchronous on
- *    `stream` (a cudaStream_t passed as void*, NULL = the context's own stream).
+ *  - Host pointers are the default: the library copies inputs in and results out on its
+ *    own stream, and the call returns when the results are in host memory. With
+ *    RT_FLAG_DEVICE_PTRS the ray/hit/image pointers are CUDA device pointers and the work
+ *    is ordered on `stream` (a cudaStream_t passed as void*; NULL is the CUDA default
+ *    stream, as everywhere in CUDA); rt_* queries then return without waiting.
  *  - Matrices are 4x4 column-major float[16] (glm layout), NULL meaning identity.
  *  - A context is bound to the CUDA device given at creation. Calls on one context must
  *    not overlap from several host threads.

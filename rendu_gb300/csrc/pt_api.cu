@@ -402,7 +402,7 @@ int pt_render(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, uint3
     if (samples == 0) return arg_error("samples must be at least 1");
     if ((uint64_t)width * height >= (1ull << 31)) return arg_error("image too large");
     DeviceGuard g(s->device);
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : s->rc->stream;
+    cudaStream_t st = (flags & RT_FLAG_DEVICE_PTRS) ? static_cast<cudaStream_t>(stream) : s->rc->stream;
 
     // Power-of-two sample count and stratification grid (PathTracer.cpp:169-178, 57-69).
     const uint32_t spp = (uint32_t)std::pow(2.0, std::round(std::log2((float)samples)));

@@ -86,26 +86,34 @@ int require_built(rt_ctx *ctx) {
     return RT_OK;
 }
 
-// Runs `fn(d_in, count, d_out, stream)` over host buffers in chunks: copy in, compute,
-// copy out, all on the context stream (device allocations grow once and are reused).
+// Runs `fn(d_in, count, d_out, stream)` over host buffers in chunks of 2M records that
+// alternate between two streams with their own staging buffers: the copy-in of chunk k+1,
+// the kernel of chunk k and the copy-out of chunk k-1 overlap (separate copy engines for
+// each direction). Pinned host buffers get asynchronous DMA; pageable ones still work but
+// their copies do not overlap.
 template <class Fn>
 int host_chunked(rt_ctx *ctx, const void *h_in, size_t in_stride, size_t n, void *h_out, size_t out_stride, Fn fn) {
-    const size_t chunk = size_t(1) << 22;
+    const size_t chunk = size_t(1) << 21;
     const size_t cn = n < chunk ? n : chunk;
-    if (ctx->d_rays.reserve(cn * in_stride) != RT_OK) return RT_ERR_OOM;
-    if (ctx->d_out.reserve(cn * out_stride) != RT_OK) return RT_ERR_OOM;
-    cudaStream_t st = ctx->stream;
-    for (size_t s = 0; s < n; s += chunk) {
+    DevBuf *in[2] = {&ctx->d_rays, &ctx->d_rays2};
+    DevBuf *out[2] = {&ctx->d_out, &ctx->d_out3};
+    for (int k = 0; k < 2; ++k)
+        if (in[k]->reserve(cn * in_stride) != RT_OK || out[k]->reserve(cn * out_stride) != RT_OK) return RT_ERR_OOM;
+    cudaStream_t st[2] = {ctx->stream, ctx->stream2};
+    size_t idx = 0;
+    for (size_t s = 0; s < n; s += chunk, ++idx) {
+        const int b = (int)(idx & 1);
         const size_t m = (n - s) < chunk ? (n - s) : chunk;
-        RT_CUDA_TRY(cudaMemcpyAsync(ctx->d_rays.ptr, static_cast<const char *>(h_in) + s * in_stride, m * in_stride,
-                                    cudaMemcpyHostToDevice, st));
-        const int r = fn(ctx->d_rays.ptr, m, ctx->d_out.ptr, st);
+        RT_CUDA_TRY(cudaMemcpyAsync(in[b]->ptr, static_cast<const char *>(h_in) + s * in_stride, m * in_stride,
+                                    cudaMemcpyHostToDevice, st[b]));
+        const int r = fn(in[b]->ptr, m, out[b]->ptr, st[b]);
         if (r != RT_OK) return r;
-        RT_CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(h_out) + s * out_stride, ctx->d_out.ptr, m * out_stride,
-                                    cudaMemcpyDeviceToHost, st));
+        RT_CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(h_out) + s * out_stride, out[b]->ptr, m * out_stride,
+                                    cudaMemcpyDeviceToHost, st[b]));
     }
-    RT_CUDA_TRY(cudaStreamSynchronize(st));
-    return check_status(ctx, st);
+    RT_CUDA_TRY(cudaStreamSynchronize(st[1]));
+    RT_CUDA_TRY(cudaStreamSynchronize(st[0]));
+    return check_status(ctx, st[0]);
 }
 
 }  // namespace
@@ -131,6 +139,7 @@ int rt_create(rt_ctx **out, int device) {
     rt_ctx *ctx = new rt_ctx();
     ctx->device = device;
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&ctx->ev_a) != cudaSuccess || cudaEventCreate(&ctx->ev_b) != cudaSuccess) {
         set_error(std::string("stream/event creation failed: ") + cudaGetErrorString(cudaGetLastError()));
         delete ctx;
@@ -156,6 +165,12 @@ int rt_destroy(rt_ctx *ctx) {
     ctx->d_rays.release();
     ctx->d_out.release();
     ctx->d_out2.release();
+    ctx->d_rays2.release();
+    ctx->d_out3.release();
+    if (ctx->stream2) {
+        cudaStreamSynchronize(ctx->stream2);
+        cudaStreamDestroy(ctx->stream2);
+    }
     if (ctx->ev_a) cudaEventDestroy(ctx->ev_a);
     if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -237,7 +252,7 @@ int rt_intersect(rt_ctx *ctx, const rt_ray *rays, size_t n, rt_hit *hits, void *
     }
     DeviceGuard g(ctx->device);
     if (flags & RT_FLAG_DEVICE_PTRS) {
-        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
         return trace_closest(ctx, rays, n, hits, st);
     }
     return host_chunked(ctx, rays, sizeof(rt_ray), n, hits, sizeof(rt_hit),
@@ -256,7 +271,7 @@ int rt_intersect_any(rt_ctx *ctx, const rt_ray *rays, size_t n, uint8_t *occlude
     }
     DeviceGuard g(ctx->device);
     if (flags & RT_FLAG_DEVICE_PTRS) {
-        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
         return trace_any(ctx, rays, n, occluded, st);
     }
     return host_chunked(ctx, rays, sizeof(rt_ray), n, occluded, 1,
@@ -274,19 +289,21 @@ int rt_visible(rt_ctx *ctx, const float *segs, size_t n, uint8_t *visible, void 
         return RT_ERR_ARG;
     }
     DeviceGuard g(ctx->device);
-    auto run = [ctx](const float *d_segs, size_t m, uint8_t *d_vis, cudaStream_t st) -> int {
-        if (ctx->d_out2.reserve(m * sizeof(rt_ray)) != RT_OK) return RT_ERR_OOM;
-        rt_ray *d_r = ctx->d_out2.as<rt_ray>();
+    // Scratch rays: one region per stream of the pipelined host path (reserved up front,
+    // never reallocated while work is in flight).
+    const size_t chunk = size_t(1) << 21;
+    const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
+    const size_t region = dev ? n : (n < chunk ? n : chunk);
+    if (ctx->d_out2.reserve((dev ? 1 : 2) * region * sizeof(rt_ray) + 16) != RT_OK) return RT_ERR_OOM;
+    auto run = [ctx, region](const float *d_segs, size_t m, uint8_t *d_vis, cudaStream_t st) -> int {
+        rt_ray *d_r = ctx->d_out2.as<rt_ray>() + (st == ctx->stream2 ? region : 0);
         int rr = segments_to_rays(d_segs, m, d_r, st);
         if (rr != RT_OK) return rr;
         rr = trace_any(ctx, d_r, m, d_vis, st);
         if (rr != RT_OK) return rr;
         return invert_bytes(d_vis, m, st);
     };
-    if (flags & RT_FLAG_DEVICE_PTRS) {
-        cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-        return run(segs, n, visible, st);
-    }
+    if (dev) return run(segs, n, visible, static_cast<cudaStream_t>(stream));
     return host_chunked(ctx, segs, 6 * sizeof(float), n, visible, 1,
                         [run](void *in, size_t m, void *out, cudaStream_t st) {
                             return run(static_cast<const float *>(in), m, static_cast<uint8_t *>(out), st);
@@ -303,11 +320,12 @@ int rt_count_visits(rt_ctx *ctx, const rt_ray *rays, size_t n, uint32_t *node_vi
         return RT_ERR_ARG;
     }
     DeviceGuard g(ctx->device);
-    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
     if (flags & RT_FLAG_DEVICE_PTRS) {
         if (ctx->d_out2.reserve(n * sizeof(rt_hit)) != RT_OK) return RT_ERR_OOM;
-        return trace_count(ctx, rays, n, node_visits, tri_visits, ctx->d_out2.as<rt_hit>(), st);
+        return trace_count(ctx, rays, n, node_visits, tri_visits, ctx->d_out2.as<rt_hit>(),
+                           static_cast<cudaStream_t>(stream));
     }
+    cudaStream_t st = ctx->stream;
     DevBuf dr, dn, dt, dh;
     if (dr.reserve(n * sizeof(rt_ray)) || dn.reserve(n * 4) || dt.reserve(n * 4) || dh.reserve(n * sizeof(rt_hit))) {
         dr.release(); dn.release(); dt.release(); dh.release();

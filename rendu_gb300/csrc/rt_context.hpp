@@ -39,7 +39,8 @@ struct MeshRecord {
 
 struct rt_ctx {
     int device = 0;
-    cudaStream_t stream = nullptr;  // the context's own stream
+    cudaStream_t stream = nullptr;   // the context's own stream
+    cudaStream_t stream2 = nullptr;  // second stream of the pipelined host-buffer path
     // Host copies appended by rt_add_mesh (raw positions; indices already offset).
     std::vector<float> h_positions;
     std::vector<uint32_t> h_indices;
@@ -64,6 +65,8 @@ struct rt_ctx {
     rgb::DevBuf d_rays;
     rgb::DevBuf d_out;
     rgb::DevBuf d_out2;
+    rgb::DevBuf d_rays2;
+    rgb::DevBuf d_out3;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
 };
 
