@@ -20,7 +20,8 @@
  *    stream, as everywhere in CUDA); rt_* queries then return without waiting.
  *  - Matrices are 4x4 column-major float[16] (glm layout), NULL meaning identity.
  *  - A context is bound to the CUDA device given at creation. Calls on one context must
- *    not overlap from several host threads.
+ *    not overlap from several host threads, and device-pointer queries on one context
+ *    must be ordered on one stream.
  */
 #ifndef RENDU_GB300_H
 #define RENDU_GB300_H

@@ -145,11 +145,12 @@ int rt_create(rt_ctx **out, int device) {
         delete ctx;
         return RT_ERR_CUDA;
     }
-    if (ctx->d_status.reserve(16) != RT_OK) {
+    // Status word at offset 0, three traversal fetch counters at offsets 8, 16, 24.
+    if (ctx->d_status.reserve(64) != RT_OK) {
         delete ctx;
         return RT_ERR_OOM;
     }
-    cudaMemset(ctx->d_status.ptr, 0, 16);
+    cudaMemset(ctx->d_status.ptr, 0, 64);
     *out = ctx;
     return RT_OK;
 }

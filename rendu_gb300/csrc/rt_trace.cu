@@ -38,6 +38,64 @@ __global__ void __launch_bounds__(128) k_trace(const BvhNode *__restrict__ nodes
     }
 }
 
+// Persistent variant: a grid sized to fill the GPU once; lanes refill from `counter`
+// (zeroed before the launch). n is read from n_dev when given (device-side queue length).
+template <bool ANY, int STACK>
+__global__ void __launch_bounds__(128) k_trace_persistent(const BvhNode *__restrict__ nodes,
+                                                          const BvhTri *__restrict__ tris,
+                                                          const rt_ray *__restrict__ rays, size_t n_host,
+                                                          const uint32_t *__restrict__ n_dev, rt_hit *__restrict__ hits,
+                                                          uint8_t *__restrict__ occ, unsigned *__restrict__ status,
+                                                          unsigned long long *__restrict__ counter) {
+    const size_t n = n_dev ? (size_t)*n_dev : n_host;
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    int stack_node[STACK];
+    float stack_near[STACK];
+    RayState r;
+    TravState t;
+    size_t idx = 0;
+    bool active = false, exhausted = false;
+    while (true) {
+        const unsigned need = __ballot_sync(0xffffffffu, !active);
+        if (need && !exhausted) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if ((int)lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base + __popc(need) >= n) exhausted = true;
+            if (!active) {
+                idx = (size_t)base + __popc(need & lt_mask);
+                if (idx < n) {
+                    const float4 *rp = reinterpret_cast<const float4 *>(rays + idx);
+                    r = make_ray_state(__ldcs(rp), __ldcs(rp + 1));
+                    trav_init(t, r);
+                    active = r.valid;
+                    if (!active) {  // never hits: write the miss now
+                        if (ANY) occ[idx] = 0;
+                        else __stcs(reinterpret_cast<float4 *>(hits + idx),
+                                    make_float4(FLT_MAX, 0.0f, 0.0f, __uint_as_float(RT_NO_HIT)));
+                    }
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (active && trav_step<ANY, STACK>(nodes, tris, r, t, stack_node, stack_near, status)) {
+            active = false;
+            if (ANY) {
+                occ[idx] = t.res.found ? 1 : 0;
+            } else {
+                __stcs(reinterpret_cast<float4 *>(hits + idx),
+                       make_float4(t.res.found ? t.res.t : FLT_MAX, t.res.u, t.res.v,
+                                   __uint_as_float(t.res.found ? t.res.prim : RT_NO_HIT)));
+            }
+        }
+    }
+}
+
 // Raycaster::visible (Raycaster.cpp:226-230): window (1e-4, |p1 - p0|) along p1 - p0.
 __global__ void k_segments_to_rays(const float *__restrict__ segs, size_t n, rt_ray *__restrict__ rays) {
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -54,10 +112,37 @@ __global__ void k_invert(uint8_t *__restrict__ v, size_t n) {
     if (i < n) v[i] = v[i] ? 0 : 1;
 }
 
+template <bool ANY, int STACK>
+int launch_persistent(rt_ctx *ctx, const rt_ray *rays, size_t n, const uint32_t *n_dev, rt_hit *hits, uint8_t *occ,
+                      cudaStream_t st) {
+    static int grid[2][2] = {{0, 0}, {0, 0}};
+    int &g = grid[ANY ? 1 : 0][STACK == 64 ? 0 : 1];
+    if (g == 0) {
+        int per_sm = 0, sms = 0, dev = 0;
+        RT_CUDA_TRY(cudaGetDevice(&dev));
+        RT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        RT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_persistent<ANY, STACK>, 128, 0));
+        g = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    // One fetch counter per stream the context launches on: the caller's stream and the two
+    // streams of the pipelined host path may run traversals concurrently.
+    const int slot = st == ctx->stream ? 1 : (st == ctx->stream2 ? 2 : 0);
+    unsigned long long *counter = reinterpret_cast<unsigned long long *>(ctx->d_status.as<char>() + 8 + 8 * slot);
+    RT_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
+    k_trace_persistent<ANY, STACK><<<g, 128, 0, st>>>(ctx->d_nodes.as<BvhNode>(), ctx->d_tris.as<BvhTri>(), rays, n,
+                                                      n_dev, hits, occ, ctx->d_status.as<unsigned>(), counter);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
 template <bool ANY, bool COUNT>
 int launch(rt_ctx *ctx, const rt_ray *rays, size_t n, rt_hit *hits, uint8_t *occ, uint32_t *nc, uint32_t *tc,
            cudaStream_t st) {
     if (n == 0) return RT_OK;
+    if (!COUNT && ctx->n_tris > 0) {
+        if (ctx->depth <= 64) return launch_persistent<ANY, 64>(ctx, rays, n, nullptr, hits, occ, st);
+        return launch_persistent<ANY, 256>(ctx, rays, n, nullptr, hits, occ, st);
+    }
     const unsigned blocks = (unsigned)((n + 127) / 128);
     const BvhNode *nodes = ctx->d_nodes.as<BvhNode>();
     const BvhTri *tris = ctx->d_tris.as<BvhTri>();

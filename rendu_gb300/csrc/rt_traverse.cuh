@@ -185,4 +185,103 @@ __device__ __forceinline__ TraceResult traverse(const BvhNode *__restrict__ node
     return res;
 }
 
+// ---- persistent traversal with per-lane ray refill ---------------------------------------
+// One iteration = one node visit (two child box tests, leaf triangles of entered children,
+// push/pop). A lane whose ray has finished takes the next unclaimed ray at the start of
+// the following iteration (one atomic per warp per refill), so rays that stop at the root
+// and rays that descend deep share warps without idling lanes.
+struct TravState {
+    int node, sp;
+    float cur_max;
+    TraceResult res;
+};
+
+__device__ __forceinline__ void trav_init(TravState &t, const RayState &r) {
+    t.node = 0;
+    t.sp = 0;
+    t.cur_max = r.tmax;
+    t.res.t = FLT_MAX;
+    t.res.u = 0.0f;
+    t.res.v = 0.0f;
+    t.res.prim = RT_NO_HIT;
+    t.res.found = false;
+}
+
+// Returns true when the ray is finished.
+template <bool ANY, int STACK>
+__device__ __forceinline__ bool trav_step(const BvhNode *__restrict__ nodes, const BvhTri *__restrict__ tris,
+                                          const RayState &r, TravState &t, int *stack_node, float *stack_near,
+                                          unsigned *__restrict__ status) {
+    const float4 *np = reinterpret_cast<const float4 *>(nodes + t.node);
+    const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
+    const int4 d = __ldg(reinterpret_cast<const int4 *>(np + 3));
+    float t0 = slab(r, a.x, a.y, a.z, a.w, c.x, c.y, r.tmin, t.cur_max);
+    float t1 = d.y >= 0 ? slab(r, b.x, b.y, b.z, b.w, c.z, c.w, r.tmin, t.cur_max) : INFINITY;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        const float ts = s ? t1 : t0;
+        const int cnt = s ? d.w : d.z;
+        if (cnt == 0 || ts == INFINITY) continue;
+        const int first = s ? d.y : d.x;
+        for (int k = 0; k < cnt; ++k) {
+            const float4 *tp = reinterpret_cast<const float4 *>(tris + first + k);
+            const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
+            float tt, u, v;
+            if (!mt_exact(r, v0, e1, e2, tt, u, v)) continue;
+            if (!(tt > r.tmin)) continue;
+            const uint32_t prim = __float_as_uint(v0.w);
+            if (ANY) {
+                if (tt < t.cur_max) {
+                    t.res.found = true;
+                    t.res.t = tt;
+                    t.res.u = u;
+                    t.res.v = v;
+                    t.res.prim = prim;
+                    return true;
+                }
+                continue;
+            }
+            if (tt < t.cur_max || (t.res.found && tt == t.cur_max && prim < t.res.prim)) {
+                t.res.found = true;
+                t.res.t = tt;
+                t.res.u = u;
+                t.res.v = v;
+                t.res.prim = prim;
+                t.cur_max = tt;
+            }
+        }
+        if (s) t1 = INFINITY;
+        else t0 = INFINITY;
+    }
+    const bool h0 = t0 <= t.cur_max, h1 = t1 <= t.cur_max;
+    if (h0 && h1) {
+        const bool first0 = t0 <= t1;
+        if (t.sp >= STACK) {
+            atomicOr(status, RT_DEV_STACK_OVERFLOW);
+            return true;
+        }
+        stack_node[t.sp] = first0 ? d.y : d.x;
+        stack_near[t.sp] = first0 ? t1 : t0;
+        ++t.sp;
+        t.node = first0 ? d.x : d.y;
+        return false;
+    }
+    if (h0) {
+        t.node = d.x;
+        return false;
+    }
+    if (h1) {
+        t.node = d.y;
+        return false;
+    }
+    while (t.sp > 0) {
+        --t.sp;
+        if (stack_near[t.sp] <= t.cur_max) {
+            t.node = stack_node[t.sp];
+            return false;
+        }
+    }
+    return true;
+}
+
 }  // namespace rgb
