@@ -121,6 +121,23 @@ RT_API int rt_intersect_any(rt_ctx *ctx, const rt_ray *rays, size_t n, uint8_t *
  * (Raycaster.cpp:226-230): window (1e-4, |p1 - p0|). */
 RT_API int rt_visible(rt_ctx *ctx, const float *segs, size_t n, uint8_t *visible, void *stream, uint32_t flags);
 
+/* Largest batch rt_visible_noalloc accepts. */
+#define RT_NOALLOC_MAX_SEGMENTS 262144
+
+/* rt_visible for callers that cannot allocate device memory (cudaMalloc forbidden or too
+ * slow where they run: fixed-budget frame loops and callbacks, plugin hosts that own every
+ * allocation, code that must avoid the implicit synchronisation of cudaMalloc/cudaFree).
+ * No counterpart in the reference (its Raycaster::visible is a single CPU query).
+ * segs (n x 6 floats) and visible (n bytes) are DEVICE pointers; the work is ordered on
+ * `stream` (NULL = CUDA default stream) and the call returns without waiting. The call
+ * allocates nothing: its scratch (converted rays, fetch counter, status word) is one
+ * static device array of 8 MiB + 256 B that every GPU loading the library holds until
+ * exit, so n must not exceed RT_NOALLOC_MAX_SEGMENTS (RT_ERR_ARG otherwise). All calls
+ * share that array: calls that overlap on the GPU race and must be serialised by the
+ * caller. The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, once per device); make it before any stream capture. */
+RT_API int rt_visible_noalloc(rt_ctx *ctx, const float *segs, size_t n, uint8_t *visible, void *stream);
+
 /* Map a global triangle id to (meshId, localId) as stored in Raycaster::Hit. */
 RT_API int rt_prim_info(const rt_ctx *ctx, uint32_t prim, uint32_t *mesh_id, uint32_t *local_id);
 
