@@ -18,6 +18,10 @@ beside it.
                tested, visit counts measured on a 1M-ray sample of the same set.
 * cpu_baseline -- the C restatement of the reference Raycaster (oracle/port), reference
                threading (hardware threads - 1), on a bounded sample of the same rays.
+* pathtracer -- the path tracer on the small (Cornell room, 256x256, 16 spp, depth 5) and
+               large (200 instances, ~2M triangles, 1920x1080, 64 spp, depth 8) scenes:
+               Mrays/s counting primary, bounce and shadow rays, device time inside
+               pt_render, beside the C restatement of PathTracer::render on host cores.
 * --impl reference -- only that CPU path, as the reference arm.
 Under torchrun (N > 1) every rank traces its own 16M rays (weak scaling, no collective on
 the data path); value = all rays / max-over-ranks time.
@@ -155,6 +159,70 @@ def cpu_raycaster_rate(mesh, rays, target_s: float, threads: int):
     return m / dt / 1e6, m, build_s
 
 
+PT_CONFIGS = {
+    # name: (scene factory, width, height, spp, depth, cpu spp)
+    "cornell_256": ("cornell", 256, 256, 16, 5, 16),
+    "instanced_1080p": ("instanced", 1920, 1080, 64, 8, 1),
+}
+
+
+def _pt_scene(kind):
+    from rendu_gb300 import scenes as S
+
+    return S.cornell_scene(20261204) if kind == "cornell" else S.instanced_scene(20261206)
+
+
+def run_pathtracer(name, steps, cpu: bool):
+    """One path-tracer configuration: GPU Mrays/s (device time inside pt_render), e2e with a
+    host image, and the C restatement on host cores at `cpu spp` (cost is linear in spp)."""
+    import torch
+
+    import rendu_gb300 as R
+
+    kind, w, h, spp, depth, cpu_spp = PT_CONFIGS[name]
+    sc = _pt_scene(kind)
+    cam = dict(sc.camera, ratio=w / h)
+    t0 = time.perf_counter()
+    tr = R.PathTracer(sc)
+    commit_s = time.perf_counter() - t0
+    img = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
+    tr.render(cam, spp, depth, img, seed=1)  # warm-up
+    rays, dev_ms = 0, 0.0
+    for k in range(steps):
+        img.zero_()
+        tr.render(cam, spp, depth, img, seed=2 + k)
+        st = tr.last_stats()
+        rays += st["rays"]
+        dev_ms += st["device_ms"]
+    host = np.zeros((h, w, 3), np.float32)
+    t0 = time.perf_counter()
+    tr.render(cam, spp, depth, host, seed=99)
+    e2e_s = time.perf_counter() - t0
+    e2e_rays = tr.last_stats()["rays"]
+    out = {"workload": f"{kind}: {sc.triangle_count} triangles, {len(sc.objects)} objects, {w}x{h}, {spp} spp, "
+                       f"depth {depth}",
+           "value": round(rays / (dev_ms * 1e3), 1), "unit": "Mrays/s", "ms_per_render": round(dev_ms / steps, 2),
+           "rays_per_render": rays // steps, "e2e": {"value": round(e2e_rays / e2e_s / 1e6, 1), "unit": "Mrays/s",
+                                                      "s_per_render": round(e2e_s, 3)},
+           "scene_upload_and_build_s": round(commit_s, 2)}
+    if cpu:
+        from oracle import oracle as O
+
+        O.build_port()
+        threads = max((os.cpu_count() or 2) - 1, 1)
+        port = O.PortPathTracer(sc)
+        t0 = time.perf_counter()
+        port.render(cam, cpu_spp, depth, w, h, seed=1, threads=threads)
+        dt = time.perf_counter() - t0
+        cpu_rays = int(port.rays.sum())
+        cpu_rate = cpu_rays / dt / 1e6
+        out["cpu_baseline"] = {"value": round(cpu_rate, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                               "sample": f"full image at {cpu_spp} spp (cost linear in spp)",
+                               "render_s_at_full_spp": round(dt * spp / cpu_spp, 1)}
+        out["speedup_vs_cpu"] = round(out["value"] / cpu_rate, 1)
+    return out
+
+
 def run_reference(args):
     """Reference arm: the reference's Raycaster algorithm (C restatement; the reference's own
     sources do not travel to this host) on all host threads, same workload and metric."""
@@ -208,6 +276,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-pt", action="store_true", help="skip the path-tracer lines")
     ap.add_argument("--profile-run", action="store_true",
                     help="only one closest-hit and one any-hit launch over the workload (for ncu captures)")
     args = ap.parse_args()
@@ -324,6 +393,8 @@ def main():
             "bvh": {"build_ms": round(st["build_ms"], 2), "nodes": st["nodes"], "leaves": st["leaves"],
                     "sah_cost": round(st["sah_cost"], 2), "device_mb": round(st["device_bytes"] / 2**20, 1)},
         }
+        if not args.no_pt:
+            out["pathtracer"] = {name: run_pathtracer(name, 3, not args.no_cpu) for name in PT_CONFIGS}
         if not args.no_cpu:
             threads = max((os.cpu_count() or 2) - 1, 1)
             rate, m, build_s = cpu_raycaster_rate(mesh, rays, args.cpu_seconds, threads)

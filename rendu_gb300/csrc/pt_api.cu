@@ -481,7 +481,7 @@ int pt_render(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, uint3
         r = pt_launch_raygen(f, w, st);
         int cur = 0;
         for (uint32_t did = 0; r == RT_OK && did < depth; ++did) {
-            r = pt_launch_trace(s->dev, w, cur, cap, did == 0 ? 0 : 1, st);
+            r = pt_launch_trace(s->rc, w, cur, cap, st);
             if (r != RT_OK) break;
             if (cudaMemsetAsync(&w.counters[cur ^ 1], 0, 4, st) != cudaSuccess ||
                 cudaMemsetAsync(&w.counters[2], 0, 4, st) != cudaSuccess) {

@@ -3,7 +3,8 @@
 //
 // One wave = every pixel x a run of S consecutive sample indices (P = W*H*S paths).
 // Per bounce:
-//   trace  -- closest hit for the compacted ray queue (rt_traverse.cuh);
+//   trace  -- closest hit for the compacted ray queue (the persistent traversal of
+//             rt_trace.cu, queue length read on the device);
 //   shade  -- the reference's hit logic (background on miss, alpha cut-out, emission,
 //             local frame, NEE light pick + evaluation, BSDF sampling), appending
 //             continuing paths to the next queue and shadow rays to the shadow queue with
@@ -55,26 +56,6 @@ __global__ void k_raygen(PtFrame f, PtWave w) {
     w.ndc[p] = make_float2(nx, ny);
 }
 
-template <int STACK>
-__global__ void __launch_bounds__(128) k_trace_queue(PtScene s, const rt_ray *__restrict__ q,
-                                                     const uint32_t *__restrict__ count, rt_hit *__restrict__ hits,
-                                                     unsigned long long *stats, int stat_slot) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = *count;
-    if (i == 0) atomicAdd(&stats[stat_slot], (unsigned long long)n);
-    if (i >= n) return;
-    const float4 *rp = reinterpret_cast<const float4 *>(q + i);
-    const RayState r = make_ray_state(rp[0], rp[1]);
-    TraceResult res;
-    res.found = false;
-    res.t = FLT_MAX;
-    res.u = res.v = 0.0f;
-    res.prim = RT_NO_HIT;
-    uint32_t a = 0, b = 0;
-    if (r.valid && !s.empty) res = traverse<false, false, STACK>(s.nodes, s.tris, r, s.status, a, b);
-    hits[i] = rt_hit{res.t, res.u, res.v, res.found ? res.prim : RT_NO_HIT};
-}
-
 struct SurfaceHit {
     int obj;
     uint32_t i0, i1, i2;  // global vertex indices into the attribute pools
@@ -112,6 +93,7 @@ __device__ __forceinline__ float2 interp_uv(const float *a, const SurfaceHit &h)
 __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, int cur, uint32_t did) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = w.counters[cur];
+    if (i == 0) atomicAdd(&w.stats[did == 0 ? 0 : 1], (unsigned long long)n);  // rays traced this bounce
     if (i >= n) return;
     const int nxt = cur ^ 1;
     const uint32_t path = w.qpath[cur][i];
@@ -345,14 +327,8 @@ int pt_launch_raygen(const PtFrame &f, const PtWave &w, cudaStream_t st) {
     return RT_OK;
 }
 
-int pt_launch_trace(const PtScene &s, const PtWave &w, int cur, uint32_t cap, int stat_slot, cudaStream_t st) {
-    const unsigned blocks = (cap + 127) / 128;
-    if (s.big_stack)
-        k_trace_queue<256><<<blocks, 128, 0, st>>>(s, w.qray[cur], &w.counters[cur], w.hits, w.stats, stat_slot);
-    else
-        k_trace_queue<64><<<blocks, 128, 0, st>>>(s, w.qray[cur], &w.counters[cur], w.hits, w.stats, stat_slot);
-    RT_CUDA_TRY(cudaGetLastError());
-    return RT_OK;
+int pt_launch_trace(rt_ctx *rc, const PtWave &w, int cur, uint32_t cap, cudaStream_t st) {
+    return trace_closest_queue(rc, w.qray[cur], &w.counters[cur], cap, w.hits, st);
 }
 
 int pt_launch_shade(const PtScene &s, const PtFrame &f, const PtWave &w, int cur, uint32_t did, uint32_t cap,

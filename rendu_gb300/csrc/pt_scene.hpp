@@ -48,7 +48,7 @@ struct HostObject {
 
 int pt_launch_material(const float *cases, const float *uniforms, uint32_t n, float *out, cudaStream_t st);
 int pt_launch_raygen(const PtFrame &f, const PtWave &w, cudaStream_t st);
-int pt_launch_trace(const PtScene &s, const PtWave &w, int cur, uint32_t cap, int stat_slot, cudaStream_t st);
+int pt_launch_trace(rt_ctx *rc, const PtWave &w, int cur, uint32_t cap, cudaStream_t st);
 int pt_launch_shade(const PtScene &s, const PtFrame &f, const PtWave &w, int cur, uint32_t did, uint32_t cap,
                     cudaStream_t st);
 int pt_launch_shadow(const PtScene &s, const PtWave &w, uint32_t cap, cudaStream_t st);

@@ -74,6 +74,9 @@ namespace rgb {
 // Launchers used across units (all asynchronous on `stream`).
 int trace_closest(rt_ctx *ctx, const rt_ray *d_rays, size_t n, rt_hit *d_hits, cudaStream_t stream);
 int trace_any(rt_ctx *ctx, const rt_ray *d_rays, size_t n, uint8_t *d_occ, cudaStream_t stream);
+// Closest hit for a device-side queue: the length is read from d_count (at most cap).
+int trace_closest_queue(rt_ctx *ctx, const rt_ray *d_rays, const uint32_t *d_count, uint32_t cap, rt_hit *d_hits,
+                        cudaStream_t stream);
 int check_status(rt_ctx *ctx, cudaStream_t stream);  // reads and clears the device status word
 }  // namespace rgb
 

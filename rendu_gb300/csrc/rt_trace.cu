@@ -171,6 +171,25 @@ int trace_count(rt_ctx *ctx, const rt_ray *d_rays, size_t n, uint32_t *nc, uint3
     return launch<false, true>(ctx, d_rays, n, scratch, nullptr, nc, tc, st);
 }
 
+namespace {
+__global__ void k_fill_miss(const uint32_t *__restrict__ count, rt_hit *__restrict__ hits, uint32_t cap) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < cap && i < *count) hits[i] = rt_hit{FLT_MAX, 0.0f, 0.0f, RT_NO_HIT};
+}
+}  // namespace
+
+int trace_closest_queue(rt_ctx *ctx, const rt_ray *d_rays, const uint32_t *d_count, uint32_t cap, rt_hit *d_hits,
+                        cudaStream_t st) {
+    if (cap == 0) return RT_OK;
+    if (ctx->n_tris == 0) {
+        k_fill_miss<<<(cap + 255) / 256, 256, 0, st>>>(d_count, d_hits, cap);
+        RT_CUDA_TRY(cudaGetLastError());
+        return RT_OK;
+    }
+    if (ctx->depth <= 64) return launch_persistent<false, 64>(ctx, d_rays, cap, d_count, d_hits, nullptr, st);
+    return launch_persistent<false, 256>(ctx, d_rays, cap, d_count, d_hits, nullptr, st);
+}
+
 int segments_to_rays(const float *d_segs, size_t n, rt_ray *d_rays, cudaStream_t st) {
     if (n == 0) return RT_OK;
     k_segments_to_rays<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_segs, n, d_rays);

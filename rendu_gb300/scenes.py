@@ -429,3 +429,106 @@ def feature_scene(seed: int = 20261204) -> Scene:
     sc.background = {"mode": 2, "color": (0, 0, 0), "tex": tuple(faces)}
     sc.camera = {"eye": (0.0, 1.2, 3.0), "center": (0.0, 0.4, 0.0), "up": (0.0, 1.0, 0.0), "fov": 1.1, "ratio": 1.0}
     return sc
+
+
+def sky_equirect(width: int = 1024, height: int = 512, sun_dir=(0.4, 0.55, -0.5), sun_radiance: float = 5e4,
+                 sun_radius: float = 0.02) -> np.ndarray:
+    """Synthetic HDR environment (equirectangular, float32 RGB): a sky gradient from a
+    horizon colour to a zenith colour, a darker ground half, and a sun disc of the given
+    radiance and angular radius (radians)."""
+    j, i = np.meshgrid(np.arange(width), np.arange(height))
+    phi = (j + 0.5) / width * 2 * np.pi
+    theta = (i + 0.5) / height * np.pi
+    d = np.stack([np.sin(theta) * np.cos(phi), np.cos(theta), np.sin(theta) * np.sin(phi)], -1)
+    return _sky_radiance(d, sun_dir, sun_radiance, sun_radius).astype(np.float32)
+
+
+def _sky_radiance(d, sun_dir, sun_radiance, sun_radius):
+    s = np.asarray(sun_dir, np.float64)
+    s = s / np.linalg.norm(s)
+    up = np.clip(d[..., 1], -1.0, 1.0)
+    t = np.clip(up, 0.0, 1.0)[..., None]
+    horizon = np.array([0.9, 0.85, 0.8])
+    zenith = np.array([0.25, 0.45, 0.9])
+    ground = np.array([0.25, 0.22, 0.2])
+    col = np.where(up[..., None] >= 0.0, horizon * (1 - t) + zenith * t, ground * (0.5 + 0.5 * (1 + up[..., None])))
+    cosang = d @ s
+    col = col + np.where(cosang[..., None] > np.cos(sun_radius), sun_radiance, 0.0)
+    return col
+
+
+def equirect_to_cubemap(env: np.ndarray, face: int = 256):
+    """Resample an equirectangular map into the six faces (+x,-x,+y,-y,+z,-z) in the
+    orientation Texture::sampleCubemap reads them (Texture.cpp:141-191): face texel (x, y)
+    looks along the direction whose projection onto that face gives u = x, v = y."""
+    h, w = env.shape[:2]
+    c = (np.arange(face) + 0.5) / face * 2.0 - 1.0  # [-1, 1]
+    xs, ys = np.meshgrid(c, c)  # xs: column (u), ys: row (v); v = 0.5*(-y/denom)+0.5 -> y = -v
+    faces = []
+    for f in range(6):
+        u, v = xs, ys
+        if f == 0:
+            d = np.stack([np.ones_like(u), -v, -u], -1)
+        elif f == 1:
+            d = np.stack([-np.ones_like(u), -v, u], -1)
+        elif f == 2:
+            d = np.stack([u, np.ones_like(u), v], -1)
+        elif f == 3:
+            d = np.stack([u, -np.ones_like(u), -v], -1)
+        elif f == 4:
+            d = np.stack([u, -v, np.ones_like(u)], -1)
+        else:
+            d = np.stack([-u, -v, -np.ones_like(u)], -1)
+        d = d / np.linalg.norm(d, axis=-1, keepdims=True)
+        theta = np.arccos(np.clip(d[..., 1], -1, 1))
+        phi = np.mod(np.arctan2(d[..., 2], d[..., 0]), 2 * np.pi)
+        px = np.clip((phi / (2 * np.pi) * w).astype(np.int64), 0, w - 1)
+        py = np.clip((theta / np.pi * h).astype(np.int64), 0, h - 1)
+        faces.append(np.ascontiguousarray(env[py, px], np.float32))
+    return faces
+
+
+def instanced_scene(seed: int = 20261206, instances: int = 200, subdivisions: int = 5, prototypes: int = 6,
+                    env_face: int = 256) -> Scene:
+    """The large path-tracer workload: `instances` seeded instances, alternating displaced
+    icospheres (20,480 triangles at 5 subdivisions) and boxes, on a 2-triangle ground plane
+    (~2M triangles at 200 instances). Materials: GGX roughness U[0.05, 1], metalness
+    Bernoulli(0.3), base colour U[0.2, 0.9]^3. Four emissive quads. Background: a synthetic
+    1024x512 HDR sky (gradient + sun disc of radiance 5e4) resampled to a cubemap, the
+    reference's SKYBOX mode. Camera for 1920x1080."""
+    rng = np.random.default_rng(seed)
+    sc = Scene()
+    ground = sc.add_mesh(quad_mesh((-40, 0, 40), (80, 0, 0), (0, 0, -80)))
+    sc.add_object(ground, sc.add_material((0.5, 0.5, 0.5), rough=0.9, metal=0.0))
+    protos = []
+    for k in range(prototypes):
+        m = icosphere_mesh(subdivisions, seed=seed + 17 * k, displacement=0.1)
+        m.with_frames()
+        protos.append(sc.add_mesh(m))
+    box = sc.add_mesh(box_mesh())
+    side = int(math.ceil(math.sqrt(instances)))
+    cells = rng.permutation(side * side)[:instances]
+    for k in range(instances):
+        cx, cz = cells[k] % side, cells[k] // side
+        x = (cx + 0.5) / side * 48.0 - 24.0 + rng.uniform(-0.6, 0.6)
+        z = (cz + 0.5) / side * 48.0 - 24.0 + rng.uniform(-0.6, 0.6)
+        s = rng.uniform(0.5, 1.2)
+        metal = float(rng.random() < 0.3)
+        mat = sc.add_material(rng.uniform(0.2, 0.9, 3), rough=float(rng.uniform(0.05, 1.0)), metal=metal)
+        if k % 2 == 0:
+            mesh = protos[int(rng.integers(0, prototypes))]
+            model = translation((x, s * 1.1, z)) @ rotation_y(rng.uniform(0, 2 * math.pi)) @ scaling(s)
+        else:
+            mesh = box
+            model = translation((x, s, z)) @ rotation_y(rng.uniform(0, 2 * math.pi)) @ scaling((1.6 * s, 2 * s, 1.6 * s))
+        sc.add_object(mesh, mat, model)
+    for k in range(4):
+        ang = k * math.pi / 2 + 0.4
+        c = (14 * math.cos(ang), 9.0, 14 * math.sin(ang))
+        q = sc.add_mesh(quad_mesh((c[0] - 1.5, c[1], c[2] + 1.5), (3, 0, 0), (0, 0, -3), normal=(0, -1, 0)))
+        sc.add_object(q, sc.add_material((25.0, 22.0, 18.0), emissive=True))
+    faces = equirect_to_cubemap(sky_equirect(), env_face)
+    sc.background = {"mode": 2, "color": (0, 0, 0), "tex": tuple(sc.add_texture(f) for f in faces)}
+    sc.camera = {"eye": (0.0, 9.0, 34.0), "center": (0.0, 1.0, 0.0), "up": (0.0, 1.0, 0.0), "fov": 0.9,
+                 "ratio": 1920.0 / 1080.0}
+    return sc
