@@ -279,9 +279,24 @@ def main():
     ap.add_argument("--no-pt", action="store_true", help="skip the path-tracer lines")
     ap.add_argument("--profile-run", action="store_true",
                     help="only one closest-hit and one any-hit launch over the workload (for ncu captures)")
+    ap.add_argument("--profile-pt", default=None, choices=list(PT_CONFIGS),
+                    help="only one render of the given path-tracer configuration (for ncu captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile_pt:
+        import rendu_gb300 as R
+        import torch
+        from rendu_gb300 import build as B
+
+        B.build()
+        kind, w, h, spp, depth, _ = PT_CONFIGS[args.profile_pt]
+        sc = _pt_scene(kind)
+        img = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
+        tr = R.PathTracer(sc)
+        tr.render(dict(sc.camera, ratio=w / h), spp, depth, img, seed=1)
+        print(json.dumps({"profile_pt": args.profile_pt, **tr.last_stats()}))
         return
 
     import torch
@@ -321,14 +336,16 @@ def main():
     _sync_all(dist, torch)
 
     # ---- timed: closest hit, rays resident in HBM (512 MB of rays per step > L2) --------
+    # Clocks are sampled (every 200 ms) across all timed GPU work of this run: the closest-
+    # and any-hit loops, the e2e loop and the path-tracer renders.
+    clk = ClockSampler(local).__enter__()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        _sync_all(dist, torch)
-        ev0.record(stream)
-        for _ in range(args.steps):
-            rc.intersect_batch(d_rays, out=d_hits)
-        ev1.record(stream)
-        _sync_all(dist, torch)
+    _sync_all(dist, torch)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        rc.intersect_batch(d_rays, out=d_hits)
+    ev1.record(stream)
+    _sync_all(dist, torch)
     t_closest = ev0.elapsed_time(ev1) / 1000.0
     t_closest = _max_over_ranks(dist, torch, t_closest)
 
@@ -388,13 +405,14 @@ def main():
                          "peak_kind": peak_kind, "bytes_per_ray": round(bytes_per_ray, 1),
                          "node_visits_per_ray": round(v_node, 3), "tri_tests_per_ray": round(v_tri, 3),
                          "io_only_frac": round(48 * n / avg_launch / 1e9 / peak, 4)},
-            "clocks": clk.summary(),
             "gpu_launches": args.steps,
             "bvh": {"build_ms": round(st["build_ms"], 2), "nodes": st["nodes"], "leaves": st["leaves"],
                     "sah_cost": round(st["sah_cost"], 2), "device_mb": round(st["device_bytes"] / 2**20, 1)},
         }
         if not args.no_pt:
             out["pathtracer"] = {name: run_pathtracer(name, 3, not args.no_cpu) for name in PT_CONFIGS}
+        clk.__exit__(None, None, None)
+        out["clocks"] = clk.summary()
         if not args.no_cpu:
             threads = max((os.cpu_count() or 2) - 1, 1)
             rate, m, build_s = cpu_raycaster_rate(mesh, rays, args.cpu_seconds, threads)
@@ -402,6 +420,8 @@ def main():
                                    "sample": f"first {m} rays of the same 16,777,216-ray set",
                                    "build_s": round(build_s, 2)}
         print(json.dumps(out), flush=True)
+    if rank != 0:
+        clk.__exit__(None, None, None)
     if dist is not None:
         dist.destroy_process_group()
 
