@@ -14,7 +14,7 @@ beside it.
 * e2e       -- Mrays/s through the public API with host (pinned) buffers: host->device copy
                of the rays and device->host copy of the hits inside the timed region.
 * roofline  -- the traversal kernel against the measured HBM bandwidth; algorithmic bytes
-               per ray = 32 (ray) + 16 (hit) + 64 x inner nodes visited + 48 x triangles
+               per ray = 32 (ray) + 16 (hit) + 128 x 4-wide nodes visited + 48 x triangles
                tested, visit counts measured on a 1M-ray sample of the same set.
 * cpu_baseline -- the C restatement of the reference Raycaster (oracle/port), reference
                threading (hardware threads - 1), on a bounded sample of the same rays.
@@ -372,7 +372,7 @@ def main():
     # ---- algorithmic bytes per ray (visit counts on a 1M-ray sample) -------------------
     nv, nt = rc.count_visits(rays[: 1 << 20])
     v_node, v_tri = float(nv.mean()), float(nt.mean())
-    bytes_per_ray = 32 + 16 + 64 * v_node + 48 * v_tri
+    bytes_per_ray = 32 + 16 + 128 * v_node + 48 * v_tri
     avg_launch = t_closest / args.steps
     achieved = bytes_per_ray * n / avg_launch / 1e9
     peak, peak_kind = _peaks()

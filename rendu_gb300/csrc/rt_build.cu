@@ -19,6 +19,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <utility>
 
 #include "rt_context.hpp"
 
@@ -275,45 +276,90 @@ __global__ void k_bottom_up(uint64_t nt, const uint32_t *__restrict__ child, con
     }
 }
 
-// Emit 64-byte nodes. Nodes inside collapsed subtrees are written but never referenced.
-__global__ void k_emit(uint64_t ninner, const uint32_t *__restrict__ child, const uint32_t *__restrict__ range_first,
-                       const uint32_t *__restrict__ range_last, const float4 *__restrict__ slo,
-                       const float4 *__restrict__ shi, const float4 *__restrict__ ilo, const float4 *__restrict__ ihi,
-                       const uint8_t *__restrict__ collapse, BvhNode *__restrict__ nodes) {
-    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= ninner) return;
-    float4 lo[2], hi[2];
-    int idx[2], cnt[2];
-    for (int s = 0; s < 2; ++s) {
-        const uint32_t ch = child[2 * i + s];
-        const uint32_t id = ch >> 1;
-        if (ch & 1u) {
-            lo[s] = slo[id];
-            hi[s] = shi[id];
-            idx[s] = (int)id;
-            cnt[s] = 1;
-        } else {
-            lo[s] = ilo[id];
-            hi[s] = ihi[id];
-            if (collapse[id]) {
-                idx[s] = (int)range_first[id];
-                cnt[s] = (int)(range_last[id] - range_first[id] + 1);
-            } else {
-                idx[s] = (int)id;
-                cnt[s] = 0;
-            }
-        }
-    }
-    BvhNode nd;
-    nd.a = make_float4(lo[0].x, hi[0].x, lo[0].y, hi[0].y);
-    nd.b = make_float4(lo[1].x, hi[1].x, lo[1].y, hi[1].y);
-    nd.c = make_float4(lo[0].z, hi[0].z, lo[1].z, hi[1].z);
-    nd.d = make_int4(idx[0], idx[1], cnt[0], cnt[1]);
-    nodes[i] = nd;
+__device__ __forceinline__ void set_slot(BvhNode &nd, int c, float4 lo, float4 hi, int child, int count) {
+    float *lx = &nd.lox.x, *hx = &nd.hix.x, *ly = &nd.loy.x, *hy = &nd.hiy.x, *lz = &nd.loz.x, *hz = &nd.hiz.x;
+    lx[c] = lo.x; hx[c] = hi.x; ly[c] = lo.y; hy[c] = hi.y; lz[c] = lo.z; hz[c] = hi.z;
+    (&nd.child.x)[c] = child;
+    (&nd.count.x)[c] = count;
 }
 
-// A root whose whole tree is one leaf (or a single triangle): child 0 = the leaf, child 1
-// = an empty box that no ray enters.
+__device__ __forceinline__ void set_empty(BvhNode &nd, int c) {
+    const float4 inf = make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
+    set_slot(nd, c, inf, inf, -1, -1);
+}
+
+struct CollapseItem {
+    uint32_t bin;   // inner node of the binary tree
+    uint32_t slot;  // node of the 4-wide hierarchy it becomes
+};
+
+// One level of the binary -> 4-wide collapse: each queued binary inner node becomes a 4-wide
+// node whose children are found by repeatedly opening the largest-area inner child (the
+// surface-area-greedy rule); leaves and collapsed subtrees become leaf slots, remaining
+// inner children get new slots and are queued for the next level.
+__global__ void k_collapse(const CollapseItem *__restrict__ in, uint32_t n_in, CollapseItem *__restrict__ out,
+                           uint32_t *__restrict__ n_out, uint32_t *__restrict__ node_count, uint32_t node_cap,
+                           const uint32_t *__restrict__ child, const uint32_t *__restrict__ range_first,
+                           const uint32_t *__restrict__ range_last, const float4 *__restrict__ slo,
+                           const float4 *__restrict__ shi, const float4 *__restrict__ ilo,
+                           const float4 *__restrict__ ihi, const uint8_t *__restrict__ collapse,
+                           BvhNode *__restrict__ nodes, uint32_t *__restrict__ leaf_count,
+                           unsigned *__restrict__ status) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_in) return;
+    const CollapseItem item = in[i];
+    uint32_t e[4];
+    int ne = 2;
+    e[0] = child[2 * item.bin];
+    e[1] = child[2 * item.bin + 1];
+    while (ne < 4) {
+        int best = -1;
+        float besta = -1.0f;
+        for (int k = 0; k < ne; ++k) {
+            if (e[k] & 1u) continue;
+            const uint32_t id = e[k] >> 1;
+            if (collapse[id]) continue;
+            const float a = half_area(ilo[id], ihi[id]);
+            if (a > besta) {
+                besta = a;
+                best = k;
+            }
+        }
+        if (best < 0) break;
+        const uint32_t b = e[best] >> 1;
+        e[best] = child[2 * b];
+        e[ne++] = child[2 * b + 1];
+    }
+    BvhNode nd;
+    uint32_t leaves = 0;
+    for (int c = 0; c < 4; ++c) {
+        if (c >= ne) {
+            set_empty(nd, c);
+            continue;
+        }
+        const uint32_t id = e[c] >> 1;
+        if (e[c] & 1u) {
+            set_slot(nd, c, slo[id], shi[id], (int)id, 1);
+            ++leaves;
+        } else if (collapse[id]) {
+            set_slot(nd, c, ilo[id], ihi[id], (int)range_first[id], (int)(range_last[id] - range_first[id] + 1));
+            ++leaves;
+        } else {
+            const uint32_t slot = atomicAdd(node_count, 1u);
+            if (slot >= node_cap) {  // cannot happen for a well-formed tree; never write out of bounds
+                atomicOr(status, RT_DEV_QUEUE_OVERFLOW);
+                set_empty(nd, c);
+                continue;
+            }
+            set_slot(nd, c, ilo[id], ihi[id], (int)slot, 0);
+            out[atomicAdd(n_out, 1u)] = CollapseItem{id, slot};
+        }
+    }
+    nodes[item.slot] = nd;
+    atomicAdd(leaf_count, leaves);
+}
+
+// A root whose whole tree is one leaf (or a single triangle): slot 0 = the leaf.
 __global__ void k_root_leaf(uint64_t nt, const float4 *__restrict__ slo, const float4 *__restrict__ shi,
                             BvhNode *__restrict__ nodes) {
     float4 lo = make_float4(INFINITY, INFINITY, INFINITY, 0), hi = make_float4(-INFINITY, -INFINITY, -INFINITY, 0);
@@ -322,12 +368,9 @@ __global__ void k_root_leaf(uint64_t nt, const float4 *__restrict__ slo, const f
         lo = make_float4(fminf(lo.x, a.x), fminf(lo.y, a.y), fminf(lo.z, a.z), 0);
         hi = make_float4(fmaxf(hi.x, b.x), fmaxf(hi.y, b.y), fmaxf(hi.z, b.z), 0);
     }
-    // Child 1 is absent: index -1 (the traversal skips it) and a box at +infinity.
     BvhNode nd;
-    nd.a = make_float4(lo.x, hi.x, lo.y, hi.y);
-    nd.b = make_float4(INFINITY, INFINITY, INFINITY, INFINITY);
-    nd.c = make_float4(lo.z, hi.z, INFINITY, INFINITY);
-    nd.d = make_int4(0, -1, (int)nt, 0);
+    set_slot(nd, 0, lo, hi, 0, (int)nt);
+    for (int c = 1; c < 4; ++c) set_empty(nd, c);
     nodes[0] = nd;
 }
 
@@ -430,7 +473,7 @@ int build_hierarchy(rt_ctx *ctx) {
         k_root_leaf<<<1, 1, 0, st>>>(nt, d_slo.p, d_shi.p, ctx->d_nodes.as<BvhNode>());
         ctx->n_inner = 1;
         ctx->n_leaves = 1;
-        ctx->depth = 1;
+        ctx->depth = 3;
         ctx->sah_cost = 1.0f;
     } else {
         const uint64_t ni = nt - 1;
@@ -465,48 +508,53 @@ int build_hierarchy(rt_ctx *ctx) {
         RT_CUDA_TRY(cudaMemcpyAsync(&rlo, d_ilo.p, sizeof(float4), cudaMemcpyDeviceToHost, st));
         RT_CUDA_TRY(cudaMemcpyAsync(&rhi, d_ihi.p, sizeof(float4), cudaMemcpyDeviceToHost, st));
         RT_CUDA_TRY(cudaStreamSynchronize(st));
-        if (root_col) {
-            k_root_leaf<<<1, 1, 0, st>>>(nt, d_slo.p, d_shi.p, ctx->d_nodes.as<BvhNode>());
-            ctx->n_inner = 1;
-            ctx->depth = 1;
-        } else {
-            k_emit<<<ib, 256, 0, st>>>(ni, d_child.p, d_rf.p, d_rl.p, d_slo.p, d_shi.p, d_ilo.p, d_ihi.p, d_col.p,
-                                       ctx->d_nodes.as<BvhNode>());
-            ctx->n_inner = ni;
-            ctx->depth = root_h;
-        }
         const float ra = std::fmax((rhi.x - rlo.x) * (rhi.y - rlo.y) + (rhi.y - rlo.y) * (rhi.z - rlo.z) +
                                        (rhi.z - rlo.z) * (rhi.x - rlo.x), 1e-30f);
         ctx->sah_cost = root_cost / ra;
         ctx->root_box[0] = rlo.x; ctx->root_box[1] = rlo.y; ctx->root_box[2] = rlo.z;
         ctx->root_box[3] = rhi.x; ctx->root_box[4] = rhi.y; ctx->root_box[5] = rhi.z;
-        // Count leaves = reachable leaf references (for statistics only).
-        std::vector<uint8_t> col(ni);
-        std::vector<uint32_t> chh(2 * ni);
-        RT_CUDA_TRY(cudaMemcpyAsync(col.data(), d_col.p, ni, cudaMemcpyDeviceToHost, st));
-        RT_CUDA_TRY(cudaMemcpyAsync(chh.data(), d_child.p, 2 * ni * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        RT_CUDA_TRY(cudaStreamSynchronize(st));
-        uint64_t leaves = 0, inner_reach = 0;
-        if (!root_col) {
-            std::vector<uint32_t> stack{0};
-            while (!stack.empty()) {
-                const uint32_t nd = stack.back();
-                stack.pop_back();
-                ++inner_reach;
-                for (int s = 0; s < 2; ++s) {
-                    const uint32_t ch = chh[2 * nd + s];
-                    if ((ch & 1u) || col[ch >> 1]) ++leaves;
-                    else stack.push_back(ch >> 1);
+        if (root_col) {
+            k_root_leaf<<<1, 1, 0, st>>>(nt, d_slo.p, d_shi.p, ctx->d_nodes.as<BvhNode>());
+            ctx->n_inner = 1;
+            ctx->n_leaves = 1;
+            ctx->depth = 3;
+        } else {
+            // Binary -> 4-wide collapse, one level per launch (breadth-first slot order).
+            Scratch<CollapseItem> d_q0, d_q1;
+            Scratch<uint32_t> d_cnt;  // [0] n_out, [1] node count, [2] leaf count
+            RT_CUDA_TRY(d_q0.alloc(ni));
+            RT_CUDA_TRY(d_q1.alloc(ni));
+            RT_CUDA_TRY(d_cnt.alloc(4));
+            const CollapseItem root{0u, 0u};
+            const uint32_t cnt_init[4] = {0u, 1u, 0u, 0u};
+            RT_CUDA_TRY(cudaMemcpyAsync(d_q0.p, &root, sizeof(root), cudaMemcpyHostToDevice, st));
+            RT_CUDA_TRY(cudaMemcpyAsync(d_cnt.p, cnt_init, sizeof(cnt_init), cudaMemcpyHostToDevice, st));
+            uint32_t n_in = 1, levels = 0;
+            CollapseItem *qin = d_q0.p, *qout = d_q1.p;
+            while (n_in > 0) {
+                RT_CUDA_TRY(cudaMemsetAsync(d_cnt.p, 0, sizeof(uint32_t), st));
+                k_collapse<<<(n_in + 127) / 128, 128, 0, st>>>(qin, n_in, qout, d_cnt.p, d_cnt.p + 1, (uint32_t)ni,
+                                                               d_child.p, d_rf.p, d_rl.p, d_slo.p, d_shi.p, d_ilo.p,
+                                                               d_ihi.p, d_col.p, ctx->d_nodes.as<BvhNode>(),
+                                                               d_cnt.p + 2, ctx->d_status.as<unsigned>());
+                RT_CUDA_TRY(cudaMemcpyAsync(&n_in, d_cnt.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+                RT_CUDA_TRY(cudaStreamSynchronize(st));
+                std::swap(qin, qout);
+                ++levels;
+                if (levels > 200) {
+                    set_error("hierarchy collapse did not terminate");
+                    return RT_ERR_STATE;
                 }
             }
-        } else {
-            leaves = 1;
-            inner_reach = 1;
+            uint32_t cnt[4];
+            RT_CUDA_TRY(cudaMemcpyAsync(cnt, d_cnt.p, sizeof(cnt), cudaMemcpyDeviceToHost, st));
+            RT_CUDA_TRY(cudaStreamSynchronize(st));
+            ctx->n_inner = cnt[1];
+            ctx->n_leaves = cnt[2];
+            // The traversal pushes at most 3 entries per level.
+            ctx->depth = 3 * (int)levels;
+            (void)root_h;
         }
-        ctx->n_leaves = leaves;
-        ctx->n_inner = root_col ? 1 : ni;
-        ctx->sah_cost = ctx->sah_cost;
-        (void)inner_reach;
     }
     RT_CUDA_TRY(cudaEventRecord(ctx->ev_b, st));
     RT_CUDA_TRY(cudaEventSynchronize(ctx->ev_b));

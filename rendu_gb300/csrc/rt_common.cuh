@@ -63,16 +63,14 @@ __host__ __device__ __forceinline__ f3 fmin3(f3 a, f3 b) { return f3{fminf(a.x, 
 __host__ __device__ __forceinline__ f3 fmax3(f3 a, f3 b) { return f3{fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)}; }
 
 // ---- device data layout ------------------------------------------------------------------
-// Inner node of the binary hierarchy, 64 bytes, both children's boxes inline:
-//   a = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
-//   b = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
-//   c = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
-//   d = (child0, child1, count0, count1)  count == 0: child is an inner node index;
-//                                          count  > 0: child is a leaf = triangles
-//                                                      [child, child + count) in leaf order.
+// 4-wide node, 128 bytes (one L2 line): child boxes in structure-of-arrays form,
+//   lox = (c0.lo.x, c1.lo.x, c2.lo.x, c3.lo.x), hix, loy, hiy, loz, hiz likewise;
+//   child = inner node index, or the first triangle of a leaf (leaf order);
+//   count = 0: inner node; > 0: leaf of `count` triangles; -1: empty slot (box at +inf).
 struct __align__(16) BvhNode {
-    float4 a, b, c;
-    int4 d;
+    float4 lox, hix, loy, hiy, loz, hiz;
+    int4 child;
+    int4 count;
 };
 
 // Triangle in leaf order, 48 bytes: v0 and the two edges v1 - v0, v2 - v0 (computed with

@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(128) k_noalloc_visible(const BvhNode *__restri
     TravState t;
     uint32_t idx = 0;
     bool active = false, exhausted = false;
+    uint32_t nv_ = 0, nt_ = 0;
     while (true) {
         const unsigned need = __ballot_sync(0xffffffffu, !active);
         if (need && !exhausted) {
@@ -79,7 +80,7 @@ __global__ void __launch_bounds__(128) k_noalloc_visible(const BvhNode *__restri
             if (exhausted) break;
             continue;
         }
-        if (active && trav_step<true, STACK>(nodes, tris, r, t, stack_node, stack_near, status)) {
+        if (active && trav_step<true, false, STACK>(nodes, tris, r, t, stack_node, stack_near, status, nv_, nt_)) {
             active = false;
             visible[idx] = t.res.found ? 0 : 1;
         }

@@ -56,6 +56,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent(const BvhNode *__restr
     TravState t;
     size_t idx = 0;
     bool active = false, exhausted = false;
+    uint32_t nv_ = 0, nt_ = 0;
     while (true) {
         const unsigned need = __ballot_sync(0xffffffffu, !active);
         if (need && !exhausted) {
@@ -83,7 +84,7 @@ __global__ void __launch_bounds__(128) k_trace_persistent(const BvhNode *__restr
             if (exhausted) break;
             continue;
         }
-        if (active && trav_step<ANY, STACK>(nodes, tris, r, t, stack_node, stack_near, status)) {
+        if (active && trav_step<ANY, false, STACK>(nodes, tris, r, t, stack_node, stack_near, status, nv_, nt_)) {
             active = false;
             if (ANY) {
                 occ[idx] = t.res.found ? 1 : 0;

@@ -86,113 +86,10 @@ struct TraceResult {
     bool found;
 };
 
-// Traverse the hierarchy (root = node 0). ANY: stop at the first accepted triangle.
-template <bool ANY, bool COUNT, int STACK>
-__device__ __forceinline__ TraceResult traverse(const BvhNode *__restrict__ nodes, const BvhTri *__restrict__ tris,
-                                                const RayState &r, unsigned *__restrict__ status, uint32_t &nvis,
-                                                uint32_t &ntri) {
-    TraceResult res;
-    res.t = FLT_MAX;
-    res.u = 0.0f;
-    res.v = 0.0f;
-    res.prim = RT_NO_HIT;
-    res.found = false;
-    float cur_max = r.tmax;  // shrinks to the best distance (Raycaster.cpp:170)
-    int stack_node[STACK];
-    float stack_near[STACK];
-    int sp = 0;
-    int node = 0;
-    while (true) {
-        const float4 *np = reinterpret_cast<const float4 *>(nodes + node);
-        const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
-        const int4 d = __ldg(reinterpret_cast<const int4 *>(np + 3));
-        if (COUNT) ++nvis;
-        float t0 = slab(r, a.x, a.y, a.z, a.w, c.x, c.y, r.tmin, cur_max);
-        float t1 = d.y >= 0 ? slab(r, b.x, b.y, b.z, b.w, c.z, c.w, r.tmin, cur_max) : INFINITY;
-        // Leaves are tested as soon as their box is entered.
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-            const float ts = s ? t1 : t0;
-            const int cnt = s ? d.w : d.z;
-            if (cnt == 0 || ts == INFINITY) continue;
-            const int first = s ? d.y : d.x;
-            for (int k = 0; k < cnt; ++k) {
-                const float4 *tp = reinterpret_cast<const float4 *>(tris + first + k);
-                const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
-                if (COUNT) ++ntri;
-                float t, u, v;
-                if (!mt_exact(r, v0, e1, e2, t, u, v)) continue;
-                if (!(t > r.tmin)) continue;
-                const uint32_t prim = __float_as_uint(v0.w);
-                if (ANY) {
-                    if (t < cur_max) {
-                        res.found = true;
-                        res.t = t;
-                        res.u = u;
-                        res.v = v;
-                        res.prim = prim;
-                        break;
-                    }
-                    continue;
-                }
-                if (t < cur_max || (res.found && t == cur_max && prim < res.prim)) {
-                    res.found = true;
-                    res.t = t;
-                    res.u = u;
-                    res.v = v;
-                    res.prim = prim;
-                    cur_max = t;
-                }
-            }
-            if (ANY && res.found) break;
-            if (s) t1 = INFINITY;
-            else t0 = INFINITY;
-        }
-        if (ANY && res.found) break;
-        const bool h0 = t0 <= cur_max, h1 = t1 <= cur_max;
-        if (h0 && h1) {
-            const bool first0 = t0 <= t1;
-            if (sp >= STACK) {
-                atomicOr(status, RT_DEV_STACK_OVERFLOW);
-                break;
-            }
-            stack_node[sp] = first0 ? d.y : d.x;
-            stack_near[sp] = first0 ? t1 : t0;
-            ++sp;
-            node = first0 ? d.x : d.y;
-            continue;
-        }
-        if (h0) {
-            node = d.x;
-            continue;
-        }
-        if (h1) {
-            node = d.y;
-            continue;
-        }
-        // Pop the next entry still within the (possibly shrunk) window.
-        bool popped = false;
-        while (sp > 0) {
-            --sp;
-            if (stack_near[sp] <= cur_max) {
-                node = stack_node[sp];
-                popped = true;
-                break;
-            }
-        }
-        if (!popped) break;
-    }
-    return res;
-}
-
-// ---- persistent traversal with per-lane ray refill ---------------------------------------
-// One iteration = one node visit (two child box tests, leaf triangles of entered children,
-// push/pop). A lane whose ray has finished takes the next unclaimed ray at the start of
-// the following iteration (one atomic per warp per refill), so rays that stop at the root
-// and rays that descend deep share warps without idling lanes.
+// ---- traversal state and one node visit -----------------------------------------------------
 struct TravState {
     int node, sp;
-    float cur_max;
+    float cur_max;  // shrinks to the best distance (Raycaster.cpp:170)
     TraceResult res;
 };
 
@@ -207,25 +104,48 @@ __device__ __forceinline__ void trav_init(TravState &t, const RayState &r) {
     t.res.found = false;
 }
 
-// Returns true when the ray is finished.
-template <bool ANY, int STACK>
+__device__ __forceinline__ void cswap(float &ka, int &ia, float &kb, int &ib) {
+    if (kb < ka) {
+        const float k = ka;
+        ka = kb;
+        kb = k;
+        const int i = ia;
+        ia = ib;
+        ib = i;
+    }
+}
+
+// Visit node t.node of the 4-wide hierarchy: slab-test its children, test the triangles of
+// entered leaves (updating the window), then continue with the nearest entered inner child
+// and push the others far-to-near; pop when none was entered. Returns true when the ray is
+// finished (stack empty, or ANY and a hit was found).
+template <bool ANY, bool COUNT, int STACK>
 __device__ __forceinline__ bool trav_step(const BvhNode *__restrict__ nodes, const BvhTri *__restrict__ tris,
                                           const RayState &r, TravState &t, int *stack_node, float *stack_near,
-                                          unsigned *__restrict__ status) {
+                                          unsigned *__restrict__ status, uint32_t &nvis, uint32_t &ntri) {
     const float4 *np = reinterpret_cast<const float4 *>(nodes + t.node);
-    const float4 a = __ldg(np), b = __ldg(np + 1), c = __ldg(np + 2);
-    const int4 d = __ldg(reinterpret_cast<const int4 *>(np + 3));
-    float t0 = slab(r, a.x, a.y, a.z, a.w, c.x, c.y, r.tmin, t.cur_max);
-    float t1 = d.y >= 0 ? slab(r, b.x, b.y, b.z, b.w, c.z, c.w, r.tmin, t.cur_max) : INFINITY;
+    const float4 lox = __ldg(np), hix = __ldg(np + 1), loy = __ldg(np + 2), hiy = __ldg(np + 3);
+    const float4 loz = __ldg(np + 4), hiz = __ldg(np + 5);
+    const int4 ch = __ldg(reinterpret_cast<const int4 *>(np + 6));
+    const int4 cn = __ldg(reinterpret_cast<const int4 *>(np + 7));
+    if (COUNT) ++nvis;
+    float k[4];
+    int id[4];
+    const int cc[4] = {cn.x, cn.y, cn.z, cn.w};
+    id[0] = ch.x; id[1] = ch.y; id[2] = ch.z; id[3] = ch.w;
+    k[0] = cc[0] >= 0 ? slab(r, lox.x, hix.x, loy.x, hiy.x, loz.x, hiz.x, r.tmin, t.cur_max) : INFINITY;
+    k[1] = cc[1] >= 0 ? slab(r, lox.y, hix.y, loy.y, hiy.y, loz.y, hiz.y, r.tmin, t.cur_max) : INFINITY;
+    k[2] = cc[2] >= 0 ? slab(r, lox.z, hix.z, loy.z, hiy.z, loz.z, hiz.z, r.tmin, t.cur_max) : INFINITY;
+    k[3] = cc[3] >= 0 ? slab(r, lox.w, hix.w, loy.w, hiy.w, loz.w, hiz.w, r.tmin, t.cur_max) : INFINITY;
+    // Leaves first: they can only shrink the window for the inner children.
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        const float ts = s ? t1 : t0;
-        const int cnt = s ? d.w : d.z;
-        if (cnt == 0 || ts == INFINITY) continue;
-        const int first = s ? d.y : d.x;
-        for (int k = 0; k < cnt; ++k) {
-            const float4 *tp = reinterpret_cast<const float4 *>(tris + first + k);
+    for (int c = 0; c < 4; ++c) {
+        if (cc[c] <= 0 || k[c] == INFINITY) continue;
+        const int first = id[c];
+        for (int q = 0; q < cc[c]; ++q) {
+            const float4 *tp = reinterpret_cast<const float4 *>(tris + first + q);
             const float4 v0 = __ldg(tp), e1 = __ldg(tp + 1), e2 = __ldg(tp + 2);
+            if (COUNT) ++ntri;
             float tt, u, v;
             if (!mt_exact(r, v0, e1, e2, tt, u, v)) continue;
             if (!(tt > r.tmin)) continue;
@@ -250,28 +170,30 @@ __device__ __forceinline__ bool trav_step(const BvhNode *__restrict__ nodes, con
                 t.cur_max = tt;
             }
         }
-        if (s) t1 = INFINITY;
-        else t0 = INFINITY;
+        k[c] = INFINITY;
     }
-    const bool h0 = t0 <= t.cur_max, h1 = t1 <= t.cur_max;
-    if (h0 && h1) {
-        const bool first0 = t0 <= t1;
-        if (t.sp >= STACK) {
-            atomicOr(status, RT_DEV_STACK_OVERFLOW);
-            return true;
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+        if (cc[c] != 0 || !(k[c] <= t.cur_max)) k[c] = INFINITY;
+    // Sort the four (distance, child) pairs.
+    cswap(k[0], id[0], k[1], id[1]);
+    cswap(k[2], id[2], k[3], id[3]);
+    cswap(k[0], id[0], k[2], id[2]);
+    cswap(k[1], id[1], k[3], id[3]);
+    cswap(k[1], id[1], k[2], id[2]);
+    if (k[0] != INFINITY) {
+#pragma unroll
+        for (int j = 3; j >= 1; --j) {
+            if (k[j] == INFINITY) continue;
+            if (t.sp >= STACK) {
+                atomicOr(status, RT_DEV_STACK_OVERFLOW);
+                return true;
+            }
+            stack_node[t.sp] = id[j];
+            stack_near[t.sp] = k[j];
+            ++t.sp;
         }
-        stack_node[t.sp] = first0 ? d.y : d.x;
-        stack_near[t.sp] = first0 ? t1 : t0;
-        ++t.sp;
-        t.node = first0 ? d.x : d.y;
-        return false;
-    }
-    if (h0) {
-        t.node = d.x;
-        return false;
-    }
-    if (h1) {
-        t.node = d.y;
+        t.node = id[0];
         return false;
     }
     while (t.sp > 0) {
@@ -282,6 +204,20 @@ __device__ __forceinline__ bool trav_step(const BvhNode *__restrict__ nodes, con
         }
     }
     return true;
+}
+
+// Whole traversal for one ray (root = node 0).
+template <bool ANY, bool COUNT, int STACK>
+__device__ __forceinline__ TraceResult traverse(const BvhNode *__restrict__ nodes, const BvhTri *__restrict__ tris,
+                                                const RayState &r, unsigned *__restrict__ status, uint32_t &nvis,
+                                                uint32_t &ntri) {
+    int stack_node[STACK];
+    float stack_near[STACK];
+    TravState t;
+    trav_init(t, r);
+    while (!trav_step<ANY, COUNT, STACK>(nodes, tris, r, t, stack_node, stack_near, status, nvis, ntri)) {
+    }
+    return t.res;
 }
 
 }  // namespace rgb
