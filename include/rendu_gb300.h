@@ -263,6 +263,30 @@ RT_API int pt_scene_commit(pt_scene *scene);
 RT_API int pt_render(pt_scene *scene, const pt_camera_desc *camera, uint32_t samples, uint32_t depth, uint64_t seed,
               float *image, uint32_t width, uint32_t height, uint32_t components, void *stream, uint32_t flags);
 
+/* Estimators of pt_render_ex. */
+#define PT_MODE_REFERENCE 0 /* PathTracer::render's estimator, as pt_render                        */
+#define PT_MODE_EXTENDED 1  /* + next-event estimation on emissive triangles and on the environment
+                               map, each combined with BSDF sampling by multiple importance sampling
+                               (power heuristic); no counterpart in the reference                  */
+
+typedef struct pt_render_options {
+    int32_t mode;  /* PT_MODE_REFERENCE or PT_MODE_EXTENDED                                      */
+    float clamp;   /* per-sample radiance clamp; the reference uses 5 (PathTracer.cpp:288);
+                      <= 0 disables it                                                            */
+} pt_render_options;
+
+/* Environment map for PT_MODE_EXTENDED: an equirectangular float image (texture id from
+ * pt_scene_add_texture; u = phi / 2pi with phi = atan2(z, x), v = theta / pi from +y),
+ * scaled by `intensity`. It replaces the background for every miss in that mode and is
+ * importance-sampled by luminance x sin(theta). No counterpart in the reference, whose
+ * backgrounds are COLOR / IMAGE / SKYBOX / ATMOSPHERE (Scene.hpp:70-75). */
+RT_API int pt_scene_set_environment(pt_scene *scene, uint32_t tex_id, float intensity);
+
+/* pt_render with options (NULL = the reference estimator, clamp 5). */
+RT_API int pt_render_ex(pt_scene *scene, const pt_camera_desc *camera, uint32_t samples, uint32_t depth, uint64_t seed,
+                        float *image, uint32_t width, uint32_t height, uint32_t components,
+                        const pt_render_options *options, void *stream, uint32_t flags);
+
 /* Counters of the last pt_render on this scene. */
 RT_API int pt_get_render_stats(const pt_scene *scene, pt_render_stats *out);
 

@@ -286,6 +286,9 @@ class _OracleTracer:
         bg = scene.background
         col = (C.c_float * 3)(*[float(x) for x in bg.get("color", (0, 0, 0))])
         f("set_background")(self.h, int(bg["mode"]), col, (C.c_uint32 * 6)(*bg.get("tex", (0,) * 6)))
+        env = getattr(scene, "environment", None)
+        if env is not None and hasattr(lib, prefix + "set_environment"):
+            f("set_environment")(self.h, int(env["tex"]), C.c_float(float(env.get("intensity", 1.0))))
         f("commit")(self.h)
 
     def close(self):
@@ -309,20 +312,23 @@ class PortPathTracer(_OracleTracer):
             _pt_sigs(_Names(lib), "port_pt_")
             lib.port_pt_render.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, _f32p,
                                            C.c_uint32, C.c_uint32, C.c_int, _u64p]
+            lib.port_pt_render_ex.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, _f32p,
+                                              C.c_uint32, C.c_uint32, C.c_int, _u64p, C.c_int, C.c_float]
+            lib.port_pt_set_environment.argtypes = [C.c_void_p, C.c_uint32, C.c_float]
             lib.port_ggx_eval.argtypes = [_f32p, C.c_size_t, _f32p]
             lib.port_ggx_sample.argtypes = [_f32p, _f32p, C.c_size_t, _f32p]
             lib.port_pixel_shifts.argtypes = [C.c_void_p, _f32p]
             lib._pt_ready = True
         super().__init__(lib, "port_pt_", scene)
 
-    def render(self, camera, samples, depth, width, height, seed=0, threads=0, image=None):
+    def render(self, camera, samples, depth, width, height, seed=0, threads=0, image=None, mode=0, clamp=5.0):
         from rendu_gb300.pathtracer import camera_desc
 
         img = np.zeros((height, width, 3), np.float32) if image is None else image
         rays = np.zeros(3, np.uint64)
         cam = camera_desc(camera)
-        r = self.lib.port_pt_render(self.h, C.byref(cam), int(samples), int(depth), int(seed), img.reshape(-1), width,
-                                    height, int(threads), rays)
+        r = self.lib.port_pt_render_ex(self.h, C.byref(cam), int(samples), int(depth), int(seed), img.reshape(-1),
+                                       width, height, int(threads), rays, int(mode), float(clamp))
         if r != 0:
             raise RuntimeError("port render failed")
         self.rays = rays

@@ -101,11 +101,36 @@ struct port_pt {
     uint32_t bg_tex[6];
     port_rc *rc;
     int any_masked;
+    /* extended estimator */
+    int env_tex;
+    float env_intensity;
+    struct emitter_t *emitters;
+    float *ecdf;
+    int nemit;
+    double epower;
+    uint32_t ew, eh;
+    float *efunc, *emarg, *econd;
+    double eint;
+    float p_env;
 };
+
+typedef struct emitter_t {
+    float v0[3], e1[3], e2[3], emission[3], lum;
+} emitter_t;
 
 #define GROW(arr, n) ((arr) = realloc((arr), sizeof(*(arr)) * ((n) + 1)))
 
-port_pt *port_pt_create(void) { return (port_pt *)calloc(1, sizeof(port_pt)); }
+port_pt *port_pt_create(void) {
+    port_pt *s = (port_pt *)calloc(1, sizeof(port_pt));
+    if (s) s->env_tex = -1;
+    return s;
+}
+
+int port_pt_set_environment(port_pt *s, uint32_t tex, float intensity) {
+    s->env_tex = (int)tex;
+    s->env_intensity = intensity;
+    return 0;
+}
 
 void port_pt_destroy(port_pt *s) {
     if (!s) return;
@@ -115,6 +140,7 @@ void port_pt_destroy(port_pt *s) {
         free(s->mesh[k].bit); free(s->mesh[k].uv); free(s->mesh[k].idx);
     }
     free(s->tex); free(s->mesh); free(s->mat); free(s->obj); free(s->light);
+    free(s->emitters); free(s->ecdf); free(s->efunc); free(s->emarg); free(s->econd);
     if (s->rc) port_rc_destroy(s->rc);
     free(s);
 }
@@ -222,6 +248,95 @@ int port_pt_commit(port_pt *s) {
         s->obj[o].use_uv = m->uv != NULL; /* Object::Object (Object.cpp:4-8) */
         if (s->mat[s->obj[o].material].masked) s->any_masked = 1;
     }
+    /* Extended estimator tables: emissive triangles (power CDF) and the environment's
+     * piecewise-constant distribution (luminance x sin(theta)), as the CUDA path tracer. */
+    free(s->emitters); free(s->ecdf); free(s->efunc); free(s->emarg); free(s->econd);
+    s->emitters = NULL; s->ecdf = NULL; s->efunc = NULL; s->emarg = NULL; s->econd = NULL;
+    s->nemit = 0;
+    s->epower = 0.0;
+    for (size_t o = 0; o < s->nobj; ++o) {
+        const obj_t *ob = &s->obj[o];
+        const pt_material_desc *md = &s->mat[ob->material];
+        if (md->type != PT_MAT_EMISSIVE) continue;
+        const tex_t *t = &s->tex[md->tex[0]];
+        double e[3] = {0, 0, 0};
+        const size_t np = (size_t)t->w * t->h;
+        for (size_t q = 0; q < np; ++q)
+            for (int c = 0; c < 3; ++c) e[c] += t->rgba[4 * q + c];
+        for (int c = 0; c < 3; ++c) e[c] /= (double)np;
+        const double lum = 0.2126 * e[0] + 0.7152 * e[1] + 0.0722 * e[2];
+        if (!(lum > 0.0)) continue;
+        const mesh_t *m = &s->mesh[ob->mesh];
+        for (size_t tri = 0; tri + 2 < m->ni; tri += 3) {
+            double v[3][3];
+            for (int k = 0; k < 3; ++k) {
+                const float *pp = &m->pos[3 * (size_t)m->idx[tri + k]];
+                for (int r2 = 0; r2 < 3; ++r2)
+                    v[k][r2] = (double)ob->model[r2] * pp[0] + (double)ob->model[4 + r2] * pp[1] +
+                               (double)ob->model[8 + r2] * pp[2] + (double)ob->model[12 + r2];
+            }
+            const double u[3] = {v[1][0] - v[0][0], v[1][1] - v[0][1], v[1][2] - v[0][2]};
+            const double w[3] = {v[2][0] - v[0][0], v[2][1] - v[0][1], v[2][2] - v[0][2]};
+            const double cr[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+            const double area = 0.5 * sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+            if (!(area > 0.0)) continue;
+            s->emitters = (emitter_t *)realloc(s->emitters, sizeof(emitter_t) * (s->nemit + 1));
+            s->ecdf = (float *)realloc(s->ecdf, sizeof(float) * (s->nemit + 1));
+            emitter_t *em = &s->emitters[s->nemit];
+            for (int q = 0; q < 3; ++q) {
+                em->v0[q] = (float)v[0][q];
+                em->e1[q] = (float)u[q];
+                em->e2[q] = (float)w[q];
+                em->emission[q] = (float)e[q];
+            }
+            em->lum = (float)lum;
+            s->epower += area * lum;
+            s->ecdf[s->nemit] = (float)s->epower;
+            s->nemit++;
+        }
+    }
+    for (int k = 0; k < s->nemit; ++k) s->ecdf[k] = (float)(s->ecdf[k] / s->epower);
+    if (s->nemit) s->ecdf[s->nemit - 1] = 1.0f;
+    s->eint = 0.0;
+    if (s->env_tex >= 0) {
+        const tex_t *t = &s->tex[s->env_tex];
+        const uint32_t ew = t->w, eh = t->h;
+        s->ew = ew;
+        s->eh = eh;
+        s->efunc = (float *)malloc(sizeof(float) * (size_t)ew * eh);
+        s->econd = (float *)malloc(sizeof(float) * (size_t)eh * (ew + 1));
+        s->emarg = (float *)malloc(sizeof(float) * (eh + 1));
+        double *rows = (double *)malloc(sizeof(double) * eh);
+        for (uint32_t y = 0; y < eh; ++y) {
+            const double st = sin(3.14159265358979323846 * (y + 0.5) / eh);
+            double acc = 0.0;
+            float *cr = s->econd + (size_t)y * (ew + 1);
+            cr[0] = 0.0f;
+            for (uint32_t x = 0; x < ew; ++x) {
+                const float *px = &t->rgba[4 * ((size_t)y * ew + x)];
+                const double f = (0.2126 * px[0] + 0.7152 * px[1] + 0.0722 * px[2]) * st * s->env_intensity;
+                s->efunc[(size_t)y * ew + x] = (float)f;
+                acc += f;
+                cr[x + 1] = (float)acc;
+            }
+            for (uint32_t x = 1; x <= ew; ++x) cr[x] = acc > 0.0 ? (float)(cr[x] / acc) : (float)x / ew;
+            cr[ew] = 1.0f;
+            rows[y] = acc / ew;
+            s->eint += acc;
+        }
+        double racc = 0.0;
+        s->emarg[0] = 0.0f;
+        for (uint32_t y = 0; y < eh; ++y) {
+            racc += rows[y];
+            s->emarg[y + 1] = (float)racc;
+        }
+        for (uint32_t y = 1; y <= eh; ++y) s->emarg[y] = racc > 0.0 ? (float)(s->emarg[y] / racc) : (float)y / eh;
+        s->emarg[eh] = 1.0f;
+        s->eint /= (double)ew * eh;
+        free(rows);
+    }
+    if (!(s->eint > 0.0)) s->env_tex = s->env_tex >= 0 && s->eint > 0.0 ? s->env_tex : -1;
+    s->p_env = s->env_tex >= 0 ? (s->nemit > 0 ? 0.5f : 1.0f) : 0.0f;
     return port_rc_build(s->rc);
 }
 
@@ -428,6 +543,81 @@ void port_pixel_shifts(const pt_camera_desc *c, float *out) {
     memcpy(out, v, sizeof(v));
 }
 
+/* ---- extended estimator helpers (same definitions as the CUDA path tracer) ----------- */
+static float luminance3(f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+static float mis_power(float a, float b) {
+    const float a2 = a * a, b2 = b * b;
+    return a2 + b2 > 0.0f ? a2 / (a2 + b2) : 0.0f;
+}
+static void dir_to_uv(f3 d, float *u, float *v) {
+    float phi = atan2f(d.z, d.x);
+    if (phi < 0.0f) phi += TWO_PI;
+    *u = phi * (1.0f / TWO_PI);
+    *v = acosf(fminf(fmaxf(d.y, -1.0f), 1.0f)) * ONE_OVER_PI;
+}
+static f3 env_radiance(const port_pt *s, f3 d) {
+    float u, v;
+    dir_to_uv(d, &u, &v);
+    const f4 c = rgbal(&s->tex[s->env_tex], u, v);
+    return mk3(c.x * s->env_intensity, c.y * s->env_intensity, c.z * s->env_intensity);
+}
+static float env_pdf(const port_pt *s, f3 d) {
+    float u, v;
+    dir_to_uv(d, &u, &v);
+    const float st = sqrtf(fmaxf(0.0f, 1.0f - d.y * d.y));
+    if (st <= 0.0f || s->eint <= 0.0) return 0.0f;
+    uint32_t x = (uint32_t)(u * s->ew), y = (uint32_t)(v * s->eh);
+    if (x > s->ew - 1) x = s->ew - 1;
+    if (y > s->eh - 1) y = s->eh - 1;
+    const float p_uv = s->efunc[(size_t)y * s->ew + x] / (float)s->eint;
+    return p_uv / (2.0f * PI_F * PI_F * st);
+}
+static float sample_cdf(const float *cdf, uint32_t n, float u, uint32_t *idx) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (cdf[mid] <= u) lo = mid;
+        else hi = mid;
+    }
+    *idx = lo;
+    const float w = cdf[lo + 1] - cdf[lo];
+    float du = w > 0.0f ? (u - cdf[lo]) / w : 0.0f;
+    du = fminf(fmaxf(du, 0.0f), 0.99999994f);
+    return ((float)lo + du) / (float)n;
+}
+static f3 env_sample(const port_pt *s, float u0, float u1, float *pdf) {
+    uint32_t row, col;
+    const float v = sample_cdf(s->emarg, s->eh, u0, &row);
+    const float u = sample_cdf(s->econd + (size_t)row * (s->ew + 1), s->ew, u1, &col);
+    const float theta = v * PI_F, phi = u * TWO_PI;
+    const float st = sinf(theta);
+    const f3 d = mk3(st * cosf(phi), cosf(theta), st * sinf(phi));
+    const float p_uv = s->efunc[(size_t)row * s->ew + col] / (float)s->eint;
+    *pdf = st > 0.0f ? p_uv / (2.0f * PI_F * PI_F * st) : 0.0f;
+    return d;
+}
+static int emitter_pick(const port_pt *s, float u) {
+    int lo = 0, hi = s->nemit - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s->ecdf[mid] <= u) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+static float ggx_pdf(f3 wo, f3 base, float rough, float metal, f3 wi) {
+    if (wi.z < 0.0f) return 0.0f;
+    const float pdiff = 1.0f / (dot3(base, mk3(1, 1, 1)) / 3.0f + 1.0f);
+    const float ps = pdiff + metal * (1.0f - pdiff);
+    const float alpha = alpha_from_roughness(rough);
+    const f3 h = norm3(add3(wi, wo));
+    const float NdotH = fmaxf_g(h.z, 0.0f);
+    const float VdotH = fmaxf_g(dot3(wi, h), 0.0f);
+    const float pdfSpec = ggx_D(NdotH, alpha) * NdotH / (4.0f * fmaxf_g(0.0001f, VdotH));
+    const float pd = ONE_OVER_PI * fmaxf_g(wi.z, 0.0f);
+    return pd + ps * (pdfSpec - pd);
+}
+
 /* ---- render ------------------------------------------------------------------------------ */
 typedef struct {
     int obj;
@@ -503,6 +693,8 @@ typedef struct {
     uint32_t W, H, spp, depth, cx, cy;
     float cellx, celly;
     uint32_t seed_lo, seed_hi;
+    int mode;
+    float clamp;
     float *image;
     size_t y0, y1;
     uint64_t rays[3];
@@ -524,13 +716,21 @@ static void render_pixel(job_t *j, uint32_t x, uint32_t y) {
         const f3 eye = mk3(j->eye[0], j->eye[1], j->eye[2]);
         f3 pos = eye, dir = norm3(sub3(world, eye));
         f3 color = mk3(0, 0, 0), atten = mk3(1, 1, 1);
+        const int ext = j->mode == PT_MODE_EXTENDED;
+        float prev_pdf = 0.0f;
         for (uint32_t did = 0; did < j->depth; ++did) {
             float r[8];
             ray8(r, pos, 1e-4f, dir, 1e8f);
             port_hit h;
             j->rays[did == 0 ? 0 : 1]++;
             if (!port_rc_closest1(s->rc, r, &h)) {
-                color = add3(color, mul3(atten, background(s, dir, nx, ny, did == 0)));
+                if (ext && s->env_tex >= 0) {
+                    float wgt = 1.0f;
+                    if (did > 0 && prev_pdf > 0.0f) wgt = mis_power(prev_pdf, s->p_env * env_pdf(s, dir));
+                    color = add3(color, mul3(atten, scl3(wgt, env_radiance(s, dir))));
+                } else {
+                    color = add3(color, mul3(atten, background(s, dir, nx, ny, did == 0)));
+                }
                 break;
             }
             const surf_t sh = surface(s, &h);
@@ -546,7 +746,19 @@ static void render_pixel(job_t *j, uint32_t x, uint32_t y) {
                 continue;
             }
             if (mat->type == PT_MAT_EMISSIVE) {
-                color = add3(color, mul3(atten, mk3(bcol.x, bcol.y, bcol.z)));
+                f3 le = mk3(bcol.x, bcol.y, bcol.z);
+                if (ext && did > 0 && prev_pdf > 0.0f && s->nemit > 0) {
+                    const f3 p0 = mk3(mesh->pos[3 * sh.i0], mesh->pos[3 * sh.i0 + 1], mesh->pos[3 * sh.i0 + 2]);
+                    const f3 p1 = mk3(mesh->pos[3 * sh.i1], mesh->pos[3 * sh.i1 + 1], mesh->pos[3 * sh.i1 + 2]);
+                    const f3 p2 = mk3(mesh->pos[3 * sh.i2], mesh->pos[3 * sh.i2 + 1], mesh->pos[3 * sh.i2 + 2]);
+                    const f3 ng = norm3(mat3mul(o->invtp, cross3(sub3(p1, p0), sub3(p2, p0))));
+                    const float cosl = fabsf(dot3(ng, dir));
+                    const float pl = cosl > 0.0f
+                                         ? (1.0f - s->p_env) * luminance3(le) * h.t * h.t / ((float)s->epower * cosl)
+                                         : 0.0f;
+                    le = scl3(mis_power(prev_pdf, pl), le);
+                }
+                color = add3(color, mul3(atten, le));
                 break;
             }
             /* buildLocalFrame */
@@ -589,8 +801,53 @@ static void render_pixel(job_t *j, uint32_t x, uint32_t y) {
                     color = add3(color, mul3(atten, ill));
                 }
             }
+            if (ext && (s->nemit > 0 || s->env_tex >= 0)) {
+                const u4 r2 = philox((u4){pixel, sid, did + 1u, 1u}, j->seed_lo, j->seed_hi);
+                const float usel = u01(r2.x);
+                const f3 ps = add3(p, scl3(0.001f, t2));
+                f3 ld = mk3(0, 0, 1), le = mk3(0, 0, 0);
+                float pl = 0.0f, dist = 1e8f;
+                int ok = 0;
+                if (s->env_tex >= 0 && (s->nemit == 0 || usel < s->p_env)) {
+                    ld = env_sample(s, u01(r2.y), u01(r2.z), &pl);
+                    pl *= s->p_env;
+                    le = env_radiance(s, ld);
+                    ok = pl > 0.0f;
+                } else if (s->nemit > 0) {
+                    float ue = s->env_tex >= 0 ? (usel - s->p_env) / (1.0f - s->p_env) : usel;
+                    ue = fminf(fmaxf(ue, 0.0f), 0.99999994f);
+                    const emitter_t *em = &s->emitters[emitter_pick(s, ue)];
+                    const float su = sqrtf(u01(r2.y)), b1 = 1.0f - su, b2 = u01(r2.z) * su;
+                    const f3 e1 = mk3(em->e1[0], em->e1[1], em->e1[2]), e2 = mk3(em->e2[0], em->e2[1], em->e2[2]);
+                    const f3 q = add3(add3(mk3(em->v0[0], em->v0[1], em->v0[2]), scl3(b1, e1)), scl3(b2, e2));
+                    const f3 dq = sub3(q, ps);
+                    const float d2 = dot3(dq, dq);
+                    dist = sqrtf(d2);
+                    ld = mk3(dq.x / dist, dq.y / dist, dq.z / dist);
+                    const f3 ng = norm3(cross3(e1, e2));
+                    const float cosl = fabsf(dot3(ng, ld));
+                    le = mk3(em->emission[0], em->emission[1], em->emission[2]);
+                    pl = cosl > 0.0f ? (1.0f - s->p_env) * em->lum * d2 / ((float)s->epower * cosl) : 0.0f;
+                    ok = pl > 0.0f && dist > 0.0f;
+                }
+                if (ok) {
+                    const f3 lwi = norm3(mk3(dot3(t0, ld), dot3(t1, ld), dot3(t2, ld)));
+                    const f3 ev = ggx_eval(wo, base, rmao.x, rmao.y, lwi);
+                    const float pb = ggx_pdf(wo, base, rmao.x, rmao.y, lwi);
+                    const float wgt = mis_power(pl, pb) / pl;
+                    const f3 contrib = scl3(wgt, mul3(atten, mul3(ev, le)));
+                    if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
+                        j->rays[2]++;
+                        uint64_t extra = 0;
+                        const int vis = check_visibility(s, ps, ld, dist < 1e8f ? dist * (1.0f - 1e-3f) : 1e8f, &extra);
+                        j->rays[2] += extra - 1;
+                        if (vis) color = add3(color, contrib);
+                    }
+                }
+            }
             f3 wi;
             const f3 w = ggx_sample_eval(wo, base, rmao.x, rmao.y, u01(rnd.y), u01(rnd.z), u01(rnd.w), &wi);
+            if (ext) prev_pdf = (w.x > 0.0f || w.y > 0.0f || w.z > 0.0f) ? ggx_pdf(wo, base, rmao.x, rmao.y, wi) : 0.0f;
             const f3 nd = norm3(add3(add3(scl3(wi.x, t0), scl3(wi.y, t1)), scl3(wi.z, t2)));
             atten = mul3(atten, w);
             if (did < j->depth - 1) {
@@ -598,10 +855,17 @@ static void render_pixel(job_t *j, uint32_t x, uint32_t y) {
                 dir = norm3(nd);
             }
         }
-        /* render.rgb(x,y) += min(sampleColor, 5.0f) */
-        px[0] += (5.0f < color.x) ? 5.0f : color.x;
-        px[1] += (5.0f < color.y) ? 5.0f : color.y;
-        px[2] += (5.0f < color.z) ? 5.0f : color.z;
+        /* render.rgb(x,y) += min(sampleColor, 5.0f) (clamp value: an option of the extended mode) */
+        if (j->clamp > 0.0f) {
+            const float cl = j->clamp;
+            px[0] += (cl < color.x) ? cl : color.x;
+            px[1] += (cl < color.y) ? cl : color.y;
+            px[2] += (cl < color.z) ? cl : color.z;
+        } else {
+            px[0] += color.x;
+            px[1] += color.y;
+            px[2] += color.z;
+        }
     }
     px[0] = px[0] / (float)j->spp;
     px[1] = px[1] / (float)j->spp;
@@ -617,6 +881,11 @@ static void *render_rows(void *arg) {
 
 int port_pt_render(port_pt *s, const pt_camera_desc *cam, uint32_t samples, uint32_t depth, uint64_t seed, float *image,
                    uint32_t W, uint32_t H, int threads, uint64_t *rays_out) {
+    return port_pt_render_ex(s, cam, samples, depth, seed, image, W, H, threads, rays_out, PT_MODE_REFERENCE, 5.0f);
+}
+
+int port_pt_render_ex(port_pt *s, const pt_camera_desc *cam, uint32_t samples, uint32_t depth, uint64_t seed,
+                      float *image, uint32_t W, uint32_t H, int threads, uint64_t *rays_out, int mode, float clamp) {
     if (!s || !s->rc || !cam || !image || samples == 0 || W == 0 || H == 0) return -1;
     job_t base;
     memset(&base, 0, sizeof(base));
@@ -642,6 +911,8 @@ int port_pt_render(port_pt *s, const pt_camera_desc *cam, uint32_t samples, uint
     base.depth = depth;
     base.seed_lo = (uint32_t)seed;
     base.seed_hi = (uint32_t)(seed >> 32);
+    base.mode = mode;
+    base.clamp = clamp;
     base.image = image;
     if (threads <= 0) threads = port_default_threads();
     size_t count = (size_t)threads < H ? (size_t)threads : H;

@@ -29,6 +29,10 @@ int port_pt_commit(port_pt *s);
  * counters: primary, bounce, shadow) may be NULL. threads <= 0: hardware threads - 1. */
 int port_pt_render(port_pt *s, const pt_camera_desc *cam, uint32_t samples, uint32_t depth, uint64_t seed, float *image,
                    uint32_t w, uint32_t h, int threads, uint64_t *rays_out);
+/* Extended estimator (PT_MODE_EXTENDED): environment map and render options. */
+int port_pt_set_environment(port_pt *s, uint32_t tex, float intensity);
+int port_pt_render_ex(port_pt *s, const pt_camera_desc *cam, uint32_t samples, uint32_t depth, uint64_t seed,
+                      float *image, uint32_t w, uint32_t h, int threads, uint64_t *rays_out, int mode, float clamp);
 /* MaterialGGX::eval / sampleAndEval with given uniforms (see include/rendu_gb300.h). */
 void port_ggx_eval(const float *cases, size_t n, float *out);
 void port_ggx_sample(const float *cases, const float *uniforms, size_t n, float *out);

@@ -20,6 +20,8 @@ RT_ERR_TIMEOUT = 4
 RT_ERR_STATE = 5
 RT_ERR_OVERFLOW = 6
 RT_FLAG_DEVICE_PTRS = 0x1
+PT_MODE_REFERENCE = 0
+PT_MODE_EXTENDED = 1
 RT_NO_HIT = 0xFFFFFFFF
 
 _STATUS_NAMES = {1: "RT_ERR_ARG", 2: "RT_ERR_OOM", 3: "RT_ERR_CUDA", 4: "RT_ERR_TIMEOUT", 5: "RT_ERR_STATE",
@@ -59,6 +61,10 @@ class pt_camera_desc(C.Structure):
                 ("ratio", C.c_float)]
 
 
+class pt_render_options(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("clamp", C.c_float)]
+
+
 class pt_render_stats(C.Structure):
     _fields_ = [("primary_rays", C.c_uint64), ("bounce_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("paths", C.c_uint64), ("device_ms", C.c_float)]
@@ -92,6 +98,10 @@ _SIGS = {
     "pt_render": ([_VP, C.POINTER(pt_camera_desc), C.c_uint32, C.c_uint32, C.c_uint64, _VP, C.c_uint32, C.c_uint32,
                    C.c_uint32, _VP, C.c_uint32], C.c_int),
     "pt_get_render_stats": ([_VP, C.POINTER(pt_render_stats)], C.c_int),
+    "pt_scene_set_environment": ([_VP, C.c_uint32, C.c_float], C.c_int),
+    "pt_render_ex": ([_VP, C.POINTER(pt_camera_desc), C.c_uint32, C.c_uint32, C.c_uint64, _VP, C.c_uint32, C.c_uint32,
+                      C.c_uint32, C.POINTER(pt_render_options), _VP, C.c_uint32], C.c_int),
+    "rt_visible_noalloc": ([_VP, _VP, C.c_size_t, _VP, _VP], C.c_int),
     "pt_scene_raycaster": ([_VP], _VP),
     "pt_material_eval": ([_VP, C.c_size_t, _VP, C.c_int], C.c_int),
     "pt_material_sample": ([_VP, _VP, C.c_size_t, _VP, C.c_int], C.c_int),

@@ -117,7 +117,8 @@ int pt_scene_destroy(pt_scene *s) {
     if (!s) return RT_OK;
     DeviceGuard g(s->device);
     if (s->rc) rt_destroy(s->rc);
-    for (DevBuf *b : {&s->d_objects, &s->d_meshes, &s->d_materials, &s->d_tex, &s->d_texels, &s->d_normals,
+    for (DevBuf *b : {&s->d_positions, &s->d_emitters, &s->d_emitter_cdf, &s->d_env_marg, &s->d_env_cond,
+                      &s->d_env_func, &s->d_objects, &s->d_meshes, &s->d_materials, &s->d_tex, &s->d_texels, &s->d_normals,
                       &s->d_tangents, &s->d_bitangents, &s->d_uvs, &s->d_indices, &s->d_lights, &s->w_atten,
                       &s->w_color, &s->w_ndc, &s->w_qray0, &s->w_qray1, &s->w_qpath0, &s->w_qpath1, &s->w_hits,
                       &s->w_sray, &s->w_scontrib, &s->w_counters, &s->w_stats, &s->w_accum, &s->w_image})
@@ -221,6 +222,17 @@ int pt_scene_set_background(pt_scene *s, int32_t mode, const float *color, const
     return RT_OK;
 }
 
+int pt_scene_set_environment(pt_scene *s, uint32_t tex_id, float intensity) {
+    clear_error();
+    if (!s) return arg_error("null scene");
+    if (tex_id >= s->textures.size()) return arg_error("environment texture id out of range");
+    if (!(intensity >= 0.0f)) return arg_error("environment intensity must be >= 0");
+    s->env_tex = (int)tex_id;
+    s->env_intensity = intensity;
+    s->committed = false;
+    return RT_OK;
+}
+
 int pt_scene_commit(pt_scene *s) {
     clear_error();
     if (!s) return arg_error("null scene");
@@ -240,13 +252,14 @@ int pt_scene_commit(pt_scene *s) {
     cudaStream_t st = s->rc->stream;
 
     std::vector<PtMesh> meshes(s->meshes.size());
-    std::vector<float> nrm, tan, bit, uv;
+    std::vector<float> posp, nrm, tan, bit, uv;
     std::vector<uint32_t> idx;
     for (size_t k = 0; k < s->meshes.size(); ++k) {
         const HostMesh &m = s->meshes[k];
         meshes[k].first_vertex = (uint32_t)(nrm.size() / 3);
         meshes[k].first_index = (uint32_t)idx.size();
         meshes[k].has_uv = m.uv.empty() ? 0 : 1;
+        posp.insert(posp.end(), m.pos.begin(), m.pos.end());
         nrm.insert(nrm.end(), m.nrm.begin(), m.nrm.end());
         tan.insert(tan.end(), m.tan.begin(), m.tan.end());
         bit.insert(bit.end(), m.bit.begin(), m.bit.end());
@@ -306,6 +319,96 @@ int pt_scene_commit(pt_scene *s) {
         l.half_inner = 0.5f * d.inner_angle;  // SpotLight.cpp:8
         l.half_outer = 0.5f * d.outer_angle;
     }
+    // Extended estimator: emissive triangles in world space with a power CDF.
+    std::vector<PtEmitter> emitters;
+    std::vector<float> ecdf;
+    double epower = 0.0;
+    for (size_t k = 0; k < s->objects.size(); ++k) {
+        const HostObject &o = s->objects[k];
+        const pt_material_desc &md = s->materials[o.material];
+        if (md.type != PT_MAT_EMISSIVE) continue;
+        const HostTex &t = s->textures[md.tex[0]];
+        double e[3] = {0, 0, 0};
+        const size_t np = (size_t)t.w * t.h;
+        for (size_t q = 0; q < np; ++q)
+            for (int c = 0; c < 3; ++c) e[c] += t.rgba[4 * q + c];
+        for (int c = 0; c < 3; ++c) e[c] /= (double)np;
+        const double lum = 0.2126 * e[0] + 0.7152 * e[1] + 0.0722 * e[2];
+        if (!(lum > 0.0)) continue;
+        const HostMesh &m = s->meshes[o.mesh];
+        auto xf = [&](uint32_t v, double out[3]) {
+            const float *pp = &m.pos[3 * (size_t)v];
+            for (int r2 = 0; r2 < 3; ++r2)
+                out[r2] = (double)o.model[r2] * pp[0] + (double)o.model[4 + r2] * pp[1] + (double)o.model[8 + r2] * pp[2] +
+                          (double)o.model[12 + r2];
+        };
+        for (size_t tri = 0; tri + 2 < m.idx.size(); tri += 3) {
+            double a[3], b[3], c[3];
+            xf(m.idx[tri], a);
+            xf(m.idx[tri + 1], b);
+            xf(m.idx[tri + 2], c);
+            const double u[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, v[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+            const double cr[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+            const double area = 0.5 * std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+            if (!(area > 0.0)) continue;
+            PtEmitter em;
+            for (int q = 0; q < 3; ++q) {
+                em.v0[q] = (float)a[q];
+                em.e1[q] = (float)u[q];
+                em.e2[q] = (float)v[q];
+                em.emission[q] = (float)e[q];
+            }
+            em.lum = (float)lum;
+            emitters.push_back(em);
+            epower += area * lum;
+            ecdf.push_back((float)epower);
+        }
+    }
+    for (float &c : ecdf) c = (float)(c / epower);
+    if (!ecdf.empty()) ecdf.back() = 1.0f;
+    // Environment: piecewise-constant distribution over texels, weight = luminance x sin(theta).
+    std::vector<float> efunc, emarg, econd;
+    double eint = 0.0;
+    uint32_t ew = 0, eh = 0;
+    if (s->env_tex >= 0) {
+        const HostTex &t = s->textures[(size_t)s->env_tex];
+        ew = t.w;
+        eh = t.h;
+        efunc.resize((size_t)ew * eh);
+        econd.resize((size_t)eh * (ew + 1));
+        emarg.resize(eh + 1);
+        std::vector<double> rows(eh);
+        for (uint32_t y = 0; y < eh; ++y) {
+            const double st = std::sin(3.14159265358979323846 * (y + 0.5) / eh);
+            double acc = 0.0;
+            econd[(size_t)y * (ew + 1)] = 0.0f;
+            for (uint32_t x = 0; x < ew; ++x) {
+                const float *px = &t.rgba[4 * ((size_t)y * ew + x)];
+                const double f = (0.2126 * px[0] + 0.7152 * px[1] + 0.0722 * px[2]) * st * s->env_intensity;
+                efunc[(size_t)y * ew + x] = (float)f;
+                acc += f;
+                econd[(size_t)y * (ew + 1) + x + 1] = (float)acc;
+            }
+            for (uint32_t x = 1; x <= ew; ++x)
+                econd[(size_t)y * (ew + 1) + x] = acc > 0.0 ? (float)(econd[(size_t)y * (ew + 1) + x] / acc) : (float)x / ew;
+            econd[(size_t)y * (ew + 1) + ew] = 1.0f;
+            rows[y] = acc / ew;
+            eint += acc;
+        }
+        double racc = 0.0;
+        emarg[0] = 0.0f;
+        for (uint32_t y = 0; y < eh; ++y) {
+            racc += rows[y];
+            emarg[y + 1] = (float)racc;
+        }
+        for (uint32_t y = 1; y <= eh; ++y) emarg[y] = racc > 0.0 ? (float)(emarg[y] / racc) : (float)y / eh;
+        emarg[eh] = 1.0f;
+        eint /= (double)ew * eh;  // mean over the unit square
+    }
+    if ((r = upload(s->d_positions, posp, st)) || (r = upload(s->d_emitters, emitters, st)) ||
+        (r = upload(s->d_emitter_cdf, ecdf, st)) || (r = upload(s->d_env_func, efunc, st)) ||
+        (r = upload(s->d_env_marg, emarg, st)) || (r = upload(s->d_env_cond, econd, st)))
+        return r;
     if ((r = upload(s->d_meshes, meshes, st)) || (r = upload(s->d_normals, nrm, st)) || (r = upload(s->d_tangents, tan, st)) ||
         (r = upload(s->d_bitangents, bit, st)) || (r = upload(s->d_uvs, uv, st)) || (r = upload(s->d_indices, idx, st)) ||
         (r = upload(s->d_objects, objects, st)) || (r = upload(s->d_materials, mats, st)) ||
@@ -325,6 +428,7 @@ int pt_scene_commit(pt_scene *s) {
     d.materials = s->d_materials.as<PtMaterial>();
     d.textures = s->d_tex.as<PtTex>();
     d.texels = s->d_texels.as<float4>();
+    d.positions = s->d_positions.as<float>();
     d.normals = s->d_normals.as<float>();
     d.tangents = s->d_tangents.as<float>();
     d.bitangents = s->d_bitangents.as<float>();
@@ -337,6 +441,19 @@ int pt_scene_commit(pt_scene *s) {
     std::memcpy(d.bg_color, s->bg_color, sizeof(d.bg_color));
     std::memcpy(d.bg_tex, s->bg_tex, sizeof(d.bg_tex));
     (void)any_shadow;
+    d.emitters = s->d_emitters.as<PtEmitter>();
+    d.emitter_cdf = s->d_emitter_cdf.as<float>();
+    d.nemitters = (int)emitters.size();
+    d.emit_power = (float)epower;
+    d.env_tex = (s->env_tex >= 0 && eint > 0.0) ? s->env_tex : -1;
+    d.env_intensity = s->env_intensity;
+    d.env_w = ew;
+    d.env_h = eh;
+    d.env_marg = s->d_env_marg.as<float>();
+    d.env_cond = s->d_env_cond.as<float>();
+    d.env_func = s->d_env_func.as<float>();
+    d.env_integral = (float)eint;
+    d.p_env = d.env_tex >= 0 ? (d.nemitters > 0 ? 0.5f : 1.0f) : 0.0f;
     s->committed = true;
     return RT_OK;
 }
@@ -391,6 +508,12 @@ int pt_get_render_stats(const pt_scene *s, pt_render_stats *out) {
 
 int pt_render(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, uint32_t depth, uint64_t seed, float *image,
               uint32_t width, uint32_t height, uint32_t components, void *stream, uint32_t flags) {
+    return pt_render_ex(s, camera, samples, depth, seed, image, width, height, components, nullptr, stream, flags);
+}
+
+int pt_render_ex(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, uint32_t depth, uint64_t seed,
+                 float *image, uint32_t width, uint32_t height, uint32_t components, const pt_render_options *opts,
+                 void *stream, uint32_t flags) {
     clear_error();
     if (!s || !camera || !image) return arg_error("null argument");
     if (!s->committed) {
@@ -425,6 +548,9 @@ int pt_render(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, uint3
     f.depth = depth;
     f.seed_lo = (uint32_t)seed;
     f.seed_hi = (uint32_t)(seed >> 32);
+    f.mode = opts ? opts->mode : PT_MODE_REFERENCE;
+    f.clamp = opts ? opts->clamp : 5.0f;
+    if (f.mode != PT_MODE_REFERENCE && f.mode != PT_MODE_EXTENDED) return arg_error("unknown render mode");
     // Wave: every pixel x S samples, S a power of two dividing spp, about 8M paths.
     const uint64_t target = 1ull << 23;
     uint32_t S = 1;
@@ -437,8 +563,8 @@ int pt_render(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, uint3
         int r = RT_OK;
         if ((r = s->w_atten.reserve(P * 16)) || (r = s->w_color.reserve(P * 16)) || (r = s->w_ndc.reserve(P * 8)) ||
             (r = s->w_qray0.reserve(P * 32)) || (r = s->w_qray1.reserve(P * 32)) || (r = s->w_qpath0.reserve(P * 4)) ||
-            (r = s->w_qpath1.reserve(P * 4)) || (r = s->w_hits.reserve(P * 16)) || (r = s->w_sray.reserve(P * 32)) ||
-            (r = s->w_scontrib.reserve(P * 16)))
+            (r = s->w_qpath1.reserve(P * 4)) || (r = s->w_hits.reserve(P * 16)) || (r = s->w_sray.reserve(2 * P * 32)) ||
+            (r = s->w_scontrib.reserve(2 * P * 16)))
             return r;
         s->wave_cap = P;
     }
@@ -490,7 +616,10 @@ int pt_render(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, uint3
                 break;
             }
             r = pt_launch_shade(s->dev, f, w, cur, did, cap, st);
-            if (r == RT_OK && s->dev.nlights > 0) r = pt_launch_shadow(s->dev, w, cap, st);
+            // Up to two shadow rays per path and bounce (analytic light + emitter/environment).
+            if (r == RT_OK && (s->dev.nlights > 0 || (f.mode == PT_MODE_EXTENDED &&
+                                                       (s->dev.nemitters > 0 || s->dev.env_tex >= 0))))
+                r = pt_launch_shadow(s->dev, w, 2 * cap, st);
             cur ^= 1;
         }
         if (r == RT_OK) r = pt_launch_accumulate(f, w, st);

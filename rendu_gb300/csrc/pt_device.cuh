@@ -85,6 +85,13 @@ struct PtLight {
     float radius, half_inner, half_outer;
 };
 
+// Emissive triangle in world space (extended estimator).
+struct PtEmitter {
+    float v0[3], e1[3], e2[3];
+    float emission[3];
+    float lum;  // luminance of the emission
+};
+
 struct PtScene {
     const BvhNode *nodes;
     const BvhTri *tris;
@@ -96,7 +103,7 @@ struct PtScene {
     const PtMaterial *materials;
     const PtTex *textures;
     const float4 *texels;
-    const float *normals, *tangents, *bitangents, *uvs;
+    const float *positions, *normals, *tangents, *bitangents, *uvs;  // model space, per mesh vertex
     const uint32_t *indices;
     const PtLight *lights;
     int nlights;
@@ -104,6 +111,19 @@ struct PtScene {
     int bg_mode;
     float bg_color[3];
     uint32_t bg_tex[6];
+    // Extended estimator: emitter table + power CDF, environment map + 2-D distribution.
+    const PtEmitter *emitters;
+    const float *emitter_cdf;  // inclusive cumulative, last = 1
+    int nemitters;
+    float emit_power;          // sum of area x luminance
+    int env_tex;               // -1: none
+    float env_intensity;
+    uint32_t env_w, env_h;
+    const float *env_marg;     // env_h + 1 cumulative (first 0, last 1)
+    const float *env_cond;     // env_h rows of env_w + 1 cumulative
+    const float *env_func;     // env_h x env_w piecewise-constant weights
+    float env_integral;        // mean of env_func over the unit square
+    float p_env;               // probability of sampling the environment in NEE
 };
 
 // ---- textures ----------------------------------------------------------------------------
@@ -272,6 +292,22 @@ __device__ __forceinline__ f3 ggx_sample_eval(f3 wo, f3 base, float roughness, f
     return mk(brdf.x / pdf, brdf.y / pdf, brdf.z / pdf);
 }
 
+// Mixture pdf of ggx_sample_eval for a given wi (the `pdf` of MaterialGGX.cpp:86-87),
+// used by the extended estimator's multiple importance sampling.
+__device__ __forceinline__ float ggx_pdf(f3 wo, f3 base, float roughness, float metallic, f3 wi) {
+    if (wi.z < 0.0f) return 0.0f;
+    const float pmean = (base.x + base.y + base.z) / 3.0f;
+    const float pdiff = 1.0f / (pmean + 1.0f);
+    const float probaSpecular = pdiff + (1.0f - pdiff) * metallic;
+    const float alpha = alpha_from_roughness(roughness);
+    const f3 h = normalize(wi + wo);
+    const float NdotH = fmaxf(h.z, 0.0f);
+    const float VdotH = fmaxf(dot(wi, h), 0.0f);
+    const float pdfSpec = ggx_D(NdotH, alpha) * NdotH / (4.0f * fmaxf(0.0001f, VdotH));
+    const float pd = kOneOverPi * fmaxf(wi.z, 0.0f);
+    return pd + (pdfSpec - pd) * probaSpecular;
+}
+
 // MaterialGGX::eval (MaterialGGX.cpp:94-101).
 __device__ __forceinline__ f3 ggx_eval(f3 wo, f3 base, float roughness, float metallic, f3 wi) {
     if (wi.z < 0.0f) return mk(0.0f, 0.0f, 0.0f);
@@ -305,6 +341,77 @@ __device__ __forceinline__ f3 light_sample(const PtLight &l, f3 p, float &dist, 
     const float ang = fminf(fmaxf((currentCos - outerCos) / (innerCos - outerCos), 0.0f), 1.0f);
     atten = ang * num * num;
     return d;
+}
+
+// ---- extended estimator: environment map and emitters --------------------------------------
+__device__ __forceinline__ float luminance(f3 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+
+__device__ __forceinline__ float mis_power(float a, float b) {
+    const float a2 = a * a, b2 = b * b;
+    return a2 + b2 > 0.0f ? a2 / (a2 + b2) : 0.0f;
+}
+
+// Direction <-> equirectangular (u, v): d = (sin t cos p, cos t, sin t sin p), u = p / 2pi, v = t / pi.
+__device__ __forceinline__ void dir_to_uv(f3 d, float &u, float &v) {
+    float phi = atan2f(d.z, d.x);
+    if (phi < 0.0f) phi += kTwoPi;
+    u = phi * (1.0f / kTwoPi);
+    v = acosf(fminf(fmaxf(d.y, -1.0f), 1.0f)) * kOneOverPi;
+}
+
+__device__ __forceinline__ f3 env_radiance(const PtScene &s, f3 d) {
+    float u, v;
+    dir_to_uv(d, u, v);
+    const float4 c = tex_rgbal(s, (uint32_t)s.env_tex, u, v);
+    return mk(c.x * s.env_intensity, c.y * s.env_intensity, c.z * s.env_intensity);
+}
+
+// Solid-angle pdf of env_sample for direction d (piecewise-constant in (u, v)).
+__device__ __forceinline__ float env_pdf(const PtScene &s, f3 d) {
+    float u, v;
+    dir_to_uv(d, u, v);
+    const float st = sqrtf(fmaxf(0.0f, 1.0f - d.y * d.y));
+    if (st <= 0.0f || s.env_integral <= 0.0f) return 0.0f;
+    const uint32_t x = min((uint32_t)(u * s.env_w), s.env_w - 1), y = min((uint32_t)(v * s.env_h), s.env_h - 1);
+    const float p_uv = s.env_func[(size_t)y * s.env_w + x] / s.env_integral;
+    return p_uv / (2.0f * kPi * kPi * st);
+}
+
+// Sample a piecewise-constant 1-D distribution given its cumulative table (n + 1 entries).
+__device__ __forceinline__ float sample_cdf(const float *cdf, uint32_t n, float u, uint32_t &idx) {
+    uint32_t lo = 0, hi = n;  // largest i with cdf[i] <= u
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (cdf[mid] <= u) lo = mid;
+        else hi = mid;
+    }
+    idx = lo;
+    const float w = cdf[lo + 1] - cdf[lo];
+    const float du = w > 0.0f ? (u - cdf[lo]) / w : 0.0f;
+    return ((float)lo + fminf(fmaxf(du, 0.0f), 0.99999994f)) / (float)n;
+}
+
+__device__ __forceinline__ f3 env_sample(const PtScene &s, float u0, float u1, float &pdf) {
+    uint32_t row, col;
+    const float v = sample_cdf(s.env_marg, s.env_h, u0, row);
+    const float u = sample_cdf(s.env_cond + (size_t)row * (s.env_w + 1), s.env_w, u1, col);
+    const float theta = v * kPi, phi = u * kTwoPi;
+    const float st = sinf(theta);
+    const f3 d = mk(st * cosf(phi), cosf(theta), st * sinf(phi));
+    const float p_uv = s.env_func[(size_t)row * s.env_w + col] / s.env_integral;
+    pdf = st > 0.0f ? p_uv / (2.0f * kPi * kPi * st) : 0.0f;
+    return d;
+}
+
+// Pick an emitter by power (inclusive CDF) and a uniform point on it.
+__device__ __forceinline__ int emitter_pick(const PtScene &s, float u) {
+    int lo = 0, hi = s.nemitters - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s.emitter_cdf[mid] <= u) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
 }
 
 // ---- geometry helpers --------------------------------------------------------------------

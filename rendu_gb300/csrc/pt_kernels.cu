@@ -90,11 +90,18 @@ __device__ __forceinline__ float2 interp_uv(const float *a, const SurfaceHit &h)
                        h.w * a[2 * h.i0 + 1] + h.u * a[2 * h.i1 + 1] + h.v * a[2 * h.i2 + 1]);
 }
 
+__device__ __forceinline__ void push_shadow(const PtWave &w, uint32_t slot, f3 o, f3 d, float tmax, f3 c, uint32_t path) {
+    w.sray[slot] = rt_ray{o.x, o.y, o.z, 0.001f, d.x, d.y, d.z, tmax};
+    w.scontrib[slot] = make_float4(c.x, c.y, c.z, __uint_as_float(path));
+}
+
+template <bool EXT>
 __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, int cur, uint32_t did) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = w.counters[cur];
     if (i == 0) atomicAdd(&w.stats[did == 0 ? 0 : 1], (unsigned long long)n);  // rays traced this bounce
     if (i >= n) return;
+    constexpr bool ext = EXT;
     const int nxt = cur ^ 1;
     const uint32_t path = w.qpath[cur][i];
     const rt_ray ray = w.qray[cur][i];
@@ -103,14 +110,24 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
     const f3 dir = mk(ray.dx, ray.dy, ray.dz);
     float4 c4 = w.color[path], a4 = w.atten[path];
     f3 color = mk(c4.x, c4.y, c4.z), atten = mk(a4.x, a4.y, a4.z);
-    bool cont = false, shadow = false;
-    f3 next_o = pos, next_d = dir, sh_o = pos, sh_d = dir, sh_c = mk(0, 0, 0);
-    float sh_max = 0.0f;
+    float prev_pdf = a4.w;  // solid-angle pdf of the BSDF sample that produced this ray (0: none)
+    bool cont = false;
+    bool sh_a = false, sh_b = false;  // analytic-light and emitter/environment shadow rays
+    f3 next_o = pos, next_d = dir;
+    f3 sa_o = pos, sa_d = dir, sa_c = mk(0, 0, 0), sb_o = pos, sb_d = dir, sb_c = mk(0, 0, 0);
+    float sa_max = 0.0f, sb_max = 0.0f;
 
     if (hit.prim == RT_NO_HIT) {
-        // PathTracer.cpp:206-209.
-        const float2 ndc = w.ndc[path];
-        color += atten * eval_background(s, dir, ndc.x, ndc.y, did == 0);
+        if (ext && s.env_tex >= 0) {
+            const f3 le = env_radiance(s, dir);
+            float wgt = 1.0f;
+            if (did > 0 && prev_pdf > 0.0f) wgt = mis_power(prev_pdf, s.p_env * env_pdf(s, dir));
+            color += atten * (le * wgt);
+        } else {
+            // PathTracer.cpp:206-209.
+            const float2 ndc = w.ndc[path];
+            color += atten * eval_background(s, dir, ndc.x, ndc.y, did == 0);
+        }
     } else {
         const SurfaceHit sh = surface(s, hit.prim, hit.u, hit.v);
         const PtObject &obj = s.objects[sh.obj];
@@ -123,7 +140,18 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
             cont = did + 1 < f.depth;
             next_o = p;
         } else if (mat.type == PT_MAT_EMISSIVE) {
-            color += atten * mk(bcol.x, bcol.y, bcol.z);  // :228-234
+            f3 le = mk(bcol.x, bcol.y, bcol.z);  // :228-234
+            if (ext && did > 0 && prev_pdf > 0.0f && s.nemitters > 0) {
+                // Solid-angle pdf with which emitter sampling would have produced this point:
+                // (area * lum / power) * (1 / area) * t^2 / |cos| = lum * t^2 / (power * |cos|).
+                const f3 p0 = ld3(s.positions, sh.i0), p1 = ld3(s.positions, sh.i1), p2 = ld3(s.positions, sh.i2);
+                const f3 ng = normalize(mat3_mul(obj.invtp, cross(p1 - p0, p2 - p0)));
+                const float cosl = fabsf(dot(ng, dir));
+                const float pl = cosl > 0.0f ? (1.0f - s.p_env) * luminance(le) * hit.t * hit.t / (s.emit_power * cosl)
+                                             : 0.0f;
+                le = le * mis_power(prev_pdf, pl);
+            }
+            color += atten * le;
         } else {
             // PathTracer::buildLocalFrame (:86-122).
             const f3 nn = normalize(interp3(s.normals, sh));
@@ -145,11 +173,12 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
             const f3 wo = normalize(mk(dot(t0, mdir), dot(t1, mdir), dot(t2, mdir)));
             const f3 base = mk(powf(bcol.x, 2.2f), powf(bcol.y, 2.2f), powf(bcol.z, 2.2f));
             const float4 rmao = tex_rgbal(s, mat.tex[2], uv.x, uv.y);
-            const U4 rnd = philox(U4{path % f.npix, f.s0 + path / f.npix, did + 1u, 0u}, f.seed_lo, f.seed_hi);
+            const uint32_t pix = path % f.npix, sid = f.s0 + path / f.npix;
+            const U4 rnd = philox(U4{pix, sid, did + 1u, 0u}, f.seed_lo, f.seed_hi);
+            const f3 ps = mk(p.x + 0.001f * t2.x, p.y + 0.001f * t2.y, p.z + 0.001f * t2.z);
             if (s.nlights > 0) {
                 // Next-event estimation on one uniformly picked analytic light (:248-272).
                 const PtLight &L = s.lights[uint_below(rnd.x, (uint32_t)s.nlights)];
-                const f3 ps = mk(p.x + 0.001f * t2.x, p.y + 0.001f * t2.y, p.z + 0.001f * t2.z);
                 float maxd, fall;
                 const f3 ld = light_sample(L, ps, maxd, fall);
                 if (fall > 0.0f) {
@@ -160,13 +189,57 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
                                       fall * ev.z * L.color[2] * inv_pdf);
                     const f3 contrib = atten * ill;
                     if (L.shadows) {
-                        shadow = true;
-                        sh_o = ps;
-                        sh_d = ld;
-                        sh_max = maxd;
-                        sh_c = contrib;
+                        sh_a = true;
+                        sa_o = ps;
+                        sa_d = ld;
+                        sa_max = maxd;
+                        sa_c = contrib;
                     } else {
                         color += contrib;
+                    }
+                }
+            }
+            if (ext && (s.nemitters > 0 || s.env_tex >= 0)) {
+                // Extended: one emitter-or-environment sample, MIS against BSDF sampling.
+                const U4 r2 = philox(U4{pix, sid, did + 1u, 1u}, f.seed_lo, f.seed_hi);
+                const float usel = u01(r2.x);
+                f3 ld, le;
+                float pl = 0.0f, dist = 1e8f;
+                bool ok = false;
+                if (s.env_tex >= 0 && (s.nemitters == 0 || usel < s.p_env)) {
+                    ld = env_sample(s, u01(r2.y), u01(r2.z), pl);
+                    pl *= s.p_env;
+                    le = env_radiance(s, ld);
+                    ok = pl > 0.0f;
+                } else if (s.nemitters > 0) {
+                    const float ue = s.env_tex >= 0 ? (usel - s.p_env) / (1.0f - s.p_env) : usel;
+                    const PtEmitter em = s.emitters[emitter_pick(s, fminf(fmaxf(ue, 0.0f), 0.99999994f))];
+                    const float su = sqrtf(u01(r2.y)), b1 = 1.0f - su, b2 = u01(r2.z) * su;
+                    const f3 e1 = mk(em.e1[0], em.e1[1], em.e1[2]), e2 = mk(em.e2[0], em.e2[1], em.e2[2]);
+                    const f3 q = mk(em.v0[0] + b1 * e1.x + b2 * e2.x, em.v0[1] + b1 * e1.y + b2 * e2.y,
+                                    em.v0[2] + b1 * e1.z + b2 * e2.z);
+                    const f3 dq = q - ps;
+                    const float d2 = dot(dq, dq);
+                    dist = sqrtf(d2);
+                    ld = dq / dist;
+                    const f3 ng = normalize(cross(e1, e2));
+                    const float cosl = fabsf(dot(ng, ld));
+                    le = mk(em.emission[0], em.emission[1], em.emission[2]);
+                    pl = cosl > 0.0f ? (1.0f - s.p_env) * em.lum * d2 / (s.emit_power * cosl) : 0.0f;
+                    ok = pl > 0.0f && dist > 0.0f;
+                }
+                if (ok) {
+                    const f3 lwi = normalize(mk(dot(t0, ld), dot(t1, ld), dot(t2, ld)));
+                    const f3 ev = ggx_eval(wo, base, rmao.x, rmao.y, lwi);
+                    const float pb = ggx_pdf(wo, base, rmao.x, rmao.y, lwi);
+                    const float wgt = mis_power(pl, pb) / pl;
+                    const f3 contrib = atten * (ev * le) * wgt;
+                    if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
+                        sh_b = true;
+                        sb_o = ps;
+                        sb_d = ld;
+                        sb_max = dist < 1e8f ? dist * (1.0f - 1e-3f) : 1e8f;
+                        sb_c = contrib;
                     }
                 }
             }
@@ -175,6 +248,8 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
             const f3 nd = normalize(mk(t0.x * wi.x + t1.x * wi.y + t2.x * wi.z, t0.y * wi.x + t1.y * wi.y + t2.y * wi.z,
                                        t0.z * wi.x + t1.z * wi.y + t2.z * wi.z));
             atten *= weight;
+            if (ext) prev_pdf = (weight.x > 0.0f || weight.y > 0.0f || weight.z > 0.0f)
+                                    ? ggx_pdf(wo, base, rmao.x, rmao.y, wi) : 0.0f;
             if (did + 1 < f.depth) {
                 cont = true;
                 next_o = p;
@@ -183,17 +258,16 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
         }
     }
     w.color[path] = make_float4(color.x, color.y, color.z, 0.0f);
-    w.atten[path] = make_float4(atten.x, atten.y, atten.z, 0.0f);
+    w.atten[path] = make_float4(atten.x, atten.y, atten.z, prev_pdf);
     const uint32_t slot = warp_append(&w.counters[nxt], cont);
     if (cont) {
         w.qray[nxt][slot] = rt_ray{next_o.x, next_o.y, next_o.z, 1e-4f, next_d.x, next_d.y, next_d.z, 1e8f};
         w.qpath[nxt][slot] = path;
     }
-    const uint32_t ss = warp_append(&w.counters[2], shadow);
-    if (shadow) {
-        w.sray[ss] = rt_ray{sh_o.x, sh_o.y, sh_o.z, 0.001f, sh_d.x, sh_d.y, sh_d.z, sh_max};
-        w.scontrib[ss] = make_float4(sh_c.x, sh_c.y, sh_c.z, __uint_as_float(path));
-    }
+    const uint32_t sa = warp_append(&w.counters[2], sh_a);
+    if (sh_a) push_shadow(w, sa, sa_o, sa_d, sa_max, sa_c, path);
+    const uint32_t sb = warp_append(&w.counters[2], sh_b);
+    if (sh_b) push_shadow(w, sb, sb_o, sb_d, sb_max, sb_c, path);
 }
 
 // PathTracer::checkVisibility (PathTracer.cpp:124-157).
@@ -257,16 +331,18 @@ __global__ void __launch_bounds__(128) k_shadow(PtScene s, PtWave w) {
     }
 }
 
-// render.rgb(x, y) += min(sampleColor, 5) in sample order (PathTracer.cpp:288).
+// render.rgb(x, y) += min(sampleColor, 5) in sample order (PathTracer.cpp:288); the clamp
+// value is an option of the extended estimator.
 __global__ void k_accumulate(PtFrame f, PtWave w) {
     const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
     if (px >= f.npix) return;
     float r = w.accum[3 * (size_t)px], g = w.accum[3 * (size_t)px + 1], b = w.accum[3 * (size_t)px + 2];
+    const bool clamp = f.clamp > 0.0f;
     for (uint32_t s = 0; s < f.S; ++s) {
         const float4 c = w.color[(size_t)s * f.npix + px];
-        r += gmin(c.x, 5.0f);
-        g += gmin(c.y, 5.0f);
-        b += gmin(c.z, 5.0f);
+        r += clamp ? gmin(c.x, f.clamp) : c.x;
+        g += clamp ? gmin(c.y, f.clamp) : c.y;
+        b += clamp ? gmin(c.z, f.clamp) : c.z;
     }
     w.accum[3 * (size_t)px] = r;
     w.accum[3 * (size_t)px + 1] = g;
@@ -333,7 +409,8 @@ int pt_launch_trace(rt_ctx *rc, const PtWave &w, int cur, uint32_t cap, cudaStre
 
 int pt_launch_shade(const PtScene &s, const PtFrame &f, const PtWave &w, int cur, uint32_t did, uint32_t cap,
                     cudaStream_t st) {
-    k_shade<<<(cap + 127) / 128, 128, 0, st>>>(s, f, w, cur, did);
+    if (f.mode == PT_MODE_EXTENDED) k_shade<true><<<(cap + 127) / 128, 128, 0, st>>>(s, f, w, cur, did);
+    else k_shade<false><<<(cap + 127) / 128, 128, 0, st>>>(s, f, w, cur, did);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

@@ -15,6 +15,8 @@ struct PtFrame {
     float cell_x, cell_y;
     uint32_t s0, S;  // this wave covers sample indices [s0, s0 + S)
     uint32_t seed_lo, seed_hi;
+    int mode;     // PT_MODE_REFERENCE / PT_MODE_EXTENDED
+    float clamp;  // per-sample clamp (<= 0: none)
 };
 
 // Device buffers of one wave (capacity P = npix * S paths).
@@ -72,8 +74,10 @@ struct pt_scene {
     bool committed = false;
 
     // Scene pools on the device.
-    rgb::DevBuf d_objects, d_meshes, d_materials, d_tex, d_texels, d_normals, d_tangents, d_bitangents, d_uvs,
-        d_indices, d_lights;
+    rgb::DevBuf d_objects, d_meshes, d_materials, d_tex, d_texels, d_positions, d_normals, d_tangents, d_bitangents,
+        d_uvs, d_indices, d_lights, d_emitters, d_emitter_cdf, d_env_marg, d_env_cond, d_env_func;
+    int env_tex = -1;
+    float env_intensity = 1.0f;
     rgb::PtScene dev{};
 
     // Wave buffers (grow-only).

@@ -75,25 +75,32 @@ class PathTracer:
         bg = sc.background
         L.call("pt_scene_set_background", self._h, int(bg["mode"]), _f3(bg.get("color", (0, 0, 0))),
                (C.c_uint32 * 6)(*bg.get("tex", (0,) * 6)))
+        if getattr(sc, "environment", None) is not None:
+            L.call("pt_scene_set_environment", self._h, int(sc.environment["tex"]),
+                   float(sc.environment.get("intensity", 1.0)))
         L.call("pt_scene_commit", self._h)
 
-    def render(self, camera, samples: int, depth: int, image, seed: int = 0):
+    def render(self, camera, samples: int, depth: int, image, seed: int = 0, mode: int = 0, clamp: float = 5.0):
         """PathTracer::render(camera, samples, depth, image): accumulate and normalise into
-        ``image`` (H, W, C) float32, host array or CUDA tensor; returns ``image``."""
+        ``image`` (H, W, C) float32, host array or CUDA tensor; returns ``image``.
+        ``mode`` 1 selects the extended estimator (NEE on emitters and the environment
+        map with MIS); ``clamp`` is the per-sample clamp (the reference's 5; <= 0: none)."""
         cam = camera_desc(camera if isinstance(camera, dict) else camera.__dict__)
+        opts = L.pt_render_options(int(mode), float(clamp))
         if type(image).__module__.startswith("torch") and getattr(image, "is_cuda", False):
             import torch
 
             hgt, wid, comp = image.shape
             assert image.is_contiguous() and image.dtype == torch.float32
-            L.call("pt_render", self._h, C.byref(cam), int(samples), int(depth), int(seed), C.c_void_p(image.data_ptr()),
-                   wid, hgt, comp, C.c_void_p(torch.cuda.current_stream().cuda_stream), L.RT_FLAG_DEVICE_PTRS)
+            L.call("pt_render_ex", self._h, C.byref(cam), int(samples), int(depth), int(seed),
+                   C.c_void_p(image.data_ptr()), wid, hgt, comp, C.byref(opts),
+                   C.c_void_p(torch.cuda.current_stream().cuda_stream), L.RT_FLAG_DEVICE_PTRS)
             return image
         if not (isinstance(image, np.ndarray) and image.dtype == np.float32 and image.flags.c_contiguous):
             raise TypeError("image must be a C-contiguous float32 array (H, W, C)")
         hgt, wid, comp = image.shape
-        L.call("pt_render", self._h, C.byref(cam), int(samples), int(depth), int(seed), image.ctypes.data, wid, hgt,
-               comp, None, 0)
+        L.call("pt_render_ex", self._h, C.byref(cam), int(samples), int(depth), int(seed), image.ctypes.data, wid, hgt,
+               comp, C.byref(opts), None, 0)
         return image
 
     def last_stats(self) -> dict:

@@ -306,6 +306,7 @@ class Scene:
     lights: list = field(default_factory=list)  # dict(type, color, position, direction, radius, inner, outer, shadows)
     background: dict = field(default_factory=lambda: {"mode": 0, "color": (0.0, 0.0, 0.0), "tex": (0,) * 6})
     camera: dict = field(default_factory=dict)
+    environment: dict | None = None  # {"tex": id, "intensity": s}: equirect map of the extended estimator
 
     def add_texture(self, img) -> int:
         self.textures.append(np.ascontiguousarray(img, np.float32))
@@ -527,8 +528,31 @@ def instanced_scene(seed: int = 20261206, instances: int = 200, subdivisions: in
         c = (14 * math.cos(ang), 9.0, 14 * math.sin(ang))
         q = sc.add_mesh(quad_mesh((c[0] - 1.5, c[1], c[2] + 1.5), (3, 0, 0), (0, 0, -3), normal=(0, -1, 0)))
         sc.add_object(q, sc.add_material((25.0, 22.0, 18.0), emissive=True))
-    faces = equirect_to_cubemap(sky_equirect(), env_face)
+    env = sky_equirect()
+    faces = equirect_to_cubemap(env, env_face)
     sc.background = {"mode": 2, "color": (0, 0, 0), "tex": tuple(sc.add_texture(f) for f in faces)}
+    sc.environment = {"tex": sc.add_texture(env), "intensity": 1.0}
     sc.camera = {"eye": (0.0, 9.0, 34.0), "center": (0.0, 1.0, 0.0), "up": (0.0, 1.0, 0.0), "fov": 0.9,
                  "ratio": 1920.0 / 1080.0}
+    return sc
+
+
+def constant_environment(scene: Scene, radiance=(1.0, 1.0, 1.0), size: int = 16) -> Scene:
+    """Give `scene` the same constant radiance both as a SKYBOX cubemap (the reference's
+    background) and as an equirectangular environment (the extended estimator's), so the
+    two estimators integrate exactly the same lighting."""
+    img = np.broadcast_to(np.asarray(radiance, np.float32), (size, size, 3)).copy()
+    faces = tuple(scene.add_texture(img) for _ in range(6))
+    scene.background = {"mode": 2, "color": (0, 0, 0), "tex": faces}
+    env = np.broadcast_to(np.asarray(radiance, np.float32), (size, 2 * size, 3)).copy()
+    scene.environment = {"tex": scene.add_texture(env), "intensity": 1.0}
+    return scene
+
+
+def open_cornell_scene(seed: int = 20261204) -> Scene:
+    """The Cornell room without its ceiling and front, lit by its emitter and by whatever
+    environment is attached (see constant_environment)."""
+    sc = cornell_scene(seed)
+    keep = [o for k, o in enumerate(sc.objects) if k != 1]  # drop the ceiling (object 1)
+    sc.objects = keep
     return sc

@@ -137,3 +137,38 @@ def test_argument_errors(cuda_lib):
         tr.render(sc.camera, 0, 3, np.zeros((2, 2, 3), np.float32))
     with pytest.raises(cuda_lib.RenduError):
         tr.render(sc.camera, 4, 3, np.zeros((2, 2, 2), np.float32))
+
+
+def _ext_scene(name):
+    from rendu_gb300 import scenes as S
+
+    if name == "open_env":
+        return S.constant_environment(S.open_cornell_scene(20261203), (0.8, 0.9, 1.0))
+    if name == "instanced_small":
+        return S.instanced_scene(20261206, instances=24, subdivisions=3)
+    return _scene(name)
+
+
+@pytest.mark.parametrize("name,spp,depth", [("cornell_lit", 8, 5), ("open_env", 8, 5), ("instanced_small", 4, 6)])
+def test_extended_render_matches_port_on_the_same_random_stream(cuda_lib, port_lib, name, spp, depth):
+    sc = _ext_scene(name)
+    w, h = 64, 48
+    cam = dict(sc.camera, ratio=w / h)
+    gpu = cuda_lib.PathTracer(sc)
+    img = np.zeros((h, w, 3), np.float32)
+    gpu.render(cam, spp, depth, img, seed=5, mode=1, clamp=0.0)
+    ref = port_lib.PortPathTracer(sc).render(cam, spp, depth, w, h, seed=5, mode=1, clamp=0.0)
+    rel = np.abs(img - ref) / (np.abs(ref) + 1e-2)
+    assert np.isfinite(img).all()
+    assert np.mean(rel < 1e-3) > 0.95, f"only {np.mean(rel < 1e-3):.3f} of values agree to 1e-3"
+
+
+def test_extended_estimator_converges_to_reference_estimator(cuda_lib):
+    sc = _ext_scene("open_env")
+    tr = cuda_lib.PathTracer(sc)
+    imgs = []
+    for seed, mode in ((1, 0), (2, 0), (3, 1)):
+        img = np.zeros((32, 32, 3), np.float32)
+        tr.render(sc.camera, 1024, 5, img, seed=seed, mode=mode, clamp=0.0)
+        imgs.append(img)
+    assert_same_distribution(imgs[2], imgs[0], imgs[1], factor=1.3)

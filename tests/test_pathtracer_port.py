@@ -66,3 +66,27 @@ def test_port_render_is_deterministic_and_thread_independent(port_lib):
     c = tr.render(sc.camera, 8, 4, 24, 20, seed=12, threads=5)
     assert np.array_equal(a, b)
     assert not np.array_equal(a, c)
+
+
+def _ext_scenes():
+    from rendu_gb300 import scenes as S
+
+    return {"cornell": S.cornell_scene(20261203),
+            "open_env": S.constant_environment(S.open_cornell_scene(20261203), (0.8, 0.9, 1.0))}
+
+
+@pytest.mark.parametrize("name", ["cornell", "open_env"])
+def test_port_extended_estimator_converges_to_reference_estimator(port_lib, name):
+    """Next-event estimation with MIS changes the variance, not the expectation: with the
+    clamp off, both estimators converge to the same image (constant environment given both
+    as the reference's cubemap and as the extended estimator's equirect map)."""
+    sc = _ext_scenes()[name]
+    tr = port_lib.PortPathTracer(sc)
+    w = h = 24
+    a = tr.render(sc.camera, 256, 5, w, h, seed=1, mode=0, clamp=0.0)
+    b = tr.render(sc.camera, 256, 5, w, h, seed=2, mode=0, clamp=0.0)
+    x = tr.render(sc.camera, 256, 5, w, h, seed=3, mode=1, clamp=0.0)
+    assert_same_distribution(x, a, b, factor=1.3)
+    # and the extended estimator is the less noisy one
+    y = tr.render(sc.camera, 256, 5, w, h, seed=4, mode=1, clamp=0.0)
+    assert np.sqrt(np.mean((x - y) ** 2)) < np.sqrt(np.mean((a - b) ** 2))
