@@ -160,9 +160,12 @@ def cpu_raycaster_rate(mesh, rays, target_s: float, threads: int):
 
 
 PT_CONFIGS = {
-    # name: (scene factory, width, height, spp, depth, cpu spp)
-    "cornell_256": ("cornell", 256, 256, 16, 5, 16),
-    "instanced_1080p": ("instanced", 1920, 1080, 64, 8, 1),
+    # name: (scene factory, width, height, spp, depth, cpu spp, estimator)
+    #   estimator 0 = the reference's (PathTracer::render), 1 = extended (NEE on the emissive
+    #   quads and the importance-sampled environment map, MIS) as the large workload asks.
+    "cornell_256": ("cornell", 256, 256, 16, 5, 16, 0),
+    "instanced_1080p": ("instanced", 1920, 1080, 64, 8, 1, 1),
+    "instanced_1080p_reference_estimator": ("instanced", 1920, 1080, 64, 8, 1, 0),
 }
 
 
@@ -179,28 +182,28 @@ def run_pathtracer(name, steps, cpu: bool):
 
     import rendu_gb300 as R
 
-    kind, w, h, spp, depth, cpu_spp = PT_CONFIGS[name]
+    kind, w, h, spp, depth, cpu_spp, mode = PT_CONFIGS[name]
     sc = _pt_scene(kind)
     cam = dict(sc.camera, ratio=w / h)
     t0 = time.perf_counter()
     tr = R.PathTracer(sc)
     commit_s = time.perf_counter() - t0
     img = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
-    tr.render(cam, spp, depth, img, seed=1)  # warm-up
+    tr.render(cam, spp, depth, img, seed=1, mode=mode)  # warm-up
     rays, dev_ms = 0, 0.0
     for k in range(steps):
         img.zero_()
-        tr.render(cam, spp, depth, img, seed=2 + k)
+        tr.render(cam, spp, depth, img, seed=2 + k, mode=mode)
         st = tr.last_stats()
         rays += st["rays"]
         dev_ms += st["device_ms"]
     host = np.zeros((h, w, 3), np.float32)
     t0 = time.perf_counter()
-    tr.render(cam, spp, depth, host, seed=99)
+    tr.render(cam, spp, depth, host, seed=99, mode=mode)
     e2e_s = time.perf_counter() - t0
     e2e_rays = tr.last_stats()["rays"]
     out = {"workload": f"{kind}: {sc.triangle_count} triangles, {len(sc.objects)} objects, {w}x{h}, {spp} spp, "
-                       f"depth {depth}",
+                       f"depth {depth}, {'extended' if mode else 'reference'} estimator",
            "value": round(rays / (dev_ms * 1e3), 1), "unit": "Mrays/s", "ms_per_render": round(dev_ms / steps, 2),
            "rays_per_render": rays // steps, "e2e": {"value": round(e2e_rays / e2e_s / 1e6, 1), "unit": "Mrays/s",
                                                       "s_per_render": round(e2e_s, 3)},
@@ -212,7 +215,7 @@ def run_pathtracer(name, steps, cpu: bool):
         threads = max((os.cpu_count() or 2) - 1, 1)
         port = O.PortPathTracer(sc)
         t0 = time.perf_counter()
-        port.render(cam, cpu_spp, depth, w, h, seed=1, threads=threads)
+        port.render(cam, cpu_spp, depth, w, h, seed=1, threads=threads, mode=mode)
         dt = time.perf_counter() - t0
         cpu_rays = int(port.rays.sum())
         cpu_rate = cpu_rays / dt / 1e6
@@ -291,11 +294,11 @@ def main():
         from rendu_gb300 import build as B
 
         B.build()
-        kind, w, h, spp, depth, _ = PT_CONFIGS[args.profile_pt]
+        kind, w, h, spp, depth, _, mode = PT_CONFIGS[args.profile_pt]
         sc = _pt_scene(kind)
         img = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
         tr = R.PathTracer(sc)
-        tr.render(dict(sc.camera, ratio=w / h), spp, depth, img, seed=1)
+        tr.render(dict(sc.camera, ratio=w / h), spp, depth, img, seed=1, mode=mode)
         print(json.dumps({"profile_pt": args.profile_pt, **tr.last_stats()}))
         return
 

@@ -587,6 +587,7 @@ int pt_render_ex(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, ui
     w.counters = s->w_counters.as<uint32_t>();
     w.stats = s->w_stats.as<unsigned long long>();
     w.accum = s->w_accum.as<float>();
+    w.shadow_cap = (uint32_t)s->wave_cap;
 
     const size_t img_bytes = (size_t)f.npix * components * sizeof(float);
     float *d_img = image;
@@ -610,16 +611,16 @@ int pt_render_ex(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, ui
             r = pt_launch_trace(s->rc, w, cur, cap, st);
             if (r != RT_OK) break;
             if (cudaMemsetAsync(&w.counters[cur ^ 1], 0, 4, st) != cudaSuccess ||
-                cudaMemsetAsync(&w.counters[2], 0, 4, st) != cudaSuccess) {
+                cudaMemsetAsync(&w.counters[2], 0, 8, st) != cudaSuccess) {
                 set_error("cudaMemsetAsync failed");
                 r = RT_ERR_CUDA;
                 break;
             }
             r = pt_launch_shade(s->dev, f, w, cur, did, cap, st);
-            // Up to two shadow rays per path and bounce (analytic light + emitter/environment).
-            if (r == RT_OK && (s->dev.nlights > 0 || (f.mode == PT_MODE_EXTENDED &&
-                                                       (s->dev.nemitters > 0 || s->dev.env_tex >= 0))))
-                r = pt_launch_shadow(s->dev, w, 2 * cap, st);
+            // Shadow rays: analytic lights first, then emitters/environment (extended mode).
+            if (r == RT_OK && s->dev.nlights > 0) r = pt_launch_shadow(s->dev, w, cap, 0, st);
+            if (r == RT_OK && f.mode == PT_MODE_EXTENDED && (s->dev.nemitters > 0 || s->dev.env_tex >= 0))
+                r = pt_launch_shadow(s->dev, w, cap, 1, st);
             cur ^= 1;
         }
         if (r == RT_OK) r = pt_launch_accumulate(f, w, st);

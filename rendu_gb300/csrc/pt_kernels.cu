@@ -264,21 +264,25 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
         w.qray[nxt][slot] = rt_ray{next_o.x, next_o.y, next_o.z, 1e-4f, next_d.x, next_d.y, next_d.z, 1e8f};
         w.qpath[nxt][slot] = path;
     }
+    // Two shadow queues (analytic lights; emitters/environment), resolved by two launches
+    // in that order: a path never has two shadow rays in one queue, so the radiance update
+    // in k_shadow is race-free and the summation order is fixed.
     const uint32_t sa = warp_append(&w.counters[2], sh_a);
     if (sh_a) push_shadow(w, sa, sa_o, sa_d, sa_max, sa_c, path);
-    const uint32_t sb = warp_append(&w.counters[2], sh_b);
-    if (sh_b) push_shadow(w, sb, sb_o, sb_d, sb_max, sb_c, path);
+    const uint32_t sb = warp_append(&w.counters[3], sh_b);
+    if (sh_b) push_shadow(w, w.shadow_cap + sb, sb_o, sb_d, sb_max, sb_c, path);
 }
 
 // PathTracer::checkVisibility (PathTracer.cpp:124-157).
 template <int STACK>
-__global__ void __launch_bounds__(128) k_shadow(PtScene s, PtWave w) {
+__global__ void __launch_bounds__(128) k_shadow(PtScene s, PtWave w, int queue) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = w.counters[2];
+    const uint32_t n = w.counters[2 + queue];
     if (i == 0) atomicAdd(&w.stats[2], (unsigned long long)n);
     if (i >= n) return;
-    const rt_ray ray = w.sray[i];
-    const float4 c = w.scontrib[i];
+    const uint32_t e = (queue ? w.shadow_cap : 0u) + i;
+    const rt_ray ray = w.sray[e];
+    const float4 c = w.scontrib[e];
     const uint32_t path = __float_as_uint(c.w);
     bool visible = true;
     uint32_t a = 0, b = 0;
@@ -415,10 +419,10 @@ int pt_launch_shade(const PtScene &s, const PtFrame &f, const PtWave &w, int cur
     return RT_OK;
 }
 
-int pt_launch_shadow(const PtScene &s, const PtWave &w, uint32_t cap, cudaStream_t st) {
+int pt_launch_shadow(const PtScene &s, const PtWave &w, uint32_t cap, int queue, cudaStream_t st) {
     const unsigned blocks = (cap + 127) / 128;
-    if (s.big_stack) k_shadow<256><<<blocks, 128, 0, st>>>(s, w);
-    else k_shadow<64><<<blocks, 128, 0, st>>>(s, w);
+    if (s.big_stack) k_shadow<256><<<blocks, 128, 0, st>>>(s, w, queue);
+    else k_shadow<64><<<blocks, 128, 0, st>>>(s, w, queue);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

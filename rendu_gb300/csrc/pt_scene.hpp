@@ -28,7 +28,8 @@ struct PtWave {
     rt_hit *hits;
     rt_ray *sray;
     float4 *scontrib;
-    uint32_t *counters;  // [0], [1]: ray queues, [2]: shadow queue
+    uint32_t *counters;  // [0], [1]: ray queues, [2]: analytic-light shadow queue, [3]: emitter/env shadow queue
+    uint32_t shadow_cap; // the second shadow queue starts at this entry
     unsigned long long *stats;  // [0] primary, [1] bounce, [2] shadow rays
     float *accum;       // npix x 3
 };
@@ -53,7 +54,7 @@ int pt_launch_raygen(const PtFrame &f, const PtWave &w, cudaStream_t st);
 int pt_launch_trace(rt_ctx *rc, const PtWave &w, int cur, uint32_t cap, cudaStream_t st);
 int pt_launch_shade(const PtScene &s, const PtFrame &f, const PtWave &w, int cur, uint32_t did, uint32_t cap,
                     cudaStream_t st);
-int pt_launch_shadow(const PtScene &s, const PtWave &w, uint32_t cap, cudaStream_t st);
+int pt_launch_shadow(const PtScene &s, const PtWave &w, uint32_t cap, int queue, cudaStream_t st);
 int pt_launch_accumulate(const PtFrame &f, const PtWave &w, cudaStream_t st);
 int pt_launch_load(const float *img, uint32_t comps, uint32_t npix, float *accum, cudaStream_t st);
 int pt_launch_store(const float *accum, uint32_t npix, float spp, uint32_t comps, float *img, cudaStream_t st);
