@@ -287,6 +287,47 @@ RT_API int pt_render_ex(pt_scene *scene, const pt_camera_desc *camera, uint32_t 
                         float *image, uint32_t width, uint32_t height, uint32_t components,
                         const pt_render_options *options, void *stream, uint32_t flags);
 
+/* ---- batched rendering ---------------------------------------------------------------
+ * Many renders of different scenes, resolutions, sample counts and depths in one call:
+ * their pixels x samples are cut into tiles and packed into shared waves; every wave is one
+ * replay of a CUDA graph holding the whole per-wave launch sequence (ray generation, the
+ * persistent traversal, shading, shadow rays, accumulation). Each job's image is exactly
+ * what pt_render of that job alone gives (same random stream, same summation order). No
+ * counterpart in the reference, which renders one image per PathTracer::render call. */
+typedef struct pt_batch pt_batch;
+
+typedef struct pt_batch_job {
+    pt_scene *scene; /* committed scene                                                */
+    pt_camera_desc camera;
+    uint32_t samples, depth;
+    uint64_t seed;
+    float *image; /* width x height x components floats, accumulated into as pt_render  */
+    uint32_t width, height, components;
+} pt_batch_job;
+
+/* Wave capacity (paths), pixels per tile, most samples of a pixel in one wave. */
+typedef struct pt_batch_tuning {
+    uint32_t wave_paths, tile_pixels, max_samples;
+} pt_batch_tuning;
+
+RT_API int pt_batch_create(pt_batch **batch, int device);
+RT_API int pt_batch_destroy(pt_batch *batch);
+
+/* Render all jobs (host images, or device images with RT_FLAG_DEVICE_PTRS on `stream`);
+ * returns when every image is final. tuning NULL: the cached autotuned values for this
+ * device if any, else defaults. */
+RT_API int pt_batch_render(pt_batch *batch, const pt_batch_job *jobs, size_t n, const pt_render_options *options,
+                           const pt_batch_tuning *tuning, void *stream, uint32_t flags);
+
+/* Time a reduced copy of the batch (1/8 of each job's samples) under candidate tunings,
+ * cache the fastest for this device in `cache_path` (NULL: $RENDU_GB300_TUNING, else
+ * ~/.cache/rendu_gb300/batch_tuning.json) and return it in *out. */
+RT_API int pt_batch_autotune(pt_batch *batch, const pt_batch_job *jobs, size_t n, const pt_render_options *options,
+                             const char *cache_path, pt_batch_tuning *out);
+
+/* Counters of the last pt_batch_render. */
+RT_API int pt_batch_get_stats(const pt_batch *batch, pt_render_stats *out);
+
 /* Counters of the last pt_render on this scene. */
 RT_API int pt_get_render_stats(const pt_scene *scene, pt_render_stats *out);
 

@@ -6,6 +6,6 @@ Python classes here only marshal arguments to its C-ABI (include/rendu_gb300.h).
 """
 from ._lib import RenduError, lib  # noqa: F401
 from .raycaster import HIT_DTYPE, RAY_DTYPE, Hit, Raycaster  # noqa: F401
-from .pathtracer import PathTracer  # noqa: F401
+from .pathtracer import BatchRenderer, PathTracer  # noqa: F401
 
-__all__ = ["Raycaster", "PathTracer", "Hit", "HIT_DTYPE", "RAY_DTYPE", "RenduError", "lib"]
+__all__ = ["Raycaster", "PathTracer", "BatchRenderer", "Hit", "HIT_DTYPE", "RAY_DTYPE", "RenduError", "lib"]

@@ -65,6 +65,16 @@ class pt_render_options(C.Structure):
     _fields_ = [("mode", C.c_int32), ("clamp", C.c_float)]
 
 
+class pt_batch_job(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", pt_camera_desc), ("samples", C.c_uint32), ("depth", C.c_uint32),
+                ("seed", C.c_uint64), ("image", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("components", C.c_uint32)]
+
+
+class pt_batch_tuning(C.Structure):
+    _fields_ = [("wave_paths", C.c_uint32), ("tile_pixels", C.c_uint32), ("max_samples", C.c_uint32)]
+
+
 class pt_render_stats(C.Structure):
     _fields_ = [("primary_rays", C.c_uint64), ("bounce_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
                 ("paths", C.c_uint64), ("device_ms", C.c_float)]
@@ -102,6 +112,13 @@ _SIGS = {
     "pt_render_ex": ([_VP, C.POINTER(pt_camera_desc), C.c_uint32, C.c_uint32, C.c_uint64, _VP, C.c_uint32, C.c_uint32,
                       C.c_uint32, C.POINTER(pt_render_options), _VP, C.c_uint32], C.c_int),
     "rt_visible_noalloc": ([_VP, _VP, C.c_size_t, _VP, _VP], C.c_int),
+    "pt_batch_create": ([C.POINTER(C.c_void_p), C.c_int], C.c_int),
+    "pt_batch_destroy": ([_VP], C.c_int),
+    "pt_batch_render": ([_VP, _VP, C.c_size_t, C.POINTER(pt_render_options), C.POINTER(pt_batch_tuning), _VP,
+                         C.c_uint32], C.c_int),
+    "pt_batch_autotune": ([_VP, _VP, C.c_size_t, C.POINTER(pt_render_options), C.c_char_p,
+                           C.POINTER(pt_batch_tuning)], C.c_int),
+    "pt_batch_get_stats": ([_VP, C.POINTER(pt_render_stats)], C.c_int),
     "pt_scene_raycaster": ([_VP], _VP),
     "pt_material_eval": ([_VP, C.c_size_t, _VP, C.c_int], C.c_int),
     "pt_material_sample": ([_VP, _VP, C.c_size_t, _VP, C.c_int], C.c_int),

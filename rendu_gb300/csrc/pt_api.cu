@@ -29,6 +29,19 @@ int arg_error(const char *msg) {
     return RT_ERR_ARG;
 }
 
+// Validation shared by pt_render and the batch jobs (PathTracer.cpp:162-173).
+int check_job(const pt_scene *s, uint32_t samples, uint32_t width, uint32_t height, uint32_t components) {
+    if (!s->committed) {
+        set_error("pt_scene_commit must be called after the last scene change");
+        return RT_ERR_STATE;
+    }
+    if (width == 0 || height == 0) return arg_error("empty image");
+    if (components < 3) return arg_error("the image needs at least 3 components (PathTracer.cpp:166-168)");
+    if (samples == 0) return arg_error("samples must be at least 1");
+    if ((uint64_t)width * height >= (1ull << 28)) return arg_error("image too large");
+    return RT_OK;
+}
+
 template <class T>
 int upload(DevBuf &b, const std::vector<T> &v, cudaStream_t st) {
     if (b.reserve(sizeof(T) * (v.empty() ? 1 : v.size())) != RT_OK) return RT_ERR_OOM;
@@ -36,39 +49,12 @@ int upload(DevBuf &b, const std::vector<T> &v, cudaStream_t st) {
     return RT_OK;
 }
 
-// ---- float vector helpers in glm's operation order (host) --------------------------------
 struct V3 {
     float x, y, z;
 };
-V3 vsub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
-V3 vadd(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
-V3 vscale(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
-float vdot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-V3 vcross(V3 x, V3 y) { return {x.y * y.z - y.y * x.z, x.z * y.x - y.z * x.x, x.x * y.y - y.x * x.y}; }
 V3 vnormalize(V3 v) {
-    const float s = 1.0f / std::sqrt(vdot(v, v));
+    const float s = 1.0f / std::sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
     return {v.x * s, v.y * s, v.z * s};
-}
-
-// Camera::pose (Camera.cpp:10-18) followed by Camera::pixelShifts (Camera.cpp:42-49).
-void pixel_shifts(const pt_camera_desc &c, float corner[3], float dx[3], float dy[3], float eye[3]) {
-    const V3 e{c.eye[0], c.eye[1], c.eye[2]}, ce{c.center[0], c.center[1], c.center[2]};
-    V3 up = vnormalize(V3{c.up[0], c.up[1], c.up[2]});
-    const V3 view = vnormalize(vsub(ce, e));
-    const V3 right = vcross(view, up);
-    up = vcross(right, view);
-    const float hs = std::tan(0.5f * c.fov);
-    const float ws = c.ratio * hs;
-    const V3 de = vsub(ce, e);
-    const float dist = std::sqrt(vdot(de, de));
-    const V3 k = vadd(vscale(-ws, right), vscale(hs, up));
-    const V3 co = vadd(ce, vscale(dist, k));
-    const V3 ddx = vscale(2.0f * ws * dist, right);
-    const V3 ddy = vscale(-2.0f * hs * dist, up);
-    corner[0] = co.x; corner[1] = co.y; corner[2] = co.z;
-    dx[0] = ddx.x; dx[1] = ddx.y; dx[2] = ddx.z;
-    dy[0] = ddy.x; dy[1] = ddy.y; dy[2] = ddy.z;
-    eye[0] = e.x; eye[1] = e.y; eye[2] = e.z;
 }
 
 // inverse(transpose(mat3(model))) as a row-major 3x3 acting on column vectors.
@@ -119,10 +105,9 @@ int pt_scene_destroy(pt_scene *s) {
     if (s->rc) rt_destroy(s->rc);
     for (DevBuf *b : {&s->d_positions, &s->d_emitters, &s->d_emitter_cdf, &s->d_env_marg, &s->d_env_cond,
                       &s->d_env_func, &s->d_objects, &s->d_meshes, &s->d_materials, &s->d_tex, &s->d_texels, &s->d_normals,
-                      &s->d_tangents, &s->d_bitangents, &s->d_uvs, &s->d_indices, &s->d_lights, &s->w_atten,
-                      &s->w_color, &s->w_ndc, &s->w_qray0, &s->w_qray1, &s->w_qpath0, &s->w_qpath1, &s->w_hits,
-                      &s->w_sray, &s->w_scontrib, &s->w_counters, &s->w_stats, &s->w_accum, &s->w_image})
+                      &s->d_tangents, &s->d_bitangents, &s->d_uvs, &s->d_indices, &s->d_lights})
         b->release();
+    s->engine.reset();
     delete s;
     return RT_OK;
 }
@@ -516,140 +501,83 @@ int pt_render_ex(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, ui
                  void *stream, uint32_t flags) {
     clear_error();
     if (!s || !camera || !image) return arg_error("null argument");
-    if (!s->committed) {
-        set_error("pt_scene_commit must be called after the last scene change");
-        return RT_ERR_STATE;
-    }
-    if (width == 0 || height == 0) return arg_error("empty image");
-    if (components < 3) return arg_error("the image needs at least 3 components (PathTracer.cpp:166-168)");
-    if (samples == 0) return arg_error("samples must be at least 1");
-    if ((uint64_t)width * height >= (1ull << 31)) return arg_error("image too large");
+    int r = check_job(s, samples, width, height, components);
+    if (r != RT_OK) return r;
+    const int mode = opts ? opts->mode : PT_MODE_REFERENCE;
+    if (mode != PT_MODE_REFERENCE && mode != PT_MODE_EXTENDED) return arg_error("unknown render mode");
     DeviceGuard g(s->device);
-    cudaStream_t st = (flags & RT_FLAG_DEVICE_PTRS) ? static_cast<cudaStream_t>(stream) : s->rc->stream;
-
-    // Power-of-two sample count and stratification grid (PathTracer.cpp:169-178, 57-69).
-    const uint32_t spp = (uint32_t)std::pow(2.0, std::round(std::log2((float)samples)));
-    const int k = (int)std::floor(std::log2((double)spp));
-    uint32_t cx = (uint32_t)std::pow(2, k / 2), cy = cx;
-    if (k % 2 == 1) {
-        cx = (uint32_t)std::pow(2, (k + 1) / 2);
-        cy = (uint32_t)std::pow(2, (k - 1) / 2);
-    }
-    PtFrame f{};
-    pixel_shifts(*camera, f.corner, f.dx, f.dy, f.eye);
-    f.W = width;
-    f.H = height;
-    f.npix = width * height;
-    f.spp = spp;
-    f.cx = cx;
-    f.cy = cy;
-    f.cell_x = 1.0f / (float)cx;
-    f.cell_y = 1.0f / (float)cy;
-    f.depth = depth;
-    f.seed_lo = (uint32_t)seed;
-    f.seed_hi = (uint32_t)(seed >> 32);
-    f.mode = opts ? opts->mode : PT_MODE_REFERENCE;
-    f.clamp = opts ? opts->clamp : 5.0f;
-    if (f.mode != PT_MODE_REFERENCE && f.mode != PT_MODE_EXTENDED) return arg_error("unknown render mode");
-    // Wave: every pixel x S samples, S a power of two dividing spp, about 8M paths.
-    const uint64_t target = 1ull << 23;
-    uint32_t S = 1;
-    while (S * 2 <= spp && (uint64_t)f.npix * S * 2 <= target) S *= 2;
-    f.S = S;
-    const uint64_t P = (uint64_t)f.npix * S;
-    if (P >= (1ull << 31)) return arg_error("image too large for one wave");
-
-    if (P > s->wave_cap) {
-        int r = RT_OK;
-        if ((r = s->w_atten.reserve(P * 16)) || (r = s->w_color.reserve(P * 16)) || (r = s->w_ndc.reserve(P * 8)) ||
-            (r = s->w_qray0.reserve(P * 32)) || (r = s->w_qray1.reserve(P * 32)) || (r = s->w_qpath0.reserve(P * 4)) ||
-            (r = s->w_qpath1.reserve(P * 4)) || (r = s->w_hits.reserve(P * 16)) || (r = s->w_sray.reserve(2 * P * 32)) ||
-            (r = s->w_scontrib.reserve(2 * P * 16)))
-            return r;
-        s->wave_cap = P;
-    }
-    if (s->w_counters.reserve(64) || s->w_stats.reserve(64)) return RT_ERR_OOM;
-    if (f.npix > s->accum_cap) {
-        if (s->w_accum.reserve((size_t)f.npix * 12)) return RT_ERR_OOM;
-        s->accum_cap = f.npix;
-    }
-    PtWave w{};
-    w.atten = s->w_atten.as<float4>();
-    w.color = s->w_color.as<float4>();
-    w.ndc = s->w_ndc.as<float2>();
-    w.qray[0] = s->w_qray0.as<rt_ray>();
-    w.qray[1] = s->w_qray1.as<rt_ray>();
-    w.qpath[0] = s->w_qpath0.as<uint32_t>();
-    w.qpath[1] = s->w_qpath1.as<uint32_t>();
-    w.hits = s->w_hits.as<rt_hit>();
-    w.sray = s->w_sray.as<rt_ray>();
-    w.scontrib = s->w_scontrib.as<float4>();
-    w.counters = s->w_counters.as<uint32_t>();
-    w.stats = s->w_stats.as<unsigned long long>();
-    w.accum = s->w_accum.as<float>();
-    w.shadow_cap = (uint32_t)s->wave_cap;
-
-    const size_t img_bytes = (size_t)f.npix * components * sizeof(float);
-    float *d_img = image;
-    if (!(flags & RT_FLAG_DEVICE_PTRS)) {
-        if (s->w_image.reserve(img_bytes)) return RT_ERR_OOM;
-        d_img = s->w_image.as<float>();
-        RT_CUDA_TRY(cudaMemcpyAsync(d_img, image, img_bytes, cudaMemcpyHostToDevice, st));
-    }
-    cudaEvent_t e0, e1;
-    RT_CUDA_TRY(cudaEventCreate(&e0));
-    RT_CUDA_TRY(cudaEventCreate(&e1));
-    RT_CUDA_TRY(cudaEventRecord(e0, st));
-    RT_CUDA_TRY(cudaMemsetAsync(w.stats, 0, 64, st));
-    int r = pt_launch_load(d_img, components, f.npix, w.accum, st);
-    const uint32_t cap = (uint32_t)P;
-    for (uint32_t s0 = 0; r == RT_OK && s0 < spp; s0 += S) {
-        f.s0 = s0;
-        r = pt_launch_raygen(f, w, st);
-        int cur = 0;
-        for (uint32_t did = 0; r == RT_OK && did < depth; ++did) {
-            r = pt_launch_trace(s->rc, w, cur, cap, st);
-            if (r != RT_OK) break;
-            if (cudaMemsetAsync(&w.counters[cur ^ 1], 0, 4, st) != cudaSuccess ||
-                cudaMemsetAsync(&w.counters[2], 0, 8, st) != cudaSuccess) {
-                set_error("cudaMemsetAsync failed");
-                r = RT_ERR_CUDA;
-                break;
-            }
-            r = pt_launch_shade(s->dev, f, w, cur, did, cap, st);
-            // Shadow rays: analytic lights first, then emitters/environment (extended mode).
-            if (r == RT_OK && s->dev.nlights > 0) r = pt_launch_shadow(s->dev, w, cap, 0, st);
-            if (r == RT_OK && f.mode == PT_MODE_EXTENDED && (s->dev.nemitters > 0 || s->dev.env_tex >= 0))
-                r = pt_launch_shadow(s->dev, w, cap, 1, st);
-            cur ^= 1;
-        }
-        if (r == RT_OK) r = pt_launch_accumulate(f, w, st);
-    }
-    if (r == RT_OK) r = pt_launch_store(w.accum, f.npix, (float)spp, components, d_img, st);
-    if (r == RT_OK && cudaEventRecord(e1, st) != cudaSuccess) r = RT_ERR_CUDA;
-    unsigned long long stats[3] = {0, 0, 0};
-    if (r == RT_OK && cudaMemcpyAsync(stats, w.stats, sizeof(stats), cudaMemcpyDeviceToHost, st) != cudaSuccess)
-        r = RT_ERR_CUDA;
-    if (r == RT_OK && !(flags & RT_FLAG_DEVICE_PTRS) &&
-        cudaMemcpyAsync(image, d_img, img_bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess)
-        r = RT_ERR_CUDA;
-    if (r == RT_OK && cudaStreamSynchronize(st) != cudaSuccess) {
-        set_error(std::string("render failed: ") + cudaGetErrorString(cudaGetLastError()));
-        r = RT_ERR_CUDA;
-    }
-    if (r == RT_OK) {
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        s->last.primary_rays = stats[0];
-        s->last.bounce_rays = stats[1];
-        s->last.shadow_rays = stats[2];
-        s->last.paths = (uint64_t)f.npix * spp;
-        s->last.device_ms = ms;
-        r = check_status(s->rc, st);
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    if (!s->engine) s->engine.reset(new WaveEngine(s->device));
+    const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
+    cudaStream_t st = dev ? static_cast<cudaStream_t>(stream) : s->rc->stream;
+    JobSpec js{s, *camera, samples, depth, seed, image, width, height, components, opts ? opts->clamp : 5.0f};
+    // One tile of every pixel per wave, as many samples per wave as ~8M paths allow.
+    Tuning t{1u << 23, width * height, 1u << 30};
+    if ((uint64_t)width * height > t.wave_paths) t.wave_paths = width * height;
+    r = s->engine->run({js}, mode, t, dev, st, &s->last);
     return r;
+}
+
+int pt_batch_create(pt_batch **out, int device) {
+    clear_error();
+    if (!out) return arg_error("null output pointer");
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        set_error("CUDA device " + std::to_string(device) + " is not available");
+        return RT_ERR_CUDA;
+    }
+    pt_batch *b = new pt_batch();
+    b->device = device;
+    b->engine.reset(new WaveEngine(device));
+    *out = b;
+    return RT_OK;
+}
+
+int pt_batch_destroy(pt_batch *b) {
+    if (!b) return RT_OK;
+    DeviceGuard g(b->device);
+    b->engine.reset();
+    delete b;
+    return RT_OK;
+}
+
+static int batch_specs(const pt_batch_job *jobs, size_t n, const pt_render_options *opts, std::vector<JobSpec> &out) {
+    if (!jobs || n == 0) return arg_error("empty batch");
+    out.clear();
+    for (size_t k = 0; k < n; ++k) {
+        const pt_batch_job &j = jobs[k];
+        if (!j.scene || !j.image) return arg_error("batch job without scene or image");
+        const int r = check_job(j.scene, j.samples, j.width, j.height, j.components);
+        if (r != RT_OK) return r;
+        out.push_back(JobSpec{j.scene, j.camera, j.samples, j.depth, j.seed, j.image, j.width, j.height, j.components,
+                              opts ? opts->clamp : 5.0f});
+    }
+    return RT_OK;
+}
+
+int pt_batch_render(pt_batch *b, const pt_batch_job *jobs, size_t n, const pt_render_options *opts,
+                    const pt_batch_tuning *tuning, void *stream, uint32_t flags) {
+    clear_error();
+    if (!b) return arg_error("null batch");
+    std::vector<JobSpec> specs;
+    int r = batch_specs(jobs, n, opts, specs);
+    if (r != RT_OK) return r;
+    const int mode = opts ? opts->mode : PT_MODE_REFERENCE;
+    if (mode != PT_MODE_REFERENCE && mode != PT_MODE_EXTENDED) return arg_error("unknown render mode");
+    Tuning t = default_tuning();
+    if (tuning) t = Tuning{tuning->wave_paths, tuning->tile_pixels, tuning->max_samples};
+    else load_tuning(nullptr, t);
+    DeviceGuard g(b->device);
+    const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
+    return b->engine->run(specs, mode, t, dev, static_cast<cudaStream_t>(stream), &b->last);
+}
+
+int pt_batch_get_stats(const pt_batch *b, pt_render_stats *out) {
+    clear_error();
+    if (!b || !out) return arg_error("null argument");
+    *out = b->last;
+    return RT_OK;
 }
 
 }  // extern "C"

@@ -1,0 +1,135 @@
+// Autotuner of the batched wave engine: wave capacity, tile size and samples per wave are
+// chosen by timing a reduced copy of the caller's batch (every job at 1/8 of its samples)
+// under each candidate; the winner is cached per device in a small JSON file that
+// pt_batch_render reads when called without explicit tuning.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <sys/stat.h>
+
+#include "pt_scene.hpp"
+
+namespace rgb {
+
+Tuning default_tuning() { return Tuning{1u << 23, 1u << 16, 16}; }
+
+namespace {
+
+std::string device_name() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return "unknown";
+    return p.name;
+}
+
+std::string cache_path(const char *path) {
+    if (path && *path) return path;
+    if (const char *e = std::getenv("RENDU_GB300_TUNING")) return e;
+    const char *home = std::getenv("HOME");
+    return std::string(home ? home : ".") + "/.cache/rendu_gb300/batch_tuning.json";
+}
+
+bool json_number(const std::string &text, const char *key, double &out) {
+    const std::string k = std::string("\"") + key + "\"";
+    const size_t p = text.find(k);
+    if (p == std::string::npos) return false;
+    const size_t c = text.find(':', p + k.size());
+    if (c == std::string::npos) return false;
+    char *end = nullptr;
+    out = std::strtod(text.c_str() + c + 1, &end);
+    return end != text.c_str() + c + 1;
+}
+
+}  // namespace
+
+// Reads the cached tuning of this device; leaves `t` unchanged when there is none.
+bool load_tuning(const char *path, Tuning &t) {
+    FILE *f = std::fopen(cache_path(path).c_str(), "rb");
+    if (!f) return false;
+    std::string text;
+    char buf[1024];
+    size_t n;
+    while ((n = std::fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, n);
+    std::fclose(f);
+    const std::string dev = "\"device\": \"" + device_name() + "\"";
+    if (text.find(dev) == std::string::npos) return false;
+    double a, b, c;
+    if (!json_number(text, "wave_paths", a) || !json_number(text, "tile_pixels", b) || !json_number(text, "max_samples", c))
+        return false;
+    if (a < 4096 || b < 1 || c < 1) return false;
+    t = Tuning{(uint32_t)a, (uint32_t)b, (uint32_t)c};
+    return true;
+}
+
+static bool save_tuning(const char *path, const Tuning &t, double ms) {
+    const std::string p = cache_path(path);
+    const size_t slash = p.rfind('/');
+    if (slash != std::string::npos) {  // create the directory chain
+        std::string dir;
+        for (size_t i = 0; i <= slash; ++i) {
+            dir += p[i];
+            if (p[i] == '/' && i > 0) mkdir(dir.c_str(), 0755);
+        }
+    }
+    FILE *f = std::fopen(p.c_str(), "wb");
+    if (!f) return false;
+    std::fprintf(f, "{\"device\": \"%s\", \"wave_paths\": %u, \"tile_pixels\": %u, \"max_samples\": %u, \"ms\": %.4f}\n",
+                 device_name().c_str(), t.wave_paths, t.tile_pixels, t.max_samples, ms);
+    std::fclose(f);
+    return true;
+}
+
+}  // namespace rgb
+
+using namespace rgb;
+
+extern "C" int pt_batch_autotune(pt_batch *b, const pt_batch_job *jobs, size_t n, const pt_render_options *opts,
+                                 const char *cache, pt_batch_tuning *out) {
+    clear_error();
+    if (!b || !jobs || n == 0) {
+        set_error("null batch or empty job list");
+        return RT_ERR_ARG;
+    }
+    const int mode = opts ? opts->mode : PT_MODE_REFERENCE;
+    std::vector<JobSpec> specs;
+    for (size_t k = 0; k < n; ++k) {
+        const pt_batch_job &j = jobs[k];
+        if (!j.scene || !j.scene->committed || j.width == 0 || j.height == 0 || j.components < 3 || j.samples == 0) {
+            set_error("invalid batch job " + std::to_string(k));
+            return RT_ERR_ARG;
+        }
+        // Reduced copy: 1/8 of the samples, results discarded (no image).
+        const uint32_t spp = j.samples >= 8 ? j.samples / 8 : 1;
+        specs.push_back(JobSpec{j.scene, j.camera, spp, j.depth, j.seed, nullptr, j.width, j.height, j.components,
+                                opts ? opts->clamp : 5.0f});
+    }
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != b->device) cudaSetDevice(b->device);
+    const uint32_t waves[] = {1u << 21, 1u << 22, 1u << 23, 1u << 24};
+    const uint32_t tilesz[] = {1u << 14, 1u << 16, 1u << 18};
+    const uint32_t samples[] = {4, 16, 64};
+    Tuning best = default_tuning();
+    double best_ms = 1e30;
+    int r = RT_OK;
+    for (uint32_t wp : waves)
+        for (uint32_t tp : tilesz)
+            for (uint32_t ms : samples) {
+                const Tuning t{wp, tp, ms};
+                pt_render_stats st{};
+                r = b->engine->run(specs, mode, t, false, nullptr, &st);  // first run: capture + warm-up
+                if (r == RT_OK) r = b->engine->run(specs, mode, t, false, nullptr, &st);
+                if (r != RT_OK) break;
+                if (st.device_ms < best_ms) {
+                    best_ms = st.device_ms;
+                    best = t;
+                }
+            }
+    if (prev >= 0 && prev != b->device) cudaSetDevice(prev);
+    if (r != RT_OK) return r;
+    save_tuning(cache, best, best_ms);
+    if (out) *out = pt_batch_tuning{best.wave_paths, best.tile_pixels, best.max_samples};
+    return RT_OK;
+}

@@ -1,19 +1,23 @@
 // Wavefront kernels of the path tracer: replace the per-sample loop body of
-// PathTracer::render (PathTracer.cpp:186-293 of kosua20/Rendu).
+// PathTracer::render (PathTracer.cpp:186-293 of kosua20/Rendu), for one render or for a
+// batch of renders of different scenes, resolutions, sample counts and depths.
 //
-// One wave = every pixel x a run of S consecutive sample indices (P = W*H*S paths).
-// Per bounce:
-//   trace  -- closest hit for the compacted ray queue (the persistent traversal of
-//             rt_trace.cu, queue length read on the device);
-//   shade  -- the reference's hit logic (background on miss, alpha cut-out, emission,
-//             local frame, NEE light pick + evaluation, BSDF sampling), appending
-//             continuing paths to the next queue and shadow rays to the shadow queue with
-//             one atomic per warp;
-//   shadow -- PathTracer::checkVisibility for every queued shadow ray: one any-hit query
-//             when the scene has no alpha-masked material, else the reference's walk of
-//             closest hits through transparent texels.
-// After the last bounce, `accumulate` adds min(L, 5) of each sample to its pixel in sample
-// order (the reference's order), and `store` divides by spp.
+// A wave is a list of tiles (job, pixel range, run of S consecutive samples) packed from
+// all jobs of the call; every path carries its job, pixel and sample. Per wave:
+//   wave_begin -- queue counters for this wave;
+//   raygen     -- primary rays from each job's camera (PathTracer.cpp:186-198);
+//   per bounce:
+//     trace    -- closest hit of the compacted ray queue: the persistent traversal with
+//                 per-lane refill (rt_trace.cu), each ray against its own job's hierarchy;
+//     shade    -- the reference's hit logic (background on miss, alpha cut-out, emission,
+//                 local frame, NEE light pick + evaluation, BSDF sampling); continuing
+//                 paths and shadow rays are appended to queues with one atomic per warp;
+//     shadow   -- PathTracer::checkVisibility for each queued shadow ray (two queues,
+//                 resolved in a fixed order);
+//   accumulate -- min(L, clamp) of each sample added to its pixel in sample order;
+//   wave_end   -- advance the wave index.
+// The whole per-wave sequence reads its wave from device memory, so it is captured once in
+// a CUDA graph and replayed for every wave (pt_engine.cu).
 #include "pt_scene.hpp"
 #include "rt_traverse.cuh"
 
@@ -31,26 +35,53 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t *counter, bool pred) {
     return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
 }
 
-__global__ void k_raygen(PtFrame f, PtWave w) {
+// Tile of the current wave containing wave path p (tiles sorted by path0).
+__device__ __forceinline__ uint32_t find_tile(const PtWave &w, uint32_t t0, uint32_t t1, uint32_t p) {
+    uint32_t lo = t0, hi = t1 - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (w.tiles[mid].path0 <= p) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_wave_begin(PtWave w) {
+    const uint32_t wave = w.counters[4];
+    w.counters[0] = w.wave_paths[wave];
+    w.counters[1] = 0u;
+    w.counters[2] = 0u;
+    w.counters[3] = 0u;
+    *w.fetch = 0ull;
+}
+
+__global__ void k_wave_end(PtWave w) { w.counters[4] += 1u; }
+
+__global__ void k_raygen(PtWave w) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t P = f.npix * f.S;
-    if (p == 0) w.counters[0] = P;
-    if (p >= P) return;
-    const uint32_t pixel = p % f.npix;
-    const uint32_t sid = f.s0 + p / f.npix;
-    const uint32_t x = pixel % f.W, y = pixel / f.W;
-    const U4 r = philox(U4{pixel, sid, 0u, 0u}, f.seed_lo, f.seed_hi);
+    const uint32_t wave = w.counters[4];
+    if (p >= w.wave_paths[wave]) return;
+    const PtTile tile = w.tiles[find_tile(w, w.wave_tiles[wave], w.wave_tiles[wave + 1], p)];
+    const uint32_t local = p - tile.path0;
+    const uint32_t pixel = tile.pixel0 + local % tile.npix;
+    const uint32_t sid = tile.s0 + local / tile.npix;
+    const PtJob &J = w.jobs[tile.job];
+    const uint32_t x = pixel % J.W, y = pixel / J.W;
+    const U4 r = philox(U4{pixel, sid, 0u, 0u}, J.seed_lo, J.seed_hi);
     const float jx = u01(r.x), jy = u01(r.y);
     // PathTracer::getSamplePosition (PathTracer.cpp:71-84) and the ray set-up (:191-198).
-    const int sidy = (int)sid / (int)f.cx, sidx = (int)sid % (int)f.cx;
-    const float sx = (float)x + ((float)sidx + jx) * f.cell_x;
-    const float sy = (float)y + ((float)sidy + jy) * f.cell_y;
-    const float nx = sx / (float)f.W, ny = sy / (float)f.H;
-    const f3 world = mk(f.corner[0] + nx * f.dx[0] + ny * f.dy[0], f.corner[1] + nx * f.dx[1] + ny * f.dy[1],
-                        f.corner[2] + nx * f.dx[2] + ny * f.dy[2]);
-    const f3 dir = xnormalize(xsub(world, mk(f.eye[0], f.eye[1], f.eye[2])));
-    w.qray[0][p] = rt_ray{f.eye[0], f.eye[1], f.eye[2], 1e-4f, dir.x, dir.y, dir.z, 1e8f};
+    const int sidy = (int)sid / (int)J.cx, sidx = (int)sid % (int)J.cx;
+    const float sx = (float)x + ((float)sidx + jx) * J.cell_x;
+    const float sy = (float)y + ((float)sidy + jy) * J.cell_y;
+    const float nx = sx / (float)J.W, ny = sy / (float)J.H;
+    const f3 world = mk(J.corner[0] + nx * J.dx[0] + ny * J.dy[0], J.corner[1] + nx * J.dx[1] + ny * J.dy[1],
+                        J.corner[2] + nx * J.dx[2] + ny * J.dy[2]);
+    const f3 dir = xnormalize(xsub(world, mk(J.eye[0], J.eye[1], J.eye[2])));
+    w.qray[0][p] = rt_ray{J.eye[0], J.eye[1], J.eye[2], 1e-4f, dir.x, dir.y, dir.z, 1e8f};
     w.qpath[0][p] = p;
+    w.pjob[p] = tile.job;
+    w.ppix[p] = pixel;
+    w.psamp[p] = sid;
     w.atten[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     w.color[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     w.ndc[p] = make_float2(nx, ny);
@@ -96,14 +127,19 @@ __device__ __forceinline__ void push_shadow(const PtWave &w, uint32_t slot, f3 o
 }
 
 template <bool EXT>
-__global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, int cur, uint32_t did) {
+__global__ void __launch_bounds__(128) k_shade(PtWave w, int cur, uint32_t did) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = w.counters[cur];
-    if (i == 0) atomicAdd(&w.stats[did == 0 ? 0 : 1], (unsigned long long)n);  // rays traced this bounce
+    if (i == 0) {
+        atomicAdd(&w.stats[did == 0 ? 0 : 1], (unsigned long long)n);  // rays traced this bounce
+        *w.fetch = 0ull;  // ray-fetch counter of the next bounce's traversal
+    }
     if (i >= n) return;
     constexpr bool ext = EXT;
     const int nxt = cur ^ 1;
     const uint32_t path = w.qpath[cur][i];
+    const PtJob &J = w.jobs[w.pjob[path]];
+    const PtScene &s = J.scene;
     const rt_ray ray = w.qray[cur][i];
     const rt_hit hit = w.hits[i];
     const f3 pos = mk(ray.ox, ray.oy, ray.oz);
@@ -137,7 +173,7 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
         const float4 bcol = tex_rgbal(s, mat.tex[0], uv.x, uv.y);
         if (mat.masked && bcol.w < 0.01f) {
             // Alpha cut-out: same direction from the hit point, one bounce consumed (:223-226).
-            cont = did + 1 < f.depth;
+            cont = did + 1 < J.depth;
             next_o = p;
         } else if (mat.type == PT_MAT_EMISSIVE) {
             f3 le = mk(bcol.x, bcol.y, bcol.z);  // :228-234
@@ -173,8 +209,8 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
             const f3 wo = normalize(mk(dot(t0, mdir), dot(t1, mdir), dot(t2, mdir)));
             const f3 base = mk(powf(bcol.x, 2.2f), powf(bcol.y, 2.2f), powf(bcol.z, 2.2f));
             const float4 rmao = tex_rgbal(s, mat.tex[2], uv.x, uv.y);
-            const uint32_t pix = path % f.npix, sid = f.s0 + path / f.npix;
-            const U4 rnd = philox(U4{pix, sid, did + 1u, 0u}, f.seed_lo, f.seed_hi);
+            const uint32_t pix = w.ppix[path], sid = w.psamp[path];
+            const U4 rnd = philox(U4{pix, sid, did + 1u, 0u}, J.seed_lo, J.seed_hi);
             const f3 ps = mk(p.x + 0.001f * t2.x, p.y + 0.001f * t2.y, p.z + 0.001f * t2.z);
             if (s.nlights > 0) {
                 // Next-event estimation on one uniformly picked analytic light (:248-272).
@@ -201,7 +237,7 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
             }
             if (ext && (s.nemitters > 0 || s.env_tex >= 0)) {
                 // Extended: one emitter-or-environment sample, MIS against BSDF sampling.
-                const U4 r2 = philox(U4{pix, sid, did + 1u, 1u}, f.seed_lo, f.seed_hi);
+                const U4 r2 = philox(U4{pix, sid, did + 1u, 1u}, J.seed_lo, J.seed_hi);
                 const float usel = u01(r2.x);
                 f3 ld, le;
                 float pl = 0.0f, dist = 1e8f;
@@ -250,7 +286,7 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
             atten *= weight;
             if (ext) prev_pdf = (weight.x > 0.0f || weight.y > 0.0f || weight.z > 0.0f)
                                     ? ggx_pdf(wo, base, rmao.x, rmao.y, wi) : 0.0f;
-            if (did + 1 < f.depth) {
+            if (did + 1 < J.depth) {
                 cont = true;
                 next_o = p;
                 next_d = normalize(nd);
@@ -275,7 +311,7 @@ __global__ void __launch_bounds__(128) k_shade(PtScene s, PtFrame f, PtWave w, i
 
 // PathTracer::checkVisibility (PathTracer.cpp:124-157).
 template <int STACK>
-__global__ void __launch_bounds__(128) k_shadow(PtScene s, PtWave w, int queue) {
+__global__ void __launch_bounds__(128) k_shadow(PtWave w, int queue) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = w.counters[2 + queue];
     if (i == 0) atomicAdd(&w.stats[2], (unsigned long long)n);
@@ -284,13 +320,14 @@ __global__ void __launch_bounds__(128) k_shadow(PtScene s, PtWave w, int queue) 
     const rt_ray ray = w.sray[e];
     const float4 c = w.scontrib[e];
     const uint32_t path = __float_as_uint(c.w);
+    const PtScene &s = w.jobs[w.pjob[path]].scene;
     bool visible = true;
     uint32_t a = 0, b = 0;
     if (!s.empty) {
         if (!s.any_masked) {
             const float4 *rp = reinterpret_cast<const float4 *>(&ray);
             const RayState r = make_ray_state(rp[0], rp[1]);
-            if (r.valid) visible = !traverse<true, false, STACK>(s.nodes, s.tris, r, s.status, a, b).found;
+            if (r.valid) visible = !traverse<true, false, STACK>(s.nodes, s.tris, r, w.status, a, b).found;
         } else {
             f3 lpos = mk(ray.ox, ray.oy, ray.oz);
             const f3 d = mk(ray.dx, ray.dy, ray.dz);
@@ -298,7 +335,7 @@ __global__ void __launch_bounds__(128) k_shadow(PtScene s, PtWave w, int queue) 
             int steps = 0;
             while (maxd > 0.0f) {
                 if (++steps > 256) {  // bounded walk: report and treat as occluded
-                    atomicOr(s.status, RT_DEV_TIMEOUT);
+                    atomicOr(w.status, RT_DEV_TIMEOUT);
                     visible = false;
                     break;
                 }
@@ -306,7 +343,7 @@ __global__ void __launch_bounds__(128) k_shadow(PtScene s, PtWave w, int queue) 
                 const RayState r = make_ray_state(make_float4(lpos.x, lpos.y, lpos.z, 0.001f),
                                                   make_float4(d.x, d.y, d.z, maxd));
                 if (!r.valid) break;
-                const TraceResult h = traverse<false, false, STACK>(s.nodes, s.tris, r, s.status, a, b);
+                const TraceResult h = traverse<false, false, STACK>(s.nodes, s.tris, r, w.status, a, b);
                 if (!h.found) break;
                 const SurfaceHit sh = surface(s, h.prim, h.u, h.v);
                 const PtObject &obj = s.objects[sh.obj];
@@ -335,22 +372,78 @@ __global__ void __launch_bounds__(128) k_shadow(PtScene s, PtWave w, int queue) 
     }
 }
 
-// render.rgb(x, y) += min(sampleColor, 5) in sample order (PathTracer.cpp:288); the clamp
-// value is an option of the extended estimator.
-__global__ void k_accumulate(PtFrame f, PtWave w) {
-    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
-    if (px >= f.npix) return;
-    float r = w.accum[3 * (size_t)px], g = w.accum[3 * (size_t)px + 1], b = w.accum[3 * (size_t)px + 2];
-    const bool clamp = f.clamp > 0.0f;
-    for (uint32_t s = 0; s < f.S; ++s) {
-        const float4 c = w.color[(size_t)s * f.npix + px];
-        r += clamp ? gmin(c.x, f.clamp) : c.x;
-        g += clamp ? gmin(c.y, f.clamp) : c.y;
-        b += clamp ? gmin(c.z, f.clamp) : c.z;
+// Closest hit of ray queue `cur` with the persistent per-lane refill of rt_trace.cu; each
+// lane traverses the hierarchy of its ray's job.
+template <int STACK>
+__global__ void __launch_bounds__(128) k_trace_batch(PtWave w, int cur) {
+    const size_t n = w.counters[cur];
+    const rt_ray *__restrict__ rays = w.qray[cur];
+    const uint32_t *__restrict__ qpath = w.qpath[cur];
+    const unsigned lane = threadIdx.x & 31;
+    int stack_node[STACK];
+    float stack_near[STACK];
+    RayState r;
+    TravState t;
+    JobBvh jb;
+    size_t idx = 0;
+    bool active = false, exhausted = false;
+    uint32_t nv_ = 0, nt_ = 0;
+    while (true) {
+        const unsigned need = __ballot_sync(0xffffffffu, !active);
+        if (need && !exhausted) {
+            const int leader = __ffs(need) - 1;
+            unsigned long long base = 0;
+            if ((int)lane == leader) base = atomicAdd(w.fetch, (unsigned long long)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base + __popc(need) >= n) exhausted = true;
+            if (!active) {
+                idx = (size_t)base + __popc(need & ((1u << lane) - 1u));
+                if (idx < n) {
+                    const float4 *rp = reinterpret_cast<const float4 *>(rays + idx);
+                    r = make_ray_state(rp[0], rp[1]);
+                    jb = w.bvhs[w.pjob[qpath[idx]]];
+                    trav_init(t, r);
+                    active = r.valid && !jb.empty;
+                    if (!active) w.hits[idx] = rt_hit{FLT_MAX, 0.0f, 0.0f, RT_NO_HIT};
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (active &&
+            trav_step<false, false, STACK>(jb.nodes, jb.tris, r, t, stack_node, stack_near, w.status, nv_, nt_)) {
+            active = false;
+            w.hits[idx] = rt_hit{t.res.found ? t.res.t : FLT_MAX, t.res.u, t.res.v,
+                                 t.res.found ? t.res.prim : RT_NO_HIT};
+        }
     }
-    w.accum[3 * (size_t)px] = r;
-    w.accum[3 * (size_t)px + 1] = g;
-    w.accum[3 * (size_t)px + 2] = b;
+}
+
+// render.rgb(x, y) += min(sampleColor, 5) in sample order (PathTracer.cpp:288); the clamp
+// value is an option of the extended estimator. One thread per (tile, pixel).
+__global__ void k_accumulate(PtWave w) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t wave = w.counters[4];
+    if (p >= w.wave_paths[wave]) return;
+    const PtTile tile = w.tiles[find_tile(w, w.wave_tiles[wave], w.wave_tiles[wave + 1], p)];
+    const uint32_t local = p - tile.path0;
+    if (local >= tile.npix) return;
+    const PtJob &J = w.jobs[tile.job];
+    float *acc = w.accum + 3 * ((size_t)J.accum_offset + tile.pixel0 + local);
+    float r = acc[0], g = acc[1], b = acc[2];
+    const float cl = J.clamp;
+    const bool clamp = cl > 0.0f;
+    for (uint32_t s = 0; s < tile.S; ++s) {
+        const float4 c = w.color[(size_t)tile.path0 + (size_t)s * tile.npix + local];
+        r += clamp ? gmin(c.x, cl) : c.x;
+        g += clamp ? gmin(c.y, cl) : c.y;
+        b += clamp ? gmin(c.z, cl) : c.z;
+    }
+    acc[0] = r;
+    acc[1] = g;
+    acc[2] = b;
 }
 
 __global__ void k_load(const float *__restrict__ img, uint32_t comps, uint32_t npix, float *__restrict__ accum) {
@@ -400,35 +493,70 @@ int pt_launch_material(const float *cases, const float *uniforms, uint32_t n, fl
     return RT_OK;
 }
 
-int pt_launch_raygen(const PtFrame &f, const PtWave &w, cudaStream_t st) {
-    const uint32_t P = f.npix * f.S;
-    k_raygen<<<(P + 255) / 256, 256, 0, st>>>(f, w);
+int pt_launch_wave_begin(const PtWave &w, cudaStream_t st) {
+    k_wave_begin<<<1, 1, 0, st>>>(w);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
 
-int pt_launch_trace(rt_ctx *rc, const PtWave &w, int cur, uint32_t cap, cudaStream_t st) {
-    return trace_closest_queue(rc, w.qray[cur], &w.counters[cur], cap, w.hits, st);
-}
-
-int pt_launch_shade(const PtScene &s, const PtFrame &f, const PtWave &w, int cur, uint32_t did, uint32_t cap,
-                    cudaStream_t st) {
-    if (f.mode == PT_MODE_EXTENDED) k_shade<true><<<(cap + 127) / 128, 128, 0, st>>>(s, f, w, cur, did);
-    else k_shade<false><<<(cap + 127) / 128, 128, 0, st>>>(s, f, w, cur, did);
+int pt_launch_wave_end(const PtWave &w, cudaStream_t st) {
+    k_wave_end<<<1, 1, 0, st>>>(w);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
 
-int pt_launch_shadow(const PtScene &s, const PtWave &w, uint32_t cap, int queue, cudaStream_t st) {
-    const unsigned blocks = (cap + 127) / 128;
-    if (s.big_stack) k_shadow<256><<<blocks, 128, 0, st>>>(s, w, queue);
-    else k_shadow<64><<<blocks, 128, 0, st>>>(s, w, queue);
+int pt_launch_raygen(const PtWave &w, cudaStream_t st) {
+    k_raygen<<<(w.cap + 255) / 256, 256, 0, st>>>(w);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
 
-int pt_launch_accumulate(const PtFrame &f, const PtWave &w, cudaStream_t st) {
-    k_accumulate<<<(f.npix + 255) / 256, 256, 0, st>>>(f, w);
+int pt_launch_shade(const PtWave &w, int cur, uint32_t did, bool ext, cudaStream_t st) {
+    if (ext) k_shade<true><<<(w.cap + 127) / 128, 128, 0, st>>>(w, cur, did);
+    else k_shade<false><<<(w.cap + 127) / 128, 128, 0, st>>>(w, cur, did);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pt_launch_shadow(const PtWave &w, int queue, bool big_stack, cudaStream_t st) {
+    const unsigned blocks = (w.cap + 127) / 128;
+    if (big_stack) k_shadow<256><<<blocks, 128, 0, st>>>(w, queue);
+    else k_shadow<64><<<blocks, 128, 0, st>>>(w, queue);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+static int g_batch_grid[2] = {0, 0};
+
+// Grid of the persistent batch traversal (one full residency of the GPU); computed outside
+// any stream capture.
+int trace_closest_batch_prepare(bool big_stack) {
+    int &g = g_batch_grid[big_stack ? 1 : 0];
+    if (g == 0) {
+        int per_sm = 0, sms = 0, dev = 0;
+        RT_CUDA_TRY(cudaGetDevice(&dev));
+        RT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        if (big_stack) RT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_batch<256>, 128, 0));
+        else RT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_batch<64>, 128, 0));
+        g = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    return RT_OK;
+}
+
+int trace_closest_batch(const PtWave &w, int cur, bool big_stack, cudaStream_t st) {
+    const int g = g_batch_grid[big_stack ? 1 : 0];
+    if (g == 0) {
+        set_error("batch traversal grid not prepared");
+        return RT_ERR_STATE;
+    }
+    if (big_stack) k_trace_batch<256><<<g, 128, 0, st>>>(w, cur);
+    else k_trace_batch<64><<<g, 128, 0, st>>>(w, cur);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pt_launch_accumulate(const PtWave &w, cudaStream_t st) {
+    k_accumulate<<<(w.cap + 255) / 256, 256, 0, st>>>(w);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

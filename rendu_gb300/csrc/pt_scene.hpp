@@ -1,6 +1,7 @@
 // Host-side state of a path-tracer scene and the per-render launch parameters.
 #pragma once
 
+#include <memory>
 #include <vector>
 
 #include "pt_device.cuh"
@@ -8,30 +9,45 @@
 
 namespace rgb {
 
-// Per-render constants (camera, sampling grid, wave window).
-struct PtFrame {
+// One render of a call (a batch has many): its scene, camera frame, sampling grid, options.
+struct PtJob {
+    PtScene scene;
     float corner[3], dx[3], dy[3], eye[3];
-    uint32_t W, H, npix, spp, cx, cy, depth;
+    uint32_t W, H, npix, spp, cx, cy, depth, comps;
     float cell_x, cell_y;
-    uint32_t s0, S;  // this wave covers sample indices [s0, s0 + S)
-    uint32_t seed_lo, seed_hi;
-    int mode;     // PT_MODE_REFERENCE / PT_MODE_EXTENDED
     float clamp;  // per-sample clamp (<= 0: none)
+    uint32_t seed_lo, seed_hi;
+    uint32_t accum_offset;  // first pixel of this job in the accumulation buffer
 };
 
-// Device buffers of one wave (capacity P = npix * S paths).
+// Pixels [pixel0, pixel0 + npix) of `job` x samples [s0, s0 + S), laid out sample-major
+// from wave path `path0`.
+struct PtTile {
+    uint32_t job, pixel0, npix, s0, S, path0;
+};
+
+// Device buffers and tables of the wave engine (capacity `cap` paths per wave).
 struct PtWave {
-    float4 *atten, *color;
+    float4 *atten, *color;  // atten.w: pdf of the BSDF sample that made the current ray
     float2 *ndc;
+    uint32_t *pjob, *ppix, *psamp;  // per path: job, pixel, sample
     rt_ray *qray[2];
     uint32_t *qpath[2];
     rt_hit *hits;
     rt_ray *sray;
     float4 *scontrib;
-    uint32_t *counters;  // [0], [1]: ray queues, [2]: analytic-light shadow queue, [3]: emitter/env shadow queue
-    uint32_t shadow_cap; // the second shadow queue starts at this entry
+    uint32_t shadow_cap;  // the second shadow queue starts at this entry
+    uint32_t *counters;   // [0], [1] ray queues, [2] analytic-light shadows, [3] emitter/env shadows, [4] wave
+    unsigned long long *fetch;  // ray-fetch counter of the persistent traversal
     unsigned long long *stats;  // [0] primary, [1] bounce, [2] shadow rays
-    float *accum;       // npix x 3
+    float *accum;               // 3 floats per pixel of every job
+    const PtJob *jobs;
+    const JobBvh *bvhs;
+    const PtTile *tiles;
+    const uint32_t *wave_tiles;  // tiles of wave k: [wave_tiles[k], wave_tiles[k + 1])
+    const uint32_t *wave_paths;  // paths of wave k
+    unsigned *status;
+    uint32_t cap;
 };
 
 struct HostTex {
@@ -50,14 +66,67 @@ struct HostObject {
 };
 
 int pt_launch_material(const float *cases, const float *uniforms, uint32_t n, float *out, cudaStream_t st);
-int pt_launch_raygen(const PtFrame &f, const PtWave &w, cudaStream_t st);
-int pt_launch_trace(rt_ctx *rc, const PtWave &w, int cur, uint32_t cap, cudaStream_t st);
-int pt_launch_shade(const PtScene &s, const PtFrame &f, const PtWave &w, int cur, uint32_t did, uint32_t cap,
-                    cudaStream_t st);
-int pt_launch_shadow(const PtScene &s, const PtWave &w, uint32_t cap, int queue, cudaStream_t st);
-int pt_launch_accumulate(const PtFrame &f, const PtWave &w, cudaStream_t st);
+int pt_launch_wave_begin(const PtWave &w, cudaStream_t st);
+int pt_launch_wave_end(const PtWave &w, cudaStream_t st);
+int pt_launch_raygen(const PtWave &w, cudaStream_t st);
+int pt_launch_shade(const PtWave &w, int cur, uint32_t did, bool ext, cudaStream_t st);
+int pt_launch_shadow(const PtWave &w, int queue, bool big_stack, cudaStream_t st);
+int pt_launch_accumulate(const PtWave &w, cudaStream_t st);
 int pt_launch_load(const float *img, uint32_t comps, uint32_t npix, float *accum, cudaStream_t st);
 int pt_launch_store(const float *accum, uint32_t npix, float spp, uint32_t comps, float *img, cudaStream_t st);
+// Closest hit for the wave's ray queue `cur`, each ray against its job's hierarchy.
+int trace_closest_batch(const PtWave &w, int cur, bool big_stack, cudaStream_t st);
+int trace_closest_batch_prepare(bool big_stack);
+// Camera::pose + Camera::pixelShifts (Camera.cpp:10-18, 42-49).
+void pixel_shifts(const pt_camera_desc &c, float corner[3], float dx[3], float dy[3], float eye[3]);
+
+// One render request of the engine.
+struct JobSpec {
+    pt_scene *scene;
+    pt_camera_desc camera;
+    uint32_t samples, depth;
+    uint64_t seed;
+    float *image;
+    uint32_t width, height, components;
+    float clamp;
+};
+
+// Wave-engine tuning (chosen by pt_batch_autotune or defaults).
+struct Tuning {
+    uint32_t wave_paths;   // capacity of a wave
+    uint32_t tile_pixels;  // pixels per tile
+    uint32_t max_samples;  // most samples of one pixel in one wave (power of two)
+};
+
+Tuning default_tuning();
+bool load_tuning(const char *path, Tuning &t);
+
+// Runs renders as waves replayed from one captured CUDA graph. Owns every device buffer it
+// uses (grow-only) and the instantiated graph, reused while the launch shape is unchanged.
+class WaveEngine {
+  public:
+    explicit WaveEngine(int device) : device_(device) {}
+    ~WaveEngine();
+    int run(const std::vector<JobSpec> &jobs, int mode, const Tuning &t, bool device_images, cudaStream_t st,
+            pt_render_stats *stats);
+
+  private:
+    int ensure_capacity(uint64_t cap, uint64_t accum_pixels, uint64_t ntiles, uint64_t nwaves, size_t njobs,
+                        uint64_t staging_floats);
+    int capture(const PtWave &w, uint32_t depth, bool ext, bool shadow_a, bool shadow_b, bool big_stack);
+    int device_;
+    cudaStream_t capture_stream_ = nullptr;
+    DevBuf atten_, color_, ndc_, pjob_, ppix_, psamp_, qray0_, qray1_, qpath0_, qpath1_, hits_, sray_, scontrib_;
+    DevBuf counters_, accum_, jobs_, bvhs_, tiles_, wave_tiles_, wave_paths_, staging_;
+    uint64_t cap_ = 0;
+    uint64_t generation_ = 0;  // bumped whenever a buffer the graph refers to moves
+    cudaGraphExec_t exec_ = nullptr;
+    struct Key {
+        uint64_t generation, cap;
+        uint32_t depth;
+        bool ext, shadow_a, shadow_b, big_stack;
+    } key_{};
+};
 
 }  // namespace rgb
 
@@ -81,11 +150,13 @@ struct pt_scene {
     float env_intensity = 1.0f;
     rgb::PtScene dev{};
 
-    // Wave buffers (grow-only).
-    rgb::DevBuf w_atten, w_color, w_ndc, w_qray0, w_qray1, w_qpath0, w_qpath1, w_hits, w_sray, w_scontrib,
-        w_counters, w_stats, w_accum, w_image;
-    size_t wave_cap = 0;
-    size_t accum_cap = 0;
+    std::unique_ptr<rgb::WaveEngine> engine;  // runs pt_render
 
+    pt_render_stats last{};
+};
+
+struct pt_batch {
+    int device = 0;
+    std::unique_ptr<rgb::WaveEngine> engine;
     pt_render_stats last{};
 };

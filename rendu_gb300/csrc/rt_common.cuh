@@ -82,6 +82,14 @@ struct __align__(16) BvhTri {
     float4 e2;  // xyz, w unused
 };
 
+// Hierarchy of one job of a batch (the traversal picks it per ray).
+struct JobBvh {
+    const BvhNode *nodes;
+    const BvhTri *tris;
+    int empty;  // no triangles: every ray misses
+    int pad;
+};
+
 // Device status word bits (set with atomicOr by kernels, read by the host).
 enum : unsigned {
     RT_DEV_STACK_OVERFLOW = 1u,

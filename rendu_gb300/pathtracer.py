@@ -142,3 +142,71 @@ def material_sample(cases, uniforms):
     out = np.zeros((len(c), 6), np.float32)
     L.call("pt_material_sample", c.ctypes.data, u.ctypes.data, len(c), out.ctypes.data, 0)
     return out
+
+
+class BatchRenderer:
+    """Many renders in one call (pt_batch_render): jobs of different scenes, resolutions,
+    sample counts and depths share waves replayed from one CUDA graph. Each job is a dict
+    with ``tracer`` (a PathTracer), ``camera``, ``samples``, ``depth``, ``seed`` and
+    ``image`` (host float32 (H, W, C) arrays, or CUDA tensors for all jobs)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        L.call("pt_batch_create", C.byref(h), int(device))
+        self._h = h
+        self.device = device
+
+    @staticmethod
+    def _jobs(jobs):
+        arr = (L.pt_batch_job * len(jobs))()
+        dev = None
+        for k, j in enumerate(jobs):
+            img = j["image"]
+            is_dev = type(img).__module__.startswith("torch") and getattr(img, "is_cuda", False)
+            if dev is None:
+                dev = is_dev
+            if dev != is_dev:
+                raise TypeError("all images of a batch must be on the host or all on the device")
+            hgt, wid, comp = img.shape
+            ptr = img.data_ptr() if is_dev else img.ctypes.data
+            cam = j["camera"]
+            arr[k] = L.pt_batch_job(j["tracer"]._h.value, camera_desc(cam), int(j["samples"]), int(j["depth"]),
+                                    int(j.get("seed", 0)), ptr, wid, hgt, comp)
+        return arr, bool(dev)
+
+    def render(self, jobs, mode: int = 0, clamp: float = 5.0, tuning=None) -> dict:
+        arr, dev = self._jobs(jobs)
+        opts = L.pt_render_options(int(mode), float(clamp))
+        t = None if tuning is None else L.pt_batch_tuning(*(int(tuning[k]) for k in ("wave_paths", "tile_pixels",
+                                                                                       "max_samples")))
+        stream = None
+        if dev:
+            import torch
+
+            stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        L.call("pt_batch_render", self._h, arr, len(jobs), C.byref(opts), C.byref(t) if t is not None else None,
+               stream, L.RT_FLAG_DEVICE_PTRS if dev else 0)
+        s = L.pt_render_stats()
+        L.call("pt_batch_get_stats", self._h, C.byref(s))
+        d = {k: getattr(s, k) for k, _ in s._fields_}
+        d["rays"] = d["primary_rays"] + d["bounce_rays"] + d["shadow_rays"]
+        return d
+
+    def autotune(self, jobs, mode: int = 0, clamp: float = 5.0, cache_path: str | None = None) -> dict:
+        arr, _ = self._jobs(jobs)
+        opts = L.pt_render_options(int(mode), float(clamp))
+        out = L.pt_batch_tuning()
+        L.call("pt_batch_autotune", self._h, arr, len(jobs), C.byref(opts),
+               cache_path.encode() if cache_path else None, C.byref(out))
+        return {"wave_paths": out.wave_paths, "tile_pixels": out.tile_pixels, "max_samples": out.max_samples}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            L.lib().pt_batch_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -556,3 +556,53 @@ def open_cornell_scene(seed: int = 20261204) -> Scene:
     keep = [o for k, o in enumerate(sc.objects) if k != 1]  # drop the ceiling (object 1)
     sc.objects = keep
     return sc
+
+
+def batch_workload(seed: int = 20261207, jobs: int = 64, tri_range=(10_000, 500_000), res_range=(128, 1024),
+                   spp_range=(4, 256), depth_range=(3, 10)):
+    """The batched-rendering workload: `jobs` seeded scenes, each with a log-uniform triangle
+    count in `tri_range` (instances of displaced icospheres and boxes on a ground plane,
+    emissive quads, cubemap sky), a log-uniform square resolution in `res_range`, a
+    log-uniform sample count in `spp_range` rounded to a power of two and a uniform depth in
+    `depth_range`. Returns a list of dicts (scene, width, height, samples, depth, seed)."""
+    rng = np.random.default_rng(seed)
+    protos = {}
+    out = []
+    for k in range(jobs):
+        tris = int(np.exp(rng.uniform(np.log(tri_range[0]), np.log(tri_range[1]))))
+        res = int(np.exp(rng.uniform(np.log(res_range[0]), np.log(res_range[1]))))
+        spp = int(2 ** round(np.log2(np.exp(rng.uniform(np.log(spp_range[0]), np.log(spp_range[1]))))))
+        depth = int(rng.integers(depth_range[0], depth_range[1] + 1))
+        sub = 4 if tris < 60_000 else 5
+        per = 20 * 4 ** sub
+        inst = max(2, int(round(tris / per)))
+        sc = _batch_scene(rng, inst, sub, protos)
+        out.append({"scene": sc, "width": res, "height": res, "samples": spp, "depth": depth,
+                    "seed": int(seed * 100 + k)})
+    return out
+
+
+def _batch_scene(rng, instances, sub, protos):
+    sc = Scene()
+    key = ("ico", sub)
+    if key not in protos:
+        protos[key] = [icosphere_mesh(sub, seed=100 + j, displacement=0.1).with_frames() for j in range(3)]
+    meshes = [sc.add_mesh(m) for m in protos[key]]
+    box = sc.add_mesh(box_mesh())
+    sc.add_object(sc.add_mesh(quad_mesh((-20, 0, 20), (40, 0, 0), (0, 0, -40))), sc.add_material((0.5, 0.5, 0.5)))
+    side = int(math.ceil(math.sqrt(instances)))
+    for k in range(instances):
+        x = ((k % side) + 0.5) / side * 24 - 12
+        z = ((k // side) + 0.5) / side * 24 - 12
+        s = float(rng.uniform(0.4, 1.0))
+        mat = sc.add_material(rng.uniform(0.2, 0.9, 3), rough=float(rng.uniform(0.05, 1.0)), metal=float(rng.random() < 0.3))
+        if k % 4 == 3:
+            sc.add_object(box, mat, translation((x, s, z)) @ rotation_y(rng.uniform(0, 6.28)) @ scaling(1.5 * s))
+        else:
+            sc.add_object(meshes[k % 3], mat, translation((x, s * 1.1, z)) @ scaling(s))
+    sc.add_object(sc.add_mesh(quad_mesh((-2, 7, 2), (4, 0, 0), (0, 0, -4), normal=(0, -1, 0))),
+                  sc.add_material((20.0, 18.0, 16.0), emissive=True))
+    faces = [constant_texture([0.4 + 0.05 * f, 0.5, 0.7], 4) for f in range(6)]
+    sc.background = {"mode": 2, "color": (0, 0, 0), "tex": tuple(sc.add_texture(f) for f in faces)}
+    sc.camera = {"eye": (0.0, 8.0, 20.0), "center": (0.0, 1.0, 0.0), "up": (0.0, 1.0, 0.0), "fov": 1.0, "ratio": 1.0}
+    return sc
