@@ -116,6 +116,12 @@ int WaveEngine::capture(const PtWave &w, uint32_t depth, bool ext, bool shadow_a
     int cur = 0;
     for (uint32_t did = 0; r == RT_OK && did < depth; ++did) {
         r = trace_closest_batch(w, cur, big_stack, cs);
+        // The queues shading appends to start empty: the next ray queue and both shadow queues.
+        if (r == RT_OK && (cudaMemsetAsync(&w.counters[cur ^ 1], 0, 4, cs) != cudaSuccess ||
+                           cudaMemsetAsync(&w.counters[2], 0, 8, cs) != cudaSuccess)) {
+            set_error("cudaMemsetAsync failed during capture");
+            r = RT_ERR_CUDA;
+        }
         if (r == RT_OK) r = pt_launch_shade(w, cur, did, ext, cs);
         if (r == RT_OK && shadow_a) r = pt_launch_shadow(w, 0, big_stack, cs);
         if (r == RT_OK && shadow_b) r = pt_launch_shadow(w, 1, big_stack, cs);

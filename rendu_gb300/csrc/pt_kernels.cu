@@ -129,7 +129,7 @@ __device__ __forceinline__ void push_shadow(const PtWave &w, uint32_t slot, f3 o
 template <bool EXT>
 __global__ void __launch_bounds__(128) k_shade(PtWave w, int cur, uint32_t did) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = w.counters[cur];
+    const uint32_t n = min(w.counters[cur], w.cap);
     if (i == 0) {
         atomicAdd(&w.stats[did == 0 ? 0 : 1], (unsigned long long)n);  // rays traced this bounce
         *w.fetch = 0ull;  // ray-fetch counter of the next bounce's traversal
@@ -295,7 +295,11 @@ __global__ void __launch_bounds__(128) k_shade(PtWave w, int cur, uint32_t did) 
     }
     w.color[path] = make_float4(color.x, color.y, color.z, 0.0f);
     w.atten[path] = make_float4(atten.x, atten.y, atten.z, prev_pdf);
-    const uint32_t slot = warp_append(&w.counters[nxt], cont);
+    uint32_t slot = warp_append(&w.counters[nxt], cont);
+    if (cont && slot >= w.cap) {  // cannot happen (one append per path); never write past the queue
+        atomicOr(w.status, RT_DEV_QUEUE_OVERFLOW);
+        cont = false;
+    }
     if (cont) {
         w.qray[nxt][slot] = rt_ray{next_o.x, next_o.y, next_o.z, 1e-4f, next_d.x, next_d.y, next_d.z, 1e8f};
         w.qpath[nxt][slot] = path;
@@ -304,16 +308,18 @@ __global__ void __launch_bounds__(128) k_shade(PtWave w, int cur, uint32_t did) 
     // in that order: a path never has two shadow rays in one queue, so the radiance update
     // in k_shadow is race-free and the summation order is fixed.
     const uint32_t sa = warp_append(&w.counters[2], sh_a);
-    if (sh_a) push_shadow(w, sa, sa_o, sa_d, sa_max, sa_c, path);
+    if (sh_a && sa < w.shadow_cap) push_shadow(w, sa, sa_o, sa_d, sa_max, sa_c, path);
+    else if (sh_a) atomicOr(w.status, RT_DEV_QUEUE_OVERFLOW);
     const uint32_t sb = warp_append(&w.counters[3], sh_b);
-    if (sh_b) push_shadow(w, w.shadow_cap + sb, sb_o, sb_d, sb_max, sb_c, path);
+    if (sh_b && sb < w.shadow_cap) push_shadow(w, w.shadow_cap + sb, sb_o, sb_d, sb_max, sb_c, path);
+    else if (sh_b) atomicOr(w.status, RT_DEV_QUEUE_OVERFLOW);
 }
 
 // PathTracer::checkVisibility (PathTracer.cpp:124-157).
 template <int STACK>
 __global__ void __launch_bounds__(128) k_shadow(PtWave w, int queue) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t n = w.counters[2 + queue];
+    const uint32_t n = min(w.counters[2 + queue], w.shadow_cap);
     if (i == 0) atomicAdd(&w.stats[2], (unsigned long long)n);
     if (i >= n) return;
     const uint32_t e = (queue ? w.shadow_cap : 0u) + i;
@@ -376,7 +382,7 @@ __global__ void __launch_bounds__(128) k_shadow(PtWave w, int queue) {
 // lane traverses the hierarchy of its ray's job.
 template <int STACK>
 __global__ void __launch_bounds__(128) k_trace_batch(PtWave w, int cur) {
-    const size_t n = w.counters[cur];
+    const size_t n = min(w.counters[cur], w.cap);
     const rt_ray *__restrict__ rays = w.qray[cur];
     const uint32_t *__restrict__ qpath = w.qpath[cur];
     const unsigned lane = threadIdx.x & 31;
