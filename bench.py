@@ -22,6 +22,9 @@ beside it.
                large (200 instances, ~2M triangles, 1920x1080, 64 spp, depth 8) scenes:
                Mrays/s counting primary, bounce and shadow rays, device time inside
                pt_render, beside the C restatement of PathTracer::render on host cores.
+* batch    -- 64 seeded jobs (10k-500k triangles, 128^2-1024^2, 4-256 spp, depth 3-10) in
+               one batched call (waves replayed from a CUDA graph, autotuned), vs the same
+               jobs rendered one call after another.
 * --impl reference -- only that CPU path, as the reference arm.
 Under torchrun (N > 1) every rank traces its own 16M rays (weak scaling, no collective on
 the data path); value = all rays / max-over-ranks time.
@@ -226,6 +229,73 @@ def run_pathtracer(name, steps, cpu: bool):
     return out
 
 
+def run_batch(cpu: bool, tune: bool = True):
+    """Batched rendering: 64 seeded jobs (10k-500k triangles, 128^2-1024^2, 4-256 spp,
+    depth 3-10) in one pt_batch_render call (waves replayed from one CUDA graph, autotuned
+    tuning), against the same jobs rendered one pt_render call after another."""
+    import torch
+
+    import rendu_gb300 as R
+    from rendu_gb300 import scenes as S
+
+    wl = S.batch_workload()
+    t0 = time.perf_counter()
+    tracers = [R.PathTracer(j["scene"]) for j in wl]
+    upload_s = time.perf_counter() - t0
+    jobs = []
+    for j, tr in zip(wl, tracers):
+        jobs.append({"tracer": tr, "camera": dict(j["scene"].camera, ratio=1.0), "samples": j["samples"],
+                     "depth": j["depth"], "seed": j["seed"],
+                     "image": torch.zeros((j["height"], j["width"], 3), dtype=torch.float32, device="cuda")})
+    br = R.BatchRenderer(0)
+    tuning, tune_s = None, 0.0
+    if tune:
+        t0 = time.perf_counter()
+        tuning = br.autotune(jobs, cache_path=os.path.join(ROOT, "gpurun_out", "batch_tuning.json")
+                             if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None)
+        tune_s = time.perf_counter() - t0
+    br.render(jobs, tuning=tuning)  # warm-up (graph capture)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = br.render(jobs, tuning=tuning)
+    torch.cuda.synchronize()
+    batch_s = time.perf_counter() - t0
+    seq_ms, seq_rays = 0.0, 0
+    t0 = time.perf_counter()
+    for j in jobs:
+        j["tracer"].render(j["camera"], j["samples"], j["depth"], j["image"], seed=j["seed"])
+        s1 = j["tracer"].last_stats()
+        seq_ms += s1["device_ms"]
+        seq_rays += s1["rays"]
+    torch.cuda.synchronize()
+    seq_s = time.perf_counter() - t0
+    out = {"workload": f"{len(jobs)} jobs, {sum(j['scene'].triangle_count for j in wl)} triangles in total, "
+                       f"{sum(j['width'] * j['height'] for j in wl)} pixels, "
+                       f"{sum(j['width'] * j['height'] * j['samples'] for j in wl)} paths",
+           "value": round(st["rays"] / (st["device_ms"] * 1e3), 1), "unit": "Mrays/s",
+           "batch_device_ms": round(st["device_ms"], 1), "batch_wall_s": round(batch_s, 3),
+           "sequential_device_ms": round(seq_ms, 1), "sequential_wall_s": round(seq_s, 3),
+           "speedup_vs_sequential": round(seq_s / batch_s, 2), "rays": st["rays"], "tuning": tuning,
+           "autotune_s": round(tune_s, 1), "scene_uploads_s": round(upload_s, 2)}
+    if cpu:
+        from oracle import oracle as O
+
+        O.build_port()
+        threads = max((os.cpu_count() or 2) - 1, 1)
+        rays, dt = 0, 0.0
+        for j in wl[:8]:  # bounded sample: the first 8 jobs at 1 spp
+            port = O.PortPathTracer(j["scene"])
+            t0 = time.perf_counter()
+            port.render(dict(j["scene"].camera, ratio=1.0), 1, j["depth"], j["width"], j["height"], seed=1,
+                        threads=threads)
+            dt += time.perf_counter() - t0
+            rays += int(port.rays.sum())
+        out["cpu_baseline"] = {"value": round(rays / dt / 1e6, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
+                               "sample": "first 8 jobs at 1 spp"}
+        out["speedup_vs_cpu"] = round(out["value"] / out["cpu_baseline"]["value"], 1)
+    return out
+
+
 def run_reference(args):
     """Reference arm: the reference's Raycaster algorithm (C restatement; the reference's own
     sources do not travel to this host) on all host threads, same workload and metric."""
@@ -414,6 +484,7 @@ def main():
         }
         if not args.no_pt:
             out["pathtracer"] = {name: run_pathtracer(name, 3, not args.no_cpu) for name in PT_CONFIGS}
+            out["batch"] = run_batch(not args.no_cpu)
         clk.__exit__(None, None, None)
         out["clocks"] = clk.summary()
         if not args.no_cpu:
