@@ -273,6 +273,11 @@ typedef struct pt_render_options {
     int32_t mode;  /* PT_MODE_REFERENCE or PT_MODE_EXTENDED                                      */
     float clamp;   /* per-sample radiance clamp; the reference uses 5 (PathTracer.cpp:288);
                       <= 0 disables it                                                            */
+    int32_t accum_fp64; /* accumulate the samples of each pixel in double precision (for
+                           high-spp reference images); the image itself stays float       */
+    float *aov;    /* optional feature buffer, width x height x 7 floats (host or device like
+                      the image): first-hit albedo (rgb), shading normal (xyz), distance,
+                      averaged over the pixel's samples; overwritten, not accumulated     */
 } pt_render_options;
 
 /* Environment map for PT_MODE_EXTENDED: an equirectangular float image (texture id from

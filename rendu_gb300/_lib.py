@@ -62,7 +62,7 @@ class pt_camera_desc(C.Structure):
 
 
 class pt_render_options(C.Structure):
-    _fields_ = [("mode", C.c_int32), ("clamp", C.c_float)]
+    _fields_ = [("mode", C.c_int32), ("clamp", C.c_float), ("accum_fp64", C.c_int32), ("aov", C.c_void_p)]
 
 
 class pt_batch_job(C.Structure):

@@ -509,7 +509,11 @@ int pt_render_ex(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, ui
     if (!s->engine) s->engine.reset(new WaveEngine(s->device));
     const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
     cudaStream_t st = dev ? static_cast<cudaStream_t>(stream) : s->rc->stream;
-    JobSpec js{s, *camera, samples, depth, seed, image, width, height, components, opts ? opts->clamp : 5.0f};
+    JobSpec js{s,          *camera,          samples,
+               depth,      seed,             image,
+               width,      height,           components,
+               opts ? opts->clamp : 5.0f,    opts ? opts->accum_fp64 : 0,
+               opts ? opts->aov : nullptr};
     // One tile of every pixel per wave, as many samples per wave as ~8M paths allow.
     Tuning t{1u << 23, width * height, 1u << 30};
     if ((uint64_t)width * height > t.wave_paths) t.wave_paths = width * height;
@@ -551,7 +555,7 @@ static int batch_specs(const pt_batch_job *jobs, size_t n, const pt_render_optio
         const int r = check_job(j.scene, j.samples, j.width, j.height, j.components);
         if (r != RT_OK) return r;
         out.push_back(JobSpec{j.scene, j.camera, j.samples, j.depth, j.seed, j.image, j.width, j.height, j.components,
-                              opts ? opts->clamp : 5.0f});
+                              opts ? opts->clamp : 5.0f, opts ? opts->accum_fp64 : 0, nullptr});
     }
     return RT_OK;
 }

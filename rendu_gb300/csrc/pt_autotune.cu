@@ -103,7 +103,7 @@ extern "C" int pt_batch_autotune(pt_batch *b, const pt_batch_job *jobs, size_t n
         // Reduced copy: 1/8 of the samples, results discarded (no image).
         const uint32_t spp = j.samples >= 8 ? j.samples / 8 : 1;
         specs.push_back(JobSpec{j.scene, j.camera, spp, j.depth, j.seed, nullptr, j.width, j.height, j.components,
-                                opts ? opts->clamp : 5.0f});
+                                opts ? opts->clamp : 5.0f, opts ? opts->accum_fp64 : 0, nullptr});
     }
     int prev = -1;
     cudaGetDevice(&prev);

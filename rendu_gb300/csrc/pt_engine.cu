@@ -68,14 +68,14 @@ WaveEngine::~WaveEngine() {
     if (exec_) cudaGraphExecDestroy(exec_);
     if (capture_stream_) cudaStreamDestroy(capture_stream_);
     for (DevBuf *b : {&atten_, &color_, &ndc_, &pjob_, &ppix_, &psamp_, &qray0_, &qray1_, &qpath0_, &qpath1_, &hits_,
-                      &sray_, &scontrib_, &counters_, &accum_, &jobs_, &bvhs_, &tiles_, &wave_tiles_, &wave_paths_,
-                      &staging_})
+                      &sray_, &scontrib_, &counters_, &accum_, &accum64_, &aov0_, &aov1_, &aov_accum_, &aov_staging_,
+                      &jobs_, &bvhs_, &tiles_, &wave_tiles_, &wave_paths_, &staging_})
         b->release();
     if (prev >= 0 && prev != device_) cudaSetDevice(prev);
 }
 
 int WaveEngine::ensure_capacity(uint64_t cap, uint64_t accum_pixels, uint64_t ntiles, uint64_t nwaves, size_t njobs,
-                                uint64_t staging_floats) {
+                                uint64_t staging_floats, bool fp64, bool aov) {
     bool moved = false;
     int r = RT_OK;
     auto grow = [&](DevBuf &b, uint64_t bytes) {
@@ -99,6 +99,13 @@ int WaveEngine::ensure_capacity(uint64_t cap, uint64_t accum_pixels, uint64_t nt
     grow(wave_tiles_, (nwaves + 1) * 4);
     grow(wave_paths_, std::max<uint64_t>(nwaves, 1) * 4);
     if (staging_floats) grow(staging_, staging_floats * 4);
+    if (fp64) grow(accum64_, std::max<uint64_t>(accum_pixels, 1) * 24);
+    if (aov) {
+        grow(aov0_, cap_ * 16);
+        grow(aov1_, cap_ * 16);
+        grow(aov_accum_, std::max<uint64_t>(accum_pixels, 1) * 28);
+        grow(aov_staging_, std::max<uint64_t>(accum_pixels, 1) * 28);
+    }
     if (moved) ++generation_;
     return r;
 }
@@ -160,7 +167,7 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
     std::vector<uint32_t> S(jobs.size()), chunk(jobs.size()), passes(jobs.size());
     uint64_t accum_pixels = 0, staging = 0;
     uint32_t depth = 0, max_passes = 0;
-    bool shadow_a = false, shadow_b = false, big_stack = false;
+    bool shadow_a = false, shadow_b = false, big_stack = false, any_fp64 = false, any_aov = false;
     for (size_t j = 0; j < jobs.size(); ++j) {
         const JobSpec &js = jobs[j];
         PtJob &J = hj[j];
@@ -187,6 +194,10 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
         J.seed_lo = (uint32_t)js.seed;
         J.seed_hi = (uint32_t)(js.seed >> 32);
         J.accum_offset = (uint32_t)accum_pixels;
+        J.fp64 = js.fp64 ? 1 : 0;
+        J.aov = js.aov ? 1 : 0;
+        any_fp64 |= js.fp64 != 0;
+        any_aov |= js.aov != nullptr;
         accum_pixels += J.npix;
         staging += (uint64_t)J.npix * J.comps;
         hb[j] = JobBvh{J.scene.nodes, J.scene.tris, J.scene.empty, 0};
@@ -234,7 +245,8 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
     }
     close_wave();
     const uint64_t nwaves = wave_paths.size();
-    int r = ensure_capacity(cap, accum_pixels, tiles.size(), nwaves, jobs.size(), device_images ? 0 : staging);
+    int r = ensure_capacity(cap, accum_pixels, tiles.size(), nwaves, jobs.size(), device_images ? 0 : staging, any_fp64,
+                            any_aov);
     if (r != RT_OK) return r;
 
     PtWave w{};
@@ -257,6 +269,10 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
     w.stats = reinterpret_cast<unsigned long long *>(counters_.as<char>() + 64);
     w.status = reinterpret_cast<unsigned *>(counters_.as<char>() + 96);
     w.accum = accum_.as<float>();
+    w.accum64 = any_fp64 ? accum64_.as<double>() : nullptr;
+    w.aov0 = any_aov ? aov0_.as<float4>() : nullptr;
+    w.aov1 = any_aov ? aov1_.as<float4>() : nullptr;
+    w.aov_accum = any_aov ? aov_accum_.as<float>() : nullptr;
     w.jobs = jobs_.as<PtJob>();
     w.bvhs = bvhs_.as<JobBvh>();
     w.tiles = tiles_.as<PtTile>();
@@ -270,6 +286,7 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
     RT_CUDA_TRY(cudaMemcpyAsync(wave_tiles_.ptr, wave_tiles.data(), wave_tiles.size() * 4, cudaMemcpyHostToDevice, st));
     RT_CUDA_TRY(cudaMemcpyAsync(wave_paths_.ptr, wave_paths.data(), wave_paths.size() * 4, cudaMemcpyHostToDevice, st));
     RT_CUDA_TRY(cudaMemsetAsync(counters_.ptr, 0, 128, st));
+    if (any_aov) RT_CUDA_TRY(cudaMemsetAsync(aov_accum_.ptr, 0, accum_pixels * 28, st));
     // Images: accumulate into what the caller passed (PathTracer.cpp:288).
     std::vector<float *> dimg(jobs.size());
     uint64_t off = 0;
@@ -285,7 +302,8 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
                 RT_CUDA_TRY(cudaMemsetAsync(dimg[j], 0, n * 4, st));
             off += n;
         }
-        r = pt_launch_load(dimg[j], hj[j].comps, hj[j].npix, w.accum + 3 * (size_t)hj[j].accum_offset, st);
+        r = pt_launch_load(dimg[j], hj[j].comps, hj[j].npix, w.accum + 3 * (size_t)hj[j].accum_offset,
+                           hj[j].fp64 ? w.accum64 + 3 * (size_t)hj[j].accum_offset : nullptr, st);
         if (r != RT_OK) return r;
     }
     // ---- the graph ------------------------------------------------------------------------------
@@ -316,14 +334,23 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
             r = RT_ERR_CUDA;
         }
     if (r == RT_OK && cudaEventRecord(e1, st) != cudaSuccess) r = RT_ERR_CUDA;
-    for (size_t j = 0; j < jobs.size() && r == RT_OK; ++j)
-        r = pt_launch_store(w.accum + 3 * (size_t)hj[j].accum_offset, hj[j].npix, (float)hj[j].spp, hj[j].comps,
-                            dimg[j], st);
+    std::vector<float *> daov(jobs.size(), nullptr);
+    for (size_t j = 0; j < jobs.size() && r == RT_OK; ++j) {
+        const size_t off3 = 3 * (size_t)hj[j].accum_offset, off7 = 7 * (size_t)hj[j].accum_offset;
+        if (jobs[j].aov) daov[j] = device_images ? jobs[j].aov : aov_staging_.as<float>() + off7;
+        r = pt_launch_store(w.accum + off3, hj[j].fp64 ? w.accum64 + off3 : nullptr, hj[j].npix, (float)hj[j].spp,
+                            hj[j].comps, dimg[j], jobs[j].aov ? w.aov_accum + off7 : nullptr, daov[j], st);
+    }
     unsigned long long hs[3] = {0, 0, 0};
     unsigned hstatus = 0;
     if (r == RT_OK && (cudaMemcpyAsync(hs, w.stats, sizeof(hs), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
                        cudaMemcpyAsync(&hstatus, w.status, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess))
         r = RT_ERR_CUDA;
+    if (r == RT_OK && !device_images)
+        for (size_t j = 0; j < jobs.size() && r == RT_OK; ++j)
+            if (jobs[j].aov && cudaMemcpyAsync(jobs[j].aov, daov[j], (size_t)hj[j].npix * 28, cudaMemcpyDeviceToHost,
+                                               st) != cudaSuccess)
+                r = RT_ERR_CUDA;
     if (r == RT_OK && !device_images)
         for (size_t j = 0; j < jobs.size() && r == RT_OK; ++j)
             if (jobs[j].image &&

@@ -85,6 +85,10 @@ __global__ void k_raygen(PtWave w) {
     w.atten[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     w.color[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     w.ndc[p] = make_float2(nx, ny);
+    if (J.aov) {
+        w.aov0[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        w.aov1[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
 }
 
 struct SurfaceHit {
@@ -177,6 +181,10 @@ __global__ void __launch_bounds__(128) k_shade(PtWave w, int cur, uint32_t did) 
             next_o = p;
         } else if (mat.type == PT_MAT_EMISSIVE) {
             f3 le = mk(bcol.x, bcol.y, bcol.z);  // :228-234
+            if (did == 0 && J.aov) {  // feature buffer: emitted colour scaled into [0, 1]
+                const float m = fmaxf(fmaxf(fmaxf(le.x, le.y), le.z), 1.0f);
+                w.aov0[path] = make_float4(le.x / m, le.y / m, le.z / m, hit.t);
+            }
             if (ext && did > 0 && prev_pdf > 0.0f && s.nemitters > 0) {
                 // Solid-angle pdf with which emitter sampling would have produced this point:
                 // (area * lum / power) * (1 / area) * t^2 / |cos| = lum * t^2 / (power * |cos|).
@@ -209,6 +217,10 @@ __global__ void __launch_bounds__(128) k_shade(PtWave w, int cur, uint32_t did) 
             const f3 wo = normalize(mk(dot(t0, mdir), dot(t1, mdir), dot(t2, mdir)));
             const f3 base = mk(powf(bcol.x, 2.2f), powf(bcol.y, 2.2f), powf(bcol.z, 2.2f));
             const float4 rmao = tex_rgbal(s, mat.tex[2], uv.x, uv.y);
+            if (did == 0 && J.aov) {  // feature buffers: linear base colour, shading normal, distance
+                w.aov0[path] = make_float4(base.x, base.y, base.z, hit.t);
+                w.aov1[path] = make_float4(t2.x, t2.y, t2.z, 0.0f);
+            }
             const uint32_t pix = w.ppix[path], sid = w.psamp[path];
             const U4 rnd = philox(U4{pix, sid, did + 1u, 0u}, J.seed_lo, J.seed_hi);
             const f3 ps = mk(p.x + 0.001f * t2.x, p.y + 0.001f * t2.y, p.z + 0.001f * t2.z);
@@ -437,33 +449,70 @@ __global__ void k_accumulate(PtWave w) {
     const uint32_t local = p - tile.path0;
     if (local >= tile.npix) return;
     const PtJob &J = w.jobs[tile.job];
-    float *acc = w.accum + 3 * ((size_t)J.accum_offset + tile.pixel0 + local);
-    float r = acc[0], g = acc[1], b = acc[2];
+    const size_t px = (size_t)J.accum_offset + tile.pixel0 + local;
     const float cl = J.clamp;
     const bool clamp = cl > 0.0f;
-    for (uint32_t s = 0; s < tile.S; ++s) {
-        const float4 c = w.color[(size_t)tile.path0 + (size_t)s * tile.npix + local];
-        r += clamp ? gmin(c.x, cl) : c.x;
-        g += clamp ? gmin(c.y, cl) : c.y;
-        b += clamp ? gmin(c.z, cl) : c.z;
+    if (J.fp64) {
+        double *acc = w.accum64 + 3 * px;
+        double r = acc[0], g = acc[1], b = acc[2];
+        for (uint32_t s = 0; s < tile.S; ++s) {
+            const float4 c = w.color[(size_t)tile.path0 + (size_t)s * tile.npix + local];
+            r += (double)(clamp ? gmin(c.x, cl) : c.x);
+            g += (double)(clamp ? gmin(c.y, cl) : c.y);
+            b += (double)(clamp ? gmin(c.z, cl) : c.z);
+        }
+        acc[0] = r;
+        acc[1] = g;
+        acc[2] = b;
+    } else {
+        float *acc = w.accum + 3 * px;
+        float r = acc[0], g = acc[1], b = acc[2];
+        for (uint32_t s = 0; s < tile.S; ++s) {
+            const float4 c = w.color[(size_t)tile.path0 + (size_t)s * tile.npix + local];
+            r += clamp ? gmin(c.x, cl) : c.x;
+            g += clamp ? gmin(c.y, cl) : c.y;
+            b += clamp ? gmin(c.z, cl) : c.z;
+        }
+        acc[0] = r;
+        acc[1] = g;
+        acc[2] = b;
     }
-    acc[0] = r;
-    acc[1] = g;
-    acc[2] = b;
+    if (J.aov) {
+        float *a = w.aov_accum + 7 * px;
+        float f[7] = {a[0], a[1], a[2], a[3], a[4], a[5], a[6]};
+        for (uint32_t s = 0; s < tile.S; ++s) {
+            const size_t q = (size_t)tile.path0 + (size_t)s * tile.npix + local;
+            const float4 a0 = w.aov0[q], a1 = w.aov1[q];
+            f[0] += a0.x; f[1] += a0.y; f[2] += a0.z;
+            f[3] += a1.x; f[4] += a1.y; f[5] += a1.z;
+            f[6] += a0.w;
+        }
+        for (int k = 0; k < 7; ++k) a[k] = f[k];
+    }
 }
 
-__global__ void k_load(const float *__restrict__ img, uint32_t comps, uint32_t npix, float *__restrict__ accum) {
+__global__ void k_load(const float *__restrict__ img, uint32_t comps, uint32_t npix, float *__restrict__ accum,
+                       double *__restrict__ accum64) {
     const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
     if (px >= npix) return;
-    for (int k = 0; k < 3; ++k) accum[3 * (size_t)px + k] = img[(size_t)px * comps + k];
+    for (int k = 0; k < 3; ++k) {
+        const float v = img[(size_t)px * comps + k];
+        if (accum64) accum64[3 * (size_t)px + k] = (double)v;
+        else accum[3 * (size_t)px + k] = v;
+    }
 }
 
-// render.rgb(x, y) /= samples (PathTracer.cpp:291-292).
-__global__ void k_store(const float *__restrict__ accum, uint32_t npix, float spp, uint32_t comps,
-                        float *__restrict__ img) {
+// render.rgb(x, y) /= samples (PathTracer.cpp:291-292); feature buffers averaged likewise.
+__global__ void k_store(const float *__restrict__ accum, const double *__restrict__ accum64, uint32_t npix,
+                        float spp, uint32_t comps, float *__restrict__ img, const float *__restrict__ aov_accum,
+                        float *__restrict__ aov) {
     const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
     if (px >= npix) return;
-    for (int k = 0; k < 3; ++k) img[(size_t)px * comps + k] = accum[3 * (size_t)px + k] / spp;
+    for (int k = 0; k < 3; ++k)
+        img[(size_t)px * comps + k] =
+            accum64 ? (float)(accum64[3 * (size_t)px + k] / (double)spp) : accum[3 * (size_t)px + k] / spp;
+    if (aov)
+        for (int k = 0; k < 7; ++k) aov[7 * (size_t)px + k] = aov_accum[7 * (size_t)px + k] / spp;
 }
 
 __global__ void k_mat_eval(const float *__restrict__ c, uint32_t n, float *__restrict__ out) {
@@ -567,14 +616,15 @@ int pt_launch_accumulate(const PtWave &w, cudaStream_t st) {
     return RT_OK;
 }
 
-int pt_launch_load(const float *img, uint32_t comps, uint32_t npix, float *accum, cudaStream_t st) {
-    k_load<<<(npix + 255) / 256, 256, 0, st>>>(img, comps, npix, accum);
+int pt_launch_load(const float *img, uint32_t comps, uint32_t npix, float *accum, double *accum64, cudaStream_t st) {
+    k_load<<<(npix + 255) / 256, 256, 0, st>>>(img, comps, npix, accum, accum64);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
 
-int pt_launch_store(const float *accum, uint32_t npix, float spp, uint32_t comps, float *img, cudaStream_t st) {
-    k_store<<<(npix + 255) / 256, 256, 0, st>>>(accum, npix, spp, comps, img);
+int pt_launch_store(const float *accum, const double *accum64, uint32_t npix, float spp, uint32_t comps, float *img,
+                    const float *aov_accum, float *aov, cudaStream_t st) {
+    k_store<<<(npix + 255) / 256, 256, 0, st>>>(accum, accum64, npix, spp, comps, img, aov_accum, aov);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

@@ -18,6 +18,8 @@ struct PtJob {
     float clamp;  // per-sample clamp (<= 0: none)
     uint32_t seed_lo, seed_hi;
     uint32_t accum_offset;  // first pixel of this job in the accumulation buffer
+    int fp64;               // accumulate in the double buffer
+    int aov;                // collect first-hit features
 };
 
 // Pixels [pixel0, pixel0 + npix) of `job` x samples [s0, s0 + S), laid out sample-major
@@ -41,6 +43,9 @@ struct PtWave {
     unsigned long long *fetch;  // ray-fetch counter of the persistent traversal
     unsigned long long *stats;  // [0] primary, [1] bounce, [2] shadow rays
     float *accum;               // 3 floats per pixel of every job
+    double *accum64;            // 3 doubles per pixel of every job (jobs with fp64)
+    float4 *aov0, *aov1;        // per path: albedo.rgb + distance, normal.xyz (jobs with aov)
+    float *aov_accum;           // 7 floats per pixel of every job (jobs with aov)
     const PtJob *jobs;
     const JobBvh *bvhs;
     const PtTile *tiles;
@@ -72,8 +77,9 @@ int pt_launch_raygen(const PtWave &w, cudaStream_t st);
 int pt_launch_shade(const PtWave &w, int cur, uint32_t did, bool ext, cudaStream_t st);
 int pt_launch_shadow(const PtWave &w, int queue, bool big_stack, cudaStream_t st);
 int pt_launch_accumulate(const PtWave &w, cudaStream_t st);
-int pt_launch_load(const float *img, uint32_t comps, uint32_t npix, float *accum, cudaStream_t st);
-int pt_launch_store(const float *accum, uint32_t npix, float spp, uint32_t comps, float *img, cudaStream_t st);
+int pt_launch_load(const float *img, uint32_t comps, uint32_t npix, float *accum, double *accum64, cudaStream_t st);
+int pt_launch_store(const float *accum, const double *accum64, uint32_t npix, float spp, uint32_t comps, float *img,
+                    const float *aov_accum, float *aov, cudaStream_t st);
 // Closest hit for the wave's ray queue `cur`, each ray against its job's hierarchy.
 int trace_closest_batch(const PtWave &w, int cur, bool big_stack, cudaStream_t st);
 int trace_closest_batch_prepare(bool big_stack);
@@ -89,6 +95,8 @@ struct JobSpec {
     float *image;
     uint32_t width, height, components;
     float clamp;
+    int fp64;
+    float *aov;  // width x height x 7 output (host or device like the image), or null
 };
 
 // Wave-engine tuning (chosen by pt_batch_autotune or defaults).
@@ -112,12 +120,13 @@ class WaveEngine {
 
   private:
     int ensure_capacity(uint64_t cap, uint64_t accum_pixels, uint64_t ntiles, uint64_t nwaves, size_t njobs,
-                        uint64_t staging_floats);
+                        uint64_t staging_floats, bool fp64, bool aov);
     int capture(const PtWave &w, uint32_t depth, bool ext, bool shadow_a, bool shadow_b, bool big_stack);
     int device_;
     cudaStream_t capture_stream_ = nullptr;
     DevBuf atten_, color_, ndc_, pjob_, ppix_, psamp_, qray0_, qray1_, qpath0_, qpath1_, hits_, sray_, scontrib_;
-    DevBuf counters_, accum_, jobs_, bvhs_, tiles_, wave_tiles_, wave_paths_, staging_;
+    DevBuf counters_, accum_, accum64_, aov0_, aov1_, aov_accum_, aov_staging_, jobs_, bvhs_, tiles_, wave_tiles_,
+        wave_paths_, staging_;
     uint64_t cap_ = 0;
     uint64_t generation_ = 0;  // bumped whenever a buffer the graph refers to moves
     cudaGraphExec_t exec_ = nullptr;

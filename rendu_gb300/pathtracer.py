@@ -80,13 +80,19 @@ class PathTracer:
                    float(sc.environment.get("intensity", 1.0)))
         L.call("pt_scene_commit", self._h)
 
-    def render(self, camera, samples: int, depth: int, image, seed: int = 0, mode: int = 0, clamp: float = 5.0):
+    def render(self, camera, samples: int, depth: int, image, seed: int = 0, mode: int = 0, clamp: float = 5.0,
+               fp64: bool = False, aov=None):
         """PathTracer::render(camera, samples, depth, image): accumulate and normalise into
         ``image`` (H, W, C) float32, host array or CUDA tensor; returns ``image``.
         ``mode`` 1 selects the extended estimator (NEE on emitters and the environment
-        map with MIS); ``clamp`` is the per-sample clamp (the reference's 5; <= 0: none)."""
+        map with MIS); ``clamp`` is the per-sample clamp (the reference's 5; <= 0: none);
+        ``fp64`` accumulates each pixel's samples in double precision; ``aov`` (H, W, 7)
+        float32 (same place as ``image``) receives first-hit albedo, normal and distance."""
         cam = camera_desc(camera if isinstance(camera, dict) else camera.__dict__)
-        opts = L.pt_render_options(int(mode), float(clamp))
+        aov_ptr = None
+        if aov is not None:
+            aov_ptr = aov.data_ptr() if type(aov).__module__.startswith("torch") else aov.ctypes.data
+        opts = L.pt_render_options(int(mode), float(clamp), int(bool(fp64)), aov_ptr)
         if type(image).__module__.startswith("torch") and getattr(image, "is_cuda", False):
             import torch
 
@@ -176,7 +182,7 @@ class BatchRenderer:
 
     def render(self, jobs, mode: int = 0, clamp: float = 5.0, tuning=None) -> dict:
         arr, dev = self._jobs(jobs)
-        opts = L.pt_render_options(int(mode), float(clamp))
+        opts = L.pt_render_options(int(mode), float(clamp), 0, None)
         t = None if tuning is None else L.pt_batch_tuning(*(int(tuning[k]) for k in ("wave_paths", "tile_pixels",
                                                                                        "max_samples")))
         stream = None
@@ -194,7 +200,7 @@ class BatchRenderer:
 
     def autotune(self, jobs, mode: int = 0, clamp: float = 5.0, cache_path: str | None = None) -> dict:
         arr, _ = self._jobs(jobs)
-        opts = L.pt_render_options(int(mode), float(clamp))
+        opts = L.pt_render_options(int(mode), float(clamp), 0, None)
         out = L.pt_batch_tuning()
         L.call("pt_batch_autotune", self._h, arr, len(jobs), C.byref(opts),
                cache_path.encode() if cache_path else None, C.byref(out))

@@ -172,3 +172,27 @@ def test_extended_estimator_converges_to_reference_estimator(cuda_lib):
         tr.render(sc.camera, 1024, 5, img, seed=seed, mode=mode, clamp=0.0)
         imgs.append(img)
     assert_same_distribution(imgs[2], imgs[0], imgs[1], factor=1.3)
+
+
+def test_feature_buffers_and_fp64_accumulation(cuda_lib):
+    """First-hit features: a camera-facing quad of one linear albedo gives that albedo, the
+    normal facing the camera and the hit distance at every pixel; double-precision
+    accumulation gives the same image up to float rounding."""
+    from rendu_gb300 import scenes as S
+
+    sc = S.Scene()
+    m = sc.add_mesh(S.quad_mesh((-50, -50, -2), (100, 0, 0), (0, 100, 0)))
+    sc.add_object(m, sc.add_material((0.5, 0.25, 0.75), rough=1.0))
+    sc.lights.append({"type": 1, "color": (1.0, 1.0, 1.0), "direction": (0.0, 0.0, -1.0), "shadows": False})
+    sc.camera = {"eye": (0, 0, 1), "center": (0, 0, 0), "up": (0, 1, 0), "fov": 1.0, "ratio": 1.0}
+    tr = cuda_lib.PathTracer(sc)
+    img = np.zeros((16, 16, 3), np.float32)
+    aov = np.zeros((16, 16, 7), np.float32)
+    tr.render(sc.camera, 4, 2, img, seed=1, aov=aov)
+    np.testing.assert_allclose(aov[..., 0:3], np.broadcast_to(np.float32([0.5, 0.25, 0.75]) ** np.float32(2.2),
+                                                              (16, 16, 3)), rtol=1e-5)
+    np.testing.assert_allclose(aov[..., 3:6], np.broadcast_to(np.float32([0, 0, 1]), (16, 16, 3)), atol=1e-5)
+    assert (aov[..., 6] >= 3.0).all() and (aov[..., 6] < 3.6).all()  # distance 3 at the centre, more off-axis
+    img64 = np.zeros_like(img)
+    tr.render(sc.camera, 4, 2, img64, seed=1, fp64=True)
+    np.testing.assert_allclose(img64, img, rtol=1e-6, atol=1e-7)
