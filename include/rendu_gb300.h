@@ -350,6 +350,82 @@ RT_API int pt_material_sample(const float *cases, const float *uniforms, size_t 
 /* The raycaster built by pt_scene_commit (PathTracer::raycaster(), PathTracer.hpp:29). */
 RT_API rt_ctx *pt_scene_raycaster(pt_scene *scene);
 
+/* ==== Learned denoiser (dn_*) ==============================================================
+ * No counterpart in the reference (its only image filter is the real-time bilateral blur of
+ * src/engine/processing/BilateralBlur.cpp:7-11): a U-Net that maps a few-sample render and
+ * its first-hit feature buffers to a converged image, trained here on path-tracer output.
+ *
+ * Network: 5 levels of two 3x3 convolutions + ReLU with 32, 48, 64, 96, 128 channels, 2x2
+ * max pooling down, nearest 2x upsampling + skip concatenation up, a final 3x3 convolution to
+ * 16 channels of which the first 3 are a correction of log(1 + radiance). Activations are
+ * NHWC BF16, accumulation FP32 (tensor-core implicit GEMMs); master weights FP32.
+ * Features: per pixel DN_FEATURES floats {radiance rgb, albedo rgb, normal xyz, distance}
+ * (pt_render's image + its feature buffer). Images of any size are padded to multiples of
+ * 16 for inference; training crops must be multiples of 16.
+ * Parameters (flat FP32): for each layer in dn_layer order, weights [3][3][cin][cout]
+ * (tap-major: tap = 3 dy + dx over the 3x3 window, then input, then output channel)
+ * followed by bias [cout]. Loss: mean L1 distance in log(1 + radiance). Optimiser: Adam. */
+#define DN_FEATURES 10
+typedef struct dn_net dn_net;
+
+typedef struct dn_layer {
+    uint32_t cin0;   /* channels of the first input (half resolution when up0)          */
+    uint32_t cin1;   /* channels of the concatenated skip input (0: none)                */
+    uint32_t cout;
+    int32_t up0;     /* 1: first input upsampled 2x (nearest)                            */
+    int32_t relu;
+    int32_t level;   /* resolution level: width and height divided by 2^level            */
+    uint64_t weight_offset; /* into the flat parameter vector                            */
+    uint64_t bias_offset;
+} dn_layer;
+
+/* Create the network on `device` with He-initialised parameters (seed 0). */
+RT_API int dn_create(dn_net **out, int device);
+RT_API int dn_destroy(dn_net *net);
+/* Re-initialise parameters (He normal, seeded) and reset the optimiser state. */
+RT_API int dn_init(dn_net *net, uint64_t seed);
+RT_API int dn_layer_count(const dn_net *net, uint32_t *count);
+RT_API int dn_layer_info(const dn_net *net, uint32_t layer, dn_layer *out);
+RT_API int dn_param_count(const dn_net *net, size_t *count);
+/* Host copies of the FP32 parameters / the last computed gradients (count = dn_param_count). */
+RT_API int dn_get_params(dn_net *net, float *out, size_t count);
+RT_API int dn_set_params(dn_net *net, const float *in, size_t count); /* also resets Adam */
+RT_API int dn_get_grads(dn_net *net, float *out, size_t count);
+
+/* Denoise `batch` images: features (batch, height, width, DN_FEATURES) -> out (batch,
+ * height, width, 3) radiance. Host pointers by default (blocking); device pointers with
+ * RT_FLAG_DEVICE_PTRS (ordered on `stream`). */
+RT_API int dn_denoise(dn_net *net, const float *features, uint32_t width, uint32_t height, uint32_t batch, float *out,
+                      void *stream, uint32_t flags);
+/* Loss and parameter gradients for one batch of crops (width, height multiples of 16):
+ * target (batch, height, width, 3) converged radiance. *loss (may be NULL: no read-back,
+ * no synchronisation for device pointers) receives the loss. */
+RT_API int dn_backward(dn_net *net, const float *features, const float *target, uint32_t width, uint32_t height,
+                       uint32_t batch, float *loss, void *stream, uint32_t flags);
+/* One Adam step (beta 0.9, 0.999, eps 1e-8) with learning rate lr on the last gradients,
+ * ordered on `stream` (NULL: the network's own stream, and the call blocks). */
+RT_API int dn_adam_step(dn_net *net, float lr, void *stream);
+/* dn_backward + dn_adam_step. */
+RT_API int dn_train_step(dn_net *net, const float *features, const float *target, uint32_t width, uint32_t height,
+                         uint32_t batch, float lr, float *loss, void *stream, uint32_t flags);
+
+/* One 3x3 convolution layer on device buffers, ordered on `stream` (the network's building
+ * block, exported for tests and custom networks). Input: x0 (batch, height >> up0, width >>
+ * up0, c0) BF16 NHWC, then x1 (batch, height, width, c1) BF16 (NULL when c1 = 0), channels
+ * concatenated; weights BF16 [3][3][c0 + c1][cout]; bias FP32 [cout] or NULL. out (batch,
+ * height, width, cout) BF16, or FP32 when out_fp32. c0, c1, cout multiples of 8; pointers
+ * 16-byte aligned. */
+RT_API int dn_conv3x3(const void *x0, uint32_t c0, int32_t up0, const void *x1, uint32_t c1, uint32_t batch,
+                      uint32_t height, uint32_t width, const void *weights, const float *bias, uint32_t cout,
+                      int32_t relu, void *out, int32_t out_fp32, void *stream);
+/* Gradients of dn_conv3x3 (without bias or ReLU) for the output gradient gy (batch, height,
+ * width, cout) BF16: dx (batch, height, width, c0 + c1) FP32 with respect to the
+ * concatenated, upsampled input (NULL: skipped) and dw [3][3][c0 + c1][cout] FP32 (NULL:
+ * skipped); weights FP32 [3][3][c0 + c1][cout]. Scratch is allocated on `stream`. */
+RT_API int dn_conv3x3_backward(const void *x0, uint32_t c0, int32_t up0, const void *x1, uint32_t c1, uint32_t batch,
+                               uint32_t height, uint32_t width, const float *weights, uint32_t cout, const void *gy,
+                               float *dx, float *dw, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

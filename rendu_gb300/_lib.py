@@ -80,6 +80,13 @@ class pt_render_stats(C.Structure):
                 ("paths", C.c_uint64), ("device_ms", C.c_float)]
 
 
+class dn_layer(C.Structure):
+    _fields_ = [("cin0", C.c_uint32), ("cin1", C.c_uint32), ("cout", C.c_uint32), ("up0", C.c_int32),
+                ("relu", C.c_int32), ("level", C.c_int32), ("weight_offset", C.c_uint64), ("bias_offset", C.c_uint64)]
+
+
+DN_FEATURES = 10
+
 _lib = None
 _lock = threading.Lock()
 
@@ -122,6 +129,25 @@ _SIGS = {
     "pt_scene_raycaster": ([_VP], _VP),
     "pt_material_eval": ([_VP, C.c_size_t, _VP, C.c_int], C.c_int),
     "pt_material_sample": ([_VP, _VP, C.c_size_t, _VP, C.c_int], C.c_int),
+    "dn_create": ([C.POINTER(C.c_void_p), C.c_int], C.c_int),
+    "dn_destroy": ([_VP], C.c_int),
+    "dn_init": ([_VP, C.c_uint64], C.c_int),
+    "dn_layer_count": ([_VP, C.POINTER(C.c_uint32)], C.c_int),
+    "dn_layer_info": ([_VP, C.c_uint32, C.POINTER(dn_layer)], C.c_int),
+    "dn_param_count": ([_VP, C.POINTER(C.c_size_t)], C.c_int),
+    "dn_get_params": ([_VP, _VP, C.c_size_t], C.c_int),
+    "dn_set_params": ([_VP, _VP, C.c_size_t], C.c_int),
+    "dn_get_grads": ([_VP, _VP, C.c_size_t], C.c_int),
+    "dn_denoise": ([_VP, _VP, C.c_uint32, C.c_uint32, C.c_uint32, _VP, _VP, C.c_uint32], C.c_int),
+    "dn_backward": ([_VP, _VP, _VP, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_float), _VP, C.c_uint32],
+                    C.c_int),
+    "dn_adam_step": ([_VP, C.c_float, _VP], C.c_int),
+    "dn_train_step": ([_VP, _VP, _VP, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.POINTER(C.c_float), _VP,
+                       C.c_uint32], C.c_int),
+    "dn_conv3x3": ([_VP, C.c_uint32, C.c_int32, _VP, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _VP, _VP,
+                    C.c_uint32, C.c_int32, _VP, C.c_int32, _VP], C.c_int),
+    "dn_conv3x3_backward": ([_VP, C.c_uint32, C.c_int32, _VP, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, _VP,
+                             C.c_uint32, _VP, _VP, _VP, _VP], C.c_int),
 }
 
 

@@ -1,0 +1,582 @@
+// C-ABI of the learned denoiser (include/rendu_gb300.h, dn_*): the U-Net's layer graph, its
+// activation and gradient buffers, the forward and backward passes over the kernels of
+// dn_kernels.cu, and the Adam update.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dn_net.hpp"
+
+using namespace rgb;
+using namespace rgb::dn;
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+int arg_error(const char *msg) {
+    set_error(msg);
+    return RT_ERR_ARG;
+}
+
+struct Tensor {
+    int level;  // resolution divided by 2^level
+    int ch;
+    bool f32;   // FP32 (network output) instead of BF16
+};
+
+struct Conv {
+    int src0, up0, src1;  // tensor indices (src1 = -1: no skip input)
+    int cin0, cin1, cout;
+    int relu;
+    int out;
+    size_t woff, boff;
+};
+
+struct Op {
+    bool pool;
+    int conv;      // index into convs (when !pool)
+    int src, out;  // tensors of a pooling op
+};
+
+constexpr int kLevels = 5;
+constexpr int kChannels[kLevels] = {32, 48, 64, 96, 128};
+constexpr int kInC = 16, kOutC = 16;
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+struct dn_net {
+    int device = 0;
+    cudaStream_t stream = nullptr;  // for host-pointer calls
+    std::vector<Tensor> tensors;
+    std::vector<Conv> convs;
+    std::vector<Op> ops;
+    size_t nparams = 0;
+    LayerTable table{};
+    DevBuf params, grads, adam_m, adam_v, wb, wt, hyper;
+    float lr_dev = -1.0f;  // learning rate held in device memory
+    // Shape-dependent buffers.
+    int B = 0, Hp = 0, Wp = 0;
+    bool train_ready = false;
+    DevBuf act, gact, gin, gbf, partial, feat, target, out, loss_partial;
+    std::vector<size_t> act_off, gact_off;
+
+    bf16 *bf(int t) { return reinterpret_cast<bf16 *>(static_cast<char *>(act.ptr) + act_off[t]); }
+    float *f(int t) { return reinterpret_cast<float *>(static_cast<char *>(act.ptr) + act_off[t]); }
+    float *g(int t) { return reinterpret_cast<float *>(static_cast<char *>(gact.ptr) + gact_off[t]); }
+    Hyper *hyp() { return hyper.as<Hyper>(); }
+    long pixels(int level) const { return (long)B * (Hp >> level) * (Wp >> level); }
+};
+
+namespace {
+
+// The U-Net: per level two 3x3 convolutions + ReLU (32, 48, 64, 96, 128 channels) with 2x2
+// max pooling between levels; on the way up, each level's first convolution reads the
+// level below upsampled 2x concatenated with the skip tensor of its own level; a final
+// convolution to 16 channels (no ReLU, FP32).
+void build_graph(dn_net *n) {
+    auto tensor = [&](int level, int ch, bool f32) {
+        n->tensors.push_back({level, ch, f32});
+        return (int)n->tensors.size() - 1;
+    };
+    auto conv = [&](int s0, int up0, int s1, int cout, int relu, bool f32) {
+        Conv c;
+        c.src0 = s0;
+        c.up0 = up0;
+        c.src1 = s1;
+        c.cin0 = n->tensors[s0].ch;
+        c.cin1 = s1 >= 0 ? n->tensors[s1].ch : 0;
+        c.cout = cout;
+        c.relu = relu;
+        const int level = n->tensors[s0].level - (up0 ? 1 : 0);
+        c.out = tensor(level, cout, f32);
+        c.woff = n->nparams;
+        n->nparams += (size_t)9 * (c.cin0 + c.cin1) * cout;
+        c.boff = n->nparams;
+        n->nparams += cout;
+        n->convs.push_back(c);
+        n->ops.push_back({false, (int)n->convs.size() - 1, -1, -1});
+        return c.out;
+    };
+    auto pool_op = [&](int s) {
+        const int o = tensor(n->tensors[s].level + 1, n->tensors[s].ch, false);
+        n->ops.push_back({true, -1, s, o});
+        return o;
+    };
+    int cur = tensor(0, kInC, false);
+    int skip[kLevels];
+    for (int l = 0; l < kLevels; ++l) {
+        if (l) cur = pool_op(cur);
+        cur = conv(cur, 0, -1, kChannels[l], 1, false);
+        cur = conv(cur, 0, -1, kChannels[l], 1, false);
+        skip[l] = cur;
+    }
+    for (int l = kLevels - 2; l >= 0; --l) {
+        cur = conv(cur, 1, skip[l], kChannels[l], 1, false);
+        cur = conv(cur, 0, -1, kChannels[l], 1, false);
+    }
+    conv(cur, 0, -1, kOutC, 0, true);
+    n->table.n = (int)n->convs.size();
+    for (size_t i = 0; i < n->convs.size(); ++i) {
+        const Conv &c = n->convs[i];
+        n->table.l[i] = {(uint32_t)c.woff, (uint32_t)(c.cin0 + c.cin1), (uint32_t)c.cout};
+    }
+}
+
+// BF16 forward and dgrad copies of every layer's weights from the FP32 master copy.
+int refresh_weights(dn_net *n, cudaStream_t st) {
+    for (const Conv &c : n->convs) {
+        const int r = convert_weights(n->params.as<float>() + c.woff, c.cin0 + c.cin1, c.cout,
+                                      n->wb.as<bf16>() + c.woff, n->wt.as<bf16>() + c.woff, st);
+        if (r != RT_OK) return r;
+    }
+    return RT_OK;
+}
+
+int reset_optimizer(dn_net *n, cudaStream_t st) {
+    RT_CUDA_TRY(cudaMemsetAsync(n->adam_m.ptr, 0, n->nparams * sizeof(float), st));
+    RT_CUDA_TRY(cudaMemsetAsync(n->adam_v.ptr, 0, n->nparams * sizeof(float), st));
+    RT_CUDA_TRY(cudaMemsetAsync(n->grads.ptr, 0, n->nparams * sizeof(float), st));
+    const Hyper h{1e-3f, 0.9f, 0.999f, 1e-8f, 1.0f, 1.0f, 0, 0.0f};
+    RT_CUDA_TRY(cudaMemcpyAsync(n->hyper.ptr, &h, sizeof(Hyper), cudaMemcpyHostToDevice, st));
+    n->lr_dev = h.lr;
+    return RT_OK;
+}
+
+int upload_params(dn_net *n, const float *host, cudaStream_t st) {
+    RT_CUDA_TRY(cudaMemcpyAsync(n->params.ptr, host, n->nparams * sizeof(float), cudaMemcpyHostToDevice, st));
+    int r = refresh_weights(n, st);
+    if (r == RT_OK) r = reset_optimizer(n, st);
+    if (r == RT_OK) RT_CUDA_TRY(cudaStreamSynchronize(st));
+    return r;
+}
+
+// He-normal weights (std sqrt(2 / fan_in), the last layer scaled by 0.1 so that the
+// network starts close to the identity on its noisy input), zero biases. splitmix64 +
+// Box-Muller: deterministic for a seed on every platform.
+std::vector<float> he_init(const dn_net *n, uint64_t seed) {
+    std::vector<float> h(n->nparams, 0.0f);
+    uint64_t s = seed ^ 0x6A09E667F3BCC909ull;
+    auto next = [&]() {
+        s += 0x9E3779B97F4A7C15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    auto unif = [&]() { return ((double)(next() >> 11) + 0.5) * (1.0 / 9007199254740992.0); };
+    for (size_t li = 0; li < n->convs.size(); ++li) {
+        const Conv &c = n->convs[li];
+        const size_t nw = (size_t)9 * (c.cin0 + c.cin1) * c.cout;
+        double sd = std::sqrt(2.0 / (9.0 * (c.cin0 + c.cin1)));
+        if (li + 1 == n->convs.size()) sd *= 0.1;
+        for (size_t i = 0; i < nw; ++i) {
+            const double u1 = unif(), u2 = unif();
+            h[c.woff + i] = (float)(sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2));
+        }
+    }
+    return h;
+}
+
+int ensure_shape(dn_net *n, int B, int Hp, int Wp, bool train) {
+    if (n->B == B && n->Hp == Hp && n->Wp == Wp && (!train || n->train_ready)) return RT_OK;
+    n->B = B;
+    n->Hp = Hp;
+    n->Wp = Wp;
+    n->act_off.assign(n->tensors.size(), 0);
+    n->gact_off.assign(n->tensors.size(), 0);
+    size_t a = 0, g = 0, max_el = 0, max_gin = 0, max_part = 0;
+    for (size_t t = 0; t < n->tensors.size(); ++t) {
+        const Tensor &T = n->tensors[t];
+        const size_t el = (size_t)n->pixels(T.level) * T.ch;
+        n->act_off[t] = a;
+        a += align_up(el * (T.f32 ? 4 : 2), 256);
+        n->gact_off[t] = g;
+        g += align_up(el * 4, 256);
+        max_el = std::max(max_el, el);
+    }
+    for (const Conv &c : n->convs) {
+        const long P = n->pixels(n->tensors[c.out].level);
+        const int cin = c.cin0 + c.cin1;
+        if (c.cin1 || c.up0) max_gin = std::max(max_gin, (size_t)P * cin);
+        max_part = std::max({max_part, wgrad_partial_floats(P, cin, c.cout), colsum_partial_floats(P, c.cout)});
+    }
+    if (n->act.reserve(a) != RT_OK) return RT_ERR_OOM;
+    n->train_ready = false;
+    if (train) {
+        const long P0 = n->pixels(0);
+        if (n->gact.reserve(g) != RT_OK || n->gin.reserve(std::max<size_t>(max_gin, 1) * 4) != RT_OK ||
+            n->gbf.reserve(max_el * 2) != RT_OK || n->partial.reserve(max_part * 4) != RT_OK ||
+            n->loss_partial.reserve((size_t)((P0 + 255) / 256) * 4) != RT_OK)
+            return RT_ERR_OOM;
+        n->train_ready = true;
+    }
+    return RT_OK;
+}
+
+int forward(dn_net *n, cudaStream_t st) {
+    for (const Op &op : n->ops) {
+        int r;
+        if (op.pool) {
+            const Tensor &s = n->tensors[op.src];
+            r = pool(n->bf(op.src), n->B, n->Hp >> s.level, n->Wp >> s.level, s.ch, n->bf(op.out), st);
+        } else {
+            const Conv &c = n->convs[op.conv];
+            const Tensor &o = n->tensors[c.out];
+            ConvIn in;
+            in.p0 = n->bf(c.src0);
+            in.c0 = c.cin0;
+            in.up0 = c.up0;
+            in.p1 = c.src1 >= 0 ? n->bf(c.src1) : nullptr;
+            in.c1 = c.cin1;
+            r = conv_forward(in, n->B, n->Hp >> o.level, n->Wp >> o.level, n->wb.as<bf16>() + c.woff,
+                             n->params.as<float>() + c.boff, c.cout, c.relu != 0, o.f32 ? nullptr : n->bf(c.out),
+                             o.f32 ? n->f(c.out) : nullptr, st);
+        }
+        if (r != RT_OK) return r;
+    }
+    return RT_OK;
+}
+
+int backward(dn_net *n, const float *target, cudaStream_t st) {
+    const int last = n->convs.back().out;
+    int r = l1_loss(n->bf(0), n->f(last), target, n->pixels(0), n->g(last), n->loss_partial.as<float>(), n->hyp(), st);
+    if (r != RT_OK) return r;
+    float *grads = n->grads.as<float>();
+    for (auto it = n->ops.rbegin(); it != n->ops.rend() && r == RT_OK; ++it) {
+        const Op &op = *it;
+        if (op.pool) {
+            const Tensor &s = n->tensors[op.src];
+            r = pool_back(n->bf(op.src), n->bf(op.out), n->g(op.out), n->B, n->Hp >> s.level, n->Wp >> s.level, s.ch,
+                          n->g(op.src), st);
+            continue;
+        }
+        const Conv &c = n->convs[op.conv];
+        const Tensor &o = n->tensors[c.out];
+        const int H = n->Hp >> o.level, W = n->Wp >> o.level;
+        const long P = n->pixels(o.level);
+        bf16 *gb = n->gbf.as<bf16>();
+        r = relu_grad(n->g(c.out), c.relu ? n->bf(c.out) : nullptr, (size_t)P * c.cout, c.relu != 0, gb, st);
+        if (r != RT_OK) break;
+        ConvIn in;
+        in.p0 = n->bf(c.src0);
+        in.c0 = c.cin0;
+        in.up0 = c.up0;
+        in.p1 = c.src1 >= 0 ? n->bf(c.src1) : nullptr;
+        in.c1 = c.cin1;
+        r = conv_wgrad(in, n->B, H, W, gb, c.cout, n->partial.as<float>(), grads + c.woff, st);
+        if (r == RT_OK) r = colsum(n->g(c.out), P, c.cout, n->partial.as<float>(), grads + c.boff, st);
+        if (r != RT_OK || c.src0 == 0) continue;  // no gradient for the network input
+        ConvIn gi;
+        gi.p0 = gb;
+        gi.c0 = c.cout;
+        const bool split = c.cin1 || c.up0;
+        float *dst = split ? n->gin.as<float>() : n->g(c.src0);
+        r = conv_forward(gi, n->B, H, W, n->wt.as<bf16>() + c.woff, nullptr, c.cin0 + c.cin1, false, nullptr, dst, st);
+        if (r == RT_OK && split)
+            r = split_grad(dst, n->B, H, W, c.cin0, c.up0, c.cin1, n->g(c.src0), c.src1 >= 0 ? n->g(c.src1) : nullptr,
+                           st);
+    }
+    return r;
+}
+
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+int stage_in(DevBuf &buf, const float *host, size_t n, cudaStream_t st) {
+    if (buf.reserve(n * sizeof(float)) != RT_OK) return RT_ERR_OOM;
+    RT_CUDA_TRY(cudaMemcpyAsync(buf.ptr, host, n * sizeof(float), cudaMemcpyHostToDevice, st));
+    return RT_OK;
+}
+
+int backward_call(dn_net *n, const float *features, const float *target, uint32_t width, uint32_t height,
+                  uint32_t batch, cudaStream_t st, bool dev) {
+    if (!features || !target || width == 0 || height == 0 || batch == 0) return arg_error("empty denoiser batch");
+    if (width % 16 || height % 16) return arg_error("training crops must be multiples of 16 pixels wide and high");
+    if ((uint64_t)width * height * batch >= (1ull << 31)) return arg_error("denoiser batch too large");
+    int r = ensure_shape(n, (int)batch, (int)height, (int)width, true);
+    if (r != RT_OK) return r;
+    const size_t np = (size_t)batch * height * width;
+    const float *f = features, *t = target;
+    if (!dev) {
+        if ((r = stage_in(n->feat, features, np * DN_FEATURES, st)) != RT_OK) return r;
+        if ((r = stage_in(n->target, target, np * 3, st)) != RT_OK) return r;
+        f = n->feat.as<float>();
+        t = n->target.as<float>();
+    }
+    r = prepare(f, (int)batch, (int)height, (int)width, (int)height, (int)width, n->bf(0), st);
+    if (r == RT_OK) r = forward(n, st);
+    if (r == RT_OK) r = backward(n, t, st);
+    return r;
+}
+
+int adam_call(dn_net *n, float lr, cudaStream_t st) {
+    if (!(lr >= 0.0f) || !std::isfinite(lr)) return arg_error("learning rate must be finite and >= 0");
+    if (lr != n->lr_dev) {
+        RT_CUDA_TRY(cudaMemcpyAsync(&n->hyp()->lr, &lr, sizeof(float), cudaMemcpyHostToDevice, st));
+        n->lr_dev = lr;
+    }
+    return adam(n->params.as<float>(), n->grads.as<float>(), n->adam_m.as<float>(), n->adam_v.as<float>(), n->nparams,
+                n->table, n->hyp(), n->wb.as<bf16>(), n->wt.as<bf16>(), st);
+}
+
+int read_loss(dn_net *n, float *loss, cudaStream_t st) {
+    if (!loss) return RT_OK;
+    RT_CUDA_TRY(cudaMemcpyAsync(loss, &n->hyp()->loss, sizeof(float), cudaMemcpyDeviceToHost, st));
+    RT_CUDA_TRY(cudaStreamSynchronize(st));
+    return RT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+RT_API int dn_create(dn_net **out, int device) {
+    if (!out) return arg_error("null output handle");
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        set_error("CUDA device " + std::to_string(device) + " is not available");
+        return RT_ERR_CUDA;
+    }
+    DeviceGuard guard(device);
+    dn_net *n = new dn_net();
+    n->device = device;
+    build_graph(n);
+    int r = RT_OK;
+    if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("stream creation failed");
+        r = RT_ERR_CUDA;
+    }
+    const size_t pb = n->nparams * sizeof(float);
+    if (r == RT_OK &&
+        (n->params.reserve(pb) != RT_OK || n->grads.reserve(pb) != RT_OK || n->adam_m.reserve(pb) != RT_OK ||
+         n->adam_v.reserve(pb) != RT_OK || n->wb.reserve(n->nparams * 2) != RT_OK ||
+         n->wt.reserve(n->nparams * 2) != RT_OK || n->hyper.reserve(sizeof(Hyper)) != RT_OK))
+        r = RT_ERR_OOM;
+    if (r == RT_OK) {
+        const std::vector<float> h = he_init(n, 0);
+        r = upload_params(n, h.data(), n->stream);
+    }
+    if (r != RT_OK) {
+        dn_destroy(n);
+        return r;
+    }
+    clear_error();
+    *out = n;
+    return RT_OK;
+}
+
+RT_API int dn_destroy(dn_net *n) {
+    if (!n) return RT_OK;
+    DeviceGuard guard(n->device);
+    if (n->stream) cudaStreamSynchronize(n->stream);
+    for (DevBuf *b : {&n->params, &n->grads, &n->adam_m, &n->adam_v, &n->wb, &n->wt, &n->hyper, &n->act, &n->gact,
+                      &n->gin, &n->gbf, &n->partial, &n->feat, &n->target, &n->out, &n->loss_partial})
+        b->release();
+    if (n->stream) cudaStreamDestroy(n->stream);
+    delete n;
+    return RT_OK;
+}
+
+RT_API int dn_init(dn_net *n, uint64_t seed) {
+    if (!n) return arg_error("null network");
+    DeviceGuard guard(n->device);
+    const std::vector<float> h = he_init(n, seed);
+    return upload_params(n, h.data(), n->stream);
+}
+
+RT_API int dn_layer_count(const dn_net *n, uint32_t *count) {
+    if (!n || !count) return arg_error("null argument");
+    *count = (uint32_t)n->convs.size();
+    return RT_OK;
+}
+
+RT_API int dn_layer_info(const dn_net *n, uint32_t layer, dn_layer *out) {
+    if (!n || !out) return arg_error("null argument");
+    if (layer >= n->convs.size()) return arg_error("layer index out of range");
+    const Conv &c = n->convs[layer];
+    out->cin0 = (uint32_t)c.cin0;
+    out->cin1 = (uint32_t)c.cin1;
+    out->cout = (uint32_t)c.cout;
+    out->up0 = c.up0;
+    out->relu = c.relu;
+    out->level = n->tensors[c.out].level;
+    out->weight_offset = c.woff;
+    out->bias_offset = c.boff;
+    return RT_OK;
+}
+
+RT_API int dn_param_count(const dn_net *n, size_t *count) {
+    if (!n || !count) return arg_error("null argument");
+    *count = n->nparams;
+    return RT_OK;
+}
+
+RT_API int dn_get_params(dn_net *n, float *out, size_t count) {
+    if (!n || !out || count != n->nparams) return arg_error("parameter count mismatch");
+    DeviceGuard guard(n->device);
+    RT_CUDA_TRY(cudaDeviceSynchronize());
+    RT_CUDA_TRY(cudaMemcpy(out, n->params.ptr, count * sizeof(float), cudaMemcpyDeviceToHost));
+    return RT_OK;
+}
+
+RT_API int dn_set_params(dn_net *n, const float *in, size_t count) {
+    if (!n || !in || count != n->nparams) return arg_error("parameter count mismatch");
+    DeviceGuard guard(n->device);
+    RT_CUDA_TRY(cudaDeviceSynchronize());
+    return upload_params(n, in, n->stream);
+}
+
+RT_API int dn_get_grads(dn_net *n, float *out, size_t count) {
+    if (!n || !out || count != n->nparams) return arg_error("parameter count mismatch");
+    DeviceGuard guard(n->device);
+    RT_CUDA_TRY(cudaDeviceSynchronize());
+    RT_CUDA_TRY(cudaMemcpy(out, n->grads.ptr, count * sizeof(float), cudaMemcpyDeviceToHost));
+    return RT_OK;
+}
+
+RT_API int dn_denoise(dn_net *n, const float *features, uint32_t width, uint32_t height, uint32_t batch, float *out,
+                      void *stream, uint32_t flags) {
+    if (!n || !features || !out) return arg_error("null argument");
+    if (width == 0 || height == 0 || batch == 0) return arg_error("empty image");
+    const uint32_t Hp = (height + 15) / 16 * 16, Wp = (width + 15) / 16 * 16;
+    if ((uint64_t)Wp * Hp * batch >= (1ull << 31)) return arg_error("image too large");
+    DeviceGuard guard(n->device);
+    const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
+    cudaStream_t st = dev ? static_cast<cudaStream_t>(stream) : n->stream;
+    int r = ensure_shape(n, (int)batch, (int)Hp, (int)Wp, false);
+    if (r != RT_OK) return r;
+    const size_t np = (size_t)batch * height * width;
+    const float *f = features;
+    float *o = out;
+    if (!dev) {
+        if ((r = stage_in(n->feat, features, np * DN_FEATURES, st)) != RT_OK) return r;
+        if (n->out.reserve(np * 3 * sizeof(float)) != RT_OK) return RT_ERR_OOM;
+        f = n->feat.as<float>();
+        o = n->out.as<float>();
+    }
+    r = prepare(f, (int)batch, (int)height, (int)width, (int)Hp, (int)Wp, n->bf(0), st);
+    if (r == RT_OK) r = forward(n, st);
+    if (r == RT_OK)
+        r = finish(n->bf(0), n->f(n->convs.back().out), (int)batch, (int)height, (int)width, (int)Hp, (int)Wp, o, st);
+    if (r != RT_OK) return r;
+    if (!dev) {
+        RT_CUDA_TRY(cudaMemcpyAsync(out, o, np * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
+        RT_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    return RT_OK;
+}
+
+RT_API int dn_backward(dn_net *n, const float *features, const float *target, uint32_t width, uint32_t height,
+                       uint32_t batch, float *loss, void *stream, uint32_t flags) {
+    if (!n) return arg_error("null network");
+    DeviceGuard guard(n->device);
+    const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
+    cudaStream_t st = dev ? static_cast<cudaStream_t>(stream) : n->stream;
+    int r = backward_call(n, features, target, width, height, batch, st, dev);
+    if (r == RT_OK) r = read_loss(n, loss, st);
+    if (r == RT_OK && !dev) RT_CUDA_TRY(cudaStreamSynchronize(st));
+    return r;
+}
+
+RT_API int dn_adam_step(dn_net *n, float lr, void *stream) {
+    if (!n) return arg_error("null network");
+    DeviceGuard guard(n->device);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : n->stream;
+    int r = adam_call(n, lr, st);
+    if (r == RT_OK && !stream) RT_CUDA_TRY(cudaStreamSynchronize(st));
+    return r;
+}
+
+RT_API int dn_train_step(dn_net *n, const float *features, const float *target, uint32_t width, uint32_t height,
+                         uint32_t batch, float lr, float *loss, void *stream, uint32_t flags) {
+    if (!n) return arg_error("null network");
+    DeviceGuard guard(n->device);
+    const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
+    cudaStream_t st = dev ? static_cast<cudaStream_t>(stream) : n->stream;
+    int r = backward_call(n, features, target, width, height, batch, st, dev);
+    if (r == RT_OK) r = adam_call(n, lr, st);
+    if (r == RT_OK) r = read_loss(n, loss, st);
+    if (r == RT_OK && !dev) RT_CUDA_TRY(cudaStreamSynchronize(st));
+    return r;
+}
+
+RT_API int dn_conv3x3(const void *x0, uint32_t c0, int32_t up0, const void *x1, uint32_t c1, uint32_t batch,
+                      uint32_t height, uint32_t width, const void *weights, const float *bias, uint32_t cout,
+                      int32_t relu, void *out, int32_t out_fp32, void *stream) {
+    if (!x0 || !weights || !out || (c1 && !x1)) return arg_error("null argument");
+    if (c0 == 0 || c0 % 8 || c1 % 8 || cout == 0 || cout % 8) return arg_error("channel counts must be multiples of 8");
+    if (batch == 0 || height == 0 || width == 0) return arg_error("empty input");
+    if (up0 && (height % 2 || width % 2)) return arg_error("an upsampled input needs an even output size");
+    if (!aligned16(x0) || (x1 && !aligned16(x1)) || !aligned16(weights))
+        return arg_error("inputs and weights must be 16-byte aligned");
+    ConvIn in;
+    in.p0 = static_cast<const bf16 *>(x0);
+    in.c0 = (int)c0;
+    in.up0 = up0 ? 1 : 0;
+    in.p1 = static_cast<const bf16 *>(x1);
+    in.c1 = (int)c1;
+    return conv_forward(in, (int)batch, (int)height, (int)width, static_cast<const bf16 *>(weights), bias, (int)cout,
+                        relu != 0, out_fp32 ? nullptr : static_cast<bf16 *>(out),
+                        out_fp32 ? static_cast<float *>(out) : nullptr, static_cast<cudaStream_t>(stream));
+}
+
+RT_API int dn_conv3x3_backward(const void *x0, uint32_t c0, int32_t up0, const void *x1, uint32_t c1, uint32_t batch,
+                               uint32_t height, uint32_t width, const float *weights, uint32_t cout, const void *gy,
+                               float *dx, float *dw, void *stream) {
+    if (!x0 || !gy || (c1 && !x1) || (dx && !weights)) return arg_error("null argument");
+    if (c0 == 0 || c0 % 8 || c1 % 8 || cout == 0 || cout % 8) return arg_error("channel counts must be multiples of 8");
+    if (batch == 0 || height == 0 || width == 0) return arg_error("empty input");
+    if (up0 && (height % 2 || width % 2)) return arg_error("an upsampled input needs an even output size");
+    if (!aligned16(x0) || (x1 && !aligned16(x1)) || !aligned16(gy)) return arg_error("inputs must be 16-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int cin = (int)(c0 + c1);
+    const long P = (long)batch * height * width;
+    int r = RT_OK;
+    if (dx) {
+        void *wt = nullptr;
+        RT_CUDA_TRY(cudaMallocAsync(&wt, (size_t)9 * cin * cout * sizeof(bf16), st));
+        r = convert_weights(weights, cin, (int)cout, nullptr, static_cast<bf16 *>(wt), st);
+        if (r == RT_OK) {
+            ConvIn gi;
+            gi.p0 = static_cast<const bf16 *>(gy);
+            gi.c0 = (int)cout;
+            r = conv_forward(gi, (int)batch, (int)height, (int)width, static_cast<const bf16 *>(wt), nullptr, cin, false,
+                             nullptr, dx, st);
+        }
+        cudaFreeAsync(wt, st);
+        if (r != RT_OK) return r;
+    }
+    if (dw) {
+        void *part = nullptr;
+        RT_CUDA_TRY(cudaMallocAsync(&part, wgrad_partial_floats(P, cin, (int)cout) * sizeof(float), st));
+        ConvIn in;
+        in.p0 = static_cast<const bf16 *>(x0);
+        in.c0 = (int)c0;
+        in.up0 = up0 ? 1 : 0;
+        in.p1 = static_cast<const bf16 *>(x1);
+        in.c1 = (int)c1;
+        r = conv_wgrad(in, (int)batch, (int)height, (int)width, static_cast<const bf16 *>(gy), (int)cout,
+                       static_cast<float *>(part), dw, st);
+        cudaFreeAsync(part, st);
+    }
+    return r;
+}
+
+}  // extern "C"

@@ -1,0 +1,782 @@
+// Denoiser kernels. The 3x3 convolutions are implicit GEMMs on the BF16 tensor cores
+// (mma.sync.m16n8k16, FP32 accumulation) fed by a 3-stage cp.async pipeline with ldmatrix
+// fragment loads; the rest are the element-wise pieces of a U-Net's forward and backward
+// passes (pooling, gradient routing, loss, Adam). Activations are NHWC BF16.
+//
+// Convolution input: up to two tensors concatenated along channels -- the first optionally
+// read at half resolution (nearest-neighbour 2x upsampling folded into the gather), the
+// second at full resolution (the U-Net skip connection) -- so the decoder never
+// materialises the upsampled or concatenated tensors. With off(tap) = (tap/3 - 1, tap%3 - 1):
+//   forward : out[p, co]      = act(bias[co] + sum_{tap, ci} x[p + off(tap), ci] w[tap][ci][co])
+//             GEMM M = pixels, N = Cout, K = 9 Cin (k = tap Cin + ci), zero padding.
+//   dgrad   : dx[p, ci]       = sum_{tap, co} g[p - off(tap), co] w[tap][ci][co]
+//             = the forward GEMM on g with wt[8 - tap][co][ci] = w[tap][ci][co].
+//   wgrad   : dw[tap][ci][co] = sum_p x[p + off(tap), ci] g[p, co]
+//             GEMM M = 9 Cin, N = Cout, K = pixels, split over pixel chunks and reduced in a
+//             fixed order (deterministic).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "dn_net.hpp"
+
+namespace rgb {
+namespace dn {
+namespace {
+
+constexpr int BM = 128;  // GEMM rows per CTA (pixels for conv, taps x channels for wgrad)
+constexpr int BK = 32;   // K per pipeline stage
+constexpr int STAGES = 3;
+
+// ---- PTX wrappers ------------------------------------------------------------------------------
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// 16-byte global -> shared copy; zero-filled when !valid (src is then never read).
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_addr(dst)), "l"(src),
+                 "r"(valid ? 16 : 0));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void ldsm_x4_t(unsigned (&r)[4], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Address of channels [c, c + 8) of the (concatenated, possibly upsampled) input at pixel
+// (n, y, x) of the full-resolution grid; the caller has checked the pixel is inside.
+__device__ __forceinline__ const bf16 *in_addr(const ConvIn &in, int n, int y, int x, int H, int W, int c) {
+    if (c < in.c0) {
+        const int h0 = H >> in.up0, w0 = W >> in.up0;
+        return in.p0 + (((size_t)n * h0 + (y >> in.up0)) * w0 + (x >> in.up0)) * in.c0 + c;
+    }
+    return in.p1 + (((size_t)n * H + y) * W + x) * in.c1 + (c - in.c0);
+}
+
+// One warp's MI x NI tile of m16n8 accumulators over a BK slice held in shared memory.
+// A_TRANS: A stored [k][m] (wgrad) instead of [m][k] (conv). B is stored [k][n].
+template <int MI, int NI, bool A_TRANS, int LDA, int LDB>
+__device__ __forceinline__ void warp_mma(float (&acc)[MI][NI][4], const bf16 *a, const bf16 *b, int wm0, int wn0,
+                                         int lane) {
+#pragma unroll
+    for (int kk = 0; kk < BK / 16; ++kk) {
+        unsigned af[MI][4], bfr[NI][2];
+#pragma unroll
+        for (int mi = 0; mi < MI; ++mi) {
+            if (A_TRANS) {
+                const int i = lane >> 3, r = lane & 7;
+                ldsm_x4_t(af[mi], a + (kk * 16 + r + (i >> 1) * 8) * LDA + wm0 + mi * 16 + (i & 1) * 8);
+            } else {
+                ldsm_x4(af[mi], a + (wm0 + mi * 16 + (lane & 15)) * LDA + kk * 16 + (lane >> 4) * 8);
+            }
+        }
+#pragma unroll
+        for (int nj = 0; nj < NI / 2; ++nj) {
+            unsigned t[4];
+            ldsm_x4_t(t, b + (kk * 16 + (lane & 15)) * LDB + wn0 + nj * 16 + (lane >> 4) * 8);
+            bfr[2 * nj][0] = t[0];
+            bfr[2 * nj][1] = t[1];
+            bfr[2 * nj + 1][0] = t[2];
+            bfr[2 * nj + 1][1] = t[3];
+        }
+#pragma unroll
+        for (int mi = 0; mi < MI; ++mi)
+#pragma unroll
+            for (int ni = 0; ni < NI; ++ni) mma_bf16(acc[mi][ni], af[mi], bfr[ni][0], bfr[ni][1]);
+    }
+}
+
+template <int BN, int WARPS_M, int WARPS_N>
+struct Tile {
+    static constexpr int NT = 32 * WARPS_M * WARPS_N;
+    static constexpr int WM = BM / WARPS_M, WN = BN / WARPS_N;
+    static constexpr int MI = WM / 16, NI = WN / 8;
+    static constexpr int LDB = BN + 8;
+    static_assert(WM % 16 == 0 && WN % 16 == 0, "warp tile must be a multiple of 16x16");
+};
+
+// ---- forward / dgrad convolution -----------------------------------------------------------------
+template <int BN, int WARPS_M, int WARPS_N>
+__global__ void __launch_bounds__(32 * WARPS_M *WARPS_N)
+    k_conv(ConvIn in, int B, int H, int W, const bf16 *__restrict__ w, int Cout, const float *__restrict__ bias,
+           int relu, bf16 *__restrict__ out_bf, float *__restrict__ out_f) {
+    using T = Tile<BN, WARPS_M, WARPS_N>;
+    constexpr int NT = T::NT, LDA = BK + 8, LDB = T::LDB;
+    constexpr int A_ITER = BM * BK / 8 / NT;
+    constexpr int B_CHUNKS = BK * BN / 8;
+    extern __shared__ __align__(128) unsigned char smem[];
+    bf16 *sA = reinterpret_cast<bf16 *>(smem);
+    bf16 *sB = sA + STAGES * BM * LDA;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp / WARPS_N, wn = warp % WARPS_N;
+    const long HW = (long)H * W, P = (long)B * HW;
+    const long m0 = (long)blockIdx.x * BM;
+    const int n0 = blockIdx.y * BN;
+    const int Cin = in.c0 + in.c1, K = 9 * Cin, KT = (K + BK - 1) / BK;
+
+    // Gather state: this thread copies channel group g (8 channels) of rows tid/4 + i NT/4.
+    const int g = tid & 3;
+    int an[A_ITER], ay[A_ITER], ax[A_ITER];
+#pragma unroll
+    for (int i = 0; i < A_ITER; ++i) {
+        const long p = m0 + (tid >> 2) + i * (NT / 4);
+        if (p < P) {
+            an[i] = (int)(p / HW);
+            const long r = p - (long)an[i] * HW;
+            ay[i] = (int)(r / W);
+            ax[i] = (int)(r - (long)ay[i] * W);
+        } else {
+            an[i] = 0;
+            ay[i] = -(1 << 28);  // never inside the image
+            ax[i] = 0;
+        }
+    }
+    int tap = 0, ci = g * 8;  // k = tap Cin + ci of this thread's group at the next load
+    while (ci >= Cin) ci -= Cin, ++tap;
+
+    auto load_stage = [&](int stage, int kc) {
+        bf16 *a = sA + stage * BM * LDA;
+        const bool kvalid = kc + g * 8 < K;
+        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+#pragma unroll
+        for (int i = 0; i < A_ITER; ++i) {
+            const int row = (tid >> 2) + i * (NT / 4);
+            const int yy = ay[i] + dy, xx = ax[i] + dx;
+            const bool v = kvalid && yy >= 0 && yy < H && xx >= 0 && xx < W;
+            const bf16 *src = v ? in_addr(in, an[i], yy, xx, H, W, ci) : in.p0;
+            cp_async16(a + row * LDA + g * 8, src, v);
+        }
+        ci += BK;
+        while (ci >= Cin) ci -= Cin, ++tap;
+        bf16 *b = sB + stage * BK * LDB;
+        for (int q = tid; q < B_CHUNKS; q += NT) {
+            const int kr = q / (BN / 8), c8 = (q % (BN / 8)) * 8;
+            const int k = kc + kr, co = n0 + c8;
+            const bool v = k < K && co < Cout;
+            cp_async16(b + kr * LDB + c8, v ? w + (size_t)k * Cout + co : w, v);
+        }
+    };
+
+    float acc[T::MI][T::NI][4];
+#pragma unroll
+    for (int mi = 0; mi < T::MI; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < T::NI; ++ni)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[mi][ni][e] = 0.0f;
+
+#pragma unroll
+    for (int s = 0; s < STAGES - 1; ++s) {
+        if (s < KT) load_stage(s, s * BK);
+        cp_commit();
+    }
+    for (int kt = 0; kt < KT; ++kt) {
+        cp_wait<STAGES - 2>();
+        __syncthreads();
+        const int nk = kt + STAGES - 1;
+        if (nk < KT) load_stage(nk % STAGES, nk * BK);
+        cp_commit();
+        const int st = kt % STAGES;
+        warp_mma<T::MI, T::NI, false, LDA, LDB>(acc, sA + st * BM * LDA, sB + st * BK * LDB, wm * T::WM,
+                                                 wn * T::WN, lane);
+    }
+    cp_wait<0>();
+
+    const int gq = lane >> 2, tq = lane & 3;
+#pragma unroll
+    for (int mi = 0; mi < T::MI; ++mi)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const long p = m0 + wm * T::WM + mi * 16 + gq + h * 8;
+            if (p >= P) continue;
+#pragma unroll
+            for (int ni = 0; ni < T::NI; ++ni) {
+                const int co = n0 + wn * T::WN + ni * 8 + tq * 2;
+                if (co >= Cout) continue;
+                float v0 = acc[mi][ni][2 * h], v1 = acc[mi][ni][2 * h + 1];
+                if (bias) {
+                    v0 += bias[co];
+                    v1 += bias[co + 1];
+                }
+                if (relu) {
+                    v0 = fmaxf(v0, 0.0f);
+                    v1 = fmaxf(v1, 0.0f);
+                }
+                if (out_bf)
+                    *reinterpret_cast<__nv_bfloat162 *>(out_bf + p * Cout + co) = __floats2bfloat162_rn(v0, v1);
+                if (out_f) *reinterpret_cast<float2 *>(out_f + p * Cout + co) = make_float2(v0, v1);
+            }
+        }
+}
+
+// ---- weight gradient -------------------------------------------------------------------------------
+template <int BN, int WARPS_M, int WARPS_N>
+__global__ void __launch_bounds__(32 * WARPS_M *WARPS_N)
+    k_wgrad(ConvIn in, int B, int H, int W, const bf16 *__restrict__ g, int Cout, long chunk,
+            float *__restrict__ partial) {
+    using T = Tile<BN, WARPS_M, WARPS_N>;
+    constexpr int NT = T::NT, LDA = BM + 8, LDB = T::LDB;
+    constexpr int A_ITER = BK * BM / 8 / NT;
+    constexpr int B_CHUNKS = BK * BN / 8;
+    extern __shared__ __align__(128) unsigned char smem[];
+    bf16 *sA = reinterpret_cast<bf16 *>(smem);
+    bf16 *sB = sA + STAGES * BK * LDA;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp / WARPS_N, wn = warp % WARPS_N;
+    const long HW = (long)H * W, P = (long)B * HW;
+    const int Cin = in.c0 + in.c1, M = 9 * Cin;
+    const int m0 = blockIdx.y * BM, n0 = blockIdx.z * BN;
+    const long pbeg = (long)blockIdx.x * chunk, pend = min(P, pbeg + chunk);
+    const int KT = (int)((pend - pbeg + BK - 1) / BK);
+
+    // A gather: this thread copies m-group mg (8 rows of M: one tap, 8 channels) for the
+    // pixels tid/16 + i NT/16 of each stage.
+    const int mg = tid & 15;
+    const int m = m0 + mg * 8;
+    const bool mvalid = m < M;
+    const int tap = mvalid ? m / Cin : 0, ci = m - tap * Cin;
+    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+    long pp[A_ITER];
+    int pn[A_ITER], py[A_ITER], px[A_ITER];
+#pragma unroll
+    for (int i = 0; i < A_ITER; ++i) {
+        pp[i] = pbeg + (tid >> 4) + i * (NT / 16);
+        const long q = min(pp[i], P - 1);
+        pn[i] = (int)(q / HW);
+        const long r = q - (long)pn[i] * HW;
+        py[i] = (int)(r / W);
+        px[i] = (int)(r - (long)py[i] * W);
+    }
+
+    auto load_stage = [&](int stage, long pk) {
+        bf16 *a = sA + stage * BK * LDA;
+#pragma unroll
+        for (int i = 0; i < A_ITER; ++i) {
+            const int row = (tid >> 4) + i * (NT / 16);
+            const int yy = py[i] + dy, xx = px[i] + dx;
+            const bool v = mvalid && pp[i] < pend && yy >= 0 && yy < H && xx >= 0 && xx < W;
+            const bf16 *src = v ? in_addr(in, pn[i], yy, xx, H, W, ci) : in.p0;
+            cp_async16(a + row * LDA + mg * 8, src, v);
+            // advance this row's pixel by BK
+            pp[i] += BK;
+            px[i] += BK;
+            while (px[i] >= W) px[i] -= W, ++py[i];
+            while (py[i] >= H) py[i] -= H, ++pn[i];
+        }
+        bf16 *b = sB + stage * BK * LDB;
+        for (int q = tid; q < B_CHUNKS; q += NT) {
+            const int kr = q / (BN / 8), c8 = (q % (BN / 8)) * 8;
+            const long p = pk + kr;
+            const int co = n0 + c8;
+            const bool v = p < pend && co < Cout;
+            cp_async16(b + kr * LDB + c8, v ? g + p * Cout + co : g, v);
+        }
+    };
+
+    float acc[T::MI][T::NI][4];
+#pragma unroll
+    for (int mi = 0; mi < T::MI; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < T::NI; ++ni)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[mi][ni][e] = 0.0f;
+
+#pragma unroll
+    for (int s = 0; s < STAGES - 1; ++s) {
+        if (s < KT) load_stage(s, pbeg + (long)s * BK);
+        cp_commit();
+    }
+    for (int kt = 0; kt < KT; ++kt) {
+        cp_wait<STAGES - 2>();
+        __syncthreads();
+        const int nk = kt + STAGES - 1;
+        if (nk < KT) load_stage(nk % STAGES, pbeg + (long)nk * BK);
+        cp_commit();
+        const int st = kt % STAGES;
+        warp_mma<T::MI, T::NI, true, LDA, LDB>(acc, sA + st * BK * LDA, sB + st * BK * LDB, wm * T::WM, wn * T::WN,
+                                                lane);
+    }
+    cp_wait<0>();
+
+    float *dst = partial + (size_t)blockIdx.x * M * Cout;
+    const int gq = lane >> 2, tq = lane & 3;
+#pragma unroll
+    for (int mi = 0; mi < T::MI; ++mi)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = m0 + wm * T::WM + mi * 16 + gq + h * 8;
+            if (r >= M) continue;
+#pragma unroll
+            for (int ni = 0; ni < T::NI; ++ni) {
+                const int co = n0 + wn * T::WN + ni * 8 + tq * 2;
+                if (co >= Cout) continue;
+                *reinterpret_cast<float2 *>(dst + (size_t)r * Cout + co) =
+                    make_float2(acc[mi][ni][2 * h], acc[mi][ni][2 * h + 1]);
+            }
+        }
+}
+
+// out[i] = sum over chunks of partial[c][i], in chunk order (deterministic).
+__global__ void k_reduce_chunks(const float *__restrict__ partial, int chunks, size_t n, float *__restrict__ out) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = 0.0f;
+    for (int c = 0; c < chunks; ++c) s += partial[(size_t)c * n + i];
+    out[i] = s;
+}
+
+// Column sums of a (P x C) FP32 matrix over one chunk of rows per block (C <= 256).
+__global__ void k_colsum(const float *__restrict__ g, long P, int C, long chunk, float *__restrict__ partial) {
+    __shared__ float red[256];
+    const int R = 256 / C;
+    const int r = threadIdx.x / C, c = threadIdx.x % C;
+    const long pbeg = (long)blockIdx.x * chunk, pend = min(P, pbeg + chunk);
+    float s = 0.0f;
+    if (r < R)
+        for (long p = pbeg + r; p < pend; p += R) s += g[p * C + c];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    if ((int)threadIdx.x < C) {
+        float t = 0.0f;
+        for (int k = 0; k < R; ++k) t += red[k * C + threadIdx.x];
+        partial[(size_t)blockIdx.x * C + threadIdx.x] = t;
+    }
+}
+
+__global__ void k_convert(const float *__restrict__ w, int Cin, int Cout, bf16 *__restrict__ wb,
+                          bf16 *__restrict__ wt) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t n = (size_t)9 * Cin * Cout;
+    if (i >= n) return;
+    const bf16 v = __float2bfloat16_rn(w[i]);
+    if (wb) wb[i] = v;
+    if (wt) {
+        const int tap = (int)(i / ((size_t)Cin * Cout));
+        const int r = (int)(i % ((size_t)Cin * Cout));
+        const int ci = r / Cout, co = r % Cout;
+        wt[((size_t)(8 - tap) * Cout + co) * Cin + ci] = v;
+    }
+}
+
+// 2x2 max pooling, NHWC.
+__global__ void k_pool(const bf16 *__restrict__ x, int B, int H, int W, int C, bf16 *__restrict__ y) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const int h = H / 2, w = W / 2;
+    const size_t n = (size_t)B * h * w * C;
+    if (i >= n) return;
+    const int c = (int)(i % C);
+    size_t r = i / C;
+    const int xo = (int)(r % w);
+    r /= w;
+    const int yo = (int)(r % h);
+    const int b = (int)(r / h);
+    const bf16 *s = x + (((size_t)b * H + 2 * yo) * W + 2 * xo) * C + c;
+    const size_t row = (size_t)W * C;
+    const float m = fmaxf(fmaxf(__bfloat162float(s[0]), __bfloat162float(s[C])),
+                          fmaxf(__bfloat162float(s[row]), __bfloat162float(s[row + C])));
+    y[i] = __float2bfloat16_rn(m);
+}
+
+// Pooling gradient: each pooled gradient goes to the first maximal input of its window (row
+// major order), added into gx.
+__global__ void k_pool_back(const bf16 *__restrict__ x, const bf16 *__restrict__ y, const float *__restrict__ gy,
+                            int B, int H, int W, int C, float *__restrict__ gx) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const int h = H / 2, w = W / 2;
+    const size_t n = (size_t)B * h * w * C;
+    if (i >= n) return;
+    const int c = (int)(i % C);
+    size_t r = i / C;
+    const int xo = (int)(r % w);
+    r /= w;
+    const int yo = (int)(r % h);
+    const int b = (int)(r / h);
+    const float m = __bfloat162float(y[i]);
+    const size_t base = (((size_t)b * H + 2 * yo) * W + 2 * xo) * C + c;
+    const size_t row = (size_t)W * C;
+    const size_t off[4] = {0, (size_t)C, row, row + C};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (__bfloat162float(x[base + off[k]]) == m) {
+            gx[base + off[k]] += gy[i];
+            break;
+        }
+}
+
+// Gradient of a concatenated input: channels [0, c0) go to g0 -- summed over each 2x2 block
+// (the adjoint of nearest upsampling) when up0 -- and channels [c0, c0 + c1) to g1.
+// Both are assigned (each is the first gradient its tensor receives).
+__global__ void k_split_grad(const float *__restrict__ gin, int B, int H, int W, int c0, int up0, int c1,
+                             float *__restrict__ g0, float *__restrict__ g1) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const int Cin = c0 + c1;
+    const size_t n = (size_t)B * H * W * Cin;
+    if (i >= n) return;
+    const int c = (int)(i % Cin);
+    const size_t p = i / Cin;
+    if (c >= c0) {
+        g1[p * c1 + (c - c0)] = gin[i];
+        return;
+    }
+    if (!up0) {
+        g0[p * c0 + c] = gin[i];
+        return;
+    }
+    const int x = (int)(p % W);
+    const size_t q = p / W;
+    const int y = (int)(q % H);
+    const int b = (int)(q / H);
+    if ((x & 1) || (y & 1)) return;
+    const size_t rowc = (size_t)W * Cin;
+    const float s = (gin[i] + gin[i + Cin]) + (gin[i + rowc] + gin[i + rowc + Cin]);
+    g0[(((size_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * c0 + c] = s;
+}
+
+__global__ void k_relu_grad(float *__restrict__ g, const bf16 *__restrict__ y, size_t n, int relu,
+                            bf16 *__restrict__ gb) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float v = g[i];
+    if (relu && !(__bfloat162float(y[i]) > 0.0f)) {
+        v = 0.0f;
+        g[i] = 0.0f;
+    }
+    gb[i] = __float2bfloat16_rn(v);
+}
+
+// Features {radiance rgb, albedo rgb, normal xyz, distance} -> 16 channels:
+// log(1 + radiance), albedo, normal / 2 + 1/2, distance / (1 + distance), zeros; padded
+// pixels replicate the nearest edge pixel.
+__global__ void k_prepare(const float *__restrict__ f, int B, int H, int W, int Hp, int Wp, bf16 *__restrict__ x) {
+    const size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t n = (size_t)B * Hp * Wp;
+    if (q >= n) return;
+    const int xp = (int)(q % Wp);
+    const size_t r = q / Wp;
+    const int yp = (int)(r % Hp);
+    const int b = (int)(r / Hp);
+    const float *s = f + (((size_t)b * H + min(yp, H - 1)) * W + min(xp, W - 1)) * 10;
+    float v[16];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) v[k] = log1pf(fmaxf(s[k], 0.0f));
+#pragma unroll
+    for (int k = 3; k < 6; ++k) v[k] = s[k];
+#pragma unroll
+    for (int k = 6; k < 9; ++k) v[k] = s[k] * 0.5f + 0.5f;
+    const float d = fmaxf(s[9], 0.0f);
+    v[9] = d / (1.0f + d);
+#pragma unroll
+    for (int k = 10; k < 16; ++k) v[k] = 0.0f;
+    __nv_bfloat162 o[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) o[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+    uint4 *dst = reinterpret_cast<uint4 *>(x + q * 16);
+    dst[0] = *reinterpret_cast<uint4 *>(&o[0]);
+    dst[1] = *reinterpret_cast<uint4 *>(&o[4]);
+}
+
+// radiance = max(exp(log(1 + input) + y) - 1, 0): the network predicts a correction of the
+// noisy input in log space.
+__global__ void k_finish(const bf16 *__restrict__ x, const float *__restrict__ y, int B, int H, int W, int Hp, int Wp,
+                         float *__restrict__ out) {
+    const size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t n = (size_t)B * H * W;
+    if (o >= n) return;
+    const int xx = (int)(o % W);
+    const size_t r = o / W;
+    const int yy = (int)(r % H);
+    const int b = (int)(r / H);
+    const size_t q = ((size_t)b * Hp + yy) * Wp + xx;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) out[o * 3 + k] = fmaxf(expm1f(__bfloat162float(x[q * 16 + k]) + y[q * 16 + k]), 0.0f);
+}
+
+// L1 loss in log space: mean over pixels and channels of |log(1+x) + y - log(1 + target)|.
+__global__ void k_l1(const bf16 *__restrict__ x, const float *__restrict__ y, const float *__restrict__ t, long P,
+                     float *__restrict__ gy, float *__restrict__ partial) {
+    __shared__ float red[256];
+    const long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    float l = 0.0f;
+    if (p < P) {
+        const float inv = 1.0f / (3.0f * (float)P);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            float gk = 0.0f;
+            if (k < 3) {
+                const float d = __bfloat162float(x[p * 16 + k]) + y[p * 16 + k] - log1pf(fmaxf(t[p * 3 + k], 0.0f));
+                l += fabsf(d);
+                gk = d > 0.0f ? inv : (d < 0.0f ? -inv : 0.0f);
+            }
+            gy[p * 16 + k] = gk;
+        }
+    }
+    red[threadIdx.x] = l;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+__global__ void k_loss_total(const float *__restrict__ partial, int n, float scale, Hyper *h) {
+    __shared__ float red[256];
+    float s = 0.0f;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) h->loss = red[0] * scale;
+}
+
+__global__ void k_adam_step(Hyper *h) {
+    const int s = h->step + 1;
+    h->step = s;
+    h->c1 = 1.0f - powf(h->b1, (float)s);
+    h->c2 = 1.0f - powf(h->b2, (float)s);
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master parameters; refreshes the BF16 forward and
+// dgrad copies of each updated weight.
+__global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
+                       float *__restrict__ v, size_t n, LayerTable tab, const Hyper *__restrict__ h,
+                       bf16 *__restrict__ wb, bf16 *__restrict__ wt) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = h->b1 * m[i] + (1.0f - h->b1) * gi;
+    const float vi = h->b2 * v[i] + (1.0f - h->b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - h->lr * (mi / h->c1) / (sqrtf(vi / h->c2) + h->eps);
+    w[i] = wi;
+    for (int l = 0; l < tab.n; ++l) {
+        const LayerW L = tab.l[l];
+        const size_t nw = (size_t)9 * L.cin * L.cout;
+        if (i >= L.woff && i < L.woff + nw) {
+            const size_t j = i - L.woff;
+            const bf16 b = __float2bfloat16_rn(wi);
+            wb[i] = b;
+            const int tap = (int)(j / ((size_t)L.cin * L.cout));
+            const int r = (int)(j % ((size_t)L.cin * L.cout));
+            const int ci = r / L.cout, co = r % L.cout;
+            wt[L.woff + ((size_t)(8 - tap) * L.cout + co) * L.cin + ci] = b;
+            break;
+        }
+    }
+}
+
+inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+// ---- tile selection ------------------------------------------------------------------------------
+// Output-channel tile: the candidate minimising tiles x BN + 32 x tiles, i.e. MMA work on
+// padded channels plus one re-gather of the activations per tile.
+int pick_bn(int N) {
+    static const int cand[] = {16, 32, 48, 64, 96, 128};
+    int best = 128, bestc = 1 << 30;
+    for (int bn : cand) {
+        const int tiles = (N + bn - 1) / bn;
+        const int c = tiles * bn + 32 * tiles;
+        if (c < bestc) bestc = c, best = bn;
+    }
+    return best;
+}
+
+template <int BN>
+constexpr size_t conv_smem() {
+    return (size_t)STAGES * (BM * (BK + 8) + BK * (BN + 8)) * sizeof(bf16);
+}
+template <int BN>
+constexpr size_t wgrad_smem() {
+    return (size_t)STAGES * (BK * (BM + 8) + BK * (BN + 8)) * sizeof(bf16);
+}
+
+template <int BN, int WARPS_M, int WARPS_N>
+int launch_conv(const ConvIn &in, int B, int H, int W, const bf16 *w, int Cout, const float *bias, bool relu,
+                bf16 *out_bf, float *out_f, cudaStream_t st) {
+    constexpr size_t smem = conv_smem<BN>();
+    static bool attr = false;
+    if (!attr) {
+        RT_CUDA_TRY(cudaFuncSetAttribute(k_conv<BN, WARPS_M, WARPS_N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+        attr = true;
+    }
+    const long P = (long)B * H * W;
+    const dim3 grid((unsigned)((P + BM - 1) / BM), (unsigned)((Cout + BN - 1) / BN));
+    k_conv<BN, WARPS_M, WARPS_N><<<grid, 32 * WARPS_M * WARPS_N, smem, st>>>(in, B, H, W, w, Cout, bias, relu ? 1 : 0,
+                                                                               out_bf, out_f);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+struct WgradPlan {
+    int bn, mtiles, ntiles, chunks;
+    long chunk;
+};
+
+// Pixel chunks of the split-K weight gradient: about four CTAs per SM in total, at least
+// 256 pixels per chunk, chunk lengths a multiple of BK.
+WgradPlan wgrad_plan(long P, int Cin, int Cout) {
+    WgradPlan p;
+    p.bn = pick_bn(Cout);
+    p.mtiles = (9 * Cin + BM - 1) / BM;
+    p.ntiles = (Cout + p.bn - 1) / p.bn;
+    const long tiles = (long)p.mtiles * p.ntiles;
+    const long target = (4L * 152 + tiles - 1) / tiles;
+    const long chunks = std::max(1L, std::min(target, (P + 255) / 256));
+    long chunk = (P + chunks - 1) / chunks;
+    chunk = (chunk + BK - 1) / BK * BK;
+    p.chunk = chunk;
+    p.chunks = (int)((P + chunk - 1) / chunk);
+    return p;
+}
+
+template <int BN, int WARPS_M, int WARPS_N>
+int launch_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, const WgradPlan &pl, float *partial,
+                 cudaStream_t st) {
+    constexpr size_t smem = wgrad_smem<BN>();
+    static bool attr = false;
+    if (!attr) {
+        RT_CUDA_TRY(cudaFuncSetAttribute(k_wgrad<BN, WARPS_M, WARPS_N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+        attr = true;
+    }
+    const dim3 grid((unsigned)pl.chunks, (unsigned)pl.mtiles, (unsigned)pl.ntiles);
+    k_wgrad<BN, WARPS_M, WARPS_N><<<grid, 32 * WARPS_M * WARPS_N, smem, st>>>(in, B, H, W, g, Cout, pl.chunk, partial);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+constexpr long kColsumRows = 1024;
+
+}  // namespace
+
+// ---- launchers -------------------------------------------------------------------------------
+int conv_forward(const ConvIn &in, int B, int H, int W, const bf16 *w, const float *bias, int Cout, bool relu,
+                 bf16 *out_bf, float *out_f, cudaStream_t st) {
+    switch (pick_bn(Cout)) {
+        case 16: return launch_conv<16, 4, 1>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
+        case 32: return launch_conv<32, 4, 1>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
+        case 48: return launch_conv<48, 4, 1>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
+        case 64: return launch_conv<64, 2, 2>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
+        case 96: return launch_conv<96, 4, 2>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
+        default: return launch_conv<128, 4, 2>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
+    }
+}
+
+size_t wgrad_partial_floats(long P, int Cin, int Cout) {
+    const WgradPlan pl = wgrad_plan(P, Cin, Cout);
+    return (size_t)pl.chunks * 9 * Cin * Cout;
+}
+
+int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, float *partial, float *dw,
+               cudaStream_t st) {
+    const long P = (long)B * H * W;
+    const int Cin = in.c0 + in.c1;
+    const WgradPlan pl = wgrad_plan(P, Cin, Cout);
+    int rc;
+    switch (pl.bn) {
+        case 16: rc = launch_wgrad<16, 4, 1>(in, B, H, W, g, Cout, pl, partial, st); break;
+        case 32: rc = launch_wgrad<32, 4, 1>(in, B, H, W, g, Cout, pl, partial, st); break;
+        case 48: rc = launch_wgrad<48, 4, 1>(in, B, H, W, g, Cout, pl, partial, st); break;
+        case 64: rc = launch_wgrad<64, 2, 2>(in, B, H, W, g, Cout, pl, partial, st); break;
+        case 96: rc = launch_wgrad<96, 4, 2>(in, B, H, W, g, Cout, pl, partial, st); break;
+        default: rc = launch_wgrad<128, 4, 2>(in, B, H, W, g, Cout, pl, partial, st); break;
+    }
+    if (rc != RT_OK) return rc;
+    const size_t n = (size_t)9 * Cin * Cout;
+    k_reduce_chunks<<<blocks(n), 256, 0, st>>>(partial, pl.chunks, n, dw);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+size_t colsum_partial_floats(long P, int C) { return (size_t)((P + kColsumRows - 1) / kColsumRows) * C; }
+
+int colsum(const float *g, long P, int C, float *partial, float *db, cudaStream_t st) {
+    const int chunks = (int)((P + kColsumRows - 1) / kColsumRows);
+    k_colsum<<<chunks, 256, 0, st>>>(g, P, C, kColsumRows, partial);
+    k_reduce_chunks<<<blocks(C), 256, 0, st>>>(partial, chunks, (size_t)C, db);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int convert_weights(const float *w, int Cin, int Cout, bf16 *wb, bf16 *wt, cudaStream_t st) {
+    k_convert<<<blocks((size_t)9 * Cin * Cout), 256, 0, st>>>(w, Cin, Cout, wb, wt);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st) {
+    k_pool<<<blocks((size_t)B * (H / 2) * (W / 2) * C), 256, 0, st>>>(x, B, H, W, C, y);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pool_back(const bf16 *x, const bf16 *y, const float *gy, int B, int H, int W, int C, float *gx, cudaStream_t st) {
+    k_pool_back<<<blocks((size_t)B * (H / 2) * (W / 2) * C), 256, 0, st>>>(x, y, gy, B, H, W, C, gx);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int split_grad(const float *gin, int B, int H, int W, int c0, int up0, int c1, float *g0, float *g1, cudaStream_t st) {
+    k_split_grad<<<blocks((size_t)B * H * W * (c0 + c1)), 256, 0, st>>>(gin, B, H, W, c0, up0, c1, g0, g1);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int relu_grad(float *g, const bf16 *y, size_t n, bool relu, bf16 *gb, cudaStream_t st) {
+    k_relu_grad<<<blocks(n), 256, 0, st>>>(g, y, n, relu ? 1 : 0, gb);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int prepare(const float *f, int B, int H, int W, int Hp, int Wp, bf16 *x, cudaStream_t st) {
+    k_prepare<<<blocks((size_t)B * Hp * Wp), 256, 0, st>>>(f, B, H, W, Hp, Wp, x);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int finish(const bf16 *x, const float *y, int B, int H, int W, int Hp, int Wp, float *out, cudaStream_t st) {
+    k_finish<<<blocks((size_t)B * H * W), 256, 0, st>>>(x, y, B, H, W, Hp, Wp, out);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int l1_loss(const bf16 *x, const float *y, const float *target, long P, float *gy, float *partial, Hyper *hyper,
+            cudaStream_t st) {
+    const unsigned nb = blocks((size_t)P);
+    k_l1<<<nb, 256, 0, st>>>(x, y, target, P, gy, partial);
+    k_loss_total<<<1, 256, 0, st>>>(partial, (int)nb, 1.0f / (3.0f * (float)P), hyper);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int adam(float *params, const float *grads, float *m, float *v, size_t n, const LayerTable &tab, Hyper *hyper,
+         bf16 *wb, bf16 *wt, cudaStream_t st) {
+    k_adam_step<<<1, 1, 0, st>>>(hyper);
+    k_adam<<<blocks(n), 256, 0, st>>>(params, grads, m, v, n, tab, hyper, wb, wt);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+}  // namespace dn
+}  // namespace rgb

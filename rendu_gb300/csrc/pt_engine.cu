@@ -269,10 +269,13 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
     w.stats = reinterpret_cast<unsigned long long *>(counters_.as<char>() + 64);
     w.status = reinterpret_cast<unsigned *>(counters_.as<char>() + 96);
     w.accum = accum_.as<float>();
-    w.accum64 = any_fp64 ? accum64_.as<double>() : nullptr;
-    w.aov0 = any_aov ? aov0_.as<float4>() : nullptr;
-    w.aov1 = any_aov ? aov1_.as<float4>() : nullptr;
-    w.aov_accum = any_aov ? aov_accum_.as<float>() : nullptr;
+    // The optional buffers go into the captured graph whether or not this call uses them:
+    // a graph replayed by a later call whose jobs do use them must hold their addresses.
+    // They are null only until first allocated, and that allocation forces a new capture.
+    w.accum64 = accum64_.as<double>();
+    w.aov0 = aov0_.as<float4>();
+    w.aov1 = aov1_.as<float4>();
+    w.aov_accum = aov_accum_.as<float>();
     w.jobs = jobs_.as<PtJob>();
     w.bvhs = bvhs_.as<JobBvh>();
     w.tiles = tiles_.as<PtTile>();

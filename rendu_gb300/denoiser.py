@@ -1,0 +1,273 @@
+"""Learned denoiser over the C-ABI ``dn_*`` entry points.
+
+A 5-level U-Net (3x3 convolutions with 32, 48, 64, 96 and 128 channels, BF16 activations,
+FP32 accumulation on the tensor cores) that maps a few-sample render plus its first-hit
+feature buffers (albedo, normal, distance: ``PathTracer.render(..., aov=...)``) to a
+converged image. The reference has no learned denoiser; this module completes the
+renderer with one that is trained here on the path tracer's own output.
+
+Arrays are float32 NHWC: features (B, H, W, 10) = radiance rgb, albedo rgb, normal xyz,
+distance; images (B, H, W, 3). Host numpy arrays or CUDA tensors (all of one kind per call).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+FEATURES = L.DN_FEATURES
+
+
+def _is_cuda(a) -> bool:
+    return type(a).__module__.startswith("torch") and getattr(a, "is_cuda", False)
+
+
+def _ptr(a):
+    if _is_cuda(a):
+        import torch
+
+        if not a.is_contiguous() or a.dtype != torch.float32:
+            raise TypeError("CUDA tensors must be contiguous float32")
+        return C.c_void_p(a.data_ptr())
+    if not (isinstance(a, np.ndarray) and a.dtype == np.float32 and a.flags.c_contiguous):
+        raise TypeError("arrays must be C-contiguous float32")
+    return C.c_void_p(a.ctypes.data)
+
+
+def _stream():
+    import torch
+
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _nhwc(a, channels):
+    shape = tuple(a.shape)
+    if len(shape) == 3:
+        shape = (1,) + shape
+    if len(shape) != 4 or shape[3] != channels:
+        raise ValueError(f"expected (B, H, W, {channels}) or (H, W, {channels}), got {tuple(a.shape)}")
+    return shape
+
+
+def rel_rmse(x, ref, eps: float = 1e-2) -> float:
+    """Relative RMSE, sqrt(mean(((x - ref) / (ref + eps))^2)), over every pixel and channel."""
+    x = np.asarray(x, np.float64)
+    ref = np.asarray(ref, np.float64)
+    return float(np.sqrt(np.mean(((x - ref) / (ref + eps)) ** 2)))
+
+
+def features_from_render(image, aov) -> np.ndarray:
+    """Stack a render (H, W, >=3) and its feature buffer (H, W, 7) into (H, W, 10)."""
+    return np.ascontiguousarray(np.concatenate([np.asarray(image)[..., :3], np.asarray(aov)], axis=-1), np.float32)
+
+
+class Denoiser:
+    """The U-Net on one device. ``denoise`` runs inference; ``train_step`` one Adam step on
+    a batch of (features, converged target) crops whose sides are multiples of 16."""
+
+    def __init__(self, device: int = 0, seed: int | None = None):
+        h = C.c_void_p()
+        L.call("dn_create", C.byref(h), int(device))
+        self._h = h
+        self.device = device
+        if seed is not None:
+            L.call("dn_init", self._h, int(seed))
+
+    # ---- structure and parameters ------------------------------------------------------------
+    def layers(self) -> list[dict]:
+        n = C.c_uint32()
+        L.call("dn_layer_count", self._h, C.byref(n))
+        out = []
+        for i in range(n.value):
+            d = L.dn_layer()
+            L.call("dn_layer_info", self._h, i, C.byref(d))
+            out.append({k: getattr(d, k) for k, _ in d._fields_})
+        return out
+
+    @property
+    def param_count(self) -> int:
+        n = C.c_size_t()
+        L.call("dn_param_count", self._h, C.byref(n))
+        return n.value
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.param_count, np.float32)
+        L.call("dn_get_params", self._h, out.ctypes.data, out.size)
+        return out
+
+    def set_params(self, params) -> None:
+        p = np.ascontiguousarray(params, np.float32).reshape(-1)
+        L.call("dn_set_params", self._h, p.ctypes.data, p.size)
+
+    def get_grads(self) -> np.ndarray:
+        out = np.empty(self.param_count, np.float32)
+        L.call("dn_get_grads", self._h, out.ctypes.data, out.size)
+        return out
+
+    def init(self, seed: int) -> None:
+        L.call("dn_init", self._h, int(seed))
+
+    def save(self, path: str) -> None:
+        np.save(path, self.get_params())
+
+    def load(self, path: str) -> None:
+        self.set_params(np.load(path))
+
+    def flops(self, height: int, width: int, batch: int = 1) -> float:
+        """Multiply-add FLOPs of one forward pass (2 x MACs of every convolution) at the
+        padded size the network runs at."""
+        hp, wp = -(-height // 16) * 16, -(-width // 16) * 16
+        total = 0.0
+        for l in self.layers():
+            px = batch * (hp >> l["level"]) * (wp >> l["level"])
+            total += 2.0 * px * 9 * (l["cin0"] + l["cin1"]) * l["cout"]
+        return total
+
+    # ---- compute -----------------------------------------------------------------------------
+    def denoise(self, features, out=None):
+        """features (B, H, W, 10) or (H, W, 10) -> radiance of the same leading shape x 3."""
+        b, h, w, _ = _nhwc(features, FEATURES)
+        dev = _is_cuda(features)
+        if out is None:
+            if dev:
+                import torch
+
+                out = torch.empty(tuple(features.shape[:-1]) + (3,), dtype=torch.float32, device=features.device)
+            else:
+                out = np.empty(tuple(features.shape[:-1]) + (3,), np.float32)
+        L.call("dn_denoise", self._h, _ptr(features), w, h, b, _ptr(out), _stream() if dev else None,
+               L.RT_FLAG_DEVICE_PTRS if dev else 0)
+        return out
+
+    def backward(self, features, target, read_loss: bool = True):
+        """Loss and gradients of one batch (kept on the device; ``get_grads`` reads them)."""
+        b, h, w, _ = _nhwc(features, FEATURES)
+        dev = _is_cuda(features)
+        loss = C.c_float()
+        L.call("dn_backward", self._h, _ptr(features), _ptr(target), w, h, b, C.byref(loss) if read_loss else None,
+               _stream() if dev else None, L.RT_FLAG_DEVICE_PTRS if dev else 0)
+        return loss.value if read_loss else None
+
+    def adam_step(self, lr: float) -> None:
+        L.call("dn_adam_step", self._h, float(lr), _stream() if _torch_cuda() else None)
+
+    def train_step(self, features, target, lr: float, read_loss: bool = True):
+        b, h, w, _ = _nhwc(features, FEATURES)
+        dev = _is_cuda(features)
+        loss = C.c_float()
+        L.call("dn_train_step", self._h, _ptr(features), _ptr(target), w, h, b, float(lr),
+               C.byref(loss) if read_loss else None, _stream() if dev else None, L.RT_FLAG_DEVICE_PTRS if dev else 0)
+        return loss.value if read_loss else None
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            L.lib().dn_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def render_pairs(tracer, cameras, width: int, height: int, spp_in: int = 4, spp_ref: int = 1024, depth: int = 5,
+                 mode: int = 1, clamp: float = 5.0, seed: int = 0):
+    """Denoiser inputs and targets rendered by the path tracer itself: for each camera, the
+    features of a ``spp_in``-sample render (radiance + first-hit albedo, normal, distance)
+    and, when ``spp_ref`` > 0, a ``spp_ref``-sample render accumulated in double precision.
+    Returns CUDA tensors (N, H, W, 10) and (N, H, W, 3) (targets None without spp_ref)."""
+    import torch
+
+    n = len(cameras)
+    dev = torch.device("cuda", tracer.device)
+    feats = torch.empty((n, height, width, FEATURES), dtype=torch.float32, device=dev)
+    targets = torch.empty((n, height, width, 3), dtype=torch.float32, device=dev) if spp_ref else None
+    img = torch.empty((height, width, 3), dtype=torch.float32, device=dev)
+    aov = torch.empty((height, width, 7), dtype=torch.float32, device=dev)
+    for k, cam in enumerate(cameras):
+        cam = dict(cam, ratio=width / height)
+        img.zero_()
+        tracer.render(cam, spp_in, depth, img, seed=seed + 2 * k, mode=mode, clamp=clamp, aov=aov)
+        feats[k, ..., :3] = img
+        feats[k, ..., 3:] = aov
+        if spp_ref:
+            img.zero_()
+            tracer.render(cam, spp_ref, depth, img, seed=seed + 2 * k + 1, mode=mode, clamp=clamp, fp64=True)
+            targets[k] = img
+    return feats, targets
+
+
+def train(denoiser, feats, targets, steps: int, batch: int = 8, crop: int = 64, lr: float = 2e-3, seed: int = 0,
+          log_every: int = 0):
+    """Adam on random ``crop`` x ``crop`` crops of (feats, targets) -- CUDA tensors as
+    render_pairs returns them -- with a cosine-decayed learning rate. Crops are gathered on
+    the device; only the logged losses (every ``log_every`` steps) synchronise. Returns
+    [(step, loss)]."""
+    import math
+
+    import torch
+
+    n, h, w, _ = feats.shape
+    if crop % 16 or crop > min(h, w):
+        raise ValueError("crop must be a multiple of 16 no larger than the images")
+    gen = torch.Generator(device=feats.device)
+    gen.manual_seed(int(seed))
+    ar = torch.arange(crop, device=feats.device)
+    losses = []
+    for s in range(steps):
+        i = torch.randint(0, n, (batch,), generator=gen, device=feats.device)
+        y = torch.randint(0, h - crop + 1, (batch,), generator=gen, device=feats.device)
+        x = torch.randint(0, w - crop + 1, (batch,), generator=gen, device=feats.device)
+        bi, rows, cols = i[:, None, None], (y[:, None] + ar)[:, :, None], (x[:, None] + ar)[:, None, :]
+        f = feats[bi, rows, cols].contiguous()
+        t = targets[bi, rows, cols].contiguous()
+        lr_s = lr * 0.5 * (1.0 + math.cos(math.pi * s / steps))
+        read = bool(log_every) and (s % log_every == 0 or s == steps - 1)
+        loss = denoiser.train_step(f, t, lr_s, read_loss=read)
+        if read:
+            losses.append((s, loss))
+    return losses
+
+
+def _torch_cuda() -> bool:
+    try:
+        import torch
+
+        return torch.cuda.is_available() and torch.cuda.is_initialized()
+    except Exception:
+        return False
+
+
+def conv3x3(x0, weights, cout: int, x1=None, up0: bool = False, bias=None, relu: bool = False, out_fp32=True):
+    """One dn_conv3x3 layer on CUDA tensors: x0 (B, H>>up0, W>>up0, c0) and x1 (B, H, W, c1)
+    bfloat16, weights bfloat16 (9, c0 + c1, cout), bias float32 (cout,) or None."""
+    import torch
+
+    b, h0, w0, c0 = x0.shape
+    h, w = (2 * h0, 2 * w0) if up0 else (h0, w0)
+    c1 = 0 if x1 is None else x1.shape[3]
+    out = torch.empty((b, h, w, cout), dtype=torch.float32 if out_fp32 else torch.bfloat16, device=x0.device)
+    L.call("dn_conv3x3", C.c_void_p(x0.data_ptr()), c0, int(up0), C.c_void_p(x1.data_ptr()) if x1 is not None else None,
+           c1, b, h, w, C.c_void_p(weights.data_ptr()), C.c_void_p(bias.data_ptr()) if bias is not None else None, cout,
+           int(relu), C.c_void_p(out.data_ptr()), int(out_fp32), _stream())
+    return out
+
+
+def conv3x3_backward(x0, weights_f32, gy, x1=None, up0: bool = False, want_dx=True, want_dw=True):
+    """dn_conv3x3_backward on CUDA tensors: returns (dx (B, H, W, c0 + c1) float32 or None,
+    dw (9, c0 + c1, cout) float32 or None) for the bfloat16 output gradient gy."""
+    import torch
+
+    b, h, w, cout = gy.shape
+    c0 = x0.shape[3]
+    c1 = 0 if x1 is None else x1.shape[3]
+    dx = torch.empty((b, h, w, c0 + c1), dtype=torch.float32, device=gy.device) if want_dx else None
+    dw = torch.empty((9, c0 + c1, cout), dtype=torch.float32, device=gy.device) if want_dw else None
+    L.call("dn_conv3x3_backward", C.c_void_p(x0.data_ptr()), c0, int(up0),
+           C.c_void_p(x1.data_ptr()) if x1 is not None else None, c1, b, h, w, C.c_void_p(weights_f32.data_ptr()),
+           cout, C.c_void_p(gy.data_ptr()), C.c_void_p(dx.data_ptr()) if dx is not None else None,
+           C.c_void_p(dw.data_ptr()) if dw is not None else None, _stream())
+    return dx, dw

@@ -606,3 +606,29 @@ def _batch_scene(rng, instances, sub, protos):
     sc.background = {"mode": 2, "color": (0, 0, 0), "tex": tuple(sc.add_texture(f) for f in faces)}
     sc.camera = {"eye": (0.0, 8.0, 20.0), "center": (0.0, 1.0, 0.0), "up": (0.0, 1.0, 0.0), "fov": 1.0, "ratio": 1.0}
     return sc
+
+
+def denoiser_scene(seed: int = 20261208, instances: int = 60) -> Scene:
+    """The denoiser's scenes: the large workload's kind of scene at a smaller size --
+    `instances` seeded displaced icospheres (1,280 triangles at 3 subdivisions) and boxes
+    with GGX materials on a ground plane, four emissive quads, the procedural HDR sky as a
+    cubemap background and as the extended estimator's environment map."""
+    return instanced_scene(seed, instances=instances, subdivisions=3, prototypes=3, env_face=64)
+
+
+def random_cameras(seed: int, count: int, ratio: float = 1.0):
+    """Seeded viewpoints over an instanced scene: eyes on rings 8-30 units from the centre
+    at heights 1.5-10, looking at points near the ground within 10 units of the centre,
+    vertical field of view 0.6-1.2 rad."""
+    rng = np.random.default_rng(seed)
+    cams = []
+    for _ in range(count):
+        a = rng.uniform(0, 2 * math.pi)
+        r = rng.uniform(8.0, 30.0)
+        eye = (r * math.cos(a), rng.uniform(1.5, 10.0), r * math.sin(a))
+        b = rng.uniform(0, 2 * math.pi)
+        q = rng.uniform(0.0, 10.0)
+        center = (q * math.cos(b), rng.uniform(0.5, 1.5), q * math.sin(b))
+        cams.append({"eye": eye, "center": center, "up": (0.0, 1.0, 0.0), "fov": float(rng.uniform(0.6, 1.2)),
+                     "ratio": ratio})
+    return cams

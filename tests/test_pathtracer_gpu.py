@@ -174,6 +174,40 @@ def test_extended_estimator_converges_to_reference_estimator(cuda_lib):
     assert_same_distribution(imgs[2], imgs[0], imgs[1], factor=1.3)
 
 
+def test_optional_buffers_survive_graph_reuse(cuda_lib):
+    """The wave engine replays one captured graph across calls. A render with feature
+    buffers after a call that re-captured it without them (the first double-precision
+    accumulation allocates and forces a new capture), and a double-precision render after
+    a capture made without one, both still get their buffers."""
+    from rendu_gb300 import scenes as S
+
+    sc = S.cornell_scene(3)
+    tr = cuda_lib.PathTracer(sc)
+    img = np.zeros((24, 24, 3), np.float32)
+    aov = np.zeros((24, 24, 7), np.float32)
+    tr.render(sc.camera, 2, 3, img, seed=1, aov=aov)
+    ref_img, ref_aov = img.copy(), aov.copy()
+    img64 = np.zeros_like(img)
+    tr.render(sc.camera, 2, 3, img64, seed=1, fp64=True)
+    np.testing.assert_allclose(img64, ref_img, rtol=1e-6, atol=1e-7)
+    img[:] = 0
+    aov2 = np.zeros_like(aov)
+    tr.render(sc.camera, 2, 3, img, seed=1, aov=aov2)
+    np.testing.assert_array_equal(aov2, ref_aov)
+    np.testing.assert_array_equal(img, ref_img)
+    # A different depth re-captures during a render without either option ...
+    tmp = np.zeros_like(img)
+    tr.render(sc.camera, 2, 4, tmp, seed=1)
+    # ... and both options still work at that depth afterwards.
+    a = np.zeros_like(img)
+    tr.render(sc.camera, 2, 4, a, seed=1, fp64=True)
+    np.testing.assert_allclose(a, tmp, rtol=1e-6, atol=1e-7)
+    aov3 = np.zeros_like(aov)
+    b = np.zeros_like(img)
+    tr.render(sc.camera, 2, 4, b, seed=1, aov=aov3)
+    np.testing.assert_array_equal(aov3, ref_aov)
+
+
 def test_feature_buffers_and_fp64_accumulation(cuda_lib):
     """First-hit features: a camera-facing quad of one linear albedo gives that albedo, the
     normal facing the camera and the hit distance at every pixel; double-precision
@@ -192,7 +226,11 @@ def test_feature_buffers_and_fp64_accumulation(cuda_lib):
     np.testing.assert_allclose(aov[..., 0:3], np.broadcast_to(np.float32([0.5, 0.25, 0.75]) ** np.float32(2.2),
                                                               (16, 16, 3)), rtol=1e-5)
     np.testing.assert_allclose(aov[..., 3:6], np.broadcast_to(np.float32([0, 0, 1]), (16, 16, 3)), atol=1e-5)
-    assert (aov[..., 6] >= 3.0).all() and (aov[..., 6] < 3.6).all()  # distance 3 at the centre, more off-axis
+    # Distance: 3 along the axis, 3 |d| / |d.z| off-axis for the pixel-centre direction d
+    # (the per-sample jitter moves it by well under 3% inside a pixel at this resolution).
+    t = np.tan(0.5) * ((np.arange(16) + 0.5) / 16 * 2 - 1)
+    dist = 3.0 * np.sqrt(1.0 + t[None, :] ** 2 + t[:, None] ** 2)
+    np.testing.assert_allclose(aov[..., 6], dist, rtol=3e-2)
     img64 = np.zeros_like(img)
     tr.render(sc.camera, 4, 2, img64, seed=1, fp64=True)
     np.testing.assert_allclose(img64, img, rtol=1e-6, atol=1e-7)
