@@ -25,6 +25,10 @@ beside it.
 * batch    -- 64 seeded jobs (10k-500k triangles, 128^2-1024^2, 4-256 spp, depth 3-10) in
                one batched call (waves replayed from a CUDA graph, autotuned), vs the same
                jobs rendered one call after another.
+* denoiser -- the learned denoiser (BF16 tensor-core U-Net) trained on path-tracer pairs:
+               inference TFLOP/s at 1920x1080 against the BF16 peak, training-step
+               throughput, and plain vs denoised path tracing at equal time (relative RMSE
+               against a 4096-spp render of a held-out scene).
 * --impl reference -- only that CPU path, as the reference arm.
 Under torchrun (N > 1) every rank traces its own 16M rays (weak scaling, no collective on
 the data path); value = all rays / max-over-ranks time.
@@ -296,6 +300,133 @@ def run_batch(cpu: bool, tune: bool = True):
     return out
 
 
+def _bf16_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["bf16_tflops"]), "measured (burst)"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def _events_ms(fn, iters):
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(iters):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / iters
+
+
+def run_denoiser(cpu: bool):
+    """The learned denoiser: trained here on path-tracer pairs (C3-type seeded scenes,
+    128^2 views, 4-64 spp inputs with first-hit features, 512-spp double-precision
+    targets), then (1) inference throughput at 1920x1080 and training-step throughput at
+    8 x 256^2 against the BF16 tensor peak, and (2) plain path tracing vs path tracing +
+    denoiser on a held-out scene at 480x270, relative RMSE against a 4096-spp
+    double-precision render, and the time each needs to reach given error levels."""
+    import torch
+
+    import rendu_gb300 as R
+    from rendu_gb300 import denoiser as D
+    from rendu_gb300 import scenes as S
+
+    sc = S.denoiser_scene(20261208)
+    tr = R.PathTracer(sc)
+    t0 = time.perf_counter()
+    feats, targets = D.render_pairs(tr, S.random_cameras(20261208, 48), 128, 128, spp_in=[4, 8, 16, 32, 64],
+                                    spp_ref=512, seed=1)
+    torch.cuda.synchronize()
+    data_s = time.perf_counter() - t0
+    net = D.Denoiser(seed=1)
+    steps = 4000
+    t0 = time.perf_counter()
+    losses = D.train(net, feats, targets, steps, batch=8, crop=64, lr=2e-3, log_every=1000)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+
+    # ---- throughput -----------------------------------------------------------------------
+    peak, peak_kind = _bf16_peak()
+    x = torch.rand((1, 1080, 1920, D.FEATURES), device="cuda")
+    o = torch.empty((1, 1080, 1920, 3), device="cuda")
+    for _ in range(3):
+        net.denoise(x, o)
+    inf_ms = _events_ms(lambda: net.denoise(x, o), 20)
+    inf_flop = net.flops(1080, 1920)
+    fb = torch.rand((8, 256, 256, D.FEATURES), device="cuda")
+    tb = torch.rand((8, 256, 256, 3), device="cuda")
+    snap = net.get_params()
+    for _ in range(3):
+        net.train_step(fb, tb, 0.0, read_loss=False)
+    tr_ms = _events_ms(lambda: net.train_step(fb, tb, 0.0, read_loss=False), 20)
+    tr_flop = 3 * net.flops(256, 256, 8)
+    net.set_params(snap)
+
+    # ---- quality at equal time ------------------------------------------------------------
+    sc2 = S.denoiser_scene(20261210)
+    tr2 = R.PathTracer(sc2)
+    cam = S.random_cameras(20261210, 1, ratio=480 / 270)[0]
+    w, h = 480, 270
+    gt = torch.zeros((h, w, 3), device="cuda")
+    tr2.render(cam, 4096, 5, gt, seed=7, mode=1, fp64=True)
+    gt_np = gt.cpu().numpy()
+    plain, den = [], []
+    img = torch.zeros((h, w, 3), device="cuda")
+    aov = torch.zeros((h, w, 7), device="cuda")
+    for spp in (4, 16, 64, 256, 1024):
+        img.zero_()
+        tr2.render(cam, spp, 5, img, seed=100 + spp, mode=1)
+        plain.append({"spp": spp, "s": tr2.last_stats()["device_ms"] / 1e3,
+                      "rel_rmse": D.rel_rmse(img.cpu().numpy(), gt_np)})
+    for spp in (4, 16, 64):
+        img.zero_()
+        tr2.render(cam, spp, 5, img, seed=200 + spp, mode=1, aov=aov)
+        render_s = tr2.last_stats()["device_ms"] / 1e3
+        f = torch.cat([img, aov], -1).unsqueeze(0).contiguous()
+        out = torch.empty((1, h, w, 3), device="cuda")
+        net.denoise(f, out)
+        dn_ms = _events_ms(lambda: net.denoise(f, out), 5)
+        den.append({"spp": spp, "s": render_s + dn_ms / 1e3, "denoise_ms": round(dn_ms, 3),
+                    "rel_rmse": D.rel_rmse(out[0].cpu().numpy(), gt_np)})
+
+    def time_to(curve, thr):
+        """Seconds to reach rel-RMSE thr, interpolated log-log between measured points (None
+        when no measured point reaches it)."""
+        pts = sorted((p["s"], p["rel_rmse"]) for p in curve)
+        for (t0_, e0_), (t1_, e1_) in zip(pts, pts[1:]):
+            if e0_ > thr >= e1_:
+                a = (np.log(thr) - np.log(e0_)) / (np.log(e1_) - np.log(e0_))
+                return float(np.exp(np.log(t0_) + a * (np.log(t1_) - np.log(t0_))))
+        return pts[0][0] if pts[0][1] <= thr else None
+
+    levels = {}
+    for thr in (0.3, 0.2, 0.1, 0.05, 0.01):
+        tp, td = time_to(plain, thr), time_to(den, thr)
+        levels[str(thr)] = {"plain_s": tp and round(tp, 4), "denoised_s": td and round(td, 4),
+                            "speedup": round(tp / td, 1) if tp and td else None}
+    for p in plain + den:
+        p["s"] = round(p["s"], 4)
+        p["rel_rmse"] = round(p["rel_rmse"], 4)
+    inf_tflops = inf_flop / inf_ms / 1e9
+    out = {"workload": "5-level U-Net (32-128 channels, 3x3 conv, BF16 activations, FP32 accumulation); "
+                       "inference 1920x1080, training 8 x 256^2",
+           "value": round(inf_tflops, 1), "unit": "TFLOP/s (inference, 1920x1080)",
+           "inference_ms_1080p": round(inf_ms, 3), "inference_gflop": round(inf_flop / 1e9, 1),
+           "train_step_ms_8x256": round(tr_ms, 3), "train_tflops": round(tr_flop / tr_ms / 1e9, 1),
+           "roofline": {"bound": "tensor", "achieved": round(inf_tflops, 1), "peak": peak, "unit": "TFLOP/s",
+                        "frac": round(inf_tflops / peak, 4), "peak_kind": peak_kind, "traffic": None},
+           "training": {"pairs": int(feats.shape[0]), "input_spp": [4, 8, 16, 32, 64], "target_spp": 512,
+                        "steps": steps, "batch": "8 x 64^2 crops", "data_s": round(data_s, 2),
+                        "train_s": round(train_s, 2), "losses": [(s_, round(l_, 5)) for s_, l_ in losses]},
+           "quality": {"view": f"held-out scene, {w}x{h}, extended estimator, depth 5",
+                       "ground_truth": "4096 spp, double-precision accumulation", "plain": plain, "denoised": den,
+                       "time_to_rel_rmse": levels}}
+    return out
+
+
 def run_reference(args):
     """Reference arm: the reference's Raycaster algorithm (C restatement; the reference's own
     sources do not travel to this host) on all host threads, same workload and metric."""
@@ -350,6 +481,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-pt", action="store_true", help="skip the path-tracer lines")
+    ap.add_argument("--denoiser-only", action="store_true", help="only the denoiser measurement (one JSON line)")
+    ap.add_argument("--profile-dn", action="store_true",
+                    help="only two 1920x1080 denoiser inferences and one 8 x 256^2 training step (for ncu captures)")
     ap.add_argument("--profile-run", action="store_true",
                     help="only one closest-hit and one any-hit launch over the workload (for ncu captures)")
     ap.add_argument("--profile-pt", default=None, choices=list(PT_CONFIGS),
@@ -357,6 +491,29 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile_dn:
+        import torch
+
+        from rendu_gb300 import build as B
+        from rendu_gb300 import denoiser as D
+
+        B.build()
+        net = D.Denoiser(seed=1)
+        x = torch.rand((1, 1080, 1920, D.FEATURES), device="cuda")
+        o = torch.empty((1, 1080, 1920, 3), device="cuda")
+        net.denoise(x, o)
+        net.denoise(x, o)
+        fb = torch.rand((8, 256, 256, D.FEATURES), device="cuda")
+        net.train_step(fb, torch.rand((8, 256, 256, 3), device="cuda"), 1e-4, read_loss=False)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_dn": "2 x inference 1920x1080 + 1 training step 8 x 256^2"}))
+        return
+    if args.denoiser_only:
+        from rendu_gb300 import build as B
+
+        B.build()
+        print(json.dumps({"denoiser": run_denoiser(False)}), flush=True)
         return
     if args.profile_pt:
         import rendu_gb300 as R
@@ -485,6 +642,7 @@ def main():
         if not args.no_pt:
             out["pathtracer"] = {name: run_pathtracer(name, 3, not args.no_cpu) for name in PT_CONFIGS}
             out["batch"] = run_batch(not args.no_cpu)
+            out["denoiser"] = run_denoiser(not args.no_cpu)
         clk.__exit__(None, None, None)
         out["clocks"] = clk.summary()
         if not args.no_cpu:

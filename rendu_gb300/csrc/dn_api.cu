@@ -43,7 +43,8 @@ struct Conv {
     int cin0, cin1, cout;
     int relu;
     int out;
-    size_t woff, boff;
+    size_t woff, boff;        // FP32 weights and bias in the flat parameters
+    size_t wk_off, wkd_off;   // packed forward / data-gradient BF16 weights
 };
 
 struct Op {
@@ -58,6 +59,20 @@ constexpr int kInC = 16, kOutC = 16;
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// What a captured step depends on: the shape and every buffer address baked into it.
+struct GraphSig {
+    const void *p[10];
+    int B, H, W, Hp, Wp;
+};
+
+// One captured step: the first call with a new signature runs eagerly (and configures
+// the kernels), the second captures, later ones replay.
+struct GraphSlot {
+    cudaGraphExec_t exec = nullptr;
+    GraphSig sig{};
+    bool seen = false;
+};
+
 }  // namespace
 
 struct dn_net {
@@ -67,14 +82,15 @@ struct dn_net {
     std::vector<Conv> convs;
     std::vector<Op> ops;
     size_t nparams = 0;
-    LayerTable table{};
-    DevBuf params, grads, adam_m, adam_v, wb, wt, hyper;
+    PackTable table{};
+    DevBuf params, grads, adam_m, adam_v, wk, wkd, hyper;  // wk, wkd: packed BF16 weight copies
     float lr_dev = -1.0f;  // learning rate held in device memory
     // Shape-dependent buffers.
     int B = 0, Hp = 0, Wp = 0;
     bool train_ready = false;
-    DevBuf act, gact, gin, gbf, partial, feat, target, out, loss_partial;
+    DevBuf act, gact, gin, gbf, partial, feat, target, out, loss_partial, ups;
     std::vector<size_t> act_off, gact_off;
+    GraphSlot g_train, g_infer;
 
     bf16 *bf(int t) { return reinterpret_cast<bf16 *>(static_cast<char *>(act.ptr) + act_off[t]); }
     float *f(int t) { return reinterpret_cast<float *>(static_cast<char *>(act.ptr) + act_off[t]); }
@@ -132,20 +148,22 @@ void build_graph(dn_net *n) {
     }
     conv(cur, 0, -1, kOutC, 0, true);
     n->table.n = (int)n->convs.size();
+    uint64_t fo = 0, bo = 0;
     for (size_t i = 0; i < n->convs.size(); ++i) {
-        const Conv &c = n->convs[i];
-        n->table.l[i] = {(uint32_t)c.woff, (uint32_t)(c.cin0 + c.cin1), (uint32_t)c.cout};
+        Conv &c = n->convs[i];
+        c.wk_off = fo;
+        c.wkd_off = bo;
+        n->table.e[i] = {(uint32_t)c.woff, (uint32_t)c.cin0, (uint32_t)c.cin1, (uint32_t)c.cout, fo, bo};
+        fo += (uint64_t)c.cout * packed_k(c.cin0, c.cin1);
+        bo += (uint64_t)(c.cin0 + c.cin1) * packed_k(c.cout, 0);
     }
+    n->table.fwd_total = fo;
+    n->table.bwd_total = bo;
 }
 
-// BF16 forward and dgrad copies of every layer's weights from the FP32 master copy.
+// Packed BF16 forward and data-gradient copies of every layer's weights.
 int refresh_weights(dn_net *n, cudaStream_t st) {
-    for (const Conv &c : n->convs) {
-        const int r = convert_weights(n->params.as<float>() + c.woff, c.cin0 + c.cin1, c.cout,
-                                      n->wb.as<bf16>() + c.woff, n->wt.as<bf16>() + c.woff, st);
-        if (r != RT_OK) return r;
-    }
-    return RT_OK;
+    return pack_all(n->params.as<float>(), n->table, n->wk.as<bf16>(), n->wkd.as<bf16>(), st);
 }
 
 int reset_optimizer(dn_net *n, cudaStream_t st) {
@@ -200,7 +218,7 @@ int ensure_shape(dn_net *n, int B, int Hp, int Wp, bool train) {
     n->Wp = Wp;
     n->act_off.assign(n->tensors.size(), 0);
     n->gact_off.assign(n->tensors.size(), 0);
-    size_t a = 0, g = 0, max_el = 0, max_gin = 0, max_part = 0;
+    size_t a = 0, g = 0, max_el = 0, max_gin = 0, max_part = 0, max_ups = 0;
     for (size_t t = 0; t < n->tensors.size(); ++t) {
         const Tensor &T = n->tensors[t];
         const size_t el = (size_t)n->pixels(T.level) * T.ch;
@@ -214,9 +232,10 @@ int ensure_shape(dn_net *n, int B, int Hp, int Wp, bool train) {
         const long P = n->pixels(n->tensors[c.out].level);
         const int cin = c.cin0 + c.cin1;
         if (c.cin1 || c.up0) max_gin = std::max(max_gin, (size_t)P * cin);
+        if (c.up0) max_ups = std::max(max_ups, (size_t)P * c.cin0);
         max_part = std::max({max_part, wgrad_partial_floats(P, cin, c.cout), colsum_partial_floats(P, c.cout)});
     }
-    if (n->act.reserve(a) != RT_OK) return RT_ERR_OOM;
+    if (n->act.reserve(a) != RT_OK || n->ups.reserve(std::max<size_t>(max_ups, 8) * 2) != RT_OK) return RT_ERR_OOM;
     n->train_ready = false;
     if (train) {
         const long P0 = n->pixels(0);
@@ -244,9 +263,9 @@ int forward(dn_net *n, cudaStream_t st) {
             in.up0 = c.up0;
             in.p1 = c.src1 >= 0 ? n->bf(c.src1) : nullptr;
             in.c1 = c.cin1;
-            r = conv_forward(in, n->B, n->Hp >> o.level, n->Wp >> o.level, n->wb.as<bf16>() + c.woff,
-                             n->params.as<float>() + c.boff, c.cout, c.relu != 0, o.f32 ? nullptr : n->bf(c.out),
-                             o.f32 ? n->f(c.out) : nullptr, st);
+            r = conv_forward_umma(in, n->B, n->Hp >> o.level, n->Wp >> o.level, n->wk.as<bf16>() + c.wk_off,
+                                  n->params.as<float>() + c.boff, c.cout, c.relu != 0, o.f32 ? nullptr : n->bf(c.out),
+                                  o.f32 ? n->f(c.out) : nullptr, n->ups.as<bf16>(), st);
         }
         if (r != RT_OK) return r;
     }
@@ -287,7 +306,8 @@ int backward(dn_net *n, const float *target, cudaStream_t st) {
         gi.c0 = c.cout;
         const bool split = c.cin1 || c.up0;
         float *dst = split ? n->gin.as<float>() : n->g(c.src0);
-        r = conv_forward(gi, n->B, H, W, n->wt.as<bf16>() + c.woff, nullptr, c.cin0 + c.cin1, false, nullptr, dst, st);
+        r = conv_forward_umma(gi, n->B, H, W, n->wkd.as<bf16>() + c.wkd_off, nullptr, c.cin0 + c.cin1, false, nullptr,
+                              dst, nullptr, st);
         if (r == RT_OK && split)
             r = split_grad(dst, n->B, H, W, c.cin0, c.up0, c.cin1, n->g(c.src0), c.src1 >= 0 ? n->g(c.src1) : nullptr,
                            st);
@@ -297,48 +317,111 @@ int backward(dn_net *n, const float *target, cudaStream_t st) {
 
 bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
-int stage_in(DevBuf &buf, const float *host, size_t n, cudaStream_t st) {
-    if (buf.reserve(n * sizeof(float)) != RT_OK) return RT_ERR_OOM;
-    RT_CUDA_TRY(cudaMemcpyAsync(buf.ptr, host, n * sizeof(float), cudaMemcpyHostToDevice, st));
-    return RT_OK;
-}
 
-int backward_call(dn_net *n, const float *features, const float *target, uint32_t width, uint32_t height,
-                  uint32_t batch, cudaStream_t st, bool dev) {
+int check_train_shape(const float *features, const float *target, uint32_t width, uint32_t height, uint32_t batch) {
     if (!features || !target || width == 0 || height == 0 || batch == 0) return arg_error("empty denoiser batch");
     if (width % 16 || height % 16) return arg_error("training crops must be multiples of 16 pixels wide and high");
     if ((uint64_t)width * height * batch >= (1ull << 31)) return arg_error("denoiser batch too large");
-    int r = ensure_shape(n, (int)batch, (int)height, (int)width, true);
-    if (r != RT_OK) return r;
-    const size_t np = (size_t)batch * height * width;
-    const float *f = features, *t = target;
-    if (!dev) {
-        if ((r = stage_in(n->feat, features, np * DN_FEATURES, st)) != RT_OK) return r;
-        if ((r = stage_in(n->target, target, np * 3, st)) != RT_OK) return r;
-        f = n->feat.as<float>();
-        t = n->target.as<float>();
+    return RT_OK;
+}
+
+// Copy a caller's array (host, or device with dev) into an internal buffer.
+int stage(DevBuf &buf, const float *src, size_t n, bool dev, cudaStream_t st) {
+    if (buf.reserve(n * sizeof(float)) != RT_OK) return RT_ERR_OOM;
+    RT_CUDA_TRY(cudaMemcpyAsync(buf.ptr, src, n * sizeof(float), dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                st));
+    return RT_OK;
+}
+
+int set_lr(dn_net *n, float lr, cudaStream_t st) {
+    if (!(lr >= 0.0f) || !std::isfinite(lr)) return arg_error("learning rate must be finite and >= 0");
+    if (lr != n->lr_dev) {
+        const int r = set_learning_rate(n->hyp(), lr, st);
+        if (r != RT_OK) return r;
+        n->lr_dev = lr;
     }
-    r = prepare(f, (int)batch, (int)height, (int)width, (int)height, (int)width, n->bf(0), st);
+    return RT_OK;
+}
+
+int adam_launch(dn_net *n, cudaStream_t st) {
+    const int r = adam(n->params.as<float>(), n->grads.as<float>(), n->adam_m.as<float>(), n->adam_v.as<float>(),
+                       n->nparams, n->hyp(), st);
+    return r == RT_OK ? refresh_weights(n, st) : r;
+}
+
+// Forward + loss + backward over the staged batch in n->feat / n->target.
+int train_body(dn_net *n, bool with_adam, cudaStream_t st) {
+    int r = prepare(n->feat.as<float>(), n->B, n->Hp, n->Wp, n->Hp, n->Wp, n->bf(0), st);
     if (r == RT_OK) r = forward(n, st);
-    if (r == RT_OK) r = backward(n, t, st);
+    if (r == RT_OK) r = backward(n, n->target.as<float>(), st);
+    if (r == RT_OK && with_adam) r = adam_launch(n, st);
     return r;
 }
 
-int adam_call(dn_net *n, float lr, cudaStream_t st) {
-    if (!(lr >= 0.0f) || !std::isfinite(lr)) return arg_error("learning rate must be finite and >= 0");
-    if (lr != n->lr_dev) {
-        RT_CUDA_TRY(cudaMemcpyAsync(&n->hyp()->lr, &lr, sizeof(float), cudaMemcpyHostToDevice, st));
-        n->lr_dev = lr;
+GraphSig signature(dn_net *n, int H, int W) {
+    GraphSig g;
+    std::memset(&g, 0, sizeof(g));
+    const DevBuf *bufs[10] = {&n->act, &n->gact, &n->gin, &n->gbf, &n->partial, &n->feat, &n->target, &n->out,
+                              &n->loss_partial, &n->ups};
+    for (int i = 0; i < 10; ++i) g.p[i] = bufs[i]->ptr;
+    g.B = n->B;
+    g.H = H;
+    g.W = W;
+    g.Hp = n->Hp;
+    g.Wp = n->Wp;
+    return g;
+}
+
+template <class Body>
+int run_graph(dn_net *n, GraphSlot &slot, const GraphSig &sig, Body body, cudaStream_t st) {
+    if (!slot.seen || std::memcmp(&slot.sig, &sig, sizeof(GraphSig)) != 0) {
+        if (slot.exec) cudaGraphExecDestroy(slot.exec);
+        slot.exec = nullptr;
+        slot.sig = sig;
+        slot.seen = true;
+        return body(st);
     }
-    return adam(n->params.as<float>(), n->grads.as<float>(), n->adam_m.as<float>(), n->adam_v.as<float>(), n->nparams,
-                n->table, n->hyp(), n->wb.as<bf16>(), n->wt.as<bf16>(), st);
+    if (!slot.exec) {
+        RT_CUDA_TRY(cudaStreamBeginCapture(n->stream, cudaStreamCaptureModeThreadLocal));
+        const int r = body(n->stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(n->stream, &g);
+        cudaError_t ei = cudaSuccess;
+        if (r == RT_OK && e == cudaSuccess) ei = cudaGraphInstantiate(&slot.exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (r != RT_OK || e != cudaSuccess || ei != cudaSuccess) {
+            slot.exec = nullptr;
+            slot.seen = false;
+            cudaGetLastError();
+            if (r != RT_OK) return r;
+            set_error(std::string("denoiser graph capture failed: ") + cudaGetErrorString(e != cudaSuccess ? e : ei));
+            return RT_ERR_CUDA;
+        }
+    }
+    RT_CUDA_TRY(cudaGraphLaunch(slot.exec, st));
+    return RT_OK;
+}
+
+int stage_batch(dn_net *n, const float *features, const float *target, uint32_t width, uint32_t height,
+                uint32_t batch, bool dev, cudaStream_t st) {
+    int r = check_train_shape(features, target, width, height, batch);
+    if (r == RT_OK) r = ensure_shape(n, (int)batch, (int)height, (int)width, true);
+    const size_t np = (size_t)batch * height * width;
+    if (r == RT_OK) r = stage(n->feat, features, np * DN_FEATURES, dev, st);
+    if (r == RT_OK) r = stage(n->target, target, np * 3, dev, st);
+    return r;
 }
 
 int read_loss(dn_net *n, float *loss, cudaStream_t st) {
     if (!loss) return RT_OK;
     RT_CUDA_TRY(cudaMemcpyAsync(loss, &n->hyp()->loss, sizeof(float), cudaMemcpyDeviceToHost, st));
     RT_CUDA_TRY(cudaStreamSynchronize(st));
-    return RT_OK;
+    return umma_status(true);
+}
+
+int finish_host_call(cudaStream_t st) {
+    RT_CUDA_TRY(cudaStreamSynchronize(st));
+    return umma_status(true);
 }
 
 }  // namespace
@@ -366,8 +449,8 @@ RT_API int dn_create(dn_net **out, int device) {
     const size_t pb = n->nparams * sizeof(float);
     if (r == RT_OK &&
         (n->params.reserve(pb) != RT_OK || n->grads.reserve(pb) != RT_OK || n->adam_m.reserve(pb) != RT_OK ||
-         n->adam_v.reserve(pb) != RT_OK || n->wb.reserve(n->nparams * 2) != RT_OK ||
-         n->wt.reserve(n->nparams * 2) != RT_OK || n->hyper.reserve(sizeof(Hyper)) != RT_OK))
+         n->adam_v.reserve(pb) != RT_OK || n->wk.reserve(n->table.fwd_total * 2) != RT_OK ||
+         n->wkd.reserve(n->table.bwd_total * 2) != RT_OK || n->hyper.reserve(sizeof(Hyper)) != RT_OK))
         r = RT_ERR_OOM;
     if (r == RT_OK) {
         const std::vector<float> h = he_init(n, 0);
@@ -386,8 +469,10 @@ RT_API int dn_destroy(dn_net *n) {
     if (!n) return RT_OK;
     DeviceGuard guard(n->device);
     if (n->stream) cudaStreamSynchronize(n->stream);
-    for (DevBuf *b : {&n->params, &n->grads, &n->adam_m, &n->adam_v, &n->wb, &n->wt, &n->hyper, &n->act, &n->gact,
-                      &n->gin, &n->gbf, &n->partial, &n->feat, &n->target, &n->out, &n->loss_partial})
+    for (GraphSlot *g : {&n->g_train, &n->g_infer})
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+    for (DevBuf *b : {&n->params, &n->grads, &n->adam_m, &n->adam_v, &n->wk, &n->wkd, &n->hyper, &n->act, &n->gact,
+                      &n->gin, &n->gbf, &n->partial, &n->feat, &n->target, &n->out, &n->loss_partial, &n->ups})
         b->release();
     if (n->stream) cudaStreamDestroy(n->stream);
     delete n;
@@ -433,7 +518,7 @@ RT_API int dn_get_params(dn_net *n, float *out, size_t count) {
     DeviceGuard guard(n->device);
     RT_CUDA_TRY(cudaDeviceSynchronize());
     RT_CUDA_TRY(cudaMemcpy(out, n->params.ptr, count * sizeof(float), cudaMemcpyDeviceToHost));
-    return RT_OK;
+    return umma_status(true);
 }
 
 RT_API int dn_set_params(dn_net *n, const float *in, size_t count) {
@@ -448,7 +533,7 @@ RT_API int dn_get_grads(dn_net *n, float *out, size_t count) {
     DeviceGuard guard(n->device);
     RT_CUDA_TRY(cudaDeviceSynchronize());
     RT_CUDA_TRY(cudaMemcpy(out, n->grads.ptr, count * sizeof(float), cudaMemcpyDeviceToHost));
-    return RT_OK;
+    return umma_status(true);
 }
 
 RT_API int dn_denoise(dn_net *n, const float *features, uint32_t width, uint32_t height, uint32_t batch, float *out,
@@ -461,26 +546,22 @@ RT_API int dn_denoise(dn_net *n, const float *features, uint32_t width, uint32_t
     const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
     cudaStream_t st = dev ? static_cast<cudaStream_t>(stream) : n->stream;
     int r = ensure_shape(n, (int)batch, (int)Hp, (int)Wp, false);
-    if (r != RT_OK) return r;
     const size_t np = (size_t)batch * height * width;
-    const float *f = features;
-    float *o = out;
-    if (!dev) {
-        if ((r = stage_in(n->feat, features, np * DN_FEATURES, st)) != RT_OK) return r;
-        if (n->out.reserve(np * 3 * sizeof(float)) != RT_OK) return RT_ERR_OOM;
-        f = n->feat.as<float>();
-        o = n->out.as<float>();
-    }
-    r = prepare(f, (int)batch, (int)height, (int)width, (int)Hp, (int)Wp, n->bf(0), st);
-    if (r == RT_OK) r = forward(n, st);
-    if (r == RT_OK)
-        r = finish(n->bf(0), n->f(n->convs.back().out), (int)batch, (int)height, (int)width, (int)Hp, (int)Wp, o, st);
+    if (r == RT_OK) r = stage(n->feat, features, np * DN_FEATURES, dev, st);
+    if (r == RT_OK && n->out.reserve(np * 3 * sizeof(float)) != RT_OK) r = RT_ERR_OOM;
     if (r != RT_OK) return r;
-    if (!dev) {
-        RT_CUDA_TRY(cudaMemcpyAsync(out, o, np * 3 * sizeof(float), cudaMemcpyDeviceToHost, st));
-        RT_CUDA_TRY(cudaStreamSynchronize(st));
-    }
-    return RT_OK;
+    const int B = (int)batch, H = (int)height, W = (int)width;
+    auto body = [&](cudaStream_t s) {
+        int q = prepare(n->feat.as<float>(), B, H, W, (int)Hp, (int)Wp, n->bf(0), s);
+        if (q == RT_OK) q = forward(n, s);
+        if (q == RT_OK) q = finish(n->bf(0), n->f(n->convs.back().out), B, H, W, (int)Hp, (int)Wp, n->out.as<float>(), s);
+        return q;
+    };
+    r = run_graph(n, n->g_infer, signature(n, H, W), body, st);
+    if (r != RT_OK) return r;
+    RT_CUDA_TRY(cudaMemcpyAsync(out, n->out.ptr, np * 3 * sizeof(float),
+                                dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+    return dev ? RT_OK : finish_host_call(st);
 }
 
 RT_API int dn_backward(dn_net *n, const float *features, const float *target, uint32_t width, uint32_t height,
@@ -489,9 +570,10 @@ RT_API int dn_backward(dn_net *n, const float *features, const float *target, ui
     DeviceGuard guard(n->device);
     const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
     cudaStream_t st = dev ? static_cast<cudaStream_t>(stream) : n->stream;
-    int r = backward_call(n, features, target, width, height, batch, st, dev);
+    int r = stage_batch(n, features, target, width, height, batch, dev, st);
+    if (r == RT_OK) r = train_body(n, false, st);
     if (r == RT_OK) r = read_loss(n, loss, st);
-    if (r == RT_OK && !dev) RT_CUDA_TRY(cudaStreamSynchronize(st));
+    if (r == RT_OK && !dev) r = finish_host_call(st);
     return r;
 }
 
@@ -499,7 +581,8 @@ RT_API int dn_adam_step(dn_net *n, float lr, void *stream) {
     if (!n) return arg_error("null network");
     DeviceGuard guard(n->device);
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : n->stream;
-    int r = adam_call(n, lr, st);
+    int r = set_lr(n, lr, st);
+    if (r == RT_OK) r = adam_launch(n, st);
     if (r == RT_OK && !stream) RT_CUDA_TRY(cudaStreamSynchronize(st));
     return r;
 }
@@ -510,10 +593,13 @@ RT_API int dn_train_step(dn_net *n, const float *features, const float *target, 
     DeviceGuard guard(n->device);
     const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
     cudaStream_t st = dev ? static_cast<cudaStream_t>(stream) : n->stream;
-    int r = backward_call(n, features, target, width, height, batch, st, dev);
-    if (r == RT_OK) r = adam_call(n, lr, st);
+    int r = set_lr(n, lr, st);
+    if (r == RT_OK) r = stage_batch(n, features, target, width, height, batch, dev, st);
+    if (r == RT_OK)
+        r = run_graph(n, n->g_train, signature(n, (int)height, (int)width),
+                      [&](cudaStream_t s) { return train_body(n, true, s); }, st);
     if (r == RT_OK) r = read_loss(n, loss, st);
-    if (r == RT_OK && !dev) RT_CUDA_TRY(cudaStreamSynchronize(st));
+    if (r == RT_OK && !dev) r = finish_host_call(st);
     return r;
 }
 
@@ -526,15 +612,31 @@ RT_API int dn_conv3x3(const void *x0, uint32_t c0, int32_t up0, const void *x1, 
     if (up0 && (height % 2 || width % 2)) return arg_error("an upsampled input needs an even output size");
     if (!aligned16(x0) || (x1 && !aligned16(x1)) || !aligned16(weights))
         return arg_error("inputs and weights must be 16-byte aligned");
-    ConvIn in;
-    in.p0 = static_cast<const bf16 *>(x0);
-    in.c0 = (int)c0;
-    in.up0 = up0 ? 1 : 0;
-    in.p1 = static_cast<const bf16 *>(x1);
-    in.c1 = (int)c1;
-    return conv_forward(in, (int)batch, (int)height, (int)width, static_cast<const bf16 *>(weights), bias, (int)cout,
-                        relu != 0, out_fp32 ? nullptr : static_cast<bf16 *>(out),
-                        out_fp32 ? static_cast<float *>(out) : nullptr, static_cast<cudaStream_t>(stream));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    void *wk = nullptr, *ups = nullptr;
+    RT_CUDA_TRY(cudaMallocAsync(&wk, (size_t)cout * packed_k((int)c0, (int)c1) * sizeof(bf16), st));
+    if (up0 && cudaMallocAsync(&ups, (size_t)batch * height * width * c0 * sizeof(bf16), st) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFreeAsync(wk, st);
+        set_error("scratch allocation failed");
+        return RT_ERR_OOM;
+    }
+    int r = pack_weights_bf16(static_cast<const bf16 *>(weights), (int)c0, (int)c1, (int)cout, static_cast<bf16 *>(wk),
+                              st);
+    if (r == RT_OK) {
+        ConvIn in;
+        in.p0 = static_cast<const bf16 *>(x0);
+        in.c0 = (int)c0;
+        in.up0 = up0 ? 1 : 0;
+        in.p1 = static_cast<const bf16 *>(x1);
+        in.c1 = (int)c1;
+        r = conv_forward_umma(in, (int)batch, (int)height, (int)width, static_cast<const bf16 *>(wk), bias, (int)cout,
+                              relu != 0, out_fp32 ? nullptr : static_cast<bf16 *>(out),
+                              out_fp32 ? static_cast<float *>(out) : nullptr, static_cast<bf16 *>(ups), st);
+    }
+    cudaFreeAsync(wk, st);
+    if (ups) cudaFreeAsync(ups, st);
+    return r;
 }
 
 RT_API int dn_conv3x3_backward(const void *x0, uint32_t c0, int32_t up0, const void *x1, uint32_t c1, uint32_t batch,
@@ -550,17 +652,17 @@ RT_API int dn_conv3x3_backward(const void *x0, uint32_t c0, int32_t up0, const v
     const long P = (long)batch * height * width;
     int r = RT_OK;
     if (dx) {
-        void *wt = nullptr;
-        RT_CUDA_TRY(cudaMallocAsync(&wt, (size_t)9 * cin * cout * sizeof(bf16), st));
-        r = convert_weights(weights, cin, (int)cout, nullptr, static_cast<bf16 *>(wt), st);
+        void *wkd = nullptr;
+        RT_CUDA_TRY(cudaMallocAsync(&wkd, (size_t)cin * packed_k((int)cout, 0) * sizeof(bf16), st));
+        r = pack_weights(weights, (int)c0, (int)c1, (int)cout, nullptr, static_cast<bf16 *>(wkd), st);
         if (r == RT_OK) {
             ConvIn gi;
             gi.p0 = static_cast<const bf16 *>(gy);
             gi.c0 = (int)cout;
-            r = conv_forward(gi, (int)batch, (int)height, (int)width, static_cast<const bf16 *>(wt), nullptr, cin, false,
-                             nullptr, dx, st);
+            r = conv_forward_umma(gi, (int)batch, (int)height, (int)width, static_cast<const bf16 *>(wkd), nullptr, cin,
+                                  false, nullptr, dx, nullptr, st);
         }
-        cudaFreeAsync(wt, st);
+        cudaFreeAsync(wkd, st);
         if (r != RT_OK) return r;
     }
     if (dw) {

@@ -1,7 +1,8 @@
-// Denoiser kernels. The 3x3 convolutions are implicit GEMMs on the BF16 tensor cores
-// (mma.sync.m16n8k16, FP32 accumulation) fed by a 3-stage cp.async pipeline with ldmatrix
-// fragment loads; the rest are the element-wise pieces of a U-Net's forward and backward
-// passes (pooling, gradient routing, loss, Adam). Activations are NHWC BF16.
+// Denoiser kernels besides the tensor-core forward convolution (dn_umma.cu): the weight
+// gradient as an implicit GEMM on the BF16 tensor cores (mma.sync.m16n8k16, FP32
+// accumulation) fed by a 3-stage cp.async pipeline with ldmatrix fragment loads, and the
+// element-wise pieces of a U-Net's forward and backward passes (pooling, gradient routing,
+// loss, Adam). Activations are NHWC BF16.
 //
 // Convolution input: up to two tensors concatenated along channels -- the first optionally
 // read at half resolution (nearest-neighbour 2x upsampling folded into the gather), the
@@ -110,120 +111,6 @@ struct Tile {
     static constexpr int LDB = BN + 8;
     static_assert(WM % 16 == 0 && WN % 16 == 0, "warp tile must be a multiple of 16x16");
 };
-
-// ---- forward / dgrad convolution -----------------------------------------------------------------
-template <int BN, int WARPS_M, int WARPS_N>
-__global__ void __launch_bounds__(32 * WARPS_M *WARPS_N)
-    k_conv(ConvIn in, int B, int H, int W, const bf16 *__restrict__ w, int Cout, const float *__restrict__ bias,
-           int relu, bf16 *__restrict__ out_bf, float *__restrict__ out_f) {
-    using T = Tile<BN, WARPS_M, WARPS_N>;
-    constexpr int NT = T::NT, LDA = BK + 8, LDB = T::LDB;
-    constexpr int A_ITER = BM * BK / 8 / NT;
-    constexpr int B_CHUNKS = BK * BN / 8;
-    extern __shared__ __align__(128) unsigned char smem[];
-    bf16 *sA = reinterpret_cast<bf16 *>(smem);
-    bf16 *sB = sA + STAGES * BM * LDA;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = warp / WARPS_N, wn = warp % WARPS_N;
-    const long HW = (long)H * W, P = (long)B * HW;
-    const long m0 = (long)blockIdx.x * BM;
-    const int n0 = blockIdx.y * BN;
-    const int Cin = in.c0 + in.c1, K = 9 * Cin, KT = (K + BK - 1) / BK;
-
-    // Gather state: this thread copies channel group g (8 channels) of rows tid/4 + i NT/4.
-    const int g = tid & 3;
-    int an[A_ITER], ay[A_ITER], ax[A_ITER];
-#pragma unroll
-    for (int i = 0; i < A_ITER; ++i) {
-        const long p = m0 + (tid >> 2) + i * (NT / 4);
-        if (p < P) {
-            an[i] = (int)(p / HW);
-            const long r = p - (long)an[i] * HW;
-            ay[i] = (int)(r / W);
-            ax[i] = (int)(r - (long)ay[i] * W);
-        } else {
-            an[i] = 0;
-            ay[i] = -(1 << 28);  // never inside the image
-            ax[i] = 0;
-        }
-    }
-    int tap = 0, ci = g * 8;  // k = tap Cin + ci of this thread's group at the next load
-    while (ci >= Cin) ci -= Cin, ++tap;
-
-    auto load_stage = [&](int stage, int kc) {
-        bf16 *a = sA + stage * BM * LDA;
-        const bool kvalid = kc + g * 8 < K;
-        const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-#pragma unroll
-        for (int i = 0; i < A_ITER; ++i) {
-            const int row = (tid >> 2) + i * (NT / 4);
-            const int yy = ay[i] + dy, xx = ax[i] + dx;
-            const bool v = kvalid && yy >= 0 && yy < H && xx >= 0 && xx < W;
-            const bf16 *src = v ? in_addr(in, an[i], yy, xx, H, W, ci) : in.p0;
-            cp_async16(a + row * LDA + g * 8, src, v);
-        }
-        ci += BK;
-        while (ci >= Cin) ci -= Cin, ++tap;
-        bf16 *b = sB + stage * BK * LDB;
-        for (int q = tid; q < B_CHUNKS; q += NT) {
-            const int kr = q / (BN / 8), c8 = (q % (BN / 8)) * 8;
-            const int k = kc + kr, co = n0 + c8;
-            const bool v = k < K && co < Cout;
-            cp_async16(b + kr * LDB + c8, v ? w + (size_t)k * Cout + co : w, v);
-        }
-    };
-
-    float acc[T::MI][T::NI][4];
-#pragma unroll
-    for (int mi = 0; mi < T::MI; ++mi)
-#pragma unroll
-        for (int ni = 0; ni < T::NI; ++ni)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) acc[mi][ni][e] = 0.0f;
-
-#pragma unroll
-    for (int s = 0; s < STAGES - 1; ++s) {
-        if (s < KT) load_stage(s, s * BK);
-        cp_commit();
-    }
-    for (int kt = 0; kt < KT; ++kt) {
-        cp_wait<STAGES - 2>();
-        __syncthreads();
-        const int nk = kt + STAGES - 1;
-        if (nk < KT) load_stage(nk % STAGES, nk * BK);
-        cp_commit();
-        const int st = kt % STAGES;
-        warp_mma<T::MI, T::NI, false, LDA, LDB>(acc, sA + st * BM * LDA, sB + st * BK * LDB, wm * T::WM,
-                                                 wn * T::WN, lane);
-    }
-    cp_wait<0>();
-
-    const int gq = lane >> 2, tq = lane & 3;
-#pragma unroll
-    for (int mi = 0; mi < T::MI; ++mi)
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const long p = m0 + wm * T::WM + mi * 16 + gq + h * 8;
-            if (p >= P) continue;
-#pragma unroll
-            for (int ni = 0; ni < T::NI; ++ni) {
-                const int co = n0 + wn * T::WN + ni * 8 + tq * 2;
-                if (co >= Cout) continue;
-                float v0 = acc[mi][ni][2 * h], v1 = acc[mi][ni][2 * h + 1];
-                if (bias) {
-                    v0 += bias[co];
-                    v1 += bias[co + 1];
-                }
-                if (relu) {
-                    v0 = fmaxf(v0, 0.0f);
-                    v1 = fmaxf(v1, 0.0f);
-                }
-                if (out_bf)
-                    *reinterpret_cast<__nv_bfloat162 *>(out_bf + p * Cout + co) = __floats2bfloat162_rn(v0, v1);
-                if (out_f) *reinterpret_cast<float2 *>(out_f + p * Cout + co) = make_float2(v0, v1);
-            }
-        }
-}
 
 // ---- weight gradient -------------------------------------------------------------------------------
 template <int BN, int WARPS_M, int WARPS_N>
@@ -356,21 +243,6 @@ __global__ void k_colsum(const float *__restrict__ g, long P, int C, long chunk,
         float t = 0.0f;
         for (int k = 0; k < R; ++k) t += red[k * C + threadIdx.x];
         partial[(size_t)blockIdx.x * C + threadIdx.x] = t;
-    }
-}
-
-__global__ void k_convert(const float *__restrict__ w, int Cin, int Cout, bf16 *__restrict__ wb,
-                          bf16 *__restrict__ wt) {
-    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    const size_t n = (size_t)9 * Cin * Cout;
-    if (i >= n) return;
-    const bf16 v = __float2bfloat16_rn(w[i]);
-    if (wb) wb[i] = v;
-    if (wt) {
-        const int tap = (int)(i / ((size_t)Cin * Cout));
-        const int r = (int)(i % ((size_t)Cin * Cout));
-        const int ci = r / Cout, co = r % Cout;
-        wt[((size_t)(8 - tap) * Cout + co) * Cin + ci] = v;
     }
 }
 
@@ -548,6 +420,8 @@ __global__ void k_loss_total(const float *__restrict__ partial, int n, float sca
     if (threadIdx.x == 0) h->loss = red[0] * scale;
 }
 
+__global__ void k_set_lr(Hyper *h, float lr) { h->lr = lr; }
+
 __global__ void k_adam_step(Hyper *h) {
     const int s = h->step + 1;
     h->step = s;
@@ -555,11 +429,9 @@ __global__ void k_adam_step(Hyper *h) {
     h->c2 = 1.0f - powf(h->b2, (float)s);
 }
 
-// Adam (Kingma & Ba 2015) on the FP32 master parameters; refreshes the BF16 forward and
-// dgrad copies of each updated weight.
+// Adam (Kingma & Ba 2015) on the FP32 master parameters.
 __global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float *__restrict__ m,
-                       float *__restrict__ v, size_t n, LayerTable tab, const Hyper *__restrict__ h,
-                       bf16 *__restrict__ wb, bf16 *__restrict__ wt) {
+                       float *__restrict__ v, size_t n, const Hyper *__restrict__ h) {
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float gi = g[i];
@@ -567,22 +439,7 @@ __global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float
     const float vi = h->b2 * v[i] + (1.0f - h->b2) * gi * gi;
     m[i] = mi;
     v[i] = vi;
-    const float wi = w[i] - h->lr * (mi / h->c1) / (sqrtf(vi / h->c2) + h->eps);
-    w[i] = wi;
-    for (int l = 0; l < tab.n; ++l) {
-        const LayerW L = tab.l[l];
-        const size_t nw = (size_t)9 * L.cin * L.cout;
-        if (i >= L.woff && i < L.woff + nw) {
-            const size_t j = i - L.woff;
-            const bf16 b = __float2bfloat16_rn(wi);
-            wb[i] = b;
-            const int tap = (int)(j / ((size_t)L.cin * L.cout));
-            const int r = (int)(j % ((size_t)L.cin * L.cout));
-            const int ci = r / L.cout, co = r % L.cout;
-            wt[L.woff + ((size_t)(8 - tap) * L.cout + co) * L.cin + ci] = b;
-            break;
-        }
-    }
+    w[i] = w[i] - h->lr * (mi / h->c1) / (sqrtf(vi / h->c2) + h->eps);
 }
 
 inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
@@ -602,30 +459,8 @@ int pick_bn(int N) {
 }
 
 template <int BN>
-constexpr size_t conv_smem() {
-    return (size_t)STAGES * (BM * (BK + 8) + BK * (BN + 8)) * sizeof(bf16);
-}
-template <int BN>
 constexpr size_t wgrad_smem() {
     return (size_t)STAGES * (BK * (BM + 8) + BK * (BN + 8)) * sizeof(bf16);
-}
-
-template <int BN, int WARPS_M, int WARPS_N>
-int launch_conv(const ConvIn &in, int B, int H, int W, const bf16 *w, int Cout, const float *bias, bool relu,
-                bf16 *out_bf, float *out_f, cudaStream_t st) {
-    constexpr size_t smem = conv_smem<BN>();
-    static bool attr = false;
-    if (!attr) {
-        RT_CUDA_TRY(cudaFuncSetAttribute(k_conv<BN, WARPS_M, WARPS_N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem));
-        attr = true;
-    }
-    const long P = (long)B * H * W;
-    const dim3 grid((unsigned)((P + BM - 1) / BM), (unsigned)((Cout + BN - 1) / BN));
-    k_conv<BN, WARPS_M, WARPS_N><<<grid, 32 * WARPS_M * WARPS_N, smem, st>>>(in, B, H, W, w, Cout, bias, relu ? 1 : 0,
-                                                                               out_bf, out_f);
-    RT_CUDA_TRY(cudaGetLastError());
-    return RT_OK;
 }
 
 struct WgradPlan {
@@ -671,18 +506,6 @@ constexpr long kColsumRows = 1024;
 }  // namespace
 
 // ---- launchers -------------------------------------------------------------------------------
-int conv_forward(const ConvIn &in, int B, int H, int W, const bf16 *w, const float *bias, int Cout, bool relu,
-                 bf16 *out_bf, float *out_f, cudaStream_t st) {
-    switch (pick_bn(Cout)) {
-        case 16: return launch_conv<16, 4, 1>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
-        case 32: return launch_conv<32, 4, 1>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
-        case 48: return launch_conv<48, 4, 1>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
-        case 64: return launch_conv<64, 2, 2>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
-        case 96: return launch_conv<96, 4, 2>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
-        default: return launch_conv<128, 4, 2>(in, B, H, W, w, Cout, bias, relu, out_bf, out_f, st);
-    }
-}
-
 size_t wgrad_partial_floats(long P, int Cin, int Cout) {
     const WgradPlan pl = wgrad_plan(P, Cin, Cout);
     return (size_t)pl.chunks * 9 * Cin * Cout;
@@ -715,12 +538,6 @@ int colsum(const float *g, long P, int C, float *partial, float *db, cudaStream_
     const int chunks = (int)((P + kColsumRows - 1) / kColsumRows);
     k_colsum<<<chunks, 256, 0, st>>>(g, P, C, kColsumRows, partial);
     k_reduce_chunks<<<blocks(C), 256, 0, st>>>(partial, chunks, (size_t)C, db);
-    RT_CUDA_TRY(cudaGetLastError());
-    return RT_OK;
-}
-
-int convert_weights(const float *w, int Cin, int Cout, bf16 *wb, bf16 *wt, cudaStream_t st) {
-    k_convert<<<blocks((size_t)9 * Cin * Cout), 256, 0, st>>>(w, Cin, Cout, wb, wt);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
@@ -770,10 +587,15 @@ int l1_loss(const bf16 *x, const float *y, const float *target, long P, float *g
     return RT_OK;
 }
 
-int adam(float *params, const float *grads, float *m, float *v, size_t n, const LayerTable &tab, Hyper *hyper,
-         bf16 *wb, bf16 *wt, cudaStream_t st) {
+int set_learning_rate(Hyper *hyper, float lr, cudaStream_t st) {
+    k_set_lr<<<1, 1, 0, st>>>(hyper, lr);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int adam(float *params, const float *grads, float *m, float *v, size_t n, Hyper *hyper, cudaStream_t st) {
     k_adam_step<<<1, 1, 0, st>>>(hyper);
-    k_adam<<<blocks(n), 256, 0, st>>>(params, grads, m, v, n, tab, hyper, wb, wt);
+    k_adam<<<blocks(n), 256, 0, st>>>(params, grads, m, v, n, hyper);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

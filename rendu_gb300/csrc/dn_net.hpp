@@ -26,14 +26,18 @@ struct ConvIn {
     int c1 = 0;
 };
 
-// Per-layer weight table entry for the fused Adam update (offsets into the flat buffers).
-struct LayerW {
-    uint32_t woff, cin, cout;
-};
+// Per-layer entry of the weight-packing table: FP32 parameters at woff, packed forward
+// weights at fwd_off (Cout x packed_k(c0, c1)), packed data-gradient weights at bwd_off
+// ((c0 + c1) x packed_k(Cout, 0)).
 constexpr int kMaxLayers = 24;
-struct LayerTable {
-    LayerW l[kMaxLayers];
+struct PackEntry {
+    uint32_t woff, c0, c1, cout;
+    uint64_t fwd_off, bwd_off;
+};
+struct PackTable {
+    PackEntry e[kMaxLayers];
     int n;
+    uint64_t fwd_total, bwd_total;
 };
 
 // Hyper-parameters in device memory, so that a captured update can be replayed.
@@ -45,9 +49,22 @@ struct Hyper {
 };
 
 // ---- launchers (asynchronous on st; RT_OK or RT_ERR_CUDA) -------------------------------------
-// out[p, co] = act(bias[co] + sum_{tap, ci} in[p + off(tap), ci] * w[tap][ci][co]); K = 9 (c0 + c1).
-int conv_forward(const ConvIn &in, int B, int H, int W, const bf16 *w, const float *bias, int Cout, bool relu,
-                 bf16 *out_bf, float *out_f, cudaStream_t st);
+// Length of a packed weight row: 9 taps x (64-channel chunks of input 0 + of input 1) x 64.
+size_t packed_k(int c0, int c1);
+// Tensor-core convolution (dn_umma.cu): out[p, co] = act(bias[co] + sum_{tap, ci}
+// in[p + off(tap), ci] w[tap][ci][co]) with the weights packed by pack_weights; with the
+// data-gradient packing it computes a layer's input gradient. An upsampled input 0 is
+// first expanded into `ups` (B x H x W x c0 BF16). Cout a multiple of 8.
+int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, const float *bias, int Cout, bool relu,
+                      bf16 *out_bf, float *out_f, bf16 *ups, cudaStream_t st);
+// w FP32 [tap][c0 + c1][Cout] -> wpk [Cout][packed_k(c0, c1)] (forward) and
+// wpkd [c0 + c1][packed_k(Cout, 0)] (data gradient, taps mirrored); either may be null.
+int pack_weights(const float *w, int c0, int c1, int Cout, bf16 *wpk, bf16 *wpkd, cudaStream_t st);
+int pack_weights_bf16(const bf16 *w, int c0, int c1, int Cout, bf16 *wpk, cudaStream_t st);
+// Both packings of every layer in the table, from the flat FP32 parameters.
+int pack_all(const float *params, const PackTable &tab, bf16 *wk, bf16 *wkd, cudaStream_t st);
+// RT_ERR_TIMEOUT if a tensor-core convolution's bounded wait gave up (synchronous).
+int umma_status(bool clear);
 // dw[tap][ci][co] = sum_p in[p + off(tap), ci] * g[p, co]; partial holds wgrad_partial_floats().
 int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, float *partial, float *dw,
                cudaStream_t st);
@@ -55,8 +72,6 @@ size_t wgrad_partial_floats(long P, int Cin, int Cout);
 // db[c] = sum_p g[p, c]; partial holds colsum_partial_floats().
 int colsum(const float *g, long P, int C, float *partial, float *db, cudaStream_t st);
 size_t colsum_partial_floats(long P, int C);
-// wt[8 - tap][co][ci] = bf16(w[tap][ci][co]) (dgrad weights), wb = bf16(w).
-int convert_weights(const float *w, int Cin, int Cout, bf16 *wb, bf16 *wt, cudaStream_t st);
 int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st);
 int pool_back(const bf16 *x, const bf16 *y, const float *gy, int B, int H, int W, int C, float *gx, cudaStream_t st);
 int split_grad(const float *gin, int B, int H, int W, int c0, int up0, int c1, float *g0, float *g1, cudaStream_t st);
@@ -69,8 +84,10 @@ int finish(const bf16 *x, const float *y, int B, int H, int W, int Hp, int Wp, f
 // Loss in log space on the residual prediction; writes gy (P x 16) and hyper->loss.
 int l1_loss(const bf16 *x, const float *y, const float *target, long P, float *gy, float *partial, Hyper *hyper,
             cudaStream_t st);
-int adam(float *params, const float *grads, float *m, float *v, size_t n, const LayerTable &tab, Hyper *hyper,
-         bf16 *wb, bf16 *wt, cudaStream_t st);
+// hyper->lr = lr, ordered on st (the value travels as a kernel argument: no host buffer).
+int set_learning_rate(Hyper *hyper, float lr, cudaStream_t st);
+// Adam on the FP32 parameters (the packed BF16 copies are refreshed by pack_all).
+int adam(float *params, const float *grads, float *m, float *v, size_t n, Hyper *hyper, cudaStream_t st);
 
 }  // namespace dn
 }  // namespace rgb

@@ -1,0 +1,572 @@
+// 3x3 convolution (forward and data gradient) on the 5th-generation tensor cores: an
+// implicit GEMM whose 128 x N tiles accumulate in tensor memory (TMEM) through
+// tcgen05.mma, with both operands brought into shared memory by TMA.
+//
+//   D[m][n] = sum_k A[m][k] B[n][k],  m = output pixel, n = output channel.
+//
+// A CTA tile is a block of Wb x Hb = 128 pixels of one image (Wb = min(128, the next power
+// of two >= the width)). K runs over the 9 taps and, per tap, over 64-channel chunks of
+// the input -- first those of input 0, then those of the skip input 1. The A operand of
+// one (tap, chunk) is a single tiled TMA box of 64 channels x Wb x Hb pixels at (chunk,
+// x0 + dx, y0 + dy, image): the copy engine's zero fill outside the tensor is exactly the
+// convolution's zero padding (and the zero channels of a chunk past the channel count).
+// The weights are packed to match: K-major rows [Cout][9 x chunks x 64], zero where a
+// chunk runs past the channel count; the B operand of a k-block is one 2-D box.
+// Both boxes land in the 128-byte-swizzle K-major layout that tcgen05.mma reads (one
+// 128-byte row per pixel / output channel, 8-row groups 1024 bytes apart).
+//
+// The kernel is persistent and warp-specialised: one thread issues the TMA loads into a
+// ring of shared-memory stages (full[s]: the stage's bytes have landed; empty[s]: the MMAs
+// that read it have completed), one thread issues the MMAs into two TMEM accumulators
+// (tfull[a]: a tile is complete; tempty[a]: the epilogue has read it back), and four
+// epilogue warps read finished tiles with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31
+// = tile rows), add the bias, apply the ReLU and store BF16 or FP32 NHWC while the next
+// tile accumulates.
+//
+// Every mbarrier wait is bounded (about 2 s of %globaltimer); a wait that gives up sets
+// the status word and its role stops, and the CTA frees its TMEM before it returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <string>
+
+#include "dn_net.hpp"
+
+namespace rgb {
+namespace dn {
+
+__device__ unsigned g_umma_status;  // nonzero: a bounded wait gave up (RT_ERR_TIMEOUT)
+
+namespace {
+
+constexpr int TM = 128;       // tile rows (pixels): one TMEM lane each
+constexpr int KB = 64;        // K per stage: one 128-byte swizzle row of BF16
+constexpr int MAX_STAGES = 8;
+constexpr int EPI_WARPS = 4;  // TMEM lanes 32w..32w+31 = tile rows
+constexpr int THREADS = 32 * (EPI_WARPS + 2);  // + the TMA warp and the MMA warp
+constexpr unsigned long long kWaitNs = 2000000000ull;
+
+__device__ __forceinline__ unsigned saddr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Wait for the phase of parity `parity` to complete; false if the bound ran out. The clock
+// is read only once the first test has failed.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+    if (mbar_try(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer();
+    while (!mbar_try(bar, parity))
+        if (globaltimer() - t0 > kWaitNs) return false;
+    return true;
+}
+
+__device__ __forceinline__ void tma_4d(unsigned dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                       unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];\n" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void tma_2d(unsigned dst, const CUtensorMap *map, int c0, int c1, unsigned bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];\n" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(bar)
+        : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ unsigned long long sdesc(unsigned addr) {
+    return (unsigned long long)((addr & 0x3FFFFu) >> 4) |  // start address
+           (1ull << 16) |                                  // leading byte offset (unused here)
+           ((unsigned long long)(1024 >> 4) << 32) |       // stride byte offset
+           (1ull << 46) |                                  // descriptor version
+           (2ull << 61);                                   // 128-byte swizzle
+}
+
+// Instruction descriptor, kind::f16: BF16 A and B (K-major), FP32 D, M = 128, N.
+__device__ __forceinline__ unsigned idesc(int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(n >> 3) << 17) | ((unsigned)(TM >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma(unsigned tmem, unsigned long long a, unsigned long long b, unsigned id,
+                                     unsigned acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(unsigned bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                 : "memory");
+}
+
+struct ConvTiles {
+    int H, W, Wb, Hb, tx, ty;  // tiles of Wb x Hb pixels, tx x ty per image
+    int seg0, cpt;             // 64-channel chunks per tap: of input 0, in total
+    int Cout, N, nhalf, mtiles, ntiles, stages;
+    const float *bias;
+    int relu;
+    bf16 *out_bf;
+    float *out_f;
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_conv_umma(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
+                const __grid_constant__ CUtensorMap tmw, const ConvTiles q) {
+    extern __shared__ unsigned char smem_raw[];
+    const unsigned raw = saddr(smem_raw);
+    const unsigned base = (raw + 1023u) & ~1023u;
+    const unsigned a_bytes = TM * 128, stage_bytes = a_bytes + (unsigned)q.N * 128;
+    const int S = q.stages;
+    const unsigned bar0 = base + S * stage_bytes;
+    auto full = [&](int st) { return bar0 + 8u * st; };
+    auto empty = [&](int st) { return bar0 + 8u * (MAX_STAGES + st); };
+    auto tfull = [&](int a) { return bar0 + 8u * (2 * MAX_STAGES + a); };
+    auto tempty = [&](int a) { return bar0 + 8u * (2 * MAX_STAGES + 2 + a); };
+    const unsigned tmem_slot = bar0 + 8u * (2 * MAX_STAGES + 4);
+    const unsigned *tmem_slot_ptr = reinterpret_cast<const unsigned *>(smem_raw + (tmem_slot - raw));
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int KT = 9 * q.cpt;
+    const int my_tiles = q.ntiles > (int)blockIdx.x ? (q.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    // Tile t: output channels [N (t / mtiles), +N) of the pixel block t % mtiles.
+    auto tile_origin = [&](int t, int &x0, int &y0, int &n, int &n0) {
+        const int mt = t % q.mtiles;
+        n0 = (t / q.mtiles) * q.N;
+        x0 = (mt % q.tx) * q.Wb;
+        const int r = mt / q.tx;
+        y0 = (r % q.ty) * q.Hb;
+        n = r / q.ty;
+    };
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tmem_slot),
+                     "r"(2 * q.nhalf));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        for (int st = 0; st < S; ++st) {
+            mbar_init(full(st), 1);
+            mbar_init(empty(st), 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(tfull(a), 1);
+            mbar_init(tempty(a), 32 * EPI_WARPS);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    const unsigned tmem = *tmem_slot_ptr;
+    bool ok = true;
+
+    if (warp == EPI_WARPS) {
+        // ---- TMA producer: one thread. Stage index and phase advance incrementally (this
+        // thread's issue rate bounds the pipeline: no divisions in the loop).
+        if (lane == 0) {
+            const unsigned tx_bytes = a_bytes + (unsigned)q.N * 128;
+            int st = 0;
+            unsigned ph = 0;     // parity of the current use of stage st
+            bool refill = false;  // every stage has been used once: wait for its MMAs first
+            for (int lt = 0; lt < my_tiles && ok; ++lt) {
+                int x0, y0, n, n0;
+                tile_origin((int)blockIdx.x + lt * (int)gridDim.x, x0, y0, n, n0);
+                int kcoord = 0;
+                for (int tap = 0; tap < 9 && ok; ++tap) {
+                    const int dy = tap / 3 - 1, dx = tap - 3 * (dy + 1) - 1;
+                    for (int j = 0; j < q.cpt; ++j, kcoord += KB) {
+                        if (refill && !(ok = mbar_wait(empty(st), ph ^ 1u))) break;
+                        const unsigned sa = base + st * stage_bytes;
+                        mbar_expect_tx(full(st), tx_bytes);
+                        if (j < q.seg0)
+                            tma_4d(sa, &tm0, j * KB, x0 + dx, y0 + dy, n, full(st));
+                        else
+                            tma_4d(sa, &tm1, (j - q.seg0) * KB, x0 + dx, y0 + dy, n, full(st));
+                        tma_2d(sa + a_bytes, &tmw, kcoord, n0, full(st));
+                        if (++st == S) {
+                            st = 0;
+                            ph ^= 1u;
+                            refill = true;
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == EPI_WARPS + 1) {
+        // ---- MMA issue: one thread.
+        if (lane == 0) {
+            const unsigned id = idesc(q.N);
+            int st = 0;
+            unsigned ph = 0;
+            for (int lt = 0; lt < my_tiles && ok; ++lt) {
+                const int a = lt & 1;
+                if (lt >= 2 && !(ok = mbar_wait(tempty(a), (unsigned)((lt >> 1) - 1) & 1u))) break;
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+                const unsigned d = tmem + (unsigned)(a * q.nhalf);
+                for (int kb = 0; kb < KT; ++kb) {
+                    if (!(ok = mbar_wait(full(st), ph))) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+                    const unsigned sa = base + st * stage_bytes, sb = sa + a_bytes;
+#pragma unroll
+                    for (int j = 0; j < KB / 16; ++j)
+                        umma(d, sdesc(sa + 32 * j), sdesc(sb + 32 * j), id, (kb | j) ? 1u : 0u);
+                    umma_commit(empty(st));
+                    if (++st == S) {
+                        st = 0;
+                        ph ^= 1u;
+                    }
+                }
+                if (ok) umma_commit(tfull(a));
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue: warp w reads TMEM lanes 32w..32w+31, i.e. tile row tid.
+        const int xl = tid % q.Wb, yl = tid / q.Wb;
+        for (int lt = 0; lt < my_tiles; ++lt) {
+            const int a = lt & 1;
+            ok = __all_sync(0xffffffffu, mbar_wait(tfull(a), (unsigned)(lt >> 1) & 1u));
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+            int x0, y0, n, n0;
+            tile_origin((int)blockIdx.x + lt * (int)gridDim.x, x0, y0, n, n0);
+            const int x = x0 + xl, y = y0 + yl;
+            const bool inside = x < q.W && y < q.H;
+            const long p = ((long)n * q.H + y) * q.W + x;
+            const int Cout = q.Cout;
+            for (int c0 = 0; c0 < q.N; c0 += 16) {
+                unsigned v[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];\n"
+                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                      "=r"(v[15])
+                    : "r"(tmem + ((unsigned)(32 * warp) << 16) + (unsigned)(a * q.nhalf + c0)));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                const int cb = n0 + c0;
+                if (inside && cb < Cout) {
+                    float f[16];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        float x_ = __uint_as_float(v[j]);
+                        if (q.bias) x_ += q.bias[cb + j < Cout ? cb + j : cb];
+                        if (q.relu) x_ = fmaxf(x_, 0.0f);
+                        f[j] = x_;
+                    }
+                    if (cb + 16 <= Cout) {
+                        if (q.out_bf) {
+                            __nv_bfloat162 h[8];
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) h[j] = __floats2bfloat162_rn(f[2 * j], f[2 * j + 1]);
+                            uint4 *dst = reinterpret_cast<uint4 *>(q.out_bf + p * Cout + cb);
+                            dst[0] = *reinterpret_cast<uint4 *>(&h[0]);
+                            dst[1] = *reinterpret_cast<uint4 *>(&h[4]);
+                        }
+                        if (q.out_f) {
+                            float4 *dst = reinterpret_cast<float4 *>(q.out_f + p * Cout + cb);
+#pragma unroll
+                            for (int j = 0; j < 4; ++j)
+                                dst[j] = make_float4(f[4 * j], f[4 * j + 1], f[4 * j + 2], f[4 * j + 3]);
+                        }
+                    } else {
+                        for (int j = 0; j < 16 && cb + j < Cout; ++j) {
+                            if (q.out_bf) q.out_bf[p * Cout + cb + j] = __float2bfloat16_rn(f[j]);
+                            if (q.out_f) q.out_f[p * Cout + cb + j] = f[j];
+                        }
+                    }
+                }
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+            mbar_arrive(tempty(a));
+        }
+    }
+    if (!ok) atomicOr(&g_umma_status, 1u);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * q.nhalf));
+    }
+}
+
+// Nearest 2x upsampling, NHWC: y (B, 2h, 2w, C) from x (B, h, w, C); 8 channels a thread.
+__global__ void k_upsample2(const bf16 *__restrict__ x, int B, int h, int w, int C, bf16 *__restrict__ y) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const int c8 = C / 8;
+    const size_t n = (size_t)B * 2 * h * 2 * w * c8;
+    if (i >= n) return;
+    const int c = (int)(i % c8) * 8;
+    size_t r = i / c8;
+    const int xx = (int)(r % (2 * w));
+    r /= 2 * w;
+    const int yy = (int)(r % (2 * h));
+    const int b = (int)(r / (2 * h));
+    const uint4 v = *reinterpret_cast<const uint4 *>(x + (((size_t)b * h + yy / 2) * w + xx / 2) * C + c);
+    *reinterpret_cast<uint4 *>(y + (((size_t)b * 2 * h + yy) * 2 * w + xx) * C + c) = v;
+}
+
+// Forward packing: wpk[co][(tap cpt + j) 64 + cc] = w[tap][ci][co] for the input channel ci
+// of chunk j (chunks of input 0 first, then of input 1), zero past either channel count.
+template <class T>
+__device__ __forceinline__ float pack_fwd_value(const T *w, int c0, int c1, int cout, size_t idx) {
+    const int seg0 = (c0 + 63) / 64, cpt = seg0 + (c1 + 63) / 64;
+    const size_t kp = (size_t)9 * cpt * 64;
+    const int co = (int)(idx / kp);
+    const int k = (int)(idx % kp);
+    const int kb = k / 64, cc = k % 64;
+    const int tap = kb / cpt, j = kb % cpt;
+    int ci;
+    if (j < seg0) {
+        ci = j * 64 + cc;
+        if (ci >= c0) return 0.0f;
+    } else {
+        const int c = (j - seg0) * 64 + cc;
+        if (c >= c1) return 0.0f;
+        ci = c0 + c;
+    }
+    return (float)w[((size_t)tap * (c0 + c1) + ci) * cout + co];
+}
+
+// Data-gradient packing: wpkd[ci][(tap' cptd + j) 64 + cc] = w[8 - tap'][ci][co = 64 j + cc].
+__device__ __forceinline__ float pack_bwd_value(const float *w, int cin, int cout, size_t idx) {
+    const int cptd = (cout + 63) / 64;
+    const size_t kp = (size_t)9 * cptd * 64;
+    const int ci = (int)(idx / kp);
+    const int k = (int)(idx % kp);
+    const int kb = k / 64, cc = k % 64;
+    const int tap = kb / cptd, co = (kb % cptd) * 64 + cc;
+    if (co >= cout) return 0.0f;
+    return w[((size_t)(8 - tap) * cin + ci) * cout + co];
+}
+
+template <class T>
+__global__ void k_pack_fwd(const T *__restrict__ w, int c0, int c1, int cout, bf16 *__restrict__ out, size_t n) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = __float2bfloat16_rn(pack_fwd_value(w, c0, c1, cout, i));
+}
+
+__global__ void k_pack_bwd(const float *__restrict__ w, int cin, int cout, bf16 *__restrict__ out, size_t n) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = __float2bfloat16_rn(pack_bwd_value(w, cin, cout, i));
+}
+
+// Every layer's packed forward and data-gradient weights from the FP32 parameters.
+__global__ void k_pack_all(const float *__restrict__ params, PackTable tab, bf16 *__restrict__ wk,
+                           bf16 *__restrict__ wkd) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i < tab.fwd_total) {
+        int l = 0;
+        while (l + 1 < tab.n && i >= tab.e[l + 1].fwd_off) ++l;
+        const PackEntry &e = tab.e[l];
+        wk[i] = __float2bfloat16_rn(pack_fwd_value(params + e.woff, (int)e.c0, (int)e.c1, (int)e.cout, i - e.fwd_off));
+    } else if (i < tab.fwd_total + tab.bwd_total) {
+        const size_t j = i - tab.fwd_total;
+        int l = 0;
+        while (l + 1 < tab.n && j >= tab.e[l + 1].bwd_off) ++l;
+        const PackEntry &e = tab.e[l];
+        wkd[j] = __float2bfloat16_rn(pack_bwd_value(params + e.woff, (int)(e.c0 + e.c1), (int)e.cout, j - e.bwd_off));
+    }
+}
+
+// ---- host: tensor maps ---------------------------------------------------------------------------
+typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+int encoder(EncodeTiled *out) {
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult qr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &qr) !=
+                cudaSuccess ||
+            qr != cudaDriverEntryPointSuccess || !p) {
+            cudaGetLastError();
+            set_error("cuTensorMapEncodeTiled is not available from the driver");
+            return RT_ERR_CUDA;
+        }
+        fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    *out = fn;
+    return RT_OK;
+}
+
+// NHWC BF16 activations (B, H, W, C) read as boxes of 64 channels x Wb x Hb pixels.
+int map_activations(CUtensorMap *m, const bf16 *ptr, int B, int H, int W, int C, int Wb, int Hb) {
+    EncodeTiled enc;
+    int r = encoder(&enc);
+    if (r != RT_OK) return r;
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)KB, (cuuint32_t)Wb, (cuuint32_t)Hb, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult e = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(ptr), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (e != CUDA_SUCCESS) {
+        set_error("activation tensor map rejected (error " + std::to_string((int)e) + ")");
+        return RT_ERR_CUDA;
+    }
+    return RT_OK;
+}
+
+// Packed weights [rows][Kp] read as boxes of 64 K x N rows.
+int map_weights(CUtensorMap *m, const bf16 *ptr, int Kp, int rows, int N) {
+    EncodeTiled enc;
+    int r = encoder(&enc);
+    if (r != RT_OK) return r;
+    const cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)KB, (cuuint32_t)N};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult e = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16 *>(ptr), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (e != CUDA_SUCCESS) {
+        set_error("weight tensor map rejected (error " + std::to_string((int)e) + ")");
+        return RT_ERR_CUDA;
+    }
+    return RT_OK;
+}
+
+inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace
+
+size_t packed_k(int c0, int c1) { return (size_t)9 * ((c0 + 63) / 64 + (c1 + 63) / 64) * 64; }
+
+int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, const float *bias, int Cout, bool relu,
+                      bf16 *out_bf, float *out_f, bf16 *ups, cudaStream_t st) {
+    const bf16 *src0 = in.p0;
+    if (in.up0) {
+        if (!ups) {
+            set_error("an upsampled convolution input needs scratch space");
+            return RT_ERR_ARG;
+        }
+        const size_t n8 = (size_t)B * H * W * (in.c0 / 8);
+        k_upsample2<<<blocks(n8), 256, 0, st>>>(in.p0, B, H / 2, W / 2, in.c0, ups);
+        RT_CUDA_TRY(cudaGetLastError());
+        src0 = ups;
+    }
+    ConvTiles q;
+    q.H = H;
+    q.W = W;
+    q.Wb = 1;
+    while (q.Wb < W && q.Wb < TM) q.Wb *= 2;
+    q.Hb = TM / q.Wb;
+    q.tx = (W + q.Wb - 1) / q.Wb;
+    q.ty = (H + q.Hb - 1) / q.Hb;
+    q.seg0 = (in.c0 + 63) / 64;
+    q.cpt = q.seg0 + (in.c1 + 63) / 64;
+    q.Cout = Cout;
+    // N: the whole output in one tile when it fits the instruction (<= 256), else 128-wide tiles.
+    q.N = Cout <= 256 ? (Cout + 15) / 16 * 16 : 128;
+    q.nhalf = 32;  // TMEM columns of one of the two accumulators
+    while (q.nhalf < q.N) q.nhalf *= 2;
+    q.mtiles = B * q.tx * q.ty;
+    q.ntiles = q.mtiles * ((Cout + q.N - 1) / q.N);
+    const size_t stage_bytes = (size_t)TM * 128 + (size_t)q.N * 128;
+    const size_t fixed = 1024 + 8 * (2 * MAX_STAGES + 4) + 16;
+    q.stages = (int)std::min<size_t>(MAX_STAGES, (220 * 1024 - fixed) / stage_bytes);
+    q.bias = bias;
+    q.relu = relu ? 1 : 0;
+    q.out_bf = out_bf;
+    q.out_f = out_f;
+    const size_t smem = q.stages * stage_bytes + fixed;
+
+    CUtensorMap tm0, tm1, tmw;
+    int r = map_activations(&tm0, src0, B, H, W, in.c0, q.Wb, q.Hb);
+    if (r == RT_OK) {
+        if (in.c1)
+            r = map_activations(&tm1, in.p1, B, H, W, in.c1, q.Wb, q.Hb);
+        else
+            tm1 = tm0;
+    }
+    if (r == RT_OK) r = map_weights(&tmw, wpk, (int)packed_k(in.c0, in.c1), Cout, q.N);
+    if (r != RT_OK) return r;
+
+    static bool configured = false;
+    static int sms = 0;
+    if (!configured) {
+        RT_CUDA_TRY(cudaFuncSetAttribute(k_conv_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
+        int dev = 0;
+        RT_CUDA_TRY(cudaGetDevice(&dev));
+        RT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        configured = true;
+    }
+    const int grid = std::min(q.ntiles, sms);  // one persistent CTA per SM
+    k_conv_umma<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pack_weights(const float *w, int c0, int c1, int Cout, bf16 *wpk, bf16 *wpkd, cudaStream_t st) {
+    if (wpk) {
+        const size_t n = (size_t)Cout * packed_k(c0, c1);
+        k_pack_fwd<float><<<blocks(n), 256, 0, st>>>(w, c0, c1, Cout, wpk, n);
+    }
+    if (wpkd) {
+        const size_t n = (size_t)(c0 + c1) * packed_k(Cout, 0);
+        k_pack_bwd<<<blocks(n), 256, 0, st>>>(w, c0 + c1, Cout, wpkd, n);
+    }
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pack_weights_bf16(const bf16 *w, int c0, int c1, int Cout, bf16 *wpk, cudaStream_t st) {
+    const size_t n = (size_t)Cout * packed_k(c0, c1);
+    k_pack_fwd<bf16><<<blocks(n), 256, 0, st>>>(w, c0, c1, Cout, wpk, n);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pack_all(const float *params, const PackTable &tab, bf16 *wk, bf16 *wkd, cudaStream_t st) {
+    k_pack_all<<<blocks(tab.fwd_total + tab.bwd_total), 256, 0, st>>>(params, tab, wk, wkd);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int umma_status(bool clear) {
+    unsigned s = 0;
+    RT_CUDA_TRY(cudaMemcpyFromSymbol(&s, g_umma_status, sizeof(unsigned)));
+    if (s && clear) {
+        const unsigned z = 0;
+        RT_CUDA_TRY(cudaMemcpyToSymbol(g_umma_status, &z, sizeof(unsigned)));
+    }
+    if (s) {
+        set_error("a tensor-core convolution timed out waiting for its pipeline");
+        return RT_ERR_TIMEOUT;
+    }
+    return RT_OK;
+}
+
+}  // namespace dn
+}  // namespace rgb

@@ -176,9 +176,10 @@ class Denoiser:
 def render_pairs(tracer, cameras, width: int, height: int, spp_in: int = 4, spp_ref: int = 1024, depth: int = 5,
                  mode: int = 1, clamp: float = 5.0, seed: int = 0):
     """Denoiser inputs and targets rendered by the path tracer itself: for each camera, the
-    features of a ``spp_in``-sample render (radiance + first-hit albedo, normal, distance)
-    and, when ``spp_ref`` > 0, a ``spp_ref``-sample render accumulated in double precision.
-    Returns CUDA tensors (N, H, W, 10) and (N, H, W, 3) (targets None without spp_ref)."""
+    features of a ``spp_in``-sample render (radiance + first-hit albedo, normal, distance;
+    a sequence of sample counts is cycled through the cameras) and, when ``spp_ref`` > 0,
+    a ``spp_ref``-sample render accumulated in double precision. Returns CUDA tensors
+    (N, H, W, 10) and (N, H, W, 3) (targets None without spp_ref)."""
     import torch
 
     n = len(cameras)
@@ -190,7 +191,8 @@ def render_pairs(tracer, cameras, width: int, height: int, spp_in: int = 4, spp_
     for k, cam in enumerate(cameras):
         cam = dict(cam, ratio=width / height)
         img.zero_()
-        tracer.render(cam, spp_in, depth, img, seed=seed + 2 * k, mode=mode, clamp=clamp, aov=aov)
+        spp = spp_in[k % len(spp_in)] if isinstance(spp_in, (list, tuple)) else spp_in
+        tracer.render(cam, spp, depth, img, seed=seed + 2 * k, mode=mode, clamp=clamp, aov=aov)
         feats[k, ..., :3] = img
         feats[k, ..., 3:] = aov
         if spp_ref:

@@ -220,3 +220,25 @@ def test_invalid_arguments_are_rejected(cuda_lib):
         d.set_params(np.zeros(3, np.float32))
     with pytest.raises(RenduError, match="learning rate"):
         d.adam_step(float("nan"))
+
+
+def test_captured_steps_match_eager(cuda_lib):
+    """dn_train_step and dn_denoise run eagerly on a new shape, capture a CUDA graph on the
+    next call and replay it after: every call gives what the eager dn_backward +
+    dn_adam_step sequence gives, bit for bit."""
+    from rendu_gb300.denoiser import Denoiser
+
+    rng = np.random.default_rng(15)
+    feats = _features(rng, 2, 48, 32)
+    target = rng.exponential(0.5, (2, 48, 32, 3)).astype(np.float32)
+    a, b = Denoiser(seed=9), Denoiser(seed=9)
+    for lr in (1e-3, 1e-3, 5e-4, 5e-4, 5e-4):
+        la = a.train_step(feats, target, lr)
+        lb = b.backward(feats, target)
+        b.adam_step(lr)
+        assert la == lb
+    np.testing.assert_array_equal(a.get_params(), b.get_params())
+    f2 = _features(rng, 1, 40, 56)
+    outs = [a.denoise(f2) for _ in range(4)]
+    for o in outs[1:]:
+        np.testing.assert_array_equal(o, outs[0])
