@@ -86,34 +86,50 @@ int require_built(rt_ctx *ctx) {
     return RT_OK;
 }
 
-// Runs `fn(d_in, count, d_out, stream)` over host buffers in chunks of 2M records that
-// alternate between two streams with their own staging buffers: the copy-in of chunk k+1,
-// the kernel of chunk k and the copy-out of chunk k-1 overlap (separate copy engines for
-// each direction). Pinned host buffers get asynchronous DMA; pageable ones still work but
-// their copies do not overlap.
+// Runs `fn(d_in, count, d_out, stream)` over host buffers in chunks of 2M records through a
+// ring of four staging buffers and three streams: copies in on `stream`, kernels on
+// `stream2`, copies out on `stream3`, ordered by events, so that both copy directions and
+// the kernels stay busy at once (the host link, not the kernels, bounds this path). Pinned
+// host buffers get asynchronous DMA; pageable ones still work but their copies do not
+// overlap.
 template <class Fn>
 int host_chunked(rt_ctx *ctx, const void *h_in, size_t in_stride, size_t n, void *h_out, size_t out_stride, Fn fn) {
+    constexpr int NB = rt_ctx::kRing;
     const size_t chunk = size_t(1) << 21;
     const size_t cn = n < chunk ? n : chunk;
-    DevBuf *in[2] = {&ctx->d_rays, &ctx->d_rays2};
-    DevBuf *out[2] = {&ctx->d_out, &ctx->d_out3};
-    for (int k = 0; k < 2; ++k)
-        if (in[k]->reserve(cn * in_stride) != RT_OK || out[k]->reserve(cn * out_stride) != RT_OK) return RT_ERR_OOM;
-    cudaStream_t st[2] = {ctx->stream, ctx->stream2};
-    size_t idx = 0;
-    for (size_t s = 0; s < n; s += chunk, ++idx) {
-        const int b = (int)(idx & 1);
-        const size_t m = (n - s) < chunk ? (n - s) : chunk;
-        RT_CUDA_TRY(cudaMemcpyAsync(in[b]->ptr, static_cast<const char *>(h_in) + s * in_stride, m * in_stride,
-                                    cudaMemcpyHostToDevice, st[b]));
-        const int r = fn(in[b]->ptr, m, out[b]->ptr, st[b]);
-        if (r != RT_OK) return r;
-        RT_CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(h_out) + s * out_stride, out[b]->ptr, m * out_stride,
-                                    cudaMemcpyDeviceToHost, st[b]));
+    if (!ctx->stream3) RT_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream3, cudaStreamNonBlocking));
+    for (int b = 0; b < NB; ++b) {
+        if (ctx->ring_in[b].reserve(cn * in_stride) != RT_OK || ctx->ring_out[b].reserve(cn * out_stride) != RT_OK)
+            return RT_ERR_OOM;
+        for (cudaEvent_t *e : {&ctx->ev_in[b], &ctx->ev_k[b], &ctx->ev_out[b]})
+            if (!*e) RT_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
-    RT_CUDA_TRY(cudaStreamSynchronize(st[1]));
-    RT_CUDA_TRY(cudaStreamSynchronize(st[0]));
-    return check_status(ctx, st[0]);
+    cudaStream_t sin = ctx->stream, sk = ctx->stream2, sout = ctx->stream3;
+    size_t c = 0;
+    int r = RT_OK;
+    for (size_t s = 0; s < n && r == RT_OK; s += chunk, ++c) {
+        const int b = (int)(c % NB);
+        const size_t m = (n - s) < chunk ? (n - s) : chunk;
+        // Buffer b is free once the copy-out of the chunk NB before has finished (which
+        // itself followed that chunk's kernel).
+        if (c >= (size_t)NB) RT_CUDA_TRY(cudaStreamWaitEvent(sin, ctx->ev_out[b], 0));
+        RT_CUDA_TRY(cudaMemcpyAsync(ctx->ring_in[b].ptr, static_cast<const char *>(h_in) + s * in_stride, m * in_stride,
+                                    cudaMemcpyHostToDevice, sin));
+        RT_CUDA_TRY(cudaEventRecord(ctx->ev_in[b], sin));
+        RT_CUDA_TRY(cudaStreamWaitEvent(sk, ctx->ev_in[b], 0));
+        r = fn(ctx->ring_in[b].ptr, m, ctx->ring_out[b].ptr, sk);
+        if (r != RT_OK) break;
+        RT_CUDA_TRY(cudaEventRecord(ctx->ev_k[b], sk));
+        RT_CUDA_TRY(cudaStreamWaitEvent(sout, ctx->ev_k[b], 0));
+        RT_CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(h_out) + s * out_stride, ctx->ring_out[b].ptr, m * out_stride,
+                                    cudaMemcpyDeviceToHost, sout));
+        RT_CUDA_TRY(cudaEventRecord(ctx->ev_out[b], sout));
+    }
+    RT_CUDA_TRY(cudaStreamSynchronize(sout));
+    RT_CUDA_TRY(cudaStreamSynchronize(sk));
+    RT_CUDA_TRY(cudaStreamSynchronize(sin));
+    if (r != RT_OK) return r;
+    return check_status(ctx, sk);
 }
 
 }  // namespace
@@ -163,17 +179,23 @@ int rt_destroy(rt_ctx *ctx) {
     ctx->d_tris.release();
     ctx->d_verts.release();
     ctx->d_status.release();
-    ctx->d_rays.release();
-    ctx->d_out.release();
     ctx->d_out2.release();
-    ctx->d_rays2.release();
-    ctx->d_out3.release();
     if (ctx->stream2) {
         cudaStreamSynchronize(ctx->stream2);
         cudaStreamDestroy(ctx->stream2);
     }
     if (ctx->ev_a) cudaEventDestroy(ctx->ev_a);
     if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
+    if (ctx->stream3) {
+        cudaStreamSynchronize(ctx->stream3);
+        cudaStreamDestroy(ctx->stream3);
+    }
+    for (int b = 0; b < rt_ctx::kRing; ++b) {
+        ctx->ring_in[b].release();
+        ctx->ring_out[b].release();
+        for (cudaEvent_t e : {ctx->ev_in[b], ctx->ev_k[b], ctx->ev_out[b]})
+            if (e) cudaEventDestroy(e);
+    }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return RT_OK;

@@ -40,7 +40,7 @@ struct MeshRecord {
 struct rt_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;   // the context's own stream
-    cudaStream_t stream2 = nullptr;  // second stream of the pipelined host-buffer path
+    cudaStream_t stream2 = nullptr;  // kernels of the pipelined host-buffer path
     // Host copies appended by rt_add_mesh (raw positions; indices already offset).
     std::vector<float> h_positions;
     std::vector<uint32_t> h_indices;
@@ -61,13 +61,15 @@ struct rt_ctx {
     float sah_cost = 0.0f;
     float root_box[6] = {0, 0, 0, 0, 0, 0};
 
-    // Staging for host-pointer calls.
-    rgb::DevBuf d_rays;
-    rgb::DevBuf d_out;
+    // Scratch of rt_visible (converted rays) and rt_count_visits (hits).
     rgb::DevBuf d_out2;
-    rgb::DevBuf d_rays2;
-    rgb::DevBuf d_out3;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    // Host-buffer pipeline: copy-in on `stream`, kernels on `stream2`, copy-out on `stream3`,
+    // through a ring of staging buffers (created on first use).
+    static constexpr int kRing = 4;
+    cudaStream_t stream3 = nullptr;
+    rgb::DevBuf ring_in[kRing], ring_out[kRing];
+    cudaEvent_t ev_in[kRing] = {}, ev_k[kRing] = {}, ev_out[kRing] = {};
 };
 
 namespace rgb {
