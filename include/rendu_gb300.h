@@ -167,6 +167,7 @@ RT_API const char *rt_last_error(void);
 #define PT_BG_COLOR 0
 #define PT_BG_IMAGE 1
 #define PT_BG_SKYBOX 2
+#define PT_BG_ATMOSPHERE 3
 
 /* Light types (src/engine/scene/lights/). */
 #define PT_LIGHT_POINT 0
@@ -245,8 +246,16 @@ RT_API int pt_scene_add_object(pt_scene *scene, uint32_t mesh_id, uint32_t mater
                         uint32_t *object_id);
 RT_API int pt_scene_add_light(pt_scene *scene, const pt_light_desc *light);
 /* COLOR: color[3] used; IMAGE: tex[0]; SKYBOX: tex[0..5] = +x,-x,+y,-y,+z,-z faces
- * (Texture.cpp:141-191). */
+ * (Texture.cpp:141-191); ATMOSPHERE: color[3] = the sun direction (normalised, as Sky does,
+ * Sky.cpp:16,35), the sky of MaterialSky::eval (MaterialSky.cpp:6-87) seen by every miss. */
 RT_API int pt_scene_set_background(pt_scene *scene, int32_t mode, const float *color, const uint32_t *tex);
+
+/* ATMOSPHERE's scattering table, width x height RGBA floats (x = relative height, y =
+ * cosine of the sun's vertical angle). NULL restores the default: the table the reference
+ * ships (resources/common/scattering-precomputed.exr), i.e. AtmosphereApp::precomputeTable
+ * (AtmosphereApp.cpp:145-188) at 512 x 512 with 256 steps, in half precision, computed on
+ * the device at commit. */
+RT_API int pt_scene_set_sky_table(pt_scene *scene, const float *rgba, uint32_t width, uint32_t height);
 
 /* Upload the scene and build its raycaster: every object's mesh is added in object order
  * (so meshId == object index) and the hierarchy is built. Replaces
@@ -346,6 +355,16 @@ RT_API int pt_material_eval(const float *cases, size_t n, float *out, int device
  * the three numbers the reference draws (lobe choice, then the two lobe coordinates);
  * out = n x 6 floats {weight.rgb, wi.xyz}. */
 RT_API int pt_material_sample(const float *cases, const float *uniforms, size_t n, float *out, int device);
+
+/* AtmosphereApp::precomputeTable on device `device`: res x res RGBA floats into `out` (host),
+ * `samples` march steps, rounded to half precision when half_precision != 0. */
+RT_API int pt_sky_table(uint32_t res, uint32_t samples, int32_t half_precision, float *out, int device);
+
+/* MaterialSky::eval (MaterialSky.cpp:6-87) for n cases on device `device`: cases = n x 9
+ * floats {ray origin.xyz, normalised direction.xyz, normalised sun direction.xyz} (host);
+ * out = n x 3 radiance. table = width x height RGBA floats, or NULL for the default table. */
+RT_API int pt_sky_eval(const float *table, uint32_t width, uint32_t height, const float *cases, size_t n, float *out,
+                       int device);
 
 /* The raycaster built by pt_scene_commit (PathTracer::raycaster(), PathTracer.hpp:29). */
 RT_API rt_ctx *pt_scene_raycaster(pt_scene *scene);

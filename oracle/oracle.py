@@ -286,6 +286,10 @@ class _OracleTracer:
         bg = scene.background
         col = (C.c_float * 3)(*[float(x) for x in bg.get("color", (0, 0, 0))])
         f("set_background")(self.h, int(bg["mode"]), col, (C.c_uint32 * 6)(*bg.get("tex", (0,) * 6)))
+        if bg.get("sky_table") is not None and hasattr(lib, prefix + "set_sky_table"):
+            t = np.ascontiguousarray(bg["sky_table"], np.float32)
+            self._keep.append(t)
+            f("set_sky_table")(self.h, t.reshape(-1), t.shape[1], t.shape[0])
         env = getattr(scene, "environment", None)
         if env is not None and hasattr(lib, prefix + "set_environment"):
             f("set_environment")(self.h, int(env["tex"]), C.c_float(float(env.get("intensity", 1.0))))
@@ -315,6 +319,7 @@ class PortPathTracer(_OracleTracer):
             lib.port_pt_render_ex.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, _f32p,
                                               C.c_uint32, C.c_uint32, C.c_int, _u64p, C.c_int, C.c_float]
             lib.port_pt_set_environment.argtypes = [C.c_void_p, C.c_uint32, C.c_float]
+            lib.port_pt_set_sky_table.argtypes = [C.c_void_p, _f32p, C.c_uint32, C.c_uint32]
             lib.port_ggx_eval.argtypes = [_f32p, C.c_size_t, _f32p]
             lib.port_ggx_sample.argtypes = [_f32p, _f32p, C.c_size_t, _f32p]
             lib.port_pixel_shifts.argtypes = [C.c_void_p, _f32p]
@@ -387,4 +392,60 @@ def port_pixel_shifts(camera: dict):
     out = np.zeros(12, np.float32)
     cam = camera_desc(camera)
     lib.port_pixel_shifts(C.byref(cam), out)
+    return out
+
+
+# ---- atmosphere (MaterialSky, AtmosphereApp::precomputeTable) -------------------------------
+def port_sky_table(res: int = 512, samples: int = 256, half: bool = True) -> np.ndarray:
+    """The C restatement of AtmosphereApp::precomputeTable: (res, res, 4) float32, rounded to
+    half precision like the reference's stored table unless half=False."""
+    lib = port_lib()
+    lib.port_sky_table.argtypes = [C.c_uint32, C.c_uint32, C.c_int, _f32p]
+    out = np.zeros((res, res, 4), np.float32)
+    lib.port_sky_table(res, samples, int(half), out.reshape(-1))
+    return out
+
+
+def port_round_half(x) -> np.ndarray:
+    lib = port_lib()
+    lib.port_round_half.argtypes = [C.c_float]
+    lib.port_round_half.restype = C.c_float
+    a = np.asarray(x, np.float32).reshape(-1)
+    return np.array([lib.port_round_half(float(v)) for v in a], np.float32)
+
+
+def port_sky_eval(table, cases) -> np.ndarray:
+    """The C restatement of MaterialSky::eval for cases (n, 9) {origin, direction, sun}."""
+    lib = port_lib()
+    lib.port_sky_eval.argtypes = [_f32p, C.c_uint32, C.c_uint32, _f32p, C.c_size_t, _f32p]
+    t = np.ascontiguousarray(table, np.float32)
+    c = np.ascontiguousarray(cases, np.float32).reshape(-1, 9)
+    out = np.zeros((len(c), 3), np.float32)
+    lib.port_sky_eval(t.reshape(-1), t.shape[1], t.shape[0], c.reshape(-1), len(c), out.reshape(-1))
+    return out
+
+
+def ref_load_image(path: str, channels: int = 4, max_pixels: int = 1 << 22) -> np.ndarray:
+    """The reference's Image::load of a file (2-D texture orientation): (h, w, channels)."""
+    lib = ref_lib()
+    lib.ref_load_image.argtypes = [C.c_char_p, C.c_uint, _f32p, C.c_size_t, C.POINTER(C.c_uint32),
+                                   C.POINTER(C.c_uint32)]
+    buf = np.zeros(max_pixels * channels, np.float32)
+    w, h = C.c_uint32(), C.c_uint32()
+    r = lib.ref_load_image(path.encode(), channels, buf, buf.size, C.byref(w), C.byref(h))
+    if r != 0:
+        raise RuntimeError(f"reference Image::load failed ({r}) on {path}")
+    return buf[: w.value * h.value * channels].reshape(h.value, w.value, channels).copy()
+
+
+def ref_sky_eval(table, cases) -> np.ndarray:
+    """The reference's MaterialSky::eval with the given scattering table."""
+    lib = ref_lib()
+    lib.ref_set_sky_table.argtypes = [_f32p, C.c_uint32, C.c_uint32]
+    lib.ref_sky_eval.argtypes = [_f32p, C.c_size_t, _f32p]
+    t = np.ascontiguousarray(table, np.float32)
+    lib.ref_set_sky_table(t.reshape(-1), t.shape[1], t.shape[0])
+    c = np.ascontiguousarray(cases, np.float32).reshape(-1, 9)
+    out = np.zeros((len(c), 3), np.float32)
+    lib.ref_sky_eval(c.reshape(-1), len(c), out.reshape(-1))
     return out

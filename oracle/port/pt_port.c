@@ -99,6 +99,8 @@ struct port_pt {
     int bg_mode;
     float bg_color[3];
     uint32_t bg_tex[6];
+    f3 sun;          /* ATMOSPHERE: normalised sun direction */
+    tex_t sky;       /* ATMOSPHERE: the scattering table (computed at commit unless supplied) */
     port_rc *rc;
     int any_masked;
     /* extended estimator */
@@ -141,6 +143,7 @@ void port_pt_destroy(port_pt *s) {
     }
     free(s->tex); free(s->mesh); free(s->mat); free(s->obj); free(s->light);
     free(s->emitters); free(s->ecdf); free(s->efunc); free(s->emarg); free(s->econd);
+    free(s->sky.rgba);
     if (s->rc) port_rc_destroy(s->rc);
     free(s);
 }
@@ -233,11 +236,29 @@ int port_pt_set_background(port_pt *s, int mode, const float *color, const uint3
     s->bg_mode = mode;
     if (color) memcpy(s->bg_color, color, sizeof(s->bg_color));
     if (tex) memcpy(s->bg_tex, tex, sizeof(s->bg_tex));
+    if (mode == PT_BG_ATMOSPHERE && color) /* Sky::setDirection normalises (Sky.cpp:35) */
+        s->sun = norm3(mk3(color[0], color[1], color[2]));
+    return 0;
+}
+
+int port_pt_set_sky_table(port_pt *s, const float *rgba, uint32_t w, uint32_t h) {
+    free(s->sky.rgba);
+    s->sky.rgba = (float *)malloc(sizeof(float) * 4 * (size_t)w * h);
+    if (!s->sky.rgba) return -1;
+    memcpy(s->sky.rgba, rgba, sizeof(float) * 4 * (size_t)w * h);
+    s->sky.w = w;
+    s->sky.h = h;
     return 0;
 }
 
 /* PathTracer::PathTracer (PathTracer.cpp:11-21): one raycaster mesh per object, in order. */
 int port_pt_commit(port_pt *s) {
+    if (s->bg_mode == PT_BG_ATMOSPHERE && !s->sky.rgba) {
+        s->sky.rgba = (float *)malloc(sizeof(float) * 4 * PORT_SKY_TABLE_RES * PORT_SKY_TABLE_RES);
+        if (!s->sky.rgba) return -1;
+        port_sky_table(PORT_SKY_TABLE_RES, PORT_SKY_TABLE_SAMPLES, 1, s->sky.rgba);
+        s->sky.w = s->sky.h = PORT_SKY_TABLE_RES;
+    }
     if (s->rc) port_rc_destroy(s->rc);
     s->rc = port_rc_create();
     s->any_masked = 0;
@@ -383,9 +404,158 @@ static f3 cubemap(const port_pt *s, f3 dir) {
     return mk3(c.x, c.y, c.z);
 }
 
-/* PathTracer::evalBackground (PathTracer.cpp:23-55). */
-static f3 background(const port_pt *s, f3 dir, float nx, float ny, int direct) {
+/* ---- atmosphere ------------------------------------------------------------------------ */
+/* Sky::AtmosphereParameters (Sky.hpp:53-65): an Earth-like atmosphere. */
+static const float SKY_SUN_COLOR[3] = {1.474f, 1.8504f, 1.91198f};
+static const float SKY_K_RAYLEIGH[3] = {5.5e-6f, 13.0e-6f, 22.4e-6f};
+#define SKY_GROUND 6371e3f
+#define SKY_TOP 6471e3f
+#define SKY_SUN_INTENSITY 20.0f
+#define SKY_K_MIE 21e-6f
+#define SKY_H_RAYLEIGH 8000.0f
+#define SKY_H_MIE 1200.0f
+#define SKY_G_MIE 0.758f
+#define SKY_SUN_RADIUS 0.04675f
+#define SKY_SUN_RADIUS_COS 0.998f
+#define SKY_STEPS 16 /* MaterialSky::samplesCount (MaterialSky.hpp) */
+
+/* Intersection::sphere (Intersection.cpp:7-20): roots of |o + t d| = radius. */
+static int sphere_roots(f3 o, f3 d, float radius, float *r0, float *r1) {
+    const float a = dot3(d, d), b = dot3(o, d), c = dot3(o, o) - radius * radius;
+    const float delta = b * b - a * c;
+    if (delta < 0.0f) return 0;
+    const float ds = sqrtf(delta);
+    *r0 = (-b - ds) / a;
+    *r1 = (-b + ds) / a;
+    return 1;
+}
+
+/* AtmosphereApp::precomputeTable (AtmosphereApp.cpp:145-188): secondary attenuation towards
+ * the sun, x = relative height, y = cosine of the sun's vertical angle. */
+/* Nearest IEEE binary16 value (round to nearest, ties to even), returned as float: the
+ * precision of the reference's stored table. Exact for every float (normals, subnormals,
+ * overflow to infinity). */
+float port_round_half(float x) {
+    union { float f; uint32_t u; } v = {x};
+    const uint32_t sign = v.u & 0x80000000u;
+    uint32_t a = v.u & 0x7FFFFFFFu;
+    if (a >= 0x7F800000u) return x;                                  /* inf, nan */
+    if (a >= 0x477FF000u) { v.u = sign | 0x7F800000u; return v.f; }  /* rounds past 65504 */
+    const int e = (int)(a >> 23) - 127;
+    /* spacing of halves around x: 2^(e-10) for normal halves (e >= -14), 2^-24 below */
+    const int q = e >= -14 ? e - 10 : -24;
+    /* scale so that the spacing is 1, round to even, scale back (exact in double) */
+    const double s = ldexp((double)(v.f < 0 ? -v.f : v.f), -q);
+    double r = floor(s);
+    const double frac = s - r;
+    if (frac > 0.5 || (frac == 0.5 && fmod(r, 2.0) != 0.0)) r += 1.0;
+    union { float f; uint32_t u; } o;
+    o.f = (float)ldexp(r, q);
+    o.u |= sign;
+    return o.f;
+}
+
+void port_sky_table(uint32_t res, uint32_t samples, int half_precision, float *rgba) {
+    for (uint32_t y = 0; y < res; ++y)
+        for (uint32_t x = 0; x < res; ++x) {
+            const float xf = (float)x / ((float)res - 1.0f), yf = (float)y / ((float)res - 1.0f);
+            const f3 pos = mk3(0.0f, (SKY_TOP - SKY_GROUND) * xf + SKY_GROUND, 0.0f);
+            const float cosA = 2.0f * yf - 1.0f;
+            const float sinA = sqrtf(1.0f - cosA * cosA);
+            const f3 n = norm3(mk3(sinA, cosA, 0.0f));
+            const f3 sun = mk3(-n.x, -n.y, -n.z);
+            float r0 = 0.0f, r1 = 0.0f;
+            const int hit = sphere_roots(pos, sun, SKY_TOP, &r0, &r1);
+            const float step = hit ? r1 / (float)samples : 0.0f;
+            float rd = 0.0f, md = 0.0f;
+            for (uint32_t j = 0; j < samples; ++j) {
+                const f3 p = add3(pos, scl3(((float)j + 0.5f) * step, sun));
+                const float hgt = sqrtf(dot3(p, p)) - SKY_GROUND;
+                rd += expf(-hgt / SKY_H_RAYLEIGH) * step;
+                md += expf(-hgt / SKY_H_MIE) * step;
+            }
+            float *o = rgba + 4 * ((size_t)y * res + x);
+            for (int c = 0; c < 3; ++c) {
+                const float att = expf(-(SKY_K_MIE * md + SKY_K_RAYLEIGH[c] * rd));
+                o[c] = half_precision ? port_round_half(att) : att;
+            }
+            o[3] = 1.0f;
+        }
+}
+
+/* MaterialSky::rayleighPhase / miePhase (MaterialSky.cpp:89-98). */
+static float rayleigh_phase(float c) {
+    const float k = 1.0f / (4.0f * 3.14159265358979323846f);
+    return k * 3.0f / 4.0f * (1.0f + c * c);
+}
+static float mie_phase(float c) {
+    const float k = 1.0f / (4.0f * 3.14159265358979323846f);
+    const float g2 = SKY_G_MIE * SKY_G_MIE;
+    return k * 3.0f * (1.0f - g2) / (2.0f * (2.0f + g2)) * (1.0f + c * c) /
+           powf(1.0f + g2 - 2.0f * SKY_G_MIE * c, 3.0f / 2.0f);
+}
+
+/* MaterialSky::eval (MaterialSky.cpp:6-87): single-scattering march of 16 steps through the
+ * atmosphere along the ray, secondary attenuation from the table, plus the sun disc. */
+static f3 sky_eval(const tex_t *table, f3 origin, f3 dir, f3 sun) {
+    const f3 planet = add3(add3(origin, mk3(0.0f, SKY_GROUND, 0.0f)), mk3(0.0f, 1.0f, 0.0f));
+    float t0 = 0.0f, t1 = 0.0f, g0 = 0.0f, g1 = 0.0f;
+    if (!sphere_roots(planet, dir, SKY_TOP, &t0, &t1)) return mk3(0.0f, 0.0f, 0.0f);
+    const int ground = sphere_roots(planet, dir, SKY_GROUND, &g0, &g1);
+    const float dist = fminf_g(t1, ground ? g0 : 0.0f);
+    const float step = (dist - t0) / (float)SKY_STEPS;
+    const float cos_vs = dot3(dir, sun);
+    float rd = 0.0f, md = 0.0f;
+    f3 rs = mk3(0, 0, 0), ms = mk3(0, 0, 0), tr = mk3(0, 0, 0);
+    for (int i = 0; i < SKY_STEPS; ++i) {
+        const f3 p = add3(planet, scl3(((float)i + 0.5f) * step, dir));
+        float hgt = sqrtf(dot3(p, p)) - SKY_GROUND;
+        if (i == SKY_STEPS - 1 && hgt < 0.0f) hgt = 0.0f;
+        const float rstep = expf(-hgt / SKY_H_RAYLEIGH) * step;
+        const float mstep = expf(-hgt / SKY_H_MIE) * step;
+        rd += rstep;
+        md += mstep;
+        const f3 direct = mk3(expf(-(md * SKY_K_MIE + rd * SKY_K_RAYLEIGH[0])),
+                              expf(-(md * SKY_K_MIE + rd * SKY_K_RAYLEIGH[1])),
+                              expf(-(md * SKY_K_MIE + rd * SKY_K_RAYLEIGH[2])));
+        const float rel_h = (sqrtf(dot3(p, p)) - SKY_GROUND) / (SKY_TOP - SKY_GROUND);
+        const float rel_c = -0.5f * sun.y + 0.5f;
+        float u = (511.0f / 512.0f) * rel_h + 0.5f / 512.0f, v = (511.0f / 512.0f) * rel_c + 0.5f / 512.0f;
+        u = fminf_g(fmaxf_g(u, 0.5f / 512.0f), 511.0f / 512.0f); /* glm::clamp */
+        v = fminf_g(fmaxf_g(v, 0.5f / 512.0f), 511.0f / 512.0f);
+        const f4 sec = rgbal(table, u, v);
+        const f3 att = mul3(direct, mk3(sec.x, sec.y, sec.z));
+        rs = add3(rs, scl3(rstep, att));
+        ms = add3(ms, scl3(mstep, att));
+        tr = add3(tr, direct);
+    }
+    const f3 rp = mul3(scl3(rayleigh_phase(cos_vs), mk3(SKY_K_RAYLEIGH[0], SKY_K_RAYLEIGH[1], SKY_K_RAYLEIGH[2])), rs);
+    const f3 mp = scl3(SKY_K_MIE * mie_phase(cos_vs), ms);
+    f3 sun_r = mk3(0.0f, 0.0f, 0.0f);
+    const int ground_forward = ground && g1 > 0.0f;
+    if (!ground_forward && dot3(dir, sun) > SKY_SUN_RADIUS_COS) {
+        const float area = 3.14159265358979323846f * SKY_SUN_RADIUS * SKY_SUN_RADIUS;
+        sun_r = mk3(SKY_SUN_COLOR[0] / area, SKY_SUN_COLOR[1] / area, SKY_SUN_COLOR[2] / area);
+    }
+    return add3(scl3(SKY_SUN_INTENSITY, add3(rp, mp)), mul3(tr, sun_r));
+}
+
+void port_sky_eval(const float *table, uint32_t w, uint32_t h, const float *cases, size_t n, float *out) {
+    tex_t t = {w, h, (float *)table};
+    for (size_t i = 0; i < n; ++i) {
+        const float *c = cases + 9 * i;
+        const f3 r = sky_eval(&t, mk3(c[0], c[1], c[2]), mk3(c[3], c[4], c[5]), mk3(c[6], c[7], c[8]));
+        out[3 * i] = r.x;
+        out[3 * i + 1] = r.y;
+        out[3 * i + 2] = r.z;
+    }
+}
+
+/* PathTracer::evalBackground (PathTracer.cpp:23-55): SKYBOX and ATMOSPHERE for every miss
+ * (the atmosphere at the ray's origin), COLOR and IMAGE for primary misses only. */
+static f3 background(const port_pt *s, f3 pos, f3 dir, float nx, float ny, int direct) {
     if (s->bg_mode == PT_BG_SKYBOX) return cubemap(s, norm3(dir));
+    if (s->bg_mode == PT_BG_ATMOSPHERE) return sky_eval(&s->sky, pos, norm3(dir), s->sun);
     if (!direct) return mk3(0, 0, 0);
     if (s->bg_mode == PT_BG_IMAGE) {
         const f4 c = rgbal(&s->tex[s->bg_tex[0]], nx, ny);
@@ -729,7 +899,7 @@ static void render_pixel(job_t *j, uint32_t x, uint32_t y) {
                     if (did > 0 && prev_pdf > 0.0f) wgt = mis_power(prev_pdf, s->p_env * env_pdf(s, dir));
                     color = add3(color, mul3(atten, scl3(wgt, env_radiance(s, dir))));
                 } else {
-                    color = add3(color, mul3(atten, background(s, dir, nx, ny, did == 0)));
+                    color = add3(color, mul3(atten, background(s, pos, dir, nx, ny, did == 0)));
                 }
                 break;
             }

@@ -33,6 +33,20 @@ int port_pt_render(port_pt *s, const pt_camera_desc *cam, uint32_t samples, uint
 int port_pt_set_environment(port_pt *s, uint32_t tex, float intensity);
 int port_pt_render_ex(port_pt *s, const pt_camera_desc *cam, uint32_t samples, uint32_t depth, uint64_t seed,
                       float *image, uint32_t w, uint32_t h, int threads, uint64_t *rays_out, int mode, float clamp);
+/* ATMOSPHERE background: table override (w x h RGBA floats); by default port_pt_commit
+ * computes the 512 x 512 table with 256 samples rounded to half precision, which is the
+ * reference's shipped resources/common/scattering-precomputed.exr as loaded. */
+#define PORT_SKY_TABLE_RES 512u
+#define PORT_SKY_TABLE_SAMPLES 256u
+int port_pt_set_sky_table(port_pt *s, const float *rgba, uint32_t w, uint32_t h);
+/* AtmosphereApp::precomputeTable: res x res RGBA floats; half_precision rounds every value
+ * to the nearest half (as stored in the reference's EXR). */
+void port_sky_table(uint32_t res, uint32_t samples, int half_precision, float *rgba);
+/* Round to the nearest IEEE half (ties to even), returned as float. */
+float port_round_half(float x);
+/* MaterialSky::eval for n cases {origin.xyz, direction.xyz (normalised), sun.xyz} with the
+ * given table; out = n x 3. */
+void port_sky_eval(const float *table, uint32_t w, uint32_t h, const float *cases, size_t n, float *out);
 /* MaterialGGX::eval / sampleAndEval with given uniforms (see include/rendu_gb300.h). */
 void port_ggx_eval(const float *cases, size_t n, float *out);
 void port_ggx_sample(const float *cases, const float *uniforms, size_t n, float *out);

@@ -12,6 +12,7 @@
 #include "raycaster/Raycaster.hpp"
 #include "PathTracer.hpp"
 #include "MaterialGGX.hpp"
+#include "MaterialSky.hpp"
 #include "generation/Random.hpp"
 #include "input/Camera.hpp"
 #include "resources/Texture.hpp"
@@ -25,6 +26,8 @@
 #include <cstring>
 #include <deque>
 #include <memory>
+
+Texture &shim_sky_table();  // oracle/ref_shim.cpp
 
 namespace {
 
@@ -301,7 +304,7 @@ int ref_pt_set_background(void *h, int mode, const float *color, const uint32_t 
 	} else if(mode == PT_BG_IMAGE) {
 		s.bgMaterial.addTexture(&s.textures[tex[0]]);
 		s.scene->backgroundMode = Scene::Background::IMAGE;
-	} else {
+	} else if(mode == PT_BG_SKYBOX) {
 		// A cubemap Texture with its six faces as images (+x,-x,+y,-y,+z,-z).
 		s.textures.emplace_back("ref_cube");
 		Texture &cube = s.textures.back();
@@ -314,6 +317,8 @@ int ref_pt_set_background(void *h, int mode, const float *color, const uint32_t 
 		cube.height = cube.images[0].height;
 		s.bgMaterial.addTexture(&cube);
 		s.scene->backgroundMode = Scene::Background::SKYBOX;
+	} else {
+		return -1;  // ATMOSPHERE needs a Sky object: its model is pinned through ref_sky_eval
 	}
 	return 0;
 }
@@ -367,4 +372,41 @@ int ref_pt_render(void *h, const pt_camera_desc *c, uint32_t spp, uint32_t depth
 	return 0;
 }
 
+
+// Image::load (Image.cpp:108-113) of a file, as the resources manager would load it for a
+// 2-D texture (no vertical flip); out receives w x h x channels floats (at most cap).
+int ref_load_image(const char *path, unsigned channels, float *out, size_t cap, uint32_t *w, uint32_t *h) {
+	Image img;
+	const int ret = img.load(path, channels, false, true);
+	if(ret != 0) return ret;
+	*w = img.width;
+	*h = img.height;
+	const size_t n = img.pixels.size() < cap ? img.pixels.size() : cap;
+	std::memcpy(out, img.pixels.data(), n * sizeof(float));
+	return 0;
+}
+
+// The table MaterialSky::eval reads (w x h RGBA floats).
+int ref_set_sky_table(const float *rgba, uint32_t w, uint32_t h) {
+	Texture &t = shim_sky_table();
+	t.images.clear();
+	t.images.emplace_back(w, h, 4, 0.0f);
+	std::memcpy(t.images.back().pixels.data(), rgba, sizeof(float) * 4 * size_t(w) * h);
+	t.width  = w;
+	t.height = h;
+	return 0;
+}
+
+// MaterialSky::eval (MaterialSky.cpp:6-87) for n cases {origin, direction, sun}: n x 3 out.
+int ref_sky_eval(const float *cases, size_t n, float *out) {
+	for(size_t i = 0; i < n; ++i) {
+		const float *c = cases + 9 * i;
+		const glm::vec3 r = MaterialSky::eval(glm::vec3(c[0], c[1], c[2]), glm::vec3(c[3], c[4], c[5]),
+											  glm::vec3(c[6], c[7], c[8]));
+		out[3 * i]	   = r.x;
+		out[3 * i + 1] = r.y;
+		out[3 * i + 2] = r.z;
+	}
+	return 0;
+}
 } // extern "C"

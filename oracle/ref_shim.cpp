@@ -10,8 +10,11 @@
 //  - Texture::sampleCubemap, the one piece of hot-path math that lives in Texture.cpp: it
 //    is RESTATED here from src/engine/resources/Texture.cpp:141-191 (same face order,
 //    same arithmetic) so that SKYBOX backgrounds can be rendered by the reference tracer;
-//  - aborting stubs for the loaders (scene files, meshes, textures from disk), which the
-//    oracle never reaches: scenes are assembled in memory by oracle/ref_capi.cpp.
+//  - the resources manager reduced to what MaterialSky::eval and Image::load reach: a
+//    singleton, the "scattering-precomputed" table (filled by oracle/ref_capi.cpp) and a
+//    plain file read (I/O only);
+//  - aborting stubs for the other loaders (scene files, meshes, textures from disk), which
+//    the oracle never reaches: scenes are assembled in memory by oracle/ref_capi.cpp.
 #include "resources/Mesh.hpp"
 #include "resources/Texture.hpp"
 #include "resources/ResourcesManager.hpp"
@@ -20,6 +23,7 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <new>
 
 class GPUMesh {};
 class GPUTexture {};
@@ -95,14 +99,41 @@ std::vector<std::string> Codable::encode(const glm::vec3 &) { shim_abort("Codabl
 std::vector<std::string> Codable::encode(const glm::vec4 &) { shim_abort("Codable::encode"); }
 
 // ---- Resources (src/engine/resources/ResourcesManager.cpp) ----------------------------
-Resources &Resources::manager() { shim_abort("Resources::manager"); }
+// The manager is built once in static storage and never destroyed: its maps hold types
+// (programs, fonts) whose destructors live in units the oracle does not compile.
+Resources &Resources::manager() {
+	alignas(Resources) static unsigned char storage[sizeof(Resources)];
+	static Resources *instance = new(storage) Resources();
+	return *instance;
+}
+
+// The sky's scattering table, served to MaterialSky::eval (MaterialSky.cpp:10).
+Texture &shim_sky_table() {
+	static Texture table("scattering-precomputed");
+	return table;
+}
 const Mesh *Resources::getMesh(const std::string &, Storage) { shim_abort("Resources::getMesh"); }
 char *Resources::getRawData(const std::string &, size_t &) { shim_abort("Resources::getRawData"); }
-const Texture *Resources::getTexture(const std::string &, const Layout &, Storage, const std::string &) {
+const Texture *Resources::getTexture(const std::string &name, const Layout &, Storage, const std::string &) {
+	if(name == "scattering-precomputed") return &shim_sky_table();
 	shim_abort("Resources::getTexture");
 }
-char *Resources::loadRawDataFromExternalFile(const std::string &, size_t &) {
-	shim_abort("Resources::loadRawDataFromExternalFile");
+char *Resources::loadRawDataFromExternalFile(const std::string &path, size_t &size) {
+	size = 0;
+	FILE *f = std::fopen(path.c_str(), "rb");
+	if(!f) return nullptr;
+	std::fseek(f, 0, SEEK_END);
+	const long len = std::ftell(f);
+	std::fseek(f, 0, SEEK_SET);
+	char *data = len > 0 ? static_cast<char *>(std::malloc(size_t(len))) : nullptr;
+	if(data && std::fread(data, 1, size_t(len), f) == size_t(len)) {
+		size = size_t(len);
+	} else {
+		std::free(data);
+		data = nullptr;
+	}
+	std::fclose(f);
+	return data;
 }
 std::string Resources::loadStringFromExternalFile(const std::string &) {
 	shim_abort("Resources::loadStringFromExternalFile");

@@ -22,6 +22,10 @@ RT_ERR_OVERFLOW = 6
 RT_FLAG_DEVICE_PTRS = 0x1
 PT_MODE_REFERENCE = 0
 PT_MODE_EXTENDED = 1
+PT_BG_COLOR = 0
+PT_BG_IMAGE = 1
+PT_BG_SKYBOX = 2
+PT_BG_ATMOSPHERE = 3
 RT_NO_HIT = 0xFFFFFFFF
 
 _STATUS_NAMES = {1: "RT_ERR_ARG", 2: "RT_ERR_OOM", 3: "RT_ERR_CUDA", 4: "RT_ERR_TIMEOUT", 5: "RT_ERR_STATE",
@@ -129,6 +133,9 @@ _SIGS = {
     "pt_scene_raycaster": ([_VP], _VP),
     "pt_material_eval": ([_VP, C.c_size_t, _VP, C.c_int], C.c_int),
     "pt_material_sample": ([_VP, _VP, C.c_size_t, _VP, C.c_int], C.c_int),
+    "pt_scene_set_sky_table": ([_VP, _VP, C.c_uint32, C.c_uint32], C.c_int),
+    "pt_sky_table": ([C.c_uint32, C.c_uint32, C.c_int32, _VP, C.c_int], C.c_int),
+    "pt_sky_eval": ([_VP, C.c_uint32, C.c_uint32, _VP, C.c_size_t, _VP, C.c_int], C.c_int),
     "dn_create": ([C.POINTER(C.c_void_p), C.c_int], C.c_int),
     "dn_destroy": ([_VP], C.c_int),
     "dn_init": ([_VP, C.c_uint64], C.c_int),

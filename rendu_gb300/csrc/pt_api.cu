@@ -105,7 +105,7 @@ int pt_scene_destroy(pt_scene *s) {
     if (s->rc) rt_destroy(s->rc);
     for (DevBuf *b : {&s->d_positions, &s->d_emitters, &s->d_emitter_cdf, &s->d_env_marg, &s->d_env_cond,
                       &s->d_env_func, &s->d_objects, &s->d_meshes, &s->d_materials, &s->d_tex, &s->d_texels, &s->d_normals,
-                      &s->d_tangents, &s->d_bitangents, &s->d_uvs, &s->d_indices, &s->d_lights})
+                      &s->d_tangents, &s->d_bitangents, &s->d_uvs, &s->d_indices, &s->d_lights, &s->d_sky})
         b->release();
     s->engine.reset();
     delete s;
@@ -199,10 +199,33 @@ int pt_scene_set_background(pt_scene *s, int32_t mode, const float *color, const
             if (tex[k] >= s->textures.size()) return arg_error("background texture id out of range");
             s->bg_tex[k] = tex[k];
         }
+    } else if (mode == PT_BG_ATMOSPHERE) {
+        // Sky::decode / Sky::update normalise the sun direction (Sky.cpp:16, 35).
+        if (!color) return arg_error("ATMOSPHERE background needs the sun direction");
+        const float d = (color[0] * color[0] + color[1] * color[1]) + color[2] * color[2];
+        if (!(d > 0.0f) || !std::isfinite(d)) return arg_error("invalid sun direction");
+        const float k = 1.0f / std::sqrt(d);
+        for (int c = 0; c < 3; ++c) s->sun[c] = color[c] * k;
     } else {
         return arg_error("unsupported background mode");
     }
     s->bg_mode = mode;
+    s->committed = false;
+    return RT_OK;
+}
+
+int pt_scene_set_sky_table(pt_scene *s, const float *rgba, uint32_t width, uint32_t height) {
+    clear_error();
+    if (!s) return arg_error("null scene");
+    if (!rgba) {
+        s->sky_table.clear();
+        s->sky_w = s->sky_h = 0;
+    } else {
+        if (width == 0 || height == 0 || (uint64_t)width * height > (1u << 24)) return arg_error("invalid table size");
+        s->sky_table.assign(rgba, rgba + 4 * (size_t)width * height);
+        s->sky_w = width;
+        s->sky_h = height;
+    }
     s->committed = false;
     return RT_OK;
 }
@@ -439,6 +462,27 @@ int pt_scene_commit(pt_scene *s) {
     d.env_func = s->d_env_func.as<float>();
     d.env_integral = (float)eint;
     d.p_env = d.env_tex >= 0 ? (d.nemitters > 0 ? 0.5f : 1.0f) : 0.0f;
+    // ATMOSPHERE: the caller's scattering table, or the reference's (512 x 512, 256 steps,
+    // half precision) computed here.
+    std::memcpy(d.sun, s->sun, sizeof(d.sun));
+    d.sky = nullptr;
+    d.sky_w = d.sky_h = 0;
+    if (s->bg_mode == PT_BG_ATMOSPHERE) {
+        const bool given = !s->sky_table.empty();
+        const uint32_t w = given ? s->sky_w : kSkyTableRes, h = given ? s->sky_h : kSkyTableRes;
+        if (s->d_sky.reserve((size_t)w * h * sizeof(float4)) != RT_OK) return RT_ERR_OOM;
+        if (given) {
+            RT_CUDA_TRY(cudaMemcpy(s->d_sky.ptr, s->sky_table.data(), s->sky_table.size() * sizeof(float),
+                                   cudaMemcpyHostToDevice));
+        } else {
+            const int r = pt_launch_sky_table(kSkyTableRes, kSkyTableSamples, true, s->d_sky.as<float4>(), 0);
+            if (r != RT_OK) return r;
+            RT_CUDA_TRY(cudaDeviceSynchronize());
+        }
+        d.sky = s->d_sky.as<float4>();
+        d.sky_w = w;
+        d.sky_h = h;
+    }
     s->committed = true;
     return RT_OK;
 }
@@ -480,6 +524,64 @@ int pt_material_sample(const float *cases, const float *uniforms, size_t n, floa
     clear_error();
     if (!uniforms) return arg_error("null uniforms");
     return material_batch(cases, 8, uniforms, n, out, 6, device);
+}
+
+static int check_device(int device) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
+        cudaGetLastError();
+        set_error("CUDA device " + std::to_string(device) + " is not available");
+        return RT_ERR_CUDA;
+    }
+    return RT_OK;
+}
+
+int pt_sky_table(uint32_t res, uint32_t samples, int32_t half_precision, float *out, int device) {
+    clear_error();
+    if (!out || res < 2 || res > 4096 || samples == 0) return arg_error("invalid table request");
+    int r = check_device(device);
+    if (r != RT_OK) return r;
+    DeviceGuard g(device);
+    DevBuf t;
+    if ((r = t.reserve((size_t)res * res * sizeof(float4))) != RT_OK) return r;
+    r = pt_launch_sky_table(res, samples, half_precision != 0, t.as<float4>(), 0);
+    if (r == RT_OK && cudaMemcpy(out, t.ptr, (size_t)res * res * sizeof(float4), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        set_error(std::string("sky table failed: ") + cudaGetErrorString(cudaGetLastError()));
+        r = RT_ERR_CUDA;
+    }
+    t.release();
+    return r;
+}
+
+int pt_sky_eval(const float *table, uint32_t width, uint32_t height, const float *cases, size_t n, float *out,
+                int device) {
+    clear_error();
+    if (!cases || !out || n >= (1ull << 31)) return arg_error("null argument or too many cases");
+    if (table && (width == 0 || height == 0)) return arg_error("invalid table size");
+    int r = check_device(device);
+    if (r != RT_OK || n == 0) return r;
+    DeviceGuard g(device);
+    const uint32_t w = table ? width : kSkyTableRes, h = table ? height : kSkyTableRes;
+    DevBuf t, dc, dout;
+    if ((r = t.reserve((size_t)w * h * sizeof(float4))) || (r = dc.reserve(n * 9 * sizeof(float))) ||
+        (r = dout.reserve(n * 3 * sizeof(float)))) {
+        t.release(); dc.release(); dout.release();
+        return r;
+    }
+    if (table) {
+        if (cudaMemcpy(t.ptr, table, (size_t)w * h * sizeof(float4), cudaMemcpyHostToDevice) != cudaSuccess)
+            r = RT_ERR_CUDA;
+    } else {
+        r = pt_launch_sky_table(w, kSkyTableSamples, true, t.as<float4>(), 0);
+    }
+    if (r == RT_OK && cudaMemcpy(dc.ptr, cases, n * 9 * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+        r = RT_ERR_CUDA;
+    if (r == RT_OK) r = pt_launch_sky_eval(t.as<float4>(), w, h, dc.as<float>(), (uint32_t)n, dout.as<float>(), 0);
+    if (r == RT_OK && cudaMemcpy(out, dout.ptr, n * 3 * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+        r = RT_ERR_CUDA;
+    if (r == RT_ERR_CUDA) set_error(std::string("sky evaluation failed: ") + cudaGetErrorString(cudaGetLastError()));
+    t.release(); dc.release(); dout.release();
+    return r;
 }
 
 rt_ctx *pt_scene_raycaster(pt_scene *s) { return s ? s->rc : nullptr; }

@@ -124,6 +124,10 @@ struct PtScene {
     const float *env_func;     // env_h x env_w piecewise-constant weights
     float env_integral;        // mean of env_func over the unit square
     float p_env;               // probability of sampling the environment in NEE
+    // ATMOSPHERE background: normalised sun direction and the scattering table.
+    float sun[3];
+    const float4 *sky;
+    uint32_t sky_w, sky_h;
 };
 
 // ---- textures ----------------------------------------------------------------------------
@@ -184,10 +188,103 @@ __device__ __forceinline__ f3 cubemap(const PtScene &s, f3 dir) {
     return mk(c.x, c.y, c.z);
 }
 
+// ---- atmosphere (MaterialSky.cpp:6-98; parameters Sky.hpp:53-65) ----------------------------
+// Evaluated in the reference's operation order in a unit compiled without FMA contraction.
+namespace sky {
+constexpr float kGround = 6371e3f, kTop = 6471e3f, kSunIntensity = 20.0f, kMie = 21e-6f;
+constexpr float kHRayleigh = 8000.0f, kHMie = 1200.0f, kGMie = 0.758f, kSunRadius = 0.04675f;
+constexpr float kSunRadiusCos = 0.998f, kPi = 3.14159265358979323846f;
+constexpr int kSteps = 16;  // MaterialSky::samplesCount
+__device__ __forceinline__ f3 rayleigh_k() { return mk(5.5e-6f, 13.0e-6f, 22.4e-6f); }
+__device__ __forceinline__ f3 sun_color() { return mk(1.474f, 1.8504f, 1.91198f); }
+}  // namespace sky
+
+// Intersection::sphere (Intersection.cpp:7-20).
+__device__ __forceinline__ bool sphere_roots(f3 o, f3 d, float radius, float &r0, float &r1) {
+    const float a = dot(d, d), b = dot(o, d), c = dot(o, o) - radius * radius;
+    const float delta = b * b - a * c;
+    if (delta < 0.0f) return false;
+    const float ds = sqrtf(delta);
+    r0 = (-b - ds) / a;
+    r1 = (-b + ds) / a;
+    return true;
+}
+
+// Image::rgbl (Image.cpp:64-84) on the scattering table.
+__device__ __forceinline__ f3 sky_rgbl(const float4 *t, uint32_t w, uint32_t h, float x, float y) {
+    const float xi = x * (float)w, yi = y * (float)h;
+    const float xb = floorf(xi), yb = floorf(yi);
+    const float dx = xi - xb, dy = yi - yb;
+    const int x0 = mod_pos(f2i_sat(xb), (int)w), y0 = mod_pos(f2i_sat(yb), (int)h);
+    const int x1 = mod_pos(f2i_sat(xb) + 1, (int)w), y1 = mod_pos(f2i_sat(yb) + 1, (int)h);
+    const float4 p00 = t[(size_t)y0 * w + x0], p01 = t[(size_t)y1 * w + x0];
+    const float4 p10 = t[(size_t)y0 * w + x1], p11 = t[(size_t)y1 * w + x1];
+    return mk((1.0f - dx) * ((1.0f - dy) * p00.x + dy * p01.x) + dx * ((1.0f - dy) * p10.x + dy * p11.x),
+              (1.0f - dx) * ((1.0f - dy) * p00.y + dy * p01.y) + dx * ((1.0f - dy) * p10.y + dy * p11.y),
+              (1.0f - dx) * ((1.0f - dy) * p00.z + dy * p01.z) + dx * ((1.0f - dy) * p10.z + dy * p11.z));
+}
+
+__device__ __forceinline__ float rayleigh_phase(float c) {
+    const float k = 1.0f / (4.0f * sky::kPi);
+    return k * 3.0f / 4.0f * (1.0f + c * c);
+}
+__device__ __forceinline__ float mie_phase(float c) {
+    const float k = 1.0f / (4.0f * sky::kPi);
+    const float g2 = sky::kGMie * sky::kGMie;
+    return k * 3.0f * (1.0f - g2) / (2.0f * (2.0f + g2)) * (1.0f + c * c) /
+           powf(1.0f + g2 - 2.0f * sky::kGMie * c, 3.0f / 2.0f);
+}
+
+// MaterialSky::eval: 16-step single-scattering march through the atmosphere along the ray
+// (planet centre 6371 km + 1 m below the origin), secondary attenuation from the table,
+// plus the sun disc when the ray does not hit the ground.
+__device__ __forceinline__ f3 sky_eval(const float4 *table, uint32_t tw, uint32_t th, f3 origin, f3 dir, f3 sun) {
+    const f3 planet = (origin + mk(0.0f, sky::kGround, 0.0f)) + mk(0.0f, 1.0f, 0.0f);
+    float t0 = 0.0f, t1 = 0.0f, g0 = 0.0f, g1 = 0.0f;
+    if (!sphere_roots(planet, dir, sky::kTop, t0, t1)) return mk(0.0f, 0.0f, 0.0f);
+    const bool ground = sphere_roots(planet, dir, sky::kGround, g0, g1);
+    const float dist = gmin(t1, ground ? g0 : 0.0f);
+    const float step = (dist - t0) / (float)sky::kSteps;
+    const float cos_vs = dot(dir, sun);
+    const f3 kr = sky::rayleigh_k();
+    float rd = 0.0f, md = 0.0f;
+    f3 rs = mk(0, 0, 0), ms = mk(0, 0, 0), tr = mk(0, 0, 0);
+    for (int i = 0; i < sky::kSteps; ++i) {
+        const f3 p = planet + (((float)i + 0.5f) * step) * dir;
+        float hgt = sqrtf(dot(p, p)) - sky::kGround;
+        if (i == sky::kSteps - 1 && hgt < 0.0f) hgt = 0.0f;
+        const float rstep = expf(-hgt / sky::kHRayleigh) * step;
+        const float mstep = expf(-hgt / sky::kHMie) * step;
+        rd += rstep;
+        md += mstep;
+        const f3 direct = mk(expf(-(md * sky::kMie + rd * kr.x)), expf(-(md * sky::kMie + rd * kr.y)),
+                             expf(-(md * sky::kMie + rd * kr.z)));
+        const float rel_h = (sqrtf(dot(p, p)) - sky::kGround) / (sky::kTop - sky::kGround);
+        const float rel_c = -0.5f * sun.y + 0.5f;
+        float u = (511.0f / 512.0f) * rel_h + 0.5f / 512.0f, v = (511.0f / 512.0f) * rel_c + 0.5f / 512.0f;
+        u = gmin(gmax(u, 0.5f / 512.0f), 511.0f / 512.0f);  // glm::clamp
+        v = gmin(gmax(v, 0.5f / 512.0f), 511.0f / 512.0f);
+        const f3 att = direct * sky_rgbl(table, tw, th, u, v);
+        rs += rstep * att;
+        ms += mstep * att;
+        tr += direct;
+    }
+    const f3 rp = (rayleigh_phase(cos_vs) * kr) * rs;
+    const f3 mp = (sky::kMie * mie_phase(cos_vs)) * ms;
+    f3 sun_r = mk(0.0f, 0.0f, 0.0f);
+    if (!(ground && g1 > 0.0f) && dot(dir, sun) > sky::kSunRadiusCos)
+        sun_r = sky::sun_color() / (sky::kPi * sky::kSunRadius * sky::kSunRadius);
+    return sky::kSunIntensity * (rp + mp) + tr * sun_r;
+}
+
 // PathTracer::evalBackground (PathTracer.cpp:23-55): COLOR and IMAGE only for primary
-// misses (IMAGE indexed by the screen position), SKYBOX for every miss.
-__device__ __forceinline__ f3 eval_background(const PtScene &s, f3 dir, float ndc_x, float ndc_y, bool direct) {
+// misses (IMAGE indexed by the screen position), SKYBOX and ATMOSPHERE (at the ray's
+// origin) for every miss.
+__device__ __forceinline__ f3 eval_background(const PtScene &s, f3 pos, f3 dir, float ndc_x, float ndc_y,
+                                              bool direct) {
     if (s.bg_mode == PT_BG_SKYBOX) return cubemap(s, normalize(dir));
+    if (s.bg_mode == PT_BG_ATMOSPHERE)
+        return sky_eval(s.sky, s.sky_w, s.sky_h, pos, xnormalize(dir), mk(s.sun[0], s.sun[1], s.sun[2]));
     if (!direct) return mk(0.0f, 0.0f, 0.0f);
     if (s.bg_mode == PT_BG_IMAGE) {
         const float4 c = tex_rgbal(s, s.bg_tex[0], ndc_x, ndc_y);

@@ -18,6 +18,8 @@
 //   wave_end   -- advance the wave index.
 // The whole per-wave sequence reads its wave from device memory, so it is captured once in
 // a CUDA graph and replayed for every wave (pt_engine.cu).
+#include <cuda_fp16.h>
+
 #include "pt_scene.hpp"
 #include "rt_traverse.cuh"
 
@@ -166,7 +168,7 @@ __global__ void __launch_bounds__(128) k_shade(PtWave w, int cur, uint32_t did) 
         } else {
             // PathTracer.cpp:206-209.
             const float2 ndc = w.ndc[path];
-            color += atten * eval_background(s, dir, ndc.x, ndc.y, did == 0);
+            color += atten * eval_background(s, pos, dir, ndc.x, ndc.y, did == 0);
         }
     } else {
         const SurfaceHit sh = surface(s, hit.prim, hit.u, hit.v);
@@ -539,6 +541,63 @@ __global__ void k_mat_sample(const float *__restrict__ c, const float *__restric
 }
 
 }  // namespace
+
+// AtmosphereApp::precomputeTable (AtmosphereApp.cpp:145-188): the sky's secondary
+// attenuation towards the sun, x = relative height, y = cosine of the sun's vertical angle;
+// optionally rounded to half precision like the reference's stored table.
+__global__ void k_sky_table(uint32_t res, uint32_t samples, int half_prec, float4 *__restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= res * res) return;
+    const uint32_t x = i % res, y = i / res;
+    const float xf = (float)x / ((float)res - 1.0f), yf = (float)y / ((float)res - 1.0f);
+    const f3 pos = mk(0.0f, (sky::kTop - sky::kGround) * xf + sky::kGround, 0.0f);
+    const float cosA = 2.0f * yf - 1.0f;
+    const float sinA = sqrtf(1.0f - cosA * cosA);
+    const f3 sun = -xnormalize(mk(sinA, cosA, 0.0f));
+    float r0 = 0.0f, r1 = 0.0f;
+    const bool hit = sphere_roots(pos, sun, sky::kTop, r0, r1);
+    const float step = hit ? r1 / (float)samples : 0.0f;
+    float rd = 0.0f, md = 0.0f;
+    for (uint32_t j = 0; j < samples; ++j) {
+        const f3 p = pos + (((float)j + 0.5f) * step) * sun;
+        const float hgt = sqrtf(dot(p, p)) - sky::kGround;
+        rd += expf(-hgt / sky::kHRayleigh) * step;
+        md += expf(-hgt / sky::kHMie) * step;
+    }
+    const f3 kr = sky::rayleigh_k();
+    float a[3] = {expf(-(sky::kMie * md + kr.x * rd)), expf(-(sky::kMie * md + kr.y * rd)),
+                  expf(-(sky::kMie * md + kr.z * rd))};
+    if (half_prec)
+        for (int c = 0; c < 3; ++c) a[c] = __half2float(__float2half_rn(a[c]));
+    out[i] = make_float4(a[0], a[1], a[2], 1.0f);
+}
+
+// MaterialSky::eval for n cases {origin.xyz, direction.xyz, sun.xyz}.
+__global__ void k_sky_eval(const float4 *__restrict__ table, uint32_t w, uint32_t h, const float *__restrict__ cases,
+                           uint32_t n, float *__restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *c = cases + 9 * (size_t)i;
+    const f3 r = sky_eval(table, w, h, mk(c[0], c[1], c[2]), mk(c[3], c[4], c[5]), mk(c[6], c[7], c[8]));
+    out[3 * (size_t)i] = r.x;
+    out[3 * (size_t)i + 1] = r.y;
+    out[3 * (size_t)i + 2] = r.z;
+}
+
+int pt_launch_sky_table(uint32_t res, uint32_t samples, bool half_prec, float4 *out, cudaStream_t st) {
+    const uint32_t n = res * res;
+    k_sky_table<<<(n + 255) / 256, 256, 0, st>>>(res, samples, half_prec ? 1 : 0, out);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pt_launch_sky_eval(const float4 *table, uint32_t w, uint32_t h, const float *cases, uint32_t n, float *out,
+                       cudaStream_t st) {
+    if (n == 0) return RT_OK;
+    k_sky_eval<<<(n + 127) / 128, 128, 0, st>>>(table, w, h, cases, n, out);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
 
 int pt_launch_material(const float *cases, const float *uniforms, uint32_t n, float *out, cudaStream_t st) {
     if (n == 0) return RT_OK;

@@ -71,6 +71,12 @@ struct HostObject {
 };
 
 int pt_launch_material(const float *cases, const float *uniforms, uint32_t n, float *out, cudaStream_t st);
+// The sky's scattering table (res x res, `samples` march steps, half-precision rounding
+// optional) and MaterialSky::eval over n cases {origin, direction, sun}.
+constexpr uint32_t kSkyTableRes = 512, kSkyTableSamples = 256;
+int pt_launch_sky_table(uint32_t res, uint32_t samples, bool half_prec, float4 *out, cudaStream_t st);
+int pt_launch_sky_eval(const float4 *table, uint32_t w, uint32_t h, const float *cases, uint32_t n, float *out,
+                       cudaStream_t st);
 int pt_launch_wave_begin(const PtWave &w, cudaStream_t st);
 int pt_launch_wave_end(const PtWave &w, cudaStream_t st);
 int pt_launch_raygen(const PtWave &w, cudaStream_t st);
@@ -157,6 +163,10 @@ struct pt_scene {
         d_uvs, d_indices, d_lights, d_emitters, d_emitter_cdf, d_env_marg, d_env_cond, d_env_func;
     int env_tex = -1;
     float env_intensity = 1.0f;
+    float sun[3] = {0.0f, 1.0f, 0.0f};  // ATMOSPHERE: normalised sun direction
+    std::vector<float> sky_table;      // ATMOSPHERE: caller's table (RGBA), empty = computed
+    uint32_t sky_w = 0, sky_h = 0;
+    rgb::DevBuf d_sky;
     rgb::PtScene dev{};
 
     std::unique_ptr<rgb::WaveEngine> engine;  // runs pt_render

@@ -75,6 +75,10 @@ class PathTracer:
         bg = sc.background
         L.call("pt_scene_set_background", self._h, int(bg["mode"]), _f3(bg.get("color", (0, 0, 0))),
                (C.c_uint32 * 6)(*bg.get("tex", (0,) * 6)))
+        if bg.get("sky_table") is not None:  # ATMOSPHERE: a caller-supplied scattering table
+            t = np.ascontiguousarray(bg["sky_table"], np.float32)
+            self._keep.append(t)
+            L.call("pt_scene_set_sky_table", self._h, t.ctypes.data, t.shape[1], t.shape[0])
         if getattr(sc, "environment", None) is not None:
             L.call("pt_scene_set_environment", self._h, int(sc.environment["tex"]),
                    float(sc.environment.get("intensity", 1.0)))
@@ -137,6 +141,27 @@ def material_eval(cases):
     c = np.ascontiguousarray(cases, np.float32).reshape(-1, 11)
     out = np.zeros((len(c), 3), np.float32)
     L.call("pt_material_eval", c.ctypes.data, len(c), out.ctypes.data, 0)
+    return out
+
+
+def sky_table(res: int = 512, samples: int = 256, half: bool = True, device: int = 0):
+    """AtmosphereApp::precomputeTable on the device: (res, res, 4) float32."""
+    out = np.zeros((res, res, 4), np.float32)
+    L.call("pt_sky_table", int(res), int(samples), int(bool(half)), out.ctypes.data, int(device))
+    return out
+
+
+def sky_eval(cases, table=None, device: int = 0):
+    """MaterialSky::eval on the device for cases (n, 9) {origin, direction, sun}; table
+    (h, w, 4) float32 or None for the default table."""
+    c = np.ascontiguousarray(cases, np.float32).reshape(-1, 9)
+    out = np.zeros((len(c), 3), np.float32)
+    if table is None:
+        L.call("pt_sky_eval", None, 0, 0, c.ctypes.data, len(c), out.ctypes.data, int(device))
+    else:
+        t = np.ascontiguousarray(table, np.float32)
+        L.call("pt_sky_eval", t.ctypes.data, t.shape[1], t.shape[0], c.ctypes.data, len(c), out.ctypes.data,
+               int(device))
     return out
 
 

@@ -632,3 +632,11 @@ def random_cameras(seed: int, count: int, ratio: float = 1.0):
         cams.append({"eye": eye, "center": center, "up": (0.0, 1.0, 0.0), "fov": float(rng.uniform(0.6, 1.2)),
                      "ratio": ratio})
     return cams
+
+
+def atmosphere(scene: Scene, sun=(0.3, 0.6, -0.5), table=None) -> Scene:
+    """Give `scene` the reference's ATMOSPHERE background (Scene::Background::ATMOSPHERE with
+    a Sky object): MaterialSky's sky for the given sun direction, optionally with a
+    caller-supplied scattering table (h, w, 4)."""
+    scene.background = {"mode": 3, "color": tuple(float(x) for x in sun), "tex": (0,) * 6, "sky_table": table}
+    return scene

@@ -7,6 +7,7 @@ the reference tree is only needed to regenerate them:
 
     python tests/golden/make_golden.py            (needs the reference tree)
     python tests/golden/make_golden.py --renders  (reference path-tracer renders)
+    python tests/golden/make_golden.py --sky      (the sky's scattering table and MaterialSky)
 """
 from __future__ import annotations
 
@@ -160,7 +161,7 @@ def make_camera():
     print("camera.npz: 16 cameras")
 
 
-if __name__ == "__main__" and "--renders" not in sys.argv:
+if __name__ == "__main__" and "--renders" not in sys.argv and "--sky" not in sys.argv:
     if O.build_ref() is None:
         sys.exit("the reference tree is needed to regenerate the fixtures")
     make_raycaster()
@@ -190,3 +191,37 @@ def make_renders():
 
 if __name__ == "__main__" and "--renders" in sys.argv:
     make_renders()
+
+
+def sky_cases(n=3000, seed=SEED):
+    """Rays for MaterialSky::eval: origins near the ground (heights 0-120), directions on the
+    sphere, a quarter of them aimed within the sun's disc, suns above and below the horizon."""
+    rng = np.random.default_rng(seed)
+    o = np.stack([rng.uniform(-60, 60, n), rng.uniform(0, 120, n), rng.uniform(-60, 60, n)], 1)
+    sun = rng.normal(size=(n, 3))
+    sun[: 3 * n // 4, 1] = np.abs(sun[: 3 * n // 4, 1])
+    sun /= np.linalg.norm(sun, axis=1, keepdims=True)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    k = n // 4
+    d[:k] = sun[:k] + rng.normal(scale=0.02, size=(k, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.concatenate([o, d, sun], 1).astype(np.float32)
+
+
+def make_sky(exr):
+    """The reference's scattering table (resources/common/scattering-precomputed.exr, read by
+    its own Image::load) and its MaterialSky::eval on seeded rays with that table."""
+    table = O.ref_load_image(exr, 4)
+    cases = sky_cases()
+    out = O.ref_sky_eval(table, cases)
+    np.savez_compressed(os.path.join(HERE, "sky.npz"), table_sub=table[::8, ::8, :3], table_shape=np.array(table.shape),
+                        table_row_sums=table[..., :3].astype(np.float64).sum(axis=1), cases=cases, eval_out=out)
+    print("sky.npz:", table.shape, len(cases), "cases")
+
+
+if __name__ == "__main__" and "--sky" in sys.argv:
+    if O.build_ref() is None:
+        sys.exit("the reference tree is needed to regenerate the fixtures")
+    make_sky(os.path.join(os.environ.get("RENDU_REFERENCE_ROOT", O.REF_ROOT_DEFAULT), "resources", "common",
+                          "scattering-precomputed.exr"))
