@@ -356,6 +356,16 @@ RT_API int pt_material_eval(const float *cases, size_t n, float *out, int device
  * out = n x 6 floats {weight.rgb, wi.xyz}. */
 RT_API int pt_material_sample(const float *cases, const float *uniforms, size_t n, float *out, int device);
 
+/* Write a render to disk as the reference's command-line renderer does after
+ * PathTracer::render (main.cpp:106-119): a path ending in ".exr" gets the linear image as
+ * half-precision channels (Image::saveAsHDR, Image.cpp:162-290; at least 16 x 16 pixels);
+ * any other path a PNG of 8-bit sRGB-approximated values (Image::saveAsLDR, Image.cpp:
+ * 126-160: v^(1/2.2), 255 v clamped and truncated; alpha 255), after the tone map
+ * 1 - exp(-c) of main.cpp:109-116 when `tonemap` != 0. image: width x height x components
+ * floats (host; 3 or 4 components for PNG, 1 to 4 for EXR). */
+RT_API int pt_image_save(const float *image, uint32_t width, uint32_t height, uint32_t components, const char *path,
+                         int32_t tonemap);
+
 /* AtmosphereApp::precomputeTable on device `device`: res x res RGBA floats into `out` (host),
  * `samples` march steps, rounded to half precision when half_precision != 0. */
 RT_API int pt_sky_table(uint32_t res, uint32_t samples, int32_t half_precision, float *out, int device);

@@ -449,3 +449,12 @@ def ref_sky_eval(table, cases) -> np.ndarray:
     out = np.zeros((len(c), 3), np.float32)
     lib.ref_sky_eval(c.reshape(-1), len(c), out.reshape(-1))
     return out
+
+
+def ref_save_image(image, path: str) -> int:
+    """The reference's Image::save with renderOneShot's options (main.cpp:119)."""
+    lib = ref_lib()
+    lib.ref_save_image.argtypes = [_f32p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_char_p]
+    a = np.ascontiguousarray(image, np.float32)
+    h, w, c = a.shape
+    return lib.ref_save_image(a.reshape(-1), w, h, c, path.encode())

@@ -409,4 +409,12 @@ int ref_sky_eval(const float *cases, size_t n, float *out) {
 	}
 	return 0;
 }
+
+// Image::save (Image.cpp:115-120) of w x h x c floats with the options renderOneShot uses
+// (SRGB_LDR | IGNORE_ALPHA, main.cpp:119).
+int ref_save_image(const float *px, uint32_t w, uint32_t h, uint32_t c, const char *path) {
+	Image img(w, h, c, 0.0f);
+	std::memcpy(img.pixels.data(), px, sizeof(float) * size_t(w) * h * c);
+	return img.save(path, Image::Save::SRGB_LDR | Image::Save::IGNORE_ALPHA);
+}
 } // extern "C"

@@ -11,8 +11,8 @@
 //    is RESTATED here from src/engine/resources/Texture.cpp:141-191 (same face order,
 //    same arithmetic) so that SKYBOX backgrounds can be rendered by the reference tracer;
 //  - the resources manager reduced to what MaterialSky::eval and Image::load reach: a
-//    singleton, the "scattering-precomputed" table (filled by oracle/ref_capi.cpp) and a
-//    plain file read (I/O only);
+//    singleton, the "scattering-precomputed" table (filled by oracle/ref_capi.cpp) and
+//    plain file reads and writes (I/O only);
 //  - aborting stubs for the other loaders (scene files, meshes, textures from disk), which
 //    the oracle never reaches: scenes are assembled in memory by oracle/ref_capi.cpp.
 #include "resources/Mesh.hpp"
@@ -138,6 +138,9 @@ char *Resources::loadRawDataFromExternalFile(const std::string &path, size_t &si
 std::string Resources::loadStringFromExternalFile(const std::string &) {
 	shim_abort("Resources::loadStringFromExternalFile");
 }
-void Resources::saveRawDataToExternalFile(const std::string &, char *, size_t) {
-	shim_abort("Resources::saveRawDataToExternalFile");
+void Resources::saveRawDataToExternalFile(const std::string &path, char *data, size_t size) {
+	FILE *f = std::fopen(path.c_str(), "wb");
+	if(!f) return;
+	std::fwrite(data, 1, size, f);
+	std::fclose(f);
 }

@@ -144,6 +144,16 @@ def material_eval(cases):
     return out
 
 
+def save_image(image, path: str, tonemap: bool = True) -> None:
+    """Write a render as renderOneShot does (main.cpp:106-119): ".exr" -> linear half-float
+    EXR; otherwise PNG of 1 - exp(-c) (tonemap) with the reference's 8-bit sRGB conversion."""
+    img = np.ascontiguousarray(image, np.float32)
+    if img.ndim == 2:
+        img = img[..., None]
+    h, w, c = img.shape
+    L.call("pt_image_save", img.ctypes.data, w, h, c, str(path).encode(), int(bool(tonemap)))
+
+
 def sky_table(res: int = 512, samples: int = 256, half: bool = True, device: int = 0):
     """AtmosphereApp::precomputeTable on the device: (res, res, 4) float32."""
     out = np.zeros((res, res, 4), np.float32)

@@ -8,6 +8,7 @@ the reference tree is only needed to regenerate them:
     python tests/golden/make_golden.py            (needs the reference tree)
     python tests/golden/make_golden.py --renders  (reference path-tracer renders)
     python tests/golden/make_golden.py --sky      (the sky's scattering table and MaterialSky)
+    python tests/golden/make_golden.py --image    (8-bit output of renderOneShot)
 """
 from __future__ import annotations
 
@@ -161,7 +162,7 @@ def make_camera():
     print("camera.npz: 16 cameras")
 
 
-if __name__ == "__main__" and "--renders" not in sys.argv and "--sky" not in sys.argv:
+if __name__ == "__main__" and not {"--renders", "--sky", "--image"} & set(sys.argv):
     if O.build_ref() is None:
         sys.exit("the reference tree is needed to regenerate the fixtures")
     make_raycaster()
@@ -225,3 +226,35 @@ if __name__ == "__main__" and "--sky" in sys.argv:
         sys.exit("the reference tree is needed to regenerate the fixtures")
     make_sky(os.path.join(os.environ.get("RENDU_REFERENCE_ROOT", O.REF_ROOT_DEFAULT), "resources", "common",
                           "scattering-precomputed.exr"))
+
+
+def image_io_input(seed=SEED):
+    """A 40 x 24 RGB image covering saveAsLDR's cases: values in [0, 1.3] (clamping above 1),
+    negatives, exact 8-bit boundaries k/255, zeros and a NaN."""
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(0.0, 1.3, (24, 40, 3)).astype(np.float32)
+    x[0, :10] = -rng.uniform(0, 1, (10, 3))
+    x[1, :, :] = (np.arange(40 * 3).reshape(40, 3) % 256 / 255.0) ** 2.2
+    x[2, 0, 0] = np.nan
+    x[3, :5] = 0.0
+    return x
+
+
+def make_image_io():
+    """The reference's Image::save with renderOneShot's options (main.cpp:119) of a seeded
+    image, read back with its own Image::load (bytes = value x 255)."""
+    import tempfile
+
+    x = image_io_input()
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "ref.png")
+        O.ref_save_image(x, path)
+        back = O.ref_load_image(path, 3)
+    np.savez_compressed(os.path.join(HERE, "image_io.npz"), image=x, ldr=np.rint(back * 255.0).astype(np.uint8))
+    print("image_io.npz:", x.shape)
+
+
+if __name__ == "__main__" and "--image" in sys.argv:
+    if O.build_ref() is None:
+        sys.exit("the reference tree is needed to regenerate the fixtures")
+    make_image_io()
