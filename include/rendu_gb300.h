@@ -366,6 +366,14 @@ RT_API int pt_material_sample(const float *cases, const float *uniforms, size_t 
 RT_API int pt_image_save(const float *image, uint32_t width, uint32_t height, uint32_t components, const char *path,
                          int32_t tonemap);
 
+/* Scene textures: the scanline filters of a PNG (sub)image undone on the host, the step of
+ * the PNG decoding behind Image::loadLDR (Image.cpp:291-333) that is sequential along each
+ * row. filtered: rows x (1 + row_bytes) bytes, a filter type byte (0..4) before each row;
+ * pixel_bytes: bytes per complete pixel (1 for bit depths below 8); out: rows x row_bytes.
+ * RT_ERR_ARG for a filter type above 4. */
+RT_API int pt_png_unfilter(const uint8_t *filtered, uint32_t rows, uint32_t row_bytes, uint32_t pixel_bytes,
+                           uint8_t *out);
+
 /* AtmosphereApp::precomputeTable on device `device`: res x res RGBA floats into `out` (host),
  * `samples` march steps, rounded to half precision when half_precision != 0. */
 RT_API int pt_sky_table(uint32_t res, uint32_t samples, int32_t half_precision, float *out, int device);

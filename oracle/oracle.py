@@ -458,3 +458,58 @@ def ref_save_image(image, path: str) -> int:
     a = np.ascontiguousarray(image, np.float32)
     h, w, c = a.shape
     return lib.ref_save_image(a.reshape(-1), w, h, c, path.encode())
+
+
+def ref_mesh_load_obj(text) -> dict:
+    """The reference's mesh loading of an OBJ text (getMesh with FORCE_FRAME, restated in
+    oracle/ref_mesh.cpp around the reference's glm and mikktspace.c)."""
+    lib = ref_lib()
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    counts = np.zeros(3, np.uint64)
+    lib.ref_mesh_load_obj.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(C.c_uint64)]
+    lib.ref_mesh_error.restype = C.c_char_p
+    r = lib.ref_mesh_load_obj(data, len(data), counts.ctypes.data_as(C.POINTER(C.c_uint64)))
+    if r != 0:
+        raise ValueError(lib.ref_mesh_error().decode())
+    nv, ni = int(counts[0]), int(counts[1])
+    out = {k: np.zeros((nv, d), np.float32) for k, d in (("positions", 3), ("normals", 3), ("texcoords", 2),
+                                                          ("tangents", 3), ("bitangents", 3))}
+    out["indices"] = np.zeros(ni, np.uint32)
+    lib.ref_mesh_get.argtypes = [_f32p, _f32p, _f32p, _f32p, _f32p, _u32p]
+    lib.ref_mesh_get(*(out[k].reshape(-1) for k in ("positions", "normals", "texcoords", "tangents", "bitangents",
+                                                     "indices")))
+    out["had_uv"] = bool(counts[2])
+    return out
+
+
+def ref_mikktspace(positions, normals, texcoords, indices) -> np.ndarray:
+    """The reference's own mikktspace.c: per-corner (tangent xyz, sign), (len(indices), 4)."""
+    lib = ref_lib()
+    lib.ref_mikktspace.argtypes = [_f32p, _f32p, _f32p, C.c_size_t, _u32p, C.c_size_t, _f32p]
+    p = np.ascontiguousarray(positions, np.float32)
+    n = np.ascontiguousarray(normals, np.float32)
+    u = np.ascontiguousarray(texcoords, np.float32)
+    i = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+    out = np.zeros((len(i), 4), np.float32)
+    if lib.ref_mikktspace(p.reshape(-1), n.reshape(-1), u.reshape(-1), len(p), i, len(i), out.reshape(-1)) != 0:
+        raise ValueError("mikktspace failed")
+    return out
+
+
+def ref_transformation(axis, angle, trans, scale) -> np.ndarray:
+    """glm's translate * rotate * scale of Codable::decodeTransformation: row-major 4x4."""
+    lib = ref_lib()
+    lib.ref_transformation.argtypes = [_f32p, C.c_float, _f32p, C.c_float, _f32p]
+    out = np.zeros(16, np.float32)
+    lib.ref_transformation(np.asarray(axis, np.float32), float(angle), np.asarray(trans, np.float32), float(scale), out)
+    return out.reshape(4, 4).T.copy()
+
+
+def ref_mat_mul(a, b) -> np.ndarray:
+    """glm's mat4 product of two row-major 4x4 matrices."""
+    lib = ref_lib()
+    lib.ref_mat_mul.argtypes = [_f32p, _f32p, _f32p]
+    out = np.zeros(16, np.float32)
+    lib.ref_mat_mul(np.ascontiguousarray(np.asarray(a, np.float32).T).reshape(-1),
+                    np.ascontiguousarray(np.asarray(b, np.float32).T).reshape(-1), out)
+    return out.reshape(4, 4).T.copy()

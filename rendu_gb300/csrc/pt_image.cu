@@ -10,6 +10,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -234,6 +235,53 @@ int pt_image_save(const float *image, uint32_t width, uint32_t height, uint32_t 
     if (!ok) {
         rgb::set_error("writing " + p + " failed");
         return RT_ERR_ARG;
+    }
+    return RT_OK;
+}
+
+// PNG filters (None, Sub, Up, Average, Paeth), each byte predicted from the byte one pixel
+// to the left (a), the byte above (b) and the byte above-left (c); the first row sees a zero
+// row above it.
+int pt_png_unfilter(const uint8_t *filtered, uint32_t rows, uint32_t row_bytes, uint32_t pixel_bytes, uint8_t *out) {
+    rgb::clear_error();
+    if ((!filtered || !out) && rows && row_bytes) {
+        rgb::set_error("null argument");
+        return RT_ERR_ARG;
+    }
+    if (pixel_bytes == 0 || pixel_bytes > 8) {
+        rgb::set_error("pixel_bytes must be 1..8");
+        return RT_ERR_ARG;
+    }
+    const size_t fb = pixel_bytes;
+    for (uint32_t y = 0; y < rows; ++y) {
+        const uint8_t *in = filtered + (size_t)y * (row_bytes + 1);
+        const uint8_t type = in[0];
+        ++in;
+        uint8_t *cur = out + (size_t)y * row_bytes;
+        const uint8_t *up = y ? cur - row_bytes : nullptr;
+        if (type > 4) {
+            rgb::set_error("PNG filter type " + std::to_string(type) + " is invalid");
+            return RT_ERR_ARG;
+        }
+        for (size_t x = 0; x < row_bytes; ++x) {
+            const int a = x >= fb ? cur[x - fb] : 0;
+            const int b = up ? up[x] : 0;
+            const int c = (up && x >= fb) ? up[x - fb] : 0;
+            int pred = 0;
+            switch (type) {
+            case 1: pred = a; break;
+            case 2: pred = b; break;
+            case 3: pred = (a + b) >> 1; break;
+            case 4: {
+                const int p = a + b - c;
+                const int pa = std::abs(p - a), pb = std::abs(p - b), pc = std::abs(p - c);
+                pred = (pa <= pb && pa <= pc) ? a : (pb <= pc ? b : c);
+                break;
+            }
+            default: break;
+            }
+            cur[x] = (uint8_t)(in[x] + pred);
+        }
     }
     return RT_OK;
 }

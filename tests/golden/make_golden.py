@@ -9,6 +9,8 @@ the reference tree is only needed to regenerate them:
     python tests/golden/make_golden.py --renders  (reference path-tracer renders)
     python tests/golden/make_golden.py --sky      (the sky's scattering table and MaterialSky)
     python tests/golden/make_golden.py --image    (8-bit output of renderOneShot)
+    python tests/golden/make_golden.py --scene-io (scene loading: meshes, MikkTSpace,
+                                                   texture decoding, transformations)
 """
 from __future__ import annotations
 
@@ -162,7 +164,7 @@ def make_camera():
     print("camera.npz: 16 cameras")
 
 
-if __name__ == "__main__" and not {"--renders", "--sky", "--image"} & set(sys.argv):
+if __name__ == "__main__" and not {"--renders", "--sky", "--image", "--scene-io"} & set(sys.argv):
     if O.build_ref() is None:
         sys.exit("the reference tree is needed to regenerate the fixtures")
     make_raycaster()
@@ -258,3 +260,135 @@ if __name__ == "__main__" and "--image" in sys.argv:
     if O.build_ref() is None:
         sys.exit("the reference tree is needed to regenerate the fixtures")
     make_image_io()
+
+
+# --------------------------------------------------------------------------------------
+# scene loading: meshes, tangent spaces, textures, transformations
+# --------------------------------------------------------------------------------------
+
+SCENE_DEMO = os.path.join(HERE, "scene_demo")
+
+
+def synthetic_meshes(seed=SEED):
+    """Triangle lists that stress the tangent-space generator: a grid with random UV islands
+    (mirrored and rotated), duplicated corners, position-degenerate and UV-degenerate
+    triangles, a fan with exactly opposite tangents, and constant UVs."""
+    rng = np.random.default_rng(seed)
+    out = []
+    # 1. 9 x 9 grid, heights and UVs jittered; four UV islands, two of them mirrored
+    n = 9
+    g = np.stack(np.meshgrid(np.linspace(-1, 1, n), np.linspace(-1, 1, n)), -1).reshape(-1, 2)
+    pos = np.concatenate([g[:, :1], 0.2 * np.sin(3 * g[:, :1] + 2 * g[:, 1:]), g[:, 1:]], 1)
+    idx = []
+    for i in range(n - 1):
+        for j in range(n - 1):
+            a, b, c, d = i * n + j, i * n + j + 1, (i + 1) * n + j + 1, (i + 1) * n + j
+            idx += [a, b, c, a, c, d]
+    idx = np.asarray(idx)
+    P, U = pos[idx], g[idx] * 0.5 + 0.5
+    island = (np.arange(len(idx)) // 3 // 16) % 4
+    U = np.where((island == 1)[:, None], U[:, ::-1], U)
+    U = np.where((island == 2)[:, None], U * np.array([-1.0, 1.0]), U)
+    N = np.tile([0.0, 1.0, 0.0], (len(idx), 1)) + 0.1 * rng.standard_normal((len(idx), 3))
+    N /= np.linalg.norm(N, axis=1, keepdims=True)
+    # weld what is identical: corners of the same grid vertex in the same island share data
+    key = np.concatenate([P, N * 0 + np.round(N, 1), U], 1)
+    _, first, inv = np.unique(np.round(key, 6), axis=0, return_index=True, return_inverse=True)
+    N = N[first][inv.reshape(-1)]
+    verts, ind = np.unique(np.concatenate([P, N, U], 1), axis=0, return_inverse=True)
+    tri = ind.reshape(-1).astype(np.uint32)
+    tri[6:9] = tri[[6, 6, 7]]  # a position-degenerate triangle
+    out.append(("grid_islands", verts[:, :3], verts[:, 3:6], verts[:, 6:8], tri))
+    # 2. random soup with shared vertices, some UV-degenerate triangles
+    m = 60
+    v = rng.normal(size=(m, 3))
+    nn = v / np.linalg.norm(v, axis=1, keepdims=True)
+    uv = rng.uniform(0, 1, (m, 2))
+    uv[:5] = uv[0]
+    tri = rng.integers(0, m, (120, 3))
+    tri = tri[(tri[:, 0] != tri[:, 1]) & (tri[:, 1] != tri[:, 2]) & (tri[:, 0] != tri[:, 2])]
+    tri[:4] = [[0, 1, 2], [1, 2, 3], [2, 3, 4], [0, 3, 4]]
+    out.append(("soup", v, nn, uv, tri.reshape(-1).astype(np.uint32)))
+    # 3. a symmetric pole fan: opposite triangles have exactly opposite tangents
+    k = 8
+    ring = np.stack([np.cos(2 * np.pi * np.arange(k) / k), np.zeros(k), np.sin(2 * np.pi * np.arange(k) / k)], 1)
+    v = np.concatenate([[[0.0, 1.0, 0.0]], ring * 0.5 + [0, 0.8, 0]], 0)
+    nn = v / np.linalg.norm(v, axis=1, keepdims=True)
+    uv = np.concatenate([[[0.5, 0.5]], ring[:, [0, 2]] * 0.5 + 0.5], 0)
+    tri = np.asarray([[0, 1 + (i + 1) % k, 1 + i] for i in range(k)]).reshape(-1).astype(np.uint32)
+    out.append(("pole_fan", v, nn, uv, tri))
+    # 4. constant UVs (what a mesh without texture coordinates gets)
+    v = rng.normal(size=(30, 3))
+    tri = np.asarray([[i, (i + 1) % 30, (i + 7) % 30] for i in range(30)]).reshape(-1).astype(np.uint32)
+    out.append(("constant_uv", v, v / np.linalg.norm(v, axis=1, keepdims=True), np.full((30, 2), 0.5), tri))
+    return [(name, np.asarray(p, np.float32), np.asarray(nr, np.float32), np.asarray(u, np.float32), t)
+            for name, p, nr, u, t in out]
+
+
+def png_variants():
+    """(name, samples, writer kwargs) of PNG files covering the colour types and bit depths."""
+    rng = np.random.default_rng(SEED + 7)
+    h, w = 13, 11
+    pal = rng.integers(0, 256, (16, 3)).astype(np.uint8)
+    return [
+        ("grey1", rng.integers(0, 2, (h, w, 1)), dict(ctype=0, depth=1)),
+        ("grey2", rng.integers(0, 4, (h, w, 1)), dict(ctype=0, depth=2)),
+        ("grey4_interlaced", rng.integers(0, 16, (h, w, 1)), dict(ctype=0, depth=4, interlace=True)),
+        ("grey8_key", rng.integers(0, 4, (h, w, 1)) * 60, dict(ctype=0, depth=8, trns=b"\x00\x3c")),
+        ("grey16", rng.integers(0, 65536, (h, w, 1)), dict(ctype=0, depth=16)),
+        ("rgb8_key", rng.integers(0, 2, (h, w, 3)) * 200, dict(ctype=2, depth=8, trns=b"\x00\xc8\x00\x00\x00\xc8")),
+        ("rgb16_interlaced", rng.integers(0, 65536, (h, w, 3)), dict(ctype=2, depth=16, interlace=True)),
+        ("palette2", rng.integers(0, 4, (h, w, 1)), dict(ctype=3, depth=2, palette=pal[:4], trns=b"\x10\xff")),
+        ("palette8", rng.integers(0, 16, (h, w, 1)), dict(ctype=3, depth=8, palette=pal)),
+        ("greyalpha16", rng.integers(0, 65536, (h, w, 2)), dict(ctype=4, depth=16)),
+        ("rgba8_interlaced", rng.integers(0, 256, (h, w, 4)), dict(ctype=6, depth=8, interlace=True)),
+        ("rgba16", rng.integers(0, 65536, (h, w, 4)), dict(ctype=6, depth=16, filters=(4, 3))),
+    ]
+
+
+def transformation_cases(n=200, seed=SEED):
+    rng = np.random.default_rng(seed)
+    axis = rng.normal(size=(n, 3)).astype(np.float32)
+    angle = rng.uniform(-7, 7, n).astype(np.float32)
+    angle[:10] = 0.0
+    trans = (rng.normal(size=(n, 3)) * 5).astype(np.float32)
+    scale = rng.uniform(0.1, 4, n).astype(np.float32)
+    return axis, angle, trans, scale
+
+
+def make_scene_io():
+    import glob
+    import tempfile
+
+    sys.path.insert(0, SCENE_DEMO)
+    import make_scene as MS  # noqa: E402
+
+    out = {}
+    for path in sorted(glob.glob(os.path.join(SCENE_DEMO, "*.obj"))):
+        name = os.path.basename(path)[:-4]
+        r = O.ref_mesh_load_obj(open(path, "rb").read())
+        for k in ("positions", "normals", "texcoords", "tangents", "bitangents", "indices"):
+            out[f"obj_{name}_{k}"] = r[k]
+        out[f"obj_{name}_had_uv"] = np.asarray(r["had_uv"])
+    for name, p, n, u, t in synthetic_meshes():
+        out[f"mk_{name}_in_pos"], out[f"mk_{name}_in_nor"], out[f"mk_{name}_in_uv"], out[f"mk_{name}_in_idx"] = p, n, u, t
+        out[f"mk_{name}_out"] = O.ref_mikktspace(p, n, u, t)
+    for path in sorted(glob.glob(os.path.join(SCENE_DEMO, "*.png")) + glob.glob(os.path.join(SCENE_DEMO, "*.exr"))):
+        out[f"img_{os.path.basename(path)}"] = O.ref_load_image(path, 4)
+    with tempfile.TemporaryDirectory() as d:
+        for name, samples, kw in png_variants():
+            path = os.path.join(d, name + ".png")
+            MS.write_png(path, samples, **kw)
+            for ch in (3, 4):
+                out[f"png_{name}_{ch}"] = O.ref_load_image(path, ch)
+    axis, angle, trans, scale = transformation_cases()
+    out["tf_axis"], out["tf_angle"], out["tf_trans"], out["tf_scale"] = axis, angle, trans, scale
+    out["tf_out"] = np.stack([O.ref_transformation(a, g, t, s) for a, g, t, s in zip(axis, angle, trans, scale)])
+    np.savez_compressed(os.path.join(HERE, "scene_io.npz"), **out)
+    print("scene_io.npz:", len(out), "arrays")
+
+
+if __name__ == "__main__" and "--scene-io" in sys.argv:
+    if O.build_ref() is None:
+        sys.exit("the reference tree is needed to regenerate the fixtures")
+    make_scene_io()
