@@ -374,6 +374,14 @@ RT_API int pt_image_save(const float *image, uint32_t width, uint32_t height, ui
 RT_API int pt_png_unfilter(const uint8_t *filtered, uint32_t rows, uint32_t row_bytes, uint32_t pixel_bytes,
                            uint8_t *out);
 
+/* Scene textures: decode a JPEG file held in memory (Image::loadLDR, Image.cpp:291-333, reads
+ * .jpg / .jpeg textures through stb_image): sequential or progressive Huffman JPEG with 1 or 3
+ * components, as width x height x channels bytes (channels 1..4: grey, grey + alpha, RGB,
+ * RGBA with alpha 255). With out == NULL only *width and *height are filled. RT_ERR_ARG for
+ * data it does not decode (arithmetic coding, lossless, 12-bit, CMYK) or a small buffer. */
+RT_API int pt_jpeg_decode(const uint8_t *data, size_t size, uint32_t channels, uint8_t *out, size_t out_capacity,
+                          uint32_t *width, uint32_t *height);
+
 /* AtmosphereApp::precomputeTable on device `device`: res x res RGBA floats into `out` (host),
  * `samples` march steps, rounded to half precision when half_precision != 0. */
 RT_API int pt_sky_table(uint32_t res, uint32_t samples, int32_t half_precision, float *out, int device);

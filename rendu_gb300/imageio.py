@@ -10,9 +10,15 @@
     files, uncompressed, RLE, ZIPS or ZIP, half / float / uint channels; R, G, B, A taken
     by name, a missing colour channel is 0 and a missing alpha 1.
 
+  * JPEG (Image::loadLDR through stb_image): sequential and progressive Huffman files with
+    1 or 3 components, decoded by the native library (pt_jpeg_decode). Its inverse DCT,
+    chroma upsampling and colour conversion are computed in the standard way rather than
+    with stb_image's fixed-point approximations, so samples may differ from the
+    reference's by a few units of 1/255.
+
 ``flip`` mirrors the rows, as the reference does for the faces of cube maps
-(ResourcesManager.cpp:509). JPEG, BMP and TGA files (also accepted by stb_image) are not
-decoded here: loading one raises ``ImageFormatError`` naming the file.
+(ResourcesManager.cpp:509). BMP and TGA files (also accepted by stb_image) are not decoded:
+loading one raises ``ImageFormatError`` naming the file.
 """
 from __future__ import annotations
 
@@ -291,6 +297,26 @@ def decode_exr(data: bytes, channels: int = 3, flip: bool = False) -> np.ndarray
     return np.ascontiguousarray(out)
 
 
+def decode_jpeg(data: bytes, channels: int = 4, flip: bool = False) -> np.ndarray:
+    """JPEG bytes -> (h, w, channels) float32 in [0, 1] (native decoder, pt_jpeg_decode)."""
+    import ctypes as C
+
+    from . import _lib as L
+
+    w, h = C.c_uint32(), C.c_uint32()
+    src = np.frombuffer(data, np.uint8)
+    try:
+        L.call("pt_jpeg_decode", src.ctypes.data, len(src), channels, None, 0, C.byref(w), C.byref(h))
+        out = np.empty((h.value, w.value, channels), np.uint8)
+        L.call("pt_jpeg_decode", src.ctypes.data, len(src), channels, out.ctypes.data, out.size, C.byref(w),
+               C.byref(h))
+    except L.RenduError as e:
+        raise ImageFormatError(str(e)) from None
+    if flip:
+        out = out[::-1]
+    return np.ascontiguousarray(out).astype(np.float32) / np.float32(255.0)
+
+
 def load_image(path: str, channels: int = 4, flip: bool = False) -> np.ndarray:
     """Image::load(path, channels, flip): (h, w, channels) float32 from a PNG or EXR file.
     A channel count of 0 means the reference's defaults: 4 for 8-bit files, 3 for EXR."""
@@ -300,4 +326,9 @@ def load_image(path: str, channels: int = 4, flip: bool = False) -> np.ndarray:
         return decode_exr(data, channels or 3, flip)
     if data[:8] == _PNG_SIG:
         return decode_png(data, channels or 4, flip)
-    raise ImageFormatError(f"{path}: only PNG and OpenEXR images are decoded (JPEG, BMP and TGA are not)")
+    if data[:2] == b"\xff\xd8":
+        try:
+            return decode_jpeg(data, channels or 4, flip)
+        except ImageFormatError as e:
+            raise ImageFormatError(f"{path}: {e}") from None
+    raise ImageFormatError(f"{path}: only PNG, JPEG and OpenEXR images are decoded (BMP and TGA are not)")

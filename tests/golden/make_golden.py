@@ -373,7 +373,8 @@ def make_scene_io():
     for name, p, n, u, t in synthetic_meshes():
         out[f"mk_{name}_in_pos"], out[f"mk_{name}_in_nor"], out[f"mk_{name}_in_uv"], out[f"mk_{name}_in_idx"] = p, n, u, t
         out[f"mk_{name}_out"] = O.ref_mikktspace(p, n, u, t)
-    for path in sorted(glob.glob(os.path.join(SCENE_DEMO, "*.png")) + glob.glob(os.path.join(SCENE_DEMO, "*.exr"))):
+    for path in sorted(glob.glob(os.path.join(SCENE_DEMO, "*.png")) + glob.glob(os.path.join(SCENE_DEMO, "*.exr"))
+                       + glob.glob(os.path.join(SCENE_DEMO, "*.jpg"))):
         out[f"img_{os.path.basename(path)}"] = O.ref_load_image(path, 4)
     with tempfile.TemporaryDirectory() as d:
         for name, samples, kw in png_variants():

@@ -6,8 +6,9 @@ exercises what the loader has to get right: nested and array tokens, comments, c
 a scene-wide transformation; OBJ files with and without texture coordinates and normals,
 single-slash face tokens and a UV sphere with a seam and poles; PNG textures of several
 colour types (RGB with every filter type, palette with tRNS alpha, grey + alpha, 16-bit,
-interlaced), constant-colour textures, an OpenEXR cube map (uncompressed half, ZIP
-compressed, float RGBA faces); point, spot and directional lights; an object with
+interlaced), JPEG textures (sequential 4:2:0 with restart markers; progressive 4:4:4 with
+spectral selection and DC successive approximation), constant-colour textures, an OpenEXR
+cube map (uncompressed half, ZIP compressed, float RGBA faces); point, spot and directional lights; an object with
 ``skipuvs``; a masked material and an emissive one; a probe block.
 
     python tests/golden/scene_demo/make_scene.py
@@ -150,6 +151,238 @@ def write_exr(path, img, ptype=1, compression=0):
     del sz
 
 
+class _BitWriter:
+    def __init__(self):
+        self.out = bytearray()
+        self.acc = 0
+        self.n = 0
+
+    def put(self, value: int, length: int):
+        for k in range(length - 1, -1, -1):
+            self.acc = (self.acc << 1) | ((value >> k) & 1)
+            self.n += 1
+            if self.n == 8:
+                self.out.append(self.acc)
+                if self.acc == 0xFF:
+                    self.out.append(0)
+                self.acc = self.n = 0
+
+    def flush(self):
+        if self.n:
+            self.put((1 << (8 - self.n)) - 1, 8 - self.n)
+
+
+_ZZ = [0, 1, 8, 16, 9, 2, 3, 10, 17, 24, 32, 25, 18, 11, 4, 5, 12, 19, 26, 33, 40, 48, 41, 34, 27, 20, 13, 6, 7, 14,
+       21, 28, 35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51, 58, 59, 52, 45, 38, 31, 39, 46, 53,
+       60, 61, 54, 47, 55, 62, 63]
+
+
+def _category(v: int) -> int:
+    return int(abs(v)).bit_length()
+
+
+def _bits_of(v: int, s: int) -> int:
+    return v if v >= 0 else v + (1 << s) - 1
+
+
+def _code_table(symbols):
+    """Canonical code for a symbol set: the 16 most frequent symbols get 5-bit codes, the
+    others 12-bit codes (exercises both short and long code paths of a decoder)."""
+    freq = {}
+    for sym in symbols:
+        freq[sym] = freq.get(sym, 0) + 1
+    order = sorted(freq, key=lambda s_: (-freq[s_], s_))
+    short, long_ = order[:16], order[16:]
+    counts = [0] * 17
+    counts[5], counts[12] = len(short), len(long_)
+    codes, code = {}, 0
+    for length, group in ((5, short), (12, long_)):
+        for sym in group:
+            codes[sym] = (code, length)
+            code += 1
+        if length == 5:
+            code <<= 7
+    return counts, short + long_, codes
+
+
+def write_jpeg(path, rgb, subsample=True, restart=0, progressive=False):
+    """Huffman JPEG of an 8-bit RGB image: JFIF YCbCr, 4:2:0 (or 4:4:4), quality-75 style
+    quantisation, a float forward DCT. Sequential (optionally with restart markers), or
+    progressive with an interleaved DC scan at Al = 1, a DC refinement scan and per
+    component AC scans by spectral selection (bands 1-5 and 6-63, one EOB per block)."""
+    rgb = np.asarray(rgb, np.float64)
+    h, w, _ = rgb.shape
+    y = 0.299 * rgb[..., 0] + 0.587 * rgb[..., 1] + 0.114 * rgb[..., 2]
+    cb = -0.168736 * rgb[..., 0] - 0.331264 * rgb[..., 1] + 0.5 * rgb[..., 2] + 128
+    cr = 0.5 * rgb[..., 0] - 0.418688 * rgb[..., 1] - 0.081312 * rgb[..., 2] + 128
+    hs = 2 if subsample else 1
+    mw, mh = 8 * hs, 8 * hs
+    W, H = -(-w // mw) * mw, -(-h // mh) * mh
+    pad = lambda a: np.pad(a, ((0, H - h), (0, W - w)), mode="edge")  # noqa: E731
+    planes = [pad(y)]
+    for c in (cb, cr):
+        c = pad(c)
+        if subsample:
+            c = c.reshape(H // 2, 2, W // 2, 2).mean((1, 3))
+        planes.append(c)
+    qy = np.array([8 + (k % 8 + k // 8) * 3 for k in range(64)], np.int32)
+    qc = np.array([10 + (k % 8 + k // 8) * 4 for k in range(64)], np.int32)
+    qts = [qy, qc, qc]
+    xs = np.arange(8)
+    basis = np.array([[(np.sqrt(0.125) if u == 0 else 0.5) * np.cos((2 * x + 1) * u * np.pi / 16) for x in xs]
+                      for u in range(8)])
+    blocks = []  # per component: (by, bx) -> quantised natural-order coefficients
+    for ci, pl in enumerate(planes):
+        bh, bw = pl.shape[0] // 8, pl.shape[1] // 8
+        t = pl.reshape(bh, 8, bw, 8).transpose(0, 2, 1, 3) - 128.0
+        f = np.einsum("ux,abxy,vy->abuv", basis, t, basis)
+        blocks.append(np.round(f.reshape(bh, bw, 64) / qts[ci]).astype(np.int64))
+    ids = (1, 2, 3)
+    samp = (hs * 16 + hs, 0x11, 0x11)
+    mcu_order = []  # (component, by, bx) in interleaved MCU order
+    for my in range(H // mh):
+        for mx in range(W // mw):
+            for v in range(hs):
+                for u in range(hs):
+                    mcu_order.append((0, my * hs + v, mx * hs + u))
+            mcu_order += [(1, my, mx), (2, my, mx)]
+
+    def seg(marker, body):
+        return bytes([0xFF, marker]) + struct.pack(">H", len(body) + 2) + body
+
+    def dht(tc, th, counts, vals):
+        return seg(0xC4, bytes([tc * 16 + th]) + bytes(counts[1:]) + bytes(vals))
+
+    out = bytearray(b"\xff\xd8")
+    out += seg(0xE0, b"JFIF\0" + bytes([1, 1, 0, 0, 1, 0, 1, 0, 0]))
+    for t, q in enumerate((qy, qc)):
+        out += seg(0xDB, bytes([t]) + bytes(int(q[_ZZ[k]]) for k in range(64)))
+    sof = 0xC2 if progressive else 0xC0
+    out += seg(sof, bytes([8]) + struct.pack(">HH", h, w) + bytes([3]) +
+               b"".join(bytes([ids[c], samp[c], 0 if c == 0 else 1]) for c in range(3)))
+    if restart:
+        out += seg(0xDD, struct.pack(">H", restart))
+
+    def dc_symbols(units, al):
+        pred = [0, 0, 0]
+        syms = []
+        for c, by, bx in units:
+            dcv = int(blocks[c][by, bx, 0]) >> al
+            d = dcv - pred[c]
+            pred[c] = dcv
+            syms.append((c, _category(d), d))
+        return syms
+
+    def ac_symbols(coefs, ss, se):
+        syms, run = [], 0
+        last = max([k for k in range(ss, se + 1) if coefs[_ZZ[k]] != 0], default=-1)
+        for k in range(ss, se + 1):
+            if k > last:
+                syms.append((0x00, 0, 0))
+                break
+            v = int(coefs[_ZZ[k]])
+            if v == 0:
+                run += 1
+                continue
+            while run > 15:
+                syms.append((0xF0, 0, 0))
+                run -= 16
+            s_ = _category(v)
+            syms.append((run * 16 + s_, s_, v))
+            run = 0
+        return syms
+
+    if not progressive:
+        per_unit = []
+        for c, by, bx in mcu_order:
+            per_unit.append((c, by, bx))
+        # symbol statistics per table class
+        dc_s = dc_symbols(per_unit, 0)
+        ac_s = [ac_symbols(blocks[c][by, bx], 1, 63) for c, by, bx in per_unit]
+        tables = {}
+        for cls in (0, 1):
+            comps = (0,) if cls == 0 else (1, 2)
+            dsyms = [s_[1] for s_ in dc_s if s_[0] in comps]
+            asyms = [a[0] for (c, _, _), syms in zip(per_unit, ac_s) if c in comps for a in syms]
+            tables[cls] = (_code_table(dsyms), _code_table(asyms))
+            out += dht(0, cls, tables[cls][0][0], tables[cls][0][1]) + dht(1, cls, tables[cls][1][0], tables[cls][1][1])
+        out += seg(0xDA, bytes([3]) + b"".join(bytes([ids[c], 0 if c == 0 else 0x11]) for c in range(3)) +
+                   bytes([0, 63, 0]))
+        bw_ = _BitWriter()
+        units_per_mcu = hs * hs + 2
+        rst = 0
+        for i, ((c, by, bx), d, syms) in enumerate(zip(per_unit, dc_s, ac_s)):
+            if restart and i and i % (units_per_mcu * restart) == 0:
+                bw_.flush()
+                out += bw_.out + bytes([0xFF, 0xD0 + rst % 8])
+                bw_ = _BitWriter()
+                rst += 1
+                # predictors restart: recompute the remaining DC differences
+                dc_s[i:] = dc_symbols(per_unit[i:], 0)
+                d = dc_s[i]
+            cls = 0 if c == 0 else 1
+            (_, _, dcodes), (_, _, acodes) = tables[cls]
+            code, length = dcodes[d[1]]
+            bw_.put(code, length)
+            if d[1]:
+                bw_.put(_bits_of(d[2], d[1]), d[1])
+            for sym, s_, v in syms:
+                code, length = acodes[sym]
+                bw_.put(code, length)
+                if s_:
+                    bw_.put(_bits_of(v, s_), s_)
+        bw_.flush()
+        out += bw_.out
+    else:
+        # DC first (Al = 1), interleaved
+        dc_s = dc_symbols(mcu_order, 1)
+        for cls in (0, 1):
+            comps = (0,) if cls == 0 else (1, 2)
+            counts, vals, _ = _code_table([s_[1] for s_ in dc_s if s_[0] in comps])
+            out += dht(0, cls, counts, vals)
+        codes = {cls: _code_table([s_[1] for s_ in dc_s if s_[0] in ((0,) if cls == 0 else (1, 2))])[2]
+                 for cls in (0, 1)}
+        out += seg(0xDA, bytes([3]) + b"".join(bytes([ids[c], 0 if c == 0 else 0x10]) for c in range(3)) +
+                   bytes([0, 0, 0x01]))
+        bw_ = _BitWriter()
+        for c, _, d in dc_s:
+            code, length = codes[0 if c == 0 else 1][_category(d)]
+            bw_.put(code, length)
+            if _category(d):
+                bw_.put(_bits_of(d, _category(d)), _category(d))
+        bw_.flush()
+        out += bw_.out
+        # DC refinement (Ah = 1, Al = 0): the low bit of every DC value
+        out += seg(0xDA, bytes([3]) + b"".join(bytes([ids[c], 0]) for c in range(3)) + bytes([0, 0, 0x10]))
+        bw_ = _BitWriter()
+        for c, by, bx in mcu_order:
+            bw_.put(int(blocks[c][by, bx, 0]) & 1, 1)
+        bw_.flush()
+        out += bw_.out
+        # AC first scans, one component each, bands 1-5 and 6-63 (non-interleaved order)
+        for c in range(3):
+            hc = hs if c == 0 else 1  # the component's sampling factor (hmax = vmax = hs)
+            cw_ = -(-(-(-w * hc // hs)) // 8)  # blocks covering the component's own size
+            ch_ = -(-(-(-h * hc // hs)) // 8)
+            for ss, se in ((1, 5), (6, 63)):
+                syms = [ac_symbols(blocks[c][by, bx], ss, se) for by in range(ch_) for bx in range(cw_)]
+                counts, vals, acodes = _code_table([a[0] for sy in syms for a in sy])
+                out += dht(1, 0, counts, vals)
+                out += seg(0xDA, bytes([1, ids[c], 0x00, ss, se, 0]))
+                bw_ = _BitWriter()
+                for sy in syms:
+                    for sym, s_, v in sy:
+                        code, length = acodes[sym]
+                        bw_.put(code, length)
+                        if s_:
+                            bw_.put(_bits_of(v, s_), s_)
+                bw_.flush()
+                out += bw_.out
+    out += b"\xff\xd9"
+    with open(path, "wb") as f:
+        f.write(bytes(out))
+
+
 # --------------------------------------------------------------------------------------
 # meshes
 # --------------------------------------------------------------------------------------
@@ -251,6 +484,12 @@ def write_textures(rng):
     ind[(np.mgrid[0:24, 0:20][0] - 12) ** 2 + (np.mgrid[0:24, 0:20][1] - 10) ** 2 > 90] = 3
     write_png(os.path.join(HERE, "demo_leaf_color.png"), ind[..., None], ctype=3, depth=4, palette=pal,
               trns=bytes([255, 255, 255, 0, 255]))
+    # JPEG colour textures: sequential 4:2:0 with restart markers, progressive 4:4:4
+    wood = np.stack([120 + 60 * np.sin(xx * 0.7 + 2 * np.sin(yy * 0.2)), 80 + 30 * np.sin(xx * 0.7), 40 + 10 * yy / n],
+                    -1)
+    wood = np.clip(np.kron(wood, np.ones((2, 2, 1)))[:58, :46] + rng.integers(-6, 7, (58, 46, 3)), 0, 255)
+    write_jpeg(os.path.join(HERE, "demo_crate_color.jpg"), wood.astype(np.uint8), subsample=True, restart=3)
+    write_jpeg(os.path.join(HERE, "demo_wall_color.jpg"), rgb[:, :27], subsample=False, progressive=True)
     # sky cube map faces: +y bright, -y dark, sides a gradient; three encodings
     for k, suf in enumerate(("px", "nx", "ny", "py", "pz", "nz")):
         m = 8

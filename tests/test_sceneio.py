@@ -223,13 +223,45 @@ def test_random_meshes_against_reference_mikktspace():
 # --------------------------------------------------------------------------------------
 
 
+def _assert_jpeg_close(a, b, what):
+    """JPEG samples: the inverse DCT, chroma upsampling and colour conversion are exact here
+    and fixed-point in stb_image, so samples may differ by a few 1/255 steps."""
+    assert a.shape == b.shape, what
+    d = np.abs(a.astype(np.float64) - b) * 255.0
+    assert d.max() <= 3.01 and d.mean() < 0.1 and (d > 1.01).mean() < 0.05, (what, d.max(), d.mean())
+
+
 def test_demo_textures_match_reference(golden, lib):
     from rendu_gb300 import imageio
 
-    files = sorted(glob.glob(os.path.join(DEMO, "*.png")) + glob.glob(os.path.join(DEMO, "*.exr")))
-    assert len(files) == 10
+    files = sorted(glob.glob(os.path.join(DEMO, "*.png")) + glob.glob(os.path.join(DEMO, "*.exr"))
+                   + glob.glob(os.path.join(DEMO, "*.jpg")))
+    assert len(files) == 12
     for path in files:
-        assert _bits_equal(imageio.load_image(path, 4), golden[f"img_{os.path.basename(path)}"]), path
+        ref = golden[f"img_{os.path.basename(path)}"]
+        if path.endswith(".jpg"):
+            _assert_jpeg_close(imageio.load_image(path, 4), ref, path)
+        else:
+            assert _bits_equal(imageio.load_image(path, 4), ref), path
+
+
+def test_jpeg_errors(lib):
+    from rendu_gb300 import imageio
+
+    data = open(os.path.join(DEMO, "demo_crate_color.jpg"), "rb").read()
+    img = imageio.decode_jpeg(data, 3)
+    assert img.shape == (58, 46, 3)
+    np.testing.assert_array_equal(imageio.decode_jpeg(data, 4)[..., 3], 1.0)
+    grey = imageio.decode_jpeg(data, 1)[..., 0]
+    rgb255 = np.rint(img * 255).astype(np.int32)
+    expect = (rgb255[..., 0] * 77 + rgb255[..., 1] * 150 + rgb255[..., 2] * 29) >> 8
+    np.testing.assert_array_equal(np.rint(grey * 255).astype(np.int32), expect)
+    for bad in (data[:40], data[:2] + b"\xff\xc9\x00\x0b" + bytes(9) + data[2:], b"\xff\xd8\xff\xd9"):
+        with pytest.raises(imageio.ImageFormatError, match="JPEG"):
+            imageio.decode_jpeg(bad)
+    # a truncated entropy-coded segment decodes to something, without reading out of bounds
+    out = imageio.decode_jpeg(data[: len(data) - 200] + b"\xff\xd9")
+    assert out.shape == (58, 46, 4)
 
 
 def test_png_variants_match_stb(golden, lib):
@@ -270,6 +302,10 @@ def test_reference_images_directly(lib):
     assert paths
     for p in paths:
         assert _bits_equal(imageio.load_image(p, 4), O.ref_load_image(p, 4, max_pixels=1 << 24)), p
+    jpegs = sorted(glob.glob(os.path.join(REF_RES, "**", "*.jpg"), recursive=True))
+    assert jpegs  # progressive and sequential, 4:2:0 and 4:4:4, grey
+    for p in jpegs:
+        _assert_jpeg_close(imageio.load_image(p, 4), O.ref_load_image(p, 4, max_pixels=1 << 24), p)
 
 
 # --------------------------------------------------------------------------------------
@@ -350,11 +386,15 @@ def test_reference_scenes_load(lib):
     assert ls.camera["eye"] == pytest.approx((0.0, 1.0, 2.5)) and ls.camera["fov"] == pytest.approx(1.3)
     assert all(sc.meshes[o["mesh"]].texcoords is None for o in sc.objects)  # every object skips UVs
     assert sc.background == {"mode": 0, "color": (0.0, 0.0, 0.0), "tex": (0,) * 6}
-    for name, objects in (("furnace-test", 22), ("parameter-spheres", 22), ("boxes", 443), ("multi-probes", 3),
-                          ("cornellbox-emissive", 7)):
-        assert len(sceneio.load_scene(name, resources=roots).scene.objects) == objects
-    with pytest.raises(imageio.ImageFormatError, match=r"\.jpg"):
-        sceneio.load_scene("cornellbox-textured", resources=roots)
+    counts = {"furnace-test": 22, "parameter-spheres": 22, "boxes": 443, "multi-probes": 3, "cornellbox-emissive": 7,
+              "cornellbox-cutout": 7, "cornellbox-parallax": 3, "cornellbox-reflections": 8, "cornellbox-textured": 8,
+              "cornellbox-transparent": 7, "gallery-materials": 52}
+    for name, objects in counts.items():
+        assert len(sceneio.load_scene(name, resources=roots).scene.objects) == objects, name
+    cut = sceneio.load_scene("cornellbox-cutout", resources=roots).scene
+    assert any(m["masked"] for m in cut.materials) and [l["type"] for l in cut.lights] == [2, 2]
+    assert sceneio.load_scene("cornellbox-reflections", resources=roots).scene.background["mode"] == 3
+    del imageio
 
 
 def test_cli_arguments():
