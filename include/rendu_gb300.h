@@ -150,6 +150,20 @@ RT_API int rt_get_stats(const rt_ctx *ctx, rt_stats *out);
 RT_API int rt_count_visits(rt_ctx *ctx, const rt_ray *rays, size_t n, uint32_t *node_visits, uint32_t *tri_visits,
                     void *stream, uint32_t flags);
 
+/* Hierarchy inspection (the geometry of RaycasterVisualisation::getAllLevels,
+ * RaycasterVisualisation.cpp:9-33, for this library's own hierarchy): the box of every node
+ * in breadth-first order, the root's first. boxes: count x 6 floats {lo.xyz, hi.xyz}; info:
+ * count x 2 int32 {depth (root 0), triangles (0 for an inner node, > 0 for a leaf)}. At most
+ * `capacity` entries are written; *count receives the total (NULL arrays: count only). */
+RT_API int rt_hierarchy_boxes(const rt_ctx *ctx, float *boxes, int32_t *info, size_t capacity, size_t *count);
+
+/* The boxes one ray enters, in visiting order, and its closest hit
+ * (RaycasterVisualisation::getRayLevels, RaycasterVisualisation.cpp:35-81): a host walk of
+ * the device hierarchy with the device traversal's order and arithmetic; *hit equals what
+ * rt_intersect returns for the ray. boxes / info / capacity / count as rt_hierarchy_boxes. */
+RT_API int rt_ray_levels(const rt_ctx *ctx, const rt_ray *ray, float *boxes, int32_t *info, size_t capacity,
+                         size_t *count, rt_hit *hit);
+
 /* Message of the calling thread's last failed call ("" if none). */
 RT_API const char *rt_last_error(void);
 

@@ -135,6 +135,8 @@ _SIGS = {
     "pt_material_sample": ([_VP, _VP, C.c_size_t, _VP, C.c_int], C.c_int),
     "pt_scene_set_sky_table": ([_VP, _VP, C.c_uint32, C.c_uint32], C.c_int),
     "pt_image_save": ([_VP, C.c_uint32, C.c_uint32, C.c_uint32, C.c_char_p, C.c_int32], C.c_int),
+    "rt_hierarchy_boxes": ([_VP, _VP, _VP, C.c_size_t, C.POINTER(C.c_size_t)], C.c_int),
+    "rt_ray_levels": ([_VP, _VP, _VP, _VP, C.c_size_t, C.POINTER(C.c_size_t), _VP], C.c_int),
     "pt_png_unfilter": ([_VP, C.c_uint32, C.c_uint32, C.c_uint32, _VP], C.c_int),
     "pt_jpeg_decode": ([_VP, C.c_size_t, C.c_uint32, _VP, C.c_size_t, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)],
                        C.c_int),

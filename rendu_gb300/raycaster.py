@@ -65,6 +65,7 @@ class Raycaster:
             self._h = C.c_void_p(_handle)
         self.device = device
         self._meshes = []  # (first_tri, tri_count) per mesh
+        self._mesh_data = []  # (positions, indices, model) per mesh, for triangle()
 
     # ---- construction (Raycaster.cpp:14-142) ------------------------------------------
     def addMesh(self, mesh, model=None) -> int:
@@ -80,7 +81,21 @@ class Raycaster:
                m.ctypes.data if m is not None else None, C.byref(mid))
         first = sum(c for _, c in self._meshes)
         self._meshes.append((first, len(idx) // 3))
+        self._mesh_data.append((pos, idx, None if model is None else np.asarray(model, np.float32).reshape(4, 4)))
         return mid.value
+
+    def triangle(self, mesh_id: int, local_id: int) -> np.ndarray:
+        """The three vertices (3, 3) of triangle localId / 3 of a mesh, transformed by its model
+        matrix as addMesh stores them (Raycaster.cpp:22-36)."""
+        pos, idx, model = self._mesh_data[mesh_id]
+        v = pos.reshape(-1, 3)[idx[local_id:local_id + 3]].astype(np.float32)
+        if model is None:
+            return v
+        m = model
+        out = np.empty_like(v)
+        for k in range(3):  # glm's mat4 * vec4(p, 1) in column order
+            out[:, k] = ((m[k, 0] * v[:, 0] + m[k, 1] * v[:, 1]) + m[k, 2] * v[:, 2]) + m[k, 3]
+        return out
 
     def updateHierarchy(self):
         """Raycaster::updateHierarchy (Raycaster.cpp:54-142): builds the device hierarchy."""
@@ -195,3 +210,111 @@ class Raycaster:
             self.close()
         except Exception:
             pass
+
+
+# ---- hierarchy display geometry -------------------------------------------------------------
+
+# the 12 edges of a box as degenerate triangles over BoundingBox::getCorners' corner order
+# (x slowest, z fastest) -- RaycasterVisualisation.cpp:128-129
+_BOX_LINES = np.array([0, 1, 0, 0, 2, 0, 1, 3, 1, 2, 3, 2, 4, 5, 4, 4, 6, 4, 5, 7, 5, 6, 7, 6, 1, 5, 1, 0, 4, 0, 2, 6,
+                       2, 3, 7, 3], np.uint32)
+
+
+def _hsv_to_rgb(h: float, s: float, v: float) -> np.ndarray:
+    """Hue in degrees, saturation and value to RGB (single precision)."""
+    h, s, v = np.float32(h), np.float32(s), np.float32(v)
+    if s == 0:
+        return np.array([v, v, v], np.float32)
+    sector = np.floor(h * (np.float32(1) / np.float32(60)))
+    frac = h * (np.float32(1) / np.float32(60)) - sector
+    o = v * (np.float32(1) - s)
+    p = v * (np.float32(1) - s * frac)
+    q = v * (np.float32(1) - s * (np.float32(1) - frac))
+    table = {1: (p, v, o), 2: (o, v, q), 3: (o, p, v), 4: (q, o, v), 5: (v, o, p)}
+    return np.array(table.get(int(sector), (v, q, o)), np.float32)
+
+
+def _box_meshes(boxes: np.ndarray, depths: np.ndarray) -> list:
+    """createBVHMeshes (RaycasterVisualisation.cpp:107-157): one line mesh per depth, every
+    box as its 8 corners and 12 edges, coloured by relative depth (hue 300 depth^2,
+    value 0.75 - 0.5 depth^2)."""
+    if len(boxes) == 0:
+        return []
+    max_depth = int(depths.max())
+    meshes = []
+    for d in range(max_depth + 1):
+        sel = boxes[depths == d]
+        lo, hi = sel[:, :3], sel[:, 3:]
+        corners = np.stack([np.where([(k >> 2) & 1, (k >> 1) & 1, k & 1], hi, lo) for k in range(8)], 1)
+        rel = np.float32(d) / np.float32(max_depth) if max_depth else np.float32(0)
+        rel = rel * rel
+        color = _hsv_to_rgb(np.float32(300) * rel, 1.0, np.float32(0.5) * (np.float32(1) - rel) + np.float32(0.25))
+        idx = (np.arange(len(sel), dtype=np.uint32)[:, None] * 8 + _BOX_LINES[None, :]).reshape(-1)
+        meshes.append({"name": f"Level {d}", "positions": corners.reshape(-1, 3).astype(np.float32), "indices": idx,
+                       "colors": np.tile(color, (len(sel) * 8, 1))})
+    return meshes
+
+
+class RaycasterVisualisation:
+    """RaycasterVisualisation (src/engine/raycaster/RaycasterVisualisation.hpp) over the
+    device hierarchy: line meshes of node boxes by depth, for display or for writing out
+    with ``save_line_obj``. The boxes are those of this library's 4-wide hierarchy."""
+
+    def __init__(self, raycaster: Raycaster):
+        self._rc = raycaster
+
+    def _call(self, func, *args):
+        """Two calls of a box query: the count, then the boxes, their info and the hit."""
+        count = C.c_size_t()
+        hit = np.zeros(1, HIT_DTYPE)
+        extra = [] if func == "rt_hierarchy_boxes" else [hit.ctypes.data]
+        L.call(func, self._rc._h, *args, None, None, 0, C.byref(count), *extra)
+        n = count.value
+        boxes = np.zeros((n, 6), np.float32)
+        info = np.zeros((n, 2), np.int32)
+        L.call(func, self._rc._h, *args, boxes.ctypes.data, info.ctypes.data, n, C.byref(count), *extra)
+        return boxes, info, hit[0]
+
+    def getAllLevels(self) -> list:
+        """Every node of the hierarchy (getAllLevels, RaycasterVisualisation.cpp:9-33)."""
+        boxes, info, _ = self._call("rt_hierarchy_boxes")
+        return _box_meshes(boxes, info[:, 0])
+
+    def getRayLevels(self, origin, direction, mini: float = 1e-4, maxi: float = 1e8):
+        """The boxes a ray enters and its closest hit (getRayLevels, RaycasterVisualisation.cpp:
+        35-81): (line meshes, Hit)."""
+        ray = np.zeros(1, RAY_DTYPE)
+        ray[0] = (*origin, mini, *direction, maxi)
+        boxes, info, hit = self._call("rt_ray_levels", ray.ctypes.data)
+        return _box_meshes(boxes, info[:, 0]), self._rc.to_hit(hit)
+
+    def getRayMesh(self, ray_pos, ray_dir, hit: Hit, default_length: float = 1.0) -> dict:
+        """getRayMesh (RaycasterVisualisation.cpp:83-105): the ray segment up to the hit (or
+        default_length), green when it hit and red otherwise, plus the hit triangle."""
+        d = np.asarray(ray_dir, np.float32)
+        d = d * (np.float32(1) / np.sqrt(np.float32((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2])))
+        length = np.float32(hit.dist if hit.hit else default_length)
+        p0 = np.asarray(ray_pos, np.float32)
+        color = np.array([0.0, 1.0, 0.0] if hit.hit else [1.0, 0.0, 0.0], np.float32)
+        pos = [p0, p0 + length * d]
+        idx = [0, 1, 0]
+        if hit.hit:
+            pos += list(self._rc.triangle(hit.meshId, hit.localId))
+            idx += [2, 3, 4]
+        return {"name": "Ray", "positions": np.asarray(pos, np.float32), "indices": np.asarray(idx, np.uint32),
+                "colors": np.tile(color, (len(pos), 1))}
+
+
+def save_line_obj(meshes: list, path: str) -> None:
+    """Write line meshes (degenerate-triangle edges) as an OBJ of 'l' records, one group per
+    mesh, with the colour appended to each vertex (a common OBJ extension)."""
+    with open(path, "w") as f:
+        base = 1
+        for m in meshes:
+            f.write(f"g {m['name'].replace(' ', '_')}\n")
+            for p, c in zip(m["positions"], m["colors"]):
+                f.write(f"v {p[0]:.6g} {p[1]:.6g} {p[2]:.6g} {c[0]:.4g} {c[1]:.4g} {c[2]:.4g}\n")
+            tri = m["indices"].reshape(-1, 3)
+            for a, b, _ in tri:
+                f.write(f"l {a + base} {b + base}\n")
+            base += len(m["positions"])
