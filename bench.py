@@ -255,8 +255,8 @@ def run_batch(cpu: bool, tune: bool = True):
     tuning, tune_s = None, 0.0
     if tune:
         t0 = time.perf_counter()
-        tuning = br.autotune(jobs, cache_path=os.path.join(ROOT, "gpurun_out", "batch_tuning.json")
-                             if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None)
+        # an optional tuning cache shared between runs (RENDU_TUNING_CACHE=path)
+        tuning = br.autotune(jobs, cache_path=os.environ.get("RENDU_TUNING_CACHE") or None)
         tune_s = time.perf_counter() - t0
     br.render(jobs, tuning=tuning)  # warm-up (graph capture)
     torch.cuda.synchronize()

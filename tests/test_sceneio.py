@@ -24,7 +24,13 @@ import pytest
 from conftest import GOLDEN, load_golden
 
 DEMO = os.path.join(GOLDEN, "scene_demo")
-REF_RES = os.path.join(os.environ.get("RENDU_REFERENCE_ROOT", "/root/reference"), "resources")
+def _ref_root():
+    from oracle.oracle import REF_ROOT_DEFAULT
+
+    return os.environ.get("RENDU_REFERENCE_ROOT", REF_ROOT_DEFAULT)
+
+
+REF_RES = os.path.join(_ref_root(), "resources")
 
 
 def _golden_module():
