@@ -475,6 +475,12 @@ int build_hierarchy(rt_ctx *ctx) {
         ctx->n_leaves = 1;
         ctx->depth = 3;
         ctx->sah_cost = 1.0f;
+        float4 lo1, hi1;  // the whole hierarchy is the one (grown) leaf box
+        RT_CUDA_TRY(cudaMemcpyAsync(&lo1, d_slo.p, sizeof(float4), cudaMemcpyDeviceToHost, st));
+        RT_CUDA_TRY(cudaMemcpyAsync(&hi1, d_shi.p, sizeof(float4), cudaMemcpyDeviceToHost, st));
+        RT_CUDA_TRY(cudaStreamSynchronize(st));
+        ctx->root_box[0] = lo1.x; ctx->root_box[1] = lo1.y; ctx->root_box[2] = lo1.z;
+        ctx->root_box[3] = hi1.x; ctx->root_box[4] = hi1.y; ctx->root_box[5] = hi1.z;
     } else {
         const uint64_t ni = nt - 1;
         Scratch<uint32_t> d_child, d_pin, d_pleaf, d_rf, d_rl;

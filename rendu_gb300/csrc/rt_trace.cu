@@ -40,13 +40,19 @@ __global__ void __launch_bounds__(128) k_trace(const BvhNode *__restrict__ nodes
 
 // Persistent variant: a grid sized to fill the GPU once; lanes refill from `counter`
 // (zeroed before the launch). n is read from n_dev when given (device-side queue length).
+// The box of the whole hierarchy (the union of the grown leaf boxes): a ray that misses it
+// misses every child box of the root, so it is answered without a node fetch.
+struct RootBox {
+    float lo[3], hi[3];
+};
+
 template <bool ANY, int STACK>
 __global__ void __launch_bounds__(128) k_trace_persistent(const BvhNode *__restrict__ nodes,
                                                           const BvhTri *__restrict__ tris,
                                                           const rt_ray *__restrict__ rays, size_t n_host,
                                                           const uint32_t *__restrict__ n_dev, rt_hit *__restrict__ hits,
                                                           uint8_t *__restrict__ occ, unsigned *__restrict__ status,
-                                                          unsigned long long *__restrict__ counter) {
+                                                          unsigned long long *__restrict__ counter, const RootBox root) {
     const size_t n = n_dev ? (size_t)*n_dev : n_host;
     const unsigned lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -71,7 +77,8 @@ __global__ void __launch_bounds__(128) k_trace_persistent(const BvhNode *__restr
                     const float4 *rp = reinterpret_cast<const float4 *>(rays + idx);
                     r = make_ray_state(__ldcs(rp), __ldcs(rp + 1));
                     trav_init(t, r);
-                    active = r.valid;
+                    active = r.valid && slab(r, root.lo[0], root.hi[0], root.lo[1], root.hi[1], root.lo[2],
+                                             root.hi[2], r.tmin, r.tmax) != INFINITY;
                     if (!active) {  // never hits: write the miss now
                         if (ANY) occ[idx] = 0;
                         else __stcs(reinterpret_cast<float4 *>(hits + idx),
@@ -130,8 +137,10 @@ int launch_persistent(rt_ctx *ctx, const rt_ray *rays, size_t n, const uint32_t 
     const int slot = st == ctx->stream ? 1 : (st == ctx->stream2 ? 2 : 0);
     unsigned long long *counter = reinterpret_cast<unsigned long long *>(ctx->d_status.as<char>() + 8 + 8 * slot);
     RT_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
+    const RootBox root{{ctx->root_box[0], ctx->root_box[1], ctx->root_box[2]},
+                       {ctx->root_box[3], ctx->root_box[4], ctx->root_box[5]}};
     k_trace_persistent<ANY, STACK><<<g, 128, 0, st>>>(ctx->d_nodes.as<BvhNode>(), ctx->d_tris.as<BvhTri>(), rays, n,
-                                                      n_dev, hits, occ, ctx->d_status.as<unsigned>(), counter);
+                                                      n_dev, hits, occ, ctx->d_status.as<unsigned>(), counter, root);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
