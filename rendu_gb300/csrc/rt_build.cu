@@ -200,7 +200,12 @@ __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
 }
 
 constexpr float kCostInner = 1.2f;  // relative cost of one node visit (two box tests)
-constexpr float kCostTri = 1.0f;    // relative cost of one triangle test
+// Relative cost of one triangle test. A leaf's triangles are tested in a loop whose length
+// varies from lane to lane, so on the GPU a triangle costs more than a node visit: with
+// this weight nearly every leaf holds one triangle, which measured fastest (closest hit on
+// 16M random rays into 1.3M triangles -6 %, the 2M-triangle path-traced scene -3 %,
+// against a weight of 1).
+constexpr float kCostTri = 3.0f;
 
 // Gather sorted triangle boxes (inflated by eps, making the traversal's box tests
 // conservative) and write leaf-order triangles.
