@@ -5,19 +5,15 @@
 //   D[m][n] = sum_k A[m][k] B[n][k],  m = output pixel, n = output channel.
 //
 // A CTA tile is a block of Wb x Hb = 128 pixels of one image (Wb = min(128, the next power
-// of two >= the width)). K runs over the 9 taps and, per tap, over channel chunks of the
-// input -- first those of input 0, then those of the skip input 1. A chunk is 64 channels,
-// or 32 when that pads the inputs' channel counts less (the 16- and 32-channel layers of
-// the finest level: half the K work of 64-channel chunks). The A operand of one (tap,
-// chunk) is a single tiled TMA box of CW channels x Wb x Hb pixels at (chunk, x0 + dx,
-// y0 + dy, image): the copy engine's zero fill outside the tensor is exactly the
+// of two >= the width)). K runs over the 9 taps and, per tap, over 64-channel chunks of
+// the input -- first those of input 0, then those of the skip input 1. The A operand of
+// one (tap, chunk) is a single tiled TMA box of 64 channels x Wb x Hb pixels at (chunk,
+// x0 + dx, y0 + dy, image): the copy engine's zero fill outside the tensor is exactly the
 // convolution's zero padding (and the zero channels of a chunk past the channel count).
-// The weights are packed to match: K-major rows [Cout][9 x chunks x CW], zero where a
+// The weights are packed to match: K-major rows [Cout][9 x chunks x 64], zero where a
 // chunk runs past the channel count; the B operand of a k-block is one 2-D box.
-// Both boxes land in the K-major swizzled layout that tcgen05.mma reads: one 128-byte row
-// per pixel / output channel with the 128-byte swizzle (8-row groups 1024 bytes apart) for
-// 64-channel chunks, one 64-byte row with the 64-byte swizzle (groups 512 bytes apart) for
-// 32-channel chunks.
+// Both boxes land in the 128-byte-swizzle K-major layout that tcgen05.mma reads (one
+// 128-byte row per pixel / output channel, 8-row groups 1024 bytes apart).
 //
 // The kernel is persistent and warp-specialised: one thread issues the TMA loads into a
 // ring of shared-memory stages (full[s]: the stage's bytes have landed; empty[s]: the MMAs
@@ -45,18 +41,11 @@ __device__ unsigned g_umma_status;  // nonzero: a bounded wait gave up (RT_ERR_T
 namespace {
 
 constexpr int TM = 128;       // tile rows (pixels): one TMEM lane each
+constexpr int KB = 64;        // K per stage: one 128-byte swizzle row of BF16
 constexpr int MAX_STAGES = 8;
 constexpr int EPI_WARPS = 4;  // TMEM lanes 32w..32w+31 = tile rows
 constexpr int THREADS = 32 * (EPI_WARPS + 2);  // + the TMA warp and the MMA warp
 constexpr unsigned long long kWaitNs = 2000000000ull;
-
-// Channels per K chunk for inputs of c0 and c1 channels: 32 when that pads the channel
-// counts less than 64-channel chunks do (the layers of 16 and 32 channels), else 64.
-__host__ __device__ __forceinline__ int chunk_width(int c0, int c1) {
-    const int p64 = (c0 + 63) / 64 * 64 + (c1 + 63) / 64 * 64;
-    const int p32 = (c0 + 31) / 32 * 32 + (c1 + 31) / 32 * 32;
-    return p32 < p64 ? 32 : 64;
-}
 
 __device__ __forceinline__ unsigned saddr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -110,16 +99,13 @@ __device__ __forceinline__ void tma_2d(unsigned dst, const CUtensorMap *map, int
         : "memory");
 }
 
-// Shared-memory matrix descriptor, K-major: rows of cw BF16 (64: 128-byte swizzle, 8-row
-// groups 1024 bytes apart; 32: 64-byte swizzle, groups 512 bytes apart).
-__device__ __forceinline__ unsigned long long sdesc(unsigned addr, int cw) {
-    const unsigned long long sbo = cw == 64 ? 1024 : 512;
-    const unsigned long long mode = cw == 64 ? 2 : 4;  // swizzling mode field: 128 B / 64 B
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ unsigned long long sdesc(unsigned addr) {
     return (unsigned long long)((addr & 0x3FFFFu) >> 4) |  // start address
            (1ull << 16) |                                  // leading byte offset (unused here)
-           ((sbo >> 4) << 32) |                            // stride byte offset
+           ((unsigned long long)(1024 >> 4) << 32) |       // stride byte offset
            (1ull << 46) |                                  // descriptor version
-           (mode << 61);
+           (2ull << 61);                                   // 128-byte swizzle
 }
 
 // Instruction descriptor, kind::f16: BF16 A and B (K-major), FP32 D, M = 128, N.
@@ -141,7 +127,7 @@ __device__ __forceinline__ void umma_commit(unsigned bar) {
 
 struct ConvTiles {
     int H, W, Wb, Hb, tx, ty;  // tiles of Wb x Hb pixels, tx x ty per image
-    int cw, seg0, cpt;         // channels per chunk (32 / 64); chunks per tap: of input 0, in total
+    int seg0, cpt;             // 64-channel chunks per tap: of input 0, in total
     int Cout, N, nhalf, mtiles, ntiles, stages;
     const float *bias;
     int relu;
@@ -155,8 +141,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     extern __shared__ unsigned char smem_raw[];
     const unsigned raw = saddr(smem_raw);
     const unsigned base = (raw + 1023u) & ~1023u;
-    const unsigned row_bytes = 2u * (unsigned)q.cw;
-    const unsigned a_bytes = TM * row_bytes, stage_bytes = a_bytes + (unsigned)q.N * row_bytes;
+    const unsigned a_bytes = TM * 128, stage_bytes = a_bytes + (unsigned)q.N * 128;
     const int S = q.stages;
     const unsigned bar0 = base + S * stage_bytes;
     auto full = [&](int st) { return bar0 + 8u * st; };
@@ -205,8 +190,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         // ---- TMA producer: one thread. Stage index and phase advance incrementally (this
         // thread's issue rate bounds the pipeline: no divisions in the loop).
         if (lane == 0) {
-            const unsigned tx_bytes = stage_bytes;
-            const int cw = q.cw;
+            const unsigned tx_bytes = a_bytes + (unsigned)q.N * 128;
             int st = 0;
             unsigned ph = 0;     // parity of the current use of stage st
             bool refill = false;  // every stage has been used once: wait for its MMAs first
@@ -216,14 +200,14 @@ __global__ void __launch_bounds__(THREADS, 1)
                 int kcoord = 0;
                 for (int tap = 0; tap < 9 && ok; ++tap) {
                     const int dy = tap / 3 - 1, dx = tap - 3 * (dy + 1) - 1;
-                    for (int j = 0; j < q.cpt; ++j, kcoord += cw) {
+                    for (int j = 0; j < q.cpt; ++j, kcoord += KB) {
                         if (refill && !(ok = mbar_wait(empty(st), ph ^ 1u))) break;
                         const unsigned sa = base + st * stage_bytes;
                         mbar_expect_tx(full(st), tx_bytes);
                         if (j < q.seg0)
-                            tma_4d(sa, &tm0, j * cw, x0 + dx, y0 + dy, n, full(st));
+                            tma_4d(sa, &tm0, j * KB, x0 + dx, y0 + dy, n, full(st));
                         else
-                            tma_4d(sa, &tm1, (j - q.seg0) * cw, x0 + dx, y0 + dy, n, full(st));
+                            tma_4d(sa, &tm1, (j - q.seg0) * KB, x0 + dx, y0 + dy, n, full(st));
                         tma_2d(sa + a_bytes, &tmw, kcoord, n0, full(st));
                         if (++st == S) {
                             st = 0;
@@ -239,7 +223,6 @@ __global__ void __launch_bounds__(THREADS, 1)
         // ---- MMA issue: one thread.
         if (lane == 0) {
             const unsigned id = idesc(q.N);
-            const int cw = q.cw, ksteps = q.cw / 16;
             int st = 0;
             unsigned ph = 0;
             for (int lt = 0; lt < my_tiles && ok; ++lt) {
@@ -251,8 +234,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if (!(ok = mbar_wait(full(st), ph))) break;
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
                     const unsigned sa = base + st * stage_bytes, sb = sa + a_bytes;
-                    for (int j = 0; j < ksteps; ++j)
-                        umma(d, sdesc(sa + 32 * j, cw), sdesc(sb + 32 * j, cw), id, (kb | j) ? 1u : 0u);
+#pragma unroll
+                    for (int j = 0; j < KB / 16; ++j)
+                        umma(d, sdesc(sa + 32 * j), sdesc(sb + 32 * j), id, (kb | j) ? 1u : 0u);
                     umma_commit(empty(st));
                     if (++st == S) {
                         st = 0;
@@ -349,38 +333,36 @@ __global__ void k_upsample2(const bf16 *__restrict__ x, int B, int h, int w, int
     *reinterpret_cast<uint4 *>(y + (((size_t)b * 2 * h + yy) * 2 * w + xx) * C + c) = v;
 }
 
-// Forward packing: wpk[co][(tap cpt + j) cw + cc] = w[tap][ci][co] for the input channel ci
+// Forward packing: wpk[co][(tap cpt + j) 64 + cc] = w[tap][ci][co] for the input channel ci
 // of chunk j (chunks of input 0 first, then of input 1), zero past either channel count.
 template <class T>
 __device__ __forceinline__ float pack_fwd_value(const T *w, int c0, int c1, int cout, size_t idx) {
-    const int cw = chunk_width(c0, c1);
-    const int seg0 = (c0 + cw - 1) / cw, cpt = seg0 + (c1 + cw - 1) / cw;
-    const size_t kp = (size_t)9 * cpt * cw;
+    const int seg0 = (c0 + 63) / 64, cpt = seg0 + (c1 + 63) / 64;
+    const size_t kp = (size_t)9 * cpt * 64;
     const int co = (int)(idx / kp);
     const int k = (int)(idx % kp);
-    const int kb = k / cw, cc = k % cw;
+    const int kb = k / 64, cc = k % 64;
     const int tap = kb / cpt, j = kb % cpt;
     int ci;
     if (j < seg0) {
-        ci = j * cw + cc;
+        ci = j * 64 + cc;
         if (ci >= c0) return 0.0f;
     } else {
-        const int c = (j - seg0) * cw + cc;
+        const int c = (j - seg0) * 64 + cc;
         if (c >= c1) return 0.0f;
         ci = c0 + c;
     }
     return (float)w[((size_t)tap * (c0 + c1) + ci) * cout + co];
 }
 
-// Data-gradient packing: wpkd[ci][(tap' cptd + j) cw + cc] = w[8 - tap'][ci][co = cw j + cc].
+// Data-gradient packing: wpkd[ci][(tap' cptd + j) 64 + cc] = w[8 - tap'][ci][co = 64 j + cc].
 __device__ __forceinline__ float pack_bwd_value(const float *w, int cin, int cout, size_t idx) {
-    const int cw = chunk_width(cout, 0);
-    const int cptd = (cout + cw - 1) / cw;
-    const size_t kp = (size_t)9 * cptd * cw;
+    const int cptd = (cout + 63) / 64;
+    const size_t kp = (size_t)9 * cptd * 64;
     const int ci = (int)(idx / kp);
     const int k = (int)(idx % kp);
-    const int kb = k / cw, cc = k % cw;
-    const int tap = kb / cptd, co = (kb % cptd) * cw + cc;
+    const int kb = k / 64, cc = k % 64;
+    const int tap = kb / cptd, co = (kb % cptd) * 64 + cc;
     if (co >= cout) return 0.0f;
     return w[((size_t)(8 - tap) * cin + ci) * cout + co];
 }
@@ -437,19 +419,18 @@ int encoder(EncodeTiled *out) {
     return RT_OK;
 }
 
-// NHWC BF16 activations (B, H, W, C) read as boxes of cw channels x Wb x Hb pixels.
-int map_activations(CUtensorMap *m, const bf16 *ptr, int B, int H, int W, int C, int Wb, int Hb, int cw) {
+// NHWC BF16 activations (B, H, W, C) read as boxes of 64 channels x Wb x Hb pixels.
+int map_activations(CUtensorMap *m, const bf16 *ptr, int B, int H, int W, int C, int Wb, int Hb) {
     EncodeTiled enc;
     int r = encoder(&enc);
     if (r != RT_OK) return r;
     const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
     const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
-    const cuuint32_t box[4] = {(cuuint32_t)cw, (cuuint32_t)Wb, (cuuint32_t)Hb, 1};
+    const cuuint32_t box[4] = {(cuuint32_t)KB, (cuuint32_t)Wb, (cuuint32_t)Hb, 1};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     const CUresult e = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(ptr), dims, strides, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE,
-                           cw == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
-                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (e != CUDA_SUCCESS) {
         set_error("activation tensor map rejected (error " + std::to_string((int)e) + ")");
         return RT_ERR_CUDA;
@@ -457,19 +438,18 @@ int map_activations(CUtensorMap *m, const bf16 *ptr, int B, int H, int W, int C,
     return RT_OK;
 }
 
-// Packed weights [rows][Kp] read as boxes of cw K x N rows.
-int map_weights(CUtensorMap *m, const bf16 *ptr, int Kp, int rows, int N, int cw) {
+// Packed weights [rows][Kp] read as boxes of 64 K x N rows.
+int map_weights(CUtensorMap *m, const bf16 *ptr, int Kp, int rows, int N) {
     EncodeTiled enc;
     int r = encoder(&enc);
     if (r != RT_OK) return r;
     const cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
-    const cuuint32_t box[2] = {(cuuint32_t)cw, (cuuint32_t)N};
+    const cuuint32_t box[2] = {(cuuint32_t)KB, (cuuint32_t)N};
     const cuuint32_t estr[2] = {1, 1};
     const CUresult e = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<bf16 *>(ptr), dims, strides, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE,
-                           cw == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
-                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (e != CUDA_SUCCESS) {
         set_error("weight tensor map rejected (error " + std::to_string((int)e) + ")");
         return RT_ERR_CUDA;
@@ -481,10 +461,7 @@ inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / 
 
 }  // namespace
 
-size_t packed_k(int c0, int c1) {
-    const int cw = chunk_width(c0, c1);
-    return (size_t)9 * ((c0 + cw - 1) / cw + (c1 + cw - 1) / cw) * cw;
-}
+size_t packed_k(int c0, int c1) { return (size_t)9 * ((c0 + 63) / 64 + (c1 + 63) / 64) * 64; }
 
 int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, const float *bias, int Cout, bool relu,
                       bf16 *out_bf, float *out_f, bf16 *ups, cudaStream_t st) {
@@ -507,9 +484,8 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
     q.Hb = TM / q.Wb;
     q.tx = (W + q.Wb - 1) / q.Wb;
     q.ty = (H + q.Hb - 1) / q.Hb;
-    q.cw = chunk_width(in.c0, in.c1);
-    q.seg0 = (in.c0 + q.cw - 1) / q.cw;
-    q.cpt = q.seg0 + (in.c1 + q.cw - 1) / q.cw;
+    q.seg0 = (in.c0 + 63) / 64;
+    q.cpt = q.seg0 + (in.c1 + 63) / 64;
     q.Cout = Cout;
     // N: the whole output in one tile when it fits the instruction (<= 256), else 128-wide tiles.
     q.N = Cout <= 256 ? (Cout + 15) / 16 * 16 : 128;
@@ -517,7 +493,7 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
     while (q.nhalf < q.N) q.nhalf *= 2;
     q.mtiles = B * q.tx * q.ty;
     q.ntiles = q.mtiles * ((Cout + q.N - 1) / q.N);
-    const size_t stage_bytes = ((size_t)TM + q.N) * 2 * q.cw;  // a multiple of 1024 (N % 16 == 0)
+    const size_t stage_bytes = (size_t)TM * 128 + (size_t)q.N * 128;
     const size_t fixed = 1024 + 8 * (2 * MAX_STAGES + 4) + 16;
     q.stages = (int)std::min<size_t>(MAX_STAGES, (220 * 1024 - fixed) / stage_bytes);
     q.bias = bias;
@@ -527,14 +503,14 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
     const size_t smem = q.stages * stage_bytes + fixed;
 
     CUtensorMap tm0, tm1, tmw;
-    int r = map_activations(&tm0, src0, B, H, W, in.c0, q.Wb, q.Hb, q.cw);
+    int r = map_activations(&tm0, src0, B, H, W, in.c0, q.Wb, q.Hb);
     if (r == RT_OK) {
         if (in.c1)
-            r = map_activations(&tm1, in.p1, B, H, W, in.c1, q.Wb, q.Hb, q.cw);
+            r = map_activations(&tm1, in.p1, B, H, W, in.c1, q.Wb, q.Hb);
         else
             tm1 = tm0;
     }
-    if (r == RT_OK) r = map_weights(&tmw, wpk, (int)packed_k(in.c0, in.c1), Cout, q.N, q.cw);
+    if (r == RT_OK) r = map_weights(&tmw, wpk, (int)packed_k(in.c0, in.c1), Cout, q.N);
     if (r != RT_OK) return r;
 
     static bool configured = false;
