@@ -120,28 +120,52 @@ class ClockSampler:
 
 
 def _dist():
+    """Process group of a torchrun launch (NCCL on GPUs, gloo without), or None for one
+    process: (dist, rank, world size)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws > 1:
+        import torch
         import torch.distributed as dist
 
-        dist.init_process_group("nccl")
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
         return dist, dist.get_rank(), ws
     return None, 0, 1
 
 
+def _device_of(dist, torch):
+    return "cuda" if (dist is None or dist.get_backend() == "nccl") and torch.cuda.is_available() else "cpu"
+
+
 def _sync_all(dist, torch):
-    torch.cuda.synchronize()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
-        torch.cuda.synchronize()
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
 
 
 def _max_over_ranks(dist, torch, v: float) -> float:
     if dist is None:
         return v
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    t = torch.tensor([v], dtype=torch.float64, device=_device_of(dist, torch))
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def _rank_seed(seed: int, rank: int) -> int:
+    """Each rank's own rays (weak scaling: fixed work per GPU, no data exchanged)."""
+    return seed + 1000 * rank
+
+
+def _job_rate(dist, torch, local_units: float, local_s: float) -> float:
+    """Whole-job throughput: the units of every rank over the slowest rank's time."""
+    total = local_units
+    if dist is not None:
+        t = torch.tensor([local_units], dtype=torch.float64, device=_device_of(dist, torch))
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        total = float(t.item())
+    return total / _max_over_ranks(dist, torch, local_s)
 
 
 def cpu_raycaster_rate(mesh, rays, target_s: float, threads: int):
@@ -540,7 +564,7 @@ def main():
     import rendu_gb300 as R
     from rendu_gb300 import scenes as S
 
-    mesh, rays = S.raycaster_workload(SUBDIV, N_RAYS, SEED + 1000 * rank)
+    mesh, rays = S.raycaster_workload(SUBDIV, N_RAYS, _rank_seed(SEED, rank))
     n = len(rays)
     rc = R.Raycaster(local)
     rc.add_mesh(mesh.positions, mesh.indices)
@@ -576,8 +600,9 @@ def main():
         rc.intersect_batch(d_rays, out=d_hits)
     ev1.record(stream)
     _sync_all(dist, torch)
-    t_closest = ev0.elapsed_time(ev1) / 1000.0
-    t_closest = _max_over_ranks(dist, torch, t_closest)
+    t_closest_local = ev0.elapsed_time(ev1) / 1000.0
+    value = _job_rate(dist, torch, n * args.steps, t_closest_local) / 1e6
+    t_closest = _max_over_ranks(dist, torch, t_closest_local)
 
     ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     _sync_all(dist, torch)
@@ -586,7 +611,9 @@ def main():
         rc.intersect_any_batch(d_rays, out=d_occ)
     eb.record(stream)
     _sync_all(dist, torch)
-    t_any = _max_over_ranks(dist, torch, ea.elapsed_time(eb) / 1000.0)
+    t_any_local = ea.elapsed_time(eb) / 1000.0
+    any_value = _job_rate(dist, torch, n * args.steps, t_any_local) / 1e6
+    t_any = _max_over_ranks(dist, torch, t_any_local)
 
     # ---- e2e through the public API with host buffers ----------------------------------
     host_hits = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy().view(R.HIT_DTYPE).reshape(-1)
@@ -597,7 +624,7 @@ def main():
     for _ in range(args.steps):
         rc.intersect_batch(host_rays, out=host_hits)
     _sync_all(dist, torch)
-    t_e2e = _max_over_ranks(dist, torch, time.perf_counter() - t0)
+    e2e_value = _job_rate(dist, torch, n * args.steps, time.perf_counter() - t0) / 1e6
 
     # ---- algorithmic bytes per ray (visit counts on a 1M-ray sample) -------------------
     nv, nt = rc.count_visits(rays[: 1 << 20])
@@ -615,8 +642,6 @@ def main():
     except OSError:
         pass
 
-    total_rays = n * world
-    value = total_rays * args.steps / t_closest / 1e6
     if rank == 0:
         out = {
             "metric": "Mrays/s (closest hit, raycaster workload)",
@@ -626,9 +651,9 @@ def main():
             "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "triangles": mesh.triangle_count, "rays_per_gpu": n,
                        "l2": "inputs larger than L2 (512 MB of rays per step)", "parallelism": f"replicas x{world}"},
-            "any_hit": {"value": round(total_rays * args.steps / t_any / 1e6, 2), "unit": "Mrays/s",
+            "any_hit": {"value": round(any_value, 2), "unit": "Mrays/s",
                         "ms_per_step": round(1000 * t_any / args.steps, 4)},
-            "e2e": {"value": round(total_rays * args.steps / t_e2e / 1e6, 2), "unit": "Mrays/s",
+            "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s",
                     "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 16},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
