@@ -15,16 +15,26 @@
 // Both boxes land in the 128-byte-swizzle K-major layout that tcgen05.mma reads (one
 // 128-byte row per pixel / output channel, 8-row groups 1024 bytes apart).
 //
-// The kernel is persistent and warp-specialised: one thread issues the TMA loads into a
+// Three kernels share that scheme. k_conv_umma takes any tile shape (small images: Wb < 128).
+// k_conv_rows takes row tiles (Wb = 128, Hb = 1) and reads one 130-pixel box per kernel row
+// for its three horizontal taps. k_conv_fold, used for row tiles whose output fits N <= 85
+// channels and whose weights fit in shared memory, moves the three horizontal taps into the
+// MMA's N dimension. On the GB300 each tcgen05.mma and tcgen05.commit costs about the same
+// whatever its N for these narrow layers (measured: tripling N changed nothing, removing the
+// MMAs removed a third of the time), so fewer and wider instructions are what pays.
+//
+// Each kernel is persistent and warp-specialised: one thread issues the TMA loads into a
 // ring of shared-memory stages (full[s]: the stage's bytes have landed; empty[s]: the MMAs
-// that read it have completed), one thread issues the MMAs into two TMEM accumulators
-// (tfull[a]: a tile is complete; tempty[a]: the epilogue has read it back), and four
-// epilogue warps read finished tiles with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31
-// = tile rows), add the bias, apply the ReLU and store BF16 or FP32 NHWC while the next
-// tile accumulates.
+// that read it have completed), one thread issues the MMAs into up to four TMEM
+// accumulators (tfull[a]: a tile is complete; tempty[a]: the epilogue has read it back),
+// and four epilogue groups of four warps, one group per accumulator, read finished tiles
+// with tcgen05.ld (the warp of lane quarter i owns TMEM lanes 32i..32i+31 = tile rows), add
+// the bias, apply the ReLU and store BF16 or FP32 NHWC while later tiles accumulate.
 //
 // Every mbarrier wait is bounded (about 2 s of %globaltimer); a wait that gives up sets
-// the status word and its role stops, and the CTA frees its TMEM before it returns.
+// the status word and its role stops, and the CTA frees its TMEM before it returns. The
+// macros DN_FOLD, DN_C32, DN_MAX_STAGES and DN_EPI_GROUPS select layout choices and are
+// kept selectable for measurement; the defaults are the measured best.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -42,10 +52,29 @@ namespace {
 
 constexpr int TM = 128;       // tile rows (pixels): one TMEM lane each
 constexpr int KB = 64;        // K per stage: one 128-byte swizzle row of BF16
-constexpr int MAX_STAGES = 8;
-constexpr int EPI_WARPS = 4;  // TMEM lanes 32w..32w+31 = tile rows
-constexpr int THREADS = 32 * (EPI_WARPS + 2);  // + the TMA warp and the MMA warp
+#ifndef DN_MAX_STAGES
+#define DN_MAX_STAGES 8
+#endif
+constexpr int MAX_STAGES = DN_MAX_STAGES;
+#ifndef DN_EPI_GROUPS
+#define DN_EPI_GROUPS 4
+#endif
+constexpr int EPI_WARPS = 4;                    // one epilogue warp per TMEM lane quarter
+constexpr int EPI_GROUPS = DN_EPI_GROUPS;       // accumulators in flight, one epilogue group each
+constexpr int PRODUCER_WARP = EPI_WARPS * EPI_GROUPS;
+constexpr int MMA_WARP = PRODUCER_WARP + 1;
+constexpr int THREADS = 32 * (MMA_WARP + 1);
+// mbarrier slots after the 2 x MAX_STAGES stage barriers
+constexpr int BAR_TFULL = 2 * MAX_STAGES, BAR_TEMPTY = BAR_TFULL + EPI_GROUPS, BAR_TMEM = BAR_TEMPTY + EPI_GROUPS,
+              BAR_W = BAR_TMEM + 1, BAR_COUNT = BAR_W + 1;
+constexpr size_t kFixed = 1024 + 8 * BAR_COUNT + 16;  // alignment slack, barriers, TMEM slot
 constexpr unsigned long long kWaitNs = 2000000000ull;
+#ifndef DN_FOLD
+#define DN_FOLD 1
+#endif
+#ifndef DN_C32
+#define DN_C32 1
+#endif
 
 __device__ __forceinline__ unsigned saddr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -108,6 +137,13 @@ __device__ __forceinline__ unsigned long long sdesc(unsigned addr) {
            (2ull << 61);                                   // 128-byte swizzle
 }
 
+// Shared-memory matrix descriptor: K-major, 64-byte swizzle (rows of 32 BF16 channels),
+// 8-row groups 512 bytes apart.
+__device__ __forceinline__ unsigned long long sdesc64(unsigned addr) {
+    return (unsigned long long)((addr & 0x3FFFFu) >> 4) | (1ull << 16) | ((unsigned long long)(512 >> 4) << 32) |
+           (1ull << 46) | (4ull << 61);
+}
+
 // Instruction descriptor, kind::f16: BF16 A and B (K-major), FP32 D, M = 128, N.
 __device__ __forceinline__ unsigned idesc(int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(n >> 3) << 17) | ((unsigned)(TM >> 4) << 24);
@@ -128,12 +164,112 @@ __device__ __forceinline__ void umma_commit(unsigned bar) {
 struct ConvTiles {
     int H, W, Wb, Hb, tx, ty;  // tiles of Wb x Hb pixels, tx x ty per image
     int seg0, cpt;             // 64-channel chunks per tap: of input 0, in total
+    int c0, c1;                // channels of input 0 and input 1
     int Cout, N, nhalf, mtiles, ntiles, stages;
+    int groups;                // accumulators in flight (groups x nhalf TMEM columns)
+    int wres;                  // row tiles: the weights stay resident in shared memory
+    int narrow0, narrow1;      // row tiles: input 0 / 1 read as 32-channel rows (64-byte swizzle)
+    unsigned astage;           // row tiles: bytes of a stage's row box
     const float *bias;
     int relu;
     bf16 *out_bf;
     float *out_f;
 };
+
+// K steps of 16 that chunk j actually holds: the MMAs over a chunk's zero-filled channels
+// (and the matching zero weights) are skipped.
+__device__ __forceinline__ int chunk_ksteps(const ConvTiles &q, int j) {
+    const int rem = j < q.seg0 ? q.c0 - KB * j : q.c1 - KB * (j - q.seg0);
+    return min(KB / 16, (rem + 15) / 16);
+}
+
+__device__ __forceinline__ void tmem_ld16(unsigned addr, unsigned (&v)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(addr));
+}
+
+// 16 output channels [cb, cb + 16) of pixel p: bias, ReLU, BF16 and/or FP32 store (channels
+// past Cout are dropped). Every array index is static, so the values stay in registers.
+__device__ __forceinline__ void store16(const ConvTiles &q, const unsigned (&v)[16], int cb, long p) {
+    const int Cout = q.Cout;
+    float f[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        float x_ = __uint_as_float(v[j]);
+        if (q.bias) x_ += __ldg(q.bias + min(cb + j, Cout - 1));
+        if (q.relu) x_ = fmaxf(x_, 0.0f);
+        f[j] = x_;
+    }
+    if (cb + 16 <= Cout) {
+        if (q.out_bf) {
+            __nv_bfloat162 h[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) h[j] = __floats2bfloat162_rn(f[2 * j], f[2 * j + 1]);
+            uint4 *dst = reinterpret_cast<uint4 *>(q.out_bf + p * Cout + cb);
+            dst[0] = *reinterpret_cast<uint4 *>(&h[0]);
+            dst[1] = *reinterpret_cast<uint4 *>(&h[4]);
+        }
+        if (q.out_f) {
+            float4 *dst = reinterpret_cast<float4 *>(q.out_f + p * Cout + cb);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) dst[j] = make_float4(f[4 * j], f[4 * j + 1], f[4 * j + 2], f[4 * j + 3]);
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            if (cb + j < Cout) {
+                if (q.out_bf) q.out_bf[p * Cout + cb + j] = __float2bfloat16_rn(f[j]);
+                if (q.out_f) q.out_f[p * Cout + cb + j] = f[j];
+            }
+    }
+}
+
+// Epilogue: group g (warps 4g..4g+3) reads the tiles of accumulator g (every groups-th tile);
+// its warp of lane quarter i reads TMEM lanes 32i..32i+31 (tile rows = pixels 32i..32i+31
+// of the Wb x Hb block) 32 columns at a time, and hands the accumulator back to the MMA
+// thread as soon as its last columns are in registers, before the bias, ReLU and NHWC
+// stores of those. Several groups keep several tiles' stores in flight on each SM
+// sub-partition. False if a wait gave up.
+template <class Origin>
+__device__ __forceinline__ bool epilogue(const ConvTiles &q, unsigned tmem, unsigned bar0, int my_tiles,
+                                         const Origin &tile_origin) {
+    const int warp = threadIdx.x >> 5, g = warp / EPI_WARPS, quarter = warp % EPI_WARPS;
+    if (g >= q.groups) return true;
+    const int row = (int)threadIdx.x & (TM - 1);  // = 32 quarter + lane
+    const int xl = row % q.Wb, yl = row / q.Wb;
+    const unsigned tfull = bar0 + 8u * (BAR_TFULL + g), tempty = bar0 + 8u * (BAR_TEMPTY + g);
+    unsigned use = 0;
+    for (int lt = g; lt < my_tiles; lt += q.groups, ++use) {
+        if (!__all_sync(0xffffffffu, mbar_wait(tfull, use & 1u))) return false;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        int x0, y0, n, n0;
+        tile_origin((int)blockIdx.x + lt * (int)gridDim.x, x0, y0, n, n0);
+        const int x = x0 + xl, y = y0 + yl;
+        const bool inside = x < q.W && y < q.H;
+        const long p = ((long)n * q.H + y) * q.W + x;
+        const unsigned taddr = tmem + ((unsigned)(32 * quarter) << 16) + (unsigned)(g * q.nhalf);
+        for (int c0 = 0; c0 < q.N; c0 += 32) {
+            const bool two = c0 + 16 < q.N;
+            unsigned va[16], vb[16];
+            tmem_ld16(taddr + c0, va);
+            if (two) tmem_ld16(taddr + c0 + 16, vb);
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (c0 + 32 >= q.N) {  // the accumulator is free for the MMAs again
+                asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+                mbar_arrive(tempty);
+            }
+            const int cb = n0 + c0;
+            if (inside && cb < q.Cout) {
+                store16(q, va, cb, p);
+                if (two && cb + 16 < q.Cout) store16(q, vb, cb + 16, p);
+            }
+        }
+    }
+    return true;
+}
 
 __global__ void __launch_bounds__(THREADS, 1)
     k_conv_umma(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
@@ -146,9 +282,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     const unsigned bar0 = base + S * stage_bytes;
     auto full = [&](int st) { return bar0 + 8u * st; };
     auto empty = [&](int st) { return bar0 + 8u * (MAX_STAGES + st); };
-    auto tfull = [&](int a) { return bar0 + 8u * (2 * MAX_STAGES + a); };
-    auto tempty = [&](int a) { return bar0 + 8u * (2 * MAX_STAGES + 2 + a); };
-    const unsigned tmem_slot = bar0 + 8u * (2 * MAX_STAGES + 4);
+    auto tfull = [&](int a) { return bar0 + 8u * (BAR_TFULL + a); };
+    auto tempty = [&](int a) { return bar0 + 8u * (BAR_TEMPTY + a); };
+    const unsigned tmem_slot = bar0 + 8u * BAR_TMEM;
     const unsigned *tmem_slot_ptr = reinterpret_cast<const unsigned *>(smem_raw + (tmem_slot - raw));
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -166,7 +302,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tmem_slot),
-                     "r"(2 * q.nhalf));
+                     "r"(q.groups * q.nhalf));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
     }
     if (tid == 0) {
@@ -174,7 +310,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             mbar_init(full(st), 1);
             mbar_init(empty(st), 1);
         }
-        for (int a = 0; a < 2; ++a) {
+        for (int a = 0; a < EPI_GROUPS; ++a) {
             mbar_init(tfull(a), 1);
             mbar_init(tempty(a), 32 * EPI_WARPS);
         }
@@ -186,7 +322,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     const unsigned tmem = *tmem_slot_ptr;
     bool ok = true;
 
-    if (warp == EPI_WARPS) {
+    if (warp == PRODUCER_WARP) {
         // ---- TMA producer: one thread. Stage index and phase advance incrementally (this
         // thread's issue rate bounds the pipeline: no divisions in the loop).
         if (lane == 0) {
@@ -219,24 +355,439 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
         }
         __syncwarp();
-    } else if (warp == EPI_WARPS + 1) {
+    } else if (warp == MMA_WARP) {
         // ---- MMA issue: one thread.
         if (lane == 0) {
             const unsigned id = idesc(q.N);
             int st = 0;
             unsigned ph = 0;
+            int a = 0;         // accumulator of tile lt
+            unsigned use = 0;  // earlier tiles in accumulator a
             for (int lt = 0; lt < my_tiles && ok; ++lt) {
-                const int a = lt & 1;
-                if (lt >= 2 && !(ok = mbar_wait(tempty(a), (unsigned)((lt >> 1) - 1) & 1u))) break;
+                if (use > 0 && !(ok = mbar_wait(tempty(a), (use - 1) & 1u))) break;
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
                 const unsigned d = tmem + (unsigned)(a * q.nhalf);
-                for (int kb = 0; kb < KT; ++kb) {
+                unsigned acc = 0;
+                for (int kb = 0, j = 0; kb < KT; ++kb) {
                     if (!(ok = mbar_wait(full(st), ph))) break;
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
                     const unsigned sa = base + st * stage_bytes, sb = sa + a_bytes;
+                    const int ks = chunk_ksteps(q, j);
+                    for (int kk = 0; kk < ks; ++kk) {
+                        umma(d, sdesc(sa + 32 * kk), sdesc(sb + 32 * kk), id, acc);
+                        acc = 1;
+                    }
+                    umma_commit(empty(st));
+                    if (++st == S) {
+                        st = 0;
+                        ph ^= 1u;
+                    }
+                    if (++j == q.cpt) j = 0;
+                }
+                if (ok) umma_commit(tfull(a));
+                if (++a == q.groups) {
+                    a = 0;
+                    ++use;
+                }
+            }
+        }
+        __syncwarp();
+    } else {
+        ok = epilogue(q, tmem, bar0, my_tiles, tile_origin);
+    }
+    if (!ok) atomicOr(&g_umma_status, 1u);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(q.groups * q.nhalf));
+    }
+}
+
+// Row tiles (Wb = 128, Hb = 1: every tile is 128 pixels of one image row). The three
+// horizontal taps of one kernel row read the same pixels shifted by one, so one TMA box of
+// 130 pixels x 64 channels at (x0 - 1, y0 + dy) serves all three: the A operand of tap dx
+// (-1, 0, 1) starts dx + 1 rows of 128 bytes into the box. Per tile and 64-channel chunk
+// that is three boxes instead of nine. The 128-byte swizzle is a function of the
+// shared-memory address (bits 4-6 XOR bits 7-9, as TMA writes it), so a descriptor that
+// starts one or two rows into the box reads the shifted rows correctly with its base-offset
+// field left at 0 (measured: the parity tests fail when that field carries the row phase).
+// When every k-block of the packed weights fits in shared memory beside the pipeline (one
+// output-channel tile), the weights are loaded once per CTA and stay resident; otherwise
+// each stage also carries the three k-blocks of its taps.
+constexpr int HALO = TM + 2;                  // pixels of a row box
+constexpr unsigned HALO_BYTES = HALO * 128;   // bytes of a row box of 64 channels (16,640)
+constexpr unsigned HALO_STAGE = 17 * 1024;    // ... rounded up to the 1024-byte swizzle period
+constexpr unsigned HALO32_BYTES = HALO * 64;  // bytes of a row box of 32 channels (8,320)
+constexpr unsigned HALO32_STAGE = 9 * 1024;
+
+// Three taps (dx = -1, 0, 1) of one row box: KS K steps of 16 each. The descriptors' address
+// field counts 16-byte units: a K step is 32 bytes (+2), a row is rstep units.
+template <int KS>
+__device__ __forceinline__ void mma_taps(unsigned d, unsigned long long ad, const unsigned long long (&bd)[3],
+                                         unsigned rstep, unsigned id, unsigned &acc) {
 #pragma unroll
-                    for (int j = 0; j < KB / 16; ++j)
-                        umma(d, sdesc(sa + 32 * j), sdesc(sb + 32 * j), id, (kb | j) ? 1u : 0u);
+    for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+        for (int kk = 0; kk < KS; ++kk) {
+            umma(d, ad + dx * rstep + 2 * kk, bd[dx] + 2 * kk, id, acc);
+            acc = 1;
+        }
+}
+
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_conv_rows(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
+                const __grid_constant__ CUtensorMap tmw, const ConvTiles q) {
+    extern __shared__ unsigned char smem_raw[];
+    const unsigned raw = saddr(smem_raw);
+    const unsigned base = (raw + 1023u) & ~1023u;
+    const unsigned kblk = (unsigned)q.N * 128;  // one k-block of weights: N rows x 64 K
+    const int KT = 9 * q.cpt;
+    const unsigned wbytes = q.wres ? (unsigned)KT * kblk : 0u;
+    const unsigned stage_bytes = q.astage + (q.wres ? 0u : 3u * kblk);
+    const int S = q.stages;
+    const unsigned sbase = base + wbytes;
+    const unsigned bar0 = sbase + S * stage_bytes;
+    auto full = [&](int st) { return bar0 + 8u * st; };
+    auto empty = [&](int st) { return bar0 + 8u * (MAX_STAGES + st); };
+    auto tfull = [&](int a) { return bar0 + 8u * (BAR_TFULL + a); };
+    auto tempty = [&](int a) { return bar0 + 8u * (BAR_TEMPTY + a); };
+    const unsigned tmem_slot = bar0 + 8u * BAR_TMEM;
+    const unsigned wfull = bar0 + 8u * BAR_W;
+    const unsigned *tmem_slot_ptr = reinterpret_cast<const unsigned *>(smem_raw + (tmem_slot - raw));
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int my_tiles = q.ntiles > (int)blockIdx.x ? (q.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    auto tile_origin = [&](int t, int &x0, int &y0, int &n, int &n0) {
+        const int mt = t % q.mtiles;
+        n0 = (t / q.mtiles) * q.N;
+        x0 = (mt % q.tx) * TM;
+        const int r = mt / q.tx;
+        y0 = r % q.ty;
+        n = r / q.ty;
+    };
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tmem_slot),
+                     "r"(q.groups * q.nhalf));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        for (int st = 0; st < S; ++st) {
+            mbar_init(full(st), 1);
+            mbar_init(empty(st), 1);
+        }
+        for (int a = 0; a < EPI_GROUPS; ++a) {
+            mbar_init(tfull(a), 1);
+            mbar_init(tempty(a), 32 * EPI_WARPS);
+        }
+        mbar_init(wfull, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    const unsigned tmem = *tmem_slot_ptr;
+    bool ok = true;
+
+    if (warp == PRODUCER_WARP) {
+        // ---- TMA producer: one thread.
+        if (lane == 0) {
+            if (q.wres && my_tiles > 0) {
+                mbar_expect_tx(wfull, wbytes);
+                for (int kb = 0; kb < KT; ++kb) tma_2d(base + kb * kblk, &tmw, kb * KB, 0, wfull);
+            }
+            const unsigned wtx = q.wres ? 0u : 3u * kblk;
+            int st = 0;
+            unsigned ph = 0;
+            bool refill = false;
+            for (int lt = 0; lt < my_tiles && ok; ++lt) {
+                int x0, y0, n, n0;
+                tile_origin((int)blockIdx.x + lt * (int)gridDim.x, x0, y0, n, n0);
+                for (int j = 0; j < q.cpt && ok; ++j) {
+                    const bool in0 = j < q.seg0;
+                    const bool narrow = in0 ? q.narrow0 : q.narrow1;
+                    const unsigned tx_bytes = (narrow ? HALO32_BYTES : HALO_BYTES) + wtx;
+                    for (int dy = -1; dy <= 1; ++dy) {
+                        if (refill && !(ok = mbar_wait(empty(st), ph ^ 1u))) break;
+                        const unsigned sa = sbase + st * stage_bytes;
+                        mbar_expect_tx(full(st), tx_bytes);
+                        if (in0)
+                            tma_4d(sa, &tm0, j * KB, x0 - 1, y0 + dy, n, full(st));
+                        else
+                            tma_4d(sa, &tm1, (j - q.seg0) * KB, x0 - 1, y0 + dy, n, full(st));
+                        if (!q.wres)
+                            for (int dx = 0; dx < 3; ++dx)
+                                tma_2d(sa + q.astage + dx * kblk, &tmw, (((dy + 1) * 3 + dx) * q.cpt + j) * KB, n0,
+                                       full(st));
+                        if (++st == S) {
+                            st = 0;
+                            ph ^= 1u;
+                            refill = true;
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == MMA_WARP) {
+        // ---- MMA issue: one thread; three taps per stage.
+        if (lane == 0) {
+            const unsigned id = idesc(q.N);
+            if (q.wres && my_tiles > 0) ok = mbar_wait(wfull, 0);
+            int st = 0;
+            unsigned ph = 0;
+            int a = 0;         // accumulator of tile lt
+            unsigned use = 0;  // earlier tiles in accumulator a
+            for (int lt = 0; lt < my_tiles && ok; ++lt) {
+                if (use > 0 && !(ok = mbar_wait(tempty(a), (use - 1) & 1u))) break;
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+                const unsigned d = tmem + (unsigned)(a * q.nhalf);
+                unsigned acc = 0;
+                for (int j = 0; j < q.cpt && ok; ++j) {
+                    const bool narrow = j < q.seg0 ? q.narrow0 : q.narrow1;
+                    const int ks = chunk_ksteps(q, j);
+                    for (int dy = 0; dy < 3; ++dy) {
+                        if (!(ok = mbar_wait(full(st), ph))) break;
+                        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+                        const unsigned sa = sbase + st * stage_bytes;
+                        const unsigned long long ad = narrow ? sdesc64(sa) : sdesc(sa);
+                        const unsigned rstep = narrow ? 4u : 8u;
+                        unsigned long long bd[3];
+#pragma unroll
+                        for (int dx = 0; dx < 3; ++dx)
+                            bd[dx] = sdesc(q.wres ? base + (unsigned)((dy * 3 + dx) * q.cpt + j) * kblk
+                                                  : sa + q.astage + dx * kblk);
+                        switch (ks) {
+                            case 1: mma_taps<1>(d, ad, bd, rstep, id, acc); break;
+                            case 2: mma_taps<2>(d, ad, bd, rstep, id, acc); break;
+                            case 3: mma_taps<3>(d, ad, bd, rstep, id, acc); break;
+                            default: mma_taps<4>(d, ad, bd, rstep, id, acc); break;
+                        }
+                        umma_commit(empty(st));
+                        if (++st == S) {
+                            st = 0;
+                            ph ^= 1u;
+                        }
+                    }
+                }
+                if (ok) umma_commit(tfull(a));
+                if (++a == q.groups) {
+                    a = 0;
+                    ++use;
+                }
+            }
+        }
+        __syncwarp();
+    } else {
+        ok = epilogue(q, tmem, bar0, my_tiles, tile_origin);
+    }
+    if (!ok) atomicOr(&g_umma_status, 1u);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(q.groups * q.nhalf));
+    }
+}
+
+// Folded row tiles. The three horizontal taps go into N instead of into three MMAs: with
+// A = 128 input pixels and B = the weights of taps (dy, -1), (dy, 0), (dy, +1) stacked as
+// 3 N rows, D[r][(b, co)] is tap dx = b - 1's contribution of input pixel r. The output at
+// pixel r sums D[r - 1][(0, co)], D[r][(1, co)] and D[r + 1][(2, co)] over dy and the
+// chunks, and the epilogue gathers the neighbours' columns with warp shuffles. So that no
+// neighbour lies in another warp, lane quarter i (A rows 32i..32i+31) holds input pixels
+// x0 - 1 + 30i + (0..31) and outputs its lanes 1..30: a tile yields 120 outputs (the widths
+// of a 1920-pixel pyramid are multiples of 120) and reads four 32-pixel boxes per row.
+// One stage holds the three rows (dy) of one chunk and is released by one commit: per tile
+// cpt x 3 x K-steps MMAs of N = 3 Cout and cpt + 1 commits (6 MMAs and 2 commits for
+// 32 -> 32 channels, against 18 MMAs of N = 32 and 4 commits unfolded). The weights are
+// resident, laid out [dy][chunk][dx][N rows].
+constexpr int FOLD_OUT = 120;               // outputs per folded tile
+constexpr int FOLD_STEP = 30;               // outputs per lane quarter
+constexpr unsigned ROW_BOX = TM * 128;      // 128 rows of 64 channels (16 KB)
+constexpr unsigned ROW32_BOX = TM * 64;     // 128 rows of 32 channels (8 KB)
+
+template <int KS>
+__device__ __forceinline__ void mma_rows3(unsigned d, unsigned long long ad, unsigned abox16,
+                                          const unsigned long long (&bd)[3], unsigned id, unsigned &acc) {
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+        for (int kk = 0; kk < KS; ++kk) {
+            umma(d, ad + dy * abox16 + 2 * kk, bd[dy] + 2 * kk, id, acc);
+            acc = 1;
+        }
+}
+
+// Epilogue of the folded tiles: group g reads accumulator g, 16 output channels at a time
+// (columns c0, N + c0, 2N + c0), adds each row's neighbours' columns and stores lanes 1..30.
+template <class Origin>
+__device__ __forceinline__ bool epilogue_fold(const ConvTiles &q, unsigned tmem, unsigned bar0, int my_tiles,
+                                              const Origin &tile_origin) {
+    const int warp = threadIdx.x >> 5, g = warp / EPI_WARPS, quarter = warp % EPI_WARPS;
+    const int lane = threadIdx.x & 31;
+    if (g >= q.groups) return true;
+    const unsigned tfull = bar0 + 8u * (BAR_TFULL + g), tempty = bar0 + 8u * (BAR_TEMPTY + g);
+    unsigned use = 0;
+    for (int lt = g; lt < my_tiles; lt += q.groups, ++use) {
+        if (!__all_sync(0xffffffffu, mbar_wait(tfull, use & 1u))) return false;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+        int x0, y0, n, n0;
+        tile_origin((int)blockIdx.x + lt * (int)gridDim.x, x0, y0, n, n0);
+        const int x = x0 - 1 + FOLD_STEP * quarter + lane;
+        const bool store = lane >= 1 && lane <= FOLD_STEP && x < q.W;
+        const long p = ((long)n * q.H + y0) * q.W + x;
+        const unsigned taddr = tmem + ((unsigned)(32 * quarter) << 16) + (unsigned)(g * q.nhalf);
+        for (int c0 = 0; c0 < q.N; c0 += 16) {
+            unsigned b0[16], b1[16], b2[16];
+            tmem_ld16(taddr + c0, b0);
+            tmem_ld16(taddr + q.N + c0, b1);
+            tmem_ld16(taddr + 2 * q.N + c0, b2);
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if (c0 + 16 >= q.N) {  // the accumulator is free for the MMAs again
+                asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+                mbar_arrive(tempty);
+            }
+            unsigned v[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const float up = __shfl_up_sync(0xffffffffu, __uint_as_float(b0[j]), 1);
+                const float dn = __shfl_down_sync(0xffffffffu, __uint_as_float(b2[j]), 1);
+                v[j] = __float_as_uint(up + __uint_as_float(b1[j]) + dn);
+            }
+            const int cb = n0 + c0;
+            if (store && cb < q.Cout) store16(q, v, cb, p);
+        }
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_conv_fold(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
+                const __grid_constant__ CUtensorMap tmw, const ConvTiles q) {
+    extern __shared__ unsigned char smem_raw[];
+    const unsigned raw = saddr(smem_raw);
+    const unsigned base = (raw + 1023u) & ~1023u;
+    const unsigned kblk = (unsigned)q.N * 128;
+    const int KT = 9 * q.cpt;
+    const unsigned wbytes = (unsigned)KT * kblk;
+    const unsigned stage_bytes = q.astage;  // three row boxes
+    const int S = q.stages;
+    const unsigned sbase = base + wbytes;
+    const unsigned bar0 = sbase + S * stage_bytes;
+    auto full = [&](int st) { return bar0 + 8u * st; };
+    auto empty = [&](int st) { return bar0 + 8u * (MAX_STAGES + st); };
+    auto tfull = [&](int a) { return bar0 + 8u * (BAR_TFULL + a); };
+    auto tempty = [&](int a) { return bar0 + 8u * (BAR_TEMPTY + a); };
+    const unsigned tmem_slot = bar0 + 8u * BAR_TMEM;
+    const unsigned wfull = bar0 + 8u * BAR_W;
+    const unsigned *tmem_slot_ptr = reinterpret_cast<const unsigned *>(smem_raw + (tmem_slot - raw));
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int my_tiles = q.ntiles > (int)blockIdx.x ? (q.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    auto tile_origin = [&](int t, int &x0, int &y0, int &n, int &n0) {
+        const int mt = t % q.mtiles;
+        n0 = 0;
+        x0 = (mt % q.tx) * FOLD_OUT;
+        const int r = mt / q.tx;
+        y0 = r % q.ty;
+        n = r / q.ty;
+    };
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tmem_slot),
+                     "r"(q.groups * q.nhalf));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        for (int st = 0; st < S; ++st) {
+            mbar_init(full(st), 1);
+            mbar_init(empty(st), 1);
+        }
+        for (int a = 0; a < EPI_GROUPS; ++a) {
+            mbar_init(tfull(a), 1);
+            mbar_init(tempty(a), 32 * EPI_WARPS);
+        }
+        mbar_init(wfull, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    const unsigned tmem = *tmem_slot_ptr;
+    bool ok = true;
+
+    if (warp == PRODUCER_WARP) {
+        if (lane == 0) {
+            if (my_tiles > 0) {
+                // packed k-block (tap, j) -> resident slot [dy][j][dx]
+                mbar_expect_tx(wfull, wbytes);
+                for (int kb = 0; kb < KT; ++kb) {
+                    const int tap = kb / q.cpt, j = kb - tap * q.cpt, dy = tap / 3, dx = tap - 3 * dy;
+                    tma_2d(base + (unsigned)((dy * q.cpt + j) * 3 + dx) * kblk, &tmw, kb * KB, 0, wfull);
+                }
+            }
+            int st = 0;
+            unsigned ph = 0;
+            bool refill = false;
+            for (int lt = 0; lt < my_tiles && ok; ++lt) {
+                int x0, y0, n, n0;
+                tile_origin((int)blockIdx.x + lt * (int)gridDim.x, x0, y0, n, n0);
+                for (int j = 0; j < q.cpt; ++j) {
+                    if (refill && !(ok = mbar_wait(empty(st), ph ^ 1u))) break;
+                    const bool in0 = j < q.seg0;
+                    const unsigned box = (in0 ? q.narrow0 : q.narrow1) ? ROW32_BOX : ROW_BOX;
+                    const unsigned sa = sbase + st * stage_bytes;
+                    mbar_expect_tx(full(st), 3 * box);
+                    for (int dy = 0; dy < 3; ++dy)
+                        for (int i = 0; i < EPI_WARPS; ++i) {  // 32-pixel boxes, 30 apart
+                            const unsigned dst = sa + dy * box + i * (box / EPI_WARPS);
+                            const int xi = x0 - 1 + FOLD_STEP * i;
+                            if (in0)
+                                tma_4d(dst, &tm0, j * KB, xi, y0 + dy - 1, n, full(st));
+                            else
+                                tma_4d(dst, &tm1, (j - q.seg0) * KB, xi, y0 + dy - 1, n, full(st));
+                        }
+                    if (++st == S) {
+                        st = 0;
+                        ph ^= 1u;
+                        refill = true;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == MMA_WARP) {
+        if (lane == 0) {
+            const unsigned id = idesc(3 * q.N);
+            if (my_tiles > 0) ok = mbar_wait(wfull, 0);
+            int st = 0;
+            unsigned ph = 0;
+            int a = 0;
+            unsigned use = 0;
+            for (int lt = 0; lt < my_tiles && ok; ++lt) {
+                if (use > 0 && !(ok = mbar_wait(tempty(a), (use - 1) & 1u))) break;
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+                const unsigned d = tmem + (unsigned)(a * q.nhalf);
+                unsigned acc = 0;
+                for (int j = 0; j < q.cpt; ++j) {
+                    if (!(ok = mbar_wait(full(st), ph))) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+                    const bool narrow = j < q.seg0 ? q.narrow0 : q.narrow1;
+                    const unsigned sa = sbase + st * stage_bytes;
+                    const unsigned long long ad = narrow ? sdesc64(sa) : sdesc(sa);
+                    const unsigned abox16 = (narrow ? ROW32_BOX : ROW_BOX) >> 4;
+                    unsigned long long bd[3];
+#pragma unroll
+                    for (int dy = 0; dy < 3; ++dy) bd[dy] = sdesc(base + (unsigned)((dy * q.cpt + j) * 3) * kblk);
+                    switch (chunk_ksteps(q, j)) {
+                        case 1: mma_rows3<1>(d, ad, abox16, bd, id, acc); break;
+                        case 2: mma_rows3<2>(d, ad, abox16, bd, id, acc); break;
+                        case 3: mma_rows3<3>(d, ad, abox16, bd, id, acc); break;
+                        default: mma_rows3<4>(d, ad, abox16, bd, id, acc); break;
+                    }
                     umma_commit(empty(st));
                     if (++st == S) {
                         st = 0;
@@ -244,76 +795,22 @@ __global__ void __launch_bounds__(THREADS, 1)
                     }
                 }
                 if (ok) umma_commit(tfull(a));
+                if (++a == q.groups) {
+                    a = 0;
+                    ++use;
+                }
             }
         }
         __syncwarp();
     } else {
-        // ---- epilogue: warp w reads TMEM lanes 32w..32w+31, i.e. tile row tid.
-        const int xl = tid % q.Wb, yl = tid / q.Wb;
-        for (int lt = 0; lt < my_tiles; ++lt) {
-            const int a = lt & 1;
-            ok = __all_sync(0xffffffffu, mbar_wait(tfull(a), (unsigned)(lt >> 1) & 1u));
-            if (!ok) break;
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-            int x0, y0, n, n0;
-            tile_origin((int)blockIdx.x + lt * (int)gridDim.x, x0, y0, n, n0);
-            const int x = x0 + xl, y = y0 + yl;
-            const bool inside = x < q.W && y < q.H;
-            const long p = ((long)n * q.H + y) * q.W + x;
-            const int Cout = q.Cout;
-            for (int c0 = 0; c0 < q.N; c0 += 16) {
-                unsigned v[16];
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                    "[%16];\n"
-                    : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                      "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
-                      "=r"(v[15])
-                    : "r"(tmem + ((unsigned)(32 * warp) << 16) + (unsigned)(a * q.nhalf + c0)));
-                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                const int cb = n0 + c0;
-                if (inside && cb < Cout) {
-                    float f[16];
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        float x_ = __uint_as_float(v[j]);
-                        if (q.bias) x_ += q.bias[cb + j < Cout ? cb + j : cb];
-                        if (q.relu) x_ = fmaxf(x_, 0.0f);
-                        f[j] = x_;
-                    }
-                    if (cb + 16 <= Cout) {
-                        if (q.out_bf) {
-                            __nv_bfloat162 h[8];
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) h[j] = __floats2bfloat162_rn(f[2 * j], f[2 * j + 1]);
-                            uint4 *dst = reinterpret_cast<uint4 *>(q.out_bf + p * Cout + cb);
-                            dst[0] = *reinterpret_cast<uint4 *>(&h[0]);
-                            dst[1] = *reinterpret_cast<uint4 *>(&h[4]);
-                        }
-                        if (q.out_f) {
-                            float4 *dst = reinterpret_cast<float4 *>(q.out_f + p * Cout + cb);
-#pragma unroll
-                            for (int j = 0; j < 4; ++j)
-                                dst[j] = make_float4(f[4 * j], f[4 * j + 1], f[4 * j + 2], f[4 * j + 3]);
-                        }
-                    } else {
-                        for (int j = 0; j < 16 && cb + j < Cout; ++j) {
-                            if (q.out_bf) q.out_bf[p * Cout + cb + j] = __float2bfloat16_rn(f[j]);
-                            if (q.out_f) q.out_f[p * Cout + cb + j] = f[j];
-                        }
-                    }
-                }
-            }
-            asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
-            mbar_arrive(tempty(a));
-        }
+        ok = epilogue_fold(q, tmem, bar0, my_tiles, tile_origin);
     }
     if (!ok) atomicOr(&g_umma_status, 1u);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(2 * q.nhalf));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(q.groups * q.nhalf));
     }
 }
 
@@ -419,18 +916,19 @@ int encoder(EncodeTiled *out) {
     return RT_OK;
 }
 
-// NHWC BF16 activations (B, H, W, C) read as boxes of 64 channels x Wb x Hb pixels.
-int map_activations(CUtensorMap *m, const bf16 *ptr, int B, int H, int W, int C, int Wb, int Hb) {
+// NHWC BF16 activations (B, H, W, C) read as boxes of 64 channels x bw x bh pixels (128-byte
+// swizzle), or of 32 channels (64-byte swizzle) when narrow.
+int map_activations(CUtensorMap *m, const bf16 *ptr, int B, int H, int W, int C, int bw, int bh, bool narrow) {
     EncodeTiled enc;
     int r = encoder(&enc);
     if (r != RT_OK) return r;
     const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
     const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
-    const cuuint32_t box[4] = {(cuuint32_t)KB, (cuuint32_t)Wb, (cuuint32_t)Hb, 1};
+    const cuuint32_t box[4] = {(cuuint32_t)(narrow ? KB / 2 : KB), (cuuint32_t)bw, (cuuint32_t)bh, 1};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     const CUresult e = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(ptr), dims, strides, box, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, narrow ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (e != CUDA_SUCCESS) {
         set_error("activation tensor map rejected (error " + std::to_string((int)e) + ")");
         return RT_ERR_CUDA;
@@ -486,27 +984,64 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
     q.ty = (H + q.Hb - 1) / q.Hb;
     q.seg0 = (in.c0 + 63) / 64;
     q.cpt = q.seg0 + (in.c1 + 63) / 64;
+    q.c0 = in.c0;
+    q.c1 = in.c1;
     q.Cout = Cout;
     // N: the whole output in one tile when it fits the instruction (<= 256), else 128-wide tiles.
     q.N = Cout <= 256 ? (Cout + 15) / 16 * 16 : 128;
-    q.nhalf = 32;  // TMEM columns of one of the two accumulators
+    q.nhalf = 32;  // TMEM columns of one accumulator
     while (q.nhalf < q.N) q.nhalf *= 2;
+    q.groups = std::min(EPI_GROUPS, 512 / q.nhalf);
     q.mtiles = B * q.tx * q.ty;
     q.ntiles = q.mtiles * ((Cout + q.N - 1) / q.N);
-    const size_t stage_bytes = (size_t)TM * 128 + (size_t)q.N * 128;
-    const size_t fixed = 1024 + 8 * (2 * MAX_STAGES + 4) + 16;
-    q.stages = (int)std::min<size_t>(MAX_STAGES, (220 * 1024 - fixed) / stage_bytes);
     q.bias = bias;
     q.relu = relu ? 1 : 0;
     q.out_bf = out_bf;
     q.out_f = out_f;
-    const size_t smem = q.stages * stage_bytes + fixed;
+    q.wres = 0;
+    q.narrow0 = q.narrow1 = 0;
+    q.astage = 0;
+    const bool rows = q.Wb == TM;  // every tile is 128 pixels of one row
+    bool fold = false;
+    size_t smem;
+    if (rows) {
+        const size_t kblk = (size_t)q.N * 128, wbytes = (size_t)9 * q.cpt * kblk;
+        const size_t budget = 220 * 1024 - kFixed;
+        q.narrow0 = DN_C32 && in.c0 <= 32;
+        q.narrow1 = DN_C32 && in.c1 > 0 && in.c1 <= 32;
+        const bool narrow_all = q.narrow0 && (in.c1 == 0 || q.narrow1);
+        // folded tiles: the three horizontal taps in N (3 N <= 256) with resident weights
+        const size_t fstage = 3 * (size_t)(narrow_all ? ROW32_BOX : ROW_BOX);
+        fold = DN_FOLD && q.ntiles == q.mtiles && 3 * q.N <= 256 && wbytes + 2 * fstage <= budget;
+        if (fold) {
+            q.tx = (W + FOLD_OUT - 1) / FOLD_OUT;
+            q.mtiles = q.ntiles = B * q.tx * q.ty;
+            while (q.nhalf < 3 * q.N) q.nhalf *= 2;
+            q.groups = std::min(EPI_GROUPS, 512 / q.nhalf);
+            q.wres = 1;
+            q.astage = (unsigned)fstage;
+            q.stages = (int)std::min<size_t>(MAX_STAGES, (budget - wbytes) / fstage);
+            smem = kFixed + wbytes + q.stages * fstage;
+        } else {
+            q.astage = narrow_all ? HALO32_STAGE : HALO_STAGE;
+            q.wres = q.ntiles == q.mtiles && wbytes + 4 * (size_t)q.astage <= budget;
+            const size_t stage_bytes = q.astage + (q.wres ? 0 : 3 * kblk);
+            const size_t avail = budget - (q.wres ? wbytes : 0);
+            q.stages = (int)std::min<size_t>(MAX_STAGES, avail / stage_bytes);
+            smem = kFixed + (q.wres ? wbytes : 0) + q.stages * stage_bytes;
+        }
+    } else {
+        const size_t stage_bytes = (size_t)TM * 128 + (size_t)q.N * 128;
+        q.stages = (int)std::min<size_t>(MAX_STAGES, (220 * 1024 - kFixed) / stage_bytes);
+        smem = q.stages * stage_bytes + kFixed;
+    }
 
     CUtensorMap tm0, tm1, tmw;
-    int r = map_activations(&tm0, src0, B, H, W, in.c0, q.Wb, q.Hb);
+    const int bw = fold ? TM / EPI_WARPS : rows ? HALO : q.Wb, bh = rows ? 1 : q.Hb;
+    int r = map_activations(&tm0, src0, B, H, W, in.c0, bw, bh, q.narrow0);
     if (r == RT_OK) {
         if (in.c1)
-            r = map_activations(&tm1, in.p1, B, H, W, in.c1, q.Wb, q.Hb);
+            r = map_activations(&tm1, in.p1, B, H, W, in.c1, bw, bh, q.narrow1);
         else
             tm1 = tm0;
     }
@@ -517,13 +1052,20 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
     static int sms = 0;
     if (!configured) {
         RT_CUDA_TRY(cudaFuncSetAttribute(k_conv_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
+        RT_CUDA_TRY(cudaFuncSetAttribute(k_conv_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
+        RT_CUDA_TRY(cudaFuncSetAttribute(k_conv_fold, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
         int dev = 0;
         RT_CUDA_TRY(cudaGetDevice(&dev));
         RT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         configured = true;
     }
     const int grid = std::min(q.ntiles, sms);  // one persistent CTA per SM
-    k_conv_umma<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
+    if (fold)
+        k_conv_fold<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
+    else if (rows)
+        k_conv_rows<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
+    else
+        k_conv_umma<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

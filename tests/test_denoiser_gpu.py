@@ -37,6 +37,11 @@ CONV_CASES = [(16, 0, 0, 32), (32, 0, 0, 32), (32, 0, 0, 48), (48, 0, 0, 48), (4
               (32, 0, 0, 16), (32, 0, 0, 80), (64, 0, 0, 112), (64, 0, 0, 160), (96, 0, 0, 224), (8, 0, 8, 8)]
 
 
+# Image sizes: 22 pixels wide (tiles of 32 x 4 pixels) and 150 wide (row tiles of 128 pixels,
+# the second one partly outside the image).
+SIZES = [(18, 22), (6, 150)]
+
+
 def _case(rng, c0, up0, c1, cout, b=2, h=18, w=22):
     x0 = OD.bf16_round(rng.normal(size=(b, h >> up0, w >> up0, c0)))
     x1 = OD.bf16_round(rng.normal(size=(b, h, w, c1))) if c1 else None
@@ -46,12 +51,13 @@ def _case(rng, c0, up0, c1, cout, b=2, h=18, w=22):
     return x0, x1, x
 
 
+@pytest.mark.parametrize("h,w", SIZES)
 @pytest.mark.parametrize("c0,up0,c1,cout", CONV_CASES)
-def test_conv_forward_matches_oracle(cuda_lib, c0, up0, c1, cout):
+def test_conv_forward_matches_oracle(cuda_lib, c0, up0, c1, cout, h, w):
     from rendu_gb300 import denoiser as D
 
-    rng = np.random.default_rng(c0 * 1000 + cout + up0)
-    x0, x1, x = _case(rng, c0, up0, c1, cout)
+    rng = np.random.default_rng(c0 * 1000 + cout + up0 + w)
+    x0, x1, x = _case(rng, c0, up0, c1, cout, h=h, w=w)
     w = OD.bf16_round(rng.normal(size=(9, c0 + c1, cout)) * 0.1)
     bias = rng.normal(size=cout).astype(np.float32)
     ref = OD.conv3x3(x, w, bias)
@@ -66,12 +72,13 @@ def test_conv_forward_matches_oracle(cuda_lib, c0, up0, c1, cout):
     assert np.all(np.abs(outb - r) <= 2 ** -8 * np.abs(r) + 1e-5 * bound + 1e-7)
 
 
+@pytest.mark.parametrize("h,w", SIZES)
 @pytest.mark.parametrize("c0,up0,c1,cout", CONV_CASES)
-def test_conv_backward_matches_oracle(cuda_lib, c0, up0, c1, cout):
+def test_conv_backward_matches_oracle(cuda_lib, c0, up0, c1, cout, h, w):
     from rendu_gb300 import denoiser as D
 
-    rng = np.random.default_rng(7 + c0 * 1000 + cout + up0)
-    x0, x1, x = _case(rng, c0, up0, c1, cout)
+    rng = np.random.default_rng(7 + c0 * 1000 + cout + up0 + w)
+    x0, x1, x = _case(rng, c0, up0, c1, cout, h=h, w=w)
     wf = (rng.normal(size=(9, c0 + c1, cout)) * 0.1).astype(np.float32)
     gy = OD.bf16_round(rng.normal(size=x.shape[:3] + (cout,)))
     dx, dw = D.conv3x3_backward(_bf16(x0), _f32(wf), _bf16(gy), x1=_bf16(x1) if c1 else None, up0=bool(up0))
