@@ -265,6 +265,40 @@ __global__ void k_pool(const bf16 *__restrict__ x, int B, int H, int W, int C, b
     y[i] = __float2bfloat16_rn(m);
 }
 
+// The same, 8 channels a thread (C a multiple of 8): four 16-byte loads, one 16-byte store.
+// The maximum of BF16 values is exact, so the result equals k_pool's.
+__global__ void k_pool8(const bf16 *__restrict__ x, int B, int H, int W, int C, bf16 *__restrict__ y) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const int h = H / 2, w = W / 2, c8 = C / 8;
+    const size_t n = (size_t)B * h * w * c8;
+    if (i >= n) return;
+    const int c = (int)(i % c8) * 8;
+    size_t r = i / c8;
+    const int xo = (int)(r % w);
+    r /= w;
+    const int yo = (int)(r % h);
+    const int b = (int)(r / h);
+    const bf16 *s = x + (((size_t)b * H + 2 * yo) * W + 2 * xo) * C + c;
+    const size_t row = (size_t)W * C;
+    uint4 v[4] = {*reinterpret_cast<const uint4 *>(s), *reinterpret_cast<const uint4 *>(s + C),
+                  *reinterpret_cast<const uint4 *>(s + row), *reinterpret_cast<const uint4 *>(s + row + C)};
+    uint4 o;
+    unsigned *ov = reinterpret_cast<unsigned *>(&o);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        float2 m = __bfloat1622float2(reinterpret_cast<const __nv_bfloat162 *>(&v[0])[k]);
+#pragma unroll
+        for (int j = 1; j < 4; ++j) {
+            const float2 t = __bfloat1622float2(reinterpret_cast<const __nv_bfloat162 *>(&v[j])[k]);
+            m.x = fmaxf(m.x, t.x);
+            m.y = fmaxf(m.y, t.y);
+        }
+        const __nv_bfloat162 hm = __floats2bfloat162_rn(m.x, m.y);
+        ov[k] = *reinterpret_cast<const unsigned *>(&hm);
+    }
+    *reinterpret_cast<uint4 *>(y + (i / c8) * C + c) = o;
+}
+
 // Pooling gradient: each pooled gradient goes to the first maximal input of its window (row
 // major order), added into gx.
 __global__ void k_pool_back(const bf16 *__restrict__ x, const bf16 *__restrict__ y, const float *__restrict__ gy,
@@ -543,7 +577,10 @@ int colsum(const float *g, long P, int C, float *partial, float *db, cudaStream_
 }
 
 int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st) {
-    k_pool<<<blocks((size_t)B * (H / 2) * (W / 2) * C), 256, 0, st>>>(x, B, H, W, C, y);
+    if (C % 8 == 0)
+        k_pool8<<<blocks((size_t)B * (H / 2) * (W / 2) * (C / 8)), 256, 0, st>>>(x, B, H, W, C, y);
+    else
+        k_pool<<<blocks((size_t)B * (H / 2) * (W / 2) * C), 256, 0, st>>>(x, B, H, W, C, y);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

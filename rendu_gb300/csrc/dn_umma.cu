@@ -814,20 +814,26 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 }
 
-// Nearest 2x upsampling, NHWC: y (B, 2h, 2w, C) from x (B, h, w, C); 8 channels a thread.
+// Nearest 2x upsampling, NHWC: y (B, 2h, 2w, C) from x (B, h, w, C); a thread copies 8
+// channels of one input pixel to its 2 x 2 output pixels.
 __global__ void k_upsample2(const bf16 *__restrict__ x, int B, int h, int w, int C, bf16 *__restrict__ y) {
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     const int c8 = C / 8;
-    const size_t n = (size_t)B * 2 * h * 2 * w * c8;
+    const size_t n = (size_t)B * h * w * c8;
     if (i >= n) return;
     const int c = (int)(i % c8) * 8;
     size_t r = i / c8;
-    const int xx = (int)(r % (2 * w));
-    r /= 2 * w;
-    const int yy = (int)(r % (2 * h));
-    const int b = (int)(r / (2 * h));
-    const uint4 v = *reinterpret_cast<const uint4 *>(x + (((size_t)b * h + yy / 2) * w + xx / 2) * C + c);
-    *reinterpret_cast<uint4 *>(y + (((size_t)b * 2 * h + yy) * 2 * w + xx) * C + c) = v;
+    const int xx = (int)(r % w);
+    r /= w;
+    const int yy = (int)(r % h);
+    const int b = (int)(r / h);
+    const uint4 v = *reinterpret_cast<const uint4 *>(x + (i / c8) * C + c);
+    bf16 *o = y + (((size_t)b * 2 * h + 2 * yy) * 2 * w + 2 * xx) * C + c;
+    const size_t row = (size_t)2 * w * C;
+    *reinterpret_cast<uint4 *>(o) = v;
+    *reinterpret_cast<uint4 *>(o + C) = v;
+    *reinterpret_cast<uint4 *>(o + row) = v;
+    *reinterpret_cast<uint4 *>(o + row + C) = v;
 }
 
 // Forward packing: wpk[co][(tap cpt + j) 64 + cc] = w[tap][ci][co] for the input channel ci
@@ -969,7 +975,7 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
             set_error("an upsampled convolution input needs scratch space");
             return RT_ERR_ARG;
         }
-        const size_t n8 = (size_t)B * H * W * (in.c0 / 8);
+        const size_t n8 = (size_t)B * (H / 2) * (W / 2) * (in.c0 / 8);
         k_upsample2<<<blocks(n8), 256, 0, st>>>(in.p0, B, H / 2, W / 2, in.c0, ups);
         RT_CUDA_TRY(cudaGetLastError());
         src0 = ups;

@@ -37,9 +37,9 @@ CONV_CASES = [(16, 0, 0, 32), (32, 0, 0, 32), (32, 0, 0, 48), (48, 0, 0, 48), (4
               (32, 0, 0, 16), (32, 0, 0, 80), (64, 0, 0, 112), (64, 0, 0, 160), (96, 0, 0, 224), (8, 0, 8, 8)]
 
 
-# Image sizes: 22 pixels wide (tiles of 32 x 4 pixels) and 150 wide (row tiles of 128 pixels,
-# the second one partly outside the image).
-SIZES = [(18, 22), (6, 150)]
+# Image sizes: 22 pixels wide (tiles of 32 x 4 pixels), 150 wide (row tiles, the second one
+# partly outside the image) and 400 wide (row tiles inside the row as well as at its ends).
+SIZES = [(18, 22), (6, 150), (4, 400)]
 
 
 def _case(rng, c0, up0, c1, cout, b=2, h=18, w=22):
