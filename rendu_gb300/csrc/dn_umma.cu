@@ -67,7 +67,7 @@ constexpr int THREADS = 32 * (MMA_WARP + 1);
 // mbarrier slots after the 2 x MAX_STAGES stage barriers
 constexpr int BAR_TFULL = 2 * MAX_STAGES, BAR_TEMPTY = BAR_TFULL + EPI_GROUPS, BAR_TMEM = BAR_TEMPTY + EPI_GROUPS,
               BAR_W = BAR_TMEM + 1, BAR_COUNT = BAR_W + 1;
-constexpr size_t kFixed = 1024 + 8 * BAR_COUNT + 16;  // alignment slack, barriers, TMEM slot
+constexpr size_t kFixed = 1024 + 8 * BAR_COUNT + 16 + 1024;  // alignment slack, barriers, bias (256 floats)
 constexpr unsigned long long kWaitNs = 2000000000ull;
 #ifndef DN_FOLD
 #define DN_FOLD 1
@@ -191,15 +191,20 @@ __device__ __forceinline__ void tmem_ld16(unsigned addr, unsigned (&v)[16]) {
         : "r"(addr));
 }
 
-// 16 output channels [cb, cb + 16) of pixel p: bias, ReLU, BF16 and/or FP32 store (channels
-// past Cout are dropped). Every array index is static, so the values stay in registers.
-__device__ __forceinline__ void store16(const ConvTiles &q, const unsigned (&v)[16], int cb, long p) {
+// 16 output channels [cb, cb + 16) of pixel p: bias (from shared memory when sbias is given:
+// N entries, zero past Cout), ReLU, BF16 and/or FP32 store (channels past Cout are dropped).
+// Every array index is static, so the values stay in registers.
+__device__ __forceinline__ void store16(const ConvTiles &q, const unsigned (&v)[16], int cb, long p,
+                                        const float *sbias = nullptr) {
     const int Cout = q.Cout;
     float f[16];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
         float x_ = __uint_as_float(v[j]);
-        if (q.bias) x_ += __ldg(q.bias + min(cb + j, Cout - 1));
+        if (sbias)
+            x_ += sbias[cb + j];
+        else if (q.bias)
+            x_ += __ldg(q.bias + min(cb + j, Cout - 1));
         if (q.relu) x_ = fmaxf(x_, 0.0f);
         f[j] = x_;
     }
@@ -624,8 +629,8 @@ __device__ __forceinline__ void mma_rows3(unsigned d, unsigned long long ad, uns
 // Epilogue of the folded tiles: group g reads accumulator g, 16 output channels at a time
 // (columns c0, N + c0, 2N + c0), adds each row's neighbours' columns and stores lanes 1..30.
 template <class Origin>
-__device__ __forceinline__ bool epilogue_fold(const ConvTiles &q, unsigned tmem, unsigned bar0, int my_tiles,
-                                              const Origin &tile_origin) {
+__device__ __forceinline__ bool epilogue_fold(const ConvTiles &q, unsigned tmem, unsigned bar0, const float *sbias,
+                                              int my_tiles, const Origin &tile_origin) {
     const int warp = threadIdx.x >> 5, g = warp / EPI_WARPS, quarter = warp % EPI_WARPS;
     const int lane = threadIdx.x & 31;
     if (g >= q.groups) return true;
@@ -658,7 +663,7 @@ __device__ __forceinline__ bool epilogue_fold(const ConvTiles &q, unsigned tmem,
                 v[j] = __float_as_uint(up + __uint_as_float(b1[j]) + dn);
             }
             const int cb = n0 + c0;
-            if (store && cb < q.Cout) store16(q, v, cb, p);
+            if (store && cb < q.Cout) store16(q, v, cb, p, sbias);
         }
     }
     return true;
@@ -684,6 +689,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     const unsigned tmem_slot = bar0 + 8u * BAR_TMEM;
     const unsigned wfull = bar0 + 8u * BAR_W;
     const unsigned *tmem_slot_ptr = reinterpret_cast<const unsigned *>(smem_raw + (tmem_slot - raw));
+    float *sbias = reinterpret_cast<float *>(smem_raw + (bar0 + 8u * BAR_COUNT - raw));  // N floats
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int my_tiles = q.ntiles > (int)blockIdx.x ? (q.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
@@ -713,6 +719,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         mbar_init(wfull, 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
     }
+    for (int c = tid; c < q.N; c += THREADS) sbias[c] = (q.bias && c < q.Cout) ? q.bias[c] : 0.0f;
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
@@ -803,7 +810,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         __syncwarp();
     } else {
-        ok = epilogue_fold(q, tmem, bar0, my_tiles, tile_origin);
+        ok = epilogue_fold(q, tmem, bar0, sbias, my_tiles, tile_origin);
     }
     if (!ok) atomicOr(&g_umma_status, 1u);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
