@@ -399,6 +399,17 @@ __global__ void __launch_bounds__(128, 8) k_shadow(PtWave w, int queue) {
 
 // Closest hit of ray queue `cur` with the persistent per-lane refill of rt_trace.cu; each
 // lane traverses the hierarchy of its ray's job.
+// Idle lanes of a warp take new rays only once at least PT_REFILL_MIN of them are idle (a warp
+// with no active lane always refills): a refill round (queue atomic, ray load, job lookup)
+// stalls the warp's active lanes, so it pays to amortise it. Measured on the 2M-triangle
+// instanced 1080p render: threshold 1 -> 64.7 ms, 8 -> 55.6, 16 -> 54.1, 20 -> 53.9,
+// 24 -> 54.1 ms per 16 spp; back-to-back rounds gained nothing.
+#ifndef PT_REFILL_MIN
+#define PT_REFILL_MIN 16
+#endif
+#ifndef PT_REFILL_ROUNDS
+#define PT_REFILL_ROUNDS 1
+#endif
 template <int STACK>
 __global__ void __launch_bounds__(128) k_trace_batch(PtWave w, int cur) {
     const size_t n = min(w.counters[cur], w.cap);
@@ -414,8 +425,9 @@ __global__ void __launch_bounds__(128) k_trace_batch(PtWave w, int cur) {
     bool active = false, exhausted = false;
     uint32_t nv_ = 0, nt_ = 0;
     while (true) {
-        const unsigned need = __ballot_sync(0xffffffffu, !active);
-        if (need && !exhausted) {
+        for (int round = 0; round < PT_REFILL_ROUNDS && !exhausted; ++round) {
+            const unsigned need = __ballot_sync(0xffffffffu, !active);
+            if (!need || (__popc(need) < PT_REFILL_MIN && need != 0xffffffffu)) break;
             const int leader = __ffs(need) - 1;
             unsigned long long base = 0;
             if ((int)lane == leader) base = atomicAdd(w.fetch, (unsigned long long)__popc(need));
