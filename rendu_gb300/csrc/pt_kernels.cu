@@ -137,199 +137,200 @@ template <bool EXT>
 // and the occupancy gained outweighs the few spilled registers (the 1080p extended render
 // measured 3.4 % faster than at 108 registers).
 __global__ void __launch_bounds__(128, 6) k_shade(PtWave w, int cur, uint32_t did) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = min(w.counters[cur], w.cap);
-    if (i == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicAdd(&w.stats[did == 0 ? 0 : 1], (unsigned long long)n);  // rays traced this bounce
         *w.fetch = 0ull;  // ray-fetch counter of the next bounce's traversal
     }
-    if (i >= n) return;
-    constexpr bool ext = EXT;
-    const int nxt = cur ^ 1;
-    const uint32_t path = w.qpath[cur][i];
-    const PtJob &J = w.jobs[w.pjob[path]];
-    const PtScene &s = J.scene;
-    const rt_ray ray = w.qray[cur][i];
-    const rt_hit hit = w.hits[i];
-    const f3 pos = mk(ray.ox, ray.oy, ray.oz);
-    const f3 dir = mk(ray.dx, ray.dy, ray.dz);
-    float4 c4 = w.color[path], a4 = w.atten[path];
-    f3 color = mk(c4.x, c4.y, c4.z), atten = mk(a4.x, a4.y, a4.z);
-    float prev_pdf = a4.w;  // solid-angle pdf of the BSDF sample that produced this ray (0: none)
-    bool cont = false;
-    bool sh_a = false, sh_b = false;  // analytic-light and emitter/environment shadow rays
-    f3 next_o = pos, next_d = dir;
-    f3 sa_o = pos, sa_d = dir, sa_c = mk(0, 0, 0), sb_o = pos, sb_d = dir, sb_c = mk(0, 0, 0);
-    float sa_max = 0.0f, sb_max = 0.0f;
+    // grid-stride over the queue, whose length is known only on the device
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        constexpr bool ext = EXT;
+        const int nxt = cur ^ 1;
+        const uint32_t path = w.qpath[cur][i];
+        const PtJob &J = w.jobs[w.pjob[path]];
+        const PtScene &s = J.scene;
+        const rt_ray ray = w.qray[cur][i];
+        const rt_hit hit = w.hits[i];
+        const f3 pos = mk(ray.ox, ray.oy, ray.oz);
+        const f3 dir = mk(ray.dx, ray.dy, ray.dz);
+        float4 c4 = w.color[path], a4 = w.atten[path];
+        f3 color = mk(c4.x, c4.y, c4.z), atten = mk(a4.x, a4.y, a4.z);
+        float prev_pdf = a4.w;  // solid-angle pdf of the BSDF sample that produced this ray (0: none)
+        bool cont = false;
+        bool sh_a = false, sh_b = false;  // analytic-light and emitter/environment shadow rays
+        f3 next_o = pos, next_d = dir;
+        f3 sa_o = pos, sa_d = dir, sa_c = mk(0, 0, 0), sb_o = pos, sb_d = dir, sb_c = mk(0, 0, 0);
+        float sa_max = 0.0f, sb_max = 0.0f;
 
-    if (hit.prim == RT_NO_HIT) {
-        if (ext && s.env_tex >= 0) {
-            const f3 le = env_radiance(s, dir);
-            float wgt = 1.0f;
-            if (did > 0 && prev_pdf > 0.0f) wgt = mis_power(prev_pdf, s.p_env * env_pdf(s, dir));
-            color += atten * (le * wgt);
+        if (hit.prim == RT_NO_HIT) {
+            if (ext && s.env_tex >= 0) {
+                const f3 le = env_radiance(s, dir);
+                float wgt = 1.0f;
+                if (did > 0 && prev_pdf > 0.0f) wgt = mis_power(prev_pdf, s.p_env * env_pdf(s, dir));
+                color += atten * (le * wgt);
+            } else {
+                // PathTracer.cpp:206-209.
+                const float2 ndc = w.ndc[path];
+                color += atten * eval_background(s, pos, dir, ndc.x, ndc.y, did == 0);
+            }
         } else {
-            // PathTracer.cpp:206-209.
-            const float2 ndc = w.ndc[path];
-            color += atten * eval_background(s, pos, dir, ndc.x, ndc.y, did == 0);
-        }
-    } else {
-        const SurfaceHit sh = surface(s, hit.prim, hit.u, hit.v);
-        const PtObject &obj = s.objects[sh.obj];
-        const PtMaterial mat = s.materials[obj.material];
-        const f3 p = mk(pos.x + hit.t * dir.x, pos.y + hit.t * dir.y, pos.z + hit.t * dir.z);
-        const float2 uv = obj.use_uv ? interp_uv(s.uvs, sh) : make_float2(0.5f, 0.5f);
-        const float4 bcol = tex_rgbal(s, mat.tex[0], uv.x, uv.y);
-        if (mat.masked && bcol.w < 0.01f) {
-            // Alpha cut-out: same direction from the hit point, one bounce consumed (:223-226).
-            cont = did + 1 < J.depth;
-            next_o = p;
-        } else if (mat.type == PT_MAT_EMISSIVE) {
-            f3 le = mk(bcol.x, bcol.y, bcol.z);  // :228-234
-            if (did == 0 && J.aov) {  // feature buffer: emitted colour scaled into [0, 1]
-                const float m = fmaxf(fmaxf(fmaxf(le.x, le.y), le.z), 1.0f);
-                w.aov0[path] = make_float4(le.x / m, le.y / m, le.z / m, hit.t);
-            }
-            if (ext && did > 0 && prev_pdf > 0.0f && s.nemitters > 0) {
-                // Solid-angle pdf with which emitter sampling would have produced this point:
-                // (area * lum / power) * (1 / area) * t^2 / |cos| = lum * t^2 / (power * |cos|).
-                const f3 p0 = ld3(s.positions, sh.i0), p1 = ld3(s.positions, sh.i1), p2 = ld3(s.positions, sh.i2);
-                const f3 ng = normalize(mat3_mul(obj.invtp, cross(p1 - p0, p2 - p0)));
-                const float cosl = fabsf(dot(ng, dir));
-                const float pl = cosl > 0.0f ? (1.0f - s.p_env) * luminance(le) * hit.t * hit.t / (s.emit_power * cosl)
-                                             : 0.0f;
-                le = le * mis_power(prev_pdf, pl);
-            }
-            color += atten * le;
-        } else {
-            // PathTracer::buildLocalFrame (:86-122).
-            const f3 nn = normalize(interp3(s.normals, sh));
-            const f3 tt = normalize(interp3(s.tangents, sh));
-            const f3 bb = normalize(interp3(s.bitangents, sh));
-            f3 t0 = mat3_mul(obj.invtp, tt), t1 = mat3_mul(obj.invtp, bb), t2 = mat3_mul(obj.invtp, nn);
-            if (!(dot(t2, dir) < 0.0f)) t2 = -t2;
-            if (obj.use_uv) {
-                const float4 img = tex_rgbal(s, mat.tex[1], uv.x, uv.y);
-                const f3 ln = normalize(mk(2.0f * img.x - 1.0f, 2.0f * img.y - 1.0f, 2.0f * img.z - 1.0f));
-                t2 = mk(t0.x * ln.x + t1.x * ln.y + t2.x * ln.z, t0.y * ln.x + t1.y * ln.y + t2.y * ln.z,
-                        t0.z * ln.x + t1.z * ln.y + t2.z * ln.z);
-            }
-            t2 = normalize(t2);
-            t1 = normalize(cross(t2, normalize(t0)));
-            t0 = normalize(cross(t1, t2));
-            // World -> local is the transpose of the frame.
-            const f3 mdir = -dir;
-            const f3 wo = normalize(mk(dot(t0, mdir), dot(t1, mdir), dot(t2, mdir)));
-            const f3 base = mk(powf(bcol.x, 2.2f), powf(bcol.y, 2.2f), powf(bcol.z, 2.2f));
-            const float4 rmao = tex_rgbal(s, mat.tex[2], uv.x, uv.y);
-            if (did == 0 && J.aov) {  // feature buffers: linear base colour, shading normal, distance
-                w.aov0[path] = make_float4(base.x, base.y, base.z, hit.t);
-                w.aov1[path] = make_float4(t2.x, t2.y, t2.z, 0.0f);
-            }
-            const uint32_t pix = w.ppix[path], sid = w.psamp[path];
-            const U4 rnd = philox(U4{pix, sid, did + 1u, 0u}, J.seed_lo, J.seed_hi);
-            const f3 ps = mk(p.x + 0.001f * t2.x, p.y + 0.001f * t2.y, p.z + 0.001f * t2.z);
-            if (s.nlights > 0) {
-                // Next-event estimation on one uniformly picked analytic light (:248-272).
-                const PtLight &L = s.lights[uint_below(rnd.x, (uint32_t)s.nlights)];
-                float maxd, fall;
-                const f3 ld = light_sample(L, ps, maxd, fall);
-                if (fall > 0.0f) {
-                    const f3 lwi = normalize(mk(dot(t0, ld), dot(t1, ld), dot(t2, ld)));
-                    const f3 ev = ggx_eval(wo, base, rmao.x, rmao.y, lwi);
-                    const float inv_pdf = (float)s.nlights;  // 1 / (1 / lights)
-                    const f3 ill = mk(fall * ev.x * L.color[0] * inv_pdf, fall * ev.y * L.color[1] * inv_pdf,
-                                      fall * ev.z * L.color[2] * inv_pdf);
-                    const f3 contrib = atten * ill;
-                    if (L.shadows) {
-                        sh_a = true;
-                        sa_o = ps;
-                        sa_d = ld;
-                        sa_max = maxd;
-                        sa_c = contrib;
-                    } else {
-                        color += contrib;
-                    }
-                }
-            }
-            if (ext && (s.nemitters > 0 || s.env_tex >= 0)) {
-                // Extended: one emitter-or-environment sample, MIS against BSDF sampling.
-                const U4 r2 = philox(U4{pix, sid, did + 1u, 1u}, J.seed_lo, J.seed_hi);
-                const float usel = u01(r2.x);
-                f3 ld, le;
-                float pl = 0.0f, dist = 1e8f;
-                bool ok = false;
-                if (s.env_tex >= 0 && (s.nemitters == 0 || usel < s.p_env)) {
-                    ld = env_sample(s, u01(r2.y), u01(r2.z), pl);
-                    pl *= s.p_env;
-                    le = env_radiance(s, ld);
-                    ok = pl > 0.0f;
-                } else if (s.nemitters > 0) {
-                    const float ue = s.env_tex >= 0 ? (usel - s.p_env) / (1.0f - s.p_env) : usel;
-                    const PtEmitter em = s.emitters[emitter_pick(s, fminf(fmaxf(ue, 0.0f), 0.99999994f))];
-                    const float su = sqrtf(u01(r2.y)), b1 = 1.0f - su, b2 = u01(r2.z) * su;
-                    const f3 e1 = mk(em.e1[0], em.e1[1], em.e1[2]), e2 = mk(em.e2[0], em.e2[1], em.e2[2]);
-                    const f3 q = mk(em.v0[0] + b1 * e1.x + b2 * e2.x, em.v0[1] + b1 * e1.y + b2 * e2.y,
-                                    em.v0[2] + b1 * e1.z + b2 * e2.z);
-                    const f3 dq = q - ps;
-                    const float d2 = dot(dq, dq);
-                    dist = sqrtf(d2);
-                    ld = dq / dist;
-                    const f3 ng = normalize(cross(e1, e2));
-                    const float cosl = fabsf(dot(ng, ld));
-                    le = mk(em.emission[0], em.emission[1], em.emission[2]);
-                    pl = cosl > 0.0f ? (1.0f - s.p_env) * em.lum * d2 / (s.emit_power * cosl) : 0.0f;
-                    ok = pl > 0.0f && dist > 0.0f;
-                }
-                if (ok) {
-                    const f3 lwi = normalize(mk(dot(t0, ld), dot(t1, ld), dot(t2, ld)));
-                    const f3 ev = ggx_eval(wo, base, rmao.x, rmao.y, lwi);
-                    const float pb = ggx_pdf(wo, base, rmao.x, rmao.y, lwi);
-                    const float wgt = mis_power(pl, pb) / pl;
-                    const f3 contrib = atten * (ev * le) * wgt;
-                    if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
-                        sh_b = true;
-                        sb_o = ps;
-                        sb_d = ld;
-                        sb_max = dist < 1e8f ? dist * (1.0f - 1e-3f) : 1e8f;
-                        sb_c = contrib;
-                    }
-                }
-            }
-            f3 wi;
-            const f3 weight = ggx_sample_eval(wo, base, rmao.x, rmao.y, u01(rnd.y), u01(rnd.z), u01(rnd.w), wi);
-            const f3 nd = normalize(mk(t0.x * wi.x + t1.x * wi.y + t2.x * wi.z, t0.y * wi.x + t1.y * wi.y + t2.y * wi.z,
-                                       t0.z * wi.x + t1.z * wi.y + t2.z * wi.z));
-            atten *= weight;
-            if (ext) prev_pdf = (weight.x > 0.0f || weight.y > 0.0f || weight.z > 0.0f)
-                                    ? ggx_pdf(wo, base, rmao.x, rmao.y, wi) : 0.0f;
-            if (did + 1 < J.depth) {
-                cont = true;
+            const SurfaceHit sh = surface(s, hit.prim, hit.u, hit.v);
+            const PtObject &obj = s.objects[sh.obj];
+            const PtMaterial mat = s.materials[obj.material];
+            const f3 p = mk(pos.x + hit.t * dir.x, pos.y + hit.t * dir.y, pos.z + hit.t * dir.z);
+            const float2 uv = obj.use_uv ? interp_uv(s.uvs, sh) : make_float2(0.5f, 0.5f);
+            const float4 bcol = tex_rgbal(s, mat.tex[0], uv.x, uv.y);
+            if (mat.masked && bcol.w < 0.01f) {
+                // Alpha cut-out: same direction from the hit point, one bounce consumed (:223-226).
+                cont = did + 1 < J.depth;
                 next_o = p;
-                next_d = normalize(nd);
+            } else if (mat.type == PT_MAT_EMISSIVE) {
+                f3 le = mk(bcol.x, bcol.y, bcol.z);  // :228-234
+                if (did == 0 && J.aov) {  // feature buffer: emitted colour scaled into [0, 1]
+                    const float m = fmaxf(fmaxf(fmaxf(le.x, le.y), le.z), 1.0f);
+                    w.aov0[path] = make_float4(le.x / m, le.y / m, le.z / m, hit.t);
+                }
+                if (ext && did > 0 && prev_pdf > 0.0f && s.nemitters > 0) {
+                    // Solid-angle pdf with which emitter sampling would have produced this point:
+                    // (area * lum / power) * (1 / area) * t^2 / |cos| = lum * t^2 / (power * |cos|).
+                    const f3 p0 = ld3(s.positions, sh.i0), p1 = ld3(s.positions, sh.i1), p2 = ld3(s.positions, sh.i2);
+                    const f3 ng = normalize(mat3_mul(obj.invtp, cross(p1 - p0, p2 - p0)));
+                    const float cosl = fabsf(dot(ng, dir));
+                    const float pl = cosl > 0.0f ? (1.0f - s.p_env) * luminance(le) * hit.t * hit.t / (s.emit_power * cosl)
+                                                 : 0.0f;
+                    le = le * mis_power(prev_pdf, pl);
+                }
+                color += atten * le;
+            } else {
+                // PathTracer::buildLocalFrame (:86-122).
+                const f3 nn = normalize(interp3(s.normals, sh));
+                const f3 tt = normalize(interp3(s.tangents, sh));
+                const f3 bb = normalize(interp3(s.bitangents, sh));
+                f3 t0 = mat3_mul(obj.invtp, tt), t1 = mat3_mul(obj.invtp, bb), t2 = mat3_mul(obj.invtp, nn);
+                if (!(dot(t2, dir) < 0.0f)) t2 = -t2;
+                if (obj.use_uv) {
+                    const float4 img = tex_rgbal(s, mat.tex[1], uv.x, uv.y);
+                    const f3 ln = normalize(mk(2.0f * img.x - 1.0f, 2.0f * img.y - 1.0f, 2.0f * img.z - 1.0f));
+                    t2 = mk(t0.x * ln.x + t1.x * ln.y + t2.x * ln.z, t0.y * ln.x + t1.y * ln.y + t2.y * ln.z,
+                            t0.z * ln.x + t1.z * ln.y + t2.z * ln.z);
+                }
+                t2 = normalize(t2);
+                t1 = normalize(cross(t2, normalize(t0)));
+                t0 = normalize(cross(t1, t2));
+                // World -> local is the transpose of the frame.
+                const f3 mdir = -dir;
+                const f3 wo = normalize(mk(dot(t0, mdir), dot(t1, mdir), dot(t2, mdir)));
+                const f3 base = mk(powf(bcol.x, 2.2f), powf(bcol.y, 2.2f), powf(bcol.z, 2.2f));
+                const float4 rmao = tex_rgbal(s, mat.tex[2], uv.x, uv.y);
+                if (did == 0 && J.aov) {  // feature buffers: linear base colour, shading normal, distance
+                    w.aov0[path] = make_float4(base.x, base.y, base.z, hit.t);
+                    w.aov1[path] = make_float4(t2.x, t2.y, t2.z, 0.0f);
+                }
+                const uint32_t pix = w.ppix[path], sid = w.psamp[path];
+                const U4 rnd = philox(U4{pix, sid, did + 1u, 0u}, J.seed_lo, J.seed_hi);
+                const f3 ps = mk(p.x + 0.001f * t2.x, p.y + 0.001f * t2.y, p.z + 0.001f * t2.z);
+                if (s.nlights > 0) {
+                    // Next-event estimation on one uniformly picked analytic light (:248-272).
+                    const PtLight &L = s.lights[uint_below(rnd.x, (uint32_t)s.nlights)];
+                    float maxd, fall;
+                    const f3 ld = light_sample(L, ps, maxd, fall);
+                    if (fall > 0.0f) {
+                        const f3 lwi = normalize(mk(dot(t0, ld), dot(t1, ld), dot(t2, ld)));
+                        const f3 ev = ggx_eval(wo, base, rmao.x, rmao.y, lwi);
+                        const float inv_pdf = (float)s.nlights;  // 1 / (1 / lights)
+                        const f3 ill = mk(fall * ev.x * L.color[0] * inv_pdf, fall * ev.y * L.color[1] * inv_pdf,
+                                          fall * ev.z * L.color[2] * inv_pdf);
+                        const f3 contrib = atten * ill;
+                        if (L.shadows) {
+                            sh_a = true;
+                            sa_o = ps;
+                            sa_d = ld;
+                            sa_max = maxd;
+                            sa_c = contrib;
+                        } else {
+                            color += contrib;
+                        }
+                    }
+                }
+                if (ext && (s.nemitters > 0 || s.env_tex >= 0)) {
+                    // Extended: one emitter-or-environment sample, MIS against BSDF sampling.
+                    const U4 r2 = philox(U4{pix, sid, did + 1u, 1u}, J.seed_lo, J.seed_hi);
+                    const float usel = u01(r2.x);
+                    f3 ld, le;
+                    float pl = 0.0f, dist = 1e8f;
+                    bool ok = false;
+                    if (s.env_tex >= 0 && (s.nemitters == 0 || usel < s.p_env)) {
+                        ld = env_sample(s, u01(r2.y), u01(r2.z), pl);
+                        pl *= s.p_env;
+                        le = env_radiance(s, ld);
+                        ok = pl > 0.0f;
+                    } else if (s.nemitters > 0) {
+                        const float ue = s.env_tex >= 0 ? (usel - s.p_env) / (1.0f - s.p_env) : usel;
+                        const PtEmitter em = s.emitters[emitter_pick(s, fminf(fmaxf(ue, 0.0f), 0.99999994f))];
+                        const float su = sqrtf(u01(r2.y)), b1 = 1.0f - su, b2 = u01(r2.z) * su;
+                        const f3 e1 = mk(em.e1[0], em.e1[1], em.e1[2]), e2 = mk(em.e2[0], em.e2[1], em.e2[2]);
+                        const f3 q = mk(em.v0[0] + b1 * e1.x + b2 * e2.x, em.v0[1] + b1 * e1.y + b2 * e2.y,
+                                        em.v0[2] + b1 * e1.z + b2 * e2.z);
+                        const f3 dq = q - ps;
+                        const float d2 = dot(dq, dq);
+                        dist = sqrtf(d2);
+                        ld = dq / dist;
+                        const f3 ng = normalize(cross(e1, e2));
+                        const float cosl = fabsf(dot(ng, ld));
+                        le = mk(em.emission[0], em.emission[1], em.emission[2]);
+                        pl = cosl > 0.0f ? (1.0f - s.p_env) * em.lum * d2 / (s.emit_power * cosl) : 0.0f;
+                        ok = pl > 0.0f && dist > 0.0f;
+                    }
+                    if (ok) {
+                        const f3 lwi = normalize(mk(dot(t0, ld), dot(t1, ld), dot(t2, ld)));
+                        const f3 ev = ggx_eval(wo, base, rmao.x, rmao.y, lwi);
+                        const float pb = ggx_pdf(wo, base, rmao.x, rmao.y, lwi);
+                        const float wgt = mis_power(pl, pb) / pl;
+                        const f3 contrib = atten * (ev * le) * wgt;
+                        if (contrib.x > 0.0f || contrib.y > 0.0f || contrib.z > 0.0f) {
+                            sh_b = true;
+                            sb_o = ps;
+                            sb_d = ld;
+                            sb_max = dist < 1e8f ? dist * (1.0f - 1e-3f) : 1e8f;
+                            sb_c = contrib;
+                        }
+                    }
+                }
+                f3 wi;
+                const f3 weight = ggx_sample_eval(wo, base, rmao.x, rmao.y, u01(rnd.y), u01(rnd.z), u01(rnd.w), wi);
+                const f3 nd = normalize(mk(t0.x * wi.x + t1.x * wi.y + t2.x * wi.z, t0.y * wi.x + t1.y * wi.y + t2.y * wi.z,
+                                           t0.z * wi.x + t1.z * wi.y + t2.z * wi.z));
+                atten *= weight;
+                if (ext) prev_pdf = (weight.x > 0.0f || weight.y > 0.0f || weight.z > 0.0f)
+                                        ? ggx_pdf(wo, base, rmao.x, rmao.y, wi) : 0.0f;
+                if (did + 1 < J.depth) {
+                    cont = true;
+                    next_o = p;
+                    next_d = normalize(nd);
+                }
             }
         }
+        w.color[path] = make_float4(color.x, color.y, color.z, 0.0f);
+        w.atten[path] = make_float4(atten.x, atten.y, atten.z, prev_pdf);
+        uint32_t slot = warp_append(&w.counters[nxt], cont);
+        if (cont && slot >= w.cap) {  // cannot happen (one append per path); never write past the queue
+            atomicOr(w.status, RT_DEV_QUEUE_OVERFLOW);
+            cont = false;
+        }
+        if (cont) {
+            w.qray[nxt][slot] = rt_ray{next_o.x, next_o.y, next_o.z, 1e-4f, next_d.x, next_d.y, next_d.z, 1e8f};
+            w.qpath[nxt][slot] = path;
+        }
+        // Two shadow queues (analytic lights; emitters/environment), resolved by two launches
+        // in that order: a path never has two shadow rays in one queue, so the radiance update
+        // in k_shadow is race-free and the summation order is fixed.
+        const uint32_t sa = warp_append(&w.counters[2], sh_a);
+        if (sh_a && sa < w.shadow_cap) push_shadow(w, sa, sa_o, sa_d, sa_max, sa_c, path);
+        else if (sh_a) atomicOr(w.status, RT_DEV_QUEUE_OVERFLOW);
+        const uint32_t sb = warp_append(&w.counters[3], sh_b);
+        if (sh_b && sb < w.shadow_cap) push_shadow(w, w.shadow_cap + sb, sb_o, sb_d, sb_max, sb_c, path);
+        else if (sh_b) atomicOr(w.status, RT_DEV_QUEUE_OVERFLOW);
     }
-    w.color[path] = make_float4(color.x, color.y, color.z, 0.0f);
-    w.atten[path] = make_float4(atten.x, atten.y, atten.z, prev_pdf);
-    uint32_t slot = warp_append(&w.counters[nxt], cont);
-    if (cont && slot >= w.cap) {  // cannot happen (one append per path); never write past the queue
-        atomicOr(w.status, RT_DEV_QUEUE_OVERFLOW);
-        cont = false;
-    }
-    if (cont) {
-        w.qray[nxt][slot] = rt_ray{next_o.x, next_o.y, next_o.z, 1e-4f, next_d.x, next_d.y, next_d.z, 1e8f};
-        w.qpath[nxt][slot] = path;
-    }
-    // Two shadow queues (analytic lights; emitters/environment), resolved by two launches
-    // in that order: a path never has two shadow rays in one queue, so the radiance update
-    // in k_shadow is race-free and the summation order is fixed.
-    const uint32_t sa = warp_append(&w.counters[2], sh_a);
-    if (sh_a && sa < w.shadow_cap) push_shadow(w, sa, sa_o, sa_d, sa_max, sa_c, path);
-    else if (sh_a) atomicOr(w.status, RT_DEV_QUEUE_OVERFLOW);
-    const uint32_t sb = warp_append(&w.counters[3], sh_b);
-    if (sh_b && sb < w.shadow_cap) push_shadow(w, w.shadow_cap + sb, sb_o, sb_d, sb_max, sb_c, path);
-    else if (sh_b) atomicOr(w.status, RT_DEV_QUEUE_OVERFLOW);
 }
 
 // Shadow ray through alpha-masked surfaces: closest-hit walks from surface to surface, passing
@@ -644,9 +645,23 @@ int pt_launch_raygen(const PtWave &w, cudaStream_t st) {
     return RT_OK;
 }
 
+// Shading launches: SHADE_WAVES full residencies of the GPU, grid-stride over the ray queue
+// (its length is known only on the device). Against one block per 128 slots of capacity:
+// Cornell 256^2 0.63 -> 0.51 ms (its later bounces hold few paths), the large 1080p render
+// within 1 % (4 residencies: 2.5 % slower there; 64: no gain on Cornell).
+#ifndef SHADE_WAVES
+#define SHADE_WAVES 16
+#endif
+static int g_shade_grid[2] = {0, 0};
+
 int pt_launch_shade(const PtWave &w, int cur, uint32_t did, bool ext, cudaStream_t st) {
-    if (ext) k_shade<true><<<(w.cap + 127) / 128, 128, 0, st>>>(w, cur, did);
-    else k_shade<false><<<(w.cap + 127) / 128, 128, 0, st>>>(w, cur, did);
+    const int g = g_shade_grid[ext ? 1 : 0];
+    if (g == 0) {
+        set_error("shading grid not prepared");
+        return RT_ERR_STATE;
+    }
+    if (ext) k_shade<true><<<g, 128, 0, st>>>(w, cur, did);
+    else k_shade<false><<<g, 128, 0, st>>>(w, cur, did);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
@@ -687,6 +702,12 @@ int trace_closest_batch_prepare(bool big_stack) {
         if (big_stack) RT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shadow<256>, 128, 0));
         else RT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shadow<64>, 128, 0));
         gs = sms * (per_sm > 0 ? per_sm : 1) * 4;
+        for (int e = 0; e < 2; ++e) {
+            per_sm = 0;
+            if (e) RT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<true>, 128, 0));
+            else RT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<false>, 128, 0));
+            g_shade_grid[e] = sms * (per_sm > 0 ? per_sm : 1) * SHADE_WAVES;
+        }
     }
     return RT_OK;
 }
