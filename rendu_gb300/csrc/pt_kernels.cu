@@ -646,16 +646,16 @@ int pt_launch_raygen(const PtWave &w, cudaStream_t st) {
 }
 
 // Shading launches: SHADE_WAVES full residencies of the GPU, grid-stride over the ray queue
-// (its length is known only on the device). Against one block per 128 slots of capacity:
-// Cornell 256^2 0.63 -> 0.51 ms (its later bounces hold few paths), the large 1080p render
-// within 1 % (4 residencies: 2.5 % slower there; 64: no gain on Cornell).
+// (its length is known only on the device); 0 = one block per 128 slots of capacity.
+// Against 0: Cornell 256^2 0.63 -> 0.51 ms (its later bounces hold few paths), the large
+// 1080p render within 1 % (4 residencies: 2.5 % slower there; 64: no gain on Cornell).
 #ifndef SHADE_WAVES
 #define SHADE_WAVES 16
 #endif
 static int g_shade_grid[2] = {0, 0};
 
 int pt_launch_shade(const PtWave &w, int cur, uint32_t did, bool ext, cudaStream_t st) {
-    const int g = g_shade_grid[ext ? 1 : 0];
+    const int g = SHADE_WAVES ? g_shade_grid[ext ? 1 : 0] : (int)((w.cap + 127) / 128);
     if (g == 0) {
         set_error("shading grid not prepared");
         return RT_ERR_STATE;
@@ -666,14 +666,17 @@ int pt_launch_shade(const PtWave &w, int cur, uint32_t did, bool ext, cudaStream
     return RT_OK;
 }
 
-// Shadow launches: four full residencies of the GPU, grid-stride over the queue (its length
-// is known only on the device). Against one block per 128 slots of queue capacity: equal on
-// the large 1080p render, 0.74 -> 0.63 ms on the 256^2 Cornell render whose queues are far
-// below capacity.
+// Shadow launches: SHADOW_WAVES full residencies of the GPU, grid-stride over the queue (its
+// length is known only on the device); 0 = one block per 128 slots of capacity. Measured
+// with shading at 16: Cornell 256^2 0.62 ms at 0, 0.51 ms at 16; the large 1080p render
+// 224.8-226.5 ms for 0, 4, 16 and 64 alike.
+#ifndef SHADOW_WAVES
+#define SHADOW_WAVES 16
+#endif
 static int g_shadow_grid[2] = {0, 0};
 
 int pt_launch_shadow(const PtWave &w, int queue, bool big_stack, cudaStream_t st) {
-    const int g = g_shadow_grid[big_stack ? 1 : 0];
+    const int g = SHADOW_WAVES ? g_shadow_grid[big_stack ? 1 : 0] : (int)((w.cap + 127) / 128);
     if (g == 0) {
         set_error("shadow traversal grid not prepared");
         return RT_ERR_STATE;
@@ -701,7 +704,7 @@ int trace_closest_batch_prepare(bool big_stack) {
         per_sm = 0;
         if (big_stack) RT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shadow<256>, 128, 0));
         else RT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shadow<64>, 128, 0));
-        gs = sms * (per_sm > 0 ? per_sm : 1) * 4;
+        gs = sms * (per_sm > 0 ? per_sm : 1) * SHADOW_WAVES;
         for (int e = 0; e < 2; ++e) {
             per_sm = 0;
             if (e) RT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_shade<true>, 128, 0));
