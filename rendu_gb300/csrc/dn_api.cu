@@ -290,7 +290,10 @@ int backward(dn_net *n, const float *target, cudaStream_t st) {
         const int H = n->Hp >> o.level, W = n->Wp >> o.level;
         const long P = n->pixels(o.level);
         bf16 *gb = n->gbf.as<bf16>();
-        r = relu_grad(n->g(c.out), c.relu ? n->bf(c.out) : nullptr, (size_t)P * c.cout, c.relu != 0, gb, st);
+        // ReLU gradient and bias gradient in one pass (its partials are reduced before the
+        // weight gradient reuses the scratch)
+        r = relu_grad_bias(n->g(c.out), c.relu ? n->bf(c.out) : nullptr, P, c.cout, c.relu != 0, gb,
+                           n->partial.as<float>(), grads + c.boff, st);
         if (r != RT_OK) break;
         ConvIn in;
         in.p0 = n->bf(c.src0);
@@ -299,7 +302,6 @@ int backward(dn_net *n, const float *target, cudaStream_t st) {
         in.p1 = c.src1 >= 0 ? n->bf(c.src1) : nullptr;
         in.c1 = c.cin1;
         r = conv_wgrad(in, n->B, H, W, gb, c.cout, n->partial.as<float>(), grads + c.woff, st);
-        if (r == RT_OK) r = colsum(n->g(c.out), P, c.cout, n->partial.as<float>(), grads + c.boff, st);
         if (r != RT_OK || c.src0 == 0) continue;  // no gradient for the network input
         ConvIn gi;
         gi.p0 = gb;

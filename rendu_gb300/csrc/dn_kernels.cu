@@ -246,6 +246,98 @@ __global__ void k_colsum(const float *__restrict__ g, long P, int C, long chunk,
     }
 }
 
+// ReLU gradient and bias-gradient partials in one pass over a (P x C) FP32 gradient: rows
+// [chunk b, chunk (b + 1)) per block; g is zeroed where the forward output y was not
+// positive (relu), gb receives its BF16 copy, and partial[b][c] the column sums of the
+// masked rows (fixed order: per thread row by row, then thread rows 0..R-1).
+__global__ void k_relu_grad_colsum(float *__restrict__ g, const bf16 *__restrict__ y, long P, int C, int relu,
+                                   long chunk, bf16 *__restrict__ gb, float *__restrict__ partial) {
+    __shared__ float red[256];
+    const int R = 256 / C;
+    const int r = threadIdx.x / C, c = threadIdx.x % C;
+    const long pbeg = (long)blockIdx.x * chunk, pend = min(P, pbeg + chunk);
+    float s = 0.0f;
+    if (r < R)
+        for (long p = pbeg + r; p < pend; p += R) {
+            const size_t i = (size_t)p * C + c;
+            float v = g[i];
+            if (relu && !(__bfloat162float(y[i]) > 0.0f)) {
+                v = 0.0f;
+                g[i] = 0.0f;
+            }
+            gb[i] = __float2bfloat16_rn(v);
+            s += v;
+        }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    if ((int)threadIdx.x < C) {
+        float t = 0.0f;
+        for (int k = 0; k < R; ++k) t += red[k * C + threadIdx.x];
+        partial[(size_t)blockIdx.x * C + threadIdx.x] = t;
+    }
+}
+
+// The same, 4 channels a thread (C a multiple of 4, C <= 1024): 16-byte gradient and 8-byte
+// BF16 accesses.
+__global__ void k_relu_grad_colsum4(float *__restrict__ g, const bf16 *__restrict__ y, long P, int C, int relu,
+                                    long chunk, bf16 *__restrict__ gb, float *__restrict__ partial) {
+    __shared__ float4 red[256];
+    const int C4 = C / 4, R = 256 / C4;
+    const int r = threadIdx.x / C4, c4 = threadIdx.x % C4;
+    const long pbeg = (long)blockIdx.x * chunk, pend = min(P, pbeg + chunk);
+    float4 s = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (r < R)
+        for (long p = pbeg + r; p < pend; p += R) {
+            const size_t i = (size_t)p * C + 4 * c4;
+            float4 v = *reinterpret_cast<const float4 *>(g + i);
+            if (relu) {
+                const uint2 yy = *reinterpret_cast<const uint2 *>(y + i);
+                const float2 y01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&yy.x));
+                const float2 y23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&yy.y));
+                const float4 m = v;
+                if (!(y01.x > 0.0f)) v.x = 0.0f;
+                if (!(y01.y > 0.0f)) v.y = 0.0f;
+                if (!(y23.x > 0.0f)) v.z = 0.0f;
+                if (!(y23.y > 0.0f)) v.w = 0.0f;
+                if (m.x != v.x || m.y != v.y || m.z != v.z || m.w != v.w) *reinterpret_cast<float4 *>(g + i) = v;
+            }
+            const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y), h23 = __floats2bfloat162_rn(v.z, v.w);
+            uint2 o;
+            o.x = *reinterpret_cast<const unsigned *>(&h01);
+            o.y = *reinterpret_cast<const unsigned *>(&h23);
+            *reinterpret_cast<uint2 *>(gb + i) = o;
+            s.x += v.x;
+            s.y += v.y;
+            s.z += v.z;
+            s.w += v.w;
+        }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    if ((int)threadIdx.x < C4) {
+        float4 t = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (int k = 0; k < R; ++k) {
+            const float4 u = red[k * C4 + threadIdx.x];
+            t.x += u.x;
+            t.y += u.y;
+            t.z += u.z;
+            t.w += u.w;
+        }
+        *reinterpret_cast<float4 *>(partial + (size_t)blockIdx.x * C + 4 * threadIdx.x) = t;
+    }
+}
+
+// out[i] = sum over c of partial[c][i], one warp per output: lane l sums chunks l, l + 32, ...
+// in order, then a fixed shuffle tree (deterministic; for few outputs and many chunks).
+__global__ void k_reduce_chunks_warp(const float *__restrict__ partial, int chunks, int n, float *__restrict__ out) {
+    const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (i >= n) return;
+    float s = 0.0f;
+    for (int c = lane; c < chunks; c += 32) s += partial[(size_t)c * n + i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[i] = s;
+}
+
 // 2x2 max pooling, NHWC.
 __global__ void k_pool(const bf16 *__restrict__ x, int B, int H, int W, int C, bf16 *__restrict__ y) {
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -352,6 +444,44 @@ __global__ void k_split_grad(const float *__restrict__ gin, int B, int H, int W,
     const size_t rowc = (size_t)W * Cin;
     const float s = (gin[i] + gin[i + Cin]) + (gin[i + rowc] + gin[i + rowc + Cin]);
     g0[(((size_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * c0 + c] = s;
+}
+
+// The same, 4 channels a thread (c0, c1 multiples of 4): indices [0, n1) copy the skip
+// input's channels, [n1, n1 + n0) the first input's (for an upsampled first input one thread
+// per low-resolution pixel sums its 2 x 2 block, in k_split_grad's order).
+__device__ __forceinline__ float4 add4(const float4 a, const float4 b) {
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+__global__ void k_split_grad4(const float *__restrict__ gin, int B, int H, int W, int c0, int up0, int c1,
+                              float *__restrict__ g0, float *__restrict__ g1) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const int Cin = c0 + c1, q0 = c0 / 4, q1 = c1 / 4;
+    const size_t n1 = (size_t)B * H * W * q1;
+    const size_t n0 = (size_t)B * (up0 ? (H / 2) * (W / 2) : H * W) * q0;
+    if (i < n1) {
+        const size_t p = i / q1;
+        const int c = (int)(i % q1) * 4;
+        *reinterpret_cast<float4 *>(g1 + p * c1 + c) = *reinterpret_cast<const float4 *>(gin + p * Cin + c0 + c);
+        return;
+    }
+    const size_t j = i - n1;
+    if (j >= n0) return;
+    const size_t p = j / q0;
+    const int c = (int)(j % q0) * 4;
+    if (!up0) {
+        *reinterpret_cast<float4 *>(g0 + p * c0 + c) = *reinterpret_cast<const float4 *>(gin + p * Cin + c);
+        return;
+    }
+    const int w = W / 2, h = H / 2;
+    const int xl = (int)(p % w);
+    const size_t r = p / w;
+    const int yl = (int)(r % h);
+    const int b = (int)(r / h);
+    const float *s = gin + (((size_t)b * H + 2 * yl) * W + 2 * xl) * Cin + c;
+    const size_t rowc = (size_t)W * Cin;
+    const float4 a = *reinterpret_cast<const float4 *>(s), bb = *reinterpret_cast<const float4 *>(s + Cin);
+    const float4 cc = *reinterpret_cast<const float4 *>(s + rowc), d = *reinterpret_cast<const float4 *>(s + rowc + Cin);
+    *reinterpret_cast<float4 *>(g0 + p * c0 + c) = add4(add4(a, bb), add4(cc, d));
 }
 
 __global__ void k_relu_grad(float *__restrict__ g, const bf16 *__restrict__ y, size_t n, int relu,
@@ -536,6 +666,7 @@ int launch_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout,
 }
 
 constexpr long kColsumRows = 1024;
+constexpr long kReluRows = 128;  // rows per block of the fused ReLU / bias-gradient pass
 
 }  // namespace
 
@@ -566,7 +697,7 @@ int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, f
     return RT_OK;
 }
 
-size_t colsum_partial_floats(long P, int C) { return (size_t)((P + kColsumRows - 1) / kColsumRows) * C; }
+size_t colsum_partial_floats(long P, int C) { return (size_t)((P + kReluRows - 1) / kReluRows) * C; }
 
 int colsum(const float *g, long P, int C, float *partial, float *db, cudaStream_t st) {
     const int chunks = (int)((P + kColsumRows - 1) / kColsumRows);
@@ -592,7 +723,24 @@ int pool_back(const bf16 *x, const bf16 *y, const float *gy, int B, int H, int W
 }
 
 int split_grad(const float *gin, int B, int H, int W, int c0, int up0, int c1, float *g0, float *g1, cudaStream_t st) {
-    k_split_grad<<<blocks((size_t)B * H * W * (c0 + c1)), 256, 0, st>>>(gin, B, H, W, c0, up0, c1, g0, g1);
+    if (c0 % 4 == 0 && c1 % 4 == 0) {
+        const size_t n = (size_t)B * H * W * (c1 / 4) + (size_t)B * (up0 ? (H / 2) * (W / 2) : H * W) * (c0 / 4);
+        k_split_grad4<<<blocks(n), 256, 0, st>>>(gin, B, H, W, c0, up0, c1, g0, g1);
+    } else {
+        k_split_grad<<<blocks((size_t)B * H * W * (c0 + c1)), 256, 0, st>>>(gin, B, H, W, c0, up0, c1, g0, g1);
+    }
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int relu_grad_bias(float *g, const bf16 *y, long P, int C, bool relu, bf16 *gb, float *partial, float *db,
+                   cudaStream_t st) {
+    const int chunks = (int)((P + kReluRows - 1) / kReluRows);
+    if (C % 4 == 0 && C <= 1024)
+        k_relu_grad_colsum4<<<chunks, 256, 0, st>>>(g, y, P, C, relu ? 1 : 0, kReluRows, gb, partial);
+    else
+        k_relu_grad_colsum<<<chunks, 256, 0, st>>>(g, y, P, C, relu ? 1 : 0, kReluRows, gb, partial);
+    k_reduce_chunks_warp<<<blocks((size_t)C * 32), 256, 0, st>>>(partial, chunks, C, db);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

@@ -77,6 +77,10 @@ int pool_back(const bf16 *x, const bf16 *y, const float *gy, int B, int H, int W
 int split_grad(const float *gin, int B, int H, int W, int c0, int up0, int c1, float *g0, float *g1, cudaStream_t st);
 // g = relu ? g * (y > 0) : g (in place), gb = bf16(g).
 int relu_grad(float *g, const bf16 *y, size_t n, bool relu, bf16 *gb, cudaStream_t st);
+// relu_grad and the bias gradient db[c] = sum over the P rows of the masked g, in one pass
+// (partial: colsum_partial_floats(P, C) floats of scratch).
+int relu_grad_bias(float *g, const bf16 *y, long P, int C, bool relu, bf16 *gb, float *partial, float *db,
+                   cudaStream_t st);
 // Features (B, H, W, 10) fp32 -> network input (B, Hp, Wp, 16) bf16, edge-replicated padding.
 int prepare(const float *f, int B, int H, int W, int Hp, int Wp, bf16 *x, cudaStream_t st);
 // Network output (B, Hp, Wp, 16) fp32 + input log radiance -> radiance (B, H, W, 3).
