@@ -228,24 +228,6 @@ __global__ void k_reduce_chunks(const float *__restrict__ partial, int chunks, s
     out[i] = s;
 }
 
-// Column sums of a (P x C) FP32 matrix over one chunk of rows per block (C <= 256).
-__global__ void k_colsum(const float *__restrict__ g, long P, int C, long chunk, float *__restrict__ partial) {
-    __shared__ float red[256];
-    const int R = 256 / C;
-    const int r = threadIdx.x / C, c = threadIdx.x % C;
-    const long pbeg = (long)blockIdx.x * chunk, pend = min(P, pbeg + chunk);
-    float s = 0.0f;
-    if (r < R)
-        for (long p = pbeg + r; p < pend; p += R) s += g[p * C + c];
-    red[threadIdx.x] = s;
-    __syncthreads();
-    if ((int)threadIdx.x < C) {
-        float t = 0.0f;
-        for (int k = 0; k < R; ++k) t += red[k * C + threadIdx.x];
-        partial[(size_t)blockIdx.x * C + threadIdx.x] = t;
-    }
-}
-
 // ReLU gradient and bias-gradient partials in one pass over a (P x C) FP32 gradient: rows
 // [chunk b, chunk (b + 1)) per block; g is zeroed where the forward output y was not
 // positive (relu), gb receives its BF16 copy, and partial[b][c] the column sums of the
@@ -484,18 +466,6 @@ __global__ void k_split_grad4(const float *__restrict__ gin, int B, int H, int W
     *reinterpret_cast<float4 *>(g0 + p * c0 + c) = add4(add4(a, bb), add4(cc, d));
 }
 
-__global__ void k_relu_grad(float *__restrict__ g, const bf16 *__restrict__ y, size_t n, int relu,
-                            bf16 *__restrict__ gb) {
-    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float v = g[i];
-    if (relu && !(__bfloat162float(y[i]) > 0.0f)) {
-        v = 0.0f;
-        g[i] = 0.0f;
-    }
-    gb[i] = __float2bfloat16_rn(v);
-}
-
 // Features {radiance rgb, albedo rgb, normal xyz, distance} -> 16 channels:
 // log(1 + radiance), albedo, normal / 2 + 1/2, distance / (1 + distance), zeros; padded
 // pixels replicate the nearest edge pixel.
@@ -665,7 +635,6 @@ int launch_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout,
     return RT_OK;
 }
 
-constexpr long kColsumRows = 1024;
 constexpr long kReluRows = 128;  // rows per block of the fused ReLU / bias-gradient pass
 
 }  // namespace
@@ -698,14 +667,6 @@ int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, f
 }
 
 size_t colsum_partial_floats(long P, int C) { return (size_t)((P + kReluRows - 1) / kReluRows) * C; }
-
-int colsum(const float *g, long P, int C, float *partial, float *db, cudaStream_t st) {
-    const int chunks = (int)((P + kColsumRows - 1) / kColsumRows);
-    k_colsum<<<chunks, 256, 0, st>>>(g, P, C, kColsumRows, partial);
-    k_reduce_chunks<<<blocks(C), 256, 0, st>>>(partial, chunks, (size_t)C, db);
-    RT_CUDA_TRY(cudaGetLastError());
-    return RT_OK;
-}
 
 int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st) {
     if (C % 8 == 0)
@@ -741,12 +702,6 @@ int relu_grad_bias(float *g, const bf16 *y, long P, int C, bool relu, bf16 *gb, 
     else
         k_relu_grad_colsum<<<chunks, 256, 0, st>>>(g, y, P, C, relu ? 1 : 0, kReluRows, gb, partial);
     k_reduce_chunks_warp<<<blocks((size_t)C * 32), 256, 0, st>>>(partial, chunks, C, db);
-    RT_CUDA_TRY(cudaGetLastError());
-    return RT_OK;
-}
-
-int relu_grad(float *g, const bf16 *y, size_t n, bool relu, bf16 *gb, cudaStream_t st) {
-    k_relu_grad<<<blocks(n), 256, 0, st>>>(g, y, n, relu ? 1 : 0, gb);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

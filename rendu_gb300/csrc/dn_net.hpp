@@ -69,15 +69,13 @@ int umma_status(bool clear);
 int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, float *partial, float *dw,
                cudaStream_t st);
 size_t wgrad_partial_floats(long P, int Cin, int Cout);
-// db[c] = sum_p g[p, c]; partial holds colsum_partial_floats().
-int colsum(const float *g, long P, int C, float *partial, float *db, cudaStream_t st);
+// Scratch floats of relu_grad_bias's bias-gradient partials.
 size_t colsum_partial_floats(long P, int C);
 int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st);
 int pool_back(const bf16 *x, const bf16 *y, const float *gy, int B, int H, int W, int C, float *gx, cudaStream_t st);
 int split_grad(const float *gin, int B, int H, int W, int c0, int up0, int c1, float *g0, float *g1, cudaStream_t st);
-// g = relu ? g * (y > 0) : g (in place), gb = bf16(g).
-int relu_grad(float *g, const bf16 *y, size_t n, bool relu, bf16 *gb, cudaStream_t st);
-// relu_grad and the bias gradient db[c] = sum over the P rows of the masked g, in one pass
+// The ReLU gradient (g zeroed where the forward output y was not positive, BF16 copy in gb)
+// and the bias gradient db[c] = sum over the P rows of the masked g, in one pass
 // (partial: colsum_partial_floats(P, C) floats of scratch).
 int relu_grad_bias(float *g, const bf16 *y, long P, int C, bool relu, bf16 *gb, float *partial, float *db,
                    cudaStream_t st);
