@@ -228,39 +228,11 @@ __global__ void k_reduce_chunks(const float *__restrict__ partial, int chunks, s
     out[i] = s;
 }
 
-// ReLU gradient and bias-gradient partials in one pass over a (P x C) FP32 gradient: rows
-// [chunk b, chunk (b + 1)) per block; g is zeroed where the forward output y was not
-// positive (relu), gb receives its BF16 copy, and partial[b][c] the column sums of the
-// masked rows (fixed order: per thread row by row, then thread rows 0..R-1).
-__global__ void k_relu_grad_colsum(float *__restrict__ g, const bf16 *__restrict__ y, long P, int C, int relu,
-                                   long chunk, bf16 *__restrict__ gb, float *__restrict__ partial) {
-    __shared__ float red[256];
-    const int R = 256 / C;
-    const int r = threadIdx.x / C, c = threadIdx.x % C;
-    const long pbeg = (long)blockIdx.x * chunk, pend = min(P, pbeg + chunk);
-    float s = 0.0f;
-    if (r < R)
-        for (long p = pbeg + r; p < pend; p += R) {
-            const size_t i = (size_t)p * C + c;
-            float v = g[i];
-            if (relu && !(__bfloat162float(y[i]) > 0.0f)) {
-                v = 0.0f;
-                g[i] = 0.0f;
-            }
-            gb[i] = __float2bfloat16_rn(v);
-            s += v;
-        }
-    red[threadIdx.x] = s;
-    __syncthreads();
-    if ((int)threadIdx.x < C) {
-        float t = 0.0f;
-        for (int k = 0; k < R; ++k) t += red[k * C + threadIdx.x];
-        partial[(size_t)blockIdx.x * C + threadIdx.x] = t;
-    }
-}
-
-// The same, 4 channels a thread (C a multiple of 4, C <= 1024): 16-byte gradient and 8-byte
-// BF16 accesses.
+// ReLU gradient and bias-gradient partials in one pass over a (P x C) FP32 gradient, 4
+// channels a thread (C a multiple of 4, C <= 1024): rows [chunk b, chunk (b + 1)) per block;
+// g is zeroed where the forward output y was not positive (relu), gb receives its BF16 copy,
+// and partial[b][c] the column sums of the masked rows (fixed order: per thread row by row,
+// then thread rows 0..R-1).
 __global__ void k_relu_grad_colsum4(float *__restrict__ g, const bf16 *__restrict__ y, long P, int C, int relu,
                                     long chunk, bf16 *__restrict__ gb, float *__restrict__ partial) {
     __shared__ float4 red[256];
@@ -401,39 +373,14 @@ __global__ void k_pool_back(const bf16 *__restrict__ x, const bf16 *__restrict__
 
 // Gradient of a concatenated input: channels [0, c0) go to g0 -- summed over each 2x2 block
 // (the adjoint of nearest upsampling) when up0 -- and channels [c0, c0 + c1) to g1.
-// Both are assigned (each is the first gradient its tensor receives).
-__global__ void k_split_grad(const float *__restrict__ gin, int B, int H, int W, int c0, int up0, int c1,
-                             float *__restrict__ g0, float *__restrict__ g1) {
-    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    const int Cin = c0 + c1;
-    const size_t n = (size_t)B * H * W * Cin;
-    if (i >= n) return;
-    const int c = (int)(i % Cin);
-    const size_t p = i / Cin;
-    if (c >= c0) {
-        g1[p * c1 + (c - c0)] = gin[i];
-        return;
-    }
-    if (!up0) {
-        g0[p * c0 + c] = gin[i];
-        return;
-    }
-    const int x = (int)(p % W);
-    const size_t q = p / W;
-    const int y = (int)(q % H);
-    const int b = (int)(q / H);
-    if ((x & 1) || (y & 1)) return;
-    const size_t rowc = (size_t)W * Cin;
-    const float s = (gin[i] + gin[i + Cin]) + (gin[i + rowc] + gin[i + rowc + Cin]);
-    g0[(((size_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * c0 + c] = s;
-}
-
-// The same, 4 channels a thread (c0, c1 multiples of 4): indices [0, n1) copy the skip
-// input's channels, [n1, n1 + n0) the first input's (for an upsampled first input one thread
-// per low-resolution pixel sums its 2 x 2 block, in k_split_grad's order).
+// Both are assigned (each is the first gradient its tensor receives). 4 channels a thread
+// (c0, c1 multiples of 4): indices [0, n1) copy the skip input's channels, [n1, n1 + n0) the
+// first input's (for an upsampled first input one thread per low-resolution pixel sums its
+// 2 x 2 block as (a + b) + (c + d), a b / c d its pixels).
 __device__ __forceinline__ float4 add4(const float4 a, const float4 b) {
     return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
 }
+
 __global__ void k_split_grad4(const float *__restrict__ gin, int B, int H, int W, int c0, int up0, int c1,
                               float *__restrict__ g0, float *__restrict__ g1) {
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -684,12 +631,12 @@ int pool_back(const bf16 *x, const bf16 *y, const float *gy, int B, int H, int W
 }
 
 int split_grad(const float *gin, int B, int H, int W, int c0, int up0, int c1, float *g0, float *g1, cudaStream_t st) {
-    if (c0 % 4 == 0 && c1 % 4 == 0) {
-        const size_t n = (size_t)B * H * W * (c1 / 4) + (size_t)B * (up0 ? (H / 2) * (W / 2) : H * W) * (c0 / 4);
-        k_split_grad4<<<blocks(n), 256, 0, st>>>(gin, B, H, W, c0, up0, c1, g0, g1);
-    } else {
-        k_split_grad<<<blocks((size_t)B * H * W * (c0 + c1)), 256, 0, st>>>(gin, B, H, W, c0, up0, c1, g0, g1);
+    if (c0 % 4 != 0 || c1 % 4 != 0) {
+        set_error("split_grad needs channel counts that are multiples of 4");
+        return RT_ERR_ARG;
     }
+    const size_t n = (size_t)B * H * W * (c1 / 4) + (size_t)B * (up0 ? (H / 2) * (W / 2) : H * W) * (c0 / 4);
+    k_split_grad4<<<blocks(n), 256, 0, st>>>(gin, B, H, W, c0, up0, c1, g0, g1);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
@@ -697,10 +644,11 @@ int split_grad(const float *gin, int B, int H, int W, int c0, int up0, int c1, f
 int relu_grad_bias(float *g, const bf16 *y, long P, int C, bool relu, bf16 *gb, float *partial, float *db,
                    cudaStream_t st) {
     const int chunks = (int)((P + kReluRows - 1) / kReluRows);
-    if (C % 4 == 0 && C <= 1024)
-        k_relu_grad_colsum4<<<chunks, 256, 0, st>>>(g, y, P, C, relu ? 1 : 0, kReluRows, gb, partial);
-    else
-        k_relu_grad_colsum<<<chunks, 256, 0, st>>>(g, y, P, C, relu ? 1 : 0, kReluRows, gb, partial);
+    if (C % 4 != 0 || C > 1024) {
+        set_error("relu_grad_bias needs a channel count that is a multiple of 4, at most 1024");
+        return RT_ERR_ARG;
+    }
+    k_relu_grad_colsum4<<<chunks, 256, 0, st>>>(g, y, P, C, relu ? 1 : 0, kReluRows, gb, partial);
     k_reduce_chunks_warp<<<blocks((size_t)C * 32), 256, 0, st>>>(partial, chunks, C, db);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
