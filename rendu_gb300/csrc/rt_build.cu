@@ -132,18 +132,24 @@ __device__ __forceinline__ uint64_t spread21(uint64_t x) {
     return x;
 }
 
+// Morton code of the triangle box centroid, 21 bits an axis. The centroid bounds are scaled
+// by their largest extent on every axis (a cube), not axis by axis: on a flat scene the
+// per-axis scaling spends as many top-level splits on the thin axis as on the wide ones.
+// Measured on the 2M-triangle instanced scene (a 200-object layer on a ground plane): the
+// 1080p extended render 224.8 -> 214.1 ms; no change on the displaced sphere (a cube
+// already). Adding 6 bits of triangle size to the key measured no further gain.
 __global__ void k_morton(const float4 *__restrict__ tlo, const float4 *__restrict__ thi, uint64_t nt,
                          const unsigned *__restrict__ cb, uint64_t *__restrict__ keys, uint32_t *__restrict__ vals) {
     const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (t >= nt) return;
     const float4 lo = tlo[t], hi = thi[t];
     const float c[3] = {0.5f * (lo.x + hi.x), 0.5f * (lo.y + hi.y), 0.5f * (lo.z + hi.z)};
+    float ext = 0.0f;
+    for (int k = 0; k < 3; ++k) ext = fmaxf(ext, ord2f(cb[3 + k]) - ord2f(cb[k]));
     uint64_t code = 0;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const float a = ord2f(cb[k]), b = ord2f(cb[3 + k]);
-        const float ext = b - a;
-        float u = ext > 0.0f ? (c[k] - a) / ext : 0.5f;
+        float u = ext > 0.0f ? (c[k] - ord2f(cb[k])) / ext : 0.5f;
         u = fminf(fmaxf(u, 0.0f), 1.0f);
         const uint64_t q = (uint64_t)fminf(u * 2097152.0f, 2097151.0f);
         code |= spread21(q) << (2 - k);
