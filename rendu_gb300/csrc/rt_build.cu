@@ -7,7 +7,8 @@
 //   1. vertices transformed by their mesh's model matrix (exact glm operator order);
 //   2. per-triangle boxes, edges and 63-bit Morton codes of the box centroids;
 //   3. radix sort of (code, triangle) pairs;
-//   4. Karras' binary radix tree over the sorted codes (one thread per inner node);
+//   4. a binary tree over the sorted leaves: Karras' radix tree (one thread per inner node)
+//      for a single mesh, locally-ordered clustering (PLOC, below) for several meshes;
 //   5. a bottom-up pass (one thread per leaf, atomics decide who climbs) that merges child
 //      boxes and collapses every subtree of <= RT_LEAF_MAX triangles into one leaf where
 //      the surface-area cost says a leaf is cheaper;
@@ -16,10 +17,12 @@
 // Query answers do not depend on the tree shape (closest hit = smallest distance, exact
 // per-triangle test), so the tree only decides speed.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include <cmath>
 #include <cstring>
 #include <utility>
+#include <vector>
 
 #include "rt_context.hpp"
 
@@ -246,8 +249,9 @@ __global__ void k_bottom_up(uint64_t nt, const uint32_t *__restrict__ child, con
     const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (k >= nt) return;
     uint32_t node = parent_leaf[k];
-    // A Karras tree over 64-bit keys with 32-bit index tie-breaks is at most 96 levels deep.
-    for (int level = 0; level < 128; ++level) {
+    // A Karras tree over 64-bit keys with 32-bit index tie-breaks is at most 96 levels deep;
+    // a clustered tree has no such bound, so the climb allows far more.
+    for (int level = 0; level < 4096; ++level) {
         if (node >= nt - 1) return;
         __threadfence();
         if (atomicAdd(&arrivals[node], 1u) == 0u) return;  // first arrival stops
@@ -285,6 +289,197 @@ __global__ void k_bottom_up(uint64_t nt, const uint32_t *__restrict__ child, con
         if (node == 0) return;
         node = parent_inner[node];
     }
+}
+
+// ---- PLOC: parallel locally-ordered clustering (Meister & Bittner 2018) ----------------------
+// The alternative to Karras' radix tree for step 4. Clusters start as the leaves in Morton
+// order. Each round, every cluster finds its nearest neighbour within kPlocRadius positions
+// (smallest half area of the union box); mutual pairs merge into a new inner node at the
+// lower position, and the array is compacted. Ties are broken by the smaller index, which for
+// a fixed cluster orders its pairs exactly like the pair key (area, min index, max index):
+// the globally closest pair is always mutual, so every round merges at least one pair. Inner
+// nodes are numbered in creation order (the root last); children always precede their
+// parent. The leaves are then renumbered in depth-first order, so that every subtree's
+// leaves are contiguous as the collapse into 4-wide nodes needs.
+// RT_PLOC: 1 = always cluster, 0 = always the radix tree, 2 (default) = cluster when the
+// context holds more than one mesh. Measured (1080p extended render of the 205-object
+// instanced scene; 16M random rays into the 1.3M-triangle displaced sphere): clustering with
+// radius 4 renders 214 -> 190 ms (SAH cost 77.4 -> 72.7), while on the single surface the
+// radix tree's spatial-median splits stay 2 % faster for closest hits (1.38 vs 1.41 ms).
+// Radii 6-64 measured no better than 4.
+#ifndef RT_PLOC
+#define RT_PLOC 2
+#endif
+#ifndef RT_PLOC_RADIUS
+#define RT_PLOC_RADIUS 4
+#endif
+constexpr int kPlocRadius = RT_PLOC_RADIUS;
+constexpr int kPlocBlock = 256;
+
+__global__ void k_ploc_nn(const float4 *__restrict__ lo, const float4 *__restrict__ hi, uint32_t n,
+                          uint32_t *__restrict__ nn) {
+    __shared__ float4 slo[kPlocBlock + 2 * kPlocRadius], shi[kPlocBlock + 2 * kPlocRadius];
+    const long b0 = (long)blockIdx.x * kPlocBlock;
+    for (int t = threadIdx.x; t < kPlocBlock + 2 * kPlocRadius; t += kPlocBlock) {
+        const long g = b0 - kPlocRadius + t;
+        if (g >= 0 && g < (long)n) {
+            slo[t] = lo[g];
+            shi[t] = hi[g];
+        }
+    }
+    __syncthreads();
+    const long i = b0 + threadIdx.x;
+    if (i >= (long)n) return;
+    const float4 a = slo[threadIdx.x + kPlocRadius], b = shi[threadIdx.x + kPlocRadius];
+    float best = INFINITY;
+    uint32_t bj = (uint32_t)i;
+    for (int o = -kPlocRadius; o <= kPlocRadius; ++o) {
+        const long j = i + o;
+        if (o == 0 || j < 0 || j >= (long)n) continue;
+        const float4 c = slo[threadIdx.x + kPlocRadius + o], d = shi[threadIdx.x + kPlocRadius + o];
+        const float area = half_area(make_float4(fminf(a.x, c.x), fminf(a.y, c.y), fminf(a.z, c.z), 0.0f),
+                                     make_float4(fmaxf(b.x, d.x), fmaxf(b.y, d.y), fmaxf(b.z, d.z), 0.0f));
+        if (area < best) {
+            best = area;
+            bj = (uint32_t)j;
+        }
+    }
+    nn[i] = bj;
+}
+
+__global__ void k_ploc_flags(const uint32_t *__restrict__ nn, uint32_t n, uint32_t *__restrict__ merge,
+                             uint32_t *__restrict__ alive) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t j = nn[i];
+    const bool mutual = j != i && j < n && nn[j] == i;
+    merge[i] = mutual && i < j ? 1u : 0u;
+    alive[i] = mutual && i > j ? 0u : 1u;
+}
+
+__global__ void k_ploc_compact(const uint32_t *__restrict__ node, const float4 *__restrict__ lo,
+                               const float4 *__restrict__ hi, const uint32_t *__restrict__ cnt,
+                               const uint32_t *__restrict__ nn, const uint32_t *__restrict__ merge,
+                               const uint32_t *__restrict__ alive, const uint32_t *__restrict__ moff,
+                               const uint32_t *__restrict__ apos, uint32_t n, uint32_t inner_base, uint32_t ni,
+                               uint32_t *__restrict__ child, uint32_t *__restrict__ icount,
+                               uint32_t *__restrict__ node2, float4 *__restrict__ lo2, float4 *__restrict__ hi2,
+                               uint32_t *__restrict__ cnt2, unsigned *__restrict__ status) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !alive[i]) return;
+    const uint32_t p = apos[i];
+    if (p >= n) {
+        atomicOr(status, RT_DEV_QUEUE_OVERFLOW);
+        return;
+    }
+    if (merge[i]) {
+        const uint32_t j = nn[i];
+        const uint32_t id = inner_base + moff[i];
+        if (id >= ni || j >= n) {
+            atomicOr(status, RT_DEV_QUEUE_OVERFLOW);
+            return;
+        }
+        child[2 * id] = node[i];
+        child[2 * id + 1] = node[j];
+        const uint32_t c = cnt[i] + cnt[j];
+        icount[id] = c;
+        const float4 a = lo[i], b = hi[i], e = lo[j], f = hi[j];
+        node2[p] = id << 1;
+        lo2[p] = make_float4(fminf(a.x, e.x), fminf(a.y, e.y), fminf(a.z, e.z), 0.0f);
+        hi2[p] = make_float4(fmaxf(b.x, f.x), fmaxf(b.y, f.y), fmaxf(b.z, f.z), 0.0f);
+        cnt2[p] = c;
+    } else {
+        node2[p] = node[i];
+        lo2[p] = lo[i];
+        hi2[p] = hi[i];
+        cnt2[p] = cnt[i];
+    }
+}
+
+__global__ void k_ploc_init(uint64_t nt, const float4 *__restrict__ slo, const float4 *__restrict__ shi,
+                            uint32_t *__restrict__ node, float4 *__restrict__ lo, float4 *__restrict__ hi,
+                            uint32_t *__restrict__ cnt) {
+    const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (k >= nt) return;
+    node[k] = ((uint32_t)k << 1) | 1u;
+    lo[k] = slo[k];
+    hi[k] = shi[k];
+    cnt[k] = 1u;
+}
+
+// First leaf position of each subtree, top-down one creation round at a time (latest round
+// first: a node's parent is always of a later round). Leaves get their position in the
+// depth-first leaf order, in which every subtree's leaves are contiguous.
+__global__ void k_ploc_topdown(uint32_t id0, uint32_t count, uint32_t ni, uint64_t nt, const uint32_t *__restrict__ child,
+                               const uint32_t *__restrict__ icount, uint32_t *__restrict__ ifirst,
+                               uint32_t *__restrict__ lpos, unsigned *__restrict__ status) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const uint32_t id = id0 + i;
+    if (id >= ni) return;
+    uint32_t f = ifirst[id];
+    for (int s = 0; s < 2; ++s) {
+        const uint32_t c = child[2 * id + s];
+        const uint32_t x = c >> 1;
+        if (c & 1u) {
+            if (x >= nt || f >= nt) {
+                atomicOr(status, RT_DEV_QUEUE_OVERFLOW);
+                return;
+            }
+            lpos[x] = f;
+            f += 1;
+        } else {
+            if (x >= ni) {
+                atomicOr(status, RT_DEV_QUEUE_OVERFLOW);
+                return;
+            }
+            ifirst[x] = f;
+            f += icount[x];
+        }
+    }
+}
+
+// The tree in the layout the bottom-up pass and the collapse read: inner node ids reversed
+// (root = 0), leaves renumbered to their depth-first positions, parents and leaf ranges.
+__global__ void k_ploc_final(uint32_t ni, uint64_t nt, const uint32_t *__restrict__ child,
+                             const uint32_t *__restrict__ icount, const uint32_t *__restrict__ ifirst,
+                             const uint32_t *__restrict__ lpos, uint32_t *__restrict__ child_out,
+                             uint32_t *__restrict__ pin, uint32_t *__restrict__ pleaf, uint32_t *__restrict__ rf,
+                             uint32_t *__restrict__ rl, unsigned *__restrict__ status) {
+    const uint32_t id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= ni) return;
+    const uint32_t id2 = ni - 1 - id;
+    for (int s = 0; s < 2; ++s) {
+        const uint32_t c = child[2 * id + s];
+        const uint32_t x = c >> 1;
+        if (c & 1u) {
+            const uint32_t k2 = x < nt ? lpos[x] : 0xFFFFFFFFu;
+            if (k2 >= nt) {
+                atomicOr(status, RT_DEV_QUEUE_OVERFLOW);
+                return;
+            }
+            child_out[2 * id2 + s] = (k2 << 1) | 1u;
+            pleaf[k2] = id2;
+        } else {
+            if (x >= ni) {
+                atomicOr(status, RT_DEV_QUEUE_OVERFLOW);
+                return;
+            }
+            const uint32_t c2 = ni - 1 - x;
+            child_out[2 * id2 + s] = c2 << 1;
+            pin[c2] = id2;
+        }
+    }
+    rf[id2] = ifirst[id];
+    rl[id2] = ifirst[id] + icount[id] - 1;
+}
+
+__global__ void k_scatter_order(const uint32_t *__restrict__ order, const uint32_t *__restrict__ lpos, uint64_t nt,
+                                uint32_t *__restrict__ order2) {
+    const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (k >= nt) return;
+    const uint32_t p = lpos[k];
+    if (p < nt) order2[p] = order[k];
 }
 
 __device__ __forceinline__ void set_slot(BvhNode &nd, int c, float4 lo, float4 hi, int child, int count) {
@@ -368,6 +563,26 @@ __global__ void k_collapse(const CollapseItem *__restrict__ in, uint32_t n_in, C
     }
     nodes[item.slot] = nd;
     atomicAdd(leaf_count, leaves);
+}
+
+// Stack bound of the traversal, bottom-up one collapse level at a time (deepest first): a
+// visit pushes at most (inner children - 1) entries and continues into one inner child, so
+// need(node) = max(0, inner children - 1) + the largest need of its inner children bounds
+// the stack depth of any walk below the node.
+__global__ void k_stack_need(const BvhNode *__restrict__ nodes, uint32_t s0, uint32_t s1, uint32_t cap,
+                             uint32_t *__restrict__ need) {
+    const uint32_t slot = s0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= s1 || slot >= cap) return;
+    const BvhNode nd = nodes[slot];
+    const int ch[4] = {nd.child.x, nd.child.y, nd.child.z, nd.child.w};
+    const int cn[4] = {nd.count.x, nd.count.y, nd.count.z, nd.count.w};
+    uint32_t inner = 0, deepest = 0;
+    for (int c = 0; c < 4; ++c)
+        if (cn[c] == 0 && ch[c] >= 0 && (uint32_t)ch[c] < cap) {
+            ++inner;
+            deepest = max(deepest, need[ch[c]]);
+        }
+    need[slot] = (inner > 0 ? inner - 1 : 0) + deepest;
 }
 
 // A root whose whole tree is one leaf (or a single triangle): slot 0 = the leaf.
@@ -512,7 +727,89 @@ int build_hierarchy(rt_ctx *ctx) {
         RT_CUDA_TRY(d_arr.alloc(ni));
         RT_CUDA_TRY(cudaMemsetAsync(d_arr.p, 0, ni * sizeof(unsigned), st));
         const unsigned ib = (unsigned)((ni + 255) / 256);
-        k_karras<<<ib, 256, 0, st>>>(d_keys2.p, (int64_t)nt, d_child.p, d_pin.p, d_pleaf.p, d_rf.p, d_rl.p);
+        const bool cluster = RT_PLOC == 1 || (RT_PLOC == 2 && ctx->meshes.size() > 1);
+        if (!cluster) {
+            k_karras<<<ib, 256, 0, st>>>(d_keys2.p, (int64_t)nt, d_child.p, d_pin.p, d_pleaf.p, d_rf.p, d_rl.p);
+        } else {
+            // PLOC rounds over the Morton-ordered leaf boxes.
+            Scratch<uint32_t> d_node[2], d_cnt[2], d_nn, d_merge, d_alive, d_moff, d_apos, d_pchild, d_icount, d_ifirst,
+                d_lpos, d_order2;
+            Scratch<float4> d_clo[2], d_chi[2];
+            for (int b = 0; b < 2; ++b) {
+                RT_CUDA_TRY(d_node[b].alloc(nt));
+                RT_CUDA_TRY(d_cnt[b].alloc(nt));
+                RT_CUDA_TRY(d_clo[b].alloc(nt));
+                RT_CUDA_TRY(d_chi[b].alloc(nt));
+            }
+            RT_CUDA_TRY(d_nn.alloc(nt));
+            RT_CUDA_TRY(d_merge.alloc(nt));
+            RT_CUDA_TRY(d_alive.alloc(nt));
+            RT_CUDA_TRY(d_moff.alloc(nt));
+            RT_CUDA_TRY(d_apos.alloc(nt));
+            RT_CUDA_TRY(d_pchild.alloc(2 * ni));
+            RT_CUDA_TRY(d_icount.alloc(ni));
+            RT_CUDA_TRY(d_ifirst.alloc(ni));
+            RT_CUDA_TRY(d_lpos.alloc(nt));
+            RT_CUDA_TRY(d_order2.alloc(nt));
+            size_t scan_bytes = 0;
+            RT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, d_merge.p, d_moff.p, (int)nt, st));
+            Scratch<unsigned char> d_scan;
+            RT_CUDA_TRY(d_scan.alloc(scan_bytes));
+            unsigned *status = ctx->d_status.as<unsigned>();
+            k_ploc_init<<<tb, 256, 0, st>>>(nt, d_slo.p, d_shi.p, d_node[0].p, d_clo[0].p, d_chi[0].p, d_cnt[0].p);
+            std::vector<uint32_t> round_base, round_count;
+            uint32_t n = (uint32_t)nt, inner = 0;
+            int cur = 0;
+            while (n > 1) {
+                if (round_base.size() > 100000) {
+                    set_error("hierarchy clustering did not terminate");
+                    return RT_ERR_STATE;
+                }
+                const unsigned nb = (n + kPlocBlock - 1) / kPlocBlock;
+                k_ploc_nn<<<nb, kPlocBlock, 0, st>>>(d_clo[cur].p, d_chi[cur].p, n, d_nn.p);
+                k_ploc_flags<<<nb, kPlocBlock, 0, st>>>(d_nn.p, n, d_merge.p, d_alive.p);
+                RT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(d_scan.p, scan_bytes, d_merge.p, d_moff.p, (int)n, st));
+                RT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(d_scan.p, scan_bytes, d_alive.p, d_apos.p, (int)n, st));
+                k_ploc_compact<<<nb, kPlocBlock, 0, st>>>(
+                    d_node[cur].p, d_clo[cur].p, d_chi[cur].p, d_cnt[cur].p, d_nn.p, d_merge.p, d_alive.p, d_moff.p,
+                    d_apos.p, n, inner, (uint32_t)ni, d_pchild.p, d_icount.p, d_node[cur ^ 1].p, d_clo[cur ^ 1].p,
+                    d_chi[cur ^ 1].p, d_cnt[cur ^ 1].p, status);
+                uint32_t tail[4];
+                RT_CUDA_TRY(cudaMemcpyAsync(&tail[0], d_moff.p + (n - 1), 4, cudaMemcpyDeviceToHost, st));
+                RT_CUDA_TRY(cudaMemcpyAsync(&tail[1], d_merge.p + (n - 1), 4, cudaMemcpyDeviceToHost, st));
+                RT_CUDA_TRY(cudaMemcpyAsync(&tail[2], d_apos.p + (n - 1), 4, cudaMemcpyDeviceToHost, st));
+                RT_CUDA_TRY(cudaMemcpyAsync(&tail[3], d_alive.p + (n - 1), 4, cudaMemcpyDeviceToHost, st));
+                RT_CUDA_TRY(cudaStreamSynchronize(st));
+                const uint32_t merges = tail[0] + tail[1], n_new = tail[2] + tail[3];
+                if (merges == 0 || n_new + merges != n || inner + merges > ni) {
+                    set_error("hierarchy clustering made no progress");
+                    return RT_ERR_STATE;
+                }
+                round_base.push_back(inner);
+                round_count.push_back(merges);
+                inner += merges;
+                n = n_new;
+                cur ^= 1;
+            }
+            if (inner != ni) {
+                set_error("hierarchy clustering left several roots");
+                return RT_ERR_STATE;
+            }
+            const uint32_t zero = 0;
+            RT_CUDA_TRY(cudaMemcpyAsync(d_ifirst.p + (ni - 1), &zero, 4, cudaMemcpyHostToDevice, st));
+            for (size_t r = round_base.size(); r-- > 0;)
+                k_ploc_topdown<<<(round_count[r] + 255) / 256, 256, 0, st>>>(
+                    round_base[r], round_count[r], (uint32_t)ni, nt, d_pchild.p, d_icount.p, d_ifirst.p, d_lpos.p,
+                    status);
+            k_ploc_final<<<ib, 256, 0, st>>>((uint32_t)ni, nt, d_pchild.p, d_icount.p, d_ifirst.p, d_lpos.p,
+                                             d_child.p, d_pin.p, d_pleaf.p, d_rf.p, d_rl.p, status);
+            // Leaves, their boxes and the triangles again, in the depth-first leaf order (zeroed
+            // first: a malformed permutation would leave valid triangle ids, never stray ones).
+            RT_CUDA_TRY(cudaMemsetAsync(d_order2.p, 0, nt * sizeof(uint32_t), st));
+            k_scatter_order<<<tb, 256, 0, st>>>(d_vals2.p, d_lpos.p, nt, d_order2.p);
+            k_leaves<<<tb, 256, 0, st>>>(d_order2.p, nt, d_tlo.p, d_thi.p, ctx->d_verts.as<float>(), d_idx.p, eps,
+                                         d_slo.p, d_shi.p, ctx->d_tris.as<BvhTri>());
+        }
         k_bottom_up<<<tb, 256, 0, st>>>(nt, d_child.p, d_pin.p, d_pleaf.p, d_rf.p, d_rl.p, d_slo.p, d_shi.p, d_ilo.p,
                                         d_ihi.p, d_cost.p, d_col.p, d_height.p, d_arr.p);
         uint8_t root_col = 0;
@@ -547,6 +844,7 @@ int build_hierarchy(rt_ctx *ctx) {
             RT_CUDA_TRY(cudaMemcpyAsync(d_q0.p, &root, sizeof(root), cudaMemcpyHostToDevice, st));
             RT_CUDA_TRY(cudaMemcpyAsync(d_cnt.p, cnt_init, sizeof(cnt_init), cudaMemcpyHostToDevice, st));
             uint32_t n_in = 1, levels = 0;
+            std::vector<uint32_t> level_end(1, 1u);  // slots [level_end[l-1], level_end[l]) = level l
             CollapseItem *qin = d_q0.p, *qout = d_q1.p;
             while (n_in > 0) {
                 RT_CUDA_TRY(cudaMemsetAsync(d_cnt.p, 0, sizeof(uint32_t), st));
@@ -554,8 +852,11 @@ int build_hierarchy(rt_ctx *ctx) {
                                                                d_child.p, d_rf.p, d_rl.p, d_slo.p, d_shi.p, d_ilo.p,
                                                                d_ihi.p, d_col.p, ctx->d_nodes.as<BvhNode>(),
                                                                d_cnt.p + 2, ctx->d_status.as<unsigned>());
-                RT_CUDA_TRY(cudaMemcpyAsync(&n_in, d_cnt.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+                uint32_t cn2[2];
+                RT_CUDA_TRY(cudaMemcpyAsync(cn2, d_cnt.p, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
                 RT_CUDA_TRY(cudaStreamSynchronize(st));
+                n_in = cn2[0];
+                if (n_in > 0) level_end.push_back(cn2[1]);
                 std::swap(qin, qout);
                 ++levels;
                 if (levels > 200) {
@@ -568,8 +869,19 @@ int build_hierarchy(rt_ctx *ctx) {
             RT_CUDA_TRY(cudaStreamSynchronize(st));
             ctx->n_inner = cnt[1];
             ctx->n_leaves = cnt[2];
-            // The traversal pushes at most 3 entries per level.
-            ctx->depth = 3 * (int)levels;
+            // Stack bound from the collapsed tree (at most 3 entries per level, usually far fewer).
+            Scratch<uint32_t> d_need;
+            RT_CUDA_TRY(d_need.alloc(cnt[1]));
+            for (size_t l = level_end.size(); l-- > 0;) {
+                const uint32_t s0 = l ? level_end[l - 1] : 0u, s1 = std::min(level_end[l], cnt[1]);
+                if (s1 > s0)
+                    k_stack_need<<<(s1 - s0 + 127) / 128, 128, 0, st>>>(ctx->d_nodes.as<BvhNode>(), s0, s1, cnt[1],
+                                                                      d_need.p);
+            }
+            uint32_t need0 = 0;
+            RT_CUDA_TRY(cudaMemcpyAsync(&need0, d_need.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+            RT_CUDA_TRY(cudaStreamSynchronize(st));
+            ctx->depth = std::min(3 * (int)levels, (int)need0 + 1);
             (void)root_h;
         }
     }
