@@ -222,7 +222,11 @@ constexpr float kCostInner = 1.2f;  // relative cost of one node visit (two box 
 // this weight nearly every leaf holds one triangle, which measured fastest (closest hit on
 // 16M random rays into 1.3M triangles -6 %, the 2M-triangle path-traced scene -3 %,
 // against a weight of 1).
-constexpr float kCostTri = 3.0f;
+// With the optimal 4-wide collapse, weights 2, 4 and 6 measured no better than 3.
+#ifndef RT_COST_TRI
+#define RT_COST_TRI 3.0f
+#endif
+constexpr float kCostTri = RT_COST_TRI;
 
 // Gather sorted triangle boxes (inflated by eps, making the traversal's box tests
 // conservative) and write leaf-order triangles.
