@@ -103,8 +103,9 @@ RT_API int rt_add_mesh(rt_ctx *ctx, const float *positions, size_t vertex_count,
                 size_t index_count, const float *model, uint32_t *mesh_id);
 
 /* Build the device hierarchy over every mesh added so far. Replaces
- * Raycaster::updateHierarchy (Raycaster.cpp:54-142); the hierarchy differs (a GPU LBVH
- * with surface-area leaf collapsing) but every query answers the same. */
+ * Raycaster::updateHierarchy (Raycaster.cpp:54-142); the hierarchy differs (a 4-wide GPU
+ * hierarchy: a Morton radix tree for one mesh, locally-ordered clustering for several, with
+ * surface-area leaf collapsing and 4-wide conversion) but every query answers the same. */
 RT_API int rt_update_hierarchy(rt_ctx *ctx);
 
 /* Closest hit for n rays. Replaces Raycaster::intersects(origin, direction, mini, maxi)
