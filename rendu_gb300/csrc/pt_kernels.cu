@@ -133,10 +133,13 @@ __device__ __forceinline__ void push_shadow(const PtWave &w, uint32_t slot, f3 o
 }
 
 template <bool EXT>
-// At least 6 resident blocks per SM (at most 80 registers): shading is gather-latency bound,
-// and the occupancy gained outweighs the few spilled registers (the 1080p extended render
-// measured 3.4 % faster than at 108 registers).
-__global__ void __launch_bounds__(128, 6) k_shade(PtWave w, int cur, uint32_t did) {
+// At least 7 resident blocks per SM (at most 72 registers): shading is gather-latency bound,
+// and the occupancy gained outweighs the spilled registers (the 1080p extended render:
+// 108 registers -> 6 blocks 3.4 % faster; 6 -> 7 blocks 189.4 -> 185.3 ms; 8 blocks 187.4 ms).
+#ifndef PT_SHADE_MINB
+#define PT_SHADE_MINB 7
+#endif
+__global__ void __launch_bounds__(128, PT_SHADE_MINB) k_shade(PtWave w, int cur, uint32_t did) {
     const uint32_t n = min(w.counters[cur], w.cap);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicAdd(&w.stats[did == 0 ? 0 : 1], (unsigned long long)n);  // rays traced this bounce
