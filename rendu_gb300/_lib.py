@@ -165,7 +165,7 @@ _SIGS = {
 
 
 def lib():
-    """Load the library once; raise if it is absent (build it with __graft_entry__.build())."""
+    """Load the library once; raise if it is absent (build it with rendu_gb300.build.build())."""
     global _lib
     with _lock:
         if _lib is None:
