@@ -38,10 +38,12 @@ __global__ void __launch_bounds__(128) k_trace(const BvhNode *__restrict__ nodes
     }
 }
 
-// Persistent variant: a grid sized to fill the GPU once; lanes refill from `counter`
-// (zeroed before the launch). n is read from n_dev when given (device-side queue length).
-// The box of the whole hierarchy (the union of the grown leaf boxes): a ray that misses it
-// misses every child box of the root, so it is answered without a node fetch.
+// Persistent variant: a grid sized to fill the GPU once; idle lanes take new rays from
+// their block's interleaved share through a shared-memory counter (RT_FETCH_BLOCK 1) or from
+// the global `counter` zeroed before the launch (0). n is read from n_dev when given
+// (device-side queue length). The box of the whole hierarchy (the union of the grown leaf
+// boxes): a ray that misses it misses every child box of the root, so it is answered
+// without a node fetch.
 // Refill heuristics (see k_trace_batch): on the raycaster workload, where 88 % of the rays
 // miss the root box and are answered at intake, thresholds 8-16 measured equal to 1 and
 // back-to-back rounds slower (2-4 rounds: 1.39 -> 1.55-2.02 ms per 16M rays).
