@@ -364,6 +364,7 @@ __global__ void k_bottom_up(uint64_t nt, const uint32_t *__restrict__ child, con
 #endif
 constexpr int kPlocRadius = RT_PLOC_RADIUS;
 constexpr int kPlocBlock = 256;
+constexpr size_t kPlocMaxRounds = 512;  // typical builds take about 50 rounds
 
 __global__ void k_ploc_nn(const float4 *__restrict__ lo, const float4 *__restrict__ hi, uint32_t n,
                           uint32_t *__restrict__ nn) {
@@ -817,9 +818,8 @@ int build_hierarchy(rt_ctx *ctx) {
         RT_CUDA_TRY(cudaMemsetAsync(d_arr.p, 0, ni * sizeof(unsigned), st));
         const unsigned ib = (unsigned)((ni + 255) / 256);
         const bool cluster = RT_PLOC == 1 || (RT_PLOC == 2 && ctx->meshes.size() > 1);
-        if (!cluster) {
-            k_karras<<<ib, 256, 0, st>>>(d_keys2.p, (int64_t)nt, d_child.p, d_pin.p, d_pleaf.p, d_rf.p, d_rl.p);
-        } else {
+        bool clustered = false;
+        if (cluster) {
             // PLOC rounds over the Morton-ordered leaf boxes.
             Scratch<uint32_t> d_node[2], d_cnt[2], d_nn, d_merge, d_alive, d_moff, d_apos, d_pchild, d_icount, d_ifirst,
                 d_lpos, d_order2;
@@ -849,10 +849,13 @@ int build_hierarchy(rt_ctx *ctx) {
             std::vector<uint32_t> round_base, round_count;
             uint32_t n = (uint32_t)nt, inner = 0;
             int cur = 0;
+            bool give_up = false;
             while (n > 1) {
-                if (round_base.size() > 100000) {
-                    set_error("hierarchy clustering did not terminate");
-                    return RT_ERR_STATE;
+                // Many coincident boxes merge one pair per round (every tie picks the lowest
+                // index): past kPlocMaxRounds the build falls back to the radix tree.
+                if (round_base.size() >= kPlocMaxRounds) {
+                    give_up = true;
+                    break;
                 }
                 const unsigned nb = (n + kPlocBlock - 1) / kPlocBlock;
                 k_ploc_nn<<<nb, kPlocBlock, 0, st>>>(d_clo[cur].p, d_chi[cur].p, n, d_nn.p);
@@ -880,25 +883,30 @@ int build_hierarchy(rt_ctx *ctx) {
                 n = n_new;
                 cur ^= 1;
             }
-            if (inner != ni) {
+            if (!give_up && inner != ni) {
                 set_error("hierarchy clustering left several roots");
                 return RT_ERR_STATE;
             }
-            const uint32_t zero = 0;
-            RT_CUDA_TRY(cudaMemcpyAsync(d_ifirst.p + (ni - 1), &zero, 4, cudaMemcpyHostToDevice, st));
-            for (size_t r = round_base.size(); r-- > 0;)
-                k_ploc_topdown<<<(round_count[r] + 255) / 256, 256, 0, st>>>(
-                    round_base[r], round_count[r], (uint32_t)ni, nt, d_pchild.p, d_icount.p, d_ifirst.p, d_lpos.p,
-                    status);
-            k_ploc_final<<<ib, 256, 0, st>>>((uint32_t)ni, nt, d_pchild.p, d_icount.p, d_ifirst.p, d_lpos.p,
-                                             d_child.p, d_pin.p, d_pleaf.p, d_rf.p, d_rl.p, status);
-            // Leaves, their boxes and the triangles again, in the depth-first leaf order (zeroed
-            // first: a malformed permutation would leave valid triangle ids, never stray ones).
-            RT_CUDA_TRY(cudaMemsetAsync(d_order2.p, 0, nt * sizeof(uint32_t), st));
-            k_scatter_order<<<tb, 256, 0, st>>>(d_vals2.p, d_lpos.p, nt, d_order2.p);
-            k_leaves<<<tb, 256, 0, st>>>(d_order2.p, nt, d_tlo.p, d_thi.p, ctx->d_verts.as<float>(), d_idx.p, eps,
-                                         d_slo.p, d_shi.p, ctx->d_tris.as<BvhTri>());
+            if (!give_up) {
+                const uint32_t zero = 0;
+                RT_CUDA_TRY(cudaMemcpyAsync(d_ifirst.p + (ni - 1), &zero, 4, cudaMemcpyHostToDevice, st));
+                for (size_t r = round_base.size(); r-- > 0;)
+                    k_ploc_topdown<<<(round_count[r] + 255) / 256, 256, 0, st>>>(
+                        round_base[r], round_count[r], (uint32_t)ni, nt, d_pchild.p, d_icount.p, d_ifirst.p, d_lpos.p,
+                        status);
+                k_ploc_final<<<ib, 256, 0, st>>>((uint32_t)ni, nt, d_pchild.p, d_icount.p, d_ifirst.p, d_lpos.p,
+                                                 d_child.p, d_pin.p, d_pleaf.p, d_rf.p, d_rl.p, status);
+                // Leaves, their boxes and the triangles again, in the depth-first leaf order (zeroed
+                // first: a malformed permutation would leave valid triangle ids, never stray ones).
+                RT_CUDA_TRY(cudaMemsetAsync(d_order2.p, 0, nt * sizeof(uint32_t), st));
+                k_scatter_order<<<tb, 256, 0, st>>>(d_vals2.p, d_lpos.p, nt, d_order2.p);
+                k_leaves<<<tb, 256, 0, st>>>(d_order2.p, nt, d_tlo.p, d_thi.p, ctx->d_verts.as<float>(), d_idx.p, eps,
+                                             d_slo.p, d_shi.p, ctx->d_tris.as<BvhTri>());
+                clustered = true;
+            }
         }
+        if (!clustered)
+            k_karras<<<ib, 256, 0, st>>>(d_keys2.p, (int64_t)nt, d_child.p, d_pin.p, d_pleaf.p, d_rf.p, d_rl.p);
         k_bottom_up<<<tb, 256, 0, st>>>(nt, d_child.p, d_pin.p, d_pleaf.p, d_rf.p, d_rl.p, d_slo.p, d_shi.p, d_ilo.p,
                                         d_ihi.p, d_cost.p, d_col.p, d_height.p, d_arr.p, d_cset.p, d_dec.p);
         uint8_t root_col = 0;
