@@ -56,6 +56,12 @@ WORKLOAD = ("raycaster: displaced icosphere, 1,310,720 triangles; 16,777,216 ray
             "directions uniform on the sphere; closest hit per step")
 
 
+def _config(triangles: int, rays: int, world: int) -> dict:
+    """The workload description both arms print (identical keys and values)."""
+    return {"workload": WORKLOAD, "triangles": triangles, "rays_per_gpu": rays,
+            "l2": "inputs larger than L2 (512 MB of rays per step)", "parallelism": f"replicas x{world}"}
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -206,6 +212,56 @@ def _pt_scene(kind):
     return S.cornell_scene(20261204) if kind == "cornell" else S.instanced_scene(20261206)
 
 
+def _profile_traffic(path: str) -> dict:
+    """Per-kernel-class figures from a committed ncu summary: lines
+    `traffic_bytes_per_launch <class>: <bytes>` (DRAM read + write of one launch, ncu) and
+    `launches_per_render <class>: <n>` (the launch list)."""
+    out = {}
+    try:
+        with open(os.path.join(ROOT, "profiles", path)) as f:
+            for ln in f:
+                for key in ("traffic_bytes_per_launch", "launches_per_render"):
+                    if ln.startswith(key + " "):
+                        k, v = ln[len(key) + 1:].split(":")
+                        out.setdefault(k.strip(), {})[key] = float(v)
+    except OSError:
+        pass
+    return out
+
+
+def pt_kernel_rooflines(st: dict, prof: dict) -> dict:
+    """Roofline of each path-tracer kernel class from a profiled render's per-kernel CUDA-event
+    times: achieved = the kernel's algorithmic DRAM bytes (the streams it must read and write,
+    counted per ray from the render's ray counts) / its time, against the measured HBM copy
+    bandwidth. Node, triangle, attribute and texel fetches are not counted: they are gathers
+    served mostly by L1/L2, which is what bounds these kernels.
+      trace  (k_trace_batch): per path ray 32 B ray + 4 B path id + 4 B job id + 16 B hit
+      shade  (k_shade): per shaded ray 32 B ray + 4 B path id + 16 B hit + 2 x 16 B path
+             throughput and radiance + 4 B job + 8 B pixel/sample + 8 B screen position read,
+             2 x 16 B written; + 36 B per next ray and 48 B per shadow ray queued
+      shadow (k_shadow): per shadow ray 32 B ray + 16 B contribution + 16 B radiance read and
+             written"""
+    peak, kind = _peaks()
+    rays = st["primary_rays"] + st["bounce_rays"]
+    algo = {"trace": 56 * rays, "shade": 136 * rays + 36 * st["bounce_rays"] + 48 * st["shadow_rays"],
+            "shadow": 80 * st["shadow_rays"]}
+    total_ms = sum(st["kernel_ms"].values())
+    out = {}
+    for k, b in algo.items():
+        ms = st["kernel_ms"][k]
+        if ms <= 0:
+            continue
+        gbs = b / (ms * 1e-3) / 1e9
+        p = prof.get(k, {})
+        n = int(p.get("launches_per_render", 0)) or None
+        tr = p.get("traffic_bytes_per_launch")
+        out[k] = {"ms": round(ms, 3), "share": round(ms / total_ms, 3), "launches": n,
+                  "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4),
+                  "peak_kind": kind, "bound": "hbm", "algorithmic_bytes": int(b),
+                  "traffic": tr, "dram_gbs": round(tr * n / (ms * 1e-3) / 1e9, 1) if tr and n else None}
+    return out
+
+
 def run_pathtracer(name, steps, cpu: bool):
     """One path-tracer configuration: GPU Mrays/s (device time inside pt_render), e2e with a
     host image, and the C restatement on host cores at `cpu spp` (cost is linear in spp)."""
@@ -233,12 +289,19 @@ def run_pathtracer(name, steps, cpu: bool):
     tr.render(cam, spp, depth, host, seed=99, mode=mode)
     e2e_s = time.perf_counter() - t0
     e2e_rays = tr.last_stats()["rays"]
+    # per-kernel times: one more render with the kernels launched directly, events between them
+    img.zero_()
+    tr.render(cam, spp, depth, img, seed=2, mode=mode, profile=True)
+    pst = tr.last_stats()
+    kernels = pt_kernel_rooflines(pst, _profile_traffic(f"pathtracer_{name}.txt"))
     out = {"workload": f"{kind}: {sc.triangle_count} triangles, {len(sc.objects)} objects, {w}x{h}, {spp} spp, "
                        f"depth {depth}, {'extended' if mode else 'reference'} estimator",
            "value": round(rays / (dev_ms * 1e3), 1), "unit": "Mrays/s", "ms_per_render": round(dev_ms / steps, 2),
            "rays_per_render": rays // steps, "e2e": {"value": round(e2e_rays / e2e_s / 1e6, 1), "unit": "Mrays/s",
                                                       "s_per_render": round(e2e_s, 3)},
-           "scene_upload_and_build_s": round(commit_s, 2)}
+           "scene_upload_and_build_s": round(commit_s, 2),
+           "roofline": dict(kernels.get("trace", {}), kernel="k_trace_batch"), "kernels": kernels,
+           "profiled_render_ms": round(pst["device_ms"], 2)}
     if cpu:
         from oracle import oracle as O
 
@@ -288,6 +351,8 @@ def run_batch(cpu: bool, tune: bool = True):
     st = br.render(jobs, tuning=tuning)
     torch.cuda.synchronize()
     batch_s = time.perf_counter() - t0
+    pst = br.render(jobs, tuning=tuning, profile=True)  # per-kernel times (kernels launched directly)
+    kernels = pt_kernel_rooflines(pst, _profile_traffic("pathtracer_batch_64.txt"))
     seq_ms, seq_rays = 0.0, 0
     t0 = time.perf_counter()
     for j in jobs:
@@ -304,7 +369,9 @@ def run_batch(cpu: bool, tune: bool = True):
            "batch_device_ms": round(st["device_ms"], 1), "batch_wall_s": round(batch_s, 3),
            "sequential_device_ms": round(seq_ms, 1), "sequential_wall_s": round(seq_s, 3),
            "speedup_vs_sequential": round(seq_s / batch_s, 2), "rays": st["rays"], "tuning": tuning,
-           "autotune_s": round(tune_s, 1), "scene_uploads_s": round(upload_s, 2)}
+           "autotune_s": round(tune_s, 1), "scene_uploads_s": round(upload_s, 2),
+           "roofline": dict(kernels.get("trace", {}), kernel="k_trace_batch"), "kernels": kernels,
+           "profiled_render_ms": round(pst["device_ms"], 1)}
     if cpu:
         from oracle import oracle as O
 
@@ -345,32 +412,56 @@ def _events_ms(fn, iters):
     return e0.elapsed_time(e1) / iters
 
 
+# The learned denoiser's protocol (scaled down from 20k 512^2 crops with 1024-spp targets:
+# the whole measurement has to fit in a bench run of a few minutes).
+DN_TRAIN_SCENES = (20261208, 20261209, 20261211, 20261212)  # seeded scenes of the large workload's type
+DN_TRAIN_VIEWS = 32  # views per scene, 256 x 256
+DN_TRAIN_SPP = (64, 256, 1024, 4096)  # input sample counts, cycled over the views
+DN_TRAIN_STEPS = 6000  # Adam steps of 16 random 128^2 crops
+DN_EVAL_SCENE = 20261210  # held out
+DN_EVAL_SIZE = (1920, 1080)
+DN_TRUTH_SPP = 16384  # double-precision accumulation
+DN_LEVELS = (64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384)
+
+
+def _dn_target_spp(spp_in: int) -> int:
+    """Target sample count for an input of spp_in samples: an independent render with at
+    least 4x the samples, 1024 to 4096 (the loss is unbiased for noisy targets)."""
+    return int(min(max(4 * spp_in, 1024), 4096))
+
+
 def run_denoiser(cpu: bool):
-    """The learned denoiser: trained here on path-tracer pairs (C3-type seeded scenes,
-    128^2 views, 4-64 spp inputs with first-hit features, 512-spp double-precision
-    targets), then (1) inference throughput at 1920x1080 and training-step throughput at
-    8 x 256^2 against the BF16 tensor peak, and (2) plain path tracing vs path tracing +
-    denoiser on a held-out scene at 480x270, relative RMSE against a 4096-spp
-    double-precision render, and the time each needs to reach given error levels."""
+    """The learned denoiser: trained here on path-tracer pairs (scenes of the large
+    workload's type, 256^2 views, 64-4096-spp inputs with first-hit features and the standard
+    error, independent 1024-4096-spp double-precision targets), then (1) inference
+    throughput at 1920x1080 and training-step throughput at 8 x 256^2 against the BF16
+    tensor peak, and (2) plain path tracing vs path tracing + denoiser on a held-out scene at
+    1920x1080: relative RMSE against a 16,384-spp double-precision render as the sample
+    count doubles, and the time each needs to reach given error levels."""
     import torch
 
     import rendu_gb300 as R
     from rendu_gb300 import denoiser as D
     from rendu_gb300 import scenes as S
 
-    sc = S.denoiser_scene(20261208)
-    tr = R.PathTracer(sc)
     t0 = time.perf_counter()
-    feats, targets = D.render_pairs(tr, S.random_cameras(20261208, 48), 128, 128, spp_in=[4, 8, 16, 32, 64],
-                                    spp_ref=512, seed=1)
+    feats, targets = [], []
+    for k, seed in enumerate(DN_TRAIN_SCENES):
+        tr = R.PathTracer(S.denoiser_scene(seed))
+        f, t = D.render_pairs(tr, S.random_cameras(seed, DN_TRAIN_VIEWS), 256, 256, spp_in=list(DN_TRAIN_SPP),
+                              spp_ref=_dn_target_spp, seed=1000 * k)
+        feats.append(f)
+        targets.append(t)
+        tr.close()
+    feats, targets = torch.cat(feats), torch.cat(targets)
     torch.cuda.synchronize()
     data_s = time.perf_counter() - t0
     net = D.Denoiser(seed=1)
-    steps = 4000
     t0 = time.perf_counter()
-    losses = D.train(net, feats, targets, steps, batch=8, crop=64, lr=2e-3, log_every=1000)
+    losses = D.train(net, feats, targets, DN_TRAIN_STEPS, batch=16, crop=128, lr=1e-3, log_every=1000)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
+    del feats, targets
 
     # ---- throughput -----------------------------------------------------------------------
     peak, peak_kind = _bf16_peak()
@@ -379,75 +470,55 @@ def run_denoiser(cpu: bool):
     for _ in range(3):
         net.denoise(x, o)
     inf_ms = _events_ms(lambda: net.denoise(x, o), 20)
-    inf_flop = net.flops(1080, 1920)
+    inf_flop = net.flops(1080, 1920, channels=(D.INPUT_CHANNELS, 3))  # channels that carry data
     fb = torch.rand((8, 256, 256, D.FEATURES), device="cuda")
     tb = torch.rand((8, 256, 256, 3), device="cuda")
     snap = net.get_params()
     for _ in range(3):
         net.train_step(fb, tb, 0.0, read_loss=False)
     tr_ms = _events_ms(lambda: net.train_step(fb, tb, 0.0, read_loss=False), 20)
-    tr_flop = 3 * net.flops(256, 256, 8)
+    tr_flop = 3 * net.flops(256, 256, 8, channels=(D.INPUT_CHANNELS, 3))
     net.set_params(snap)
+    del x, o, fb, tb
 
-    # ---- quality at equal time ------------------------------------------------------------
-    sc2 = S.denoiser_scene(20261210)
-    tr2 = R.PathTracer(sc2)
-    cam = S.random_cameras(20261210, 1, ratio=480 / 270)[0]
-    w, h = 480, 270
-    gt = torch.zeros((h, w, 3), device="cuda")
-    tr2.render(cam, 4096, 5, gt, seed=7, mode=1, fp64=True)
-    gt_np = gt.cpu().numpy()
-    plain, den = [], []
-    img = torch.zeros((h, w, 3), device="cuda")
-    aov = torch.zeros((h, w, 7), device="cuda")
-    for spp in (4, 16, 64, 256, 1024):
-        img.zero_()
-        tr2.render(cam, spp, 5, img, seed=100 + spp, mode=1)
-        plain.append({"spp": spp, "s": tr2.last_stats()["device_ms"] / 1e3,
-                      "rel_rmse": D.rel_rmse(img.cpu().numpy(), gt_np)})
-    for spp in (4, 16, 64):
-        img.zero_()
-        tr2.render(cam, spp, 5, img, seed=200 + spp, mode=1, aov=aov)
-        render_s = tr2.last_stats()["device_ms"] / 1e3
-        f = torch.cat([img, aov], -1).unsqueeze(0).contiguous()
-        out = torch.empty((1, h, w, 3), device="cuda")
-        net.denoise(f, out)
-        dn_ms = _events_ms(lambda: net.denoise(f, out), 5)
-        den.append({"spp": spp, "s": render_s + dn_ms / 1e3, "denoise_ms": round(dn_ms, 3),
-                    "rel_rmse": D.rel_rmse(out[0].cpu().numpy(), gt_np)})
-
-    def time_to(curve, thr):
-        """Seconds to reach rel-RMSE thr, interpolated log-log between measured points (None
-        when no measured point reaches it)."""
-        pts = sorted((p["s"], p["rel_rmse"]) for p in curve)
-        for (t0_, e0_), (t1_, e1_) in zip(pts, pts[1:]):
-            if e0_ > thr >= e1_:
-                a = (np.log(thr) - np.log(e0_)) / (np.log(e1_) - np.log(e0_))
-                return float(np.exp(np.log(t0_) + a * (np.log(t1_) - np.log(t0_))))
-        return pts[0][0] if pts[0][1] <= thr else None
-
+    # ---- quality on a held-out scene at 1080p ----------------------------------------------
+    w, h = DN_EVAL_SIZE
+    tr2 = R.PathTracer(S.denoiser_scene(DN_EVAL_SCENE))
+    cam = S.random_cameras(DN_EVAL_SCENE, 1, ratio=w / h)[0]
+    t0 = time.perf_counter()
+    truth = torch.zeros((h, w, 3), device="cuda")
+    tr2.render(dict(cam, ratio=w / h), DN_TRUTH_SPP, 5, truth, seed=7, mode=1, fp64=True)
+    truth_s = tr2.last_stats()["device_ms"] / 1e3
+    curve = D.progressive_curves(tr2, cam, w, h, DN_LEVELS, truth, denoiser=net, seed=100)
+    eval_s = time.perf_counter() - t0
+    tr2.close()
+    plain = [(p["render_s"], p["plain"]) for p in curve]
+    den = [(p["render_s"] + p["denoise_ms"] / 1e3, p["denoised"]) for p in curve]
     levels = {}
-    for thr in (0.3, 0.2, 0.1, 0.05, 0.01):
-        tp, td = time_to(plain, thr), time_to(den, thr)
+    for thr in (0.1, 0.05, 0.02, 0.01):
+        tp, td = D.time_to(plain, thr), D.time_to(den, thr)
         levels[str(thr)] = {"plain_s": tp and round(tp, 4), "denoised_s": td and round(td, 4),
-                            "speedup": round(tp / td, 1) if tp and td else None}
-    for p in plain + den:
-        p["s"] = round(p["s"], 4)
-        p["rel_rmse"] = round(p["rel_rmse"], 4)
+                            "speedup": round(tp / td, 2) if tp and td else None}
     inf_tflops = inf_flop / inf_ms / 1e9
     out = {"workload": "5-level U-Net (32-128 channels, 3x3 conv, BF16 activations, FP32 accumulation); "
                        "inference 1920x1080, training 8 x 256^2",
            "value": round(inf_tflops, 1), "unit": "TFLOP/s (inference, 1920x1080)",
            "inference_ms_1080p": round(inf_ms, 3), "inference_gflop": round(inf_flop / 1e9, 1),
+           "inference_gflop_padded": round(net.flops(1080, 1920) / 1e9, 1),
            "train_step_ms_8x256": round(tr_ms, 3), "train_tflops": round(tr_flop / tr_ms / 1e9, 1),
            "roofline": {"bound": "tensor", "achieved": round(inf_tflops, 1), "peak": peak, "unit": "TFLOP/s",
                         "frac": round(inf_tflops / peak, 4), "peak_kind": peak_kind, "traffic": None},
-           "training": {"pairs": int(feats.shape[0]), "input_spp": [4, 8, 16, 32, 64], "target_spp": 512,
-                        "steps": steps, "batch": "8 x 64^2 crops", "data_s": round(data_s, 2),
-                        "train_s": round(train_s, 2), "losses": [(s_, round(l_, 5)) for s_, l_ in losses]},
+           "training": {"scenes": len(DN_TRAIN_SCENES), "views": len(DN_TRAIN_SCENES) * DN_TRAIN_VIEWS,
+                        "view_size": "256x256", "input_spp": list(DN_TRAIN_SPP),
+                        "target_spp": [_dn_target_spp(s_) for s_ in DN_TRAIN_SPP], "steps": DN_TRAIN_STEPS,
+                        "batch": "16 x 128^2 crops", "loss": "relative squared error (eps 0.01)",
+                        "data_s": round(data_s, 2), "train_s": round(train_s, 2),
+                        "losses": [(s_, round(l_, 6)) for s_, l_ in losses]},
            "quality": {"view": f"held-out scene, {w}x{h}, extended estimator, depth 5",
-                       "ground_truth": "4096 spp, double-precision accumulation", "plain": plain, "denoised": den,
-                       "time_to_rel_rmse": levels}}
+                       "ground_truth": f"{DN_TRUTH_SPP} spp, double-precision accumulation ({truth_s:.1f} s)",
+                       "curve": [{k_: (round(v_, 5) if isinstance(v_, float) else v_) for k_, v_ in p.items()}
+                                 for p in curve],
+                       "time_to_rel_rmse": levels, "eval_s": round(eval_s, 1)}}
     return out
 
 
@@ -488,7 +559,7 @@ def run_reference(args):
         "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * sum(times) / len(times), 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "triangles": mesh.triangle_count, "rays": len(rays)},
+        "config": _config(mesh.triangle_count, len(rays), args.gpus),
         "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": f"{m} contiguous rays of the 16,777,216-ray set per step"},
         "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -510,8 +581,10 @@ def main():
                     help="only two 1920x1080 denoiser inferences and one 8 x 256^2 training step (for ncu captures)")
     ap.add_argument("--profile-run", action="store_true",
                     help="only one closest-hit and one any-hit launch over the workload (for ncu captures)")
-    ap.add_argument("--profile-pt", default=None, choices=list(PT_CONFIGS),
+    ap.add_argument("--profile-pt", default=None, choices=list(PT_CONFIGS) + ["batch_64"],
                     help="only one render of the given path-tracer configuration (for ncu captures)")
+    ap.add_argument("--pt-size", default=None,
+                    help="WxH: the --profile-pt render at another resolution (small ncu captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
@@ -545,12 +618,29 @@ def main():
         from rendu_gb300 import build as B
 
         B.build()
+        if args.profile_pt == "batch_64":
+            from rendu_gb300 import scenes as S
+
+            wl = S.batch_workload()
+            tracers = [R.PathTracer(j["scene"]) for j in wl]
+            jobs = [{"tracer": t, "camera": dict(j["scene"].camera, ratio=1.0), "samples": j["samples"],
+                     "depth": j["depth"], "seed": j["seed"],
+                     "image": torch.zeros((j["height"], j["width"], 3), dtype=torch.float32, device="cuda")}
+                    for j, t in zip(wl, tracers)]
+            st = R.BatchRenderer(0).render(jobs)
+            torch.cuda.synchronize()
+            print(json.dumps({"profile_pt": "batch_64", **{k: v for k, v in st.items() if k != "kernel_ms"}}))
+            return
         kind, w, h, spp, depth, _, mode = PT_CONFIGS[args.profile_pt]
+        if args.pt_size:
+            w, h = (int(v) for v in args.pt_size.split("x"))
         sc = _pt_scene(kind)
         img = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
         tr = R.PathTracer(sc)
         tr.render(dict(sc.camera, ratio=w / h), spp, depth, img, seed=1, mode=mode)
-        print(json.dumps({"profile_pt": args.profile_pt, **tr.last_stats()}))
+        st = tr.last_stats()
+        print(json.dumps({"profile_pt": args.profile_pt, "size": [w, h],
+                          **{k: v for k, v in st.items() if k != "kernel_ms"}}))
         return
 
     import torch
@@ -625,6 +715,16 @@ def main():
         rc.intersect_batch(host_rays, out=host_hits)
     _sync_all(dist, torch)
     e2e_value = _job_rate(dist, torch, n * args.steps, time.perf_counter() - t0) / 1e6
+    # the same with pageable host buffers (plain numpy arrays, as a C++ caller's std::vector)
+    pg_rays = np.array(host_rays, copy=True)
+    pg_hits = np.empty(n, R.HIT_DTYPE)
+    rc.intersect_batch(pg_rays, out=pg_hits)
+    _sync_all(dist, torch)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rc.intersect_batch(pg_rays, out=pg_hits)
+    _sync_all(dist, torch)
+    e2e_pageable = _job_rate(dist, torch, n * args.steps, time.perf_counter() - t0) / 1e6
 
     # ---- algorithmic bytes per ray (visit counts on a 1M-ray sample) -------------------
     nv, nt = rc.count_visits(rays[: 1 << 20])
@@ -649,12 +749,12 @@ def main():
             "warmup": args.warmup, "ms_per_step": round(1000 * t_closest / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "triangles": mesh.triangle_count, "rays_per_gpu": n,
-                       "l2": "inputs larger than L2 (512 MB of rays per step)", "parallelism": f"replicas x{world}"},
+            "config": _config(mesh.triangle_count, n, world),
             "any_hit": {"value": round(any_value, 2), "unit": "Mrays/s",
                         "ms_per_step": round(1000 * t_any / args.steps, 4)},
             "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s",
-                    "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 16},
+                    "h2d_bytes_per_step": n * 32, "d2h_bytes_per_step": n * 16, "host_memory": "pinned",
+                    "pageable": {"value": round(e2e_pageable, 2), "unit": "Mrays/s"}},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_kind": peak_kind, "bytes_per_ray": round(bytes_per_ray, 1),

@@ -110,7 +110,10 @@ RT_API int rt_update_hierarchy(rt_ctx *ctx);
 
 /* Closest hit for n rays. Replaces Raycaster::intersects(origin, direction, mini, maxi)
  * (Raycaster.cpp:144-185) for a batch. Ties at exactly equal distance go to the smaller
- * prim id (the reference keeps the first found in its own traversal order). */
+ * prim id (the reference keeps the first found in its own traversal order). With host
+ * buffers the call reports device-side failures itself; with RT_FLAG_DEVICE_PTRS it returns
+ * before the kernel has run, and rt_get_status reports them (as for rt_intersect_any,
+ * rt_visible and rt_count_visits). */
 RT_API int rt_intersect(rt_ctx *ctx, const rt_ray *rays, size_t n, rt_hit *hits, void *stream, uint32_t flags);
 
 /* Occlusion for n rays: occluded[i] = 1 if any triangle is hit inside (tmin, tmax).
@@ -131,16 +134,44 @@ RT_API int rt_visible(rt_ctx *ctx, const float *segs, size_t n, uint8_t *visible
  * No counterpart in the reference (its Raycaster::visible is a single CPU query).
  * segs (n x 6 floats) and visible (n bytes) are DEVICE pointers; the work is ordered on
  * `stream` (NULL = CUDA default stream) and the call returns without waiting. The call
- * allocates nothing: its scratch (converted rays, fetch counter, status word) is one
- * static device array of 8 MiB + 256 B that every GPU loading the library holds until
- * exit, so n must not exceed RT_NOALLOC_MAX_SEGMENTS (RT_ERR_ARG otherwise). All calls
- * share that array: calls that overlap on the GPU race and must be serialised by the
- * caller. The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress, once per device); make it before any stream capture. */
+ * allocates nothing: its scratch (converted rays, fetch counter) is one static device
+ * array of 8 MiB + 256 B that every GPU loading the library holds until exit, so n must not
+ * exceed RT_NOALLOC_MAX_SEGMENTS (RT_ERR_ARG otherwise). All calls share that array: calls
+ * that overlap on the GPU race and must be serialised by the caller. The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress, once per device); make
+ * it before any stream capture. A traversal stack overflow (only possible under
+ * rt_set_traversal_stack) is recorded in the context's status word for asynchronous calls:
+ * rt_get_status(ctx, stream, ...) reports it as RT_ERR_OVERFLOW. */
 RT_API int rt_visible_noalloc(rt_ctx *ctx, const float *segs, size_t n, uint8_t *visible, void *stream);
 
 /* Map a global triangle id to (meshId, localId) as stored in Raycaster::Hit. */
 RT_API int rt_prim_info(const rt_ctx *ctx, uint32_t prim, uint32_t *mesh_id, uint32_t *local_id);
+
+/* The Raycaster::Hit fields meshId and localId (Raycaster.hpp:16-30, set at
+ * Raycaster.cpp:177-179) for a batch of closest hits from rt_intersect: mesh_ids[i] = the
+ * addMesh index of the hit triangle's mesh, local_ids[i] = 3 x its triangle index inside that
+ * mesh (the first index of the triangle in the mesh's own index buffer); both RT_NO_HIT on a
+ * miss. Either output may be NULL. Host buffers by default; device buffers with
+ * RT_FLAG_DEVICE_PTRS (ordered on `stream`, returns without waiting). */
+RT_API int rt_hit_info(rt_ctx *ctx, const rt_hit *hits, size_t n, uint32_t *mesh_ids, uint32_t *local_ids,
+                       void *stream, uint32_t flags);
+
+/* Failures the device found during asynchronous calls. The reference logs and returns
+ * (PathTracer.cpp:162-168); here host-buffer calls return RT_ERR_OVERFLOW / RT_ERR_TIMEOUT
+ * themselves, while calls that return without waiting (RT_FLAG_DEVICE_PTRS queries on the
+ * caller's stream, rt_visible_noalloc) record them in a status word of the context. This
+ * call waits for `stream`, returns RT_ERR_OVERFLOW (a traversal stack overflowed: the
+ * affected rays ended early) or RT_ERR_TIMEOUT (a bounded device loop gave up) if any such
+ * call since the last rt_get_status failed, else RT_OK, puts the raw bits in *word (may be
+ * NULL) and clears them. */
+RT_API int rt_get_status(rt_ctx *ctx, void *stream, uint32_t *word);
+
+/* Cap the traversal stack of the queries at `entries` (1..256; 0 = automatic, the exact
+ * bound of the current hierarchy, which never overflows). The queries then run the smallest
+ * compiled stack (2, 64 or 256 entries) that holds the cap; rays that need more stop early
+ * and the call reports RT_ERR_OVERFLOW. A diagnostic: it lets tests and callers exercise the
+ * overflow path, which the automatic bound never reaches. */
+RT_API int rt_set_traversal_stack(rt_ctx *ctx, uint32_t entries);
 
 /* Statistics of the current hierarchy. */
 RT_API int rt_get_stats(const rt_ctx *ctx, rt_stats *out);
@@ -235,6 +266,14 @@ typedef struct pt_camera_desc {
     float ratio; /* width / height */
 } pt_camera_desc;
 
+/* Kernel classes of pt_render_stats.kernel_ms. */
+#define PT_KERNEL_RAYGEN 0     /* wave set-up and camera rays                              */
+#define PT_KERNEL_TRACE 1      /* closest-hit traversal of the path rays                   */
+#define PT_KERNEL_SHADE 2      /* hit shading, light sampling, next rays                   */
+#define PT_KERNEL_SHADOW 3     /* shadow rays (any hit, or the walk through cut-outs)       */
+#define PT_KERNEL_ACCUMULATE 4 /* per-pixel accumulation of the wave's samples             */
+#define PT_KERNEL_KINDS 5
+
 /* Per-render counters. rays = primary + bounce + shadow rays cast. */
 typedef struct pt_render_stats {
     uint64_t primary_rays;
@@ -242,6 +281,9 @@ typedef struct pt_render_stats {
     uint64_t shadow_rays;
     uint64_t paths;
     float device_ms;
+    float kernel_ms[PT_KERNEL_KINDS]; /* device time of each kernel class, measured with CUDA
+                                         events between the launches when the render ran with
+                                         pt_render_options.profile (else 0)                  */
 } pt_render_stats;
 
 typedef struct pt_scene pt_scene;
@@ -299,10 +341,27 @@ typedef struct pt_render_options {
                       <= 0 disables it                                                            */
     int32_t accum_fp64; /* accumulate the samples of each pixel in double precision (for
                            high-spp reference images); the image itself stays float       */
-    float *aov;    /* optional feature buffer, width x height x 7 floats (host or device like
+    float *aov;    /* optional feature buffer, width x height x 8 floats (host or device like
                       the image): first-hit albedo (rgb), shading normal (xyz), distance,
-                      averaged over the pixel's samples; overwritten, not accumulated     */
+                      averaged over the pixel's samples, and the standard error of the
+                      pixel's mean luminance (Rec. 709 weights, of the clamped samples:
+                      sqrt((E[L^2] - E[L]^2) / spp)); overwritten, not accumulated        */
+    uint32_t ranks; /* pixel split over cooperating processes (one per GPU): 0 or 1 renders
+                       every pixel; otherwise the image's pixels (row-major) form tiles of
+                       PT_RANK_TILE_PIXELS and tile k belongs to rank k % ranks. This call
+                       renders the tiles of `rank` only, as pt_render would, and sets every
+                       component of every other pixel (and its aov entries) to 0, so that
+                       the element-wise sum of all ranks' images is the whole render, bit
+                       for bit. The reference splits rows over threads instead
+                       (System::forParallel, System.hpp:72-104, PathTracer.cpp:186). */
+    uint32_t rank;  /* this process's rank, < ranks                                       */
+    int32_t profile; /* nonzero: launch every wave's kernels directly instead of replaying the
+                        captured CUDA graph, with CUDA events between them, and report the
+                        time of each kernel class in pt_render_stats.kernel_ms (slower)    */
 } pt_render_options;
+
+/* Pixels per tile of the pt_render_options rank split. */
+#define PT_RANK_TILE_PIXELS 4096
 
 /* Environment map for PT_MODE_EXTENDED: an equirectangular float image (texture id from
  * pt_scene_add_texture; u = phi / 2pi with phi = atan2(z, x), v = theta / pi from +y),
@@ -419,13 +478,18 @@ RT_API rt_ctx *pt_scene_raycaster(pt_scene *scene);
  * max pooling down, nearest 2x upsampling + skip concatenation up, a final 3x3 convolution to
  * 16 channels of which the first 3 are a correction of log(1 + radiance). Activations are
  * NHWC BF16, accumulation FP32 (tensor-core implicit GEMMs); master weights FP32.
- * Features: per pixel DN_FEATURES floats {radiance rgb, albedo rgb, normal xyz, distance}
- * (pt_render's image + its feature buffer). Images of any size are padded to multiples of
- * 16 for inference; training crops must be multiples of 16.
+ * Features: per pixel DN_FEATURES floats {radiance rgb, albedo rgb, normal xyz, distance,
+ * standard error of the mean luminance} (pt_render's image + its 8-float feature buffer).
+ * Output: max(exp(log(1 + radiance) + correction) - 1, 0), so a zero correction returns the
+ * input radiance exactly. Images of any size are padded to multiples of 16 for inference;
+ * training crops must be multiples of 16.
  * Parameters (flat FP32): for each layer in dn_layer order, weights [3][3][cin][cout]
  * (tap-major: tap = 3 dy + dx over the 3x3 window, then input, then output channel)
- * followed by bias [cout]. Loss: mean L1 distance in log(1 + radiance). Optimiser: Adam. */
-#define DN_FEATURES 10
+ * followed by bias [cout]. Loss: the relative squared error ((x - t) / (x' + 0.01))^2 of
+ * the output x against the target t, averaged over pixels and channels, x' being x held
+ * constant (the relative RMSE the output is judged by; unbiased for noisy targets).
+ * Optimiser: Adam. */
+#define DN_FEATURES 11
 typedef struct dn_net dn_net;
 
 typedef struct dn_layer {

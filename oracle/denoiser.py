@@ -24,7 +24,7 @@ import numpy as np
 LEVEL_CHANNELS = (32, 48, 64, 96, 128)
 IN_CHANNELS = 16
 OUT_CHANNELS = 16
-FEATURES = 10
+FEATURES = 11
 
 
 def bf16_round(a) -> np.ndarray:
@@ -103,8 +103,10 @@ def pool2_back(x, y, gy):
 
 
 def prepare(features):
-    """Features {radiance rgb, albedo rgb, normal xyz, distance} -> 16 input channels:
-    log(1 + radiance), albedo, normal / 2 + 1/2, distance / (1 + distance), zeros."""
+    """Features {radiance rgb, albedo rgb, normal xyz, distance, standard error} -> 16 input
+    channels: log(1 + radiance), albedo, normal / 2 + 1/2, distance / (1 + distance),
+    e / (1 + e) with the relative standard error e = se / (luminance + 0.01), log(1 + se),
+    zeros."""
     f = np.asarray(features, np.float32)
     out = np.zeros(f.shape[:-1] + (IN_CHANNELS,), np.float32)
     out[..., 0:3] = np.log1p(np.maximum(f[..., 0:3], 0.0))
@@ -112,7 +114,18 @@ def prepare(features):
     out[..., 6:9] = f[..., 6:9] * 0.5 + 0.5
     d = np.maximum(f[..., 9], 0.0)
     out[..., 9] = d / (1.0 + d)
+    se = np.maximum(f[..., 10], 0.0)
+    lum = np.maximum(0.2126 * f[..., 0] + 0.7152 * f[..., 1] + 0.0722 * f[..., 2], 0.0)
+    e = se / (lum + 0.01)
+    out[..., 10] = e / (1.0 + e)
+    out[..., 11] = np.log1p(se)
     return out
+
+
+def output(features, y):
+    """Radiance max(exp(log(1 + input) + y) - 1, 0) from the float32 input radiance."""
+    r = np.maximum(np.asarray(features, np.float64)[..., 0:3], 0.0)
+    return np.maximum(np.expm1(np.log1p(r) + np.asarray(y, np.float64)[..., 0:3]), 0.0)
 
 
 def pad16(features):
@@ -182,7 +195,7 @@ class UNet:
         return a if s1 is None else np.concatenate([a, acts[s1]], axis=-1)
 
     def forward(self, params, features, bf16=True):
-        """features (B, H, W, 10), H and W multiples of 16 -> (acts, output (B, H, W, 16)).
+        """features (B, H, W, 11), H and W multiples of 16 -> (acts, output (B, H, W, 16)).
         Activations are rounded to bfloat16 where the GPU stores them so; the output stays
         float32 (FP32 on the GPU)."""
         rnd = bf16_round if bf16 else (lambda a: np.asarray(a, np.float64))
@@ -203,22 +216,25 @@ class UNet:
         return acts, acts[self.ops[-1][4]]
 
     @staticmethod
-    def loss_and_grad(x_in, y, target):
-        """Mean L1 distance in log space between log(1 + noisy) + y[..., :3] and
-        log(1 + target); returns (loss, dL/dy)."""
-        d = np.asarray(x_in[..., :3], np.float64) + np.asarray(y[..., :3], np.float64) - \
-            np.log1p(np.maximum(np.asarray(target, np.float64), 0.0))
-        n = d.size
+    def loss_and_grad(features, y, target):
+        """Relative squared error mean(((x - t) / (x' + 0.01))^2) of the output
+        x = output(features, y) against the target t, x' = x held constant in the gradient;
+        returns (loss, dL/dy) with dL/dy = 2 (x - t) / (x' + 0.01)^2 (x + 1) where x > 0."""
+        x = output(features, y)
+        t = np.asarray(target, np.float64)
+        den = x + 0.01
+        q = (x - t) / den
+        n = q.size
         g = np.zeros(y.shape, np.float64)
-        g[..., :3] = np.sign(d) / n
-        return float(np.abs(d).mean()), g
+        g[..., :3] = np.where(x > 0.0, 2.0 * q / den * (x + 1.0), 0.0) / n
+        return float((q * q).mean()), g
 
     def backward(self, params, features, target, bf16=True):
         """(loss, flat gradient) of one batch, following the GPU's order of operations."""
         rnd = bf16_round if bf16 else (lambda a: np.asarray(a, np.float64))
         params = np.asarray(params, np.float32)
         acts, y = self.forward(params, features, bf16)
-        loss, gy = self.loss_and_grad(acts[0], y, target)
+        loss, gy = self.loss_and_grad(features, y, target)
         grads = np.zeros(self.param_count, np.float64)
         g = {self.ops[-1][4]: gy}
         for op in reversed(self.ops):

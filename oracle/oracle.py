@@ -20,7 +20,6 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "liboracle_port.so")
 REF_LIB = os.path.join(HERE, "_ref", "libref_oracle.so")
-REF_ROOT_DEFAULT = "/root/reference"
 
 NO_HIT = 0xFFFFFFFF
 HIT_DTYPE = np.dtype([("t", "<f4"), ("u", "<f4"), ("v", "<f4"), ("prim", "<u4")])
@@ -37,10 +36,21 @@ def build_port(quiet: bool = True) -> str:
     return PORT_LIB
 
 
+def reference_root() -> str:
+    """Where the reference tree is read from: $RENDU_REFERENCE_ROOT, else the build recipe's
+    REF_ROOT (oracle/Makefile is the one place that names a location)."""
+    root = os.environ.get("RENDU_REFERENCE_ROOT")
+    if root:
+        return root
+    r = subprocess.run(["make", "-s", "--no-print-directory", "-C", HERE, "print-ref-root"], capture_output=True,
+                       text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
+
 def build_ref(quiet: bool = True, jobs: int = 8) -> str | None:
     """Compile the reference oracle when the reference tree exists; None otherwise."""
-    root = os.environ.get("RENDU_REFERENCE_ROOT", REF_ROOT_DEFAULT)
-    if not os.path.isdir(os.path.join(root, "src", "engine", "raycaster")):
+    root = reference_root()
+    if not root or not os.path.isdir(os.path.join(root, "src", "engine", "raycaster")):
         return None
     subprocess.run(["make", "-s", "-C", HERE, f"-j{jobs}", "ref", f"REF_ROOT={root}"], check=True,
                    capture_output=quiet)

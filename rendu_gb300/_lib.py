@@ -27,6 +27,7 @@ PT_BG_IMAGE = 1
 PT_BG_SKYBOX = 2
 PT_BG_ATMOSPHERE = 3
 RT_NO_HIT = 0xFFFFFFFF
+PT_RANK_TILE_PIXELS = 4096
 
 _STATUS_NAMES = {1: "RT_ERR_ARG", 2: "RT_ERR_OOM", 3: "RT_ERR_CUDA", 4: "RT_ERR_TIMEOUT", 5: "RT_ERR_STATE",
                  6: "RT_ERR_OVERFLOW"}
@@ -66,7 +67,8 @@ class pt_camera_desc(C.Structure):
 
 
 class pt_render_options(C.Structure):
-    _fields_ = [("mode", C.c_int32), ("clamp", C.c_float), ("accum_fp64", C.c_int32), ("aov", C.c_void_p)]
+    _fields_ = [("mode", C.c_int32), ("clamp", C.c_float), ("accum_fp64", C.c_int32), ("aov", C.c_void_p),
+                ("ranks", C.c_uint32), ("rank", C.c_uint32), ("profile", C.c_int32)]
 
 
 class pt_batch_job(C.Structure):
@@ -81,7 +83,7 @@ class pt_batch_tuning(C.Structure):
 
 class pt_render_stats(C.Structure):
     _fields_ = [("primary_rays", C.c_uint64), ("bounce_rays", C.c_uint64), ("shadow_rays", C.c_uint64),
-                ("paths", C.c_uint64), ("device_ms", C.c_float)]
+                ("paths", C.c_uint64), ("device_ms", C.c_float), ("kernel_ms", C.c_float * 5)]
 
 
 class dn_layer(C.Structure):
@@ -89,7 +91,7 @@ class dn_layer(C.Structure):
                 ("relu", C.c_int32), ("level", C.c_int32), ("weight_offset", C.c_uint64), ("bias_offset", C.c_uint64)]
 
 
-DN_FEATURES = 10
+DN_FEATURES = 11
 
 _lib = None
 _lock = threading.Lock()
@@ -104,6 +106,9 @@ _SIGS = {
     "rt_intersect_any": ([_VP, _VP, C.c_size_t, _VP, _VP, C.c_uint32], C.c_int),
     "rt_visible": ([_VP, _VP, C.c_size_t, _VP, _VP, C.c_uint32], C.c_int),
     "rt_prim_info": ([_VP, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)], C.c_int),
+    "rt_hit_info": ([_VP, _VP, C.c_size_t, _VP, _VP, _VP, C.c_uint32], C.c_int),
+    "rt_get_status": ([_VP, _VP, C.POINTER(C.c_uint32)], C.c_int),
+    "rt_set_traversal_stack": ([_VP, C.c_uint32], C.c_int),
     "rt_get_stats": ([_VP, C.POINTER(rt_stats)], C.c_int),
     "rt_count_visits": ([_VP, _VP, C.c_size_t, _VP, _VP, _VP, C.c_uint32], C.c_int),
     "rt_last_error": ([], C.c_char_p),

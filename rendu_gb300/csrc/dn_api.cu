@@ -274,7 +274,8 @@ int forward(dn_net *n, cudaStream_t st) {
 
 int backward(dn_net *n, const float *target, cudaStream_t st) {
     const int last = n->convs.back().out;
-    int r = l1_loss(n->bf(0), n->f(last), target, n->pixels(0), n->g(last), n->loss_partial.as<float>(), n->hyp(), st);
+    int r = relmse_loss(n->feat.as<float>(), n->f(last), target, n->pixels(0), n->g(last), n->loss_partial.as<float>(),
+                        n->hyp(), st);
     if (r != RT_OK) return r;
     float *grads = n->grads.as<float>();
     for (auto it = n->ops.rbegin(); it != n->ops.rend() && r == RT_OK; ++it) {
@@ -556,7 +557,8 @@ RT_API int dn_denoise(dn_net *n, const float *features, uint32_t width, uint32_t
     auto body = [&](cudaStream_t s) {
         int q = prepare(n->feat.as<float>(), B, H, W, (int)Hp, (int)Wp, n->bf(0), s);
         if (q == RT_OK) q = forward(n, s);
-        if (q == RT_OK) q = finish(n->bf(0), n->f(n->convs.back().out), B, H, W, (int)Hp, (int)Wp, n->out.as<float>(), s);
+        if (q == RT_OK)
+            q = finish(n->feat.as<float>(), n->f(n->convs.back().out), B, H, W, (int)Hp, (int)Wp, n->out.as<float>(), s);
         return q;
     };
     r = run_graph(n, n->g_infer, signature(n, H, W), body, st);

@@ -413,8 +413,9 @@ __global__ void k_split_grad4(const float *__restrict__ gin, int B, int H, int W
     *reinterpret_cast<float4 *>(g0 + p * c0 + c) = add4(add4(a, bb), add4(cc, d));
 }
 
-// Features {radiance rgb, albedo rgb, normal xyz, distance} -> 16 channels:
-// log(1 + radiance), albedo, normal / 2 + 1/2, distance / (1 + distance), zeros; padded
+// Features {radiance rgb, albedo rgb, normal xyz, distance, standard error} -> 16 channels:
+// log(1 + radiance), albedo, normal / 2 + 1/2, distance / (1 + distance), the relative
+// standard error e = se / (luminance + 0.01) as e / (1 + e), log(1 + se), zeros; padded
 // pixels replicate the nearest edge pixel.
 __global__ void k_prepare(const float *__restrict__ f, int B, int H, int W, int Hp, int Wp, bf16 *__restrict__ x) {
     const size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -424,7 +425,7 @@ __global__ void k_prepare(const float *__restrict__ f, int B, int H, int W, int 
     const size_t r = q / Wp;
     const int yp = (int)(r % Hp);
     const int b = (int)(r / Hp);
-    const float *s = f + (((size_t)b * H + min(yp, H - 1)) * W + min(xp, W - 1)) * 10;
+    const float *s = f + (((size_t)b * H + min(yp, H - 1)) * W + min(xp, W - 1)) * DN_FEATURES;
     float v[16];
 #pragma unroll
     for (int k = 0; k < 3; ++k) v[k] = log1pf(fmaxf(s[k], 0.0f));
@@ -434,8 +435,13 @@ __global__ void k_prepare(const float *__restrict__ f, int B, int H, int W, int 
     for (int k = 6; k < 9; ++k) v[k] = s[k] * 0.5f + 0.5f;
     const float d = fmaxf(s[9], 0.0f);
     v[9] = d / (1.0f + d);
+    const float se = fmaxf(s[10], 0.0f);
+    const float lum = fmaxf(0.2126f * s[0] + 0.7152f * s[1] + 0.0722f * s[2], 0.0f);
+    const float e = se / (lum + 0.01f);
+    v[10] = e / (1.0f + e);
+    v[11] = log1pf(se);
 #pragma unroll
-    for (int k = 10; k < 16; ++k) v[k] = 0.0f;
+    for (int k = 12; k < 16; ++k) v[k] = 0.0f;
     __nv_bfloat162 o[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) o[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
@@ -445,8 +451,11 @@ __global__ void k_prepare(const float *__restrict__ f, int B, int H, int W, int 
 }
 
 // radiance = max(exp(log(1 + input) + y) - 1, 0): the network predicts a correction of the
-// noisy input in log space.
-__global__ void k_finish(const bf16 *__restrict__ x, const float *__restrict__ y, int B, int H, int W, int Hp, int Wp,
+// noisy input in log space; the input is taken from the FP32 features, so that a zero
+// correction returns the input unchanged.
+__device__ __forceinline__ float dn_output(float in, float y) { return fmaxf(expm1f(log1pf(fmaxf(in, 0.0f)) + y), 0.0f); }
+
+__global__ void k_finish(const float *__restrict__ f, const float *__restrict__ y, int B, int H, int W, int Hp, int Wp,
                          float *__restrict__ out) {
     const size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     const size_t n = (size_t)B * H * W;
@@ -457,12 +466,16 @@ __global__ void k_finish(const bf16 *__restrict__ x, const float *__restrict__ y
     const int b = (int)(r / H);
     const size_t q = ((size_t)b * Hp + yy) * Wp + xx;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) out[o * 3 + k] = fmaxf(expm1f(__bfloat162float(x[q * 16 + k]) + y[q * 16 + k]), 0.0f);
+    for (int k = 0; k < 3; ++k) out[o * 3 + k] = dn_output(f[o * DN_FEATURES + k], y[q * 16 + k]);
 }
 
-// L1 loss in log space: mean over pixels and channels of |log(1+x) + y - log(1 + target)|.
-__global__ void k_l1(const bf16 *__restrict__ x, const float *__restrict__ y, const float *__restrict__ t, long P,
-                     float *__restrict__ gy, float *__restrict__ partial) {
+// Relative squared error, the measure the denoiser is judged by: mean over pixels and
+// channels of ((x - t) / (x' + 0.01))^2 with x = dn_output(input, y) and x' the same value
+// held constant (not differentiated), as in Noise2Noise's loss for Monte Carlo renders
+// (Lehtinen et al. 2018): unbiased for noisy targets, which may then be independent renders
+// of any sample count. dL/dy = 2 (x - t) / (x' + 0.01)^2 * (x + 1) where x > 0.
+__global__ void k_relmse(const float *__restrict__ f, const float *__restrict__ y, const float *__restrict__ t, long P,
+                         float *__restrict__ gy, float *__restrict__ partial) {
     __shared__ float red[256];
     const long p = blockIdx.x * (long)blockDim.x + threadIdx.x;
     float l = 0.0f;
@@ -472,9 +485,12 @@ __global__ void k_l1(const bf16 *__restrict__ x, const float *__restrict__ y, co
         for (int k = 0; k < 16; ++k) {
             float gk = 0.0f;
             if (k < 3) {
-                const float d = __bfloat162float(x[p * 16 + k]) + y[p * 16 + k] - log1pf(fmaxf(t[p * 3 + k], 0.0f));
-                l += fabsf(d);
-                gk = d > 0.0f ? inv : (d < 0.0f ? -inv : 0.0f);
+                const float x = dn_output(f[p * DN_FEATURES + k], y[p * 16 + k]);
+                const float den = x + 0.01f;
+                const float d = x - t[p * 3 + k];
+                const float q = d / den;
+                l += q * q;
+                gk = x > 0.0f ? 2.0f * q / den * (x + 1.0f) * inv : 0.0f;
             }
             gy[p * 16 + k] = gk;
         }
@@ -660,16 +676,16 @@ int prepare(const float *f, int B, int H, int W, int Hp, int Wp, bf16 *x, cudaSt
     return RT_OK;
 }
 
-int finish(const bf16 *x, const float *y, int B, int H, int W, int Hp, int Wp, float *out, cudaStream_t st) {
-    k_finish<<<blocks((size_t)B * H * W), 256, 0, st>>>(x, y, B, H, W, Hp, Wp, out);
+int finish(const float *f, const float *y, int B, int H, int W, int Hp, int Wp, float *out, cudaStream_t st) {
+    k_finish<<<blocks((size_t)B * H * W), 256, 0, st>>>(f, y, B, H, W, Hp, Wp, out);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
 
-int l1_loss(const bf16 *x, const float *y, const float *target, long P, float *gy, float *partial, Hyper *hyper,
-            cudaStream_t st) {
+int relmse_loss(const float *f, const float *y, const float *target, long P, float *gy, float *partial, Hyper *hyper,
+                cudaStream_t st) {
     const unsigned nb = blocks((size_t)P);
-    k_l1<<<nb, 256, 0, st>>>(x, y, target, P, gy, partial);
+    k_relmse<<<nb, 256, 0, st>>>(f, y, target, P, gy, partial);
     k_loss_total<<<1, 256, 0, st>>>(partial, (int)nb, 1.0f / (3.0f * (float)P), hyper);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;

@@ -79,13 +79,15 @@ int split_grad(const float *gin, int B, int H, int W, int c0, int up0, int c1, f
 // (partial: colsum_partial_floats(P, C) floats of scratch).
 int relu_grad_bias(float *g, const bf16 *y, long P, int C, bool relu, bf16 *gb, float *partial, float *db,
                    cudaStream_t st);
-// Features (B, H, W, 10) fp32 -> network input (B, Hp, Wp, 16) bf16, edge-replicated padding.
+// Features (B, H, W, DN_FEATURES) fp32 -> network input (B, Hp, Wp, 16) bf16, edge-replicated
+// padding.
 int prepare(const float *f, int B, int H, int W, int Hp, int Wp, bf16 *x, cudaStream_t st);
-// Network output (B, Hp, Wp, 16) fp32 + input log radiance -> radiance (B, H, W, 3).
-int finish(const bf16 *x, const float *y, int B, int H, int W, int Hp, int Wp, float *out, cudaStream_t st);
-// Loss in log space on the residual prediction; writes gy (P x 16) and hyper->loss.
-int l1_loss(const bf16 *x, const float *y, const float *target, long P, float *gy, float *partial, Hyper *hyper,
-            cudaStream_t st);
+// Network output (B, Hp, Wp, 16) fp32 + the features' radiance (B, H, W) -> radiance (B, H, W, 3).
+int finish(const float *f, const float *y, int B, int H, int W, int Hp, int Wp, float *out, cudaStream_t st);
+// Relative squared error of the output against the target (P pixels, features and output at
+// the same P); writes gy (P x 16) and hyper->loss.
+int relmse_loss(const float *f, const float *y, const float *target, long P, float *gy, float *partial, Hyper *hyper,
+                cudaStream_t st);
 // hyper->lr = lr, ordered on st (the value travels as a kernel argument: no host buffer).
 int set_learning_rate(Hyper *hyper, float lr, cudaStream_t st);
 // Adam on the FP32 parameters (the packed BF16 copies are refreshed by pack_all).

@@ -616,10 +616,15 @@ int pt_render_ex(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, ui
                width,      height,           components,
                opts ? opts->clamp : 5.0f,    opts ? opts->accum_fp64 : 0,
                opts ? opts->aov : nullptr};
+    if (opts && opts->ranks > 1) {
+        if (opts->rank >= opts->ranks) return arg_error("rank must be smaller than ranks");
+        js.ranks = opts->ranks;
+        js.rank = opts->rank;
+    }
     // One tile of every pixel per wave, as many samples per wave as ~8M paths allow.
     Tuning t{1u << 23, width * height, 1u << 30};
     if ((uint64_t)width * height > t.wave_paths) t.wave_paths = width * height;
-    r = s->engine->run({js}, mode, t, dev, st, &s->last);
+    r = s->engine->run({js}, mode, t, dev, st, &s->last, opts && opts->profile);
     return r;
 }
 
@@ -676,7 +681,7 @@ int pt_batch_render(pt_batch *b, const pt_batch_job *jobs, size_t n, const pt_re
     else load_tuning(nullptr, t);
     DeviceGuard g(b->device);
     const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
-    return b->engine->run(specs, mode, t, dev, static_cast<cudaStream_t>(stream), &b->last);
+    return b->engine->run(specs, mode, t, dev, static_cast<cudaStream_t>(stream), &b->last, opts && opts->profile);
 }
 
 int pt_batch_get_stats(const pt_batch *b, pt_render_stats *out) {

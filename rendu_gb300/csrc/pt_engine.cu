@@ -103,10 +103,48 @@ int WaveEngine::ensure_capacity(uint64_t cap, uint64_t accum_pixels, uint64_t nt
     if (aov) {
         grow(aov0_, cap_ * 16);
         grow(aov1_, cap_ * 16);
-        grow(aov_accum_, std::max<uint64_t>(accum_pixels, 1) * 28);
-        grow(aov_staging_, std::max<uint64_t>(accum_pixels, 1) * 28);
+        grow(aov_accum_, std::max<uint64_t>(accum_pixels, 1) * 4 * PT_AOV_ACCUM);
+        grow(aov_staging_, std::max<uint64_t>(accum_pixels, 1) * 4 * PT_AOV);
     }
     if (moved) ++generation_;
+    return r;
+}
+
+int WaveEngine::launch_wave(const PtWave &w, uint32_t depth, bool ext, bool shadow_a, bool shadow_b, bool big_stack,
+                            cudaStream_t cs, std::vector<cudaEvent_t> *marks, std::vector<int> *kinds) {
+    auto mark = [&](int kind) -> int {
+        if (!marks) return RT_OK;
+        cudaEvent_t e = nullptr;
+        RT_CUDA_TRY(cudaEventCreate(&e));
+        marks->push_back(e);
+        kinds->push_back(kind);
+        RT_CUDA_TRY(cudaEventRecord(e, cs));
+        return RT_OK;
+    };
+    int r = mark(-1);
+    if (r == RT_OK) r = pt_launch_wave_begin(w, cs);
+    if (r == RT_OK) r = pt_launch_raygen(w, cs);
+    if (r == RT_OK) r = mark(PT_KERNEL_RAYGEN);
+    int cur = 0;
+    for (uint32_t did = 0; r == RT_OK && did < depth; ++did) {
+        r = trace_closest_batch(w, cur, big_stack, cs);
+        if (r == RT_OK) r = mark(PT_KERNEL_TRACE);
+        // The queues shading appends to start empty: the next ray queue and both shadow queues.
+        if (r == RT_OK && (cudaMemsetAsync(&w.counters[cur ^ 1], 0, 4, cs) != cudaSuccess ||
+                           cudaMemsetAsync(&w.counters[2], 0, 8, cs) != cudaSuccess)) {
+            set_error("cudaMemsetAsync failed in the wave sequence");
+            r = RT_ERR_CUDA;
+        }
+        if (r == RT_OK) r = pt_launch_shade(w, cur, did, ext, cs);
+        if (r == RT_OK) r = mark(PT_KERNEL_SHADE);
+        if (r == RT_OK && shadow_a) r = pt_launch_shadow(w, 0, big_stack, cs);
+        if (r == RT_OK && shadow_b) r = pt_launch_shadow(w, 1, big_stack, cs);
+        if (r == RT_OK && (shadow_a || shadow_b)) r = mark(PT_KERNEL_SHADOW);
+        cur ^= 1;
+    }
+    if (r == RT_OK) r = pt_launch_accumulate(w, cs);
+    if (r == RT_OK) r = pt_launch_wave_end(w, cs);
+    if (r == RT_OK) r = mark(PT_KERNEL_ACCUMULATE);
     return r;
 }
 
@@ -118,24 +156,7 @@ int WaveEngine::capture(const PtWave &w, uint32_t depth, bool ext, bool shadow_a
     }
     cudaStream_t cs = capture_stream_;
     RT_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-    int r = pt_launch_wave_begin(w, cs);
-    if (r == RT_OK) r = pt_launch_raygen(w, cs);
-    int cur = 0;
-    for (uint32_t did = 0; r == RT_OK && did < depth; ++did) {
-        r = trace_closest_batch(w, cur, big_stack, cs);
-        // The queues shading appends to start empty: the next ray queue and both shadow queues.
-        if (r == RT_OK && (cudaMemsetAsync(&w.counters[cur ^ 1], 0, 4, cs) != cudaSuccess ||
-                           cudaMemsetAsync(&w.counters[2], 0, 8, cs) != cudaSuccess)) {
-            set_error("cudaMemsetAsync failed during capture");
-            r = RT_ERR_CUDA;
-        }
-        if (r == RT_OK) r = pt_launch_shade(w, cur, did, ext, cs);
-        if (r == RT_OK && shadow_a) r = pt_launch_shadow(w, 0, big_stack, cs);
-        if (r == RT_OK && shadow_b) r = pt_launch_shadow(w, 1, big_stack, cs);
-        cur ^= 1;
-    }
-    if (r == RT_OK) r = pt_launch_accumulate(w, cs);
-    if (r == RT_OK) r = pt_launch_wave_end(w, cs);
+    const int r = launch_wave(w, depth, ext, shadow_a, shadow_b, big_stack, cs, nullptr, nullptr);
     cudaGraph_t graph = nullptr;
     const cudaError_t e = cudaStreamEndCapture(cs, &graph);
     if (r != RT_OK) {
@@ -157,7 +178,7 @@ int WaveEngine::capture(const PtWave &w, uint32_t depth, bool ext, bool shadow_a
 }
 
 int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn, bool device_images, cudaStream_t st,
-                    pt_render_stats *stats) {
+                    pt_render_stats *stats, bool profile) {
     if (jobs.empty()) return RT_OK;
     const bool ext = mode == PT_MODE_EXTENDED;
     const uint64_t cap = std::max<uint64_t>(tn.wave_paths, 1u << 12);
@@ -217,10 +238,25 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
         return RT_ERR_ARG;
     }
     // ---- tiles and waves -----------------------------------------------------------------------
+    // Pixel ranges of every job: chunks of `chunk` pixels, or under a rank split the chunks of
+    // this rank's PT_RANK_TILE_PIXELS tiles only.
+    std::vector<std::vector<std::pair<uint32_t, uint32_t>>> ranges(jobs.size());
+    for (size_t j = 0; j < jobs.size(); ++j) {
+        const uint32_t npix = hj[j].npix, ranks = std::max<uint32_t>(jobs[j].ranks, 1u);
+        if (ranks == 1) {
+            for (uint32_t p0 = 0; p0 < npix; p0 += chunk[j]) ranges[j].push_back({p0, std::min(chunk[j], npix - p0)});
+            continue;
+        }
+        const uint32_t c = std::min<uint32_t>(chunk[j], PT_RANK_TILE_PIXELS);
+        for (uint32_t t0 = jobs[j].rank * PT_RANK_TILE_PIXELS; t0 < npix; t0 += ranks * PT_RANK_TILE_PIXELS) {
+            const uint32_t t1 = std::min<uint32_t>(t0 + PT_RANK_TILE_PIXELS, npix);
+            for (uint32_t p0 = t0; p0 < t1; p0 += c) ranges[j].push_back({p0, std::min(c, t1 - p0)});
+        }
+    }
     std::vector<PtTile> tiles;
     std::vector<uint32_t> wave_tiles{0}, wave_paths;
     std::vector<std::vector<uint32_t>> last_wave(jobs.size());
-    for (size_t j = 0; j < jobs.size(); ++j) last_wave[j].assign((hj[j].npix + chunk[j] - 1) / chunk[j], UINT32_MAX);
+    for (size_t j = 0; j < jobs.size(); ++j) last_wave[j].assign(ranges[j].size(), UINT32_MAX);
     uint64_t in_wave = 0;
     auto close_wave = [&]() {
         if (in_wave == 0) return;
@@ -232,8 +268,8 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
         for (size_t j = 0; j < jobs.size(); ++j) {
             if (pass >= passes[j]) continue;
             for (uint32_t c = 0; c < last_wave[j].size(); ++c) {
-                const uint32_t p0 = c * chunk[j];
-                const uint32_t np = std::min<uint32_t>(chunk[j], hj[j].npix - p0);
+                const uint32_t p0 = ranges[j][c].first;
+                const uint32_t np = ranges[j][c].second;
                 const uint64_t paths = (uint64_t)np * S[j];
                 const uint32_t wave = (uint32_t)wave_paths.size();
                 if (in_wave + paths > cap || last_wave[j][c] == wave) close_wave();
@@ -289,7 +325,7 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
     RT_CUDA_TRY(cudaMemcpyAsync(wave_tiles_.ptr, wave_tiles.data(), wave_tiles.size() * 4, cudaMemcpyHostToDevice, st));
     RT_CUDA_TRY(cudaMemcpyAsync(wave_paths_.ptr, wave_paths.data(), wave_paths.size() * 4, cudaMemcpyHostToDevice, st));
     RT_CUDA_TRY(cudaMemsetAsync(counters_.ptr, 0, 128, st));
-    if (any_aov) RT_CUDA_TRY(cudaMemsetAsync(aov_accum_.ptr, 0, accum_pixels * 28, st));
+    if (any_aov) RT_CUDA_TRY(cudaMemsetAsync(aov_accum_.ptr, 0, accum_pixels * 4 * PT_AOV_ACCUM, st));
     // Images: accumulate into what the caller passed (PathTracer.cpp:288).
     std::vector<float *> dimg(jobs.size());
     uint64_t off = 0;
@@ -331,18 +367,37 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
     RT_CUDA_TRY(cudaEventCreate(&e0));
     RT_CUDA_TRY(cudaEventCreate(&e1));
     RT_CUDA_TRY(cudaEventRecord(e0, st));
-    for (uint64_t k = 0; k < nwaves && r == RT_OK; ++k)
-        if (cudaGraphLaunch(exec_, st) != cudaSuccess) {
-            set_error(std::string("graph launch failed: ") + cudaGetErrorString(cudaGetLastError()));
-            r = RT_ERR_CUDA;
+    float kernel_ms[PT_KERNEL_KINDS] = {0, 0, 0, 0};
+    if (!profile) {
+        for (uint64_t k = 0; k < nwaves && r == RT_OK; ++k)
+            if (cudaGraphLaunch(exec_, st) != cudaSuccess) {
+                set_error(std::string("graph launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+                r = RT_ERR_CUDA;
+            }
+    } else {
+        // Per-kernel times: the same sequence launched directly on `st`, an event after every
+        // step, read back wave by wave.
+        for (uint64_t k = 0; k < nwaves && r == RT_OK; ++k) {
+            std::vector<cudaEvent_t> marks;
+            std::vector<int> kinds;
+            r = launch_wave(w, depth, ext, shadow_a, shadow_b, big_stack, st, &marks, &kinds);
+            if (r == RT_OK && !marks.empty() && cudaEventSynchronize(marks.back()) != cudaSuccess) r = RT_ERR_CUDA;
+            for (size_t q = 1; r == RT_OK && q < marks.size(); ++q) {
+                float ms = 0.0f;
+                if (cudaEventElapsedTime(&ms, marks[q - 1], marks[q]) == cudaSuccess) kernel_ms[kinds[q]] += ms;
+            }
+            for (cudaEvent_t e : marks) cudaEventDestroy(e);
         }
+    }
     if (r == RT_OK && cudaEventRecord(e1, st) != cudaSuccess) r = RT_ERR_CUDA;
     std::vector<float *> daov(jobs.size(), nullptr);
     for (size_t j = 0; j < jobs.size() && r == RT_OK; ++j) {
-        const size_t off3 = 3 * (size_t)hj[j].accum_offset, off7 = 7 * (size_t)hj[j].accum_offset;
-        if (jobs[j].aov) daov[j] = device_images ? jobs[j].aov : aov_staging_.as<float>() + off7;
+        const size_t off3 = 3 * (size_t)hj[j].accum_offset, off_a = PT_AOV_ACCUM * (size_t)hj[j].accum_offset;
+        if (jobs[j].aov)
+            daov[j] = device_images ? jobs[j].aov : aov_staging_.as<float>() + PT_AOV * (size_t)hj[j].accum_offset;
         r = pt_launch_store(w.accum + off3, hj[j].fp64 ? w.accum64 + off3 : nullptr, hj[j].npix, (float)hj[j].spp,
-                            hj[j].comps, dimg[j], jobs[j].aov ? w.aov_accum + off7 : nullptr, daov[j], st);
+                            hj[j].comps, std::max<uint32_t>(jobs[j].ranks, 1u), jobs[j].rank, dimg[j],
+                            jobs[j].aov ? w.aov_accum + off_a : nullptr, daov[j], st);
     }
     unsigned long long hs[3] = {0, 0, 0};
     unsigned hstatus = 0;
@@ -351,7 +406,7 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
         r = RT_ERR_CUDA;
     if (r == RT_OK && !device_images)
         for (size_t j = 0; j < jobs.size() && r == RT_OK; ++j)
-            if (jobs[j].aov && cudaMemcpyAsync(jobs[j].aov, daov[j], (size_t)hj[j].npix * 28, cudaMemcpyDeviceToHost,
+            if (jobs[j].aov && cudaMemcpyAsync(jobs[j].aov, daov[j], (size_t)hj[j].npix * 4 * PT_AOV, cudaMemcpyDeviceToHost,
                                                st) != cudaSuccess)
                 r = RT_ERR_CUDA;
     if (r == RT_OK && !device_images)
@@ -371,8 +426,10 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
         stats->bounce_rays = hs[1];
         stats->shadow_rays = hs[2];
         stats->paths = 0;
-        for (const PtJob &J : hj) stats->paths += (uint64_t)J.npix * J.spp;
+        for (size_t j = 0; j < hj.size(); ++j)
+            for (const auto &rg : ranges[j]) stats->paths += (uint64_t)rg.second * hj[j].spp;
         stats->device_ms = ms;
+        for (int k = 0; k < PT_KERNEL_KINDS; ++k) stats->kernel_ms[k] = kernel_ms[k];
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

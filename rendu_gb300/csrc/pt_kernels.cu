@@ -503,16 +503,25 @@ __global__ void k_accumulate(PtWave w) {
         acc[2] = b;
     }
     if (J.aov) {
-        float *a = w.aov_accum + 7 * px;
-        float f[7] = {a[0], a[1], a[2], a[3], a[4], a[5], a[6]};
+        // First-hit features, and the sum and sum of squares of the samples' luminance
+        // (as accumulated: clamped) for the standard error of the pixel's mean.
+        float *a = w.aov_accum + PT_AOV_ACCUM * px;
+        float f[PT_AOV_ACCUM];
+#pragma unroll
+        for (int k = 0; k < PT_AOV_ACCUM; ++k) f[k] = a[k];
         for (uint32_t s = 0; s < tile.S; ++s) {
             const size_t q = (size_t)tile.path0 + (size_t)s * tile.npix + local;
-            const float4 a0 = w.aov0[q], a1 = w.aov1[q];
+            const float4 a0 = w.aov0[q], a1 = w.aov1[q], c = w.color[q];
             f[0] += a0.x; f[1] += a0.y; f[2] += a0.z;
             f[3] += a1.x; f[4] += a1.y; f[5] += a1.z;
             f[6] += a0.w;
+            const float lum = 0.2126f * (clamp ? gmin(c.x, cl) : c.x) + 0.7152f * (clamp ? gmin(c.y, cl) : c.y) +
+                              0.0722f * (clamp ? gmin(c.z, cl) : c.z);
+            f[7] += lum;
+            f[8] += lum * lum;
         }
-        for (int k = 0; k < 7; ++k) a[k] = f[k];
+#pragma unroll
+        for (int k = 0; k < PT_AOV_ACCUM; ++k) a[k] = f[k];
     }
 }
 
@@ -529,15 +538,28 @@ __global__ void k_load(const float *__restrict__ img, uint32_t comps, uint32_t n
 
 // render.rgb(x, y) /= samples (PathTracer.cpp:291-292); feature buffers averaged likewise.
 __global__ void k_store(const float *__restrict__ accum, const double *__restrict__ accum64, uint32_t npix,
-                        float spp, uint32_t comps, float *__restrict__ img, const float *__restrict__ aov_accum,
-                        float *__restrict__ aov) {
+                        float spp, uint32_t comps, uint32_t ranks, uint32_t rank, float *__restrict__ img,
+                        const float *__restrict__ aov_accum, float *__restrict__ aov) {
     const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
     if (px >= npix) return;
+    if (ranks > 1 && (px / PT_RANK_TILE_PIXELS) % ranks != rank) {
+        // Another rank's pixel: zero, so that the sum over ranks assembles the image.
+        for (uint32_t k = 0; k < comps; ++k) img[(size_t)px * comps + k] = 0.0f;
+        if (aov)
+            for (int k = 0; k < PT_AOV; ++k) aov[PT_AOV * (size_t)px + k] = 0.0f;
+        return;
+    }
     for (int k = 0; k < 3; ++k)
         img[(size_t)px * comps + k] =
             accum64 ? (float)(accum64[3 * (size_t)px + k] / (double)spp) : accum[3 * (size_t)px + k] / spp;
-    if (aov)
-        for (int k = 0; k < 7; ++k) aov[7 * (size_t)px + k] = aov_accum[7 * (size_t)px + k] / spp;
+    if (aov) {
+        const float *a = aov_accum + PT_AOV_ACCUM * (size_t)px;
+        float *o = aov + PT_AOV * (size_t)px;
+        for (int k = 0; k < 7; ++k) o[k] = a[k] / spp;
+        // Standard error of the mean luminance: sqrt((E[L^2] - E[L]^2) / spp).
+        const float m = a[7] / spp, m2 = a[8] / spp;
+        o[7] = sqrtf(fmaxf(m2 - m * m, 0.0f) / spp);
+    }
 }
 
 __global__ void k_mat_eval(const float *__restrict__ c, uint32_t n, float *__restrict__ out) {
@@ -742,9 +764,9 @@ int pt_launch_load(const float *img, uint32_t comps, uint32_t npix, float *accum
     return RT_OK;
 }
 
-int pt_launch_store(const float *accum, const double *accum64, uint32_t npix, float spp, uint32_t comps, float *img,
-                    const float *aov_accum, float *aov, cudaStream_t st) {
-    k_store<<<(npix + 255) / 256, 256, 0, st>>>(accum, accum64, npix, spp, comps, img, aov_accum, aov);
+int pt_launch_store(const float *accum, const double *accum64, uint32_t npix, float spp, uint32_t comps, uint32_t ranks,
+                    uint32_t rank, float *img, const float *aov_accum, float *aov, cudaStream_t st) {
+    k_store<<<(npix + 255) / 256, 256, 0, st>>>(accum, accum64, npix, spp, comps, ranks, rank, img, aov_accum, aov);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

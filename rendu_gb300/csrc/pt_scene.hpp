@@ -7,6 +7,12 @@
 #include "pt_device.cuh"
 #include "rt_context.hpp"
 
+// Feature buffer: PT_AOV floats per pixel out (albedo rgb, normal xyz, distance, standard
+// error of the mean luminance), PT_AOV_ACCUM accumulated (the first 7, then the sum and the
+// sum of squares of the samples' luminance).
+#define PT_AOV 8
+#define PT_AOV_ACCUM 9
+
 namespace rgb {
 
 // One render of a call (a batch has many): its scene, camera frame, sampling grid, options.
@@ -45,7 +51,7 @@ struct PtWave {
     float *accum;               // 3 floats per pixel of every job
     double *accum64;            // 3 doubles per pixel of every job (jobs with fp64)
     float4 *aov0, *aov1;        // per path: albedo.rgb + distance, normal.xyz (jobs with aov)
-    float *aov_accum;           // 7 floats per pixel of every job (jobs with aov)
+    float *aov_accum;           // PT_AOV_ACCUM floats per pixel of every job (jobs with aov)
     const PtJob *jobs;
     const JobBvh *bvhs;
     const PtTile *tiles;
@@ -84,8 +90,8 @@ int pt_launch_shade(const PtWave &w, int cur, uint32_t did, bool ext, cudaStream
 int pt_launch_shadow(const PtWave &w, int queue, bool big_stack, cudaStream_t st);
 int pt_launch_accumulate(const PtWave &w, cudaStream_t st);
 int pt_launch_load(const float *img, uint32_t comps, uint32_t npix, float *accum, double *accum64, cudaStream_t st);
-int pt_launch_store(const float *accum, const double *accum64, uint32_t npix, float spp, uint32_t comps, float *img,
-                    const float *aov_accum, float *aov, cudaStream_t st);
+int pt_launch_store(const float *accum, const double *accum64, uint32_t npix, float spp, uint32_t comps, uint32_t ranks,
+                    uint32_t rank, float *img, const float *aov_accum, float *aov, cudaStream_t st);
 // Closest hit for the wave's ray queue `cur`, each ray against its job's hierarchy.
 int trace_closest_batch(const PtWave &w, int cur, bool big_stack, cudaStream_t st);
 int trace_closest_batch_prepare(bool big_stack);
@@ -103,6 +109,7 @@ struct JobSpec {
     float clamp;
     int fp64;
     float *aov;  // width x height x 7 output (host or device like the image), or null
+    uint32_t ranks = 1, rank = 0;  // pixel split (pt_render_options.ranks / .rank)
 };
 
 // Wave-engine tuning (chosen by pt_batch_autotune or defaults).
@@ -121,13 +128,19 @@ class WaveEngine {
   public:
     explicit WaveEngine(int device) : device_(device) {}
     ~WaveEngine();
+    // profile: launch the per-wave sequence directly (not the captured graph) with events
+    // between the steps, and report the time of every kernel class in stats->kernel_ms.
     int run(const std::vector<JobSpec> &jobs, int mode, const Tuning &t, bool device_images, cudaStream_t st,
-            pt_render_stats *stats);
+            pt_render_stats *stats, bool profile = false);
 
   private:
     int ensure_capacity(uint64_t cap, uint64_t accum_pixels, uint64_t ntiles, uint64_t nwaves, size_t njobs,
                         uint64_t staging_floats, bool fp64, bool aov);
     int capture(const PtWave &w, uint32_t depth, bool ext, bool shadow_a, bool shadow_b, bool big_stack);
+    // The per-wave launch sequence on `st`. With `marks`, an event is recorded after every
+    // step and `kinds` receives the step's kernel class (PT_KERNEL_*), for per-kernel times.
+    int launch_wave(const PtWave &w, uint32_t depth, bool ext, bool shadow_a, bool shadow_b, bool big_stack,
+                    cudaStream_t st, std::vector<cudaEvent_t> *marks, std::vector<int> *kinds);
     int device_;
     cudaStream_t capture_stream_ = nullptr;
     DevBuf atten_, color_, ndc_, pjob_, ppix_, psamp_, qray0_, qray1_, qpath0_, qpath1_, hits_, sray_, scontrib_;

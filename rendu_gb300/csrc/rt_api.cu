@@ -39,12 +39,15 @@ int trace_count(rt_ctx *ctx, const rt_ray *d_rays, size_t n, uint32_t *nc, uint3
 int segments_to_rays(const float *d_segs, size_t n, rt_ray *d_rays, cudaStream_t st);
 int invert_bytes(uint8_t *d, size_t n, cudaStream_t st);
 
-int check_status(rt_ctx *ctx, cudaStream_t st) {
+// Reads the status word at `word` on stream `st` (waiting for the stream), clears it and
+// maps its bits to a status code.
+static int read_status(void *word, cudaStream_t st, unsigned *raw) {
     unsigned s = 0;
-    RT_CUDA_TRY(cudaMemcpyAsync(&s, ctx->d_status.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    RT_CUDA_TRY(cudaMemcpyAsync(&s, word, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     RT_CUDA_TRY(cudaStreamSynchronize(st));
+    if (raw) *raw = s;
     if (s) {
-        RT_CUDA_TRY(cudaMemsetAsync(ctx->d_status.ptr, 0, sizeof(unsigned), st));
+        RT_CUDA_TRY(cudaMemsetAsync(word, 0, sizeof(unsigned), st));
         if (s & RT_DEV_TIMEOUT) {
             set_error("a bounded device loop gave up");
             return RT_ERR_TIMEOUT;
@@ -53,6 +56,32 @@ int check_status(rt_ctx *ctx, cudaStream_t st) {
         return RT_ERR_OVERFLOW;
     }
     return RT_OK;
+}
+
+int check_status(rt_ctx *ctx, cudaStream_t st) { return read_status(ctx->d_status.ptr, st, nullptr); }
+
+// Hit -> (meshId, localId): the last mesh whose first triangle is <= prim (empty meshes share
+// their successor's first triangle and are never the last such mesh for a valid prim).
+__global__ void k_hit_info(const rt_hit *__restrict__ hits, size_t n, const uint32_t *__restrict__ first,
+                           uint32_t meshes, uint32_t *__restrict__ mesh_id, uint32_t *__restrict__ local_id) {
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t prim = hits[i].prim;
+    uint32_t m = RT_NO_HIT, l = RT_NO_HIT;
+    if (prim != RT_NO_HIT && meshes > 0) {
+        uint32_t lo = 0, hi = meshes;  // upper bound of prim in first[0..meshes)
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (first[mid] <= prim) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo > 0) {
+            m = lo - 1;
+            l = 3u * (prim - first[m]);
+        }
+    }
+    if (mesh_id) mesh_id[i] = m;
+    if (local_id) local_id[i] = l;
 }
 
 }  // namespace rgb
@@ -86,16 +115,39 @@ int require_built(rt_ctx *ctx) {
     return RT_OK;
 }
 
+bool is_pageable(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return a.type == cudaMemoryTypeUnregistered;
+}
+
 // Runs `fn(d_in, count, d_out, stream)` over host buffers in chunks of 2M records through a
 // ring of four staging buffers and three streams: copies in on `stream`, kernels on
 // `stream2`, copies out on `stream3`, ordered by events, so that both copy directions and
 // the kernels stay busy at once (the host link, not the kernels, bounds this path). Pinned
-// host buffers get asynchronous DMA; pageable ones still work but their copies do not
-// overlap.
+// host buffers get asynchronous DMA. Pageable buffers (a caller's std::vector or numpy
+// array), whose copies would not overlap, are read and written in place by the kernels
+// where the device reaches pageable memory (cudaDevAttrPageableMemoryAccess, e.g. through
+// the host's page tables on Grace), chunk after chunk on `stream2`; elsewhere they go
+// through the same staging ring.
 template <class Fn>
 int host_chunked(rt_ctx *ctx, const void *h_in, size_t in_stride, size_t n, void *h_out, size_t out_stride, Fn fn) {
     constexpr int NB = rt_ctx::kRing;
     const size_t chunk = size_t(1) << 21;
+    if (ctx->pageable_access && (is_pageable(h_in) || is_pageable(h_out))) {
+        int r = RT_OK;
+        for (size_t s = 0; s < n && r == RT_OK; s += chunk) {
+            const size_t m = (n - s) < chunk ? (n - s) : chunk;
+            r = fn(const_cast<char *>(static_cast<const char *>(h_in)) + s * in_stride, m,
+                   static_cast<char *>(h_out) + s * out_stride, ctx->stream2);
+        }
+        RT_CUDA_TRY(cudaStreamSynchronize(ctx->stream2));
+        if (r != RT_OK) return r;
+        return check_status(ctx, ctx->stream2);
+    }
     const size_t cn = n < chunk ? n : chunk;
     if (!ctx->stream3) RT_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream3, cudaStreamNonBlocking));
     for (int b = 0; b < NB; ++b) {
@@ -161,12 +213,19 @@ int rt_create(rt_ctx **out, int device) {
         delete ctx;
         return RT_ERR_CUDA;
     }
-    // Status word at offset 0, three traversal fetch counters at offsets 8, 16, 24.
+    // Status word of the host-buffer calls at 0, three traversal fetch counters at 8, 16, 24,
+    // status word of the asynchronous calls at 32.
     if (ctx->d_status.reserve(64) != RT_OK) {
         delete ctx;
         return RT_ERR_OOM;
     }
     cudaMemset(ctx->d_status.ptr, 0, 64);
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+        cudaGetLastError();
+        pageable = 0;
+    }
+    ctx->pageable_access = pageable != 0;
     *out = ctx;
     return RT_OK;
 }
@@ -180,6 +239,8 @@ int rt_destroy(rt_ctx *ctx) {
     ctx->d_verts.release();
     ctx->d_status.release();
     ctx->d_out2.release();
+    ctx->d_mesh_first.release();
+    ctx->d_info_stage.release();
     if (ctx->stream2) {
         cudaStreamSynchronize(ctx->stream2);
         cudaStreamDestroy(ctx->stream2);
@@ -260,6 +321,12 @@ int rt_update_hierarchy(rt_ctx *ctx) {
         set_error("hierarchy deeper than the traversal stack (256)");
         return RT_ERR_OVERFLOW;
     }
+    std::vector<uint32_t> first(ctx->meshes.size());
+    for (size_t m = 0; m < first.size(); ++m) first[m] = (uint32_t)ctx->meshes[m].first_tri;
+    if (ctx->d_mesh_first.reserve(first.size() * sizeof(uint32_t) + 16) != RT_OK) return RT_ERR_OOM;
+    if (!first.empty())
+        RT_CUDA_TRY(cudaMemcpy(ctx->d_mesh_first.ptr, first.data(), first.size() * sizeof(uint32_t),
+                               cudaMemcpyHostToDevice));
     ctx->built = true;
     ctx->dirty = false;
     return RT_OK;
@@ -386,6 +453,69 @@ int rt_prim_info(const rt_ctx *ctx, uint32_t prim, uint32_t *mesh_id, uint32_t *
     while (ctx->meshes[lo].tri_count == 0 && lo > 0) --lo;
     *mesh_id = (uint32_t)lo;
     *local_id = (uint32_t)(3 * (prim - ctx->meshes[lo].first_tri));
+    return RT_OK;
+}
+
+int rt_hit_info(rt_ctx *ctx, const rt_hit *hits, size_t n, uint32_t *mesh_ids, uint32_t *local_ids, void *stream,
+                uint32_t flags) {
+    clear_error();
+    int r = require_built(ctx);
+    if (r != RT_OK) return r;
+    if (n && (!hits || (!mesh_ids && !local_ids))) {
+        set_error("null hits or outputs");
+        return RT_ERR_ARG;
+    }
+    if (n == 0) return RT_OK;
+    DeviceGuard g(ctx->device);
+    const uint32_t meshes = (uint32_t)ctx->meshes.size();
+    const unsigned blocks = (unsigned)((n + 255) / 256);
+    if (flags & RT_FLAG_DEVICE_PTRS) {
+        k_hit_info<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+            hits, n, ctx->d_mesh_first.as<uint32_t>(), meshes, mesh_ids, local_ids);
+        RT_CUDA_TRY(cudaGetLastError());
+        return RT_OK;
+    }
+    // Host buffers: hits in, the two id arrays out, through one staging buffer on the
+    // context's stream.
+    const size_t in_bytes = n * sizeof(rt_hit), out_bytes = n * sizeof(uint32_t);
+    if (ctx->d_info_stage.reserve(in_bytes + 2 * out_bytes) != RT_OK) return RT_ERR_OOM;
+    cudaStream_t st = ctx->stream;
+    char *base = ctx->d_info_stage.as<char>();
+    uint32_t *dm = reinterpret_cast<uint32_t *>(base + in_bytes), *dl = dm + n;
+    RT_CUDA_TRY(cudaMemcpyAsync(base, hits, in_bytes, cudaMemcpyHostToDevice, st));
+    k_hit_info<<<blocks, 256, 0, st>>>(reinterpret_cast<const rt_hit *>(base), n, ctx->d_mesh_first.as<uint32_t>(),
+                                       meshes, mesh_ids ? dm : nullptr, local_ids ? dl : nullptr);
+    RT_CUDA_TRY(cudaGetLastError());
+    if (mesh_ids) RT_CUDA_TRY(cudaMemcpyAsync(mesh_ids, dm, out_bytes, cudaMemcpyDeviceToHost, st));
+    if (local_ids) RT_CUDA_TRY(cudaMemcpyAsync(local_ids, dl, out_bytes, cudaMemcpyDeviceToHost, st));
+    RT_CUDA_TRY(cudaStreamSynchronize(st));
+    return RT_OK;
+}
+
+int rt_get_status(rt_ctx *ctx, void *stream, uint32_t *word) {
+    clear_error();
+    if (!ctx) {
+        set_error("null context");
+        return RT_ERR_ARG;
+    }
+    DeviceGuard g(ctx->device);
+    unsigned raw = 0;
+    const int r = read_status(ctx->d_status.as<char>() + 32, static_cast<cudaStream_t>(stream), &raw);
+    if (word) *word = raw;
+    return r;
+}
+
+int rt_set_traversal_stack(rt_ctx *ctx, uint32_t entries) {
+    clear_error();
+    if (!ctx) {
+        set_error("null context");
+        return RT_ERR_ARG;
+    }
+    if (entries > 256) {
+        set_error("the traversal stack holds at most 256 entries");
+        return RT_ERR_ARG;
+    }
+    ctx->stack_cap = entries;
     return RT_OK;
 }
 

@@ -52,7 +52,12 @@ struct rt_ctx {
     rgb::DevBuf d_nodes;   // BvhNode[n_inner] (at least 1: a root, possibly wrapping a leaf)
     rgb::DevBuf d_tris;    // BvhTri[n_tris] in leaf order
     rgb::DevBuf d_verts;   // float3 transformed vertices (kept for the path tracer)
-    rgb::DevBuf d_status;  // unsigned status word
+    // 64 bytes: status word of the host-buffer calls at 0, three traversal fetch counters at
+    // 8, 16, 24, status word of the asynchronous calls (device pointers on the caller's
+    // stream, rt_visible_noalloc) at 32, read and cleared by rt_get_status.
+    rgb::DevBuf d_status;
+    uint32_t stack_cap = 0;  // rt_set_traversal_stack: 0 = the hierarchy's exact bound
+    bool pageable_access = false;  // kernels can read and write pageable host memory in place
     uint64_t n_tris = 0;
     uint64_t n_inner = 0;
     uint64_t n_leaves = 0;
@@ -63,6 +68,10 @@ struct rt_ctx {
 
     // Scratch of rt_visible (converted rays) and rt_count_visits (hits).
     rgb::DevBuf d_out2;
+    // First triangle of every mesh (addMesh order), uploaded by rt_update_hierarchy for
+    // rt_hit_info; and the staging of rt_hit_info's host-buffer path.
+    rgb::DevBuf d_mesh_first;
+    rgb::DevBuf d_info_stage;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
     // Host-buffer pipeline: copy-in on `stream`, kernels on `stream2`, copy-out on `stream3`,
     // through a ring of staging buffers (created on first use).
@@ -80,6 +89,21 @@ int trace_any(rt_ctx *ctx, const rt_ray *d_rays, size_t n, uint8_t *d_occ, cudaS
 int trace_closest_queue(rt_ctx *ctx, const rt_ray *d_rays, const uint32_t *d_count, uint32_t cap, rt_hit *d_hits,
                         cudaStream_t stream);
 int check_status(rt_ctx *ctx, cudaStream_t stream);  // reads and clears the device status word
+
+// The status word a traversal on `st` reports into: the host-buffer path's own streams use
+// the word check_status reads; every other stream (the caller's) the word rt_get_status reads.
+inline unsigned *status_word(rt_ctx *ctx, cudaStream_t st) {
+    const bool own = st == ctx->stream || st == ctx->stream2;
+    return reinterpret_cast<unsigned *>(ctx->d_status.as<char>() + (own ? 0 : 32));
+}
+
+// Entries of the traversal stack the kernels are instantiated with (2, 64 or 256): the
+// smallest that holds the hierarchy's exact bound, or the cap set by rt_set_traversal_stack
+// (the 2-entry kernels only exist for that diagnostic).
+inline int traversal_stack(const rt_ctx *ctx) {
+    const int need = ctx->stack_cap ? (int)ctx->stack_cap : ctx->depth;
+    return need <= 2 && ctx->stack_cap ? 2 : (need <= 64 ? 64 : 256);
+}
 }  // namespace rgb
 
 #define RT_CUDA_TRY(expr)                                                                    \

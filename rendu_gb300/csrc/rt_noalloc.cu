@@ -3,8 +3,10 @@
 // block (a frame loop or audio/robotics callback with a fixed memory budget, a plugin host
 // that owns every allocation, code that must not trigger the implicit synchronisation of
 // cudaMalloc/cudaFree). The caller passes device buffers for the segments and the answers;
-// the library's own scratch -- the converted rays, the traversal's ray-fetch counter and
-// its status word -- lives in one file-scope device array instead of cudaMalloc'd memory.
+// the library's own scratch -- the converted rays and the traversal's ray-fetch counter --
+// lives in one file-scope device array instead of cudaMalloc'd memory. A traversal stack
+// overflow is recorded in the context's status word for asynchronous calls (allocated once
+// by rt_create), which rt_get_status reads and clears.
 //
 // Limits and rules (also stated in include/rendu_gb300.h):
 //  * at most RT_NOALLOC_MAX_SEGMENTS segments per call (the array is 256 B + 32 B per
@@ -24,7 +26,7 @@
 namespace rgb {
 namespace {
 
-constexpr size_t kHeaderBytes = 256;  // status word at 0, ray-fetch counter at 8
+constexpr size_t kHeaderBytes = 256;  // ray-fetch counter at 8 (bytes 0..15 cleared per call)
 constexpr size_t kScratchBytes = kHeaderBytes + sizeof(rt_ray) * (size_t)RT_NOALLOC_MAX_SEGMENTS;
 
 // The scratch. In host code this name is only a stand-in for the symbol: its device address
@@ -94,7 +96,7 @@ struct DeviceScratch {
 
 std::mutex g_lock;
 DeviceScratch g_dev[64];
-int g_grid[64][2];
+int g_grid[64][3];
 
 }  // namespace
 }  // namespace rgb
@@ -103,6 +105,7 @@ using namespace rgb;
 
 extern "C" int rt_visible_noalloc(rt_ctx *ctx, const float *segs, size_t n, uint8_t *visible, void *stream) {
     clear_error();
+    cudaGetLastError();  // a launch error reported below then belongs to this call
     if (!ctx || (n && (!segs || !visible))) {
         set_error("null argument");
         return RT_ERR_ARG;
@@ -141,6 +144,8 @@ extern "C" int rt_visible_noalloc(rt_ctx *ctx, const float *segs, size_t n, uint
                 g_grid[ctx->device][0] = sms * (per_sm > 0 ? per_sm : 1);
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_noalloc_visible<256>, 128, 0);
                 g_grid[ctx->device][1] = sms * (per_sm > 0 ? per_sm : 1);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_noalloc_visible<2>, 128, 0);
+                g_grid[ctx->device][2] = sms * (per_sm > 0 ? per_sm : 1);
                 d.ready = true;
             }
         }
@@ -148,12 +153,15 @@ extern "C" int rt_visible_noalloc(rt_ctx *ctx, const float *segs, size_t n, uint
     }
     if (rc == RT_OK && n > 0) {
         cudaStream_t st = static_cast<cudaStream_t>(stream);
-        unsigned *status = reinterpret_cast<unsigned *>(base);
+        // Overflows go to the context's word for asynchronous calls (rt_get_status).
+        unsigned *status = status_word(ctx, st);
         unsigned long long *counter = reinterpret_cast<unsigned long long *>(base + 8);
         rt_ray *rays = reinterpret_cast<rt_ray *>(base + kHeaderBytes);
-        // The fetch counter must start at zero; the previous call's rays are overwritten.
-        if (cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st) != cudaSuccess) {
-            set_error(std::string("cudaMemsetAsync failed: ") + cudaGetErrorString(cudaGetLastError()));
+        // The header (fetch counter included) must start at zero; the previous call's rays
+        // are overwritten.
+        const cudaError_t me = cudaMemsetAsync(base, 0, 16, st);
+        if (me != cudaSuccess) {
+            set_error(std::string("cudaMemsetAsync failed: ") + cudaGetErrorString(me));
             rc = RT_ERR_CUDA;
         }
         if (rc == RT_OK) {
@@ -161,12 +169,16 @@ extern "C" int rt_visible_noalloc(rt_ctx *ctx, const float *segs, size_t n, uint
             const BvhNode *nodes = ctx->d_nodes.as<BvhNode>();
             const BvhTri *tris = ctx->d_tris.as<BvhTri>();
             const int empty = ctx->n_tris == 0 ? 1 : 0;
-            if (ctx->depth <= 64)
+            const int stack = traversal_stack(ctx);
+            if (stack == 64)
                 k_noalloc_visible<64><<<g_grid[ctx->device][0], 128, 0, st>>>(nodes, tris, rays, (uint32_t)n, visible,
                                                                               status, counter, empty);
-            else
+            else if (stack == 256)
                 k_noalloc_visible<256><<<g_grid[ctx->device][1], 128, 0, st>>>(nodes, tris, rays, (uint32_t)n,
                                                                                visible, status, counter, empty);
+            else
+                k_noalloc_visible<2><<<g_grid[ctx->device][2], 128, 0, st>>>(nodes, tris, rays, (uint32_t)n, visible,
+                                                                             status, counter, empty);
             const cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) {
                 set_error(std::string("launch failed: ") + cudaGetErrorString(e));

@@ -184,7 +184,7 @@ int launch_persistent(rt_ctx *ctx, const rt_ray *rays, size_t n, const uint32_t 
     const RootBox root{{ctx->root_box[0], ctx->root_box[1], ctx->root_box[2]},
                        {ctx->root_box[3], ctx->root_box[4], ctx->root_box[5]}};
     k_trace_persistent<ANY, STACK><<<g, 128, 0, st>>>(ctx->d_nodes.as<BvhNode>(), ctx->d_tris.as<BvhTri>(), rays, n,
-                                                      n_dev, hits, occ, ctx->d_status.as<unsigned>(), counter, root);
+                                                      n_dev, hits, occ, status_word(ctx, st), counter, root);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
@@ -193,19 +193,23 @@ template <bool ANY, bool COUNT>
 int launch(rt_ctx *ctx, const rt_ray *rays, size_t n, rt_hit *hits, uint8_t *occ, uint32_t *nc, uint32_t *tc,
            cudaStream_t st) {
     if (n == 0) return RT_OK;
+    const int stack = traversal_stack(ctx);
     if (!COUNT && ctx->n_tris > 0) {
-        if (ctx->depth <= 64) return launch_persistent<ANY, 64>(ctx, rays, n, nullptr, hits, occ, st);
-        return launch_persistent<ANY, 256>(ctx, rays, n, nullptr, hits, occ, st);
+        if (stack == 64) return launch_persistent<ANY, 64>(ctx, rays, n, nullptr, hits, occ, st);
+        if (stack == 256) return launch_persistent<ANY, 256>(ctx, rays, n, nullptr, hits, occ, st);
+        return launch_persistent<ANY, 2>(ctx, rays, n, nullptr, hits, occ, st);
     }
     const unsigned blocks = (unsigned)((n + 127) / 128);
     const BvhNode *nodes = ctx->d_nodes.as<BvhNode>();
     const BvhTri *tris = ctx->d_tris.as<BvhTri>();
-    unsigned *status = ctx->d_status.as<unsigned>();
+    unsigned *status = status_word(ctx, st);
     const int empty = ctx->n_tris == 0 ? 1 : 0;
-    if (ctx->depth <= 64)
+    if (stack == 64)
         k_trace<ANY, COUNT, 64><<<blocks, 128, 0, st>>>(nodes, tris, rays, n, hits, occ, nc, tc, status, empty);
-    else
+    else if (stack == 256)
         k_trace<ANY, COUNT, 256><<<blocks, 128, 0, st>>>(nodes, tris, rays, n, hits, occ, nc, tc, status, empty);
+    else
+        k_trace<ANY, COUNT, 2><<<blocks, 128, 0, st>>>(nodes, tris, rays, n, hits, occ, nc, tc, status, empty);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
@@ -240,8 +244,10 @@ int trace_closest_queue(rt_ctx *ctx, const rt_ray *d_rays, const uint32_t *d_cou
         RT_CUDA_TRY(cudaGetLastError());
         return RT_OK;
     }
-    if (ctx->depth <= 64) return launch_persistent<false, 64>(ctx, d_rays, cap, d_count, d_hits, nullptr, st);
-    return launch_persistent<false, 256>(ctx, d_rays, cap, d_count, d_hits, nullptr, st);
+    const int stack = traversal_stack(ctx);
+    if (stack == 64) return launch_persistent<false, 64>(ctx, d_rays, cap, d_count, d_hits, nullptr, st);
+    if (stack == 256) return launch_persistent<false, 256>(ctx, d_rays, cap, d_count, d_hits, nullptr, st);
+    return launch_persistent<false, 2>(ctx, d_rays, cap, d_count, d_hits, nullptr, st);
 }
 
 int segments_to_rays(const float *d_segs, size_t n, rt_ray *d_rays, cudaStream_t st) {

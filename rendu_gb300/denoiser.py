@@ -2,12 +2,12 @@
 
 A 5-level U-Net (3x3 convolutions with 32, 48, 64, 96 and 128 channels, BF16 activations,
 FP32 accumulation on the tensor cores) that maps a few-sample render plus its first-hit
-feature buffers (albedo, normal, distance: ``PathTracer.render(..., aov=...)``) to a
+feature buffers (albedo, normal, distance, standard error: ``PathTracer.render(..., aov=...)``) to a
 converged image. The reference has no learned denoiser; this module completes the
 renderer with one that is trained here on the path tracer's own output.
 
-Arrays are float32 NHWC: features (B, H, W, 10) = radiance rgb, albedo rgb, normal xyz,
-distance; images (B, H, W, 3). Host numpy arrays or CUDA tensors (all of one kind per call).
+Arrays are float32 NHWC: features (B, H, W, 11) = radiance rgb, albedo rgb, normal xyz,
+distance, standard error of the mean luminance; images (B, H, W, 3). Host numpy arrays or CUDA tensors (all of one kind per call).
 """
 from __future__ import annotations
 
@@ -18,6 +18,9 @@ import numpy as np
 from . import _lib as L
 
 FEATURES = L.DN_FEATURES
+# Network input channels that carry data (of the 16 the first layer reads): log radiance,
+# albedo, normal, distance, relative standard error, log standard error.
+INPUT_CHANNELS = 12
 
 
 def _is_cuda(a) -> bool:
@@ -59,7 +62,7 @@ def rel_rmse(x, ref, eps: float = 1e-2) -> float:
 
 
 def features_from_render(image, aov) -> np.ndarray:
-    """Stack a render (H, W, >=3) and its feature buffer (H, W, 7) into (H, W, 10)."""
+    """Stack a render (H, W, >=3) and its feature buffer (H, W, 8) into (H, W, 11)."""
     return np.ascontiguousarray(np.concatenate([np.asarray(image)[..., :3], np.asarray(aov)], axis=-1), np.float32)
 
 
@@ -115,19 +118,27 @@ class Denoiser:
     def load(self, path: str) -> None:
         self.set_params(np.load(path))
 
-    def flops(self, height: int, width: int, batch: int = 1) -> float:
+    def flops(self, height: int, width: int, batch: int = 1, channels=None) -> float:
         """Multiply-add FLOPs of one forward pass (2 x MACs of every convolution) at the
-        padded size the network runs at."""
+        padded size the network runs at. ``channels`` = (first layer's inputs, last layer's
+        outputs) counts only the channels that carry data (INPUT_CHANNELS and 3) instead of
+        the 16 each is padded to."""
         hp, wp = -(-height // 16) * 16, -(-width // 16) * 16
+        layers = self.layers()
         total = 0.0
-        for l in self.layers():
+        for k, l in enumerate(layers):
             px = batch * (hp >> l["level"]) * (wp >> l["level"])
-            total += 2.0 * px * 9 * (l["cin0"] + l["cin1"]) * l["cout"]
+            cin, cout = l["cin0"] + l["cin1"], l["cout"]
+            if channels is not None and k == 0:
+                cin = channels[0]
+            if channels is not None and k == len(layers) - 1:
+                cout = channels[1]
+            total += 2.0 * px * 9 * cin * cout
         return total
 
     # ---- compute -----------------------------------------------------------------------------
     def denoise(self, features, out=None):
-        """features (B, H, W, 10) or (H, W, 10) -> radiance of the same leading shape x 3."""
+        """features (B, H, W, 11) or (H, W, 11) -> radiance of the same leading shape x 3."""
         b, h, w, _ = _nhwc(features, FEATURES)
         dev = _is_cuda(features)
         if out is None:
@@ -173,13 +184,14 @@ class Denoiser:
             pass
 
 
-def render_pairs(tracer, cameras, width: int, height: int, spp_in: int = 4, spp_ref: int = 1024, depth: int = 5,
-                 mode: int = 1, clamp: float = 5.0, seed: int = 0):
+def render_pairs(tracer, cameras, width: int, height: int, spp_in=4, spp_ref=1024, depth: int = 5, mode: int = 1,
+                 clamp: float = 5.0, seed: int = 0):
     """Denoiser inputs and targets rendered by the path tracer itself: for each camera, the
-    features of a ``spp_in``-sample render (radiance + first-hit albedo, normal, distance;
-    a sequence of sample counts is cycled through the cameras) and, when ``spp_ref`` > 0,
-    a ``spp_ref``-sample render accumulated in double precision. Returns CUDA tensors
-    (N, H, W, 10) and (N, H, W, 3) (targets None without spp_ref)."""
+    features of a ``spp_in``-sample render (radiance + first-hit albedo, normal, distance and
+    the standard error of the mean luminance; a sequence of sample counts is cycled through
+    the cameras) and, when ``spp_ref`` is not 0, an independent render accumulated in double
+    precision with ``spp_ref`` samples (an int, or a function of the input's sample count).
+    Returns CUDA tensors (N, H, W, 11) and (N, H, W, 3) (targets None without spp_ref)."""
     import torch
 
     n = len(cameras)
@@ -187,7 +199,7 @@ def render_pairs(tracer, cameras, width: int, height: int, spp_in: int = 4, spp_
     feats = torch.empty((n, height, width, FEATURES), dtype=torch.float32, device=dev)
     targets = torch.empty((n, height, width, 3), dtype=torch.float32, device=dev) if spp_ref else None
     img = torch.empty((height, width, 3), dtype=torch.float32, device=dev)
-    aov = torch.empty((height, width, 7), dtype=torch.float32, device=dev)
+    aov = torch.empty((height, width, 8), dtype=torch.float32, device=dev)
     for k, cam in enumerate(cameras):
         cam = dict(cam, ratio=width / height)
         img.zero_()
@@ -197,17 +209,93 @@ def render_pairs(tracer, cameras, width: int, height: int, spp_in: int = 4, spp_
         feats[k, ..., 3:] = aov
         if spp_ref:
             img.zero_()
-            tracer.render(cam, spp_ref, depth, img, seed=seed + 2 * k + 1, mode=mode, clamp=clamp, fp64=True)
+            ref = spp_ref(spp) if callable(spp_ref) else spp_ref
+            tracer.render(cam, ref, depth, img, seed=seed + 2 * k + 1, mode=mode, clamp=clamp, fp64=True)
             targets[k] = img
     return feats, targets
+
+
+def rel_rmse_t(x, ref, eps: float = 1e-2) -> float:
+    """rel_rmse on CUDA tensors (float64 arithmetic)."""
+    d = (x.double() - ref.double()) / (ref.double() + eps)
+    return float(d.square().mean().sqrt())
+
+
+def progressive_curves(tracer, camera, width: int, height: int, spp_levels, truth, denoiser=None, depth: int = 5,
+                       mode: int = 1, clamp: float = 5.0, seed: int = 0):
+    """Plain path tracing and path tracing + denoiser at equal sample counts on one view, as
+    the sample count doubles: renders of ``spp_levels[0]`` and then of each level's
+    difference to the previous one are added up (independent random streams), so that the
+    image at level N costs the render time of N samples per pixel; the features (first-hit
+    buffers and the standard error) are combined the same way. At every level: the plain
+    image's relative RMSE against ``truth`` (H, W, 3 CUDA tensor) and the cumulative device
+    render time, and with ``denoiser`` the denoised image's error and the denoising time
+    (CUDA events). Returns [{spp, render_s, plain, denoised, denoise_ms}]."""
+    import torch
+
+    dev = torch.device("cuda", tracer.device)
+    w = torch.tensor([0.2126, 0.7152, 0.0722], dtype=torch.float64, device=dev)
+    rad = torch.zeros((height, width, 3), dtype=torch.float64, device=dev)
+    feat = torch.zeros((height, width, 7), dtype=torch.float64, device=dev)
+    s1 = torch.zeros((height, width), dtype=torch.float64, device=dev)
+    s2 = torch.zeros((height, width), dtype=torch.float64, device=dev)
+    img = torch.empty((height, width, 3), dtype=torch.float32, device=dev)
+    aov = torch.empty((height, width, 8), dtype=torch.float32, device=dev)
+    f = torch.empty((1, height, width, FEATURES), dtype=torch.float32, device=dev)
+    out = torch.empty((1, height, width, 3), dtype=torch.float32, device=dev)
+    cam = dict(camera, ratio=width / height)
+    total, render_s, curve = 0, 0.0, []
+    for k, level in enumerate(spp_levels):
+        n = level - total
+        img.zero_()
+        tracer.render(cam, n, depth, img, seed=seed + k, mode=mode, clamp=clamp, fp64=True, aov=aov)
+        render_s += tracer.last_stats()["device_ms"] / 1e3
+        m = img.double() @ w  # mean luminance of this render
+        se = aov[..., 7].double()
+        rad += n * img.double()
+        feat += n * aov[..., :7].double()
+        s1 += n * m
+        s2 += n * (n * se.square() + m.square())  # n E[L^2] = n (n se^2 + m^2)
+        total = level
+        point = {"spp": level, "render_s": render_s, "plain": rel_rmse_t(rad / total, truth)}
+        if denoiser is not None:
+            f[0, ..., :3] = (rad / total).float()
+            f[0, ..., 3:10] = (feat / total).float()
+            mean = s1 / total
+            f[0, ..., 10] = ((s2 / total - mean.square()).clamp(min=0.0) / total).sqrt().float()
+            denoiser.denoise(f, out)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(3):
+                denoiser.denoise(f, out)
+            e1.record()
+            torch.cuda.synchronize()
+            point["denoise_ms"] = e0.elapsed_time(e1) / 3
+            point["denoised"] = rel_rmse_t(out[0], truth)
+        curve.append(point)
+    return curve
+
+
+def time_to(points, threshold: float):
+    """Seconds to reach a relative RMSE of ``threshold`` along [(seconds, error)], interpolated
+    log-log between the two measured points around it; None when no measured point reaches
+    it."""
+    pts = sorted(points)
+    if pts and pts[0][1] <= threshold:
+        return pts[0][0]
+    for (t0, e0), (t1, e1) in zip(pts, pts[1:]):
+        if e0 > threshold >= e1:
+            a = (np.log(threshold) - np.log(e0)) / (np.log(e1) - np.log(e0))
+            return float(np.exp(np.log(t0) + a * (np.log(t1) - np.log(t0))))
+    return None
 
 
 def train(denoiser, feats, targets, steps: int, batch: int = 8, crop: int = 64, lr: float = 2e-3, seed: int = 0,
           log_every: int = 0):
     """Adam on random ``crop`` x ``crop`` crops of (feats, targets) -- CUDA tensors as
-    render_pairs returns them -- with a cosine-decayed learning rate. Crops are gathered on
-    the device; only the logged losses (every ``log_every`` steps) synchronise. Returns
-    [(step, loss)]."""
+    render_pairs returns them -- each crop flipped and transposed at random, with a
+    cosine-decayed learning rate. Crops are gathered on the device; only the logged losses
+    (every ``log_every`` steps) synchronise. Returns [(step, loss)]."""
     import math
 
     import torch
@@ -223,7 +311,13 @@ def train(denoiser, feats, targets, steps: int, batch: int = 8, crop: int = 64, 
         i = torch.randint(0, n, (batch,), generator=gen, device=feats.device)
         y = torch.randint(0, h - crop + 1, (batch,), generator=gen, device=feats.device)
         x = torch.randint(0, w - crop + 1, (batch,), generator=gen, device=feats.device)
-        bi, rows, cols = i[:, None, None], (y[:, None] + ar)[:, :, None], (x[:, None] + ar)[:, None, :]
+        flip = torch.randint(0, 8, (batch,), generator=gen, device=feats.device)
+        ry = torch.where((flip & 1).bool()[:, None], crop - 1 - ar, ar)
+        rx = torch.where((flip & 2).bool()[:, None], crop - 1 - ar, ar)
+        rows, cols = (y[:, None] + ry)[:, :, None], (x[:, None] + rx)[:, None, :]
+        tr = (flip & 4).bool()[:, None, None]
+        rows, cols = torch.where(tr, rows.transpose(1, 2), rows), torch.where(tr, cols.transpose(1, 2), cols)
+        bi = i[:, None, None]
         f = feats[bi, rows, cols].contiguous()
         t = targets[bi, rows, cols].contiguous()
         lr_s = lr * 0.5 * (1.0 + math.cos(math.pi * s / steps))

@@ -17,6 +17,9 @@ from . import _lib as L
 from .raycaster import Raycaster
 
 
+KERNEL_KINDS = ("raygen", "trace", "shade", "shadow", "accumulate")  # pt_render_stats.kernel_ms order
+
+
 def _f3(v):
     return (C.c_float * 3)(*[float(x) for x in v])
 
@@ -85,18 +88,22 @@ class PathTracer:
         L.call("pt_scene_commit", self._h)
 
     def render(self, camera, samples: int, depth: int, image, seed: int = 0, mode: int = 0, clamp: float = 5.0,
-               fp64: bool = False, aov=None):
+               fp64: bool = False, aov=None, ranks: int = 1, rank: int = 0, profile: bool = False):
         """PathTracer::render(camera, samples, depth, image): accumulate and normalise into
         ``image`` (H, W, C) float32, host array or CUDA tensor; returns ``image``.
         ``mode`` 1 selects the extended estimator (NEE on emitters and the environment
         map with MIS); ``clamp`` is the per-sample clamp (the reference's 5; <= 0: none);
         ``fp64`` accumulates each pixel's samples in double precision; ``aov`` (H, W, 7)
-        float32 (same place as ``image``) receives first-hit albedo, normal and distance."""
+        float32 (same place as ``image``) receives first-hit albedo, normal and distance.
+        ``ranks`` > 1 renders only the pixel tiles of ``rank`` and zeroes the others
+        (pt_render_options.ranks; see render_split). ``profile`` times every kernel class
+        (last_stats()["kernel_ms"]), launching the kernels without the captured graph."""
         cam = camera_desc(camera if isinstance(camera, dict) else camera.__dict__)
         aov_ptr = None
         if aov is not None:
             aov_ptr = aov.data_ptr() if type(aov).__module__.startswith("torch") else aov.ctypes.data
-        opts = L.pt_render_options(int(mode), float(clamp), int(bool(fp64)), aov_ptr)
+        opts = L.pt_render_options(int(mode), float(clamp), int(bool(fp64)), aov_ptr, int(ranks), int(rank),
+                                   int(bool(profile)))
         if type(image).__module__.startswith("torch") and getattr(image, "is_cuda", False):
             import torch
 
@@ -117,6 +124,7 @@ class PathTracer:
         s = L.pt_render_stats()
         L.call("pt_get_render_stats", self._h, C.byref(s))
         d = {k: getattr(s, k) for k, _ in s._fields_}
+        d["kernel_ms"] = dict(zip(KERNEL_KINDS, list(s.kernel_ms)))
         d["rays"] = d["primary_rays"] + d["bounce_rays"] + d["shadow_rays"]
         return d
 
@@ -134,6 +142,41 @@ class PathTracer:
             self.close()
         except Exception:
             pass
+
+
+def rank_tile_mask(height: int, width: int, ranks: int, rank: int) -> np.ndarray:
+    """(H, W) bool: the pixels a rank renders under pt_render_options' split (row-major
+    tiles of PT_RANK_TILE_PIXELS pixels, tile k owned by rank k % ranks)."""
+    tile = np.arange(height * width, dtype=np.int64) // L.PT_RANK_TILE_PIXELS
+    return (tile % max(ranks, 1) == rank).reshape(height, width)
+
+
+def render_split(tracer, camera, samples: int, depth: int, image, seed: int = 0, mode: int = 0, clamp: float = 5.0,
+                 fp64: bool = False, group=None, dst: int | None = None):
+    """PathTracer::render split over the processes of a torch.distributed group, one GPU each
+    (the reference splits image rows over threads: System::forParallel, System.hpp:72-104,
+    called at PathTracer.cpp:186). Every rank holds the scene and the caller's image; it
+    renders its interleaved pixel tiles (the other pixels come back as 0) and one sum over
+    the ranks -- all_reduce, or reduce to rank ``dst`` -- assembles the image. Each pixel is
+    rendered whole by one rank with the one-process random stream and summation order, and
+    the other ranks add exact zeros, so the result equals a one-process render bit for bit.
+    ``image``: (H, W, C) float32 CUDA tensor or numpy array, updated in place (on every rank
+    after all_reduce, on ``dst`` after reduce). With gloo the sum runs on host copies."""
+    import torch
+    import torch.distributed as dist
+
+    ranks, rank = dist.get_world_size(group), dist.get_rank(group)
+    tracer.render(camera, samples, depth, image, seed=seed, mode=mode, clamp=clamp, fp64=fp64, ranks=ranks, rank=rank)
+    t = image if isinstance(image, torch.Tensor) else torch.from_numpy(image)
+    nccl = dist.get_backend(group) == "nccl"
+    buf = t if t.is_cuda == nccl else (t.cuda() if nccl else t.cpu())
+    if dst is None:
+        dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=group)
+    else:
+        dist.reduce(buf, dst, op=dist.ReduceOp.SUM, group=group)
+    if buf is not t:
+        t.copy_(buf)
+    return image
 
 
 def material_eval(cases):
@@ -215,9 +258,9 @@ class BatchRenderer:
                                     int(j.get("seed", 0)), ptr, wid, hgt, comp)
         return arr, bool(dev)
 
-    def render(self, jobs, mode: int = 0, clamp: float = 5.0, tuning=None) -> dict:
+    def render(self, jobs, mode: int = 0, clamp: float = 5.0, tuning=None, profile: bool = False) -> dict:
         arr, dev = self._jobs(jobs)
-        opts = L.pt_render_options(int(mode), float(clamp), 0, None)
+        opts = L.pt_render_options(int(mode), float(clamp), 0, None, 0, 0, int(bool(profile)))
         t = None if tuning is None else L.pt_batch_tuning(*(int(tuning[k]) for k in ("wave_paths", "tile_pixels",
                                                                                        "max_samples")))
         stream = None
@@ -230,6 +273,7 @@ class BatchRenderer:
         s = L.pt_render_stats()
         L.call("pt_batch_get_stats", self._h, C.byref(s))
         d = {k: getattr(s, k) for k, _ in s._fields_}
+        d["kernel_ms"] = dict(zip(KERNEL_KINDS, list(s.kernel_ms)))
         d["rays"] = d["primary_rays"] + d["bounce_rays"] + d["shadow_rays"]
         return d
 

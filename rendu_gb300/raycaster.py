@@ -191,6 +191,37 @@ class Raycaster:
         L.call("rt_prim_info", self._h, int(prim), C.byref(m), C.byref(lid))
         return m.value, lid.value
 
+    def hit_info(self, hits):
+        """(meshId, localId) of every hit of a batch (Raycaster::Hit's fields), RT_NO_HIT on
+        misses: HIT_DTYPE numpy in -> two uint32 numpy arrays; an (n,4) CUDA tensor from
+        intersect_batch -> two int32 CUDA tensors holding the uint32 bits."""
+        if _is_torch_cuda(hits):
+            import torch
+
+            n = hits.shape[0]
+            m = torch.empty(n, dtype=torch.int32, device=hits.device)
+            lid = torch.empty(n, dtype=torch.int32, device=hits.device)
+            L.call("rt_hit_info", self._h, C.c_void_p(hits.data_ptr()), n, C.c_void_p(m.data_ptr()),
+                   C.c_void_p(lid.data_ptr()), _torch_stream(), L.RT_FLAG_DEVICE_PTRS)
+            return m, lid
+        h = np.ascontiguousarray(hits)
+        m = np.empty(len(h), np.uint32)
+        lid = np.empty(len(h), np.uint32)
+        L.call("rt_hit_info", self._h, h.ctypes.data, len(h), m.ctypes.data, lid.ctypes.data, None, 0)
+        return m, lid
+
+    def status(self, stream=None) -> int:
+        """Read and clear the failures of asynchronous (device-pointer) calls ordered on
+        `stream` (the current torch stream by default): RT_OK, RT_ERR_OVERFLOW or
+        RT_ERR_TIMEOUT, as rt_get_status returns it."""
+        word = C.c_uint32()
+        st = _torch_stream() if stream is None else C.c_void_p(stream)
+        return L.lib().rt_get_status(self._h, st, C.byref(word))
+
+    def set_traversal_stack(self, entries: int):
+        """Cap the traversal stack (0 = the hierarchy's exact bound); see rt_set_traversal_stack."""
+        L.call("rt_set_traversal_stack", self._h, int(entries))
+
     def stats(self) -> dict:
         s = L.rt_stats()
         L.call("rt_get_stats", self._h, C.byref(s))

@@ -226,7 +226,7 @@ def make_sky(exr):
 if __name__ == "__main__" and "--sky" in sys.argv:
     if O.build_ref() is None:
         sys.exit("the reference tree is needed to regenerate the fixtures")
-    make_sky(os.path.join(os.environ.get("RENDU_REFERENCE_ROOT", O.REF_ROOT_DEFAULT), "resources", "common",
+    make_sky(os.path.join(O.reference_root(), "resources", "common",
                           "scattering-precomputed.exr"))
 
 

@@ -1,8 +1,7 @@
 """The C-ABI used from plain C and C++ without Python: a program that includes only
 include/rendu_gb300.h compiles as C11 and as C++17, links against the library, and gets
 status codes and messages back for invalid arguments and for a missing device (no GPU
-needed). This is the boundary a Rendu maintainer binds (INTEGRATION.md shows the C++ class
-over it)."""
+needed). This is the boundary a Rendu maintainer binds from the reference's C++ classes."""
 import os
 import shutil
 import subprocess

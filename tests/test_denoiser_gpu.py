@@ -116,7 +116,7 @@ def _features(rng, b, h, w):
     n = rng.normal(size=(b, h, w, 3))
     n /= np.linalg.norm(n, axis=-1, keepdims=True)
     return np.concatenate([rng.exponential(0.5, (b, h, w, 3)), rng.uniform(0, 1, (b, h, w, 3)), n,
-                           rng.uniform(0, 6, (b, h, w, 1))], -1).astype(np.float32)
+                           rng.uniform(0, 6, (b, h, w, 1)), rng.exponential(0.05, (b, h, w, 1))], -1).astype(np.float32)
 
 
 def test_network_structure_matches_oracle(cuda_lib):
@@ -135,17 +135,17 @@ def test_network_gradients_match_oracle(cuda_lib):
     d = Denoiser(seed=5)
     params = d.get_params()
     feats = _features(rng, 2, 64, 80)
-    # The L1 loss's gradient is sign(residual): keep every residual far from zero (below
-    # the target in red and blue, above it in green) so that the GPU and the oracle agree
-    # on every sign and the comparison measures the backward pass, not rounding near 0.
-    feats[..., 1] += 7.0
+    # Targets away from the (near-identity) output, so that the loss gradient is large
+    # against the rounding of BF16 activations.
     x_log = np.log1p(feats[..., :3].astype(np.float64))
-    target = np.expm1(x_log + np.array([1.0, -1.0, 1.0])).astype(np.float32)
+    target = np.expm1(x_log + np.array([0.5, -0.3, 0.5])).astype(np.float32)
     loss = d.backward(feats, target)
     grads = d.get_grads()
     net = OD.UNet()
     ref_loss, ref = net.backward(params, feats, target)
-    assert abs(loss - ref_loss) <= 1e-4 * ref_loss
+    # The relative squared error divides by (output + 0.01): outputs near zero magnify the
+    # BF16 rounding of the activations more than the old log-space loss did.
+    assert abs(loss - ref_loss) <= 3e-3 * ref_loss
     errs = []
     for k, l in enumerate(net.layers):
         cin = l["cin0"] + l["cin1"]
@@ -191,7 +191,7 @@ def test_denoise_pads_and_matches_oracle(cuda_lib):
     assert out.shape == (2, 37, 45, 3)
     net = OD.UNet()
     acts, y = net.forward(d.get_params(), OD.pad16(feats))
-    ref = np.maximum(np.expm1(acts[0][..., :3].astype(np.float64) + y[..., :3]), 0)[:, :37, :45]
+    ref = OD.output(OD.pad16(feats), y)[:, :37, :45]
     diff = np.abs(np.log1p(out) - np.log1p(ref))
     assert diff.max() < 0.05 and diff.mean() < 2e-3, (diff.max(), diff.mean())
     dev = d.denoise(torch.from_numpy(feats).cuda())
@@ -219,7 +219,7 @@ def test_invalid_arguments_are_rejected(cuda_lib):
     from rendu_gb300.denoiser import Denoiser
 
     d = Denoiser()
-    f = np.zeros((1, 20, 32, 10), np.float32)
+    f = np.zeros((1, 20, 32, 11), np.float32)
     t = np.zeros((1, 20, 32, 3), np.float32)
     with pytest.raises(RenduError, match="multiples of 16"):
         d.train_step(f, t, 1e-3)

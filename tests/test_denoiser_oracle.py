@@ -93,14 +93,17 @@ def test_unet_backward_matches_autograd():
             rng.normal(0, np.sqrt(2 / (9 * cin)), 9 * cin * l["cout"])
         params[l["bias_offset"]:l["bias_offset"] + l["cout"]] = rng.normal(0, 0.05, l["cout"])
     feats = np.concatenate([rng.exponential(0.5, (2, 32, 32, 3)), rng.uniform(0, 1, (2, 32, 32, 3)),
-                            rng.normal(size=(2, 32, 32, 3)), rng.uniform(0, 4, (2, 32, 32, 1))], -1).astype(np.float32)
+                            rng.normal(size=(2, 32, 32, 3)), rng.uniform(0, 4, (2, 32, 32, 1)),
+                            rng.exponential(0.05, (2, 32, 32, 1))], -1).astype(np.float32)
     target = rng.exponential(0.5, (2, 32, 32, 3)).astype(np.float32)
     loss, grads = net.backward(params, feats, target, bf16=False)
 
     x_in = OD.prepare(feats).astype(np.float64)
     y, ws = _torch_unet(net, params, x_in)
-    pred = _nchw(x_in)[:, :3] + y[:, :3]
-    lt = (pred - torch.log1p(_nchw(target))).abs().mean()
+    # output = max(exp(log(1 + radiance) + y) - 1, 0) from the float32 radiance; relative
+    # squared error with the denominator held constant
+    pred = torch.clamp(torch.expm1(torch.log1p(_nchw(feats[..., :3]).clamp(min=0.0)) + y[:, :3]), min=0.0)
+    lt = (((pred - _nchw(target)) / (pred.detach() + 0.01)) ** 2).mean()
     lt.backward()
     assert np.isclose(loss, lt.item(), rtol=1e-12)
     for k, (wt, bt) in enumerate(ws):

@@ -184,7 +184,7 @@ def test_optional_buffers_survive_graph_reuse(cuda_lib):
     sc = S.cornell_scene(3)
     tr = cuda_lib.PathTracer(sc)
     img = np.zeros((24, 24, 3), np.float32)
-    aov = np.zeros((24, 24, 7), np.float32)
+    aov = np.zeros((24, 24, 8), np.float32)
     tr.render(sc.camera, 2, 3, img, seed=1, aov=aov)
     ref_img, ref_aov = img.copy(), aov.copy()
     img64 = np.zeros_like(img)
@@ -221,7 +221,7 @@ def test_feature_buffers_and_fp64_accumulation(cuda_lib):
     sc.camera = {"eye": (0, 0, 1), "center": (0, 0, 0), "up": (0, 1, 0), "fov": 1.0, "ratio": 1.0}
     tr = cuda_lib.PathTracer(sc)
     img = np.zeros((16, 16, 3), np.float32)
-    aov = np.zeros((16, 16, 7), np.float32)
+    aov = np.zeros((16, 16, 8), np.float32)
     tr.render(sc.camera, 4, 2, img, seed=1, aov=aov)
     np.testing.assert_allclose(aov[..., 0:3], np.broadcast_to(np.float32([0.5, 0.25, 0.75]) ** np.float32(2.2),
                                                               (16, 16, 3)), rtol=1e-5)
@@ -231,9 +231,36 @@ def test_feature_buffers_and_fp64_accumulation(cuda_lib):
     t = np.tan(0.5) * ((np.arange(16) + 0.5) / 16 * 2 - 1)
     dist = 3.0 * np.sqrt(1.0 + t[None, :] ** 2 + t[:, None] ** 2)
     np.testing.assert_allclose(aov[..., 6], dist, rtol=3e-2)
+    # Every sample of a pixel carries the same radiance here: no spread, a zero standard error
+    lum = img @ np.float32([0.2126, 0.7152, 0.0722])
+    assert (aov[..., 7] <= 1e-3 * lum + 1e-7).all()
     img64 = np.zeros_like(img)
     tr.render(sc.camera, 4, 2, img64, seed=1, fp64=True)
     np.testing.assert_allclose(img64, img, rtol=1e-6, atol=1e-7)
+
+
+def test_standard_error_channel_matches_the_spread_of_independent_renders(cuda_lib):
+    """The feature buffer's standard error of the mean luminance against the spread of two
+    independent renders a and b: E[(L_a - L_b)^2] = Var(L_a) + Var(L_b). The channel is the
+    spread of the samples as if they were independent, sqrt((E[L^2] - E[L]^2) / n); with
+    n / (n - 1) it is unbiased for independent samples, and the stratified sub-pixel positions
+    (PathTracer.cpp:57-84) make the true variance of a pixel's mean somewhat smaller, so it
+    is a close upper estimate."""
+    from rendu_gb300 import scenes as S
+
+    sc = S.cornell_scene(20261203, True)
+    tr = cuda_lib.PathTracer(sc)
+    w = np.float32([0.2126, 0.7152, 0.0722])
+    out = []
+    for seed in (1, 2):
+        img = np.zeros((96, 96, 3), np.float32)
+        aov = np.zeros((96, 96, 8), np.float32)
+        tr.render(sc.camera, 16, 4, img, seed=seed, aov=aov)
+        out.append((img @ w, aov[..., 7]))
+    (la, sa), (lb, sb) = out
+    spread = np.mean((la.astype(np.float64) - lb) ** 2)
+    predicted = np.mean(sa.astype(np.float64) ** 2 + sb.astype(np.float64) ** 2) * 16 / 15
+    assert predicted > 0 and 0.7 < spread / predicted < 1.05, (spread, predicted)
 
 
 def test_sky_table_and_eval_match_port_and_reference(cuda_lib, port_lib):

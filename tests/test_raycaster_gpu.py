@@ -228,3 +228,68 @@ def test_many_meshes_and_stats(cuda_lib, port_lib):
     st = rc.stats()
     assert st["meshes"] == 200 and st["triangles"] == 100 * (320 + 12)
     assert 0 < st["nodes"] < st["triangles"] and st["leaves"] > 0
+
+
+def test_hit_info_batch_gives_reference_mesh_and_local_ids(cuda_lib):
+    """rt_hit_info: Raycaster::Hit's meshId and localId (Raycaster.cpp:177-179) for a whole
+    batch, host and device buffers, with an empty mesh between non-empty ones."""
+    import torch
+
+    g = load_golden("raycaster_small.npz")
+    meshes = golden_meshes(g)
+    empty = (np.zeros((0, 3), np.float32), np.zeros(0, np.uint32), None)
+    meshes = meshes[:2] + [empty] + meshes[2:]
+    rc = _gpu_from_meshes(cuda_lib, meshes)
+    h = rc.intersect_batch(g["rays"])
+    assert np.array_equal(h["prim"], g["hit_prim"])
+    mesh_ids, local_ids = rc.hit_info(h)
+    sizes = [len(i) // 3 for _, i, _ in meshes]
+    offs = np.cumsum([0] + sizes)
+    hit = g["hit_prim"] != NO_HIT
+    want_mesh = np.searchsorted(offs, g["hit_prim"][hit], side="right") - 1
+    # The golden ids are global over the reference's four meshes; the empty mesh shifts the
+    # later mesh ids by one and leaves the triangle numbering unchanged.
+    assert np.array_equal(mesh_ids[hit], want_mesh)
+    assert np.array_equal(local_ids[hit], 3 * (g["hit_prim"][hit] - offs[want_mesh]))
+    assert (mesh_ids[~hit] == NO_HIT).all() and (local_ids[~hit] == NO_HIT).all()
+    assert 2 not in set(mesh_ids[hit].tolist())
+    for k in np.nonzero(hit)[0][:50]:
+        assert rc.prim_info(int(h["prim"][k])) == (mesh_ids[k], local_ids[k])
+    d_hits = rc.intersect_batch(torch.from_numpy(g["rays"]).cuda())
+    dm, dl = rc.hit_info(d_hits)
+    torch.cuda.synchronize()
+    assert np.array_equal(dm.cpu().numpy().view(np.uint32), mesh_ids)
+    assert np.array_equal(dl.cpu().numpy().view(np.uint32), local_ids)
+
+
+def test_coincident_triangles_across_meshes(cuda_lib, port_lib):
+    """Thousands of identical triangles in several meshes: the clustering build merges one
+    pair per round and falls back to the radix tree after 512 rounds. The build succeeds
+    and the answers equal the C restatement's (ties go to the smaller triangle id)."""
+    from rendu_gb300 import scenes as S
+
+    tri = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]], np.float32)
+    pos = np.tile(tri, (1500, 1))
+    idx = np.arange(len(pos), dtype=np.uint32)
+    other = S.icosphere_mesh(2, seed=3)
+    meshes = [(pos, idx, None), (pos, idx, S.translation((0.0, 0.0, 0.5))), (other.positions, other.indices,
+                                                                            S.translation((2.0, 0.0, 0.0)))]
+    rc = _gpu_from_meshes(cuda_lib, meshes)
+    port = _port_from_meshes(port_lib, meshes)
+    rng = np.random.default_rng(12)
+    n = 20000
+    o = np.stack([rng.uniform(-0.5, 3.5, n), rng.uniform(-0.5, 1.5, n), np.full(n, 3.0)], 1)
+    d = np.stack([rng.uniform(-0.2, 0.2, n), rng.uniform(-0.2, 0.2, n), -np.ones(n)], 1)
+    rays = np.concatenate([o, np.full((n, 1), 1e-4), d, np.full((n, 1), 1e8)], 1).astype(np.float32)
+    h = rc.intersect_batch(rays)
+    p = port.intersect(rays)
+    _assert_closest_equal(h, p["prim"], p["t"], p["u"], p["v"], rays, port)
+    assert (h["prim"] != NO_HIT).sum() > n // 10
+    assert np.array_equal(rc.intersect_any_batch(rays), port.intersect_any(rays))
+    # Raycaster::visible's window (1e-4, |p1 - p0|) along p1 - p0, in float32 step by step.
+    p0 = rays[:, 0:3]
+    p1 = (p0 + np.float32(5.0) * rays[:, 4:7]).astype(np.float32)
+    dv = (p1 - p0).astype(np.float32)
+    ln = np.sqrt((dv[:, 0] * dv[:, 0] + dv[:, 1] * dv[:, 1]) + dv[:, 2] * dv[:, 2]).astype(np.float32)
+    seg_rays = np.concatenate([p0, np.full((n, 1), 1e-4, np.float32), dv, ln[:, None]], 1).astype(np.float32)
+    assert np.array_equal(rc.visible_batch(np.concatenate([p0, p1], 1)), 1 - port.intersect_any(seg_rays))

@@ -25,9 +25,9 @@ from conftest import GOLDEN, load_golden
 
 DEMO = os.path.join(GOLDEN, "scene_demo")
 def _ref_root():
-    from oracle.oracle import REF_ROOT_DEFAULT
+    from oracle.oracle import reference_root
 
-    return os.environ.get("RENDU_REFERENCE_ROOT", REF_ROOT_DEFAULT)
+    return reference_root()
 
 
 REF_RES = os.path.join(_ref_root(), "resources")
