@@ -494,11 +494,28 @@ def run_denoiser(cpu: bool):
     tr2.close()
     plain = [(p["render_s"], p["plain"]) for p in curve]
     den = [(p["render_s"] + p["denoise_ms"] / 1e3, p["denoised"]) for p in curve]
+    # Plain path tracing's error against the truth: e^2(N) = a / N + b, b the truth's own
+    # noise (independent renders); fitted by least squares on the measured levels, it gives
+    # the sample count -- and, at the measured seconds per sample, the time -- at which plain
+    # path tracing would reach a level beyond the measured range.
+    inv = np.array([1.0 / p["spp"] for p in curve])
+    e2 = np.array([p["plain"] ** 2 for p in curve])
+    a_fit, b_fit = np.polyfit(inv, e2, 1)
+    s_per_spp = curve[-1]["render_s"] / curve[-1]["spp"]
     levels = {}
     for thr in (0.1, 0.05, 0.02, 0.01):
         tp, td = D.time_to(plain, thr), D.time_to(den, thr)
-        levels[str(thr)] = {"plain_s": tp and round(tp, 4), "denoised_s": td and round(td, 4),
-                            "speedup": round(tp / td, 2) if tp and td else None}
+        lv = {"plain_s": tp and round(tp, 4), "denoised_s": td and round(td, 4),
+              "speedup": round(tp / td, 2) if tp and td else None}
+        if tp is None:
+            lv["plain_not_reached_by_s"] = round(plain[-1][0], 3)
+            if thr * thr > b_fit and a_fit > 0:
+                lv["plain_extrapolated_s"] = round(a_fit / (thr * thr - b_fit) * s_per_spp, 2)
+                if td:
+                    lv["speedup_extrapolated"] = round(lv["plain_extrapolated_s"] / td, 2)
+            if td:
+                lv["speedup_at_least"] = round(plain[-1][0] / td, 2)
+        levels[str(thr)] = lv
     inf_tflops = inf_flop / inf_ms / 1e9
     out = {"workload": "5-level U-Net (32-128 channels, 3x3 conv, BF16 activations, FP32 accumulation); "
                        "inference 1920x1080, training 8 x 256^2",
@@ -518,7 +535,9 @@ def run_denoiser(cpu: bool):
                        "ground_truth": f"{DN_TRUTH_SPP} spp, double-precision accumulation ({truth_s:.1f} s)",
                        "curve": [{k_: (round(v_, 5) if isinstance(v_, float) else v_) for k_, v_ in p.items()}
                                  for p in curve],
-                       "time_to_rel_rmse": levels, "eval_s": round(eval_s, 1)}}
+                       "time_to_rel_rmse": levels, "eval_s": round(eval_s, 1),
+                       "plain_error_model": {"a": round(float(a_fit), 6), "b": float(b_fit),
+                                             "truth_rel_rmse": round(float(np.sqrt(max(b_fit, 0.0))), 5)}}}
     return out
 
 

@@ -1,8 +1,10 @@
 // C-ABI of the raycaster (include/rendu_gb300.h): context life cycle, mesh intake,
 // hierarchy build, batched queries with host or device buffers.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <thread>
 
 #include "rt_context.hpp"
 
@@ -124,30 +126,93 @@ bool is_pageable(const void *p) {
     return a.type == cudaMemoryTypeUnregistered;
 }
 
+// Pageable host buffers (a caller's std::vector or numpy array): cudaMemcpyAsync from or to
+// pageable memory returns only once the copy is done, so one host thread cannot keep both
+// copy directions and the kernels busy. Here the copy-out side runs on a second host thread:
+// this thread copies chunk c in and launches its kernel, the other waits for that kernel (an
+// event) and copies the chunk's results out; ring buffer b is reused once the second thread
+// has finished chunk c - NB.
+template <class Fn>
+int host_chunked_pageable(rt_ctx *ctx, const void *h_in, size_t in_stride, size_t n, void *h_out, size_t out_stride,
+                          size_t chunk, Fn fn) {
+    constexpr int NB = rt_ctx::kRing;
+    const size_t nchunks = (n + chunk - 1) / chunk;
+    cudaStream_t sin = ctx->stream, sk = ctx->stream2, sout = ctx->stream3;
+    std::atomic<size_t> launched{0}, drained{0};
+    std::atomic<int> fail{RT_OK};
+    std::string out_msg;
+    std::thread out([&]() {
+        if (cudaSetDevice(ctx->device) != cudaSuccess) {
+            out_msg = "cudaSetDevice failed on the copy-out thread";
+            fail.store(RT_ERR_CUDA);
+            return;
+        }
+        for (size_t c = 0; c < nchunks; ++c) {
+            while (launched.load(std::memory_order_acquire) <= c) {
+                if (fail.load() != RT_OK) return;
+                std::this_thread::yield();
+            }
+            const int b = (int)(c % NB);
+            const size_t s = c * chunk, m = (n - s) < chunk ? (n - s) : chunk;
+            cudaError_t e = cudaStreamWaitEvent(sout, ctx->ev_k[b], 0);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(static_cast<char *>(h_out) + s * out_stride, ctx->ring_out[b].ptr, m * out_stride,
+                                    cudaMemcpyDeviceToHost, sout);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(sout);
+            if (e != cudaSuccess) {
+                out_msg = std::string("copy-out failed: ") + cudaGetErrorString(e);
+                fail.store(RT_ERR_CUDA);
+                return;
+            }
+            drained.store(c + 1, std::memory_order_release);
+        }
+    });
+    int r = RT_OK;
+    for (size_t c = 0; c < nchunks && r == RT_OK; ++c) {
+        const int b = (int)(c % NB);
+        while (c >= (size_t)NB && drained.load(std::memory_order_acquire) < c - NB + 1) {
+            if (fail.load() != RT_OK) break;
+            std::this_thread::yield();
+        }
+        if (fail.load() != RT_OK) break;
+        const size_t s = c * chunk, m = (n - s) < chunk ? (n - s) : chunk;
+        cudaError_t e = cudaMemcpyAsync(ctx->ring_in[b].ptr, static_cast<const char *>(h_in) + s * in_stride,
+                                        m * in_stride, cudaMemcpyHostToDevice, sin);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_in[b], sin);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(sk, ctx->ev_in[b], 0);
+        if (e != cudaSuccess) {
+            set_error(std::string("copy-in failed: ") + cudaGetErrorString(e));
+            r = RT_ERR_CUDA;
+            break;
+        }
+        r = fn(ctx->ring_in[b].ptr, m, ctx->ring_out[b].ptr, sk);
+        if (r == RT_OK && cudaEventRecord(ctx->ev_k[b], sk) != cudaSuccess) {
+            set_error("cudaEventRecord failed");
+            r = RT_ERR_CUDA;
+        }
+        if (r == RT_OK) launched.store(c + 1, std::memory_order_release);
+    }
+    if (r != RT_OK) fail.store(r);
+    out.join();
+    if (r == RT_OK && fail.load() != RT_OK) {
+        set_error(out_msg);
+        r = fail.load();
+    }
+    RT_CUDA_TRY(cudaStreamSynchronize(sk));
+    RT_CUDA_TRY(cudaStreamSynchronize(sin));
+    if (r != RT_OK) return r;
+    return check_status(ctx, sk);
+}
+
 // Runs `fn(d_in, count, d_out, stream)` over host buffers in chunks of 2M records through a
 // ring of four staging buffers and three streams: copies in on `stream`, kernels on
 // `stream2`, copies out on `stream3`, ordered by events, so that both copy directions and
 // the kernels stay busy at once (the host link, not the kernels, bounds this path). Pinned
-// host buffers get asynchronous DMA. Pageable buffers (a caller's std::vector or numpy
-// array), whose copies would not overlap, are read and written in place by the kernels
-// where the device reaches pageable memory (cudaDevAttrPageableMemoryAccess, e.g. through
-// the host's page tables on Grace), chunk after chunk on `stream2`; elsewhere they go
-// through the same staging ring.
+// host buffers get asynchronous DMA; pageable ones go through host_chunked_pageable.
 template <class Fn>
 int host_chunked(rt_ctx *ctx, const void *h_in, size_t in_stride, size_t n, void *h_out, size_t out_stride, Fn fn) {
     constexpr int NB = rt_ctx::kRing;
     const size_t chunk = size_t(1) << 21;
-    if (ctx->pageable_access && (is_pageable(h_in) || is_pageable(h_out))) {
-        int r = RT_OK;
-        for (size_t s = 0; s < n && r == RT_OK; s += chunk) {
-            const size_t m = (n - s) < chunk ? (n - s) : chunk;
-            r = fn(const_cast<char *>(static_cast<const char *>(h_in)) + s * in_stride, m,
-                   static_cast<char *>(h_out) + s * out_stride, ctx->stream2);
-        }
-        RT_CUDA_TRY(cudaStreamSynchronize(ctx->stream2));
-        if (r != RT_OK) return r;
-        return check_status(ctx, ctx->stream2);
-    }
     const size_t cn = n < chunk ? n : chunk;
     if (!ctx->stream3) RT_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream3, cudaStreamNonBlocking));
     for (int b = 0; b < NB; ++b) {
@@ -156,6 +221,8 @@ int host_chunked(rt_ctx *ctx, const void *h_in, size_t in_stride, size_t n, void
         for (cudaEvent_t *e : {&ctx->ev_in[b], &ctx->ev_k[b], &ctx->ev_out[b]})
             if (!*e) RT_CUDA_TRY(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     }
+    if (n > chunk && (is_pageable(h_in) || is_pageable(h_out)))
+        return host_chunked_pageable(ctx, h_in, in_stride, n, h_out, out_stride, chunk, fn);
     cudaStream_t sin = ctx->stream, sk = ctx->stream2, sout = ctx->stream3;
     size_t c = 0;
     int r = RT_OK;
@@ -220,12 +287,6 @@ int rt_create(rt_ctx **out, int device) {
         return RT_ERR_OOM;
     }
     cudaMemset(ctx->d_status.ptr, 0, 64);
-    int pageable = 0;
-    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
-        cudaGetLastError();
-        pageable = 0;
-    }
-    ctx->pageable_access = pageable != 0;
     *out = ctx;
     return RT_OK;
 }

@@ -57,7 +57,6 @@ struct rt_ctx {
     // stream, rt_visible_noalloc) at 32, read and cleared by rt_get_status.
     rgb::DevBuf d_status;
     uint32_t stack_cap = 0;  // rt_set_traversal_stack: 0 = the hierarchy's exact bound
-    bool pageable_access = false;  // kernels can read and write pageable host memory in place
     uint64_t n_tris = 0;
     uint64_t n_inner = 0;
     uint64_t n_leaves = 0;

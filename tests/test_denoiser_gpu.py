@@ -135,8 +135,10 @@ def test_network_gradients_match_oracle(cuda_lib):
     d = Denoiser(seed=5)
     params = d.get_params()
     feats = _features(rng, 2, 64, 80)
-    # Targets away from the (near-identity) output, so that the loss gradient is large
-    # against the rounding of BF16 activations.
+    # Radiance away from zero (the loss divides by output + 0.01, so near-black outputs would
+    # weigh the comparison towards a few pixels' BF16 rounding) and targets away from the
+    # near-identity output, so that the gradient is large against that rounding.
+    feats[..., :3] += 0.5
     x_log = np.log1p(feats[..., :3].astype(np.float64))
     target = np.expm1(x_log + np.array([0.5, -0.3, 0.5])).astype(np.float32)
     loss = d.backward(feats, target)
