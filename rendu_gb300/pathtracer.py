@@ -93,8 +93,9 @@ class PathTracer:
         ``image`` (H, W, C) float32, host array or CUDA tensor; returns ``image``.
         ``mode`` 1 selects the extended estimator (NEE on emitters and the environment
         map with MIS); ``clamp`` is the per-sample clamp (the reference's 5; <= 0: none);
-        ``fp64`` accumulates each pixel's samples in double precision; ``aov`` (H, W, 7)
-        float32 (same place as ``image``) receives first-hit albedo, normal and distance.
+        ``fp64`` accumulates each pixel's samples in double precision; ``aov`` (H, W, 8)
+        float32 (same place as ``image``) receives first-hit albedo, normal and distance
+        and the standard error of the pixel's mean luminance.
         ``ranks`` > 1 renders only the pixel tiles of ``rank`` and zeroes the others
         (pt_render_options.ranks; see render_split). ``profile`` times every kernel class
         (last_stats()["kernel_ms"]), launching the kernels without the captured graph."""

@@ -6,7 +6,7 @@ inputs, and stores inputs and outputs as compressed .npz files. The fixtures are
 the reference tree is only needed to regenerate them:
 
     python tests/golden/make_golden.py            (needs the reference tree)
-    python tests/golden/make_golden.py --renders  (reference path-tracer renders)
+    python tests/golden/make_golden.py --renders [scene ...]  (reference path-tracer renders)
     python tests/golden/make_golden.py --sky      (the sky's scattering table and MaterialSky)
     python tests/golden/make_golden.py --image    (8-bit output of renderOneShot)
     python tests/golden/make_golden.py --scene-io (scene loading: meshes, MikkTSpace,
@@ -172,28 +172,37 @@ if __name__ == "__main__" and not {"--renders", "--sky", "--image", "--scene-io"
     make_camera()
 
 
-def make_renders():
+def make_renders(names=None):
     """Renders of the reference's own PathTracer (two independent runs per scene: the
-    second calibrates the Monte-Carlo noise floor of a same-spp comparison)."""
-    out = {}
-    for name, sc, w, h, spp, depth in [
-        ("cornell", S.cornell_scene(SEED), 48, 48, 256, 5),
-        ("cornell_lit", S.cornell_scene(SEED, with_light=True), 48, 48, 256, 5),
-        ("mixed", S.feature_scene(SEED), 40, 40, 256, 4),
+    second calibrates the Monte-Carlo noise floor of a same-spp comparison). `names`
+    regenerates only those scenes and keeps the others' stored renders."""
+    path = os.path.join(HERE, "renders.npz")
+    out = dict(np.load(path)) if names and os.path.exists(path) else {}
+    for name, make, w, h, spp, depth in [
+        ("cornell", lambda: S.cornell_scene(SEED), 48, 48, 256, 5),
+        ("cornell_lit", lambda: S.cornell_scene(SEED, with_light=True), 48, 48, 256, 5),
+        ("mixed", lambda: S.feature_scene(SEED), 40, 40, 256, 4),
+        # the large path-tracer workload's scene (2,049,210 triangles in 205 meshes, cube-map
+        # sky with the sun disc, emissive quads) at a reduced size
+        ("instanced", lambda: S.instanced_scene(20261206), 160, 90, 64, 8),
     ]:
+        if names and name not in names:
+            continue
+        sc = make()
         tr = O.RefPathTracer(sc)
-        a = tr.render(sc.camera, spp, depth, w, h, seed=SEED)
-        b = tr.render(sc.camera, spp, depth, w, h, seed=SEED + 1)
+        cam = dict(sc.camera, ratio=w / h)
+        a = tr.render(cam, spp, depth, w, h, seed=SEED)
+        b = tr.render(cam, spp, depth, w, h, seed=SEED + 1)
         out[f"{name}_a"] = a
         out[f"{name}_b"] = b
         out[f"{name}_cfg"] = np.array([w, h, spp, depth], np.int32)
         tr.close()
-    np.savez_compressed(os.path.join(HERE, "renders.npz"), **out)
+    np.savez_compressed(path, **out)
     print("renders.npz:", ", ".join(k for k in out if k.endswith("_a")))
 
 
 if __name__ == "__main__" and "--renders" in sys.argv:
-    make_renders()
+    make_renders([a for a in sys.argv[sys.argv.index("--renders") + 1:] if not a.startswith("--")] or None)
 
 
 def sky_cases(n=3000, seed=SEED):

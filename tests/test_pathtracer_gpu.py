@@ -21,7 +21,8 @@ def _scene(name):
     from rendu_gb300 import scenes as S
 
     return {"cornell": lambda: S.cornell_scene(20261203), "cornell_lit": lambda: S.cornell_scene(20261203, True),
-            "mixed": lambda: S.feature_scene(20261203)}[name]()
+            "mixed": lambda: S.feature_scene(20261203),
+            "instanced": lambda: S.instanced_scene(20261206)}[name]()
 
 
 def test_material_matches_reference(cuda_lib):
@@ -39,7 +40,8 @@ def test_material_matches_reference(cuda_lib):
     assert close.mean() > 0.999, f"{(~close).sum()} of {len(close)} samples differ"
 
 
-@pytest.mark.parametrize("name,spp,depth", [("cornell", 16, 5), ("cornell_lit", 8, 5), ("mixed", 8, 4)])
+@pytest.mark.parametrize("name,spp,depth", [("cornell", 16, 5), ("cornell_lit", 8, 5), ("mixed", 8, 4),
+                                            ("instanced", 4, 8)])
 def test_render_matches_port_on_the_same_random_stream(cuda_lib, port_lib, name, spp, depth):
     sc = _scene(name)
     w, h = 64, 48
@@ -59,13 +61,16 @@ def test_render_matches_port_on_the_same_random_stream(cuda_lib, port_lib, name,
     assert abs(st["shadow_rays"] - int(port.rays[2])) <= 0.01 * port.rays[2] + 10
 
 
-@pytest.mark.parametrize("name", ["cornell", "cornell_lit", "mixed"])
+@pytest.mark.parametrize("name", ["cornell", "cornell_lit", "mixed", "instanced"])
 def test_render_matches_reference_statistically(cuda_lib, name):
+    """Against two renders of the reference's own PathTracer. "instanced" is the large
+    workload's scene itself (2,049,210 triangles in 205 meshes under a clustered hierarchy,
+    deep traversal stacks, the cube-map sky with the sun disc) at 160x90, 64 spp, depth 8."""
     g = load_golden("renders.npz")
     w, h, spp, depth = (int(x) for x in g[f"{name}_cfg"])
     sc = _scene(name)
     img = np.zeros((h, w, 3), np.float32)
-    cuda_lib.PathTracer(sc).render(sc.camera, spp, depth, img, seed=7)
+    cuda_lib.PathTracer(sc).render(dict(sc.camera, ratio=w / h), spp, depth, img, seed=7)
     assert_same_distribution(img, g[f"{name}_a"], g[f"{name}_b"])
 
 
@@ -149,7 +154,8 @@ def _ext_scene(name):
     return _scene(name)
 
 
-@pytest.mark.parametrize("name,spp,depth", [("cornell_lit", 8, 5), ("open_env", 8, 5), ("instanced_small", 4, 6)])
+@pytest.mark.parametrize("name,spp,depth", [("cornell_lit", 8, 5), ("open_env", 8, 5), ("instanced_small", 4, 6),
+                                            ("instanced", 2, 8)])
 def test_extended_render_matches_port_on_the_same_random_stream(cuda_lib, port_lib, name, spp, depth):
     sc = _ext_scene(name)
     w, h = 64, 48
