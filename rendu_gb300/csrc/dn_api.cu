@@ -302,7 +302,7 @@ int backward(dn_net *n, const float *target, cudaStream_t st) {
         in.up0 = c.up0;
         in.p1 = c.src1 >= 0 ? n->bf(c.src1) : nullptr;
         in.c1 = c.cin1;
-        r = conv_wgrad(in, n->B, H, W, gb, c.cout, n->partial.as<float>(), grads + c.woff, st);
+        r = conv_wgrad(in, n->B, H, W, gb, c.cout, n->partial.as<float>(), grads + c.woff, n->ups.as<bf16>(), st);
         if (r != RT_OK || c.src0 == 0) continue;  // no gradient for the network input
         ConvIn gi;
         gi.p0 = gb;
@@ -670,8 +670,9 @@ RT_API int dn_conv3x3_backward(const void *x0, uint32_t c0, int32_t up0, const v
         if (r != RT_OK) return r;
     }
     if (dw) {
-        void *part = nullptr;
+        void *part = nullptr, *ups = nullptr;
         RT_CUDA_TRY(cudaMallocAsync(&part, wgrad_partial_floats(P, cin, (int)cout) * sizeof(float), st));
+        if (up0) RT_CUDA_TRY(cudaMallocAsync(&ups, (size_t)P * c0 * sizeof(bf16), st));
         ConvIn in;
         in.p0 = static_cast<const bf16 *>(x0);
         in.c0 = (int)c0;
@@ -679,8 +680,9 @@ RT_API int dn_conv3x3_backward(const void *x0, uint32_t c0, int32_t up0, const v
         in.p1 = static_cast<const bf16 *>(x1);
         in.c1 = (int)c1;
         r = conv_wgrad(in, (int)batch, (int)height, (int)width, static_cast<const bf16 *>(gy), (int)cout,
-                       static_cast<float *>(part), dw, st);
+                       static_cast<float *>(part), dw, static_cast<bf16 *>(ups), st);
         cudaFreeAsync(part, st);
+        if (ups) cudaFreeAsync(ups, st);
     }
     return r;
 }

@@ -1,20 +1,14 @@
-// Denoiser kernels besides the tensor-core forward convolution (dn_umma.cu): the weight
-// gradient as an implicit GEMM on the BF16 tensor cores (mma.sync.m16n8k16, FP32
-// accumulation) fed by a 3-stage cp.async pipeline with ldmatrix fragment loads, and the
-// element-wise pieces of a U-Net's forward and backward passes (pooling, gradient routing,
-// loss, Adam). Activations are NHWC BF16.
+// Denoiser kernels besides the tensor-core convolutions (dn_umma.cu): the element-wise
+// pieces of a U-Net's forward and backward passes (input preparation, pooling, gradient
+// routing, the ReLU and bias gradients, loss, Adam) and the fixed-order reduction of the
+// weight gradient's split-K partial sums. Activations are NHWC BF16.
 //
 // Convolution input: up to two tensors concatenated along channels -- the first optionally
-// read at half resolution (nearest-neighbour 2x upsampling folded into the gather), the
-// second at full resolution (the U-Net skip connection) -- so the decoder never
-// materialises the upsampled or concatenated tensors. With off(tap) = (tap/3 - 1, tap%3 - 1):
+// at half resolution (nearest-neighbour 2x upsampling), the second at full resolution (the
+// U-Net skip connection). With off(tap) = (tap/3 - 1, tap%3 - 1):
 //   forward : out[p, co]      = act(bias[co] + sum_{tap, ci} x[p + off(tap), ci] w[tap][ci][co])
-//             GEMM M = pixels, N = Cout, K = 9 Cin (k = tap Cin + ci), zero padding.
 //   dgrad   : dx[p, ci]       = sum_{tap, co} g[p - off(tap), co] w[tap][ci][co]
-//             = the forward GEMM on g with wt[8 - tap][co][ci] = w[tap][ci][co].
 //   wgrad   : dw[tap][ci][co] = sum_p x[p + off(tap), ci] g[p, co]
-//             GEMM M = 9 Cin, N = Cout, K = pixels, split over pixel chunks and reduced in a
-//             fixed order (deterministic).
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -24,200 +18,6 @@
 namespace rgb {
 namespace dn {
 namespace {
-
-constexpr int BM = 128;  // GEMM rows per CTA (pixels for conv, taps x channels for wgrad)
-constexpr int BK = 32;   // K per pipeline stage
-constexpr int STAGES = 3;
-
-// ---- PTX wrappers ------------------------------------------------------------------------------
-__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-// 16-byte global -> shared copy; zero-filled when !valid (src is then never read).
-__device__ __forceinline__ void cp_async16(void *dst, const void *src, bool valid) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_addr(dst)), "l"(src),
-                 "r"(valid ? 16 : 0));
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
-}
-__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const void *p) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(smem_addr(p)));
-}
-__device__ __forceinline__ void ldsm_x4_t(unsigned (&r)[4], const void *p) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(smem_addr(p)));
-}
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
-// Address of channels [c, c + 8) of the (concatenated, possibly upsampled) input at pixel
-// (n, y, x) of the full-resolution grid; the caller has checked the pixel is inside.
-__device__ __forceinline__ const bf16 *in_addr(const ConvIn &in, int n, int y, int x, int H, int W, int c) {
-    if (c < in.c0) {
-        const int h0 = H >> in.up0, w0 = W >> in.up0;
-        return in.p0 + (((size_t)n * h0 + (y >> in.up0)) * w0 + (x >> in.up0)) * in.c0 + c;
-    }
-    return in.p1 + (((size_t)n * H + y) * W + x) * in.c1 + (c - in.c0);
-}
-
-// One warp's MI x NI tile of m16n8 accumulators over a BK slice held in shared memory.
-// A_TRANS: A stored [k][m] (wgrad) instead of [m][k] (conv). B is stored [k][n].
-template <int MI, int NI, bool A_TRANS, int LDA, int LDB>
-__device__ __forceinline__ void warp_mma(float (&acc)[MI][NI][4], const bf16 *a, const bf16 *b, int wm0, int wn0,
-                                         int lane) {
-#pragma unroll
-    for (int kk = 0; kk < BK / 16; ++kk) {
-        unsigned af[MI][4], bfr[NI][2];
-#pragma unroll
-        for (int mi = 0; mi < MI; ++mi) {
-            if (A_TRANS) {
-                const int i = lane >> 3, r = lane & 7;
-                ldsm_x4_t(af[mi], a + (kk * 16 + r + (i >> 1) * 8) * LDA + wm0 + mi * 16 + (i & 1) * 8);
-            } else {
-                ldsm_x4(af[mi], a + (wm0 + mi * 16 + (lane & 15)) * LDA + kk * 16 + (lane >> 4) * 8);
-            }
-        }
-#pragma unroll
-        for (int nj = 0; nj < NI / 2; ++nj) {
-            unsigned t[4];
-            ldsm_x4_t(t, b + (kk * 16 + (lane & 15)) * LDB + wn0 + nj * 16 + (lane >> 4) * 8);
-            bfr[2 * nj][0] = t[0];
-            bfr[2 * nj][1] = t[1];
-            bfr[2 * nj + 1][0] = t[2];
-            bfr[2 * nj + 1][1] = t[3];
-        }
-#pragma unroll
-        for (int mi = 0; mi < MI; ++mi)
-#pragma unroll
-            for (int ni = 0; ni < NI; ++ni) mma_bf16(acc[mi][ni], af[mi], bfr[ni][0], bfr[ni][1]);
-    }
-}
-
-template <int BN, int WARPS_M, int WARPS_N>
-struct Tile {
-    static constexpr int NT = 32 * WARPS_M * WARPS_N;
-    static constexpr int WM = BM / WARPS_M, WN = BN / WARPS_N;
-    static constexpr int MI = WM / 16, NI = WN / 8;
-    static constexpr int LDB = BN + 8;
-    static_assert(WM % 16 == 0 && WN % 16 == 0, "warp tile must be a multiple of 16x16");
-};
-
-// ---- weight gradient -------------------------------------------------------------------------------
-template <int BN, int WARPS_M, int WARPS_N>
-__global__ void __launch_bounds__(32 * WARPS_M *WARPS_N)
-    k_wgrad(ConvIn in, int B, int H, int W, const bf16 *__restrict__ g, int Cout, long chunk,
-            float *__restrict__ partial) {
-    using T = Tile<BN, WARPS_M, WARPS_N>;
-    constexpr int NT = T::NT, LDA = BM + 8, LDB = T::LDB;
-    constexpr int A_ITER = BK * BM / 8 / NT;
-    constexpr int B_CHUNKS = BK * BN / 8;
-    extern __shared__ __align__(128) unsigned char smem[];
-    bf16 *sA = reinterpret_cast<bf16 *>(smem);
-    bf16 *sB = sA + STAGES * BK * LDA;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = warp / WARPS_N, wn = warp % WARPS_N;
-    const long HW = (long)H * W, P = (long)B * HW;
-    const int Cin = in.c0 + in.c1, M = 9 * Cin;
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.z * BN;
-    const long pbeg = (long)blockIdx.x * chunk, pend = min(P, pbeg + chunk);
-    const int KT = (int)((pend - pbeg + BK - 1) / BK);
-
-    // A gather: this thread copies m-group mg (8 rows of M: one tap, 8 channels) for the
-    // pixels tid/16 + i NT/16 of each stage.
-    const int mg = tid & 15;
-    const int m = m0 + mg * 8;
-    const bool mvalid = m < M;
-    const int tap = mvalid ? m / Cin : 0, ci = m - tap * Cin;
-    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-    long pp[A_ITER];
-    int pn[A_ITER], py[A_ITER], px[A_ITER];
-#pragma unroll
-    for (int i = 0; i < A_ITER; ++i) {
-        pp[i] = pbeg + (tid >> 4) + i * (NT / 16);
-        const long q = min(pp[i], P - 1);
-        pn[i] = (int)(q / HW);
-        const long r = q - (long)pn[i] * HW;
-        py[i] = (int)(r / W);
-        px[i] = (int)(r - (long)py[i] * W);
-    }
-
-    auto load_stage = [&](int stage, long pk) {
-        bf16 *a = sA + stage * BK * LDA;
-#pragma unroll
-        for (int i = 0; i < A_ITER; ++i) {
-            const int row = (tid >> 4) + i * (NT / 16);
-            const int yy = py[i] + dy, xx = px[i] + dx;
-            const bool v = mvalid && pp[i] < pend && yy >= 0 && yy < H && xx >= 0 && xx < W;
-            const bf16 *src = v ? in_addr(in, pn[i], yy, xx, H, W, ci) : in.p0;
-            cp_async16(a + row * LDA + mg * 8, src, v);
-            // advance this row's pixel by BK
-            pp[i] += BK;
-            px[i] += BK;
-            while (px[i] >= W) px[i] -= W, ++py[i];
-            while (py[i] >= H) py[i] -= H, ++pn[i];
-        }
-        bf16 *b = sB + stage * BK * LDB;
-        for (int q = tid; q < B_CHUNKS; q += NT) {
-            const int kr = q / (BN / 8), c8 = (q % (BN / 8)) * 8;
-            const long p = pk + kr;
-            const int co = n0 + c8;
-            const bool v = p < pend && co < Cout;
-            cp_async16(b + kr * LDB + c8, v ? g + p * Cout + co : g, v);
-        }
-    };
-
-    float acc[T::MI][T::NI][4];
-#pragma unroll
-    for (int mi = 0; mi < T::MI; ++mi)
-#pragma unroll
-        for (int ni = 0; ni < T::NI; ++ni)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) acc[mi][ni][e] = 0.0f;
-
-#pragma unroll
-    for (int s = 0; s < STAGES - 1; ++s) {
-        if (s < KT) load_stage(s, pbeg + (long)s * BK);
-        cp_commit();
-    }
-    for (int kt = 0; kt < KT; ++kt) {
-        cp_wait<STAGES - 2>();
-        __syncthreads();
-        const int nk = kt + STAGES - 1;
-        if (nk < KT) load_stage(nk % STAGES, pbeg + (long)nk * BK);
-        cp_commit();
-        const int st = kt % STAGES;
-        warp_mma<T::MI, T::NI, true, LDA, LDB>(acc, sA + st * BK * LDA, sB + st * BK * LDB, wm * T::WM, wn * T::WN,
-                                                lane);
-    }
-    cp_wait<0>();
-
-    float *dst = partial + (size_t)blockIdx.x * M * Cout;
-    const int gq = lane >> 2, tq = lane & 3;
-#pragma unroll
-    for (int mi = 0; mi < T::MI; ++mi)
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int r = m0 + wm * T::WM + mi * 16 + gq + h * 8;
-            if (r >= M) continue;
-#pragma unroll
-            for (int ni = 0; ni < T::NI; ++ni) {
-                const int co = n0 + wn * T::WN + ni * 8 + tq * 2;
-                if (co >= Cout) continue;
-                *reinterpret_cast<float2 *>(dst + (size_t)r * Cout + co) =
-                    make_float2(acc[mi][ni][2 * h], acc[mi][ni][2 * h + 1]);
-            }
-        }
-}
 
 // out[i] = sum over chunks of partial[c][i], in chunk order (deterministic).
 __global__ void k_reduce_chunks(const float *__restrict__ partial, int chunks, size_t n, float *__restrict__ out) {
@@ -541,90 +341,13 @@ __global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float
 
 inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
-// ---- tile selection ------------------------------------------------------------------------------
-// Output-channel tile: the candidate minimising tiles x BN + 32 x tiles, i.e. MMA work on
-// padded channels plus one re-gather of the activations per tile.
-int pick_bn(int N) {
-    static const int cand[] = {16, 32, 48, 64, 96, 128};
-    int best = 128, bestc = 1 << 30;
-    for (int bn : cand) {
-        const int tiles = (N + bn - 1) / bn;
-        const int c = tiles * bn + 32 * tiles;
-        if (c < bestc) bestc = c, best = bn;
-    }
-    return best;
-}
-
-template <int BN>
-constexpr size_t wgrad_smem() {
-    return (size_t)STAGES * (BK * (BM + 8) + BK * (BN + 8)) * sizeof(bf16);
-}
-
-struct WgradPlan {
-    int bn, mtiles, ntiles, chunks;
-    long chunk;
-};
-
-// Pixel chunks of the split-K weight gradient: about four CTAs per SM in total, at least
-// 256 pixels per chunk, chunk lengths a multiple of BK.
-WgradPlan wgrad_plan(long P, int Cin, int Cout) {
-    WgradPlan p;
-    p.bn = pick_bn(Cout);
-    p.mtiles = (9 * Cin + BM - 1) / BM;
-    p.ntiles = (Cout + p.bn - 1) / p.bn;
-    const long tiles = (long)p.mtiles * p.ntiles;
-    const long target = (4L * 152 + tiles - 1) / tiles;
-    const long chunks = std::max(1L, std::min(target, (P + 255) / 256));
-    long chunk = (P + chunks - 1) / chunks;
-    chunk = (chunk + BK - 1) / BK * BK;
-    p.chunk = chunk;
-    p.chunks = (int)((P + chunk - 1) / chunk);
-    return p;
-}
-
-template <int BN, int WARPS_M, int WARPS_N>
-int launch_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, const WgradPlan &pl, float *partial,
-                 cudaStream_t st) {
-    constexpr size_t smem = wgrad_smem<BN>();
-    static bool attr = false;
-    if (!attr) {
-        RT_CUDA_TRY(cudaFuncSetAttribute(k_wgrad<BN, WARPS_M, WARPS_N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem));
-        attr = true;
-    }
-    const dim3 grid((unsigned)pl.chunks, (unsigned)pl.mtiles, (unsigned)pl.ntiles);
-    k_wgrad<BN, WARPS_M, WARPS_N><<<grid, 32 * WARPS_M * WARPS_N, smem, st>>>(in, B, H, W, g, Cout, pl.chunk, partial);
-    RT_CUDA_TRY(cudaGetLastError());
-    return RT_OK;
-}
-
 constexpr long kReluRows = 128;  // rows per block of the fused ReLU / bias-gradient pass
 
 }  // namespace
 
 // ---- launchers -------------------------------------------------------------------------------
-size_t wgrad_partial_floats(long P, int Cin, int Cout) {
-    const WgradPlan pl = wgrad_plan(P, Cin, Cout);
-    return (size_t)pl.chunks * 9 * Cin * Cout;
-}
-
-int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, float *partial, float *dw,
-               cudaStream_t st) {
-    const long P = (long)B * H * W;
-    const int Cin = in.c0 + in.c1;
-    const WgradPlan pl = wgrad_plan(P, Cin, Cout);
-    int rc;
-    switch (pl.bn) {
-        case 16: rc = launch_wgrad<16, 4, 1>(in, B, H, W, g, Cout, pl, partial, st); break;
-        case 32: rc = launch_wgrad<32, 4, 1>(in, B, H, W, g, Cout, pl, partial, st); break;
-        case 48: rc = launch_wgrad<48, 4, 1>(in, B, H, W, g, Cout, pl, partial, st); break;
-        case 64: rc = launch_wgrad<64, 2, 2>(in, B, H, W, g, Cout, pl, partial, st); break;
-        case 96: rc = launch_wgrad<96, 4, 2>(in, B, H, W, g, Cout, pl, partial, st); break;
-        default: rc = launch_wgrad<128, 4, 2>(in, B, H, W, g, Cout, pl, partial, st); break;
-    }
-    if (rc != RT_OK) return rc;
-    const size_t n = (size_t)9 * Cin * Cout;
-    k_reduce_chunks<<<blocks(n), 256, 0, st>>>(partial, pl.chunks, n, dw);
+int reduce_chunks(const float *partial, int chunks, size_t n, float *out, cudaStream_t st) {
+    k_reduce_chunks<<<blocks(n), 256, 0, st>>>(partial, chunks, n, out);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

@@ -65,10 +65,14 @@ int pack_weights_bf16(const bf16 *w, int c0, int c1, int Cout, bf16 *wpk, cudaSt
 int pack_all(const float *params, const PackTable &tab, bf16 *wk, bf16 *wkd, cudaStream_t st);
 // RT_ERR_TIMEOUT if a tensor-core convolution's bounded wait gave up (synchronous).
 int umma_status(bool clear);
-// dw[tap][ci][co] = sum_p in[p + off(tap), ci] * g[p, co]; partial holds wgrad_partial_floats().
-int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, float *partial, float *dw,
+// dw[tap][ci][co] = sum_p in[p + off(tap), ci] * g[p, co] on the tensor cores (dn_umma.cu);
+// partial holds wgrad_partial_floats() floats; an upsampled input 0 is first expanded into
+// `ups` (B x H x W x c0 BF16).
+int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, float *partial, float *dw, bf16 *ups,
                cudaStream_t st);
 size_t wgrad_partial_floats(long P, int Cin, int Cout);
+// out[i] = sum_{c < chunks} partial[c n + i], in chunk order.
+int reduce_chunks(const float *partial, int chunks, size_t n, float *out, cudaStream_t st);
 // Scratch floats of relu_grad_bias's bias-gradient partials.
 size_t colsum_partial_floats(long P, int C);
 int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st);

@@ -906,6 +906,232 @@ __global__ void k_pack_all(const float *__restrict__ params, PackTable tab, bf16
     }
 }
 
+// ---- weight gradient ----------------------------------------------------------------------------
+// dw[tap][ci][co] = sum_p x[p + off(tap), ci] g[p, co] on the tensor cores: per tap an implicit
+// GEMM D[co][ci] += G^T X_tap whose K runs over pixels. Both operands are read as TMA boxes of
+// 64 channels x 64 pixels (one 128-byte row per pixel, 128-byte swizzle): channels are the
+// contiguous (M or N) dimension, so both go to tcgen05.mma in the MN-major layout (atoms of
+// 64 channels x 8 pixel rows; 8-row groups 1024 bytes apart, 64-channel atoms a box apart).
+// The box of tap (dy, dx) starts at the tile's pixel (x0 + dx, y0 + dy): the copy engine's zero
+// fill outside the image is the convolution's zero padding, and pixels of the tile outside
+// the image have G = 0 and add nothing.
+//
+// A CTA owns a group of taps (all 9 when the input is at most 48 channels, else one kernel
+// row dy), a group of 64-channel input atoms (at most two when taps are grouped by row) and a
+// contiguous range of 64-pixel tiles (split K): its accumulators, one per tap, fill at most
+// 512 TMEM columns. One thread issues the TMA loads into a ring of stages, one thread the
+// MMAs (for every 16-pixel step one MMA per tap, M = 64 or 128 output channels, N = the
+// atoms' channels), and the four warps then read the accumulators back with tcgen05.ld and
+// store FP32 partial sums per tile range, which k_reduce_chunks adds in a fixed order.
+// (TMEM rows: an M = 128 accumulator holds row r in lane r; an M = 64 one holds rows
+// 16i..16i+15 in lanes 32i..32i+15.)
+constexpr int WG_KC = 64;                        // pixels per tile (one box)
+constexpr unsigned WG_BOX = WG_KC * 128;         // bytes of one 64-channel box
+constexpr int WG_MAX_STAGES = 4;
+
+struct WgradTiles {
+    int B, H, W, Wb, Hb, tx, ty, tiles;  // 64-pixel tiles of Wb x Hb pixels
+    int Cout, M, ma, mgroups;            // output channels, MMA M (64 or 128), G atoms per
+                                         // CTA, groups of 128 output channels
+    int c0, c1, seg0, atoms;             // input channels, atoms of input 0, atoms in total
+    int T, ag, N, cols;                  // taps per CTA, atoms per CTA, MMA N, TMEM columns
+    int tiles_per_chunk, stages;
+    float *partial;                      // [chunk][tap][ci][co]
+};
+
+__device__ __forceinline__ unsigned long long sdesc_mn(unsigned addr) {
+    return (unsigned long long)((addr & 0x3FFFFu) >> 4) |    // start address
+           ((unsigned long long)(WG_BOX >> 4) << 16) |      // leading byte offset: next 64-channel atom
+           ((unsigned long long)(1024 >> 4) << 32) |        // stride byte offset: next 8 pixel rows
+           (1ull << 46) | (2ull << 61);                     // version, 128-byte swizzle
+}
+
+// kind::f16, BF16 A and B both MN-major, FP32 D, M x N.
+__device__ __forceinline__ unsigned idesc_mn(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) | ((unsigned)(n >> 3) << 17) |
+           ((unsigned)(m >> 4) << 24);
+}
+
+__global__ void __launch_bounds__(128, 1)
+    k_wgrad_umma(const __grid_constant__ CUtensorMap tmg, const __grid_constant__ CUtensorMap tm0,
+                 const __grid_constant__ CUtensorMap tm1, const WgradTiles q) {
+    extern __shared__ unsigned char smem_raw[];
+    const unsigned raw = saddr(smem_raw);
+    const unsigned base = (raw + 1023u) & ~1023u;
+    const unsigned a_bytes = (unsigned)q.ma * WG_BOX, b_tap = (unsigned)q.ag * WG_BOX;
+    const unsigned stage_bytes = a_bytes + (unsigned)q.T * b_tap;
+    const int S = q.stages;
+    const unsigned bar0 = base + S * stage_bytes;
+    auto full = [&](int st) { return bar0 + 8u * st; };
+    auto empty = [&](int st) { return bar0 + 8u * (WG_MAX_STAGES + st); };
+    const unsigned done = bar0 + 8u * (2 * WG_MAX_STAGES);
+    const unsigned tmem_slot = done + 8u;
+    const unsigned *tmem_slot_ptr = reinterpret_cast<const unsigned *>(smem_raw + (tmem_slot - raw));
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int chunk = blockIdx.x, tap0 = blockIdx.y * q.T;
+    const int mg = (int)blockIdx.z % q.mgroups, atom0 = ((int)blockIdx.z / q.mgroups) * q.ag;
+    const int t_begin = chunk * q.tiles_per_chunk;
+    const int t_end = min(q.tiles, t_begin + q.tiles_per_chunk);
+    const int my_tiles = max(0, t_end - t_begin);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(tmem_slot),
+                     "r"(q.cols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+    }
+    if (tid == 0) {
+        for (int st = 0; st < S; ++st) {
+            mbar_init(full(st), 1);
+            mbar_init(empty(st), 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    const unsigned tmem = *tmem_slot_ptr;
+    bool ok = true;
+
+    if (tid == 0 && my_tiles > 0) {
+        // TMA producer
+        const unsigned bytes = stage_bytes;
+        for (int k = 0; k < my_tiles && ok; ++k) {
+            const int st = k % S;
+            if (k >= S && !mbar_wait(empty(st), (unsigned)((k / S - 1) & 1))) {
+                ok = false;
+                break;
+            }
+            const int t = t_begin + k;
+            const int x0 = (t % q.tx) * q.Wb;
+            const int r = t / q.tx;
+            const int y0 = (r % q.ty) * q.Hb, n = r / q.ty;
+            const unsigned sa = base + st * stage_bytes;
+            mbar_expect_tx(full(st), bytes);
+            for (int a = 0; a < q.ma; ++a) tma_4d(sa + a * WG_BOX, &tmg, 128 * mg + 64 * a, x0, y0, n, full(st));
+            for (int j = 0; j < q.T; ++j) {
+                const int tap = tap0 + j, dy = tap / 3 - 1, dx = tap % 3 - 1;
+                const unsigned sb = sa + a_bytes + j * b_tap;
+                for (int i = 0; i < q.ag; ++i) {
+                    const int atom = atom0 + i;
+                    if (atom < q.seg0)
+                        tma_4d(sb + i * WG_BOX, &tm0, 64 * atom, x0 + dx, y0 + dy, n, full(st));
+                    else
+                        tma_4d(sb + i * WG_BOX, &tm1, 64 * (atom - q.seg0), x0 + dx, y0 + dy, n, full(st));
+                }
+            }
+        }
+    } else if (tid == 32 && my_tiles > 0) {
+        // MMA issuer
+        const unsigned id = idesc_mn(q.M, q.N);
+        for (int k = 0; k < my_tiles && ok; ++k) {
+            const int st = k % S;
+            if (!mbar_wait(full(st), (unsigned)((k / S) & 1))) {
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+            const unsigned sa = base + st * stage_bytes;
+#pragma unroll 1
+            for (int ks = 0; ks < WG_KC / 16; ++ks) {
+                const unsigned long long da = sdesc_mn(sa + ks * 2048);
+                for (int j = 0; j < q.T; ++j) {
+                    const unsigned long long db = sdesc_mn(sa + a_bytes + j * b_tap + ks * 2048);
+                    umma(tmem + (unsigned)(j * q.N), da, db, id, (k > 0 || ks > 0) ? 1u : 0u);
+                }
+            }
+            umma_commit(empty(st));
+        }
+        if (ok) umma_commit(done);
+    }
+    // Epilogue: all four warps; warp w reads TMEM lanes 32w..32w+31. With M = 128 they hold
+    // output channels 32w..32w+31; with M = 64 the accumulator takes the first 16 lanes of
+    // each 32-lane quarter (channels 16w..16w+15).
+    const int rows = q.M == 64 ? 16 : 32;
+    const int co = 128 * mg + rows * warp + lane;
+    const bool row_ok = lane < rows && co < q.Cout;
+    const int cin = q.c0 + q.c1;
+    float *part = q.partial + (size_t)chunk * 9 * cin * q.Cout;
+    bool have = my_tiles > 0;
+    if (have) {
+        have = __all_sync(0xffffffffu, mbar_wait(done, 0));
+        if (!have) ok = false;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+    }
+    {
+        for (int j = 0; j < q.T; ++j) {
+            const int tap = tap0 + j;
+            for (int c = 0; c < q.N; c += 16) {
+                unsigned v[16];
+                if (have) {
+                    tmem_ld16(tmem + ((unsigned)(32 * warp) << 16) + (unsigned)(j * q.N + c), v);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                }
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const int col = c + e, atom = atom0 + col / 64, off = col % 64;
+                    int ci = -1;
+                    if (atom < q.seg0) {
+                        if (64 * atom + off < q.c0) ci = 64 * atom + off;
+                    } else if (atom < q.atoms) {
+                        const int c1 = 64 * (atom - q.seg0) + off;
+                        if (c1 < q.c1) ci = q.c0 + c1;
+                    }
+                    if (ci >= 0 && row_ok)
+                        part[((size_t)tap * cin + ci) * q.Cout + co] = have ? __uint_as_float(v[e]) : 0.0f;
+                }
+            }
+        }
+    }
+    if (!ok && lane == 0) atomicOr(&g_umma_status, 1u);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(q.cols));
+}
+
+// Split of the weight gradient: tap and atom groups per CTA, 64-pixel tiles, tiles per CTA.
+WgradTiles wgrad_tiles(int B, int H, int W, int c0, int c1, int Cout) {
+    WgradTiles q{};
+    q.B = B;
+    q.H = H;
+    q.W = W;
+    q.Wb = 1;
+    while (q.Wb < W && q.Wb < WG_KC) q.Wb *= 2;
+    q.Hb = WG_KC / q.Wb;
+    q.tx = (W + q.Wb - 1) / q.Wb;
+    q.ty = (H + q.Hb - 1) / q.Hb;
+    q.tiles = B * q.tx * q.ty;
+    q.Cout = Cout;
+    q.M = Cout <= 64 ? 64 : 128;
+    q.ma = q.M / 64;
+    q.mgroups = (Cout + 127) / 128;
+    q.c0 = c0;
+    q.c1 = c1;
+    q.seg0 = (c0 + 63) / 64;
+    q.atoms = q.seg0 + (c1 + 63) / 64;
+    if (q.atoms == 1 && c0 + c1 <= 48) {
+        q.T = 9;  // every tap in one CTA: 9 x N <= 432 columns
+        q.ag = 1;
+        q.N = (c0 + c1 + 15) / 16 * 16;
+    } else {
+        q.T = 3;  // one kernel row per CTA, at most two atoms: 3 x 128 columns
+        q.ag = std::min(2, q.atoms);
+        q.N = q.atoms == 1 ? (c0 + c1 + 15) / 16 * 16 : 64 * q.ag;
+    }
+    q.cols = 32;
+    while (q.cols < q.T * q.N) q.cols *= 2;
+    const int groups = (9 / q.T) * ((q.atoms + q.ag - 1) / q.ag) * q.mgroups;
+    // About two CTAs per SM in total, but at least 16 tiles (1,024 pixels) per CTA: every
+    // CTA writes 9 x Cin x Cout partial sums, which must stay small against its MMA work.
+    const int target = 2 * 152;
+    int chunks = std::max(1, std::min((q.tiles + 15) / 16, (target + groups - 1) / groups));
+    q.tiles_per_chunk = (q.tiles + chunks - 1) / chunks;
+    const unsigned stage = (unsigned)(q.ma + q.T * q.ag) * WG_BOX;
+    q.stages = (int)std::min<size_t>(WG_MAX_STAGES, (200 * 1024) / stage);
+    return q;
+}
+
 // ---- host: tensor maps ---------------------------------------------------------------------------
 typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
@@ -1107,6 +1333,53 @@ int pack_all(const float *params, const PackTable &tab, bf16 *wk, bf16 *wkd, cud
     k_pack_all<<<blocks(tab.fwd_total + tab.bwd_total), 256, 0, st>>>(params, tab, wk, wkd);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
+}
+
+// Scratch floats of conv_wgrad's partial sums: at most ceil(2 x 152 / CTA groups) tile ranges
+// (one CTA group when the input is at most 48 channels of one atom, at least three otherwise).
+size_t wgrad_partial_floats(long P, int Cin, int Cout) {
+    (void)P;
+    const int groups = Cin <= 48 ? 1 : 3;
+    return (size_t)((2 * 152 + groups - 1) / groups) * 9 * Cin * Cout;
+}
+
+int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, float *partial, float *dw, bf16 *ups,
+               cudaStream_t st) {
+    const bf16 *src0 = in.p0;
+    if (in.up0) {
+        if (!ups) {
+            set_error("an upsampled convolution input needs scratch space");
+            return RT_ERR_ARG;
+        }
+        const size_t n8 = (size_t)B * (H / 2) * (W / 2) * (in.c0 / 8);
+        k_upsample2<<<blocks(n8), 256, 0, st>>>(in.p0, B, H / 2, W / 2, in.c0, ups);
+        RT_CUDA_TRY(cudaGetLastError());
+        src0 = ups;
+    }
+    WgradTiles q = wgrad_tiles(B, H, W, in.c0, in.c1, Cout);
+    q.partial = partial;
+    CUtensorMap tmg, tm0, tm1;
+    int r = map_activations(&tmg, g, B, H, W, Cout, q.Wb, q.Hb, false);
+    if (r == RT_OK) r = map_activations(&tm0, src0, B, H, W, in.c0, q.Wb, q.Hb, false);
+    if (r == RT_OK) {
+        if (in.c1)
+            r = map_activations(&tm1, in.p1, B, H, W, in.c1, q.Wb, q.Hb, false);
+        else
+            tm1 = tm0;
+    }
+    if (r != RT_OK) return r;
+    static bool configured = false;
+    if (!configured) {
+        RT_CUDA_TRY(cudaFuncSetAttribute(k_wgrad_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
+        configured = true;
+    }
+    const size_t stage = (size_t)(q.ma + q.T * q.ag) * WG_BOX;
+    const size_t smem = 1024 + q.stages * stage + 8 * (2 * WG_MAX_STAGES + 2);
+    const int chunks = (q.tiles + q.tiles_per_chunk - 1) / q.tiles_per_chunk;
+    const dim3 grid((unsigned)chunks, (unsigned)(9 / q.T), (unsigned)((q.atoms + q.ag - 1) / q.ag * q.mgroups));
+    k_wgrad_umma<<<grid, 128, smem, st>>>(tmg, tm0, tm1, q);
+    RT_CUDA_TRY(cudaGetLastError());
+    return reduce_chunks(partial, chunks, (size_t)9 * (in.c0 + in.c1) * Cout, dw, st);
 }
 
 int umma_status(bool clear) {
