@@ -28,6 +28,27 @@ __global__ void k_reduce_chunks(const float *__restrict__ partial, int chunks, s
     out[i] = s;
 }
 
+// The same sum for many chunks: a block of 32 x 8 threads takes 32 consecutive outputs; thread
+// row r sums chunks r, r + 8, ... (each warp reads 128 contiguous bytes per chunk), then the
+// eight row sums are added in row order (deterministic).
+__global__ void k_reduce_chunks_tiled(const float *__restrict__ partial, int chunks, size_t n,
+                                      float *__restrict__ out) {
+    __shared__ float red[8][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const size_t i = blockIdx.x * (size_t)32 + tx;
+    float s = 0.0f;
+    if (i < n)
+        for (int c = ty; c < chunks; c += 8) s += partial[(size_t)c * n + i];
+    red[ty][tx] = s;
+    __syncthreads();
+    if (ty == 0 && i < n) {
+        float t = red[0][tx];
+#pragma unroll
+        for (int r = 1; r < 8; ++r) t += red[r][tx];
+        out[i] = t;
+    }
+}
+
 // ReLU gradient and bias-gradient partials in one pass over a (P x C) FP32 gradient, 4
 // channels a thread (C a multiple of 4, C <= 1024): rows [chunk b, chunk (b + 1)) per block;
 // g is zeroed where the forward output y was not positive (relu), gb receives its BF16 copy,
@@ -347,7 +368,12 @@ constexpr long kReluRows = 128;  // rows per block of the fused ReLU / bias-grad
 
 // ---- launchers -------------------------------------------------------------------------------
 int reduce_chunks(const float *partial, int chunks, size_t n, float *out, cudaStream_t st) {
-    k_reduce_chunks<<<blocks(n), 256, 0, st>>>(partial, chunks, n, out);
+    // Many chunks: blocks of 32 outputs x 8 chunk rows; few: a thread per output. Both orders
+    // are fixed, so the result is deterministic.
+    if (chunks >= 16)
+        k_reduce_chunks_tiled<<<(unsigned)((n + 31) / 32), 256, 0, st>>>(partial, chunks, n, out);
+    else
+        k_reduce_chunks<<<blocks(n), 256, 0, st>>>(partial, chunks, n, out);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

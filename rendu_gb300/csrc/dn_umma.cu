@@ -907,59 +907,70 @@ __global__ void k_pack_all(const float *__restrict__ params, PackTable tab, bf16
 }
 
 // ---- weight gradient ----------------------------------------------------------------------------
-// dw[tap][ci][co] = sum_p x[p + off(tap), ci] g[p, co] on the tensor cores: per tap an implicit
-// GEMM D[co][ci] += G^T X_tap whose K runs over pixels. Both operands are read as TMA boxes of
-// 64 channels x 64 pixels (one 128-byte row per pixel, 128-byte swizzle): channels are the
-// contiguous (M or N) dimension, so both go to tcgen05.mma in the MN-major layout (atoms of
-// 64 channels x 8 pixel rows; 8-row groups 1024 bytes apart, 64-channel atoms a box apart).
-// The box of tap (dy, dx) starts at the tile's pixel (x0 + dx, y0 + dy): the copy engine's zero
-// fill outside the image is the convolution's zero padding, and pixels of the tile outside
-// the image have G = 0 and add nothing.
+// dw[tap][ci][co] = sum_p x[p + off(tap), ci] g[p, co] on the tensor cores, as implicit GEMMs
+//   D[(tap, ci)][co] += sum_p X_tap[p][ci] G[p][co]
+// whose K runs over pixels. The input is cut into "atoms" of AW channels (64, or 32 where that
+// needs fewer M tiles): a slot is one (tap, atom) pair, and an M tile of 128 rows holds
+// 128 / AW consecutive slots. Both operands are TMA boxes of one atom (or of 64 output
+// channels) x 64 pixels -- one 128- or 64-byte row per pixel with the matching swizzle --
+// which tcgen05.mma reads in the MN-major layout: channels contiguous, 8-pixel row groups
+// 1024 (512) bytes apart, atoms one box apart. The box of tap (dy, dx) starts at the tile's
+// pixel (x0 + dx, y0 + dy): the copy engine's zero fill outside the image is the
+// convolution's zero padding, and pixels of the tile outside the image have G = 0.
+// Putting taps and channels into M and the output channels into N makes every MMA 128 x
+// Cout x 16: on the GB300 an MMA of these narrow layers costs about the same whatever its
+// size, so few wide ones are what pays (9 taps of a 32-channel input: 3 MMAs per 16 pixels).
+// Row tiles of 32-channel atoms ("rows3") go further: one box of 68 pixels from x0 - 1 per
+// (kernel row, atom) holds the three horizontal taps, and an M tile reads it from pixel rows
+// 0, 1, 2 (and an unused 3) as its four 32-row atoms, 64 bytes apart: a third of the boxes.
 //
-// A CTA owns a group of taps (all 9 when the input is at most 48 channels, else one kernel
-// row dy), a group of 64-channel input atoms (at most two when taps are grouped by row) and a
-// contiguous range of 64-pixel tiles (split K): its accumulators, one per tap, fill at most
-// 512 TMEM columns. One thread issues the TMA loads into a ring of stages, one thread the
-// MMAs (for every 16-pixel step one MMA per tap, M = 64 or 128 output channels, N = the
-// atoms' channels), and the four warps then read the accumulators back with tcgen05.ld and
-// store FP32 partial sums per tile range, which k_reduce_chunks adds in a fixed order.
-// (TMEM rows: an M = 128 accumulator holds row r in lane r; an M = 64 one holds rows
-// 16i..16i+15 in lanes 32i..32i+15.)
-constexpr int WG_KC = 64;                        // pixels per tile (one box)
-constexpr unsigned WG_BOX = WG_KC * 128;         // bytes of one 64-channel box
-constexpr int WG_MAX_STAGES = 4;
+// A CTA owns a group of M tiles (their accumulators, Cout columns each, fill at most 512
+// TMEM columns) and a contiguous range of 64-pixel tiles (split K). One thread issues the TMA
+// loads into a ring of stages, one thread the MMAs, and the four warps then read the
+// accumulators back with tcgen05.ld (warp w: lanes = rows 32w..32w+31) and store FP32 partial
+// sums per pixel range, which reduce_chunks adds in a fixed order.
+constexpr int WG_KC = 64;                             // pixels per tile (one box)
+constexpr unsigned WG_ROWS3_BOX = (WG_KC + 4) * 64;   // rows3: 68 pixels x 32 channels
+constexpr unsigned WG_ROWS3_STRIDE = 5 * 1024;        // its slot in a stage (1024-aligned)
+constexpr int WG_MAX_STAGES = 8;
 
 struct WgradTiles {
     int B, H, W, Wb, Hb, tx, ty, tiles;  // 64-pixel tiles of Wb x Hb pixels
-    int Cout, M, ma, mgroups;            // output channels, MMA M (64 or 128), G atoms per
-                                         // CTA, groups of 128 output channels
-    int c0, c1, seg0, atoms;             // input channels, atoms of input 0, atoms in total
-    int T, ag, N, cols;                  // taps per CTA, atoms per CTA, MMA N, TMEM columns
-    int tiles_per_chunk, stages;
+    int Cout, N, ga;                     // output channels, MMA N (Cout rounded to 16), G atoms
+    int c0, c1, aw, seg0, apt;           // inputs, atom width, atoms of input 0, atoms per tap
+    int spt, mtiles, mt_per_cta;         // slots per M tile, M tiles, M tiles per CTA
+    int rows3;                           // row tiles of 32-channel atoms, one box per kernel row
+    int cols, tiles_per_chunk, stages;
     float *partial;                      // [chunk][tap][ci][co]
 };
 
-__device__ __forceinline__ unsigned long long sdesc_mn(unsigned addr) {
-    return (unsigned long long)((addr & 0x3FFFFu) >> 4) |    // start address
-           ((unsigned long long)(WG_BOX >> 4) << 16) |      // leading byte offset: next 64-channel atom
-           ((unsigned long long)(1024 >> 4) << 32) |        // stride byte offset: next 8 pixel rows
-           (1ull << 46) | (2ull << 61);                     // version, 128-byte swizzle
+// MN-major shared-memory descriptor: atoms of 64 (128-byte swizzle) or 32 (64-byte swizzle)
+// channels x 8 pixel rows; 8-row groups `sbo` apart, atoms `lbo` apart.
+__device__ __forceinline__ unsigned long long sdesc_mn(unsigned addr, unsigned lbo, unsigned sbo, bool sw64) {
+    return (unsigned long long)((addr & 0x3FFFFu) >> 4) | ((unsigned long long)(lbo >> 4) << 16) |
+           ((unsigned long long)(sbo >> 4) << 32) | (1ull << 46) | ((sw64 ? 4ull : 2ull) << 61);
 }
 
-// kind::f16, BF16 A and B both MN-major, FP32 D, M x N.
-__device__ __forceinline__ unsigned idesc_mn(int m, int n) {
+// kind::f16, BF16 A and B both MN-major, FP32 D, M = 128 x N.
+__device__ __forceinline__ unsigned idesc_mn(int n) {
     return (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) | ((unsigned)(n >> 3) << 17) |
-           ((unsigned)(m >> 4) << 24);
+           ((unsigned)(TM >> 4) << 24);
 }
 
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(128, 2)
     k_wgrad_umma(const __grid_constant__ CUtensorMap tmg, const __grid_constant__ CUtensorMap tm0,
                  const __grid_constant__ CUtensorMap tm1, const WgradTiles q) {
     extern __shared__ unsigned char smem_raw[];
     const unsigned raw = saddr(smem_raw);
     const unsigned base = (raw + 1023u) & ~1023u;
-    const unsigned a_bytes = (unsigned)q.ma * WG_BOX, b_tap = (unsigned)q.ag * WG_BOX;
-    const unsigned stage_bytes = a_bytes + (unsigned)q.T * b_tap;
+    const bool sw64 = q.aw == 32;
+    // bytes of one G box and of one X box (rows3: 68 pixels of 32 channels, 5 KB apart)
+    const unsigned gbox = WG_KC * 128, xbox = q.rows3 ? WG_ROWS3_STRIDE : WG_KC * 2 * q.aw;
+    const unsigned g_bytes = (unsigned)q.ga * gbox;
+    const int mt0 = blockIdx.y * q.mt_per_cta;
+    const int my_mt = min(q.mt_per_cta, q.mtiles - mt0);
+    const int slot0 = mt0 * q.spt, slots = min(my_mt * q.spt, 9 * q.apt - slot0);
+    const unsigned stage_bytes = g_bytes + (unsigned)(q.mt_per_cta * (q.rows3 ? 1 : q.spt)) * xbox;
     const int S = q.stages;
     const unsigned bar0 = base + S * stage_bytes;
     auto full = [&](int st) { return bar0 + 8u * st; };
@@ -969,8 +980,7 @@ __global__ void __launch_bounds__(128, 1)
     const unsigned *tmem_slot_ptr = reinterpret_cast<const unsigned *>(smem_raw + (tmem_slot - raw));
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int chunk = blockIdx.x, tap0 = blockIdx.y * q.T;
-    const int mg = (int)blockIdx.z % q.mgroups, atom0 = ((int)blockIdx.z / q.mgroups) * q.ag;
+    const int chunk = blockIdx.x;
     const int t_begin = chunk * q.tiles_per_chunk;
     const int t_end = min(q.tiles, t_begin + q.tiles_per_chunk);
     const int my_tiles = max(0, t_end - t_begin);
@@ -995,8 +1005,9 @@ __global__ void __launch_bounds__(128, 1)
     bool ok = true;
 
     if (tid == 0 && my_tiles > 0) {
-        // TMA producer
-        const unsigned bytes = stage_bytes;
+        // TMA producer: per 64-pixel tile, the G boxes and one box per slot of this CTA
+        // (rows3: one per M tile)
+        const unsigned bytes = g_bytes + (q.rows3 ? (unsigned)my_mt * WG_ROWS3_BOX : (unsigned)slots * xbox);
         for (int k = 0; k < my_tiles && ok; ++k) {
             const int st = k % S;
             if (k >= S && !mbar_wait(empty(st), (unsigned)((k / S - 1) & 1))) {
@@ -1009,22 +1020,32 @@ __global__ void __launch_bounds__(128, 1)
             const int y0 = (r % q.ty) * q.Hb, n = r / q.ty;
             const unsigned sa = base + st * stage_bytes;
             mbar_expect_tx(full(st), bytes);
-            for (int a = 0; a < q.ma; ++a) tma_4d(sa + a * WG_BOX, &tmg, 128 * mg + 64 * a, x0, y0, n, full(st));
-            for (int j = 0; j < q.T; ++j) {
-                const int tap = tap0 + j, dy = tap / 3 - 1, dx = tap % 3 - 1;
-                const unsigned sb = sa + a_bytes + j * b_tap;
-                for (int i = 0; i < q.ag; ++i) {
-                    const int atom = atom0 + i;
+            for (int a = 0; a < q.ga; ++a) tma_4d(sa + a * gbox, &tmg, 64 * a, x0, y0, n, full(st));
+            if (q.rows3) {
+                for (int j = 0; j < my_mt; ++j) {
+                    const int i = mt0 + j, dy = i / q.apt - 1, atom = i % q.apt;
+                    const unsigned dst = sa + g_bytes + j * xbox;
                     if (atom < q.seg0)
-                        tma_4d(sb + i * WG_BOX, &tm0, 64 * atom, x0 + dx, y0 + dy, n, full(st));
+                        tma_4d(dst, &tm0, 32 * atom, x0 - 1, y0 + dy, n, full(st));
                     else
-                        tma_4d(sb + i * WG_BOX, &tm1, 64 * (atom - q.seg0), x0 + dx, y0 + dy, n, full(st));
+                        tma_4d(dst, &tm1, 32 * (atom - q.seg0), x0 - 1, y0 + dy, n, full(st));
                 }
+                continue;
+            }
+            for (int j = 0; j < slots; ++j) {
+                const int slot = slot0 + j, tap = slot / q.apt, atom = slot % q.apt;
+                const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+                const unsigned dst = sa + g_bytes + j * xbox;
+                if (atom < q.seg0)
+                    tma_4d(dst, &tm0, q.aw * atom, x0 + dx, y0 + dy, n, full(st));
+                else
+                    tma_4d(dst, &tm1, q.aw * (atom - q.seg0), x0 + dx, y0 + dy, n, full(st));
             }
         }
     } else if (tid == 32 && my_tiles > 0) {
-        // MMA issuer
-        const unsigned id = idesc_mn(q.M, q.N);
+        // MMA issuer: per 16-pixel step one 128 x N MMA per M tile
+        const unsigned id = idesc_mn(q.N);
+        const unsigned xsbo = sw64 ? 512u : 1024u;
         for (int k = 0; k < my_tiles && ok; ++k) {
             const int st = k % S;
             if (!mbar_wait(full(st), (unsigned)((k / S) & 1))) {
@@ -1035,9 +1056,14 @@ __global__ void __launch_bounds__(128, 1)
             const unsigned sa = base + st * stage_bytes;
 #pragma unroll 1
             for (int ks = 0; ks < WG_KC / 16; ++ks) {
-                const unsigned long long da = sdesc_mn(sa + ks * 2048);
-                for (int j = 0; j < q.T; ++j) {
-                    const unsigned long long db = sdesc_mn(sa + a_bytes + j * b_tap + ks * 2048);
+                const unsigned long long db = sdesc_mn(sa + ks * 2048, gbox, 1024, false);
+                for (int j = 0; j < my_mt; ++j) {
+                    // rows3: the four 32-row atoms of the M tile are the box seen from pixel rows
+                    // 0, 1, 2, 3 (taps dx = -1, 0, 1 and an unused fourth): atoms 64 bytes apart
+                    const unsigned long long da =
+                        q.rows3 ? sdesc_mn(sa + g_bytes + j * xbox + ks * 2 * xsbo, 64, xsbo, true)
+                                : sdesc_mn(sa + g_bytes + (unsigned)(j * q.spt) * xbox + ks * 2 * xsbo, xbox, xsbo,
+                                           sw64);
                     umma(tmem + (unsigned)(j * q.N), da, db, id, (k > 0 || ks > 0) ? 1u : 0u);
                 }
             }
@@ -1045,12 +1071,7 @@ __global__ void __launch_bounds__(128, 1)
         }
         if (ok) umma_commit(done);
     }
-    // Epilogue: all four warps; warp w reads TMEM lanes 32w..32w+31. With M = 128 they hold
-    // output channels 32w..32w+31; with M = 64 the accumulator takes the first 16 lanes of
-    // each 32-lane quarter (channels 16w..16w+15).
-    const int rows = q.M == 64 ? 16 : 32;
-    const int co = 128 * mg + rows * warp + lane;
-    const bool row_ok = lane < rows && co < q.Cout;
+    // Epilogue: warp w reads TMEM lanes 32w..32w+31 = rows of each M tile.
     const int cin = q.c0 + q.c1;
     float *part = q.partial + (size_t)chunk * 9 * cin * q.Cout;
     bool have = my_tiles > 0;
@@ -1059,28 +1080,43 @@ __global__ void __launch_bounds__(128, 1)
         if (!have) ok = false;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
     }
-    {
-        for (int j = 0; j < q.T; ++j) {
-            const int tap = tap0 + j;
-            for (int c = 0; c < q.N; c += 16) {
-                unsigned v[16];
-                if (have) {
-                    tmem_ld16(tmem + ((unsigned)(32 * warp) << 16) + (unsigned)(j * q.N + c), v);
-                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-                }
+    const int row = 32 * warp + lane;
+    for (int j = 0; j < my_mt; ++j) {
+        int slot = slot0 + j * q.spt + row / q.aw, tap = slot / q.apt, atom = slot % q.apt;
+        const int c = row % q.aw;
+        if (q.rows3) {  // M tile (kernel row, atom); rows 32 s + c: tap dx = s - 1, s < 3
+            const int i = mt0 + j, sx = row / 32;
+            atom = i % q.apt;
+            tap = 3 * (i / q.apt) + sx;
+            slot = sx < 3 ? tap * q.apt + atom : 9 * q.apt;
+        }
+        int ci = -1;
+        if (slot < 9 * q.apt) {
+            if (atom < q.seg0) {
+                if (q.aw * atom + c < q.c0) ci = q.aw * atom + c;
+            } else if (q.aw * (atom - q.seg0) + c < q.c1) {
+                ci = q.c0 + q.aw * (atom - q.seg0) + c;
+            }
+        }
+        float *dst = part + ((size_t)tap * cin + ci) * q.Cout;
+        for (int cb = 0; cb < q.N; cb += 16) {
+            unsigned v[16];
+            if (have) {
+                tmem_ld16(tmem + ((unsigned)(32 * warp) << 16) + (unsigned)(j * q.N + cb), v);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            }
+            if (ci < 0) continue;
+            if (cb + 16 <= q.Cout) {
+                float4 *d4 = reinterpret_cast<float4 *>(dst + cb);
 #pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    const int col = c + e, atom = atom0 + col / 64, off = col % 64;
-                    int ci = -1;
-                    if (atom < q.seg0) {
-                        if (64 * atom + off < q.c0) ci = 64 * atom + off;
-                    } else if (atom < q.atoms) {
-                        const int c1 = 64 * (atom - q.seg0) + off;
-                        if (c1 < q.c1) ci = q.c0 + c1;
-                    }
-                    if (ci >= 0 && row_ok)
-                        part[((size_t)tap * cin + ci) * q.Cout + co] = have ? __uint_as_float(v[e]) : 0.0f;
-                }
+                for (int e = 0; e < 4; ++e)
+                    d4[e] = have ? make_float4(__uint_as_float(v[4 * e]), __uint_as_float(v[4 * e + 1]),
+                                               __uint_as_float(v[4 * e + 2]), __uint_as_float(v[4 * e + 3]))
+                                 : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 16; ++e)
+                    if (cb + e < q.Cout) dst[cb + e] = have ? __uint_as_float(v[e]) : 0.0f;
             }
         }
     }
@@ -1090,7 +1126,8 @@ __global__ void __launch_bounds__(128, 1)
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(q.cols));
 }
 
-// Split of the weight gradient: tap and atom groups per CTA, 64-pixel tiles, tiles per CTA.
+// Split of the weight gradient: atoms, slots per M tile, M tiles per CTA (TMEM and shared
+// memory), 64-pixel tiles, tile ranges per CTA.
 WgradTiles wgrad_tiles(int B, int H, int W, int c0, int c1, int Cout) {
     WgradTiles q{};
     q.B = B;
@@ -1103,32 +1140,42 @@ WgradTiles wgrad_tiles(int B, int H, int W, int c0, int c1, int Cout) {
     q.ty = (H + q.Hb - 1) / q.Hb;
     q.tiles = B * q.tx * q.ty;
     q.Cout = Cout;
-    q.M = Cout <= 64 ? 64 : 128;
-    q.ma = q.M / 64;
-    q.mgroups = (Cout + 127) / 128;
+    q.N = (Cout + 15) / 16 * 16;
+    q.ga = (Cout + 63) / 64;
     q.c0 = c0;
     q.c1 = c1;
-    q.seg0 = (c0 + 63) / 64;
-    q.atoms = q.seg0 + (c1 + 63) / 64;
-    if (q.atoms == 1 && c0 + c1 <= 48) {
-        q.T = 9;  // every tap in one CTA: 9 x N <= 432 columns
-        q.ag = 1;
-        q.N = (c0 + c1 + 15) / 16 * 16;
-    } else {
-        q.T = 3;  // one kernel row per CTA, at most two atoms: 3 x 128 columns
-        q.ag = std::min(2, q.atoms);
-        q.N = q.atoms == 1 ? (c0 + c1 + 15) / 16 * 16 : 64 * q.ag;
-    }
+    // Atom width: the one that needs fewer M tiles (32-channel atoms waste less on inputs
+    // like 48 + 32 channels); 64 on a tie (half the boxes).
+    auto mtiles_for = [&](int aw) {
+        const int apt = (c0 + aw - 1) / aw + (c1 + aw - 1) / aw;
+        return (9 * apt + TM / aw - 1) / (TM / aw);
+    };
+    q.aw = mtiles_for(32) < mtiles_for(64) ? 32 : 64;
+    q.seg0 = (c0 + q.aw - 1) / q.aw;
+    q.apt = q.seg0 + (c1 + q.aw - 1) / q.aw;
+    q.spt = TM / q.aw;
+    q.mtiles = mtiles_for(q.aw);
+    q.rows3 = q.aw == 32 && q.Wb == WG_KC && 3 * q.apt <= q.mtiles + q.apt;
+    if (q.rows3) q.mtiles = 3 * q.apt;
+    const unsigned gbytes = (unsigned)q.ga * WG_KC * 128,
+                   mbytes = q.rows3 ? WG_ROWS3_STRIDE : (unsigned)q.spt * WG_KC * 2 * q.aw;  // 16 KB
+    // M tiles per CTA: accumulators within 512 TMEM columns, and stages small enough for two
+    // CTAs per SM (at most 4 rows3 boxes or 2 M tiles of 16 KB next to the G boxes); the M
+    // tiles are then spread evenly over the CTA groups.
+    const int cap = std::max(1, std::min({512 / q.N, q.rows3 ? 4 : 2, (int)((72 * 1024 - gbytes) / mbytes)}));
+    const int groups = (q.mtiles + cap - 1) / cap;
+    q.mt_per_cta = (q.mtiles + groups - 1) / groups;
     q.cols = 32;
-    while (q.cols < q.T * q.N) q.cols *= 2;
-    const int groups = (9 / q.T) * ((q.atoms + q.ag - 1) / q.ag) * q.mgroups;
-    // About two CTAs per SM in total, but at least 16 tiles (1,024 pixels) per CTA: every
-    // CTA writes 9 x Cin x Cout partial sums, which must stay small against its MMA work.
+    while (q.cols < q.mt_per_cta * q.N) q.cols *= 2;
+    // About two CTAs per SM in total, but at least 4 tiles (256 pixels) per CTA: every CTA
+    // writes its partial sums, which must stay small against its MMA work.
     const int target = 2 * 152;
-    int chunks = std::max(1, std::min((q.tiles + 15) / 16, (target + groups - 1) / groups));
+    const int chunks = std::max(1, std::min((q.tiles + 3) / 4, (target + groups - 1) / groups));
     q.tiles_per_chunk = (q.tiles + chunks - 1) / chunks;
-    const unsigned stage = (unsigned)(q.ma + q.T * q.ag) * WG_BOX;
-    q.stages = (int)std::min<size_t>(WG_MAX_STAGES, (200 * 1024) / stage);
+    // Stages: up to ~100 KB of them, so that two CTAs share an SM where the accumulators
+    // allow (their MMA issue, not the tensor pipe, bounds these narrow GEMMs); at least two.
+    const unsigned stage = gbytes + (unsigned)q.mt_per_cta * mbytes;
+    q.stages = (int)std::max<size_t>(2, std::min<size_t>(WG_MAX_STAGES, (100 * 1024) / stage));
     return q;
 }
 
@@ -1335,12 +1382,10 @@ int pack_all(const float *params, const PackTable &tab, bf16 *wk, bf16 *wkd, cud
     return RT_OK;
 }
 
-// Scratch floats of conv_wgrad's partial sums: at most ceil(2 x 152 / CTA groups) tile ranges
-// (one CTA group when the input is at most 48 channels of one atom, at least three otherwise).
+// Scratch floats of conv_wgrad's partial sums: at most 2 x 152 tile ranges (wgrad_tiles).
 size_t wgrad_partial_floats(long P, int Cin, int Cout) {
     (void)P;
-    const int groups = Cin <= 48 ? 1 : 3;
-    return (size_t)((2 * 152 + groups - 1) / groups) * 9 * Cin * Cout;
+    return (size_t)2 * 152 * 9 * Cin * Cout;
 }
 
 int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, float *partial, float *dw, bf16 *ups,
@@ -1356,14 +1401,20 @@ int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, f
         RT_CUDA_TRY(cudaGetLastError());
         src0 = ups;
     }
+    if (Cout > 256) {
+        set_error("the weight gradient takes at most 256 output channels");
+        return RT_ERR_ARG;
+    }
     WgradTiles q = wgrad_tiles(B, H, W, in.c0, in.c1, Cout);
     q.partial = partial;
     CUtensorMap tmg, tm0, tm1;
+    const bool narrow = q.aw == 32;
+    const int xbw = q.rows3 ? WG_KC + 4 : q.Wb;  // rows3: 68-pixel boxes from x0 - 1
     int r = map_activations(&tmg, g, B, H, W, Cout, q.Wb, q.Hb, false);
-    if (r == RT_OK) r = map_activations(&tm0, src0, B, H, W, in.c0, q.Wb, q.Hb, false);
+    if (r == RT_OK) r = map_activations(&tm0, src0, B, H, W, in.c0, xbw, q.Hb, narrow);
     if (r == RT_OK) {
         if (in.c1)
-            r = map_activations(&tm1, in.p1, B, H, W, in.c1, q.Wb, q.Hb, false);
+            r = map_activations(&tm1, in.p1, B, H, W, in.c1, xbw, q.Hb, narrow);
         else
             tm1 = tm0;
     }
@@ -1373,10 +1424,11 @@ int conv_wgrad(const ConvIn &in, int B, int H, int W, const bf16 *g, int Cout, f
         RT_CUDA_TRY(cudaFuncSetAttribute(k_wgrad_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
         configured = true;
     }
-    const size_t stage = (size_t)(q.ma + q.T * q.ag) * WG_BOX;
+    const size_t stage = (size_t)q.ga * WG_KC * 128 +
+                         (size_t)q.mt_per_cta * (q.rows3 ? WG_ROWS3_STRIDE : (size_t)q.spt * WG_KC * 2 * q.aw);
     const size_t smem = 1024 + q.stages * stage + 8 * (2 * WG_MAX_STAGES + 2);
     const int chunks = (q.tiles + q.tiles_per_chunk - 1) / q.tiles_per_chunk;
-    const dim3 grid((unsigned)chunks, (unsigned)(9 / q.T), (unsigned)((q.atoms + q.ag - 1) / q.ag * q.mgroups));
+    const dim3 grid((unsigned)chunks, (unsigned)((q.mtiles + q.mt_per_cta - 1) / q.mt_per_cta), 1);
     k_wgrad_umma<<<grid, 128, smem, st>>>(tmg, tm0, tm1, q);
     RT_CUDA_TRY(cudaGetLastError());
     return reduce_chunks(partial, chunks, (size_t)9 * (in.c0 + in.c1) * Cout, dw, st);
