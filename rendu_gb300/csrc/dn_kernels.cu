@@ -51,10 +51,10 @@ __global__ void k_reduce_chunks_tiled(const float *__restrict__ partial, int chu
 
 // ReLU gradient and bias-gradient partials in one pass over a (P x C) FP32 gradient, 4
 // channels a thread (C a multiple of 4, C <= 1024): rows [chunk b, chunk (b + 1)) per block;
-// g is zeroed where the forward output y was not positive (relu), gb receives its BF16 copy,
-// and partial[b][c] the column sums of the masked rows (fixed order: per thread row by row,
-// then thread rows 0..R-1).
-__global__ void k_relu_grad_colsum4(float *__restrict__ g, const bf16 *__restrict__ y, long P, int C, int relu,
+// the values of g where the forward output y was not positive (relu) count as zero; gb
+// receives the masked gradient in BF16 and partial[b][c] the column sums of the masked rows
+// (fixed order: per thread row by row, then thread rows 0..R-1).
+__global__ void k_relu_grad_colsum4(const float *__restrict__ g, const bf16 *__restrict__ y, long P, int C, int relu,
                                     long chunk, bf16 *__restrict__ gb, float *__restrict__ partial) {
     __shared__ float4 red[256];
     const int C4 = C / 4, R = 256 / C4;
@@ -69,12 +69,10 @@ __global__ void k_relu_grad_colsum4(float *__restrict__ g, const bf16 *__restric
                 const uint2 yy = *reinterpret_cast<const uint2 *>(y + i);
                 const float2 y01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&yy.x));
                 const float2 y23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&yy.y));
-                const float4 m = v;
                 if (!(y01.x > 0.0f)) v.x = 0.0f;
                 if (!(y01.y > 0.0f)) v.y = 0.0f;
                 if (!(y23.x > 0.0f)) v.z = 0.0f;
                 if (!(y23.y > 0.0f)) v.w = 0.0f;
-                if (m.x != v.x || m.y != v.y || m.z != v.z || m.w != v.w) *reinterpret_cast<float4 *>(g + i) = v;
             }
             const __nv_bfloat162 h01 = __floats2bfloat162_rn(v.x, v.y), h23 = __floats2bfloat162_rn(v.z, v.w);
             uint2 o;
@@ -99,18 +97,6 @@ __global__ void k_relu_grad_colsum4(float *__restrict__ g, const bf16 *__restric
         }
         *reinterpret_cast<float4 *>(partial + (size_t)blockIdx.x * C + 4 * threadIdx.x) = t;
     }
-}
-
-// out[i] = sum over c of partial[c][i], one warp per output: lane l sums chunks l, l + 32, ...
-// in order, then a fixed shuffle tree (deterministic; for few outputs and many chunks).
-__global__ void k_reduce_chunks_warp(const float *__restrict__ partial, int chunks, int n, float *__restrict__ out) {
-    const int i = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
-    if (i >= n) return;
-    float s = 0.0f;
-    for (int c = lane; c < chunks; c += 32) s += partial[(size_t)c * n + i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) out[i] = s;
 }
 
 // 2x2 max pooling, NHWC.
@@ -362,7 +348,9 @@ __global__ void k_adam(float *__restrict__ w, const float *__restrict__ g, float
 
 inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
-constexpr long kReluRows = 128;  // rows per block of the fused ReLU / bias-gradient pass
+// Rows per block of the fused ReLU / bias-gradient pass: about 2 x 152 blocks, 128 to 1,024
+// rows each (a multiple of 32).
+long relu_rows(long P) { return std::max(128L, std::min(1024L, (P / 304 + 31) / 32 * 32)); }
 
 }  // namespace
 
@@ -378,7 +366,7 @@ int reduce_chunks(const float *partial, int chunks, size_t n, float *out, cudaSt
     return RT_OK;
 }
 
-size_t colsum_partial_floats(long P, int C) { return (size_t)((P + kReluRows - 1) / kReluRows) * C; }
+size_t colsum_partial_floats(long P, int C) { return (size_t)((P + relu_rows(P) - 1) / relu_rows(P)) * C; }
 
 int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st) {
     if (C % 8 == 0)
@@ -406,17 +394,17 @@ int split_grad(const float *gin, int B, int H, int W, int c0, int up0, int c1, f
     return RT_OK;
 }
 
-int relu_grad_bias(float *g, const bf16 *y, long P, int C, bool relu, bf16 *gb, float *partial, float *db,
+int relu_grad_bias(const float *g, const bf16 *y, long P, int C, bool relu, bf16 *gb, float *partial, float *db,
                    cudaStream_t st) {
-    const int chunks = (int)((P + kReluRows - 1) / kReluRows);
+    const long rows = relu_rows(P);
+    const int chunks = (int)((P + rows - 1) / rows);
     if (C % 4 != 0 || C > 1024) {
         set_error("relu_grad_bias needs a channel count that is a multiple of 4, at most 1024");
         return RT_ERR_ARG;
     }
-    k_relu_grad_colsum4<<<chunks, 256, 0, st>>>(g, y, P, C, relu ? 1 : 0, kReluRows, gb, partial);
-    k_reduce_chunks_warp<<<blocks((size_t)C * 32), 256, 0, st>>>(partial, chunks, C, db);
+    k_relu_grad_colsum4<<<chunks, 256, 0, st>>>(g, y, P, C, relu ? 1 : 0, rows, gb, partial);
     RT_CUDA_TRY(cudaGetLastError());
-    return RT_OK;
+    return reduce_chunks(partial, chunks, (size_t)C, db, st);
 }
 
 int prepare(const float *f, int B, int H, int W, int Hp, int Wp, bf16 *x, cudaStream_t st) {

@@ -78,10 +78,10 @@ size_t colsum_partial_floats(long P, int C);
 int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st);
 int pool_back(const bf16 *x, const bf16 *y, const float *gy, int B, int H, int W, int C, float *gx, cudaStream_t st);
 int split_grad(const float *gin, int B, int H, int W, int c0, int up0, int c1, float *g0, float *g1, cudaStream_t st);
-// The ReLU gradient (g zeroed where the forward output y was not positive, BF16 copy in gb)
-// and the bias gradient db[c] = sum over the P rows of the masked g, in one pass
-// (partial: colsum_partial_floats(P, C) floats of scratch).
-int relu_grad_bias(float *g, const bf16 *y, long P, int C, bool relu, bf16 *gb, float *partial, float *db,
+// The ReLU gradient (g with zeros where the forward output y was not positive, as a BF16 copy
+// in gb; g itself is left as it is) and the bias gradient db[c] = sum over the P rows of the
+// masked g, in one pass (partial: colsum_partial_floats(P, C) floats of scratch).
+int relu_grad_bias(const float *g, const bf16 *y, long P, int C, bool relu, bf16 *gb, float *partial, float *db,
                    cudaStream_t st);
 // Features (B, H, W, DN_FEATURES) fp32 -> network input (B, Hp, Wp, 16) bf16, edge-replicated
 // padding.
