@@ -201,8 +201,8 @@ PT_CONFIGS = {
     #   estimator 0 = the reference's (PathTracer::render), 1 = extended (NEE on the emissive
     #   quads and the importance-sampled environment map, MIS) as the large workload asks.
     "cornell_256": ("cornell", 256, 256, 16, 5, 16, 0),
-    "instanced_1080p": ("instanced", 1920, 1080, 64, 8, 1, 1),
-    "instanced_1080p_reference_estimator": ("instanced", 1920, 1080, 64, 8, 1, 0),
+    "instanced_1080p": ("instanced", 1920, 1080, 64, 8, 4, 1),
+    "instanced_1080p_reference_estimator": ("instanced", 1920, 1080, 64, 8, 4, 0),
 }
 
 
