@@ -524,7 +524,9 @@ def run_denoiser(cpu: bool):
            "inference_gflop_padded": round(net.flops(1080, 1920) / 1e9, 1),
            "train_step_ms_8x256": round(tr_ms, 3), "train_tflops": round(tr_flop / tr_ms / 1e9, 1),
            "roofline": {"bound": "tensor", "achieved": round(inf_tflops, 1), "peak": peak, "unit": "TFLOP/s",
-                        "frac": round(inf_tflops / peak, 4), "peak_kind": peak_kind, "traffic": None},
+                        "frac": round(inf_tflops / peak, 4), "peak_kind": peak_kind, "kernel": "k_conv_fold",
+                        "traffic": _profile_traffic("denoiser_conv_1080p.txt").get("k_conv_fold", {}).get(
+                            "traffic_bytes_per_launch")},
            "training": {"scenes": len(DN_TRAIN_SCENES), "views": len(DN_TRAIN_SCENES) * DN_TRAIN_VIEWS,
                         "view_size": "256x256", "input_spp": list(DN_TRAIN_SPP),
                         "target_spp": [_dn_target_spp(s_) for s_ in DN_TRAIN_SPP], "steps": DN_TRAIN_STEPS,
