@@ -61,7 +61,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // What a captured step depends on: the shape and every buffer address baked into it.
 struct GraphSig {
-    const void *p[10];
+    const void *p[11];
     int B, H, W, Hp, Wp;
 };
 
@@ -78,6 +78,10 @@ struct GraphSlot {
 struct dn_net {
     int device = 0;
     cudaStream_t stream = nullptr;  // for host-pointer calls
+    // The weight gradients run on a second stream beside the data-gradient chain (forked
+    // and joined with events, captured into the same graph).
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::vector<Tensor> tensors;
     std::vector<Conv> convs;
     std::vector<Op> ops;
@@ -88,13 +92,14 @@ struct dn_net {
     // Shape-dependent buffers.
     int B = 0, Hp = 0, Wp = 0;
     bool train_ready = false;
-    DevBuf act, gact, gin, gbf, partial, feat, target, out, loss_partial, ups;
-    std::vector<size_t> act_off, gact_off;
+    DevBuf act, gact, gin, gbf, partial, bpartial, feat, target, out, loss_partial, ups;
+    std::vector<size_t> act_off, gact_off, gb_off;  // gb_off: per convolution, its BF16 output gradient
     GraphSlot g_train, g_infer;
 
     bf16 *bf(int t) { return reinterpret_cast<bf16 *>(static_cast<char *>(act.ptr) + act_off[t]); }
     float *f(int t) { return reinterpret_cast<float *>(static_cast<char *>(act.ptr) + act_off[t]); }
     float *g(int t) { return reinterpret_cast<float *>(static_cast<char *>(gact.ptr) + gact_off[t]); }
+    bf16 *gb(size_t conv) { return reinterpret_cast<bf16 *>(static_cast<char *>(gbf.ptr) + gb_off[conv]); }
     Hyper *hyp() { return hyper.as<Hyper>(); }
     long pixels(int level) const { return (long)B * (Hp >> level) * (Wp >> level); }
 };
@@ -218,7 +223,7 @@ int ensure_shape(dn_net *n, int B, int Hp, int Wp, bool train) {
     n->Wp = Wp;
     n->act_off.assign(n->tensors.size(), 0);
     n->gact_off.assign(n->tensors.size(), 0);
-    size_t a = 0, g = 0, max_el = 0, max_gin = 0, max_part = 0, max_ups = 0;
+    size_t a = 0, g = 0, gbytes = 0, max_gin = 0, max_part = 0, max_bpart = 0, max_ups = 0;
     for (size_t t = 0; t < n->tensors.size(); ++t) {
         const Tensor &T = n->tensors[t];
         const size_t el = (size_t)n->pixels(T.level) * T.ch;
@@ -226,21 +231,26 @@ int ensure_shape(dn_net *n, int B, int Hp, int Wp, bool train) {
         a += align_up(el * (T.f32 ? 4 : 2), 256);
         n->gact_off[t] = g;
         g += align_up(el * 4, 256);
-        max_el = std::max(max_el, el);
     }
-    for (const Conv &c : n->convs) {
+    n->gb_off.assign(n->convs.size(), 0);
+    for (size_t i = 0; i < n->convs.size(); ++i) {
+        const Conv &c = n->convs[i];
         const long P = n->pixels(n->tensors[c.out].level);
         const int cin = c.cin0 + c.cin1;
         if (c.cin1 || c.up0) max_gin = std::max(max_gin, (size_t)P * cin);
         if (c.up0) max_ups = std::max(max_ups, (size_t)P * c.cin0);
-        max_part = std::max({max_part, wgrad_partial_floats(P, cin, c.cout), colsum_partial_floats(P, c.cout)});
+        max_part = std::max(max_part, wgrad_partial_floats(P, cin, c.cout));
+        max_bpart = std::max(max_bpart, colsum_partial_floats(P, c.cout));
+        n->gb_off[i] = gbytes;
+        gbytes += align_up((size_t)P * c.cout * 2, 256);
     }
     if (n->act.reserve(a) != RT_OK || n->ups.reserve(std::max<size_t>(max_ups, 8) * 2) != RT_OK) return RT_ERR_OOM;
     n->train_ready = false;
     if (train) {
         const long P0 = n->pixels(0);
         if (n->gact.reserve(g) != RT_OK || n->gin.reserve(std::max<size_t>(max_gin, 1) * 4) != RT_OK ||
-            n->gbf.reserve(max_el * 2) != RT_OK || n->partial.reserve(max_part * 4) != RT_OK ||
+            n->gbf.reserve(gbytes) != RT_OK || n->partial.reserve(max_part * 4) != RT_OK ||
+            n->bpartial.reserve(max_bpart * 4) != RT_OK ||
             n->loss_partial.reserve((size_t)((P0 + 255) / 256) * 4) != RT_OK)
             return RT_ERR_OOM;
         n->train_ready = true;
@@ -272,12 +282,18 @@ int forward(dn_net *n, cudaStream_t st) {
     return RT_OK;
 }
 
+// The backward pass. Per convolution: the ReLU mask and bias gradient give the BF16 output
+// gradient (a buffer per convolution); the data gradient follows on `st` (the critical
+// chain), the weight gradient on the side stream, which waits for the output gradient and
+// rejoins `st` at the end. Each branch has its own split-K scratch (bias partials on `st`,
+// weight partials and the upsampled input on the side stream).
 int backward(dn_net *n, const float *target, cudaStream_t st) {
     const int last = n->convs.back().out;
     int r = relmse_loss(n->feat.as<float>(), n->f(last), target, n->pixels(0), n->g(last), n->loss_partial.as<float>(),
                         n->hyp(), st);
     if (r != RT_OK) return r;
     float *grads = n->grads.as<float>();
+    bool forked = false;
     for (auto it = n->ops.rbegin(); it != n->ops.rend() && r == RT_OK; ++it) {
         const Op &op = *it;
         if (op.pool) {
@@ -290,19 +306,25 @@ int backward(dn_net *n, const float *target, cudaStream_t st) {
         const Tensor &o = n->tensors[c.out];
         const int H = n->Hp >> o.level, W = n->Wp >> o.level;
         const long P = n->pixels(o.level);
-        bf16 *gb = n->gbf.as<bf16>();
-        // ReLU gradient and bias gradient in one pass (its partials are reduced before the
-        // weight gradient reuses the scratch)
+        bf16 *gb = n->gb(op.conv);
         r = relu_grad_bias(n->g(c.out), c.relu ? n->bf(c.out) : nullptr, P, c.cout, c.relu != 0, gb,
-                           n->partial.as<float>(), grads + c.boff, st);
+                           n->bpartial.as<float>(), grads + c.boff, st);
         if (r != RT_OK) break;
+        cudaError_t e = cudaEventRecord(n->ev_fork, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(n->side, n->ev_fork, 0);
+        if (e != cudaSuccess) {
+            set_error(std::string("denoiser stream fork failed: ") + cudaGetErrorString(e));
+            r = RT_ERR_CUDA;
+            break;
+        }
+        forked = true;
         ConvIn in;
         in.p0 = n->bf(c.src0);
         in.c0 = c.cin0;
         in.up0 = c.up0;
         in.p1 = c.src1 >= 0 ? n->bf(c.src1) : nullptr;
         in.c1 = c.cin1;
-        r = conv_wgrad(in, n->B, H, W, gb, c.cout, n->partial.as<float>(), grads + c.woff, n->ups.as<bf16>(), st);
+        r = conv_wgrad(in, n->B, H, W, gb, c.cout, n->partial.as<float>(), grads + c.woff, n->ups.as<bf16>(), n->side);
         if (r != RT_OK || c.src0 == 0) continue;  // no gradient for the network input
         ConvIn gi;
         gi.p0 = gb;
@@ -314,6 +336,15 @@ int backward(dn_net *n, const float *target, cudaStream_t st) {
         if (r == RT_OK && split)
             r = split_grad(dst, n->B, H, W, c.cin0, c.up0, c.cin1, n->g(c.src0), c.src1 >= 0 ? n->g(c.src1) : nullptr,
                            st);
+    }
+    // Rejoin on every path, so that a capture always ends with one stream.
+    if (forked) {
+        cudaError_t e = cudaEventRecord(n->ev_join, n->side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, n->ev_join, 0);
+        if (e != cudaSuccess && r == RT_OK) {
+            set_error(std::string("denoiser stream join failed: ") + cudaGetErrorString(e));
+            r = RT_ERR_CUDA;
+        }
     }
     return r;
 }
@@ -364,9 +395,9 @@ int train_body(dn_net *n, bool with_adam, cudaStream_t st) {
 GraphSig signature(dn_net *n, int H, int W) {
     GraphSig g;
     std::memset(&g, 0, sizeof(g));
-    const DevBuf *bufs[10] = {&n->act, &n->gact, &n->gin, &n->gbf, &n->partial, &n->feat, &n->target, &n->out,
-                              &n->loss_partial, &n->ups};
-    for (int i = 0; i < 10; ++i) g.p[i] = bufs[i]->ptr;
+    const DevBuf *bufs[11] = {&n->act, &n->gact, &n->gin, &n->gbf, &n->partial, &n->bpartial, &n->feat, &n->target,
+                              &n->out, &n->loss_partial, &n->ups};
+    for (int i = 0; i < 11; ++i) g.p[i] = bufs[i]->ptr;
     g.B = n->B;
     g.H = H;
     g.W = W;
@@ -390,7 +421,7 @@ int run_graph(dn_net *n, GraphSlot &slot, const GraphSig &sig, Body body, cudaSt
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(n->stream, &g);
         cudaError_t ei = cudaSuccess;
-        if (r == RT_OK && e == cudaSuccess) ei = cudaGraphInstantiate(&slot.exec, g, 0);
+        if (r == RT_OK && e == cudaSuccess) ei = cudaGraphInstantiate(&slot.exec, g, cudaGraphInstantiateFlagUseNodePriority);
         if (g) cudaGraphDestroy(g);
         if (r != RT_OK || e != cudaSuccess || ei != cudaSuccess) {
             slot.exec = nullptr;
@@ -445,7 +476,16 @@ RT_API int dn_create(dn_net **out, int device) {
     n->device = device;
     build_graph(n);
     int r = RT_OK;
-    if (cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    // The data-gradient chain is the critical path of a training step: its stream gets the
+    // highest priority, the weight-gradient stream the lowest (captured into the graphs'
+    // kernel nodes, which are instantiated to use them).
+    int prio_lo = 0, prio_hi = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (cudaStreamCreateWithPriority(&n->stream, cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&n->side, cudaStreamNonBlocking, prio_lo) != cudaSuccess ||
+        cudaEventCreateWithFlags(&n->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&n->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
         set_error("stream creation failed");
         r = RT_ERR_CUDA;
     }
@@ -472,11 +512,16 @@ RT_API int dn_destroy(dn_net *n) {
     if (!n) return RT_OK;
     DeviceGuard guard(n->device);
     if (n->stream) cudaStreamSynchronize(n->stream);
+    if (n->side) cudaStreamSynchronize(n->side);
     for (GraphSlot *g : {&n->g_train, &n->g_infer})
         if (g->exec) cudaGraphExecDestroy(g->exec);
     for (DevBuf *b : {&n->params, &n->grads, &n->adam_m, &n->adam_v, &n->wk, &n->wkd, &n->hyper, &n->act, &n->gact,
-                      &n->gin, &n->gbf, &n->partial, &n->feat, &n->target, &n->out, &n->loss_partial, &n->ups})
+                      &n->gin, &n->gbf, &n->partial, &n->bpartial, &n->feat, &n->target, &n->out, &n->loss_partial,
+                      &n->ups})
         b->release();
+    if (n->ev_fork) cudaEventDestroy(n->ev_fork);
+    if (n->ev_join) cudaEventDestroy(n->ev_join);
+    if (n->side) cudaStreamDestroy(n->side);
     if (n->stream) cudaStreamDestroy(n->stream);
     delete n;
     return RT_OK;
