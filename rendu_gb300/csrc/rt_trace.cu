@@ -98,8 +98,12 @@ __global__ void __launch_bounds__(128) k_trace_persistent(const BvhNode *__restr
     bool active = false, exhausted = false;
     uint32_t nv_ = 0, nt_ = 0;
 #if RT_INTAKE_QUEUE && RT_FETCH_BLOCK
+    // Queued rays keep their record in shared memory, so that each ray is read from its
+    // buffer once (the buffer may be mapped host memory).
     __shared__ unsigned s_queue[4][kIntakeQueue];  // 128 threads = 4 warps
+    __shared__ float4 s_qray[4][kIntakeQueue][2];
     unsigned *queue = s_queue[threadIdx.x >> 5];
+    float4 (*qray)[2] = s_qray[threadIdx.x >> 5];
     int qn = 0;  // queued entries (warp-uniform)
     auto ray_of = [&](unsigned u) { return ((size_t)(u >> 8) * gridDim.x + blockIdx.x) * 256u + (u & 255u); };
     auto write_miss = [&](size_t i) {
@@ -117,15 +121,23 @@ __global__ void __launch_bounds__(128) k_trace_persistent(const BvhNode *__restr
                 if (ray_of(v + 31) >= n) exhausted = true;
                 const size_t i = ray_of(v + lane);
                 bool enters = false;
+                float4 ra = make_float4(0.0f, 0.0f, 0.0f, 0.0f), rb = ra;
                 if (i < n) {
                     const float4 *rp = reinterpret_cast<const float4 *>(rays + i);
-                    const RayState q = make_ray_state(__ldcs(rp), __ldcs(rp + 1));
+                    ra = __ldcs(rp);
+                    rb = __ldcs(rp + 1);
+                    const RayState q = make_ray_state(ra, rb);
                     enters = q.valid && slab(q, root.lo[0], root.hi[0], root.lo[1], root.hi[1], root.lo[2],
                                              root.hi[2], q.tmin, q.tmax) != INFINITY;
                     if (!enters) write_miss(i);
                 }
                 const unsigned em = __ballot_sync(0xffffffffu, enters);
-                if (enters) queue[qn + __popc(em & lt_mask)] = (unsigned)i;
+                if (enters) {
+                    const int slot = qn + __popc(em & lt_mask);
+                    queue[slot] = (unsigned)i;
+                    qray[slot][0] = ra;
+                    qray[slot][1] = rb;
+                }
                 qn += __popc(em);
                 __syncwarp();
             }
@@ -137,9 +149,9 @@ __global__ void __launch_bounds__(128) k_trace_persistent(const BvhNode *__restr
             const unsigned take = min((unsigned)qn, (unsigned)__popc(need));
             const unsigned rank = __popc(need & lt_mask);
             if (!active && rank < take) {
-                idx = queue[qn - 1 - rank];
-                const float4 *rp = reinterpret_cast<const float4 *>(rays + idx);
-                r = make_ray_state(__ldcs(rp), __ldcs(rp + 1));
+                const int slot = qn - 1 - (int)rank;
+                idx = queue[slot];
+                r = make_ray_state(qray[slot][0], qray[slot][1]);
                 trav_init(t, r);
                 active = true;
             }
@@ -243,8 +255,8 @@ __global__ void k_invert(uint8_t *__restrict__ v, size_t n) {
 template <bool ANY, int STACK>
 int launch_persistent(rt_ctx *ctx, const rt_ray *rays, size_t n, const uint32_t *n_dev, rt_hit *hits, uint8_t *occ,
                       cudaStream_t st) {
-    static int grid[2][2] = {{0, 0}, {0, 0}};
-    int &g = grid[ANY ? 1 : 0][STACK == 64 ? 0 : 1];
+    static int grid[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    int &g = grid[ANY ? 1 : 0][STACK == 64 ? 0 : (STACK == 256 ? 1 : 2)];
     if (g == 0) {
         int per_sm = 0, sms = 0, dev = 0;
         RT_CUDA_TRY(cudaGetDevice(&dev));
