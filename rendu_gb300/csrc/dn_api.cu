@@ -258,7 +258,9 @@ int ensure_shape(dn_net *n, int B, int Hp, int Wp, bool train) {
     return RT_OK;
 }
 
-int forward(dn_net *n, cudaStream_t st) {
+// The forward pass; the output layer stores its FP32 result (for the loss), or with
+// last.finish_out writes the denoised image instead.
+int forward(dn_net *n, cudaStream_t st, const FOut &last) {
     for (const Op &op : n->ops) {
         int r;
         if (op.pool) {
@@ -275,7 +277,8 @@ int forward(dn_net *n, cudaStream_t st) {
             in.c1 = c.cin1;
             r = conv_forward_umma(in, n->B, n->Hp >> o.level, n->Wp >> o.level, n->wk.as<bf16>() + c.wk_off,
                                   n->params.as<float>() + c.boff, c.cout, c.relu != 0, o.f32 ? nullptr : n->bf(c.out),
-                                  o.f32 ? n->f(c.out) : nullptr, n->ups.as<bf16>(), st);
+                                  o.f32 && !last.finish_out ? n->f(c.out) : nullptr, n->ups.as<bf16>(), st,
+                                  o.f32 ? last : FOut());
         }
         if (r != RT_OK) return r;
     }
@@ -386,7 +389,7 @@ int adam_launch(dn_net *n, cudaStream_t st) {
 // Forward + loss + backward over the staged batch in n->feat / n->target.
 int train_body(dn_net *n, bool with_adam, cudaStream_t st) {
     int r = prepare(n->feat.as<float>(), n->B, n->Hp, n->Wp, n->Hp, n->Wp, n->bf(0), st);
-    if (r == RT_OK) r = forward(n, st);
+    if (r == RT_OK) r = forward(n, st, FOut());
     if (r == RT_OK) r = backward(n, n->target.as<float>(), st);
     if (r == RT_OK && with_adam) r = adam_launch(n, st);
     return r;
@@ -600,10 +603,13 @@ RT_API int dn_denoise(dn_net *n, const float *features, uint32_t width, uint32_t
     if (r != RT_OK) return r;
     const int B = (int)batch, H = (int)height, W = (int)width;
     auto body = [&](cudaStream_t s) {
+        FOut fin;
+        fin.feat = n->feat.as<float>();
+        fin.finish_out = n->out.as<float>();
+        fin.H = H;
+        fin.W = W;
         int q = prepare(n->feat.as<float>(), B, H, W, (int)Hp, (int)Wp, n->bf(0), s);
-        if (q == RT_OK) q = forward(n, s);
-        if (q == RT_OK)
-            q = finish(n->feat.as<float>(), n->f(n->convs.back().out), B, H, W, (int)Hp, (int)Wp, n->out.as<float>(), s);
+        if (q == RT_OK) q = forward(n, s, fin);
         return q;
     };
     r = run_graph(n, n->g_infer, signature(n, H, W), body, st);

@@ -257,25 +257,6 @@ __global__ void k_prepare(const float *__restrict__ f, int B, int H, int W, int 
     dst[1] = *reinterpret_cast<uint4 *>(&o[4]);
 }
 
-// radiance = max(exp(log(1 + input) + y) - 1, 0): the network predicts a correction of the
-// noisy input in log space; the input is taken from the FP32 features, so that a zero
-// correction returns the input unchanged.
-__device__ __forceinline__ float dn_output(float in, float y) { return fmaxf(expm1f(log1pf(fmaxf(in, 0.0f)) + y), 0.0f); }
-
-__global__ void k_finish(const float *__restrict__ f, const float *__restrict__ y, int B, int H, int W, int Hp, int Wp,
-                         float *__restrict__ out) {
-    const size_t o = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    const size_t n = (size_t)B * H * W;
-    if (o >= n) return;
-    const int xx = (int)(o % W);
-    const size_t r = o / W;
-    const int yy = (int)(r % H);
-    const int b = (int)(r / H);
-    const size_t q = ((size_t)b * Hp + yy) * Wp + xx;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) out[o * 3 + k] = dn_output(f[o * DN_FEATURES + k], y[q * 16 + k]);
-}
-
 // Relative squared error, the measure the denoiser is judged by: mean over pixels and
 // channels of ((x - t) / (x' + 0.01))^2 with x = dn_output(input, y) and x' the same value
 // held constant (not differentiated), as in Noise2Noise's loss for Monte Carlo renders
@@ -409,12 +390,6 @@ int relu_grad_bias(const float *g, const bf16 *y, long P, int C, bool relu, bf16
 
 int prepare(const float *f, int B, int H, int W, int Hp, int Wp, bf16 *x, cudaStream_t st) {
     k_prepare<<<blocks((size_t)B * Hp * Wp), 256, 0, st>>>(f, B, H, W, Hp, Wp, x);
-    RT_CUDA_TRY(cudaGetLastError());
-    return RT_OK;
-}
-
-int finish(const float *f, const float *y, int B, int H, int W, int Hp, int Wp, float *out, cudaStream_t st) {
-    k_finish<<<blocks((size_t)B * H * W), 256, 0, st>>>(f, y, B, H, W, Hp, Wp, out);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

@@ -48,6 +48,21 @@ struct Hyper {
     float loss;
 };
 
+// radiance = max(exp(log(1 + input) + y) - 1, 0): the network predicts a correction of the
+// noisy input in log space; the input is taken from the FP32 features, so that a zero
+// correction returns the input unchanged.
+__device__ __forceinline__ float dn_output(float in, float y) { return fmaxf(expm1f(log1pf(fmaxf(in, 0.0f)) + y), 0.0f); }
+
+// The output layer's result finished in its epilogue (conv_forward_umma's `fo`, inference):
+// instead of storing the FP32 output, each pixel of the H x W image inside the padded grid
+// writes the denoised radiance finish_out[o, k] = dn_output(feat[o, k], y[k]), k < 3, o its
+// index in the image (Cout a multiple of 16).
+struct FOut {
+    const float *feat = nullptr;  // (B, H, W, DN_FEATURES)
+    float *finish_out = nullptr;  // (B, H, W, 3)
+    int H = 0, W = 0;
+};
+
 // ---- launchers (asynchronous on st; RT_OK or RT_ERR_CUDA) -------------------------------------
 // Length of a packed weight row: 9 taps x (64-channel chunks of input 0 + of input 1) x 64.
 size_t packed_k(int c0, int c1);
@@ -56,7 +71,7 @@ size_t packed_k(int c0, int c1);
 // data-gradient packing it computes a layer's input gradient. An upsampled input 0 is
 // first expanded into `ups` (B x H x W x c0 BF16). Cout a multiple of 8.
 int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, const float *bias, int Cout, bool relu,
-                      bf16 *out_bf, float *out_f, bf16 *ups, cudaStream_t st);
+                      bf16 *out_bf, float *out_f, bf16 *ups, cudaStream_t st, const FOut &fo = FOut());
 // w FP32 [tap][c0 + c1][Cout] -> wpk [Cout][packed_k(c0, c1)] (forward) and
 // wpkd [c0 + c1][packed_k(Cout, 0)] (data gradient, taps mirrored); either may be null.
 int pack_weights(const float *w, int c0, int c1, int Cout, bf16 *wpk, bf16 *wpkd, cudaStream_t st);
@@ -86,10 +101,8 @@ int relu_grad_bias(const float *g, const bf16 *y, long P, int C, bool relu, bf16
 // Features (B, H, W, DN_FEATURES) fp32 -> network input (B, Hp, Wp, 16) bf16, edge-replicated
 // padding.
 int prepare(const float *f, int B, int H, int W, int Hp, int Wp, bf16 *x, cudaStream_t st);
-// Network output (B, Hp, Wp, 16) fp32 + the features' radiance (B, H, W) -> radiance (B, H, W, 3).
-int finish(const float *f, const float *y, int B, int H, int W, int Hp, int Wp, float *out, cudaStream_t st);
-// Relative squared error of the output against the target (P pixels, features and output at
-// the same P); writes gy (P x 16) and hyper->loss.
+// Relative squared error of the output (y: P x 16) against the target (P pixels, features
+// and output at the same P); writes gy (P x 16) and hyper->loss.
 int relmse_loss(const float *f, const float *y, const float *target, long P, float *gy, float *partial, Hyper *hyper,
                 cudaStream_t st);
 // hyper->lr = lr, ordered on st (the value travels as a kernel argument: no host buffer).

@@ -174,6 +174,9 @@ struct ConvTiles {
     int relu;
     bf16 *out_bf;
     float *out_f;
+    const float *fin_feat;  // the finished output layer (FOut)
+    float *fin_out;
+    int fin_H, fin_W;
 };
 
 // K steps of 16 that chunk j actually holds: the MMAs over a chunk's zero-filled channels
@@ -192,8 +195,10 @@ __device__ __forceinline__ void tmem_ld16(unsigned addr, unsigned (&v)[16]) {
 }
 
 // 16 output channels [cb, cb + 16) of pixel p: bias (from shared memory when sbias is given:
-// N entries, zero past Cout), ReLU, BF16 and/or FP32 store (channels past Cout are dropped).
+// N entries, zero past Cout), ReLU, BF16 and/or FP32 store (channels past Cout are dropped);
+// XO: instead of the stores, channels 0..2 finished into the denoised image (FOut).
 // Every array index is static, so the values stay in registers.
+template <bool XO>
 __device__ __forceinline__ void store16(const ConvTiles &q, const unsigned (&v)[16], int cb, long p,
                                         const float *sbias = nullptr) {
     const int Cout = q.Cout;
@@ -217,10 +222,22 @@ __device__ __forceinline__ void store16(const ConvTiles &q, const unsigned (&v)[
             dst[0] = *reinterpret_cast<uint4 *>(&h[0]);
             dst[1] = *reinterpret_cast<uint4 *>(&h[4]);
         }
-        if (q.out_f) {
+        if (!XO && q.out_f) {
             float4 *dst = reinterpret_cast<float4 *>(q.out_f + p * Cout + cb);
 #pragma unroll
             for (int j = 0; j < 4; ++j) dst[j] = make_float4(f[4 * j], f[4 * j + 1], f[4 * j + 2], f[4 * j + 3]);
+        }
+        if (XO && cb == 0) {
+            const long x = p % q.W, r = p / q.W;
+            const long y = r % q.H, b = r / q.H;
+            if (x < q.fin_W && y < q.fin_H) {
+                const long o = (b * q.fin_H + y) * q.fin_W + x;
+                const float *in = q.fin_feat + o * DN_FEATURES;
+                float *dst = q.fin_out + o * 3;
+                dst[0] = dn_output(__ldg(in), f[0]);
+                dst[1] = dn_output(__ldg(in + 1), f[1]);
+                dst[2] = dn_output(__ldg(in + 2), f[2]);
+            }
         }
     } else {
 #pragma unroll
@@ -238,7 +255,7 @@ __device__ __forceinline__ void store16(const ConvTiles &q, const unsigned (&v)[
 // thread as soon as its last columns are in registers, before the bias, ReLU and NHWC
 // stores of those. Several groups keep several tiles' stores in flight on each SM
 // sub-partition. False if a wait gave up.
-template <class Origin>
+template <bool XO, class Origin>
 __device__ __forceinline__ bool epilogue(const ConvTiles &q, unsigned tmem, unsigned bar0, int my_tiles,
                                          const Origin &tile_origin) {
     const int warp = threadIdx.x >> 5, g = warp / EPI_WARPS, quarter = warp % EPI_WARPS;
@@ -268,14 +285,15 @@ __device__ __forceinline__ bool epilogue(const ConvTiles &q, unsigned tmem, unsi
             }
             const int cb = n0 + c0;
             if (inside && cb < q.Cout) {
-                store16(q, va, cb, p);
-                if (two && cb + 16 < q.Cout) store16(q, vb, cb + 16, p);
+                store16<XO>(q, va, cb, p);
+                if (two && cb + 16 < q.Cout) store16<XO>(q, vb, cb + 16, p);
             }
         }
     }
     return true;
 }
 
+template <bool XO>
 __global__ void __launch_bounds__(THREADS, 1)
     k_conv_umma(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
                 const __grid_constant__ CUtensorMap tmw, const ConvTiles q) {
@@ -398,7 +416,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         __syncwarp();
     } else {
-        ok = epilogue(q, tmem, bar0, my_tiles, tile_origin);
+        ok = epilogue<XO>(q, tmem, bar0, my_tiles, tile_origin);
     }
     if (!ok) atomicOr(&g_umma_status, 1u);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
@@ -441,6 +459,7 @@ __device__ __forceinline__ void mma_taps(unsigned d, unsigned long long ad, cons
 }
 
 
+template <bool XO>
 __global__ void __launch_bounds__(THREADS, 1)
     k_conv_rows(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
                 const __grid_constant__ CUtensorMap tmw, const ConvTiles q) {
@@ -586,7 +605,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         __syncwarp();
     } else {
-        ok = epilogue(q, tmem, bar0, my_tiles, tile_origin);
+        ok = epilogue<XO>(q, tmem, bar0, my_tiles, tile_origin);
     }
     if (!ok) atomicOr(&g_umma_status, 1u);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
@@ -628,7 +647,7 @@ __device__ __forceinline__ void mma_rows3(unsigned d, unsigned long long ad, uns
 
 // Epilogue of the folded tiles: group g reads accumulator g, 16 output channels at a time
 // (columns c0, N + c0, 2N + c0), adds each row's neighbours' columns and stores lanes 1..30.
-template <class Origin>
+template <bool XO, class Origin>
 __device__ __forceinline__ bool epilogue_fold(const ConvTiles &q, unsigned tmem, unsigned bar0, const float *sbias,
                                               int my_tiles, const Origin &tile_origin) {
     const int warp = threadIdx.x >> 5, g = warp / EPI_WARPS, quarter = warp % EPI_WARPS;
@@ -663,12 +682,13 @@ __device__ __forceinline__ bool epilogue_fold(const ConvTiles &q, unsigned tmem,
                 v[j] = __float_as_uint(up + __uint_as_float(b1[j]) + dn);
             }
             const int cb = n0 + c0;
-            if (store && cb < q.Cout) store16(q, v, cb, p, sbias);
+            if (store && cb < q.Cout) store16<XO>(q, v, cb, p, sbias);
         }
     }
     return true;
 }
 
+template <bool XO>
 __global__ void __launch_bounds__(THREADS, 1)
     k_conv_fold(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
                 const __grid_constant__ CUtensorMap tmw, const ConvTiles q) {
@@ -810,7 +830,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         __syncwarp();
     } else {
-        ok = epilogue_fold(q, tmem, bar0, sbias, my_tiles, tile_origin);
+        ok = epilogue_fold<XO>(q, tmem, bar0, sbias, my_tiles, tile_origin);
     }
     if (!ok) atomicOr(&g_umma_status, 1u);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
@@ -1248,7 +1268,11 @@ inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / 
 size_t packed_k(int c0, int c1) { return (size_t)9 * ((c0 + 63) / 64 + (c1 + 63) / 64) * 64; }
 
 int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, const float *bias, int Cout, bool relu,
-                      bf16 *out_bf, float *out_f, bf16 *ups, cudaStream_t st) {
+                      bf16 *out_bf, float *out_f, bf16 *ups, cudaStream_t st, const FOut &fo) {
+    if (fo.finish_out && (Cout % 16 != 0 || !fo.feat || fo.H > H || fo.W > W || out_f || out_bf)) {
+        set_error("a finished convolution output needs Cout a multiple of 16, the features and no other output");
+        return RT_ERR_ARG;
+    }
     const bf16 *src0 = in.p0;
     if (in.up0) {
         if (!ups) {
@@ -1284,6 +1308,10 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
     q.relu = relu ? 1 : 0;
     q.out_bf = out_bf;
     q.out_f = out_f;
+    q.fin_feat = fo.feat;
+    q.fin_out = fo.finish_out;
+    q.fin_H = fo.H;
+    q.fin_W = fo.W;
     q.wres = 0;
     q.narrow0 = q.narrow1 = 0;
     q.astage = 0;
@@ -1337,21 +1365,25 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
     static bool configured = false;
     static int sms = 0;
     if (!configured) {
-        RT_CUDA_TRY(cudaFuncSetAttribute(k_conv_umma, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
-        RT_CUDA_TRY(cudaFuncSetAttribute(k_conv_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
-        RT_CUDA_TRY(cudaFuncSetAttribute(k_conv_fold, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
+        for (const void *k : {(const void *)k_conv_umma<false>, (const void *)k_conv_rows<false>,
+                              (const void *)k_conv_fold<false>, (const void *)k_conv_umma<true>,
+                              (const void *)k_conv_rows<true>, (const void *)k_conv_fold<true>})
+            RT_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, 232448));
         int dev = 0;
         RT_CUDA_TRY(cudaGetDevice(&dev));
         RT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         configured = true;
     }
     const int grid = std::min(q.ntiles, sms);  // one persistent CTA per SM
+    // The finished output layer is a separate instantiation, so that the other layers'
+    // epilogues keep their registers.
+    const bool xo = fo.finish_out != nullptr;
     if (fold)
-        k_conv_fold<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
+        (xo ? k_conv_fold<true> : k_conv_fold<false>)<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
     else if (rows)
-        k_conv_rows<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
+        (xo ? k_conv_rows<true> : k_conv_rows<false>)<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
     else
-        k_conv_umma<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
+        (xo ? k_conv_umma<true> : k_conv_umma<false>)<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
