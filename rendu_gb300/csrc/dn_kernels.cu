@@ -153,29 +153,51 @@ __global__ void k_pool8(const bf16 *__restrict__ x, int B, int H, int W, int C, 
 }
 
 // Pooling gradient: each pooled gradient goes to the first maximal input of its window (row
-// major order), added into gx.
-__global__ void k_pool_back(const bf16 *__restrict__ x, const bf16 *__restrict__ y, const float *__restrict__ gy,
-                            int B, int H, int W, int C, float *__restrict__ gx) {
+// major order), added into gx. Four channels a thread (C a multiple of 4): 8-byte BF16 and
+// 16-byte FP32 accesses, one read-modify-write of gx per window input that receives any.
+__global__ void k_pool_back4(const bf16 *__restrict__ x, const bf16 *__restrict__ y, const float *__restrict__ gy,
+                             int B, int H, int W, int C, float *__restrict__ gx) {
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    const int h = H / 2, w = W / 2;
-    const size_t n = (size_t)B * h * w * C;
+    const int h = H / 2, w = W / 2, c4 = C / 4;
+    const size_t n = (size_t)B * h * w * c4;
     if (i >= n) return;
-    const int c = (int)(i % C);
-    size_t r = i / C;
+    const int c = (int)(i % c4) * 4;
+    size_t r = i / c4;
     const int xo = (int)(r % w);
     r /= w;
     const int yo = (int)(r % h);
     const int b = (int)(r / h);
-    const float m = __bfloat162float(y[i]);
+    const size_t o = (i / c4) * C + c;  // pooled element
+    const uint2 yv = *reinterpret_cast<const uint2 *>(y + o);
+    const float4 g = *reinterpret_cast<const float4 *>(gy + o);
+    const float2 m01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&yv.x));
+    const float2 m23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&yv.y));
+    const float m[4] = {m01.x, m01.y, m23.x, m23.y}, gv[4] = {g.x, g.y, g.z, g.w};
     const size_t base = (((size_t)b * H + 2 * yo) * W + 2 * xo) * C + c;
     const size_t row = (size_t)W * C;
     const size_t off[4] = {0, (size_t)C, row, row + C};
+    unsigned done = 0u;  // channels whose gradient has been placed
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
-        if (__bfloat162float(x[base + off[k]]) == m) {
-            gx[base + off[k]] += gy[i];
-            break;
+    for (int k = 0; k < 4; ++k) {
+        const uint2 xv = *reinterpret_cast<const uint2 *>(x + base + off[k]);
+        const float2 x01 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&xv.x));
+        const float2 x23 = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&xv.y));
+        const float xs[4] = {x01.x, x01.y, x23.x, x23.y};
+        unsigned hit = 0u;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (!(done >> j & 1u) && xs[j] == m[j]) hit |= 1u << j;
+        if (hit) {
+            float4 *dst = reinterpret_cast<float4 *>(gx + base + off[k]);
+            float4 v = *dst;
+            if (hit & 1u) v.x += gv[0];
+            if (hit & 2u) v.y += gv[1];
+            if (hit & 4u) v.z += gv[2];
+            if (hit & 8u) v.w += gv[3];
+            *dst = v;
+            done |= hit;
         }
+    }
 }
 
 // Gradient of a concatenated input: channels [0, c0) go to g0 -- summed over each 2x2 block
@@ -269,19 +291,24 @@ __global__ void k_relmse(const float *__restrict__ f, const float *__restrict__ 
     float l = 0.0f;
     if (p < P) {
         const float inv = 1.0f / (3.0f * (float)P);
+        const float4 yv = *reinterpret_cast<const float4 *>(y + p * 16);
+        const float ys[3] = {yv.x, yv.y, yv.z};
+        float g[3];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) {
-            float gk = 0.0f;
-            if (k < 3) {
-                const float x = dn_output(f[p * DN_FEATURES + k], y[p * 16 + k]);
-                const float den = x + 0.01f;
-                const float d = x - t[p * 3 + k];
-                const float q = d / den;
-                l += q * q;
-                gk = x > 0.0f ? 2.0f * q / den * (x + 1.0f) * inv : 0.0f;
-            }
-            gy[p * 16 + k] = gk;
+        for (int k = 0; k < 3; ++k) {
+            const float x = dn_output(f[p * DN_FEATURES + k], ys[k]);
+            const float den = x + 0.01f;
+            const float d = x - t[p * 3 + k];
+            const float q = d / den;
+            l += q * q;
+            g[k] = x > 0.0f ? 2.0f * q / den * (x + 1.0f) * inv : 0.0f;
         }
+        float4 *dst = reinterpret_cast<float4 *>(gy + p * 16);  // channels 3..15 carry no loss
+        const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        dst[0] = make_float4(g[0], g[1], g[2], 0.0f);
+        dst[1] = zero;
+        dst[2] = zero;
+        dst[3] = zero;
     }
     red[threadIdx.x] = l;
     __syncthreads();
@@ -359,7 +386,11 @@ int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st) {
 }
 
 int pool_back(const bf16 *x, const bf16 *y, const float *gy, int B, int H, int W, int C, float *gx, cudaStream_t st) {
-    k_pool_back<<<blocks((size_t)B * (H / 2) * (W / 2) * C), 256, 0, st>>>(x, y, gy, B, H, W, C, gx);
+    if (C % 4 != 0) {
+        set_error("pool_back needs a channel count that is a multiple of 4");
+        return RT_ERR_ARG;
+    }
+    k_pool_back4<<<blocks((size_t)B * (H / 2) * (W / 2) * (C / 4)), 256, 0, st>>>(x, y, gy, B, H, W, C, gx);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
