@@ -23,7 +23,7 @@ beside it.
                Mrays/s counting primary, bounce and shadow rays, device time inside
                pt_render, beside the C restatement of PathTracer::render on host cores.
 * batch    -- 64 seeded jobs (10k-500k triangles, 128^2-1024^2, 4-256 spp, depth 3-10) in
-               one batched call (waves replayed from a CUDA graph, autotuned), vs the same
+               one batched call (one CUDA graph launch looping over the waves, autotuned), vs the same
                jobs rendered one call after another.
 * denoiser -- the learned denoiser (BF16 tensor-core U-Net) trained on path-tracer pairs:
                inference TFLOP/s at 1920x1080 against the BF16 peak, training-step
@@ -322,7 +322,7 @@ def run_pathtracer(name, steps, cpu: bool):
 
 def run_batch(cpu: bool, tune: bool = True):
     """Batched rendering: 64 seeded jobs (10k-500k triangles, 128^2-1024^2, 4-256 spp,
-    depth 3-10) in one pt_batch_render call (waves replayed from one CUDA graph, autotuned
+    depth 3-10) in one pt_batch_render call (one CUDA graph launch looping over the waves, autotuned
     tuning), against the same jobs rendered one pt_render call after another."""
     import torch
 

@@ -355,9 +355,9 @@ typedef struct pt_render_options {
                        for bit. The reference splits rows over threads instead
                        (System::forParallel, System.hpp:72-104, PathTracer.cpp:186). */
     uint32_t rank;  /* this process's rank, < ranks                                       */
-    int32_t profile; /* nonzero: launch every wave's kernels directly instead of replaying the
-                        captured CUDA graph, with CUDA events between them, and report the
-                        time of each kernel class in pt_render_stats.kernel_ms (slower)    */
+    int32_t profile; /* nonzero: launch every wave's kernels directly instead of the captured
+                        CUDA graph, with CUDA events between them, and report the time of
+                        each kernel class in pt_render_stats.kernel_ms (slower)            */
 } pt_render_options;
 
 /* Pixels per tile of the pt_render_options rank split. */
@@ -377,9 +377,10 @@ RT_API int pt_render_ex(pt_scene *scene, const pt_camera_desc *camera, uint32_t 
 
 /* ---- batched rendering ---------------------------------------------------------------
  * Many renders of different scenes, resolutions, sample counts and depths in one call:
- * their pixels x samples are cut into tiles and packed into shared waves; every wave is one
- * replay of a CUDA graph holding the whole per-wave launch sequence (ray generation, the
- * persistent traversal, shading, shadow rays, accumulation). Each job's image is exactly
+ * their pixels x samples are cut into tiles and packed into shared waves; one CUDA graph
+ * launch loops over the waves on the device (a conditional while node whose body is the
+ * whole per-wave launch sequence: ray generation, the persistent traversal, shading, shadow
+ * rays, accumulation). Each job's image is exactly
  * what pt_render of that job alone gives (same random stream, same summation order). No
  * counterpart in the reference, which renders one image per PathTracer::render call. */
 typedef struct pt_batch pt_batch;

@@ -1,5 +1,6 @@
 // Wave engine: runs one render (pt_render) or a batch of renders (pt_batch_render) as a
-// sequence of waves whose launch sequence is captured once in a CUDA graph and replayed.
+// sequence of waves whose launch sequence is captured once as the body of a CUDA graph's
+// while node, which loops over the call's waves on the device (one graph launch per call).
 //
 // Scheduling. Each job is cut into tiles of at most `tile_pixels` pixels x S samples
 // (S = a power of two <= the job's sample count and <= `max_samples`). Tiles are issued
@@ -111,7 +112,8 @@ int WaveEngine::ensure_capacity(uint64_t cap, uint64_t accum_pixels, uint64_t nt
 }
 
 int WaveEngine::launch_wave(const PtWave &w, uint32_t depth, bool ext, bool shadow_a, bool shadow_b, bool big_stack,
-                            cudaStream_t cs, std::vector<cudaEvent_t> *marks, std::vector<int> *kinds) {
+                            cudaStream_t cs, std::vector<cudaEvent_t> *marks, std::vector<int> *kinds,
+                            const cudaGraphConditionalHandle *loop) {
     auto mark = [&](int kind) -> int {
         if (!marks) return RT_OK;
         cudaEvent_t e = nullptr;
@@ -143,7 +145,7 @@ int WaveEngine::launch_wave(const PtWave &w, uint32_t depth, bool ext, bool shad
         cur ^= 1;
     }
     if (r == RT_OK) r = pt_launch_accumulate(w, cs);
-    if (r == RT_OK) r = pt_launch_wave_end(w, cs);
+    if (r == RT_OK) r = pt_launch_wave_end(w, cs, loop);
     if (r == RT_OK) r = mark(PT_KERNEL_ACCUMULATE);
     return r;
 }
@@ -155,15 +157,38 @@ int WaveEngine::capture(const PtWave &w, uint32_t depth, bool ext, bool shadow_a
         exec_ = nullptr;
     }
     cudaStream_t cs = capture_stream_;
-    RT_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-    const int r = launch_wave(w, depth, ext, shadow_a, shadow_b, big_stack, cs, nullptr, nullptr);
+    // graph = { while (waves remain) { wave } }: the handle starts at 1 on every launch (a
+    // call has at least one wave) and the wave's last kernel sets it.
     cudaGraph_t graph = nullptr;
-    const cudaError_t e = cudaStreamEndCapture(cs, &graph);
+    RT_CUDA_TRY(cudaGraphCreate(&graph, 0));
+    cudaGraphConditionalHandle loop = 0;
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};  // the rest zero
+    cudaGraphNode_t node = nullptr;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&loop, graph, 1u, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) {
+        cp.conditional.handle = loop;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp);
+    }
+    if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(cs, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        cudaGetLastError();
+        set_error(std::string("wave loop graph set-up failed: ") + cudaGetErrorString(e));
+        return RT_ERR_CUDA;
+    }
+    const int r = launch_wave(w, depth, ext, shadow_a, shadow_b, big_stack, cs, nullptr, nullptr, &loop);
+    cudaGraph_t body = nullptr;
+    e = cudaStreamEndCapture(cs, &body);
     if (r != RT_OK) {
-        if (graph) cudaGraphDestroy(graph);
+        cudaGraphDestroy(graph);
         return r;
     }
     if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
         set_error(std::string("graph capture failed: ") + cudaGetErrorString(e));
         return RT_ERR_CUDA;
     }
@@ -369,11 +394,12 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
     RT_CUDA_TRY(cudaEventRecord(e0, st));
     float kernel_ms[PT_KERNEL_KINDS] = {0, 0, 0, 0};
     if (!profile) {
-        for (uint64_t k = 0; k < nwaves && r == RT_OK; ++k)
-            if (cudaGraphLaunch(exec_, st) != cudaSuccess) {
-                set_error(std::string("graph launch failed: ") + cudaGetErrorString(cudaGetLastError()));
-                r = RT_ERR_CUDA;
-            }
+        // One launch: the graph loops over the waves on the device.
+        if (nwaves > 0) r = pt_launch_set_waves(w, (uint32_t)nwaves, st);
+        if (r == RT_OK && nwaves > 0 && cudaGraphLaunch(exec_, st) != cudaSuccess) {
+            set_error(std::string("graph launch failed: ") + cudaGetErrorString(cudaGetLastError()));
+            r = RT_ERR_CUDA;
+        }
     } else {
         // Per-kernel times: the same sequence launched directly on `st`, an event after every
         // step, read back wave by wave.

@@ -15,9 +15,9 @@
 //     shadow   -- PathTracer::checkVisibility for each queued shadow ray (two queues,
 //                 resolved in a fixed order);
 //   accumulate -- min(L, clamp) of each sample added to its pixel in sample order;
-//   wave_end   -- advance the wave index.
-// The whole per-wave sequence reads its wave from device memory, so it is captured once in
-// a CUDA graph and replayed for every wave (pt_engine.cu).
+//   wave_end   -- advance the wave index (and, inside the graph, set its loop condition).
+// The whole per-wave sequence reads its wave from device memory, so it is captured once as
+// the body of a CUDA graph's while node that runs it for every wave (pt_engine.cu).
 #include <cuda_fp16.h>
 
 #include "pt_scene.hpp"
@@ -57,7 +57,13 @@ __global__ void k_wave_begin(PtWave w) {
     *w.fetch = 0ull;
 }
 
-__global__ void k_wave_end(PtWave w) { w.counters[4] += 1u; }
+__global__ void k_wave_end(PtWave w, cudaGraphConditionalHandle loop, int has_loop) {
+    const uint32_t next = w.counters[4] + 1u;
+    w.counters[4] = next;
+    if (has_loop) cudaGraphSetConditional(loop, next < w.counters[5] ? 1u : 0u);
+}
+
+__global__ void k_set_waves(PtWave w, uint32_t n) { w.counters[5] = n; }
 
 __global__ void k_raygen(PtWave w) {
     const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -658,8 +664,14 @@ int pt_launch_wave_begin(const PtWave &w, cudaStream_t st) {
     return RT_OK;
 }
 
-int pt_launch_wave_end(const PtWave &w, cudaStream_t st) {
-    k_wave_end<<<1, 1, 0, st>>>(w);
+int pt_launch_wave_end(const PtWave &w, cudaStream_t st, const cudaGraphConditionalHandle *loop) {
+    k_wave_end<<<1, 1, 0, st>>>(w, loop ? *loop : cudaGraphConditionalHandle(0), loop ? 1 : 0);
+    RT_CUDA_TRY(cudaGetLastError());
+    return RT_OK;
+}
+
+int pt_launch_set_waves(const PtWave &w, uint32_t nwaves, cudaStream_t st) {
+    k_set_waves<<<1, 1, 0, st>>>(w, nwaves);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

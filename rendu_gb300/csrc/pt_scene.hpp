@@ -84,7 +84,11 @@ int pt_launch_sky_table(uint32_t res, uint32_t samples, bool half_prec, float4 *
 int pt_launch_sky_eval(const float4 *table, uint32_t w, uint32_t h, const float *cases, uint32_t n, float *out,
                        cudaStream_t st);
 int pt_launch_wave_begin(const PtWave &w, cudaStream_t st);
-int pt_launch_wave_end(const PtWave &w, cudaStream_t st);
+// End of a wave: the wave index advances; with a conditional handle (the wave sequence is the
+// body of a graph's while node) the loop goes on while waves remain (counters[5] waves).
+int pt_launch_wave_end(const PtWave &w, cudaStream_t st, const cudaGraphConditionalHandle *loop = nullptr);
+// counters[5] = the number of waves of this call (read by the graph's loop).
+int pt_launch_set_waves(const PtWave &w, uint32_t nwaves, cudaStream_t st);
 int pt_launch_raygen(const PtWave &w, cudaStream_t st);
 int pt_launch_shade(const PtWave &w, int cur, uint32_t did, bool ext, cudaStream_t st);
 int pt_launch_shadow(const PtWave &w, int queue, bool big_stack, cudaStream_t st);
@@ -122,8 +126,10 @@ struct Tuning {
 Tuning default_tuning();
 bool load_tuning(const char *path, Tuning &t);
 
-// Runs renders as waves replayed from one captured CUDA graph. Owns every device buffer it
-// uses (grow-only) and the instantiated graph, reused while the launch shape is unchanged.
+// Runs renders as waves of one captured CUDA graph: the wave sequence is the body of the
+// graph's while node, which loops on the device until the call's last wave, so a whole
+// render or batch is one graph launch. Owns every device buffer it uses (grow-only) and the
+// instantiated graph, reused while the launch shape is unchanged.
 class WaveEngine {
   public:
     explicit WaveEngine(int device) : device_(device) {}
@@ -139,8 +145,10 @@ class WaveEngine {
     int capture(const PtWave &w, uint32_t depth, bool ext, bool shadow_a, bool shadow_b, bool big_stack);
     // The per-wave launch sequence on `st`. With `marks`, an event is recorded after every
     // step and `kinds` receives the step's kernel class (PT_KERNEL_*), for per-kernel times.
+    // With `loop`, the sequence ends by setting that while-node handle.
     int launch_wave(const PtWave &w, uint32_t depth, bool ext, bool shadow_a, bool shadow_b, bool big_stack,
-                    cudaStream_t st, std::vector<cudaEvent_t> *marks, std::vector<int> *kinds);
+                    cudaStream_t st, std::vector<cudaEvent_t> *marks, std::vector<int> *kinds,
+                    const cudaGraphConditionalHandle *loop = nullptr);
     int device_;
     cudaStream_t capture_stream_ = nullptr;
     DevBuf atten_, color_, ndc_, pjob_, ppix_, psamp_, qray0_, qray1_, qpath0_, qpath1_, hits_, sray_, scontrib_;

@@ -231,7 +231,7 @@ def material_sample(cases, uniforms):
 
 class BatchRenderer:
     """Many renders in one call (pt_batch_render): jobs of different scenes, resolutions,
-    sample counts and depths share waves replayed from one CUDA graph. Each job is a dict
+    sample counts and depths share waves run by one CUDA graph launch. Each job is a dict
     with ``tracer`` (a PathTracer), ``camera``, ``samples``, ``depth``, ``seed`` and
     ``image`` (host float32 (H, W, C) arrays, or CUDA tensors for all jobs)."""
 
