@@ -516,6 +516,13 @@ RT_API int dn_param_count(const dn_net *net, size_t *count);
 RT_API int dn_get_params(dn_net *net, float *out, size_t count);
 RT_API int dn_set_params(dn_net *net, const float *in, size_t count); /* also resets Adam */
 RT_API int dn_get_grads(dn_net *net, float *out, size_t count);
+/* The gradient buffer for data-parallel training (each process computes the gradients of its
+ * share of a batch with dn_backward, the processes sum them, dn_adam_step applies them):
+ * dn_read_grads copies the last gradients to `out`, dn_write_grads replaces them with `in`
+ * (count = dn_param_count floats). Device pointers with RT_FLAG_DEVICE_PTRS (ordered on
+ * `stream`, asynchronous); host pointers otherwise (blocking). */
+RT_API int dn_read_grads(dn_net *net, float *out, size_t count, void *stream, uint32_t flags);
+RT_API int dn_write_grads(dn_net *net, const float *in, size_t count, void *stream, uint32_t flags);
 
 /* Denoise `batch` images: features (batch, height, width, DN_FEATURES) -> out (batch,
  * height, width, 3) radiance. Host pointers by default (blocking); device pointers with

@@ -156,6 +156,8 @@ _SIGS = {
     "dn_get_params": ([_VP, _VP, C.c_size_t], C.c_int),
     "dn_set_params": ([_VP, _VP, C.c_size_t], C.c_int),
     "dn_get_grads": ([_VP, _VP, C.c_size_t], C.c_int),
+    "dn_read_grads": ([_VP, _VP, C.c_size_t, _VP, C.c_uint32], C.c_int),
+    "dn_write_grads": ([_VP, _VP, C.c_size_t, _VP, C.c_uint32], C.c_int),
     "dn_denoise": ([_VP, _VP, C.c_uint32, C.c_uint32, C.c_uint32, _VP, _VP, C.c_uint32], C.c_int),
     "dn_backward": ([_VP, _VP, _VP, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.c_float), _VP, C.c_uint32],
                     C.c_int),

@@ -587,6 +587,30 @@ RT_API int dn_get_grads(dn_net *n, float *out, size_t count) {
     return umma_status(true);
 }
 
+RT_API int dn_read_grads(dn_net *n, float *out, size_t count, void *stream, uint32_t flags) {
+    if (!n || !out || count != n->nparams) return arg_error("parameter count mismatch");
+    DeviceGuard guard(n->device);
+    if (flags & RT_FLAG_DEVICE_PTRS) {
+        RT_CUDA_TRY(cudaMemcpyAsync(out, n->grads.ptr, count * sizeof(float), cudaMemcpyDeviceToDevice,
+                                    static_cast<cudaStream_t>(stream)));
+        return RT_OK;
+    }
+    return dn_get_grads(n, out, count);
+}
+
+RT_API int dn_write_grads(dn_net *n, const float *in, size_t count, void *stream, uint32_t flags) {
+    if (!n || !in || count != n->nparams) return arg_error("parameter count mismatch");
+    DeviceGuard guard(n->device);
+    if (flags & RT_FLAG_DEVICE_PTRS) {
+        RT_CUDA_TRY(cudaMemcpyAsync(n->grads.ptr, in, count * sizeof(float), cudaMemcpyDeviceToDevice,
+                                    static_cast<cudaStream_t>(stream)));
+        return RT_OK;
+    }
+    RT_CUDA_TRY(cudaDeviceSynchronize());
+    RT_CUDA_TRY(cudaMemcpy(n->grads.ptr, in, count * sizeof(float), cudaMemcpyHostToDevice));
+    return RT_OK;
+}
+
 RT_API int dn_denoise(dn_net *n, const float *features, uint32_t width, uint32_t height, uint32_t batch, float *out,
                       void *stream, uint32_t flags) {
     if (!n || !features || !out) return arg_error("null argument");

@@ -109,6 +109,19 @@ class Denoiser:
         L.call("dn_get_grads", self._h, out.ctypes.data, out.size)
         return out
 
+    def read_grads(self, out) -> None:
+        """Copy the last gradients into ``out`` (param_count float32: a CUDA tensor, ordered on
+        the current stream, or a host array)."""
+        dev = _is_cuda(out)
+        L.call("dn_read_grads", self._h, _ptr(out), self.param_count, _stream() if dev else None,
+               L.RT_FLAG_DEVICE_PTRS if dev else 0)
+
+    def write_grads(self, src) -> None:
+        """Replace the gradients that the next ``adam_step`` applies with ``src``."""
+        dev = _is_cuda(src)
+        L.call("dn_write_grads", self._h, _ptr(src), self.param_count, _stream() if dev else None,
+               L.RT_FLAG_DEVICE_PTRS if dev else 0)
+
     def init(self, seed: int) -> None:
         L.call("dn_init", self._h, int(seed))
 
@@ -288,6 +301,40 @@ def time_to(points, threshold: float):
             a = (np.log(threshold) - np.log(e0)) / (np.log(e1) - np.log(e0))
             return float(np.exp(np.log(t0) + a * (np.log(t1) - np.log(t0))))
     return None
+
+
+def train_step_dp(net, features, target, lr: float, group=None, read_loss: bool = True):
+    """One data-parallel training step, run by every process of ``group``
+    (torch.distributed) on its own share of the batch: its loss and gradients
+    (``net.backward``), their mean over the processes (one all_reduce of the flat
+    gradient; with equal shares that is the gradient of the whole batch, whose loss is a
+    mean over pixels), then the same Adam step everywhere, so the processes' parameters stay
+    identical. CUDA tensors travel through NCCL on the device; with gloo, or host arrays,
+    through host memory. Returns the mean loss over the processes (or None)."""
+    import torch
+    import torch.distributed as dist
+
+    world = dist.get_world_size(group)
+    loss = net.backward(features, target, read_loss=read_loss)
+    dev = _is_cuda(features)
+    on_device = dev and dist.get_backend(group) == "nccl"
+    g = torch.empty(net.param_count + 1, dtype=torch.float32, device=features.device if dev else "cpu")
+    if dev:
+        net.read_grads(g[:-1])
+    else:
+        net.read_grads(g[:-1].numpy())
+    g[-1] = float(loss) if read_loss else 0.0
+    buf = g if (on_device or not dev) else g.cpu()
+    dist.all_reduce(buf, group=group)
+    buf /= world
+    if buf is not g:
+        g.copy_(buf)
+    if dev:
+        net.write_grads(g[:-1])
+    else:
+        net.write_grads(g[:-1].numpy())
+    net.adam_step(lr)
+    return float(buf[-1]) if read_loss else None
 
 
 def train(denoiser, feats, targets, steps: int, batch: int = 8, crop: int = 64, lr: float = 2e-3, seed: int = 0,
