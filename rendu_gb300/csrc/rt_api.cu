@@ -117,6 +117,9 @@ int require_built(rt_ctx *ctx) {
     return RT_OK;
 }
 
+// The traversal kernels read rays and write hits as 16-byte vectors.
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
 bool is_pageable(const void *p) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -403,6 +406,10 @@ int rt_intersect(rt_ctx *ctx, const rt_ray *rays, size_t n, rt_hit *hits, void *
     }
     DeviceGuard g(ctx->device);
     if (flags & RT_FLAG_DEVICE_PTRS) {
+        if (!aligned16(rays) || !aligned16(hits)) {
+            set_error("device ray and hit buffers must be 16-byte aligned");
+            return RT_ERR_ARG;
+        }
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         return trace_closest(ctx, rays, n, hits, st);
     }
@@ -422,6 +429,10 @@ int rt_intersect_any(rt_ctx *ctx, const rt_ray *rays, size_t n, uint8_t *occlude
     }
     DeviceGuard g(ctx->device);
     if (flags & RT_FLAG_DEVICE_PTRS) {
+        if (!aligned16(rays)) {
+            set_error("device ray buffers must be 16-byte aligned");
+            return RT_ERR_ARG;
+        }
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         return trace_any(ctx, rays, n, occluded, st);
     }
@@ -472,6 +483,10 @@ int rt_count_visits(rt_ctx *ctx, const rt_ray *rays, size_t n, uint32_t *node_vi
     }
     DeviceGuard g(ctx->device);
     if (flags & RT_FLAG_DEVICE_PTRS) {
+        if (!aligned16(rays)) {
+            set_error("device ray buffers must be 16-byte aligned");
+            return RT_ERR_ARG;
+        }
         if (ctx->d_out2.reserve(n * sizeof(rt_hit)) != RT_OK) return RT_ERR_OOM;
         return trace_count(ctx, rays, n, node_visits, tri_visits, ctx->d_out2.as<rt_hit>(),
                            static_cast<cudaStream_t>(stream));

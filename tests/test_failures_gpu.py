@@ -143,3 +143,38 @@ def test_shadow_walk_through_too_many_cut_outs_times_out(cuda_lib):
     tr.render(bad.camera, 1, 1, img, seed=1)
     assert np.isfinite(img).all() and img.mean() > 0.0
     tr.close()
+
+
+def test_misaligned_device_buffers_are_rejected(cuda_lib):
+    """The traversal reads rays and writes hits as 16-byte vectors: device pointers that are
+    not 16-byte aligned are refused before anything is launched."""
+    import torch
+
+    import rendu_gb300 as R
+    import rendu_gb300._lib as L
+    from rendu_gb300 import scenes as S
+
+    mesh = S.icosphere_mesh(2, seed=1)
+    rc = R.Raycaster(0)
+    rc.add_mesh(mesh.positions, mesh.indices)
+    rc.updateHierarchy()
+    raw = torch.zeros(8 * 64 + 4, dtype=torch.float32, device="cuda")
+    hits = torch.zeros(4 * 64 + 4, dtype=torch.float32, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    lib = L.lib()
+    for name, out in (("rt_intersect", hits), ("rt_intersect_any", hits)):
+        f = getattr(lib, name)
+        f.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_uint32]
+        code = f(C.c_void_p(rc.handle), C.c_void_p(raw.data_ptr() + 4), 64, C.c_void_p(out.data_ptr()), stream,
+                 L.RT_FLAG_DEVICE_PTRS)
+        assert code == L.RT_ERR_ARG, name
+    f = lib.rt_intersect
+    code = f(C.c_void_p(rc.handle), C.c_void_p(raw.data_ptr()), 64, C.c_void_p(hits.data_ptr() + 4), stream,
+             L.RT_FLAG_DEVICE_PTRS)
+    assert code == L.RT_ERR_ARG
+    # aligned buffers still work
+    assert f(C.c_void_p(rc.handle), C.c_void_p(raw.data_ptr()), 64, C.c_void_p(hits.data_ptr()), stream,
+             L.RT_FLAG_DEVICE_PTRS) == L.RT_OK
+    torch.cuda.synchronize()
+    assert rc.status() == L.RT_OK
+    rc.close()
