@@ -56,6 +56,9 @@ constexpr int KB = 64;        // K per stage: one 128-byte swizzle row of BF16
 #define DN_MAX_STAGES 8
 #endif
 constexpr int MAX_STAGES = DN_MAX_STAGES;
+#ifndef DN_TMA_STORE
+#define DN_TMA_STORE 1  // folded tiles store their BF16 output with TMA bulk stores
+#endif
 #ifndef DN_EPI_GROUPS
 #define DN_EPI_GROUPS 4
 #endif
@@ -120,6 +123,25 @@ __device__ __forceinline__ void tma_4d(unsigned dst, const CUtensorMap *map, int
         "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
         : "memory");
 }
+// Bulk tensor store of a shared-memory box (bulk-group completion); the box's coordinates
+// outside the tensor are not written.
+__device__ __forceinline__ void tma_store_4d(const CUtensorMap *map, unsigned src, int c0, int c1, int c2, int c3) {
+    asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%1, %2, %3, %4}], [%5];\n" ::"l"(
+                     reinterpret_cast<unsigned long long>(map)),
+                 "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(src)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+}
+// Named barrier of `threads` threads that also returns whether `pred` held for all of them.
+__device__ __forceinline__ bool bar_and(int id, int threads, bool pred) {
+    int r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.s32 p, %1, 0;\n bar.red.and.pred q, %2, %3, p;\n selp.s32 %0, 1, 0, q;\n}\n"
+        : "=r"(r)
+        : "r"((int)pred), "r"(id), "r"(threads)
+        : "memory");
+    return r != 0;
+}
 __device__ __forceinline__ void tma_2d(unsigned dst, const CUtensorMap *map, int c0, int c1, unsigned bar) {
     asm volatile(
         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
@@ -177,6 +199,8 @@ struct ConvTiles {
     const float *fin_feat;  // the finished output layer (FOut)
     float *fin_out;
     int fin_H, fin_W;
+    int tstore;     // folded tiles: the BF16 output goes out through shared memory and TMA stores
+    unsigned obuf;  // bytes of an epilogue group's output buffer (FOLD_OUT pixels x Cout)
 };
 
 // K steps of 16 that chunk j actually holds: the MMAs over a chunk's zero-filled channels
@@ -255,6 +279,29 @@ __device__ __forceinline__ void store16(const ConvTiles &q, const unsigned (&v)[
 // thread as soon as its last columns are in registers, before the bias, ReLU and NHWC
 // stores of those. Several groups keep several tiles' stores in flight on each SM
 // sub-partition. False if a wait gave up.
+// 16 output channels [cb, cb + 16) of a pixel into shared memory at `dst` (BF16, bias from
+// shared memory, ReLU; channels past Cout dropped), for the group's TMA store.
+__device__ __forceinline__ void store16_smem(const ConvTiles &q, const unsigned (&v)[16], int cb, unsigned dst,
+                                             const float *sbias) {
+    unsigned h[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        float a = __uint_as_float(v[2 * j]) + sbias[cb + 2 * j], b = __uint_as_float(v[2 * j + 1]) + sbias[cb + 2 * j + 1];
+        if (q.relu) {
+            a = fmaxf(a, 0.0f);
+            b = fmaxf(b, 0.0f);
+        }
+        const __nv_bfloat162 t = __floats2bfloat162_rn(a, b);
+        h[j] = *reinterpret_cast<const unsigned *>(&t);
+    }
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" ::"r"(dst), "r"(h[0]), "r"(h[1]), "r"(h[2]), "r"(h[3])
+                 : "memory");
+    if (cb + 16 <= q.Cout)  // Cout is a multiple of 8: the last group may hold 8 channels
+        asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" ::"r"(dst + 16u), "r"(h[4]), "r"(h[5]), "r"(h[6]),
+                     "r"(h[7])
+                     : "memory");
+}
+
 template <bool XO, class Origin>
 __device__ __forceinline__ bool epilogue(const ConvTiles &q, unsigned tmem, unsigned bar0, int my_tiles,
                                          const Origin &tile_origin) {
@@ -647,22 +694,41 @@ __device__ __forceinline__ void mma_rows3(unsigned d, unsigned long long ad, uns
 
 // Epilogue of the folded tiles: group g reads accumulator g, 16 output channels at a time
 // (columns c0, N + c0, 2N + c0), adds each row's neighbours' columns and stores lanes 1..30.
+// With q.tstore (BF16 output, XO false) the group's four warps write the tile into their
+// shared-memory buffer `obuf0 + g * q.obuf` ([pixel][channel], FOLD_OUT pixels) and one
+// thread stores it with a TMA bulk store; the group's named barrier (id 1 + g) orders the
+// buffer's reuse, and every warp of the group takes the same exits.
 template <bool XO, class Origin>
 __device__ __forceinline__ bool epilogue_fold(const ConvTiles &q, unsigned tmem, unsigned bar0, const float *sbias,
-                                              int my_tiles, const Origin &tile_origin) {
+                                              int my_tiles, const Origin &tile_origin, const CUtensorMap *tmo,
+                                              unsigned obuf0) {
     const int warp = threadIdx.x >> 5, g = warp / EPI_WARPS, quarter = warp % EPI_WARPS;
     const int lane = threadIdx.x & 31;
     if (g >= q.groups) return true;
     const unsigned tfull = bar0 + 8u * (BAR_TFULL + g), tempty = bar0 + 8u * (BAR_TEMPTY + g);
+    const bool ts = !XO && q.tstore;
+    const bool leader = quarter == 0 && lane == 0;
+    const unsigned ob = obuf0 + (unsigned)g * q.obuf;
     unsigned use = 0;
     for (int lt = g; lt < my_tiles; lt += q.groups, ++use) {
-        if (!__all_sync(0xffffffffu, mbar_wait(tfull, use & 1u))) return false;
+        const bool okw = __all_sync(0xffffffffu, mbar_wait(tfull, use & 1u));
+        if (ts) {
+            // The buffer is free once the previous bulk store has read it.
+            if (leader) asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+            if (!bar_and(1 + g, 32 * EPI_WARPS, okw)) {
+                if (leader) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
+                return false;
+            }
+        } else if (!okw) {
+            return false;
+        }
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
         int x0, y0, n, n0;
         tile_origin((int)blockIdx.x + lt * (int)gridDim.x, x0, y0, n, n0);
         const int x = x0 - 1 + FOLD_STEP * quarter + lane;
         const bool store = lane >= 1 && lane <= FOLD_STEP && x < q.W;
         const long p = ((long)n * q.H + y0) * q.W + x;
+        const unsigned orow = ob + (unsigned)((x - x0) * q.Cout) * 2u;  // this pixel's row of the buffer
         const unsigned taddr = tmem + ((unsigned)(32 * quarter) << 16) + (unsigned)(g * q.nhalf);
         for (int c0 = 0; c0 < q.N; c0 += 16) {
             unsigned b0[16], b1[16], b2[16];
@@ -682,16 +748,25 @@ __device__ __forceinline__ bool epilogue_fold(const ConvTiles &q, unsigned tmem,
                 v[j] = __float_as_uint(up + __uint_as_float(b1[j]) + dn);
             }
             const int cb = n0 + c0;
-            if (store && cb < q.Cout) store16<XO>(q, v, cb, p, sbias);
+            if (store && cb < q.Cout) {
+                if (ts) store16_smem(q, v, cb, orow + (unsigned)cb * 2u, sbias);
+                else store16<XO>(q, v, cb, p, sbias);
+            }
+        }
+        if (ts) {
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            bar_and(1 + g, 32 * EPI_WARPS, true);
+            if (leader) tma_store_4d(tmo, ob, 0, x0, y0, n);
         }
     }
+    if (ts && leader) asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
     return true;
 }
 
 template <bool XO>
 __global__ void __launch_bounds__(THREADS, 1)
     k_conv_fold(const __grid_constant__ CUtensorMap tm0, const __grid_constant__ CUtensorMap tm1,
-                const __grid_constant__ CUtensorMap tmw, const ConvTiles q) {
+                const __grid_constant__ CUtensorMap tmw, const __grid_constant__ CUtensorMap tmo, const ConvTiles q) {
     extern __shared__ unsigned char smem_raw[];
     const unsigned raw = saddr(smem_raw);
     const unsigned base = (raw + 1023u) & ~1023u;
@@ -710,6 +785,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     const unsigned wfull = bar0 + 8u * BAR_W;
     const unsigned *tmem_slot_ptr = reinterpret_cast<const unsigned *>(smem_raw + (tmem_slot - raw));
     float *sbias = reinterpret_cast<float *>(smem_raw + (bar0 + 8u * BAR_COUNT - raw));  // N floats
+    // the epilogue groups' output buffers (q.tstore), 128-byte aligned after the bias
+    const unsigned obuf0 = (bar0 + 8u * BAR_COUNT + 1024u + 127u) & ~127u;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int my_tiles = q.ntiles > (int)blockIdx.x ? (q.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
@@ -830,7 +907,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         __syncwarp();
     } else {
-        ok = epilogue_fold<XO>(q, tmem, bar0, sbias, my_tiles, tile_origin);
+        ok = epilogue_fold<XO>(q, tmem, bar0, sbias, my_tiles, tile_origin, &tmo, obuf0);
     }
     if (!ok) atomicOr(&g_umma_status, 1u);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
@@ -1261,6 +1338,26 @@ int map_weights(CUtensorMap *m, const bf16 *ptr, int Kp, int rows, int N) {
     return RT_OK;
 }
 
+// A layer's BF16 output (B, H, W, C) written as boxes of FOLD_OUT pixels x all C channels
+// from a plain [pixel][channel] shared-memory buffer.
+int map_output(CUtensorMap *m, const bf16 *ptr, int B, int H, int W, int C) {
+    EncodeTiled enc;
+    int r = encoder(&enc);
+    if (r != RT_OK) return r;
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)C, (cuuint32_t)FOLD_OUT, 1, 1};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult e = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(ptr), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (e != CUDA_SUCCESS) {
+        set_error("output tensor map rejected (error " + std::to_string((int)e) + ")");
+        return RT_ERR_CUDA;
+    }
+    return RT_OK;
+}
+
 inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
@@ -1312,6 +1409,8 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
     q.fin_out = fo.finish_out;
     q.fin_H = fo.H;
     q.fin_W = fo.W;
+    q.tstore = 0;
+    q.obuf = 0;
     q.wres = 0;
     q.narrow0 = q.narrow1 = 0;
     q.astage = 0;
@@ -1334,8 +1433,16 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
             q.groups = std::min(EPI_GROUPS, 512 / q.nhalf);
             q.wres = 1;
             q.astage = (unsigned)fstage;
-            q.stages = (int)std::min<size_t>(MAX_STAGES, (budget - wbytes) / fstage);
-            smem = kFixed + wbytes + q.stages * fstage;
+            // BF16 outputs leave through the groups' shared-memory buffers and TMA stores when
+            // the buffers fit beside two stages.
+            const size_t obuf = ((size_t)FOLD_OUT * Cout * 2 + 127) / 128 * 128;
+            const size_t stores = (size_t)q.groups * obuf + 128;
+            q.tstore = DN_TMA_STORE && out_bf && !out_f && !fo.finish_out && Cout % 8 == 0 &&
+                       wbytes + stores + 2 * fstage <= budget;
+            q.obuf = q.tstore ? (unsigned)obuf : 0u;
+            const size_t left = budget - wbytes - (q.tstore ? stores : 0);
+            q.stages = (int)std::min<size_t>(MAX_STAGES, left / fstage);
+            smem = kFixed + wbytes + q.stages * fstage + (q.tstore ? stores : 0);
         } else {
             q.astage = narrow_all ? HALO32_STAGE : HALO_STAGE;
             q.wres = q.ntiles == q.mtiles && wbytes + 4 * (size_t)q.astage <= budget;
@@ -1360,6 +1467,8 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
             tm1 = tm0;
     }
     if (r == RT_OK) r = map_weights(&tmw, wpk, (int)packed_k(in.c0, in.c1), Cout, q.N);
+    CUtensorMap tmo = tmw;  // unused unless q.tstore
+    if (r == RT_OK && q.tstore) r = map_output(&tmo, out_bf, B, H, W, Cout);
     if (r != RT_OK) return r;
 
     static bool configured = false;
@@ -1379,7 +1488,7 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
     // epilogues keep their registers.
     const bool xo = fo.finish_out != nullptr;
     if (fold)
-        (xo ? k_conv_fold<true> : k_conv_fold<false>)<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
+        (xo ? k_conv_fold<true> : k_conv_fold<false>)<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, tmo, q);
     else if (rows)
         (xo ? k_conv_rows<true> : k_conv_rows<false>)<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
     else
