@@ -535,7 +535,8 @@ RT_API int dn_denoise(dn_net *net, const float *features, uint32_t width, uint32
 RT_API int dn_backward(dn_net *net, const float *features, const float *target, uint32_t width, uint32_t height,
                        uint32_t batch, float *loss, void *stream, uint32_t flags);
 /* One Adam step (beta 0.9, 0.999, eps 1e-8) with learning rate lr on the last gradients,
- * ordered on `stream` (NULL: the network's own stream, and the call blocks). */
+ * ordered on `stream` (NULL: on the network's own stream after all work already queued on
+ * the device, including the legacy default stream's; the call blocks). */
 RT_API int dn_adam_step(dn_net *net, float lr, void *stream);
 /* dn_backward + dn_adam_step. */
 RT_API int dn_train_step(dn_net *net, const float *features, const float *target, uint32_t width, uint32_t height,

@@ -660,6 +660,10 @@ RT_API int dn_adam_step(dn_net *n, float lr, void *stream) {
     if (!n) return arg_error("null network");
     DeviceGuard guard(n->device);
     cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : n->stream;
+    // NULL: the network's own stream, after everything already queued on the device (the
+    // gradients may have been written on the legacy default stream, which the network's
+    // non-blocking stream does not wait for), and the call blocks.
+    if (!stream) RT_CUDA_TRY(cudaDeviceSynchronize());
     int r = set_lr(n, lr, st);
     if (r == RT_OK) r = adam_launch(n, st);
     if (r == RT_OK && !stream) RT_CUDA_TRY(cudaStreamSynchronize(st));

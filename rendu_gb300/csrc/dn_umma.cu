@@ -199,7 +199,8 @@ struct ConvTiles {
     const float *fin_feat;  // the finished output layer (FOut)
     float *fin_out;
     int fin_H, fin_W;
-    int tstore;     // folded tiles: the BF16 output goes out through shared memory and TMA stores
+    int tstore;     // folded tiles: the output goes out through shared memory and TMA stores
+                    // (1: BF16 out_bf, 2: FP32 out_f)
     unsigned obuf;  // bytes of an epilogue group's output buffer (FOLD_OUT pixels x Cout)
 };
 
@@ -300,6 +301,23 @@ __device__ __forceinline__ void store16_smem(const ConvTiles &q, const unsigned 
         asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" ::"r"(dst + 16u), "r"(h[4]), "r"(h[5]), "r"(h[6]),
                      "r"(h[7])
                      : "memory");
+}
+
+// The same for an FP32 output: 16 floats, channels past Cout dropped.
+__device__ __forceinline__ void store16_smem_f32(const ConvTiles &q, const unsigned (&v)[16], int cb, unsigned dst,
+                                                 const float *sbias) {
+    float f[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        f[j] = __uint_as_float(v[j]) + sbias[cb + j];
+        if (q.relu) f[j] = fmaxf(f[j], 0.0f);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        if (cb + 4 * k < q.Cout)
+            asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};\n" ::"r"(dst + 16u * k), "f"(f[4 * k]),
+                         "f"(f[4 * k + 1]), "f"(f[4 * k + 2]), "f"(f[4 * k + 3])
+                         : "memory");
 }
 
 template <bool XO, class Origin>
@@ -694,7 +712,7 @@ __device__ __forceinline__ void mma_rows3(unsigned d, unsigned long long ad, uns
 
 // Epilogue of the folded tiles: group g reads accumulator g, 16 output channels at a time
 // (columns c0, N + c0, 2N + c0), adds each row's neighbours' columns and stores lanes 1..30.
-// With q.tstore (BF16 output, XO false) the group's four warps write the tile into their
+// With q.tstore (BF16 or FP32 output, XO false) the group's four warps write the tile into their
 // shared-memory buffer `obuf0 + g * q.obuf` ([pixel][channel], FOLD_OUT pixels) and one
 // thread stores it with a TMA bulk store; the group's named barrier (id 1 + g) orders the
 // buffer's reuse, and every warp of the group takes the same exits.
@@ -728,7 +746,8 @@ __device__ __forceinline__ bool epilogue_fold(const ConvTiles &q, unsigned tmem,
         const int x = x0 - 1 + FOLD_STEP * quarter + lane;
         const bool store = lane >= 1 && lane <= FOLD_STEP && x < q.W;
         const long p = ((long)n * q.H + y0) * q.W + x;
-        const unsigned orow = ob + (unsigned)((x - x0) * q.Cout) * 2u;  // this pixel's row of the buffer
+        const unsigned esz = q.tstore == 2 ? 4u : 2u;
+        const unsigned orow = ob + (unsigned)((x - x0) * q.Cout) * esz;  // this pixel's row of the buffer
         const unsigned taddr = tmem + ((unsigned)(32 * quarter) << 16) + (unsigned)(g * q.nhalf);
         for (int c0 = 0; c0 < q.N; c0 += 16) {
             unsigned b0[16], b1[16], b2[16];
@@ -749,7 +768,8 @@ __device__ __forceinline__ bool epilogue_fold(const ConvTiles &q, unsigned tmem,
             }
             const int cb = n0 + c0;
             if (store && cb < q.Cout) {
-                if (ts) store16_smem(q, v, cb, orow + (unsigned)cb * 2u, sbias);
+                if (ts && q.tstore == 2) store16_smem_f32(q, v, cb, orow + (unsigned)cb * 4u, sbias);
+                else if (ts) store16_smem(q, v, cb, orow + (unsigned)cb * 2u, sbias);
                 else store16<XO>(q, v, cb, p, sbias);
             }
         }
@@ -1338,17 +1358,19 @@ int map_weights(CUtensorMap *m, const bf16 *ptr, int Kp, int rows, int N) {
     return RT_OK;
 }
 
-// A layer's BF16 output (B, H, W, C) written as boxes of FOLD_OUT pixels x all C channels
-// from a plain [pixel][channel] shared-memory buffer.
-int map_output(CUtensorMap *m, const bf16 *ptr, int B, int H, int W, int C) {
+// A layer's output (B, H, W, C), BF16 or FP32, written as boxes of FOLD_OUT pixels x all C
+// channels from a plain [pixel][channel] shared-memory buffer.
+int map_output(CUtensorMap *m, const void *ptr, int B, int H, int W, int C, bool f32) {
     EncodeTiled enc;
     int r = encoder(&enc);
     if (r != RT_OK) return r;
+    const cuuint64_t es = f32 ? 4 : 2;
     const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
-    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    const cuuint64_t strides[3] = {(cuuint64_t)C * es, (cuuint64_t)W * C * es, (cuuint64_t)H * W * C * es};
     const cuuint32_t box[4] = {(cuuint32_t)C, (cuuint32_t)FOLD_OUT, 1, 1};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
-    const CUresult e = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(ptr), dims, strides, box, estr,
+    const CUresult e = enc(m, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
+                           const_cast<void *>(ptr), dims, strides, box, estr,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (e != CUDA_SUCCESS) {
@@ -1435,10 +1457,14 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
             q.astage = (unsigned)fstage;
             // BF16 outputs leave through the groups' shared-memory buffers and TMA stores when
             // the buffers fit beside two stages.
-            const size_t obuf = ((size_t)FOLD_OUT * Cout * 2 + 127) / 128 * 128;
+            const int esz = out_f ? 4 : 2;
+            const size_t obuf = ((size_t)FOLD_OUT * Cout * esz + 127) / 128 * 128;
             const size_t stores = (size_t)q.groups * obuf + 128;
-            q.tstore = DN_TMA_STORE && out_bf && !out_f && !fo.finish_out && Cout % 8 == 0 &&
-                       wbytes + stores + 2 * fstage <= budget;
+            const bool one_out = (out_bf != nullptr) != (out_f != nullptr);
+            q.tstore = (DN_TMA_STORE && one_out && !fo.finish_out && Cout % 8 == 0 &&
+                        wbytes + stores + 2 * fstage <= budget)
+                           ? (out_f ? 2 : 1)
+                           : 0;
             q.obuf = q.tstore ? (unsigned)obuf : 0u;
             const size_t left = budget - wbytes - (q.tstore ? stores : 0);
             q.stages = (int)std::min<size_t>(MAX_STAGES, left / fstage);
@@ -1468,7 +1494,9 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
     }
     if (r == RT_OK) r = map_weights(&tmw, wpk, (int)packed_k(in.c0, in.c1), Cout, q.N);
     CUtensorMap tmo = tmw;  // unused unless q.tstore
-    if (r == RT_OK && q.tstore) r = map_output(&tmo, out_bf, B, H, W, Cout);
+    if (r == RT_OK && q.tstore)
+        r = map_output(&tmo, q.tstore == 2 ? static_cast<const void *>(out_f) : static_cast<const void *>(out_bf), B, H,
+                       W, Cout, q.tstore == 2);
     if (r != RT_OK) return r;
 
     static bool configured = false;
