@@ -278,7 +278,7 @@ int forward(dn_net *n, cudaStream_t st, const FOut &last) {
             r = conv_forward_umma(in, n->B, n->Hp >> o.level, n->Wp >> o.level, n->wk.as<bf16>() + c.wk_off,
                                   n->params.as<float>() + c.boff, c.cout, c.relu != 0, o.f32 ? nullptr : n->bf(c.out),
                                   o.f32 && !last.finish_out ? n->f(c.out) : nullptr, n->ups.as<bf16>(), st,
-                                  o.f32 ? last : FOut());
+                                  o.f32 ? last : FOut(), true);
         }
         if (r != RT_OK) return r;
     }
@@ -335,7 +335,7 @@ int backward(dn_net *n, const float *target, cudaStream_t st) {
         const bool split = c.cin1 || c.up0;
         float *dst = split ? n->gin.as<float>() : n->g(c.src0);
         r = conv_forward_umma(gi, n->B, H, W, n->wkd.as<bf16>() + c.wkd_off, nullptr, c.cin0 + c.cin1, false, nullptr,
-                              dst, nullptr, st);
+                              dst, nullptr, st, FOut(), true);
         if (r == RT_OK && split)
             r = split_grad(dst, n->B, H, W, c.cin0, c.up0, c.cin1, n->g(c.src0), c.src1 >= 0 ? n->g(c.src1) : nullptr,
                            st);

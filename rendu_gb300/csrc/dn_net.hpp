@@ -70,8 +70,12 @@ size_t packed_k(int c0, int c1);
 // in[p + off(tap), ci] w[tap][ci][co]) with the weights packed by pack_weights; with the
 // data-gradient packing it computes a layer's input gradient. An upsampled input 0 is
 // first expanded into `ups` (B x H x W x c0 BF16). Cout a multiple of 8.
+// pdl: launch as a programmatic dependent of the previous kernel on st (its prologue reads
+// the weights and bias before waiting for that kernel, so they must not come from it: the
+// network's own packed weights, not a caller's freshly written buffers).
 int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, const float *bias, int Cout, bool relu,
-                      bf16 *out_bf, float *out_f, bf16 *ups, cudaStream_t st, const FOut &fo = FOut());
+                      bf16 *out_bf, float *out_f, bf16 *ups, cudaStream_t st, const FOut &fo = FOut(),
+                      bool pdl = false);
 // w FP32 [tap][c0 + c1][Cout] -> wpk [Cout][packed_k(c0, c1)] (forward) and
 // wpkd [c0 + c1][packed_k(Cout, 0)] (data gradient, taps mirrored); either may be null.
 int pack_weights(const float *w, int c0, int c1, int Cout, bf16 *wpk, bf16 *wpkd, cudaStream_t st);

@@ -56,6 +56,9 @@ constexpr int KB = 64;        // K per stage: one 128-byte swizzle row of BF16
 #define DN_MAX_STAGES 8
 #endif
 constexpr int MAX_STAGES = DN_MAX_STAGES;
+#ifndef DN_PDL
+#define DN_PDL 1  // convolutions launched as programmatic dependents of the kernel before them
+#endif
 #ifndef DN_TMA_STORE
 #define DN_TMA_STORE 1  // folded tiles store their BF16 output with TMA bulk stores
 #endif
@@ -123,6 +126,14 @@ __device__ __forceinline__ void tma_4d(unsigned dst, const CUtensorMap *map, int
         "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
         : "memory");
 }
+// Programmatic dependent launch: a convolution launched with the programmatic-serialization
+// attribute may start while the kernel before it on the stream finishes. Its prologue
+// (barriers, TMEM, bias, resident weights: data no kernel of the chain writes) runs at once;
+// griddep_wait() blocks until the previous kernel has completed and its writes are visible,
+// before the first read of an activation. griddep_launch() lets the next kernel start early.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
 // Bulk tensor store of a shared-memory box (bulk-group completion); the box's coordinates
 // outside the tensor are not written.
 __device__ __forceinline__ void tma_store_4d(const CUtensorMap *map, unsigned src, int c0, int c1, int c2, int c3) {
@@ -410,10 +421,12 @@ __global__ void __launch_bounds__(THREADS, 1)
     const unsigned tmem = *tmem_slot_ptr;
     bool ok = true;
 
+    griddep_launch();
     if (warp == PRODUCER_WARP) {
         // ---- TMA producer: one thread. Stage index and phase advance incrementally (this
         // thread's issue rate bounds the pipeline: no divisions in the loop).
         if (lane == 0) {
+            griddep_wait();
             const unsigned tx_bytes = a_bytes + (unsigned)q.N * 128;
             int st = 0;
             unsigned ph = 0;     // parity of the current use of stage st
@@ -580,6 +593,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     const unsigned tmem = *tmem_slot_ptr;
     bool ok = true;
 
+    griddep_launch();
     if (warp == PRODUCER_WARP) {
         // ---- TMA producer: one thread.
         if (lane == 0) {
@@ -587,6 +601,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 mbar_expect_tx(wfull, wbytes);
                 for (int kb = 0; kb < KT; ++kb) tma_2d(base + kb * kblk, &tmw, kb * KB, 0, wfull);
             }
+            griddep_wait();
             const unsigned wtx = q.wres ? 0u : 3u * kblk;
             int st = 0;
             unsigned ph = 0;
@@ -843,6 +858,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     const unsigned tmem = *tmem_slot_ptr;
     bool ok = true;
 
+    griddep_launch();
     if (warp == PRODUCER_WARP) {
         if (lane == 0) {
             if (my_tiles > 0) {
@@ -853,6 +869,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     tma_2d(base + (unsigned)((dy * q.cpt + j) * 3 + dx) * kblk, &tmw, kb * KB, 0, wfull);
                 }
             }
+            griddep_wait();
             int st = 0;
             unsigned ph = 0;
             bool refill = false;
@@ -1387,7 +1404,7 @@ inline unsigned blocks(size_t n, int t = 256) { return (unsigned)((n + t - 1) / 
 size_t packed_k(int c0, int c1) { return (size_t)9 * ((c0 + 63) / 64 + (c1 + 63) / 64) * 64; }
 
 int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, const float *bias, int Cout, bool relu,
-                      bf16 *out_bf, float *out_f, bf16 *ups, cudaStream_t st, const FOut &fo) {
+                      bf16 *out_bf, float *out_f, bf16 *ups, cudaStream_t st, const FOut &fo, bool pdl) {
     if (fo.finish_out && (Cout % 16 != 0 || !fo.feat || fo.H > H || fo.W > W || out_f || out_bf)) {
         set_error("a finished convolution output needs Cout a multiple of 16, the features and no other output");
         return RT_ERR_ARG;
@@ -1515,13 +1532,25 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
     // The finished output layer is a separate instantiation, so that the other layers'
     // epilogues keep their registers.
     const bool xo = fo.finish_out != nullptr;
+    // With pdl, launched with programmatic stream serialisation: the kernel may start while
+    // the previous kernel on the stream drains; it waits for it (griddep_wait) before reading
+    // activations. (Without the attribute griddep_wait returns at once.)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = (DN_PDL && pdl) ? 1 : 0;
     if (fold)
-        (xo ? k_conv_fold<true> : k_conv_fold<false>)<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, tmo, q);
+        RT_CUDA_TRY(cudaLaunchKernelEx(&cfg, xo ? k_conv_fold<true> : k_conv_fold<false>, tm0, tm1, tmw, tmo, q));
     else if (rows)
-        (xo ? k_conv_rows<true> : k_conv_rows<false>)<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
+        RT_CUDA_TRY(cudaLaunchKernelEx(&cfg, xo ? k_conv_rows<true> : k_conv_rows<false>, tm0, tm1, tmw, q));
     else
-        (xo ? k_conv_umma<true> : k_conv_umma<false>)<<<grid, THREADS, smem, st>>>(tm0, tm1, tmw, q);
-    RT_CUDA_TRY(cudaGetLastError());
+        RT_CUDA_TRY(cudaLaunchKernelEx(&cfg, xo ? k_conv_umma<true> : k_conv_umma<false>, tm0, tm1, tmw, q));
     return RT_OK;
 }
 
