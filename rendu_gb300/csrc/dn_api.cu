@@ -265,7 +265,7 @@ int forward(dn_net *n, cudaStream_t st, const FOut &last) {
         int r;
         if (op.pool) {
             const Tensor &s = n->tensors[op.src];
-            r = pool(n->bf(op.src), n->B, n->Hp >> s.level, n->Wp >> s.level, s.ch, n->bf(op.out), st);
+            r = pool(n->bf(op.src), n->B, n->Hp >> s.level, n->Wp >> s.level, s.ch, n->bf(op.out), st, true);
         } else {
             const Conv &c = n->convs[op.conv];
             const Tensor &o = n->tensors[c.out];

@@ -121,6 +121,8 @@ __global__ void k_pool(const bf16 *__restrict__ x, int B, int H, int W, int C, b
 // The same, 8 channels a thread (C a multiple of 8): four 16-byte loads, one 16-byte store.
 // The maximum of BF16 values is exact, so the result equals k_pool's.
 __global__ void k_pool8(const bf16 *__restrict__ x, int B, int H, int W, int C, bf16 *__restrict__ y) {
+    griddep_wait();  // a programmatic dependent of the convolution that wrote x
+    griddep_launch();
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     const int h = H / 2, w = W / 2, c8 = C / 8;
     const size_t n = (size_t)B * h * w * c8;
@@ -376,9 +378,10 @@ int reduce_chunks(const float *partial, int chunks, size_t n, float *out, cudaSt
 
 size_t colsum_partial_floats(long P, int C) { return (size_t)((P + relu_rows(P) - 1) / relu_rows(P)) * C; }
 
-int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st) {
+int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st, bool pdl) {
     if (C % 8 == 0)
-        k_pool8<<<blocks((size_t)B * (H / 2) * (W / 2) * (C / 8)), 256, 0, st>>>(x, B, H, W, C, y);
+        RT_CUDA_TRY(launch_pdl(k_pool8, dim3(blocks((size_t)B * (H / 2) * (W / 2) * (C / 8))), dim3(256), 0, st, pdl, x, B,
+                               H, W, C, y));
     else
         k_pool<<<blocks((size_t)B * (H / 2) * (W / 2) * C), 256, 0, st>>>(x, B, H, W, C, y);
     RT_CUDA_TRY(cudaGetLastError());

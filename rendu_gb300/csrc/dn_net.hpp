@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <utility>
 #include <vector>
 
 #include "rt_context.hpp"
@@ -63,6 +64,29 @@ struct FOut {
     int H = 0, W = 0;
 };
 
+// Programmatic dependent launch: a kernel launched with the programmatic-serialisation
+// attribute (launch_pdl with pdl) may start while the kernel before it on the stream
+// finishes; griddep_wait() blocks until that kernel has completed and its writes are
+// visible (at once without the attribute), griddep_launch() lets the next such kernel start.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+
+template <class... P, class... A>
+cudaError_t launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl,
+                       A &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
+
 // ---- launchers (asynchronous on st; RT_OK or RT_ERR_CUDA) -------------------------------------
 // Length of a packed weight row: 9 taps x (64-channel chunks of input 0 + of input 1) x 64.
 size_t packed_k(int c0, int c1);
@@ -94,7 +118,7 @@ size_t wgrad_partial_floats(long P, int Cin, int Cout);
 int reduce_chunks(const float *partial, int chunks, size_t n, float *out, cudaStream_t st);
 // Scratch floats of relu_grad_bias's bias-gradient partials.
 size_t colsum_partial_floats(long P, int C);
-int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st);
+int pool(const bf16 *x, int B, int H, int W, int C, bf16 *y, cudaStream_t st, bool pdl = false);
 int pool_back(const bf16 *x, const bf16 *y, const float *gy, int B, int H, int W, int C, float *gx, cudaStream_t st);
 int split_grad(const float *gin, int B, int H, int W, int c0, int up0, int c1, float *g0, float *g1, cudaStream_t st);
 // The ReLU gradient (g with zeros where the forward output y was not positive, as a BF16 copy

@@ -126,13 +126,9 @@ __device__ __forceinline__ void tma_4d(unsigned dst, const CUtensorMap *map, int
         "l"(reinterpret_cast<unsigned long long>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
         : "memory");
 }
-// Programmatic dependent launch: a convolution launched with the programmatic-serialization
-// attribute may start while the kernel before it on the stream finishes. Its prologue
-// (barriers, TMEM, bias, resident weights: data no kernel of the chain writes) runs at once;
-// griddep_wait() blocks until the previous kernel has completed and its writes are visible,
-// before the first read of an activation. griddep_launch() lets the next kernel start early.
-__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
-__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+// Programmatic dependent launch (griddep_wait / griddep_launch, dn_net.hpp): a convolution's
+// prologue (barriers, TMEM, bias, resident weights: data no kernel of the chain writes) runs
+// while the kernel before it drains; its producer waits before the first activation load.
 
 // Bulk tensor store of a shared-memory box (bulk-group completion); the box's coordinates
 // outside the tensor are not written.
@@ -958,6 +954,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 // Nearest 2x upsampling, NHWC: y (B, 2h, 2w, C) from x (B, h, w, C); a thread copies 8
 // channels of one input pixel to its 2 x 2 output pixels.
 __global__ void k_upsample2(const bf16 *__restrict__ x, int B, int h, int w, int C, bf16 *__restrict__ y) {
+    griddep_wait();  // a programmatic dependent of the kernel that wrote x
+    griddep_launch();
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     const int c8 = C / 8;
     const size_t n = (size_t)B * h * w * c8;
@@ -1416,8 +1414,8 @@ int conv_forward_umma(const ConvIn &in, int B, int H, int W, const bf16 *wpk, co
             return RT_ERR_ARG;
         }
         const size_t n8 = (size_t)B * (H / 2) * (W / 2) * (in.c0 / 8);
-        k_upsample2<<<blocks(n8), 256, 0, st>>>(in.p0, B, H / 2, W / 2, in.c0, ups);
-        RT_CUDA_TRY(cudaGetLastError());
+        RT_CUDA_TRY(launch_pdl(k_upsample2, dim3(blocks(n8)), dim3(256), 0, st, pdl, in.p0, B, H / 2, W / 2, in.c0,
+                               ups));
         src0 = ups;
     }
     ConvTiles q;
