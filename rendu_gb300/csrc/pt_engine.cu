@@ -124,19 +124,13 @@ int WaveEngine::launch_wave(const PtWave &w, uint32_t depth, bool ext, bool shad
         return RT_OK;
     };
     int r = mark(-1);
-    if (r == RT_OK) r = pt_launch_wave_begin(w, cs);
-    if (r == RT_OK) r = pt_launch_raygen(w, cs);
+    if (r == RT_OK) r = pt_launch_raygen(w, cs);  // also starts the wave's queues
     if (r == RT_OK) r = mark(PT_KERNEL_RAYGEN);
     int cur = 0;
     for (uint32_t did = 0; r == RT_OK && did < depth; ++did) {
+        // (the traversal also empties the queues the shading appends to)
         r = trace_closest_batch(w, cur, big_stack, cs);
         if (r == RT_OK) r = mark(PT_KERNEL_TRACE);
-        // The queues shading appends to start empty: the next ray queue and both shadow queues.
-        if (r == RT_OK && (cudaMemsetAsync(&w.counters[cur ^ 1], 0, 4, cs) != cudaSuccess ||
-                           cudaMemsetAsync(&w.counters[2], 0, 8, cs) != cudaSuccess)) {
-            set_error("cudaMemsetAsync failed in the wave sequence");
-            r = RT_ERR_CUDA;
-        }
         if (r == RT_OK) r = pt_launch_shade(w, cur, did, ext, cs);
         if (r == RT_OK) r = mark(PT_KERNEL_SHADE);
         if (r == RT_OK && shadow_a) r = pt_launch_shadow(w, 0, big_stack, cs);

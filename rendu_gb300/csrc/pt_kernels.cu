@@ -4,11 +4,12 @@
 //
 // A wave is a list of tiles (job, pixel range, run of S consecutive samples) packed from
 // all jobs of the call; every path carries its job, pixel and sample. Per wave:
-//   wave_begin -- queue counters for this wave;
-//   raygen     -- primary rays from each job's camera (PathTracer.cpp:186-198);
+//   raygen     -- primary rays from each job's camera (PathTracer.cpp:186-198); also
+//                 starts the wave's queue counters;
 //   per bounce:
 //     trace    -- closest hit of the compacted ray queue: the persistent traversal with
 //                 per-lane refill (rt_trace.cu), each ray against its own job's hierarchy;
+//                 also empties the queues the shading appends to;
 //     shade    -- the reference's hit logic (background on miss, alpha cut-out, emission,
 //                 local frame, NEE light pick + evaluation, BSDF sampling); continuing
 //                 paths and shadow rays are appended to queues with one atomic per warp;
@@ -19,6 +20,8 @@
 // The whole per-wave sequence reads its wave from device memory, so it is captured once as
 // the body of a CUDA graph's while node that runs it for every wave (pt_engine.cu).
 #include <cuda_fp16.h>
+
+#include <algorithm>
 
 #include "pt_scene.hpp"
 #include "rt_traverse.cuh"
@@ -48,15 +51,6 @@ __device__ __forceinline__ uint32_t find_tile(const PtWave &w, uint32_t t0, uint
     return lo;
 }
 
-__global__ void k_wave_begin(PtWave w) {
-    const uint32_t wave = w.counters[4];
-    w.counters[0] = w.wave_paths[wave];
-    w.counters[1] = 0u;
-    w.counters[2] = 0u;
-    w.counters[3] = 0u;
-    *w.fetch = 0ull;
-}
-
 __global__ void k_wave_end(PtWave w, cudaGraphConditionalHandle loop, int has_loop) {
     const uint32_t next = w.counters[4] + 1u;
     w.counters[4] = next;
@@ -65,10 +59,7 @@ __global__ void k_wave_end(PtWave w, cudaGraphConditionalHandle loop, int has_lo
 
 __global__ void k_set_waves(PtWave w, uint32_t n) { w.counters[5] = n; }
 
-__global__ void k_raygen(PtWave w) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t wave = w.counters[4];
-    if (p >= w.wave_paths[wave]) return;
+__device__ __forceinline__ void raygen_one(const PtWave &w, uint32_t p, uint32_t wave) {
     const PtTile tile = w.tiles[find_tile(w, w.wave_tiles[wave], w.wave_tiles[wave + 1], p)];
     const uint32_t local = p - tile.path0;
     const uint32_t pixel = tile.pixel0 + local % tile.npix;
@@ -97,6 +88,19 @@ __global__ void k_raygen(PtWave w) {
         w.aov0[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         w.aov1[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     }
+}
+
+// The wave's primary rays, grid-stride over its paths (the grid is fixed in the captured
+// graph; the wave's size is read on the device). Block 0 also starts the wave's queues: the
+// first ray queue holds every path, the traversal's fetch counter restarts.
+__global__ void k_raygen(PtWave w) {
+    const uint32_t wave = w.counters[4];
+    const uint32_t n = w.wave_paths[wave];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        w.counters[0] = n;
+        *w.fetch = 0ull;
+    }
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) raygen_one(w, p, wave);
 }
 
 struct SurfaceHit {
@@ -425,6 +429,13 @@ __global__ void __launch_bounds__(128, 8) k_shadow(PtWave w, int queue) {
 template <int STACK>
 __global__ void __launch_bounds__(128) k_trace_batch(PtWave w, int cur) {
     const size_t n = min(w.counters[cur], w.cap);
+    // The queues the following shading appends to start empty: the next ray queue and both
+    // shadow queues (nothing reads them until the shading launch, which follows this one).
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        w.counters[cur ^ 1] = 0u;
+        w.counters[2] = 0u;
+        w.counters[3] = 0u;
+    }
     const rt_ray *__restrict__ rays = w.qray[cur];
     const uint32_t *__restrict__ qpath = w.qpath[cur];
     const unsigned lane = threadIdx.x & 31;
@@ -472,10 +483,7 @@ __global__ void __launch_bounds__(128) k_trace_batch(PtWave w, int cur) {
 
 // render.rgb(x, y) += min(sampleColor, 5) in sample order (PathTracer.cpp:288); the clamp
 // value is an option of the extended estimator. One thread per (tile, pixel).
-__global__ void k_accumulate(PtWave w) {
-    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t wave = w.counters[4];
-    if (p >= w.wave_paths[wave]) return;
+__device__ __forceinline__ void accumulate_one(const PtWave &w, uint32_t p, uint32_t wave) {
     const PtTile tile = w.tiles[find_tile(w, w.wave_tiles[wave], w.wave_tiles[wave + 1], p)];
     const uint32_t local = p - tile.path0;
     if (local >= tile.npix) return;
@@ -529,6 +537,13 @@ __global__ void k_accumulate(PtWave w) {
 #pragma unroll
         for (int k = 0; k < PT_AOV_ACCUM; ++k) a[k] = f[k];
     }
+}
+
+__global__ void k_accumulate(PtWave w) {
+    const uint32_t wave = w.counters[4];
+    const uint32_t n = w.wave_paths[wave];
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x)
+        accumulate_one(w, p, wave);
 }
 
 __global__ void k_load(const float *__restrict__ img, uint32_t comps, uint32_t npix, float *__restrict__ accum,
@@ -658,12 +673,6 @@ int pt_launch_material(const float *cases, const float *uniforms, uint32_t n, fl
     return RT_OK;
 }
 
-int pt_launch_wave_begin(const PtWave &w, cudaStream_t st) {
-    k_wave_begin<<<1, 1, 0, st>>>(w);
-    RT_CUDA_TRY(cudaGetLastError());
-    return RT_OK;
-}
-
 int pt_launch_wave_end(const PtWave &w, cudaStream_t st, const cudaGraphConditionalHandle *loop) {
     k_wave_end<<<1, 1, 0, st>>>(w, loop ? *loop : cudaGraphConditionalHandle(0), loop ? 1 : 0);
     RT_CUDA_TRY(cudaGetLastError());
@@ -676,8 +685,21 @@ int pt_launch_set_waves(const PtWave &w, uint32_t nwaves, cudaStream_t st) {
     return RT_OK;
 }
 
+// Grid of the wave-wide element-wise kernels (grid-stride loops): at most 16 blocks of 256
+// per SM, fewer for a small capacity.
+static unsigned wave_grid(const PtWave &w) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                      cudaSuccess)
+            sms = 152;
+    }
+    return (unsigned)std::min<uint64_t>((w.cap + 255) / 256, (uint64_t)sms * 16);
+}
+
 int pt_launch_raygen(const PtWave &w, cudaStream_t st) {
-    k_raygen<<<(w.cap + 255) / 256, 256, 0, st>>>(w);
+    k_raygen<<<wave_grid(w), 256, 0, st>>>(w);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }
@@ -765,7 +787,7 @@ int trace_closest_batch(const PtWave &w, int cur, bool big_stack, cudaStream_t s
 }
 
 int pt_launch_accumulate(const PtWave &w, cudaStream_t st) {
-    k_accumulate<<<(w.cap + 255) / 256, 256, 0, st>>>(w);
+    k_accumulate<<<wave_grid(w), 256, 0, st>>>(w);
     RT_CUDA_TRY(cudaGetLastError());
     return RT_OK;
 }

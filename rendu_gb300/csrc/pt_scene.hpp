@@ -83,7 +83,6 @@ constexpr uint32_t kSkyTableRes = 512, kSkyTableSamples = 256;
 int pt_launch_sky_table(uint32_t res, uint32_t samples, bool half_prec, float4 *out, cudaStream_t st);
 int pt_launch_sky_eval(const float4 *table, uint32_t w, uint32_t h, const float *cases, uint32_t n, float *out,
                        cudaStream_t st);
-int pt_launch_wave_begin(const PtWave &w, cudaStream_t st);
 // End of a wave: the wave index advances; with a conditional handle (the wave sequence is the
 // body of a graph's while node) the loop goes on while waves remain (counters[5] waves).
 int pt_launch_wave_end(const PtWave &w, cudaStream_t st, const cudaGraphConditionalHandle *loop = nullptr);
