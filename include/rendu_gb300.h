@@ -408,8 +408,9 @@ RT_API int pt_batch_destroy(pt_batch *batch);
 RT_API int pt_batch_render(pt_batch *batch, const pt_batch_job *jobs, size_t n, const pt_render_options *options,
                            const pt_batch_tuning *tuning, void *stream, uint32_t flags);
 
-/* Time a reduced copy of the batch (1/8 of each job's samples) under candidate tunings,
- * cache the fastest for this device in `cache_path` (NULL: $RENDU_GB300_TUNING, else
+/* Time the batch (images discarded) under candidate tunings, one parameter at a time
+ * (samples per wave, wave capacity, tile size, samples per wave again), cache the fastest
+ * for this device in `cache_path` (NULL: $RENDU_GB300_TUNING, else
  * ~/.cache/rendu_gb300/batch_tuning.json) and return it in *out. */
 RT_API int pt_batch_autotune(pt_batch *batch, const pt_batch_job *jobs, size_t n, const pt_render_options *options,
                              const char *cache_path, pt_batch_tuning *out);

@@ -1,11 +1,15 @@
 // Autotuner of the batched wave engine: wave capacity, tile size and samples per wave are
-// chosen by timing a reduced copy of the caller's batch (every job at 1/8 of its samples)
-// under each candidate; the winner is cached per device in a small JSON file that
-// pt_batch_render reads when called without explicit tuning.
+// chosen by timing the caller's batch itself (images discarded) under candidate tunings,
+// one parameter at a time (coordinate descent: samples per wave, wave capacity, tile size,
+// then samples per wave again, each from the best so far); the winner is cached per device
+// in a small JSON file that pt_batch_render reads when called without explicit tuning.
+// A copy reduced to 1/8 of the samples, timed over the full 4 x 3 x 3 grid, chose 16
+// samples per wave where the batch itself runs 7 % faster with 64.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <vector>
 #include <sys/stat.h>
 
 #include "pt_scene.hpp"
@@ -100,33 +104,45 @@ extern "C" int pt_batch_autotune(pt_batch *b, const pt_batch_job *jobs, size_t n
             set_error("invalid batch job " + std::to_string(k));
             return RT_ERR_ARG;
         }
-        // Reduced copy: 1/8 of the samples, results discarded (no image).
-        const uint32_t spp = j.samples >= 8 ? j.samples / 8 : 1;
-        specs.push_back(JobSpec{j.scene, j.camera, spp, j.depth, j.seed, nullptr, j.width, j.height, j.components,
+        // The batch itself, results discarded (no image).
+        specs.push_back(JobSpec{j.scene, j.camera, j.samples, j.depth, j.seed, nullptr, j.width, j.height, j.components,
                                 opts ? opts->clamp : 5.0f, opts ? opts->accum_fp64 : 0, nullptr});
     }
     int prev = -1;
     cudaGetDevice(&prev);
     if (prev != b->device) cudaSetDevice(b->device);
-    const uint32_t waves[] = {1u << 21, 1u << 22, 1u << 23, 1u << 24};
-    const uint32_t tilesz[] = {1u << 14, 1u << 16, 1u << 18};
-    const uint32_t samples[] = {4, 16, 64};
+    const std::vector<uint32_t> waves = {1u << 22, 1u << 23, 1u << 24, 1u << 25};
+    const std::vector<uint32_t> tilesz = {1u << 14, 1u << 16, 1u << 18};
+    const std::vector<uint32_t> samples = {8, 16, 32, 64, 128};
     Tuning best = default_tuning();
     double best_ms = 1e30;
     int r = RT_OK;
-    for (uint32_t wp : waves)
-        for (uint32_t tp : tilesz)
-            for (uint32_t ms : samples) {
-                const Tuning t{wp, tp, ms};
-                pt_render_stats st{};
-                r = b->engine->run(specs, mode, t, false, nullptr, &st);  // first run: capture + warm-up
-                if (r == RT_OK) r = b->engine->run(specs, mode, t, false, nullptr, &st);
-                if (r != RT_OK) break;
-                if (st.device_ms < best_ms) {
-                    best_ms = st.device_ms;
-                    best = t;
-                }
-            }
+    auto time_it = [&](const Tuning &t) {
+        pt_render_stats st{};
+        r = b->engine->run(specs, mode, t, false, nullptr, &st);  // first run: capture + warm-up
+        if (r == RT_OK) r = b->engine->run(specs, mode, t, false, nullptr, &st);
+        if (r == RT_OK && st.device_ms < best_ms) {
+            best_ms = st.device_ms;
+            best = t;
+        }
+    };
+    time_it(best);
+    // one parameter at a time, each pass from the best tuning found so far
+    for (int pass = 0; pass < 4 && r == RT_OK; ++pass) {
+        const int which = pass == 3 ? 0 : pass;  // samples, waves, tiles, samples again
+        const std::vector<uint32_t> &cand = which == 0 ? samples : which == 1 ? waves : tilesz;
+        const Tuning base = best;
+        for (uint32_t v : cand) {
+            Tuning t = base;
+            if (which == 0) t.max_samples = v;
+            else if (which == 1) t.wave_paths = v;
+            else t.tile_pixels = v;
+            if (t.wave_paths == base.wave_paths && t.tile_pixels == base.tile_pixels && t.max_samples == base.max_samples)
+                continue;  // already timed
+            time_it(t);
+            if (r != RT_OK) break;
+        }
+    }
     if (prev >= 0 && prev != b->device) cudaSetDevice(prev);
     if (r != RT_OK) return r;
     save_tuning(cache, best, best_ms);
