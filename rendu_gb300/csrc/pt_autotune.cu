@@ -16,7 +16,9 @@
 
 namespace rgb {
 
-Tuning default_tuning() { return Tuning{1u << 23, 1u << 16, 16}; }
+// Defaults (and the autotuner's starting point): 32M paths per wave, 64K-pixel tiles, 64
+// samples per wave -- the 64-job batch's descent ends at 32M / 64K / 128.
+Tuning default_tuning() { return Tuning{1u << 25, 1u << 16, 64}; }
 
 namespace {
 

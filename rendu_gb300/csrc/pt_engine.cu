@@ -200,7 +200,13 @@ int WaveEngine::run(const std::vector<JobSpec> &jobs, int mode, const Tuning &tn
                     pt_render_stats *stats, bool profile) {
     if (jobs.empty()) return RT_OK;
     const bool ext = mode == PT_MODE_EXTENDED;
-    const uint64_t cap = std::max<uint64_t>(tn.wave_paths, 1u << 12);
+    // Wave capacity: the tuning's, but no more than the call's paths (the path state and the
+    // queues are sized by it, so a small render does not hold a large wave's memory).
+    uint64_t total_paths = 0;
+    for (const JobSpec &js : jobs)
+        total_paths += (uint64_t)js.width * js.height *
+                       (uint64_t)std::pow(2.0, std::round(std::log2((float)std::max<uint32_t>(js.samples, 1u))));
+    const uint64_t cap = std::max<uint64_t>(std::min<uint64_t>(tn.wave_paths, total_paths), 1u << 12);
     // ---- per-job set-up -------------------------------------------------------------------
     std::vector<PtJob> hj(jobs.size());
     std::vector<JobBvh> hb(jobs.size());
