@@ -599,21 +599,19 @@ int pt_render(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, uint3
 }
 
 // Wave capacity of a single render: 32M paths, or the largest power of two whose path state
-// (about 256 bytes a path) stays within an eighth of the device's memory.
-static uint32_t render_wave_paths(int device) {
-    static uint32_t cached[64] = {};
-    if (device >= 0 && device < 64 && cached[device]) return cached[device];
+// (about 240 bytes a path) fits in an eighth of the device's free memory -- but never less
+// than the capacity the scene's engine already holds (so repeated renders keep their graph).
+static uint32_t render_wave_paths(uint64_t held) {
     uint32_t cap = 1u << 25;
-    cudaDeviceProp p;
-    if (cudaGetDeviceProperties(&p, device) == cudaSuccess) {
-        const uint64_t fit = (uint64_t)p.totalGlobalMem / 8 / 256;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+        const uint64_t fit = (uint64_t)free_b / 8 / 256;
         while (cap > (1u << 20) && cap > fit) cap >>= 1;
     } else {
         cudaGetLastError();
         cap = 1u << 23;
     }
-    if (device >= 0 && device < 64) cached[device] = cap;
-    return cap;
+    return (uint32_t)std::min<uint64_t>(std::max<uint64_t>(cap, held), 1u << 25);
 }
 
 int pt_render_ex(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, uint32_t depth, uint64_t seed,
@@ -640,10 +638,10 @@ int pt_render_ex(pt_scene *s, const pt_camera_desc *camera, uint32_t samples, ui
         js.rank = opts->rank;
     }
     // One tile of every pixel per wave, as many samples per wave as the wave capacity allows:
-    // up to 32M paths (about 8 GB of path state and queues; at most an eighth of the device's
-    // memory). Larger waves mean fewer, fuller launches: the large 1080p render took 183.8 /
-    // 172.5 / 166.3 / 163.8 ms with 8M / 16M / 32M / 64M paths per wave (same image).
-    Tuning t{render_wave_paths(s->device), width * height, 1u << 30};
+    // up to 32M paths (about 8 GB of path state and queues). Larger waves mean fewer, fuller
+    // launches: the large 1080p render took 183.8 / 172.5 / 166.3 / 163.8 ms with 8M / 16M /
+    // 32M / 64M paths per wave (same image).
+    Tuning t{render_wave_paths(s->engine->capacity()), width * height, 1u << 30};
     if ((uint64_t)width * height > t.wave_paths) t.wave_paths = width * height;
     r = s->engine->run({js}, mode, t, dev, st, &s->last, opts && opts->profile);
     return r;

@@ -137,6 +137,7 @@ class WaveEngine {
     // between the steps, and report the time of every kernel class in stats->kernel_ms.
     int run(const std::vector<JobSpec> &jobs, int mode, const Tuning &t, bool device_images, cudaStream_t st,
             pt_render_stats *stats, bool profile = false);
+    uint64_t capacity() const { return cap_; }  // paths of the wave buffers held
 
   private:
     int ensure_capacity(uint64_t cap, uint64_t accum_pixels, uint64_t ntiles, uint64_t nwaves, size_t njobs,
