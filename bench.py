@@ -603,7 +603,8 @@ def main():
     ap.add_argument("--profile-run", action="store_true",
                     help="only one closest-hit and one any-hit launch over the workload (for ncu captures)")
     ap.add_argument("--profile-pt", default=None, choices=list(PT_CONFIGS) + ["batch_64"],
-                    help="only one render of the given path-tracer configuration (for ncu captures)")
+                    help="only one render of the given path-tracer configuration, its kernels launched "
+                         "directly (for ncu captures)")
     ap.add_argument("--pt-size", default=None,
                     help="WxH: the --profile-pt render at another resolution (small ncu captures)")
     args = ap.parse_args()
@@ -648,7 +649,9 @@ def main():
                      "depth": j["depth"], "seed": j["seed"],
                      "image": torch.zeros((j["height"], j["width"], 3), dtype=torch.float32, device="cuda")}
                     for j, t in zip(wl, tracers)]
-            st = R.BatchRenderer(0).render(jobs)
+            # profile=True: the wave's kernels are launched directly rather than from the
+            # graph's device-side loop, which a profiler cannot look into kernel by kernel
+            st = R.BatchRenderer(0).render(jobs, profile=True)
             torch.cuda.synchronize()
             print(json.dumps({"profile_pt": "batch_64", **{k: v for k, v in st.items() if k != "kernel_ms"}}))
             return
@@ -658,7 +661,7 @@ def main():
         sc = _pt_scene(kind)
         img = torch.zeros((h, w, 3), dtype=torch.float32, device="cuda")
         tr = R.PathTracer(sc)
-        tr.render(dict(sc.camera, ratio=w / h), spp, depth, img, seed=1, mode=mode)
+        tr.render(dict(sc.camera, ratio=w / h), spp, depth, img, seed=1, mode=mode, profile=True)
         st = tr.last_stats()
         print(json.dumps({"profile_pt": args.profile_pt, "size": [w, h],
                           **{k: v for k, v in st.items() if k != "kernel_ms"}}))
