@@ -421,7 +421,7 @@ DN_TRAIN_STEPS = 6000  # Adam steps of 16 random 128^2 crops
 DN_EVAL_SCENE = 20261210  # held out
 DN_EVAL_SIZE = (1920, 1080)
 DN_TRUTH_SPP = 16384  # double-precision accumulation
-DN_LEVELS = (64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384)
+DN_LEVELS = (64, 128, 256, 512, 1024, 2048, 4096, 8192, 16384)  # --dn-max-spp extends it
 
 
 def _dn_target_spp(spp_in: int) -> int:
@@ -430,14 +430,14 @@ def _dn_target_spp(spp_in: int) -> int:
     return int(min(max(4 * spp_in, 1024), 4096))
 
 
-def run_denoiser(cpu: bool):
+def run_denoiser(cpu: bool, max_spp: int = DN_LEVELS[-1]):
     """The learned denoiser: trained here on path-tracer pairs (scenes of the large
     workload's type, 256^2 views, 64-4096-spp inputs with first-hit features and the standard
     error, independent 1024-4096-spp double-precision targets), then (1) inference
     throughput at 1920x1080 and training-step throughput at 8 x 256^2 against the BF16
     tensor peak, and (2) plain path tracing vs path tracing + denoiser on a held-out scene at
     1920x1080: relative RMSE against a 16,384-spp double-precision render as the sample
-    count doubles, and the time each needs to reach given error levels."""
+    count doubles (to `max_spp`), and the time each needs to reach given error levels."""
     import torch
 
     import rendu_gb300 as R
@@ -489,7 +489,8 @@ def run_denoiser(cpu: bool):
     truth = torch.zeros((h, w, 3), device="cuda")
     tr2.render(dict(cam, ratio=w / h), DN_TRUTH_SPP, 5, truth, seed=7, mode=1, fp64=True)
     truth_s = tr2.last_stats()["device_ms"] / 1e3
-    curve = D.progressive_curves(tr2, cam, w, h, DN_LEVELS, truth, denoiser=net, seed=100)
+    levels_spp = [DN_LEVELS[0] << k for k in range(64) if DN_LEVELS[0] << k <= max_spp]
+    curve = D.progressive_curves(tr2, cam, w, h, levels_spp, truth, denoiser=net, seed=100)
     eval_s = time.perf_counter() - t0
     tr2.close()
     plain = [(p["render_s"], p["plain"]) for p in curve]
@@ -598,6 +599,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-pt", action="store_true", help="skip the path-tracer lines")
     ap.add_argument("--denoiser-only", action="store_true", help="only the denoiser measurement (one JSON line)")
+    ap.add_argument("--dn-max-spp", type=int, default=DN_LEVELS[-1],
+                    help="largest sample count of the denoiser's quality curve (doubling from 64); 65536 "
+                         "carries plain path tracing to rel-RMSE 0.01 against the 16,384-spp truth")
     ap.add_argument("--profile-dn", action="store_true",
                     help="only two 1920x1080 denoiser inferences and one 8 x 256^2 training step (for ncu captures)")
     ap.add_argument("--profile-run", action="store_true",
@@ -632,7 +636,7 @@ def main():
         from rendu_gb300 import build as B
 
         B.build()
-        print(json.dumps({"denoiser": run_denoiser(False)}), flush=True)
+        print(json.dumps({"denoiser": run_denoiser(False, args.dn_max_spp)}), flush=True)
         return
     if args.profile_pt:
         import rendu_gb300 as R

@@ -1,10 +1,12 @@
 // C-ABI of the raycaster (include/rendu_gb300.h): context life cycle, mesh intake,
 // hierarchy build, batched queries with host or device buffers.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
 #include <thread>
+#include <vector>
 
 #include "rt_context.hpp"
 
@@ -92,6 +94,23 @@ using namespace rgb;
 
 namespace {
 
+// Records per chunk of the pipelined host-buffer path (rays, or segments for rt_visible,
+// whose per-stream scratch is sized by it too).
+constexpr size_t kHostChunk = size_t(1) << 21;
+
+// The kernel streams of the pipelined host path, chunk c on s[c % n]: consecutive chunks'
+// traversals overlap, so that one launch's tail (its last, longest rays, with most of the
+// GPU idle) runs beside the next launch instead of before it.
+struct KernelStreams {
+    static constexpr int n = 1 + rt_ctx::kSide;
+    cudaStream_t s[n];
+    explicit KernelStreams(const rt_ctx *ctx) {
+        s[0] = ctx->stream2;
+        for (int i = 0; i < rt_ctx::kSide; ++i) s[1 + i] = ctx->kside[i];
+    }
+    cudaStream_t operator[](size_t c) const { return s[c % (size_t)n]; }
+};
+
 struct DeviceGuard {
     int prev = -1;
     explicit DeviceGuard(int dev) {
@@ -140,7 +159,8 @@ int host_chunked_pageable(rt_ctx *ctx, const void *h_in, size_t in_stride, size_
                           size_t chunk, Fn fn) {
     constexpr int NB = rt_ctx::kRing;
     const size_t nchunks = (n + chunk - 1) / chunk;
-    cudaStream_t sin = ctx->stream, sk = ctx->stream2, sout = ctx->stream3;
+    cudaStream_t sin = ctx->stream, sout = ctx->stream3;
+    const KernelStreams ks(ctx);
     std::atomic<size_t> launched{0}, drained{0};
     std::atomic<int> fail{RT_OK};
     std::string out_msg;
@@ -179,6 +199,7 @@ int host_chunked_pageable(rt_ctx *ctx, const void *h_in, size_t in_stride, size_
         }
         if (fail.load() != RT_OK) break;
         const size_t s = c * chunk, m = (n - s) < chunk ? (n - s) : chunk;
+        const cudaStream_t sk = ks[c];
         cudaError_t e = cudaMemcpyAsync(ctx->ring_in[b].ptr, static_cast<const char *>(h_in) + s * in_stride,
                                         m * in_stride, cudaMemcpyHostToDevice, sin);
         if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_in[b], sin);
@@ -201,23 +222,44 @@ int host_chunked_pageable(rt_ctx *ctx, const void *h_in, size_t in_stride, size_
         set_error(out_msg);
         r = fail.load();
     }
-    RT_CUDA_TRY(cudaStreamSynchronize(sk));
+    for (int i = 0; i < ks.n; ++i) RT_CUDA_TRY(cudaStreamSynchronize(ks.s[i]));
     RT_CUDA_TRY(cudaStreamSynchronize(sin));
     if (r != RT_OK) return r;
-    return check_status(ctx, sk);
+    return check_status(ctx, sin);
 }
 
-// Runs `fn(d_in, count, d_out, stream)` over host buffers in chunks of 2M records through a
-// ring of four staging buffers and three streams: copies in on `stream`, kernels on
-// `stream2`, copies out on `stream3`, ordered by events, so that both copy directions and
-// the kernels stay busy at once (the host link, not the kernels, bounds this path). Pinned
-// host buffers get asynchronous DMA; pageable ones go through host_chunked_pageable.
+// Chunk sizes for n records: at most `chunk` each, the last three halving (chunk / 2,
+// chunk / 4, chunk / 8), so that what follows the last copy-in (that chunk's traversal and
+// copy-out) is short. Smaller chunks elsewhere only add launches: a traversal launch lasts
+// at least the latency of its longest rays, about 0.15 ms whatever its size.
+std::vector<size_t> chunk_plan(size_t n, size_t chunk) {
+    const size_t tail[3] = {chunk / 2, chunk / 4, chunk / 8};
+    const size_t tsum = tail[0] + tail[1] + tail[2];
+    std::vector<size_t> v;
+    if (n < tsum + 2 * chunk) {
+        for (size_t s = 0; s < n; s += chunk) v.push_back(std::min(chunk, n - s));
+        return v;
+    }
+    const size_t mid = n - tsum, k = (mid + chunk - 1) / chunk;
+    for (size_t i = 0; i < k; ++i) v.push_back(mid / k + (i < mid % k ? 1 : 0));
+    v.insert(v.end(), tail, tail + 3);
+    return v;
+}
+
+// Runs `fn(d_in, count, d_out, stream)` over host buffers in chunks of up to 2M records
+// (chunk_plan) through a ring of eight staging buffers: copies in on `stream`, kernels in
+// turn on `stream2` and `kside[0]`, copies out on `stream3`, ordered by events, so that both
+// copy directions and the kernels stay busy at once (the host link, not the kernels, bounds
+// this path). Pinned host buffers get asynchronous DMA; pageable ones go through
+// host_chunked_pageable.
 template <class Fn>
 int host_chunked(rt_ctx *ctx, const void *h_in, size_t in_stride, size_t n, void *h_out, size_t out_stride, Fn fn) {
     constexpr int NB = rt_ctx::kRing;
-    const size_t chunk = size_t(1) << 21;
+    const size_t chunk = kHostChunk;
     const size_t cn = n < chunk ? n : chunk;
     if (!ctx->stream3) RT_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream3, cudaStreamNonBlocking));
+    for (int i = 0; i < rt_ctx::kSide; ++i)
+        if (!ctx->kside[i]) RT_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->kside[i], cudaStreamNonBlocking));
     for (int b = 0; b < NB; ++b) {
         if (ctx->ring_in[b].reserve(cn * in_stride) != RT_OK || ctx->ring_out[b].reserve(cn * out_stride) != RT_OK)
             return RT_ERR_OOM;
@@ -226,12 +268,15 @@ int host_chunked(rt_ctx *ctx, const void *h_in, size_t in_stride, size_t n, void
     }
     if (n > chunk && (is_pageable(h_in) || is_pageable(h_out)))
         return host_chunked_pageable(ctx, h_in, in_stride, n, h_out, out_stride, chunk, fn);
-    cudaStream_t sin = ctx->stream, sk = ctx->stream2, sout = ctx->stream3;
-    size_t c = 0;
+    cudaStream_t sin = ctx->stream, sout = ctx->stream3;
+    const KernelStreams ks(ctx);
+    const std::vector<size_t> plan = chunk_plan(n, chunk);
     int r = RT_OK;
-    for (size_t s = 0; s < n && r == RT_OK; s += chunk, ++c) {
+    size_t s = 0;
+    for (size_t c = 0; c < plan.size() && r == RT_OK; s += plan[c], ++c) {
         const int b = (int)(c % NB);
-        const size_t m = (n - s) < chunk ? (n - s) : chunk;
+        const size_t m = plan[c];
+        const cudaStream_t sk = ks[c];
         // Buffer b is free once the copy-out of the chunk NB before has finished (which
         // itself followed that chunk's kernel).
         if (c >= (size_t)NB) RT_CUDA_TRY(cudaStreamWaitEvent(sin, ctx->ev_out[b], 0));
@@ -248,10 +293,10 @@ int host_chunked(rt_ctx *ctx, const void *h_in, size_t in_stride, size_t n, void
         RT_CUDA_TRY(cudaEventRecord(ctx->ev_out[b], sout));
     }
     RT_CUDA_TRY(cudaStreamSynchronize(sout));
-    RT_CUDA_TRY(cudaStreamSynchronize(sk));
+    for (int i = 0; i < ks.n; ++i) RT_CUDA_TRY(cudaStreamSynchronize(ks.s[i]));
     RT_CUDA_TRY(cudaStreamSynchronize(sin));
     if (r != RT_OK) return r;
-    return check_status(ctx, sk);
+    return check_status(ctx, sin);
 }
 
 }  // namespace
@@ -315,6 +360,11 @@ int rt_destroy(rt_ctx *ctx) {
         cudaStreamSynchronize(ctx->stream3);
         cudaStreamDestroy(ctx->stream3);
     }
+    for (int i = 0; i < rt_ctx::kSide; ++i)
+        if (ctx->kside[i]) {
+            cudaStreamSynchronize(ctx->kside[i]);
+            cudaStreamDestroy(ctx->kside[i]);
+        }
     for (int b = 0; b < rt_ctx::kRing; ++b) {
         ctx->ring_in[b].release();
         ctx->ring_out[b].release();
@@ -453,12 +503,16 @@ int rt_visible(rt_ctx *ctx, const float *segs, size_t n, uint8_t *visible, void 
     DeviceGuard g(ctx->device);
     // Scratch rays: one region per stream of the pipelined host path (reserved up front,
     // never reallocated while work is in flight).
-    const size_t chunk = size_t(1) << 21;
+    const size_t chunk = kHostChunk;
     const bool dev = (flags & RT_FLAG_DEVICE_PTRS) != 0;
     const size_t region = dev ? n : (n < chunk ? n : chunk);
-    if (ctx->d_out2.reserve((dev ? 1 : 2) * region * sizeof(rt_ray) + 16) != RT_OK) return RT_ERR_OOM;
+    if (ctx->d_out2.reserve((dev ? 1 : 2 + rt_ctx::kSide) * region * sizeof(rt_ray) + 16) != RT_OK)
+        return RT_ERR_OOM;
     auto run = [ctx, region](const float *d_segs, size_t m, uint8_t *d_vis, cudaStream_t st) -> int {
-        rt_ray *d_r = ctx->d_out2.as<rt_ray>() + (st == ctx->stream2 ? region : 0);
+        // Region 0 for the caller's stream, 1 for stream2, 2.. for the side streams.
+        const int side = side_index(ctx, st);
+        const size_t k = st == ctx->stream2 ? 1 : (side >= 0 ? (size_t)(2 + side) : 0);
+        rt_ray *d_r = ctx->d_out2.as<rt_ray>() + k * region;
         int rr = segments_to_rays(d_segs, m, d_r, st);
         if (rr != RT_OK) return rr;
         rr = trace_any(ctx, d_r, m, d_vis, st);

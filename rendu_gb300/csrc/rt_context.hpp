@@ -52,9 +52,10 @@ struct rt_ctx {
     rgb::DevBuf d_nodes;   // BvhNode[n_inner] (at least 1: a root, possibly wrapping a leaf)
     rgb::DevBuf d_tris;    // BvhTri[n_tris] in leaf order
     rgb::DevBuf d_verts;   // float3 transformed vertices (kept for the path tracer)
-    // 64 bytes: status word of the host-buffer calls at 0, three traversal fetch counters at
-    // 8, 16, 24, status word of the asynchronous calls (device pointers on the caller's
-    // stream, rt_visible_noalloc) at 32, read and cleared by rt_get_status.
+    // 64 bytes: status word of the host-buffer calls at 0, traversal fetch counters at 8
+    // (the caller's streams), 16 (`stream`), 24 (`stream2`) and 40 (`kside[0]`),
+    // status word of the asynchronous calls (device pointers on the caller's stream,
+    // rt_visible_noalloc) at 32, read and cleared by rt_get_status.
     rgb::DevBuf d_status;
     uint32_t stack_cap = 0;  // rt_set_traversal_stack: 0 = the hierarchy's exact bound
     uint64_t n_tris = 0;
@@ -72,10 +73,12 @@ struct rt_ctx {
     rgb::DevBuf d_mesh_first;
     rgb::DevBuf d_info_stage;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;
-    // Host-buffer pipeline: copy-in on `stream`, kernels on `stream2`, copy-out on `stream3`,
-    // through a ring of staging buffers (created on first use).
-    static constexpr int kRing = 4;
+    // Host-buffer pipeline: copy-in on `stream`, kernels in turn on `stream2` and `kside`,
+    // copy-out on `stream3`, through a ring of staging buffers (created on first use).
+    static constexpr int kRing = 8;
+    static constexpr int kSide = 1;
     cudaStream_t stream3 = nullptr;
+    cudaStream_t kside[kSide] = {};
     rgb::DevBuf ring_in[kRing], ring_out[kRing];
     cudaEvent_t ev_in[kRing] = {}, ev_k[kRing] = {}, ev_out[kRing] = {};
 };
@@ -91,14 +94,31 @@ int check_status(rt_ctx *ctx, cudaStream_t stream);  // reads and clears the dev
 
 // The status word a traversal on `st` reports into: the host-buffer path's own streams use
 // the word check_status reads; every other stream (the caller's) the word rt_get_status reads.
+// Which of the pipeline's extra kernel streams `st` is, or -1.
+inline int side_index(const rt_ctx *ctx, cudaStream_t st) {
+    for (int i = 0; st && i < rt_ctx::kSide; ++i)
+        if (st == ctx->kside[i]) return i;
+    return -1;
+}
+
 inline unsigned *status_word(rt_ctx *ctx, cudaStream_t st) {
-    const bool own = st == ctx->stream || st == ctx->stream2;
+    const bool own = st == ctx->stream || st == ctx->stream2 || side_index(ctx, st) >= 0;
     return reinterpret_cast<unsigned *>(ctx->d_status.as<char>() + (own ? 0 : 32));
 }
 
 // Entries of the traversal stack the kernels are instantiated with (2, 64 or 256): the
 // smallest that holds the hierarchy's exact bound, or the cap set by rt_set_traversal_stack
 // (the 2-entry kernels only exist for that diagnostic).
+// Byte offset in d_status of the fetch counter of a persistent traversal on `st`: one per
+// stream the context launches on, since the pipelined host path runs traversals on two
+// streams at once, and the caller's stream may run one beside them.
+inline size_t fetch_counter_offset(const rt_ctx *ctx, cudaStream_t st) {
+    if (st == ctx->stream) return 16;
+    if (st == ctx->stream2) return 24;
+    const int i = side_index(ctx, st);
+    return i >= 0 ? 40 + 8 * (size_t)i : 8;
+}
+
 inline int traversal_stack(const rt_ctx *ctx) {
     const int need = ctx->stack_cap ? (int)ctx->stack_cap : ctx->depth;
     return need <= 2 && ctx->stack_cap ? 2 : (need <= 64 ? 64 : 256);

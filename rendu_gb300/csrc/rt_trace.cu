@@ -264,10 +264,8 @@ int launch_persistent(rt_ctx *ctx, const rt_ray *rays, size_t n, const uint32_t 
         RT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_persistent<ANY, STACK>, 128, 0));
         g = sms * (per_sm > 0 ? per_sm : 1);
     }
-    // One fetch counter per stream the context launches on: the caller's stream and the two
-    // streams of the pipelined host path may run traversals concurrently.
-    const int slot = st == ctx->stream ? 1 : (st == ctx->stream2 ? 2 : 0);
-    unsigned long long *counter = reinterpret_cast<unsigned long long *>(ctx->d_status.as<char>() + 8 + 8 * slot);
+    unsigned long long *counter =
+        reinterpret_cast<unsigned long long *>(ctx->d_status.as<char>() + fetch_counter_offset(ctx, st));
     RT_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
     const RootBox root{{ctx->root_box[0], ctx->root_box[1], ctx->root_box[2]},
                        {ctx->root_box[3], ctx->root_box[4], ctx->root_box[5]}};
