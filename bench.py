@@ -284,11 +284,16 @@ def run_pathtracer(name, steps, cpu: bool):
         st = tr.last_stats()
         rays += st["rays"]
         dev_ms += st["device_ms"]
+    # e2e: the image in host memory (copied in, rendered into, copied out every call), after
+    # one warm-up call of that path; wall time per render over `steps` renders
     host = np.zeros((h, w, 3), np.float32)
-    t0 = time.perf_counter()
-    tr.render(cam, spp, depth, host, seed=99, mode=mode)
-    e2e_s = time.perf_counter() - t0
-    e2e_rays = tr.last_stats()["rays"]
+    tr.render(cam, spp, depth, host, seed=98, mode=mode)
+    e2e_rays, t0 = 0, time.perf_counter()
+    for k in range(steps):
+        tr.render(cam, spp, depth, host, seed=99 + k, mode=mode)
+        e2e_rays += tr.last_stats()["rays"]
+    e2e_s = (time.perf_counter() - t0) / steps
+    e2e_rays //= steps
     # per-kernel times: one more render with the kernels launched directly, events between them
     img.zero_()
     tr.render(cam, spp, depth, img, seed=2, mode=mode, profile=True)
@@ -298,7 +303,7 @@ def run_pathtracer(name, steps, cpu: bool):
                        f"depth {depth}, {'extended' if mode else 'reference'} estimator",
            "value": round(rays / (dev_ms * 1e3), 1), "unit": "Mrays/s", "ms_per_render": round(dev_ms / steps, 2),
            "rays_per_render": rays // steps, "e2e": {"value": round(e2e_rays / e2e_s / 1e6, 1), "unit": "Mrays/s",
-                                                      "s_per_render": round(e2e_s, 3)},
+                                                      "s_per_render": round(e2e_s, 5)},
            "scene_upload_and_build_s": round(commit_s, 2),
            "roofline": dict(kernels.get("trace", {}), kernel="k_trace_batch"), "kernels": kernels,
            "profiled_render_ms": round(pst["device_ms"], 2)}

@@ -149,6 +149,37 @@ def test_full_size_raycaster_properties(cuda_lib, port_lib):
     assert diff.sum() <= 20
 
 
+def test_host_buffer_pipeline_equals_device_path(cuda_lib):
+    """The pipelined host-buffer path (chunks of up to 2M records, the last three halving,
+    two traversal streams) at 16,777,216 rays gives the device path's answers bit for bit,
+    with pinned and with pageable buffers, for closest hit, any hit and visibility; and a
+    ray count that is no multiple of the chunk size splits correctly too."""
+    import torch
+
+    from rendu_gb300 import _lib as L
+    from rendu_gb300 import scenes as S
+
+    mesh, rays = S.raycaster_workload()
+    rc = _gpu_from_meshes(cuda_lib, [(mesh.positions, mesh.indices, None)])
+    d_rays = torch.from_numpy(rays).cuda()
+    dh = rc.intersect_batch(d_rays).cpu().numpy()
+    da = rc.intersect_any_batch(d_rays).cpu().numpy()
+    pinned = torch.from_numpy(rays).pin_memory().numpy()
+    for host in (rays, pinned):
+        h = rc.intersect_batch(host)
+        assert np.array_equal(h.view(np.uint32).reshape(-1, 4), dh.view(np.uint32))
+        assert np.array_equal(rc.intersect_any_batch(host), da)
+    m = len(rays) - 12345
+    h = rc.intersect_batch(rays[:m])
+    assert np.array_equal(h.view(np.uint32).reshape(-1, 4), dh[:m].view(np.uint32))
+    segs = np.concatenate([rays[:, 0:3], rays[:, 0:3] + 3.0 * rays[:, 4:7]], 1).astype(np.float32)
+    d_vis = torch.empty(len(segs), dtype=torch.uint8, device="cuda")
+    d_segs = torch.from_numpy(segs).cuda()
+    L.call("rt_visible", rc._h, d_segs.data_ptr(), len(segs), d_vis.data_ptr(), None, L.RT_FLAG_DEVICE_PTRS)
+    torch.cuda.synchronize()
+    assert np.array_equal(rc.visible_batch(segs), d_vis.cpu().numpy())
+
+
 def test_edge_cases(cuda_lib):
     R = cuda_lib
     # Empty raycaster: every query misses.
