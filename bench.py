@@ -494,7 +494,7 @@ def run_denoiser(cpu: bool, max_spp: int = DN_LEVELS[-1]):
     truth = torch.zeros((h, w, 3), device="cuda")
     tr2.render(dict(cam, ratio=w / h), DN_TRUTH_SPP, 5, truth, seed=7, mode=1, fp64=True)
     truth_s = tr2.last_stats()["device_ms"] / 1e3
-    levels_spp = [DN_LEVELS[0] << k for k in range(64) if DN_LEVELS[0] << k <= max_spp]
+    levels_spp = [DN_LEVELS[0] << k for k in range(64) if DN_LEVELS[0] << k <= max(max_spp, 2 * DN_LEVELS[0])]
     curve = D.progressive_curves(tr2, cam, w, h, levels_spp, truth, denoiser=net, seed=100)
     eval_s = time.perf_counter() - t0
     tr2.close()
