@@ -8,6 +8,7 @@
 #include <thread>
 #include <vector>
 
+#include "rt_chunks.hpp"
 #include "rt_context.hpp"
 
 namespace rgb {
@@ -226,24 +227,6 @@ int host_chunked_pageable(rt_ctx *ctx, const void *h_in, size_t in_stride, size_
     RT_CUDA_TRY(cudaStreamSynchronize(sin));
     if (r != RT_OK) return r;
     return check_status(ctx, sin);
-}
-
-// Chunk sizes for n records: at most `chunk` each, the last three halving (chunk / 2,
-// chunk / 4, chunk / 8), so that what follows the last copy-in (that chunk's traversal and
-// copy-out) is short. Smaller chunks elsewhere only add launches: a traversal launch lasts
-// at least the latency of its longest rays, about 0.15 ms whatever its size.
-std::vector<size_t> chunk_plan(size_t n, size_t chunk) {
-    const size_t tail[3] = {chunk / 2, chunk / 4, chunk / 8};
-    const size_t tsum = tail[0] + tail[1] + tail[2];
-    std::vector<size_t> v;
-    if (n < tsum + 2 * chunk) {
-        for (size_t s = 0; s < n; s += chunk) v.push_back(std::min(chunk, n - s));
-        return v;
-    }
-    const size_t mid = n - tsum, k = (mid + chunk - 1) / chunk;
-    for (size_t i = 0; i < k; ++i) v.push_back(mid / k + (i < mid % k ? 1 : 0));
-    v.insert(v.end(), tail, tail + 3);
-    return v;
 }
 
 // Runs `fn(d_in, count, d_out, stream)` over host buffers in chunks of up to 2M records
